@@ -1,0 +1,137 @@
+/* svxg_types.h - plain C graph, material and option records of the GB300 stress solve.
+ *
+ * These are the C-ABI images of the reference's C++ inputs:
+ *   svxg_node     <- svx::SNode            core/include/svx/stress/stress.hpp:21-26
+ *   svxg_bond     <- svx::SBond            core/include/svx/stress/stress.hpp:28-51
+ *   svxg_material <- svx::Material (the fields the solve reads)
+ *                                          core/include/svx/material/material.hpp:47-57
+ *   svxg_amg_options    <- svx::AmgOptions core/include/svx/solve/amg.hpp:46-69
+ *   svxg_stress_options <- svx::StressOptions core/include/svx/stress/stress.hpp:68-72
+ *   svxg_pcg_result     <- svx::PcgResult  core/include/svx/solve/amg.hpp:120-125
+ *
+ * Layouts are fixed (no padding left to the compiler) so that ctypes, cgo or a C++ host can
+ * fill them directly. Vectors are 3 doubles. Booleans are one byte.
+ */
+#ifndef SVXG_TYPES_H
+#define SVXG_TYPES_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct svxg_v3 {
+  double x, y, z;
+} svxg_v3;
+
+/* A fragment: 6 DOFs (translation, rotation about c). 40 bytes. */
+typedef struct svxg_node {
+  svxg_v3 c;       /* centre (the solve's frame), m */
+  double mass;     /* kg */
+  uint8_t fixed;   /* pinned: no DOFs */
+  uint8_t gone;    /* retired: an identity row, no bonds */
+  uint8_t pad[6];
+} svxg_node;
+
+/* An interface between two fragments (b < 0: a fixed support). 216 bytes. */
+typedef struct svxg_bond {
+  int32_t a, b;
+  uint8_t broken;     /* severed */
+  uint8_t in_k;       /* its stiffness is in the assembled K (kept by the problem) */
+  uint8_t ma, mb;     /* material ids (0..126) */
+  uint8_t sectioned;  /* section strengths below, else the weaker material's */
+  uint8_t pad[3];
+  svxg_v3 n, t1, t2;  /* local frame: n from a towards b */
+  double area;        /* m^2 */
+  svxg_v3 p;          /* section centroid */
+  double s1, s2;      /* second moments of area about p along t1, t2 */
+  double c1, c2;      /* extreme fibre distances */
+  double rmax;        /* largest distance of the section from p */
+  double la, lb;      /* lengths of the two sides along n */
+  double strength;    /* design strength multiplier */
+  float ft, fb, fc, coh, mu; /* section strengths (Pa) and friction */
+  int32_t faces;
+  int32_t tag;
+  int32_t pad2;
+} svxg_bond;
+
+#define SVXG_MAX_MATERIALS 127
+
+/* What the solve reads of a material. 64 bytes. A table always holds SVXG_MAX_MATERIALS
+ * resolved entries (ids never registered carry id 0's properties, as the reference table's
+ * lookup returns). */
+typedef struct svxg_material {
+  double E, G, rho;
+  double ft, fb, fc, cohesion, friction;
+} svxg_material;
+
+typedef struct svxg_amg_options {
+  int32_t coarse_max;     /* dense solve at or below this many nodes (48) */
+  int32_t smoothed;       /* smoothed aggregation (1) */
+  double strength;        /* strength-of-connection threshold (0.1) */
+  double coarse_scale;    /* unsmoothed coarse operator scale (0.6) */
+  int32_t max_levels;     /* 16 */
+  int32_t gamma;          /* 1: V-cycle (the only cycle the reference runs) */
+  int32_t sgs;            /* reference smoother switch (1); recorded for the work counters */
+  int32_t sweeps;         /* smoother sweeps per side (1) */
+  int32_t cheb_degree;    /* 3 */
+  int32_t dense_work_per_unknown; /* 0 */
+  int32_t coarsen_dense;  /* 1 */
+  int32_t reaggregate;    /* 1 */
+} svxg_amg_options;
+
+/* Arithmetic of the solve. */
+enum {
+  SVXG_PRECISION_FP64 = 0,  /* FP64 K, FP64 PCG; FP32 V-cycle (as the reference) */
+  SVXG_PRECISION_MIXED = 1  /* FP32 K and V-cycle inside FP64 iterative refinement */
+};
+
+typedef struct svxg_stress_options {
+  double rtol;             /* 2e-3 */
+  svxg_amg_options amg;
+  int32_t amg_min_nodes;   /* 160: smaller graphs get block-Jacobi */
+  int32_t precision;       /* SVXG_PRECISION_* */
+} svxg_stress_options;
+
+typedef struct svxg_pcg_result {
+  int32_t iters;
+  int32_t converged;
+  int32_t breakdown;
+  int32_t pad;
+  double rel_res;
+} svxg_pcg_result;
+
+/* Bond loads in bond terms (reference BondLoad, core/include/svx/stress/stress.hpp:61-63). */
+typedef struct svxg_bond_load {
+  double N, V1, V2, T, M1, M2;
+} svxg_bond_load;
+
+enum { SVXG_FAIL_NONE = 0, SVXG_FAIL_TENSION = 1, SVXG_FAIL_CRUSH = 2, SVXG_FAIL_SHEAR = 3 };
+
+/* Defaults of the reference's option records. */
+static inline svxg_stress_options svxg_default_options(void) {
+  svxg_stress_options o;
+  o.rtol = 2e-3;
+  o.amg.coarse_max = 48;
+  o.amg.smoothed = 1;
+  o.amg.strength = 0.1;
+  o.amg.coarse_scale = 0.6;
+  o.amg.max_levels = 16;
+  o.amg.gamma = 1;
+  o.amg.sgs = 1;
+  o.amg.sweeps = 1;
+  o.amg.cheb_degree = 3;
+  o.amg.dense_work_per_unknown = 0;
+  o.amg.coarsen_dense = 1;
+  o.amg.reaggregate = 1;
+  o.amg_min_nodes = 160;
+  o.precision = SVXG_PRECISION_FP64;
+  return o;
+}
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SVXG_TYPES_H */

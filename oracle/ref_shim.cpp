@@ -1,0 +1,345 @@
+// ref_shim.cpp - TEST INFRASTRUCTURE ONLY (the oracle). Never part of the shipped library.
+//
+// A C ABI over the reference's own svx::StressProblem / svx::Amg, compiled together with the
+// reference's solve sources (core/src/solve/amg.cpp, core/src/stress/stress.cpp,
+// core/src/material/material.cpp, core/src/base/parallel.cpp) by oracle/build_oracle.py into
+// oracle/_ref/libsvxref.so. The tests use it to pin the C restatement (oracle/svx_oracle.c) and to
+// write the golden fixtures; bench.py's reference arm times it where it exists.
+//
+// The hierarchy export needs the multigrid's levels before Amg::make_fast frees their
+// double-precision copies (core/src/solve/amg.cpp:594-628), so this file alone opens the
+// reference classes' private members (the access keyword only: layouts are unchanged) and walks
+// the build's level loop (core/src/solve/amg.cpp:285-304) itself.
+#define private public
+#include "svx/base/parallel.hpp"
+#include "svx/material/material.hpp"
+#include "svx/solve/amg.hpp"
+#include "svx/stress/stress.hpp"
+#undef private
+
+#include <chrono>
+#include <cstring>
+#include <vector>
+
+#include "svxg_types.h"
+
+using namespace svx;
+
+namespace {
+
+static_assert(sizeof(svxg_node) == 40, "svxg_node layout");
+static_assert(sizeof(svxg_bond) == 216, "svxg_bond layout");
+static_assert(sizeof(svxg_material) == 64, "svxg_material layout");
+
+V3 v3(const svxg_v3& v) { return V3{v.x, v.y, v.z}; }
+
+void fill_materials(MaterialTable& t, const svxg_material* m) {
+  for (int i = 0; i < SVXG_MAX_MATERIALS; ++i) {
+    Material x = t[static_cast<MaterialId>(i)];
+    x.E = m[i].E;
+    x.G = m[i].G;
+    x.rho = m[i].rho;
+    x.ft = m[i].ft;
+    x.fb = m[i].fb;
+    x.fc = m[i].fc;
+    x.cohesion = m[i].cohesion;
+    x.friction = m[i].friction;
+    t.set(static_cast<MaterialId>(i), x);
+  }
+}
+
+void fill_problem(StressProblem& P, const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb) {
+  P.nodes.resize(size_t(n));
+  for (int32_t i = 0; i < n; ++i) {
+    SNode& s = P.nodes[size_t(i)];
+    s.c = v3(nodes[i].c);
+    s.mass = nodes[i].mass;
+    s.fixed = nodes[i].fixed != 0;
+    s.gone = nodes[i].gone != 0;
+  }
+  P.bonds.resize(size_t(nb));
+  for (int32_t k = 0; k < nb; ++k) {
+    const svxg_bond& b = bonds[k];
+    SBond& s = P.bonds[size_t(k)];
+    s.a = b.a;
+    s.b = b.b;
+    s.broken = b.broken != 0;
+    s.in_k = b.in_k != 0;
+    s.ma = static_cast<MaterialId>(b.ma);
+    s.mb = static_cast<MaterialId>(b.mb);
+    s.n = v3(b.n);
+    s.t1 = v3(b.t1);
+    s.t2 = v3(b.t2);
+    s.area = b.area;
+    s.p = v3(b.p);
+    s.s1 = b.s1;
+    s.s2 = b.s2;
+    s.c1 = b.c1;
+    s.c2 = b.c2;
+    s.rmax = b.rmax;
+    s.la = b.la;
+    s.lb = b.lb;
+    s.strength = b.strength;
+    s.sectioned = b.sectioned != 0;
+    s.ft = b.ft;
+    s.fb = b.fb;
+    s.fc = b.fc;
+    s.coh = b.coh;
+    s.mu = b.mu;
+    s.faces = b.faces;
+    s.tag = b.tag;
+  }
+}
+
+StressOptions options(const svxg_stress_options* o) {
+  StressOptions so;
+  if (!o) return so;
+  so.rtol = o->rtol;
+  so.amg.coarse_max = o->amg.coarse_max;
+  so.amg.strength = o->amg.strength;
+  so.amg.smoothed = o->amg.smoothed != 0;
+  so.amg.coarse_scale = o->amg.coarse_scale;
+  so.amg.max_levels = o->amg.max_levels;
+  so.amg.gamma = o->amg.gamma;
+  so.amg.sgs = o->amg.sgs != 0;
+  so.amg.sweeps = o->amg.sweeps;
+  so.amg.cheb_degree = o->amg.cheb_degree;
+  so.amg.dense_work_per_unknown = o->amg.dense_work_per_unknown != 0;
+  so.amg.coarsen_dense = o->amg.coarsen_dense != 0;
+  so.amg.reaggregate = o->amg.reaggregate != 0;
+  so.amg_min_nodes = o->amg_min_nodes;
+  return so;
+}
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct Hier {
+  Amg amg;
+  std::vector<f64> lmax;  // lambda_max(D^-1 A) estimate per level (the prolongation's damping)
+};
+
+}  // namespace
+
+extern "C" {
+
+struct svxr_info {
+  int32_t nfree, levels, block_jacobi, chol_n;
+  int32_t level_sizes[16];
+  int64_t level_blocks[32];
+  int64_t matrix_blocks, work_per_iteration, assembly_work, work_per_apply, build_work;
+};
+
+void svxr_set_threads(int n) { set_num_threads(n); }
+int svxr_num_threads(void) { return num_threads(); }
+
+// assemble() + solve() of the reference problem. u: 6 per node (warm start in, solution out).
+// bonds[].in_k is written back. Returns assemble()'s result (1/0).
+int svxr_solve(const svxg_node* nodes, int32_t n, svxg_bond* bonds, int32_t nb, const svxg_material* mats,
+               const svxg_stress_options* o, const double* f, double* u, double rtol, int32_t maxit, int32_t warm,
+               svxg_pcg_result* res, svxr_info* info, double* t_assemble, double* t_solve) {
+  MaterialTable table;
+  fill_materials(table, mats);
+  StressProblem P;
+  P.mats = &table;
+  fill_problem(P, nodes, n, bonds, nb);
+  const double t0 = now_s();
+  const bool ok = P.assemble(options(o));
+  const double t1 = now_s();
+  std::vector<f64> fv(f, f + 6 * size_t(n)), uv(u, u + 6 * size_t(n));
+  PcgResult r;
+  double t2 = t1, t3 = t1;
+  if (ok) {
+    t2 = now_s();
+    r = P.solve(fv, uv, rtol, maxit, warm != 0);
+    t3 = now_s();
+    std::memcpy(u, uv.data(), sizeof(double) * 6 * size_t(n));
+  }
+  if (res) {
+    res->iters = r.iters;
+    res->converged = r.converged;
+    res->breakdown = r.breakdown;
+    res->rel_res = r.rel_res;
+  }
+  for (int32_t k = 0; k < nb; ++k) bonds[k].in_k = P.bonds[size_t(k)].in_k ? 1 : 0;
+  if (info) {
+    std::memset(info, 0, sizeof(*info));
+    info->nfree = P.free_nodes();
+    info->block_jacobi = P.block_jacobi();
+    info->levels = P.amg_.levels();
+    info->chol_n = P.amg_.chol_n_;
+    const std::vector<i32> ls = P.amg_.level_sizes();
+    const std::vector<i64> lb = P.amg_.level_blocks();
+    for (size_t i = 0; i < ls.size() && i < 16; ++i) info->level_sizes[i] = ls[i];
+    for (size_t i = 0; i < lb.size() && i < 32; ++i) info->level_blocks[i] = lb[i];
+    info->matrix_blocks = P.matrix_blocks();
+    info->work_per_iteration = P.work_per_iteration();
+    info->assembly_work = P.assembly_work();
+    info->work_per_apply = P.amg_.work_per_apply();
+    info->build_work = P.amg_.build_work();
+  }
+  if (t_assemble) *t_assemble = t1 - t0;
+  if (t_solve) *t_solve = t3 - t2;
+  return ok ? 1 : 0;
+}
+
+// The judge's per-bond work: bond_load and bond_utilization (core/src/stress/stress.cpp:477-502,
+// :23-57) of every bond at u (6 per node).
+void svxr_judge(const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb, const svxg_material* mats,
+                const double* u, double fragility, svxg_bond_load* loads, double* phi, uint8_t* mode, double* t_judge) {
+  MaterialTable table;
+  fill_materials(table, mats);
+  StressProblem P;
+  P.mats = &table;
+  fill_problem(P, nodes, n, bonds, nb);
+  std::vector<f64> uv(u, u + 6 * size_t(n));
+  const double t0 = now_s();
+  for (int32_t k = 0; k < nb; ++k) {
+    const BondLoad L = P.bond_load(k, uv);
+    FailMode m = FailMode::None;
+    const f64 ph = bond_utilization(P.bonds[size_t(k)], L, fragility, table, &m);
+    if (loads) loads[k] = svxg_bond_load{L.N, L.V1, L.V2, L.T, L.M1, L.M2};
+    if (phi) phi[k] = ph;
+    if (mode) mode[k] = static_cast<uint8_t>(m);
+  }
+  if (t_judge) *t_judge = now_s() - t0;
+}
+
+// bond_utilization of given loads (the failure-mode known answers).
+double svxr_utilization(const svxg_bond* bond, const svxg_bond_load* L, double fragility, const svxg_material* mats,
+                        uint8_t* mode) {
+  MaterialTable table;
+  fill_materials(table, mats);
+  StressProblem P;
+  svxg_node dummy[2] = {};
+  svxg_bond b = *bond;
+  b.a = 0;
+  b.b = b.b >= 0 ? 1 : -1;
+  fill_problem(P, dummy, 2, &b, 1);
+  BondLoad l;
+  l.N = L->N;
+  l.V1 = L->V1;
+  l.V2 = L->V2;
+  l.T = L->T;
+  l.M1 = L->M1;
+  l.M2 = L->M2;
+  FailMode m = FailMode::None;
+  const f64 ph = bond_utilization(P.bonds[0], l, fragility, table, &m);
+  if (mode) *mode = static_cast<uint8_t>(m);
+  return ph;
+}
+
+// K of the reference's build_matrix (core/src/stress/stress.cpp:84-132): call with null arrays
+// for the sizes, then with arrays of those sizes. dof: n; rowptr: nfree + 1; col: nnzb;
+// val: 36 nnzb.
+int svxr_matrix(const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb, const svxg_material* mats,
+                int32_t* nfree, int64_t* nnzb, int32_t* dof, int32_t* rowptr, int32_t* col, double* val, double* id_scale) {
+  MaterialTable table;
+  fill_materials(table, mats);
+  StressProblem P;
+  P.mats = &table;
+  fill_problem(P, nodes, n, bonds, nb);
+  StressOptions so;
+  so.amg_min_nodes = 1 << 30;  // (block-Jacobi: K alone)
+  if (!P.assemble(so)) return 0;
+  *nfree = P.K_.n;
+  *nnzb = P.K_.blocks();
+  if (dof) std::memcpy(dof, P.dof_.data(), sizeof(int32_t) * P.dof_.size());
+  if (rowptr) std::memcpy(rowptr, P.K_.rowptr.data(), sizeof(int32_t) * P.K_.rowptr.size());
+  if (col) std::memcpy(col, P.K_.col.data(), sizeof(int32_t) * P.K_.col.size());
+  if (val) std::memcpy(val, P.K_.val.data(), sizeof(double) * P.K_.val.size());
+  if (id_scale) *id_scale = P.id_scale_;
+  return 1;
+}
+
+// The multigrid hierarchy of K before its single-precision conversion: every level's A, D^-1,
+// aggregates (parent), prolongation and lambda_max estimate, and the coarsest dense factor.
+void* svxr_hier_build(const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb, const svxg_material* mats,
+                      const svxg_stress_options* o, int32_t* ok) {
+  MaterialTable table;
+  fill_materials(table, mats);
+  StressProblem P;
+  P.mats = &table;
+  fill_problem(P, nodes, n, bonds, nb);
+  StressOptions so = options(o);
+  const i32 min_nodes = so.amg_min_nodes;
+  so.amg_min_nodes = 1 << 30;
+  *ok = 0;
+  if (!P.assemble(so)) return nullptr;
+  (void)min_nodes;
+  std::vector<V3> pos(size_t(P.nfree_));
+  for (size_t i = 0; i < P.nodes.size(); ++i)
+    if (P.dof_[i] >= 0) pos[size_t(P.dof_[i])] = P.nodes[i].c;
+  Hier* h = new Hier;
+  Amg& a = h->amg;
+  a.opt_ = so.amg;
+  a.lv_.clear();
+  a.chol_.clear();
+  a.chol_n_ = 0;
+  a.work_ = 0;
+  a.build_work_ = 0;
+  if (P.K_.n == 0) {
+    *ok = 1;
+    return h;
+  }
+  a.lv_.emplace_back();
+  a.lv_[0].A = P.K_;
+  a.lv_[0].pos = pos;
+  if (!a.finalize(a.lv_[0])) {
+    delete h;
+    return nullptr;
+  }
+  while (static_cast<int>(a.lv_.size()) < a.opt_.max_levels && a.lv_.back().A.n > a.opt_.coarse_max) {
+    const Bsr6& L = a.lv_.back().A;
+    const bool dense = a.lv_.size() > 1 && L.blocks() > 80 * static_cast<i64>(L.n);
+    if (dense && !a.opt_.coarsen_dense) break;
+    if (!a.coarsen(a.lv_.size() - 1, !dense && a.opt_.smoothed)) break;
+    if (dense) break;
+  }
+  a.factor_coarsest();
+  for (auto& L : a.lv_) h->lmax.push_back(a.estimate_lmax(L));
+  *ok = 1;
+  return h;
+}
+
+int32_t svxr_hier_levels(void* hp) { return static_cast<Hier*>(hp)->amg.levels(); }
+
+int32_t svxr_hier_chol_n(void* hp) { return static_cast<Hier*>(hp)->amg.chol_n_; }
+
+void svxr_hier_chol(void* hp, double* out) {
+  const Hier* h = static_cast<Hier*>(hp);
+  std::memcpy(out, h->amg.chol_.data(), sizeof(double) * h->amg.chol_.size());
+}
+
+void svxr_hier_dims(void* hp, int32_t l, int32_t* n, int64_t* nnzb, int64_t* pnnz) {
+  const auto& L = static_cast<Hier*>(hp)->amg.lv_[size_t(l)];
+  *n = L.A.n;
+  *nnzb = L.A.blocks();
+  *pnnz = static_cast<int64_t>(L.Pcol.size());
+}
+
+void svxr_hier_get(void* hp, int32_t l, int32_t* rowptr, int32_t* col, double* val, double* dinv, int32_t* parent,
+                   int32_t* prow, int32_t* pcol, double* pval, double* pos, double* lmax) {
+  const Hier* h = static_cast<Hier*>(hp);
+  const auto& L = h->amg.lv_[size_t(l)];
+  if (rowptr) std::memcpy(rowptr, L.A.rowptr.data(), sizeof(int32_t) * L.A.rowptr.size());
+  if (col) std::memcpy(col, L.A.col.data(), sizeof(int32_t) * L.A.col.size());
+  if (val) std::memcpy(val, L.A.val.data(), sizeof(double) * L.A.val.size());
+  if (dinv) std::memcpy(dinv, L.Dinv.data(), sizeof(double) * L.Dinv.size());
+  if (parent) std::memcpy(parent, L.parent.data(), sizeof(int32_t) * L.parent.size());
+  if (prow) std::memcpy(prow, L.Prow.data(), sizeof(int32_t) * L.Prow.size());
+  if (pcol) std::memcpy(pcol, L.Pcol.data(), sizeof(int32_t) * L.Pcol.size());
+  if (pval) std::memcpy(pval, L.Pval.data(), sizeof(double) * L.Pval.size());
+  if (pos)
+    for (size_t i = 0; i < L.pos.size(); ++i) {
+      pos[3 * i] = L.pos[i].x;
+      pos[3 * i + 1] = L.pos[i].y;
+      pos[3 * i + 2] = L.pos[i].z;
+    }
+  if (lmax) *lmax = h->lmax[size_t(l)];
+}
+
+void svxr_hier_free(void* hp) { delete static_cast<Hier*>(hp); }
+
+}  // extern "C"

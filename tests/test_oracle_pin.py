@@ -1,0 +1,80 @@
+"""Pins the oracle (the C restatement) to the reference compiled from its own sources.
+
+Runs only where the reference tree is present (it is built into oracle/_ref/ from there); the
+committed golden fixtures (tests/test_oracle_golden.py) carry the same pin to machines without
+it. Every comparison is bit for bit: the restatement follows the reference's operation order.
+"""
+import numpy as np
+import pytest
+
+import fixtures as fx
+from opus_destruct_2_gb300.graph import StressOptions, default_materials
+from oracle import Port, Reference, reference_lib
+from opus_destruct_2_gb300 import synth
+
+pytestmark = pytest.mark.skipif(reference_lib() is None, reason="the reference is not built on this machine")
+
+MATS = default_materials()
+
+CASES = [
+    ("cantilever12", lambda: fx.cantilever(12, 0.5, 300.0), dict(amg_min_nodes=4), 1e-10),
+    ("lattice8_amg", lambda: fx.lattice(8), dict(amg_min_nodes=16), 1e-9),
+    ("lattice8_jacobi", lambda: fx.lattice(8), dict(amg_min_nodes=1 << 30), 1e-9),
+    ("lattice8_unsmoothed", lambda: fx.lattice(8), dict(smoothed=0), 1e-8),
+    ("lattice16", lambda: fx.lattice(16), dict(), 1e-8),
+    ("lattice16_once", lambda: fx.lattice(16), dict(reaggregate=0), 1e-8),
+    ("lattice16_dense_smoothed", lambda: fx.lattice(16), dict(reaggregate=0, coarsen_dense=0), 1e-8),
+    ("lattice14_retired", lambda: fx.lattice(14, keep_z=9, retire_top=True), dict(amg_min_nodes=16), 1e-8),
+    ("tower_small", lambda: synth.tower_graph(storeys=3, seed=3)[:2], dict(), 1e-8),
+    ("piece_free", lambda: synth.piece_graph(300, free=True, seed=11)[:2], dict(amg_min_nodes=0), 1e-8),
+]
+
+
+@pytest.mark.parametrize("name,make,opts,rtol", CASES, ids=[c[0] for c in CASES])
+def test_solve_bit_identical(name, make, opts, rtol):
+    nodes, bonds = make()
+    f = fx.gravity_live(nodes)
+    opt = StressOptions(**opts)
+    r = Reference(nodes, bonds, MATS).solve(f, opt, rtol=rtol, maxit=2000)
+    P = Port(nodes, bonds, MATS)
+    assert P.assemble(opt) == r["ok"]
+    u, res = P.solve(f, rtol=rtol, maxit=2000)
+    assert res.iters == r["res"].iters
+    assert res.converged == r["res"].converged and res.breakdown == r["res"].breakdown
+    assert res.rel_res == r["res"].rel_res
+    assert np.array_equal(u, r["u"])
+    a, b = P.info(), r["info"]
+    assert a.sizes() == b.sizes() and a.blocks() == b.blocks()
+    for k in ("nfree", "chol_n", "matrix_blocks", "work_per_iteration", "assembly_work", "work_per_apply",
+              "build_work", "block_jacobi"):
+        assert getattr(a, k) == getattr(b, k), k
+    # the judge: loads, utilizations and modes of every bond
+    la, pa, ma = P.judge(u)
+    lb, pb, mb = Reference(nodes, bonds, MATS).judge(u)
+    assert np.array_equal(la, lb) and np.array_equal(pa, pb) and np.array_equal(ma, mb)
+
+
+@pytest.mark.parametrize("name,make,opts,rtol", CASES[:8], ids=[c[0] for c in CASES[:8]])
+def test_matrix_and_hierarchy_bit_identical(name, make, opts, rtol):
+    nodes, bonds = make()
+    opt = StressOptions(**opts)
+    R = Reference(nodes, bonds, MATS)
+    P = Port(nodes, bonds, MATS)
+    P.keep_levels(True)
+    ka, kb = P.matrix() if P.assemble(StressOptions(amg_min_nodes=1 << 30)) else None, R.matrix()
+    for k in ("dof", "rowptr", "col", "val"):
+        assert np.array_equal(ka[k], kb[k]), k
+    assert ka["id_scale"] == kb["id_scale"]
+    if opt.amg_min_nodes > 4096:
+        return
+    P2 = Port(nodes, bonds, MATS)
+    P2.keep_levels(True)
+    assert P2.assemble(StressOptions(**dict(opts, amg_min_nodes=0)))
+    la = P2.levels()
+    lb, chol = R.levels(StressOptions(**opts))
+    assert len(la) == len(lb)
+    for A, B in zip(la, lb):
+        for k in ("rowptr", "col", "val", "dinv", "parent", "prow", "pcol", "pval", "pos"):
+            assert np.array_equal(getattr(A, k), getattr(B, k)), k
+        assert A.lmax.value == B.lmax.value
+    assert np.array_equal(P2.chol(), chol)
