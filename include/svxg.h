@@ -1,0 +1,128 @@
+/* svxg.h - C ABI of the GB300 stress solve (hand-written sm_103a kernels, one GPU).
+ *
+ * This is the boundary a host binds in place of the reference's svx::StressProblem
+ * (core/include/svx/stress/stress.hpp:74-160), the only solve type the reference's callers use
+ * (World::Impl's Structure::P and BodyGraph::P, core/src/world/world_internal.hpp:745, :768).
+ * Each entry point names the member it replaces. A problem owns its device buffers and one
+ * CUDA stream; distinct problems may be driven from distinct host threads at the same time.
+ *
+ * Conventions: functions return SVXG_OK (0) or a negative SVXG_ERR_* code and never abort;
+ * svxg_last_error() gives the calling thread's last message. Vectors f and u hold 6 doubles
+ * per node (translation, rotation) in node order, fixed nodes 0, as the reference's.
+ */
+#ifndef SVXG_H
+#define SVXG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "svxg_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SVXG_OK 0
+#define SVXG_ERR_ARG (-1)      /* bad argument or size */
+#define SVXG_ERR_CUDA (-2)     /* a CUDA call failed (message in svxg_last_error) */
+#define SVXG_ERR_NOMEM (-3)    /* device memory (or the problem's budget) exhausted */
+#define SVXG_ERR_STATE (-4)    /* not assembled / no graph */
+#define SVXG_ERR_TIMEOUT (-5)  /* a bounded device wait gave up */
+#define SVXG_ERR_NODEVICE (-6) /* no CUDA device */
+
+typedef struct svxg_problem svxg_problem;
+
+/* The reference's counters (Amg::level_sizes / level_blocks / work_per_apply / build_work,
+ * amg.hpp:77-81; StressProblem::matrix_blocks / work_per_iteration / assembly_work,
+ * stress.hpp:103-119) plus device bytes. */
+typedef struct svxg_info {
+  int32_t nfree, levels, block_jacobi, chol_n;
+  int32_t level_sizes[16];
+  int64_t level_blocks[32]; /* matrix blocks per level, then prolongation blocks per level */
+  int64_t matrix_blocks, work_per_iteration, assembly_work, work_per_apply, build_work;
+  int64_t device_bytes;     /* what the problem holds on the device now */
+  int32_t precision;        /* SVXG_PRECISION_* of the last assemble */
+  int32_t pad;
+} svxg_info;
+
+const char* svxg_last_error(void);
+int svxg_device_count(void);
+
+/* --- lifecycle (StressProblem's constructor / destructor) ----------------------------------- */
+int svxg_problem_create(svxg_problem** out, int device);
+void svxg_problem_destroy(svxg_problem* p);
+/* The problem's CUDA stream (a cudaStream_t), for callers that order their own work on it. */
+void* svxg_problem_stream(svxg_problem* p);
+
+/* The graph: replaces the public members nodes, bonds, mats (stress.hpp:76-79). Copies them to
+ * the device; the caller keeps its arrays. mats: SVXG_MAX_MATERIALS resolved entries. Call
+ * again whenever the caller changed nodes or bonds between calls (invalidates the assembly). */
+int svxg_set_graph(svxg_problem* p, const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb,
+                   const svxg_material* mats);
+
+/* StressProblem::assemble (stress.hpp:83, stress.cpp:134-176): K over the intact bonds and the
+ * preconditioner. *ok = 1 assembled, 0 singular diagonal (the reference's false). */
+int svxg_assemble(svxg_problem* p, const svxg_stress_options* opt, int32_t* ok);
+/* StressProblem::assembled / invalidate / preconditioner_current / block_jacobi (stress.hpp:84-92) */
+int svxg_assembled(const svxg_problem* p);
+int svxg_invalidate(svxg_problem* p);
+int svxg_preconditioner_current(const svxg_problem* p);
+int svxg_block_jacobi(const svxg_problem* p);
+/* StressProblem::release (stress.hpp:99, stress.cpp:326-339): frees K, the hierarchy and the
+ * run state; the graph stays. */
+int svxg_release(svxg_problem* p);
+
+/* StressProblem::remove_bond / retire_nodes (stress.hpp:108-109, stress.cpp:260-310): in-place
+ * K downdates that keep the preconditioner. */
+int svxg_remove_bond(svxg_problem* p, int32_t b);
+int svxg_retire_nodes(svxg_problem* p, const int32_t* list, int32_t count);
+/* The bonds' in_k / broken flags as the problem keeps them (the reference writes them into the
+ * caller's bonds). Either pointer may be null. */
+int svxg_bond_flags(svxg_problem* p, uint8_t* broken, uint8_t* in_k);
+
+/* --- the solve ------------------------------------------------------------------------------ */
+/* StressProblem::solve (stress.hpp:122, stress.cpp:348-360). f, u: host arrays of 6 n doubles;
+ * u is the warm start when warm != 0 and the solution on return. maxit < 0: no cap. */
+int svxg_solve(svxg_problem* p, const double* f, double* u, double rtol, int32_t maxit, int32_t warm,
+               svxg_pcg_result* res);
+/* The same with f and u in device memory (node order, 6 per node). */
+int svxg_solve_device(svxg_problem* p, const double* f_dev, double* u_dev, double rtol, int32_t maxit, int32_t warm,
+                      svxg_pcg_result* res);
+/* StressProblem::begin / iterate / running / stop / current (stress.hpp:126-130, stress.cpp:362-475).
+ * u0 may be null (cold start). */
+int svxg_begin(svxg_problem* p, const double* f, const double* u0);
+int svxg_iterate(svxg_problem* p, int32_t maxit, double rtol, svxg_pcg_result* res);
+int svxg_running(const svxg_problem* p);
+int svxg_stop(svxg_problem* p);
+int svxg_current(svxg_problem* p, double* u);
+
+/* --- bond loads and failure checks ------------------------------------------------------------ */
+/* StressProblem::bond_load (stress.hpp:132, stress.cpp:477-502) of every bond, at u (host, 6 n)
+ * or, when u is null, at the current solution. out: nb records. */
+int svxg_bond_loads(svxg_problem* p, const double* u, svxg_bond_load* out);
+/* bond_utilization (stress.hpp:64-66, stress.cpp:23-57) of every bond at the current solution:
+ * phi (nb doubles) and mode (nb bytes, SVXG_FAIL_*), either may be null; over receives the
+ * indices of the bonds with phi >= 1 in ascending order (capacity `cap`), *n_over their count. */
+int svxg_utilization(svxg_problem* p, double fragility, double* phi, uint8_t* mode, int32_t* over, int32_t cap,
+                     int32_t* n_over);
+
+/* --- counters ------------------------------------------------------------------------------- */
+int svxg_get_info(svxg_problem* p, svxg_info* info);
+
+/* --- parity access (tests) ------------------------------------------------------------------ */
+/* K as assembled: call with null arrays for *nfree / *nnzb, then with arrays of those sizes. */
+int svxg_debug_matrix(svxg_problem* p, int32_t* nfree, int64_t* nnzb, int32_t* dof, int32_t* rowptr, int32_t* col,
+                      double* val, double* id_scale);
+/* One multigrid level in double precision: sizes, then arrays (any may be null). */
+int svxg_debug_level_dims(svxg_problem* p, int32_t level, int32_t* n, int64_t* nnzb, int64_t* pnnz);
+int svxg_debug_level(svxg_problem* p, int32_t level, int32_t* rowptr, int32_t* col, double* val, double* dinv,
+                     int32_t* parent, int32_t* prow, int32_t* pcol, double* pval, double* pos, double* lmax);
+/* z = M^-1 r and y = K x over the free DOFs (host arrays of 6 nfree). */
+int svxg_debug_precondition(svxg_problem* p, const double* r, double* z);
+int svxg_debug_apply(svxg_problem* p, const double* x, double* y);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SVXG_H */

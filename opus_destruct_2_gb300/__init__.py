@@ -1,0 +1,323 @@
+"""GB300-native stress solve of fragment graphs (the svx_core StressProblem path on sm_103a).
+
+``StressProblem`` mirrors the reference's ``svx::StressProblem`` (core/include/svx/stress/stress.hpp:
+74-160) over the C ABI of ``include/svxg.h``: the same members (nodes, bonds, mats), the same
+calls (assemble, solve, begin/iterate/current, bond_load, remove_bond, retire_nodes, release ...)
+and the same results and error behaviour (assemble -> False on a singular diagonal; a solve of
+non-finite loads -> breakdown with rel_res = inf; zero load -> converged, u = 0). Every number is
+computed by the CUDA library; there is no CPU path: if the library cannot be loaded, or no GPU
+is present, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+from . import build as _build
+from .graph import (BOND_DTYPE, LOAD_DTYPE, MATERIAL_DTYPE, NODE_DTYPE, PcgResult, StressOptions, default_materials,
+                    ptr)
+
+__all__ = ["StressProblem", "StressOptions", "PcgResult", "Info", "load_library", "default_materials",
+           "NODE_DTYPE", "BOND_DTYPE", "SvxgError"]
+
+c_i32, c_i64, c_f64, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p
+
+ERRORS = {-1: "bad argument", -2: "CUDA error", -3: "out of device memory", -4: "wrong state", -5: "timeout",
+          -6: "no CUDA device"}
+
+
+class SvxgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"svxg error {code} ({ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+class Info(ctypes.Structure):
+    _fields_ = [("nfree", c_i32), ("levels", c_i32), ("block_jacobi", c_i32), ("chol_n", c_i32),
+                ("level_sizes", c_i32 * 16), ("level_blocks", c_i64 * 32), ("matrix_blocks", c_i64),
+                ("work_per_iteration", c_i64), ("assembly_work", c_i64), ("work_per_apply", c_i64),
+                ("build_work", c_i64), ("device_bytes", c_i64), ("precision", c_i32), ("pad", c_i32)]
+
+    def sizes(self) -> list[int]:
+        return [self.level_sizes[i] for i in range(self.levels)]
+
+    def blocks(self) -> list[int]:
+        return [self.level_blocks[i] for i in range(2 * self.levels)]
+
+
+_lib: ctypes.CDLL | None = None
+
+
+def library_path() -> str:
+    return os.path.join(_build.LIBDIR, _build.CUDA_LIB)
+
+
+def load_library() -> ctypes.CDLL:
+    """The CUDA library (built in-tree by __graft_entry__.build()); raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        raise RuntimeError(f"the CUDA library is not built ({path}); run __graft_entry__.build()")
+    L = ctypes.CDLL(path)
+    sig = {
+        "svxg_last_error": (ctypes.c_char_p, []),
+        "svxg_device_count": (c_i32, []),
+        "svxg_problem_create": (c_i32, [ctypes.POINTER(c_vp), c_i32]),
+        "svxg_problem_destroy": (None, [c_vp]),
+        "svxg_problem_stream": (c_vp, [c_vp]),
+        "svxg_set_graph": (c_i32, [c_vp, c_vp, c_i32, c_vp, c_i32, c_vp]),
+        "svxg_assemble": (c_i32, [c_vp, c_vp, ctypes.POINTER(c_i32)]),
+        "svxg_assembled": (c_i32, [c_vp]),
+        "svxg_invalidate": (c_i32, [c_vp]),
+        "svxg_preconditioner_current": (c_i32, [c_vp]),
+        "svxg_block_jacobi": (c_i32, [c_vp]),
+        "svxg_release": (c_i32, [c_vp]),
+        "svxg_remove_bond": (c_i32, [c_vp, c_i32]),
+        "svxg_retire_nodes": (c_i32, [c_vp, c_vp, c_i32]),
+        "svxg_bond_flags": (c_i32, [c_vp, c_vp, c_vp]),
+        "svxg_solve": (c_i32, [c_vp, c_vp, c_vp, c_f64, c_i32, c_i32, c_vp]),
+        "svxg_solve_device": (c_i32, [c_vp, c_vp, c_vp, c_f64, c_i32, c_i32, c_vp]),
+        "svxg_begin": (c_i32, [c_vp, c_vp, c_vp]),
+        "svxg_iterate": (c_i32, [c_vp, c_i32, c_f64, c_vp]),
+        "svxg_running": (c_i32, [c_vp]),
+        "svxg_stop": (c_i32, [c_vp]),
+        "svxg_current": (c_i32, [c_vp, c_vp]),
+        "svxg_bond_loads": (c_i32, [c_vp, c_vp, c_vp]),
+        "svxg_utilization": (c_i32, [c_vp, c_f64, c_vp, c_vp, c_vp, c_i32, ctypes.POINTER(c_i32)]),
+        "svxg_get_info": (c_i32, [c_vp, c_vp]),
+        "svxg_debug_matrix": (c_i32, [c_vp, ctypes.POINTER(c_i32), ctypes.POINTER(c_i64), c_vp, c_vp, c_vp, c_vp,
+                                      ctypes.POINTER(c_f64)]),
+        "svxg_debug_level_dims": (c_i32, [c_vp, c_i32, ctypes.POINTER(c_i32), ctypes.POINTER(c_i64),
+                                          ctypes.POINTER(c_i64)]),
+        "svxg_debug_level": (c_i32, [c_vp, c_i32] + [c_vp] * 9 + [ctypes.POINTER(c_f64)]),
+        "svxg_debug_precondition": (c_i32, [c_vp, c_vp, c_vp]),
+        "svxg_debug_apply": (c_i32, [c_vp, c_vp, c_vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(code: int) -> int:
+    if code < 0:
+        msg = load_library().svxg_last_error()
+        raise SvxgError(code, msg.decode() if msg else "")
+    return code
+
+
+class StressProblem:
+    """svx::StressProblem on the GPU. ``nodes``/``bonds`` are numpy records (graph.NODE_DTYPE /
+    BOND_DTYPE), ``mats`` a material table; assign them, then call assemble() (the graph is sent
+    to the device at assemble time, or whenever it changed)."""
+
+    def __init__(self, nodes=None, bonds=None, mats=None, device: int = 0):
+        L = load_library()
+        if L.svxg_device_count() <= device:
+            raise SvxgError(-6, "no CUDA device")
+        h = c_vp()
+        _check(L.svxg_problem_create(ctypes.byref(h), device))
+        self._h = h
+        self._L = L
+        self.nodes = np.zeros(0, NODE_DTYPE) if nodes is None else np.array(nodes, dtype=NODE_DTYPE)
+        self.bonds = np.zeros(0, BOND_DTYPE) if bonds is None else np.array(bonds, dtype=BOND_DTYPE)
+        self.mats = default_materials() if mats is None else np.array(mats, dtype=MATERIAL_DTYPE)
+        if len(self.mats) != 127:
+            raise ValueError("mats: 127 resolved material records")
+        self._sent = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if sys.is_finalizing():  # (the CUDA runtime may be gone already; the process frees all)
+            return
+        if h is not None and h.value:
+            self._L.svxg_problem_destroy(h)
+            self._h = None
+
+    # -- the graph -------------------------------------------------------------------------
+    def _sync_graph(self):
+        key = (self.nodes.__array_interface__["data"][0], self.nodes.tobytes(), self.bonds.tobytes(),
+               self.mats.tobytes())
+        if self._sent == key:
+            return
+        self.nodes = np.ascontiguousarray(self.nodes, dtype=NODE_DTYPE)
+        self.bonds = np.ascontiguousarray(self.bonds, dtype=BOND_DTYPE)
+        _check(self._L.svxg_set_graph(self._h, ptr(self.nodes), len(self.nodes), ptr(self.bonds), len(self.bonds),
+                                      ptr(self.mats)))
+        self._sent = key
+
+    def _pull_flags(self):
+        br = np.zeros(len(self.bonds), np.uint8)
+        ik = np.zeros(len(self.bonds), np.uint8)
+        _check(self._L.svxg_bond_flags(self._h, ptr(br), ptr(ik)))
+        self.bonds["broken"] = br
+        self.bonds["in_k"] = ik
+        self._sent = (self.nodes.__array_interface__["data"][0], self.nodes.tobytes(), self.bonds.tobytes(),
+                      self.mats.tobytes())
+
+    # -- StressProblem's calls -------------------------------------------------------------------
+    def assemble(self, opt: StressOptions | None = None) -> bool:
+        self._sync_graph()
+        ok = c_i32(0)
+        _check(self._L.svxg_assemble(self._h, ctypes.byref(opt) if opt is not None else None, ctypes.byref(ok)))
+        self._pull_flags()
+        return bool(ok.value)
+
+    def assembled(self) -> bool:
+        return bool(self._L.svxg_assembled(self._h))
+
+    def invalidate(self):
+        _check(self._L.svxg_invalidate(self._h))
+
+    def preconditioner_current(self) -> bool:
+        return bool(self._L.svxg_preconditioner_current(self._h))
+
+    def block_jacobi(self) -> bool:
+        return bool(self._L.svxg_block_jacobi(self._h))
+
+    def release(self):
+        _check(self._L.svxg_release(self._h))
+        self.bonds["in_k"] = 0
+
+    def remove_bond(self, b: int):
+        _check(self._L.svxg_remove_bond(self._h, int(b)))
+        self._pull_flags()
+
+    def retire_nodes(self, lst):
+        a = np.ascontiguousarray(lst, dtype=np.int32)
+        _check(self._L.svxg_retire_nodes(self._h, ptr(a), len(a)))
+        self.nodes["gone"][a] = 1
+        self._pull_flags()
+
+    def solve(self, f, u=None, rtol: float = 2e-3, maxit: int = -1, warm: bool = False):
+        """Returns (u, PcgResult); u: 6 per node."""
+        self._sync_graph()
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        if f.size != 6 * len(self.nodes):
+            raise ValueError("f: 6 per node")
+        u = np.zeros(6 * len(self.nodes)) if u is None else np.array(u, dtype=np.float64)
+        res = PcgResult()
+        _check(self._L.svxg_solve(self._h, ptr(f), ptr(u), float(rtol), int(maxit), int(bool(warm)),
+                                  ctypes.byref(res)))
+        self._pull_flags()
+        return u, res
+
+    def begin(self, f, u0=None):
+        self._sync_graph()
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        u0 = None if u0 is None else np.ascontiguousarray(u0, dtype=np.float64)
+        _check(self._L.svxg_begin(self._h, ptr(f), ptr(u0)))
+
+    def iterate(self, maxit: int, rtol: float) -> PcgResult:
+        res = PcgResult()
+        _check(self._L.svxg_iterate(self._h, int(maxit), float(rtol), ctypes.byref(res)))
+        return res
+
+    def running(self) -> bool:
+        return bool(self._L.svxg_running(self._h))
+
+    def stop(self):
+        _check(self._L.svxg_stop(self._h))
+
+    def current(self):
+        u = np.zeros(6 * len(self.nodes))
+        _check(self._L.svxg_current(self._h, ptr(u)))
+        return u
+
+    def bond_loads(self, u=None) -> np.ndarray:
+        out = np.zeros(len(self.bonds), LOAD_DTYPE)
+        u = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
+        _check(self._L.svxg_bond_loads(self._h, ptr(u), ptr(out)))
+        return out
+
+    def bond_load(self, b: int, u) -> np.ndarray:
+        return self.bond_loads(u)[b]
+
+    def utilization(self, fragility: float = 1.0):
+        """(phi, mode, failing bond indices) at the current solution."""
+        nb = len(self.bonds)
+        phi = np.zeros(nb)
+        mode = np.zeros(nb, np.uint8)
+        over = np.zeros(max(nb, 1), np.int32)
+        n_over = c_i32(0)
+        _check(self._L.svxg_utilization(self._h, float(fragility), ptr(phi), ptr(mode), ptr(over), len(over),
+                                        ctypes.byref(n_over)))
+        return phi, mode, over[:n_over.value].copy()
+
+    def info(self) -> Info:
+        i = Info()
+        _check(self._L.svxg_get_info(self._h, ctypes.byref(i)))
+        return i
+
+    def matrix_blocks(self) -> int:
+        return int(self.info().matrix_blocks)
+
+    def free_nodes(self) -> int:
+        return int(self.info().nfree)
+
+    def work_per_iteration(self) -> int:
+        return int(self.info().work_per_iteration)
+
+    def assembly_work(self) -> int:
+        return int(self.info().assembly_work)
+
+    def memory_bytes(self) -> int:
+        return int(self.info().device_bytes)
+
+    def stream(self) -> int:
+        return int(self._L.svxg_problem_stream(self._h) or 0)
+
+    def solve_device(self, f_ptr: int, u_ptr: int, rtol: float, maxit: int = -1, warm: bool = False) -> PcgResult:
+        res = PcgResult()
+        _check(self._L.svxg_solve_device(self._h, c_vp(f_ptr), c_vp(u_ptr), float(rtol), int(maxit),
+                                         int(bool(warm)), ctypes.byref(res)))
+        return res
+
+    # -- parity access -----------------------------------------------------------------------------
+    def debug_matrix(self) -> dict:
+        nf, nz, ids = c_i32(), c_i64(), c_f64()
+        _check(self._L.svxg_debug_matrix(self._h, ctypes.byref(nf), ctypes.byref(nz), None, None, None, None,
+                                         ctypes.byref(ids)))
+        dof = np.zeros(len(self.nodes), np.int32)
+        rowptr = np.zeros(nf.value + 1, np.int32)
+        col = np.zeros(nz.value, np.int32)
+        val = np.zeros((nz.value, 6, 6))
+        _check(self._L.svxg_debug_matrix(self._h, ctypes.byref(nf), ctypes.byref(nz), ptr(dof), ptr(rowptr),
+                                         ptr(col), ptr(val), ctypes.byref(ids)))
+        return dict(nfree=nf.value, dof=dof, rowptr=rowptr, col=col, val=val, id_scale=ids.value)
+
+    def debug_levels(self) -> list[dict]:
+        out = []
+        for l in range(self.info().levels):
+            n, nz, pn = c_i32(), c_i64(), c_i64()
+            _check(self._L.svxg_debug_level_dims(self._h, l, ctypes.byref(n), ctypes.byref(nz), ctypes.byref(pn)))
+            d = dict(rowptr=np.zeros(n.value + 1, np.int32), col=np.zeros(nz.value, np.int32),
+                     val=np.zeros((nz.value, 6, 6)), dinv=np.zeros((n.value, 6, 6)),
+                     parent=np.full(n.value, -1, np.int32), prow=np.zeros(n.value + 1, np.int32),
+                     pcol=np.zeros(pn.value, np.int32), pval=np.zeros((pn.value, 6, 6)), pos=np.zeros((n.value, 3)))
+            lm = c_f64()
+            _check(self._L.svxg_debug_level(self._h, l, ptr(d["rowptr"]), ptr(d["col"]), ptr(d["val"]),
+                                            ptr(d["dinv"]), ptr(d["parent"]), ptr(d["prow"]), ptr(d["pcol"]),
+                                            ptr(d["pval"]), ptr(d["pos"]), ctypes.byref(lm)))
+            d["lmax"] = lm.value
+            out.append(d)
+        return out
+
+    def debug_precondition(self, r):
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        z = np.zeros_like(r)
+        _check(self._L.svxg_debug_precondition(self._h, ptr(r), ptr(z)))
+        return z
+
+    def debug_apply(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros_like(x)
+        _check(self._L.svxg_debug_apply(self._h, ptr(x), ptr(y)))
+        return y

@@ -68,6 +68,8 @@ def cuda_library(force: bool = False, verbose_ptxas: bool = False) -> str:
         if s.endswith(".cu"):
             cmd = [NVCC, *ARCH, "-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC,
                    "--expt-relaxed-constexpr", "-c", s, "-o", o]
+            if os.path.basename(s).startswith("exact_"):
+                cmd.insert(1, "-fmad=false")  # (bit-exact setup arithmetic: no contraction)
             if verbose_ptxas:
                 cmd.insert(1, "-Xptxas=-v")
         else:

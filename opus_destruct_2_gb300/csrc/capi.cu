@@ -1,0 +1,629 @@
+// capi.cu - the C ABI (include/svxg.h): svx::StressProblem's lifecycle over the device state.
+//
+// Host-side bookkeeping mirrors the reference's members (core/src/stress/stress.cpp): the graph
+// is kept on the host as well so that remove_bond / retire_nodes can pick their bonds and rows
+// as the reference does; every number is computed on the device.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "problem.cuh"
+
+struct svxg_problem {
+  svxg::Problem P;
+};
+
+namespace svxg {
+
+namespace {
+thread_local std::string g_error;
+
+struct DeviceScope {
+  int prev = -1;
+  explicit DeviceScope(int d) {
+    cudaGetDevice(&prev);
+    if (prev != d) cudaSetDevice(d);
+  }
+  ~DeviceScope() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+#define TRY(x)            \
+  do {                    \
+    int e__ = (x);        \
+    if (e__) return e__;  \
+  } while (0)
+
+#define CHECK_P(p)                              \
+  do {                                          \
+    if (!(p)) {                                 \
+      set_error("null problem");                \
+      return SVXG_ERR_ARG;                      \
+    }                                           \
+  } while (0)
+
+void release_solver(Problem& P) {
+  free_run(P);
+  P.mem.release(P.K.rowptr);
+  P.mem.release(P.K.col);
+  P.mem.release(P.K.val);
+  P.mem.release(P.K.val32);
+  P.K = Bsr{};
+  P.mem.release(P.d_jinv);
+  P.mem.release(P.d_dof);
+  P.mem.release(P.d_chol);
+  for (Level& L : P.lv) {
+    P.mem.release(L.A.rowptr);
+    P.mem.release(L.A.col);
+    P.mem.release(L.A.val);
+    P.mem.release(L.A.val32);
+    P.mem.release(L.dinv);
+    P.mem.release(L.dinv32);
+    P.mem.release(L.parent);
+    P.mem.release(L.pos);
+    P.mem.release(L.prow);
+    P.mem.release(L.pcol);
+    P.mem.release(L.pval);
+    P.mem.release(L.pval32);
+    P.mem.release(L.rrow);
+    P.mem.release(L.rent_i);
+    P.mem.release(L.rent_e);
+    P.mem.release(L.b32);
+    P.mem.release(L.x32);
+    P.mem.release(L.r32);
+    P.mem.release(L.t32);
+    P.mem.release(L.u32);
+  }
+  P.mem.release(P.d_cinv);
+  P.mem.release(P.d_cvec);
+  P.lv.clear();
+  P.chol_n = 0;
+  P.amg_work = P.amg_build_work = 0;
+  P.assembled = false;
+  P.pc_current = false;
+  P.jacobi_only = false;
+  P.nfree = 0;
+  P.h_dof.clear();
+}
+
+int upload_bond_flags(Problem& P, int32_t b) {
+  // (broken and in_k of one bond, host copy -> device)
+  SVXG_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(P.d_bonds + b) + offsetof(svxg_bond, broken),
+                            &P.h_bonds[size_t(b)].broken, 2, cudaMemcpyHostToDevice, P.stream));
+  return SVXG_OK;
+}
+
+}  // namespace
+
+void set_error(const std::string& msg) { g_error = msg; }
+
+}  // namespace svxg
+
+using namespace svxg;
+
+extern "C" {
+
+const char* svxg_last_error(void) { return g_error.c_str(); }
+
+int svxg_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int svxg_problem_create(svxg_problem** out, int device) {
+  if (!out) return SVXG_ERR_ARG;
+  *out = nullptr;
+  if (svxg_device_count() <= device || device < 0) {
+    set_error("no such CUDA device");
+    return SVXG_ERR_NODEVICE;
+  }
+  DeviceScope ds(device);
+  svxg_problem* p = new (std::nothrow) svxg_problem;
+  if (!p) return SVXG_ERR_NOMEM;
+  p->P.device = device;
+  cudaError_t e = cudaStreamCreateWithFlags(&p->P.stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    set_error(std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+    delete p;
+    return SVXG_ERR_CUDA;
+  }
+  p->P.opt = svxg_default_options();
+  *out = p;
+  return SVXG_OK;
+}
+
+void svxg_problem_destroy(svxg_problem* p) {
+  if (!p) return;
+  DeviceScope ds(p->P.device);
+  cudaStreamSynchronize(p->P.stream);
+  p->P.mem.release_all();
+  if (p->P.h_s) cudaFreeHost(p->P.h_s);
+  cudaStreamDestroy(p->P.stream);
+  delete p;
+}
+
+void* svxg_problem_stream(svxg_problem* p) { return p ? static_cast<void*>(p->P.stream) : nullptr; }
+
+int svxg_set_graph(svxg_problem* p, const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb,
+                   const svxg_material* mats) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  if (n < 0 || nb < 0 || (n > 0 && !nodes) || (nb > 0 && !bonds) || !mats) {
+    set_error("svxg_set_graph: bad sizes or null arrays");
+    return SVXG_ERR_ARG;
+  }
+  for (int32_t k = 0; k < nb; ++k) {
+    const svxg_bond& b = bonds[k];
+    if (b.a < 0 || b.a >= n || b.b >= n || b.b == b.a || b.ma >= SVXG_MAX_MATERIALS || b.mb >= SVXG_MAX_MATERIALS) {
+      set_error("svxg_set_graph: bond " + std::to_string(k) + " has a bad node or material");
+      return SVXG_ERR_ARG;
+    }
+  }
+  DeviceScope ds(P.device);
+  release_solver(P);
+  P.mem.release(P.d_nodes);
+  P.mem.release(P.d_bonds);
+  P.mem.release(P.d_mats);
+  P.mem.release(P.d_un);
+  P.n = n;
+  P.nb = nb;
+  P.h_nodes.assign(nodes, nodes + n);
+  P.h_bonds.assign(bonds, bonds + nb);
+  P.h_mats.assign(mats, mats + SVXG_MAX_MATERIALS);
+  TRY(P.mem.alloc(&P.d_nodes, size_t(n)));
+  TRY(P.mem.alloc(&P.d_bonds, size_t(nb)));
+  TRY(P.mem.alloc(&P.d_mats, size_t(SVXG_MAX_MATERIALS)));
+  if (n) SVXG_CUDA(cudaMemcpyAsync(P.d_nodes, nodes, sizeof(svxg_node) * size_t(n), cudaMemcpyHostToDevice, P.stream));
+  if (nb) SVXG_CUDA(cudaMemcpyAsync(P.d_bonds, bonds, sizeof(svxg_bond) * size_t(nb), cudaMemcpyHostToDevice, P.stream));
+  SVXG_CUDA(cudaMemcpyAsync(P.d_mats, mats, sizeof(svxg_material) * SVXG_MAX_MATERIALS, cudaMemcpyHostToDevice,
+                            P.stream));
+  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  P.have_graph = true;
+  return SVXG_OK;
+}
+
+static int assemble_impl(Problem& P, const svxg_stress_options* opt, int32_t* ok) {
+  if (ok) *ok = 0;
+  if (!P.have_graph) {
+    set_error("svxg_assemble: no graph");
+    return SVXG_ERR_STATE;
+  }
+  DeviceScope ds(P.device);
+  P.opt = opt ? *opt : svxg_default_options();
+  release_solver(P);
+  P.pc_current = true;
+  TRY(assemble_matrix(P));
+  P.assembly_work = 0;
+  for (const svxg_bond& b : P.h_bonds)
+    if (b.in_k) P.assembly_work += 48;
+  P.jacobi_only = P.nfree < P.opt.amg_min_nodes;
+  if (P.jacobi_only) {
+    TRY(build_jacobi(P));
+    P.assembly_work += 12 * int64_t(P.nfree);
+  } else {
+    int32_t built = 0;
+    TRY(build_hierarchy(P, &built));
+    if (!built) {
+      P.assembled = false;
+      return SVXG_OK;
+    }
+    P.assembly_work += P.amg_build_work;
+  }
+  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  P.assembled = true;
+  if (ok) *ok = 1;
+  return SVXG_OK;
+}
+
+int svxg_assemble(svxg_problem* p, const svxg_stress_options* opt, int32_t* ok) {
+  CHECK_P(p);
+  return assemble_impl(p->P, opt, ok);
+}
+
+int svxg_assembled(const svxg_problem* p) { return p && p->P.assembled ? 1 : 0; }
+
+int svxg_invalidate(svxg_problem* p) {
+  CHECK_P(p);
+  p->P.assembled = false;
+  p->P.active = false;
+  return SVXG_OK;
+}
+
+int svxg_preconditioner_current(const svxg_problem* p) { return p && p->P.assembled && p->P.pc_current ? 1 : 0; }
+int svxg_block_jacobi(const svxg_problem* p) { return p && p->P.jacobi_only ? 1 : 0; }
+
+int svxg_release(svxg_problem* p) {
+  CHECK_P(p);
+  DeviceScope ds(p->P.device);
+  cudaStreamSynchronize(p->P.stream);
+  release_solver(p->P);
+  for (svxg_bond& b : p->P.h_bonds) b.in_k = 0;
+  return SVXG_OK;
+}
+
+int svxg_remove_bond(svxg_problem* p, int32_t b) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  if (b < 0 || b >= P.nb) {
+    set_error("svxg_remove_bond: no such bond");
+    return SVXG_ERR_ARG;
+  }
+  DeviceScope ds(P.device);
+  svxg_bond& hb = P.h_bonds[size_t(b)];
+  hb.broken = 1;
+  if (!P.assembled || !hb.in_k) {
+    TRY(upload_bond_flags(P, b));
+    SVXG_CUDA(cudaStreamSynchronize(P.stream));
+    return SVXG_OK;
+  }
+  hb.in_k = 0;
+  TRY(remove_bonds_device(P, &b, 1));
+  if (!P.jacobi_only) P.pc_current = false;
+  P.active = false;
+  return SVXG_OK;
+}
+
+int svxg_retire_nodes(svxg_problem* p, const int32_t* list, int32_t count) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  if (count <= 0) return SVXG_OK;
+  for (int32_t t = 0; t < count; ++t)
+    if (list[t] < 0 || list[t] >= P.n) {
+      set_error("svxg_retire_nodes: no such node");
+      return SVXG_ERR_ARG;
+    }
+  DeviceScope ds(P.device);
+  std::vector<uint8_t> now(size_t(P.n), 0);
+  for (int32_t t = 0; t < count; ++t) {
+    const int32_t i = list[t];
+    now[size_t(i)] = P.h_nodes[size_t(i)].gone ? 0 : 1;
+    P.h_nodes[size_t(i)].gone = 1;
+    SVXG_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(P.d_nodes + i) + offsetof(svxg_node, gone), &P.h_nodes[size_t(i)].gone,
+                              1, cudaMemcpyHostToDevice, P.stream));
+  }
+  std::vector<int32_t> rm;
+  for (int32_t b = 0; b < P.nb; ++b) {
+    svxg_bond& B = P.h_bonds[size_t(b)];
+    if (!(now[size_t(B.a)] || (B.b >= 0 && now[size_t(B.b)]))) continue;
+    B.broken = 1;
+    if (P.assembled && B.in_k) {
+      B.in_k = 0;
+      rm.push_back(b);
+      if (!P.jacobi_only) P.pc_current = false;
+    } else {
+      TRY(upload_bond_flags(P, b));
+    }
+  }
+  if (P.assembled) TRY(remove_bonds_device(P, rm.data(), int32_t(rm.size())));
+  if (P.assembled) {
+    std::vector<int32_t> rows;
+    for (int32_t t = 0; t < count; ++t) {
+      const int32_t i = list[t];
+      const int32_t d = P.h_dof[size_t(i)];
+      if (d < 0) continue;
+      if (now[size_t(i)] && !P.jacobi_only) P.pc_current = false;
+      rows.push_back(d);
+    }
+    TRY(set_identity_rows(P, rows.data(), int32_t(rows.size())));
+  }
+  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  P.active = false;
+  return SVXG_OK;
+}
+
+int svxg_bond_flags(svxg_problem* p, uint8_t* broken, uint8_t* in_k) {
+  CHECK_P(p);
+  for (int32_t k = 0; k < p->P.nb; ++k) {
+    if (broken) broken[k] = p->P.h_bonds[size_t(k)].broken;
+    if (in_k) in_k[k] = p->P.h_bonds[size_t(k)].in_k;
+  }
+  return SVXG_OK;
+}
+
+static int ensure_node_vectors(Problem& P) {
+  if (!P.d_un) TRY(P.mem.alloc(&P.d_un, 12 * size_t(std::max(P.n, 1))));  // u, then f
+  if (!P.mem.holds(P.d_un, 12 * sizeof(double) * size_t(std::max(P.n, 1)))) {
+    set_error("node vectors: buffer does not hold 12 n doubles");
+    return SVXG_ERR_STATE;
+  }
+  return SVXG_OK;
+}
+
+static int ensure_assembled(Problem& P) {
+  if (P.assembled) return SVXG_OK;
+  int32_t ok = 0;
+  const svxg_stress_options o = P.opt;
+  TRY(assemble_impl(P, &o, &ok));
+  if (!ok) return 1;  // (singular: the caller reports a breakdown)
+  return SVXG_OK;
+}
+
+static void failed_result(svxg_pcg_result* res) {
+  if (!res) return;
+  std::memset(res, 0, sizeof(*res));
+  res->rel_res = INFINITY;
+  res->breakdown = 1;
+}
+
+static int solve_common(Problem& P, const double* f_dev, double* u_dev, double rtol, int32_t maxit, int32_t warm,
+                        svxg_pcg_result* res) {
+  TRY(pcg_begin(P, f_dev, warm ? u_dev : nullptr));
+  TRY(pcg_iterate(P, maxit < 0 ? 100000 : maxit, rtol, res));
+  TRY(gather_solution(P, u_dev));
+  P.active = false;
+  return SVXG_OK;
+}
+
+int svxg_solve(svxg_problem* p, const double* f, double* u, double rtol, int32_t maxit, int32_t warm,
+               svxg_pcg_result* res) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  if (!f || !u) return SVXG_ERR_ARG;
+  DeviceScope ds(P.device);
+  const int a = ensure_assembled(P);
+  if (a < 0) return a;
+  if (a > 0) {
+    failed_result(res);
+    return SVXG_OK;
+  }
+  TRY(ensure_node_vectors(P));
+  const size_t m = 6 * size_t(P.n);
+  double* du = P.d_un;
+  double* df = P.d_un + m;
+  SVXG_CUDA(cudaMemcpyAsync(df, f, m * sizeof(double), cudaMemcpyHostToDevice, P.stream));
+  if (warm) SVXG_CUDA(cudaMemcpyAsync(du, u, m * sizeof(double), cudaMemcpyHostToDevice, P.stream));
+  TRY(solve_common(P, df, du, rtol, maxit, warm, res));
+  SVXG_CUDA(cudaMemcpyAsync(u, du, m * sizeof(double), cudaMemcpyDeviceToHost, P.stream));
+  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  return SVXG_OK;
+}
+
+int svxg_solve_device(svxg_problem* p, const double* f_dev, double* u_dev, double rtol, int32_t maxit, int32_t warm,
+                      svxg_pcg_result* res) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  if (!f_dev || !u_dev) return SVXG_ERR_ARG;
+  DeviceScope ds(P.device);
+  const int a = ensure_assembled(P);
+  if (a < 0) return a;
+  if (a > 0) {
+    failed_result(res);
+    return SVXG_OK;
+  }
+  TRY(solve_common(P, f_dev, u_dev, rtol, maxit, warm, res));
+  return SVXG_OK;
+}
+
+int svxg_begin(svxg_problem* p, const double* f, const double* u0) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  DeviceScope ds(P.device);
+  P.active = false;
+  const int a = ensure_assembled(P);
+  if (a) return a < 0 ? a : SVXG_OK;
+  TRY(ensure_node_vectors(P));
+  const size_t m = 6 * size_t(P.n);
+  double* du = P.d_un;
+  double* df = P.d_un + m;
+  SVXG_CUDA(cudaMemcpyAsync(df, f, m * sizeof(double), cudaMemcpyHostToDevice, P.stream));
+  if (u0) SVXG_CUDA(cudaMemcpyAsync(du, u0, m * sizeof(double), cudaMemcpyHostToDevice, P.stream));
+  TRY(pcg_begin(P, df, u0 ? du : nullptr));
+  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  return SVXG_OK;
+}
+
+int svxg_iterate(svxg_problem* p, int32_t maxit, double rtol, svxg_pcg_result* res) {
+  CHECK_P(p);
+  DeviceScope ds(p->P.device);
+  return pcg_iterate(p->P, maxit, rtol, res);
+}
+
+int svxg_running(const svxg_problem* p) { return p && p->P.active ? 1 : 0; }
+
+int svxg_stop(svxg_problem* p) {
+  CHECK_P(p);
+  p->P.active = false;
+  return SVXG_OK;
+}
+
+int svxg_current(svxg_problem* p, double* u) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  DeviceScope ds(P.device);
+  const size_t m = 6 * size_t(P.n);
+  if (!P.d_x || !P.assembled) {
+    std::memset(u, 0, m * sizeof(double));
+    return SVXG_OK;
+  }
+  TRY(ensure_node_vectors(P));
+  TRY(gather_solution(P, P.d_un));
+  SVXG_CUDA(cudaMemcpyAsync(u, P.d_un, m * sizeof(double), cudaMemcpyDeviceToHost, P.stream));
+  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  return SVXG_OK;
+}
+
+int svxg_bond_loads(svxg_problem* p, const double* u, svxg_bond_load* out) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  if (!out) return SVXG_ERR_ARG;
+  DeviceScope ds(P.device);
+  TRY(ensure_node_vectors(P));
+  const size_t m = 6 * size_t(P.n);
+  if (u) {
+    SVXG_CUDA(cudaMemcpyAsync(P.d_un, u, m * sizeof(double), cudaMemcpyHostToDevice, P.stream));
+  } else if (P.d_x && P.assembled) {
+    TRY(gather_solution(P, P.d_un));
+  } else {
+    SVXG_CUDA(cudaMemsetAsync(P.d_un, 0, m * sizeof(double), P.stream));
+  }
+  svxg_bond_load* d = nullptr;
+  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d), sizeof(svxg_bond_load) * size_t(std::max(P.nb, 1)), P.stream));
+  int e = bond_loads_device(P, P.d_un, d);
+  if (!e && P.nb)
+    e = cudaMemcpyAsync(out, d, sizeof(svxg_bond_load) * size_t(P.nb), cudaMemcpyDeviceToHost, P.stream) ==
+                cudaSuccess
+            ? SVXG_OK
+            : SVXG_ERR_CUDA;
+  cudaFreeAsync(d, P.stream);
+  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  return e;
+}
+
+int svxg_utilization(svxg_problem* p, double fragility, double* phi, uint8_t* mode, int32_t* over, int32_t cap,
+                     int32_t* n_over) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  DeviceScope ds(P.device);
+  TRY(ensure_node_vectors(P));
+  const size_t m = 6 * size_t(P.n);
+  if (P.d_x && P.assembled) {
+    TRY(gather_solution(P, P.d_un));
+  } else {
+    SVXG_CUDA(cudaMemsetAsync(P.d_un, 0, m * sizeof(double), P.stream));
+  }
+  const size_t nb = size_t(std::max(P.nb, 1));
+  double* dphi = nullptr;
+  uint8_t* dmode = nullptr;
+  int32_t* dover = nullptr;
+  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dphi), nb * sizeof(double), P.stream));
+  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dmode), nb, P.stream));
+  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dover), nb * sizeof(int32_t), P.stream));
+  int32_t cnt = 0;
+  int e = utilization_device(P, P.d_un, fragility, dphi, dmode, dover, &cnt);
+  if (!e && P.nb) {
+    if (phi) cudaMemcpyAsync(phi, dphi, size_t(P.nb) * sizeof(double), cudaMemcpyDeviceToHost, P.stream);
+    if (mode) cudaMemcpyAsync(mode, dmode, size_t(P.nb), cudaMemcpyDeviceToHost, P.stream);
+    if (over && cnt > 0)
+      cudaMemcpyAsync(over, dover, size_t(std::min(cnt, cap)) * sizeof(int32_t), cudaMemcpyDeviceToHost, P.stream);
+  }
+  cudaFreeAsync(dphi, P.stream);
+  cudaFreeAsync(dmode, P.stream);
+  cudaFreeAsync(dover, P.stream);
+  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  if (n_over) *n_over = cnt;
+  return e;
+}
+
+int svxg_get_info(svxg_problem* p, svxg_info* info) {
+  CHECK_P(p);
+  if (!info) return SVXG_ERR_ARG;
+  const Problem& P = p->P;
+  std::memset(info, 0, sizeof(*info));
+  info->nfree = P.nfree;
+  info->block_jacobi = P.jacobi_only ? 1 : 0;
+  info->levels = int32_t(P.lv.size());
+  info->chol_n = P.chol_n;
+  for (size_t l = 0; l < P.lv.size() && l < 16; ++l) {
+    info->level_sizes[l] = P.lv[l].A.n;
+    info->level_blocks[l] = P.lv[l].A.nnzb;
+    info->level_blocks[P.lv.size() + l] = P.lv[l].pnnz;
+  }
+  info->matrix_blocks = P.K.nnzb;
+  info->work_per_apply = P.amg_work;
+  info->work_per_iteration = 2 * P.K.nnzb + P.amg_work;
+  info->assembly_work = P.assembly_work;
+  info->build_work = P.amg_build_work;
+  info->device_bytes = P.mem.bytes;
+  info->precision = P.opt.precision;
+  return SVXG_OK;
+}
+
+int svxg_debug_matrix(svxg_problem* p, int32_t* nfree, int64_t* nnzb, int32_t* dof, int32_t* rowptr, int32_t* col,
+                      double* val, double* id_scale) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  DeviceScope ds(P.device);
+  if (nfree) *nfree = P.K.n;
+  if (nnzb) *nnzb = P.K.nnzb;
+  if (id_scale) *id_scale = P.id_scale;
+  if (!P.assembled && !P.K.val) return SVXG_OK;
+  if (dof && P.n) SVXG_CUDA(cudaMemcpy(dof, P.d_dof, sizeof(int32_t) * size_t(P.n), cudaMemcpyDeviceToHost));
+  if (rowptr) SVXG_CUDA(cudaMemcpy(rowptr, P.K.rowptr, sizeof(int32_t) * (size_t(P.K.n) + 1), cudaMemcpyDeviceToHost));
+  if (col && P.K.nnzb) SVXG_CUDA(cudaMemcpy(col, P.K.col, sizeof(int32_t) * size_t(P.K.nnzb), cudaMemcpyDeviceToHost));
+  if (val && P.K.nnzb)
+    SVXG_CUDA(cudaMemcpy(val, P.K.val, sizeof(double) * 36 * size_t(P.K.nnzb), cudaMemcpyDeviceToHost));
+  return SVXG_OK;
+}
+
+int svxg_debug_level_dims(svxg_problem* p, int32_t level, int32_t* n, int64_t* nnzb, int64_t* pnnz) {
+  CHECK_P(p);
+  const Problem& P = p->P;
+  if (level < 0 || size_t(level) >= P.lv.size()) return SVXG_ERR_ARG;
+  const Level& L = P.lv[size_t(level)];
+  if (n) *n = L.A.n;
+  if (nnzb) *nnzb = L.A.nnzb;
+  if (pnnz) *pnnz = L.pnnz;
+  return SVXG_OK;
+}
+
+int svxg_debug_level(svxg_problem* p, int32_t level, int32_t* rowptr, int32_t* col, double* val, double* dinv,
+                     int32_t* parent, int32_t* prow, int32_t* pcol, double* pval, double* pos, double* lmax) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  if (level < 0 || size_t(level) >= P.lv.size()) return SVXG_ERR_ARG;
+  DeviceScope ds(P.device);
+  const Level& L = P.lv[size_t(level)];
+  const size_t n = size_t(L.A.n);
+  auto get = [&](void* dst, const void* src, size_t bytes) -> int {
+    if (!dst || !src || bytes == 0) return SVXG_OK;
+    SVXG_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+    return SVXG_OK;
+  };
+  TRY(get(rowptr, L.A.rowptr, sizeof(int32_t) * (n + 1)));
+  TRY(get(col, L.A.col, sizeof(int32_t) * size_t(L.A.nnzb)));
+  TRY(get(val, L.A.val, sizeof(double) * 36 * size_t(L.A.nnzb)));
+  TRY(get(dinv, L.dinv, sizeof(double) * 36 * n));
+  TRY(get(parent, L.parent, sizeof(int32_t) * n));
+  TRY(get(prow, L.prow, sizeof(int32_t) * (n + 1)));
+  TRY(get(pcol, L.pcol, sizeof(int32_t) * size_t(L.pnnz)));
+  TRY(get(pval, L.pval, sizeof(double) * 36 * size_t(L.pnnz)));
+  TRY(get(pos, L.pos, sizeof(double) * 3 * n));
+  if (lmax) *lmax = L.lmax;
+  return SVXG_OK;
+}
+
+int svxg_debug_apply(svxg_problem* p, const double* x, double* y) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  if (!P.assembled) return SVXG_ERR_STATE;
+  DeviceScope ds(P.device);
+  const size_t m = 6 * size_t(P.nfree);
+  double *dx = nullptr, *dy = nullptr;
+  SVXG_CUDA(cudaMalloc(&dx, (m + 1) * sizeof(double)));
+  SVXG_CUDA(cudaMalloc(&dy, (m + 1) * sizeof(double)));
+  cudaMemcpy(dx, x, m * sizeof(double), cudaMemcpyHostToDevice);
+  int e = spmv(P, P.K, dx, dy);
+  cudaStreamSynchronize(P.stream);
+  if (!e) cudaMemcpy(y, dy, m * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(dx);
+  cudaFree(dy);
+  return e;
+}
+
+int svxg_debug_precondition(svxg_problem* p, const double* r, double* z) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  if (!P.assembled) return SVXG_ERR_STATE;
+  DeviceScope ds(P.device);
+  const size_t m = 6 * size_t(P.nfree);
+  double *dr = nullptr, *dz = nullptr;
+  SVXG_CUDA(cudaMalloc(&dr, (m + 1) * sizeof(double)));
+  SVXG_CUDA(cudaMalloc(&dz, (m + 1) * sizeof(double)));
+  cudaMemcpy(dr, r, m * sizeof(double), cudaMemcpyHostToDevice);
+  int e = precondition(P, dr, dz);
+  cudaStreamSynchronize(P.stream);
+  if (!e) cudaMemcpy(z, dz, m * sizeof(double), cudaMemcpyDeviceToHost);
+  cudaFree(dr);
+  cudaFree(dz);
+  return e;
+}
+
+}  // extern "C"

@@ -1,0 +1,1011 @@
+// exact_amg.cu - the aggregation multigrid built on the device, value for value the reference's
+// hierarchy (Amg::build / finalize / estimate_lmax / coarsen / factor_coarsest,
+// core/src/solve/amg.cpp:228-578). Compiled with -fmad=false: every sum runs in the reference's
+// order with separate multiplies and adds, divisions and square roots IEEE-rounded.
+//
+// The reference's aggregation is sequential (amg.cpp:339-349: node i becomes a root when it is
+// not aggregated and none of its strong neighbours is, then claims them). Its roots are the
+// lexicographically first independent set of the conflict graph "N[r] and N[i] meet"
+// (N[x] = x and its strong neighbours by row x): i is a root iff no lower root conflicts with it.
+// The device decides that set in rounds, each deciding every node whose lower conflicting nodes
+// are all decided:
+//   claim:  every undecided node i writes min(i) into claim[x] for x in N[i];
+//   decide: i becomes a non-root if some x in N[i] is covered by an earlier root, a root if it
+//           holds every claim in N[i] (then no undecided lower node conflicts with it);
+//   cover:  each new root covers N[r] (disjoint from other roots' by construction).
+// The smallest undecided node always decides, so the rounds end; the result is the reference's
+// root set exactly, and the aggregate ids follow as the roots' ranks. Passes 2 and 3
+// (amg.cpp:351-384) are per-node and scan steps. Sums whose order matters (coarse positions,
+// prolongation rows, Galerkin products, the power iteration's norm) run in the reference's order.
+#include <algorithm>
+#include <climits>
+#include <cmath>
+
+#include "blk6.cuh"
+#include "problem.cuh"
+
+namespace svxg {
+namespace {
+
+constexpr int kT = 256;
+inline unsigned nblk(int64_t n, int t = kT) { return unsigned(std::max<int64_t>(1, (n + t - 1) / t)); }
+
+#define TRY(x)            \
+  do {                    \
+    int e__ = (x);        \
+    if (e__) return e__;  \
+  } while (0)
+
+template <class T>
+struct Tmp {
+  T* p = nullptr;
+  cudaStream_t s;
+  explicit Tmp(cudaStream_t st) : s(st) {}
+  int alloc(size_t n) {
+    if (p) cudaFreeAsync(p, s);
+    p = nullptr;
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&p), (n ? n : 1) * sizeof(T), s);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      set_error(std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
+      p = nullptr;
+      return e == cudaErrorMemoryAllocation ? SVXG_ERR_NOMEM : SVXG_ERR_CUDA;
+    }
+    return SVXG_OK;
+  }
+  ~Tmp() {
+    if (p) cudaFreeAsync(p, s);
+  }
+};
+
+// ---- finalize (amg.cpp:228-254) --------------------------------------------------------------
+__global__ void k_dinv(int32_t n, const int32_t* rowptr, const double* val, double* dinv, int32_t* fail) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double tmp[36];
+  if (!inv6_regularised(val + 36 * int64_t(rowptr[i]), tmp)) atomicExch(fail, 1);
+  for (int q = 0; q < 36; ++q) dinv[36 * int64_t(i) + q] = tmp[q];
+}
+
+// ---- estimate_lmax (amg.cpp:256-275) ------------------------------------------------------------
+__global__ void k_lmax_init(int64_t m, double* v) {
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < m) v[k] = 1.0 + 0.001 * (double)(k % 7);
+}
+
+// y = A x in Bsr6::apply's order: one thread per (row, component), blocks in row order
+__global__ void k_spmv_exact(int32_t n, const int32_t* rowptr, const int32_t* col, const double* val, const double* x,
+                             double* y) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= 6 * int64_t(n)) return;
+  const int32_t i = int32_t(t / 6);
+  const int r = int(t % 6);
+  double yr = 0.0;
+  for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+    const double* m = val + 36 * int64_t(k) + 6 * r;
+    const double* xv = x + 6 * int64_t(col[k]);
+    yr += m[0] * xv[0] + m[1] * xv[1] + m[2] * xv[2] + m[3] * xv[3] + m[4] * xv[4] + m[5] * xv[5];
+  }
+  y[t] = yr;
+}
+
+__global__ void k_dinv_apply(int32_t n, const double* dinv, const double* w, double* v) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) mv6(dinv + 36 * int64_t(i), w + 6 * int64_t(i), v + 6 * int64_t(i));
+}
+
+// nv = sqrt(sum of v_k^2 in index order); one warp: lanes square, lane 0 adds in order.
+// lam <- nv and v /= nv happen in k_lmax_scale; a zero or non-finite norm stops the iteration.
+__global__ void k_seq_norm(int64_t m, const double* v, double* out) {
+  __shared__ double sq[32];
+  const int lane = threadIdx.x;
+  double s = 0.0;
+  for (int64_t b = 0; b < m; b += 32) {
+    const int64_t k = b + lane;
+    sq[lane] = k < m ? v[k] * v[k] : 0.0;
+    __syncwarp();
+    if (lane == 0) {
+      const int cnt = int(std::min<int64_t>(32, m - b));
+      for (int q = 0; q < cnt; ++q) s += sq[q];
+    }
+    __syncwarp();
+  }
+  if (lane == 0) out[0] = sqrt(s);
+}
+
+// state: [0] = lam, [1] = nv, [2] = stopped
+__global__ void k_lmax_scale(int64_t m, double* v, double* state) {
+  const double nv = state[1];
+  if (state[2] != 0.0) return;
+  if (!(nv > 0)) return;
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < m) v[k] /= nv;
+}
+
+__global__ void k_lmax_step(double* state) {
+  if (state[2] != 0.0) return;
+  const double nv = state[1];
+  if (!(nv > 0)) {
+    state[2] = 1.0;
+    return;
+  }
+  state[0] = nv;
+}
+
+// ---- strength (amg.cpp:324-330) ------------------------------------------------------------------
+__global__ void k_fro_blocks(int64_t nnzb, const double* val, double* fro) {
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < nnzb) fro[k] = fro6(val + 36 * k);
+}
+
+__global__ void k_block_rows(int32_t n, const int32_t* rowptr, int32_t* brow) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) brow[k] = i;
+}
+
+// strong[k] for the round's theta: j != i && fro(A_ij) >= theta sqrt(dn_i dn_j)
+__global__ void k_strong(int64_t nnzb, const int32_t* brow, const int32_t* col, const double* fro, const int32_t* rowptr,
+                         double theta, uint8_t* strong) {
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k >= nnzb) return;
+  const int32_t i = brow[k], j = col[k];
+  const double dni = fro[rowptr[i]], dnj = fro[rowptr[j]];
+  strong[k] = (j != i && fro[k] >= theta * sqrt(dni * dnj)) ? 1 : 0;
+}
+
+// ---- pass 1: the lexicographically first independent set, in rounds ---------------------------
+// state: 0 undecided, 1 root, 2 non-root (isolated rows start as non-roots: amg.cpp:340)
+__global__ void k_mis_init(int32_t n, const int32_t* rowptr, uint8_t* state, uint8_t* covered, int32_t* claim) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  state[i] = (rowptr[i + 1] - rowptr[i] <= 1) ? 2 : 0;
+  covered[i] = 0;
+  claim[i] = INT_MAX;
+}
+
+__global__ void k_mis_claim(int32_t n, const int32_t* rowptr, const int32_t* col, const uint8_t* strong,
+                            const uint8_t* state, int32_t* claim) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || state[i] != 0) return;
+  atomicMin(&claim[i], i);
+  for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+    if (strong[k]) atomicMin(&claim[col[k]], i);
+}
+
+__global__ void k_mis_decide(int32_t n, const int32_t* rowptr, const int32_t* col, const uint8_t* strong,
+                             uint8_t* state, const uint8_t* covered, const int32_t* claim, int32_t* undecided) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || state[i] != 0) return;
+  bool cov = covered[i] != 0;
+  bool mine = claim[i] == i;
+  for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+    if (strong[k]) {
+      const int32_t x = col[k];
+      cov = cov || covered[x] != 0;
+      mine = mine && claim[x] == i;
+    }
+  if (cov) {
+    state[i] = 2;
+  } else if (mine) {
+    state[i] = 3;  // (a root of this round: covers in k_mis_cover)
+  } else {
+    atomicAdd(undecided, 1);
+  }
+}
+
+__global__ void k_mis_cover(int32_t n, const int32_t* rowptr, const int32_t* col, const uint8_t* strong,
+                            uint8_t* state, uint8_t* covered, int32_t* claim) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  claim[i] = INT_MAX;
+  if (state[i] != 3) return;
+  state[i] = 1;
+  covered[i] = 1;
+  for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+    if (strong[k]) covered[col[k]] = 1;
+}
+
+__global__ void k_root_flags(int32_t n, const uint8_t* state, int32_t* flag) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) flag[i] = state[i] == 1 ? 1 : 0;
+}
+
+// agg1: roots' ranks on their N[r] (pass 1's result)
+__global__ void k_agg_pass1(int32_t n, const int32_t* rowptr, const int32_t* col, const uint8_t* strong,
+                            const uint8_t* state, const int32_t* rank, int32_t* agg1) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || state[i] != 1) return;
+  const int32_t a = rank[i];
+  agg1[i] = a;
+  for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+    if (strong[k]) agg1[col[k]] = a;
+}
+
+// pass 2 (amg.cpp:351-366): the most strongly coupled aggregated neighbour (first in row order on ties)
+__global__ void k_agg_pass2(int32_t n, const int32_t* rowptr, const int32_t* col, const double* fro,
+                            const int32_t* agg1, int32_t* agg) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (agg1[i] >= 0) {
+    agg[i] = agg1[i];
+    return;
+  }
+  double best = -1.0;
+  int32_t ba = -1;
+  for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+    const int32_t j = col[k];
+    if (j == i || agg1[j] < 0) continue;
+    const double s = fro[k];
+    if (s > best) {
+      best = s;
+      ba = agg1[j];
+    }
+  }
+  agg[i] = ba;
+}
+
+// pass 3 (amg.cpp:367-384) flags: leftovers, isolated leftovers
+__global__ void k_pass3_flags(int32_t n, const int32_t* rowptr, const int32_t* agg, int32_t* iso, int32_t* noniso) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const bool left = agg[i] < 0;
+  const bool isolated = rowptr[i + 1] - rowptr[i] <= 1;
+  iso[i] = (left && isolated) ? 1 : 0;
+  noniso[i] = (left && !isolated) ? 1 : 0;
+}
+
+// an id is opened by every non-isolated leftover and by every eighth isolated one
+__global__ void k_pass3_alloc(int32_t n, const int32_t* iso, const int32_t* isorank, const int32_t* noniso,
+                              int32_t* alloc, int32_t* group_first) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const bool opens = noniso[i] || (iso[i] && isorank[i] % 8 == 0);
+  alloc[i] = opens ? 1 : 0;
+  if (iso[i] && isorank[i] % 8 == 0) group_first[isorank[i] / 8] = i;
+}
+
+__global__ void k_pass3_assign(int32_t n, int32_t base, const int32_t* iso, const int32_t* isorank,
+                               const int32_t* noniso, const int32_t* allocscan, const int32_t* group_first,
+                               int32_t* agg) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (noniso[i]) agg[i] = base + allocscan[i];
+  else if (iso[i]) agg[i] = base + allocscan[group_first[isorank[i] / 8]];
+}
+
+// ---- coarse positions (amg.cpp:391-401) ------------------------------------------------------------
+__global__ void k_count_members(int32_t n, const int32_t* agg, int32_t* cnt) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) atomicAdd(&cnt[agg[i]], 1);
+}
+
+__global__ void k_fill_members(int32_t n, const int32_t* agg, const int32_t* off, int32_t* cursor, int32_t* members) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t a = agg[i];
+  members[off[a] + atomicAdd(&cursor[a], 1)] = i;
+}
+
+// per aggregate: members sorted, positions summed in node order, then times 1 / count
+__global__ void k_coarse_pos(int32_t na, const int32_t* off, int32_t* members, const double* fpos, double* cpos) {
+  const int32_t a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= na) return;
+  const int32_t e0 = off[a], e1 = off[a + 1];
+  for (int32_t u = e0 + 1; u < e1; ++u) {
+    const int32_t v = members[u];
+    int32_t c = u - 1;
+    while (c >= e0 && members[c] > v) {
+      members[c + 1] = members[c];
+      --c;
+    }
+    members[c + 1] = v;
+  }
+  double x = 0.0, y = 0.0, z = 0.0;
+  for (int32_t u = e0; u < e1; ++u) {
+    const int32_t i = members[u];
+    x += fpos[3 * int64_t(i)];
+    y += fpos[3 * int64_t(i) + 1];
+    z += fpos[3 * int64_t(i) + 2];
+  }
+  const double s = 1.0 / (e1 - e0);
+  cpos[3 * int64_t(a)] = x * s;
+  cpos[3 * int64_t(a) + 1] = y * s;
+  cpos[3 * int64_t(a) + 2] = z * s;
+}
+
+__global__ void k_offsets(int32_t n, const int32_t* agg, const double* fpos, const double* cpos, double* off3) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t a = agg[i];
+  for (int c = 0; c < 3; ++c) off3[3 * int64_t(i) + c] = fpos[3 * int64_t(i) + c] - cpos[3 * int64_t(a) + c];
+}
+
+__device__ __forceinline__ V3d v3at(const double* p, int64_t i) { return {p[3 * i], p[3 * i + 1], p[3 * i + 2]}; }
+
+// ---- prolongation (amg.cpp:405-452) ----------------------------------------------------------------
+// distinct coarse columns of fine row i: agg[i] and agg[col k] (all k when smoothed)
+__device__ int32_t sorted_distinct(int32_t first, const int32_t* rowptr, const int32_t* col, const int32_t* agg,
+                                   int32_t i, bool all, int32_t* out, int32_t cap) {
+  int32_t m = 0;
+  auto insert = [&](int32_t c) {
+    int32_t p = 0;
+    while (p < m && out[p] < c) ++p;
+    if (p < m && out[p] == c) return;
+    if (m >= cap) return;
+    for (int32_t q = m; q > p; --q) out[q] = out[q - 1];
+    out[p] = c;
+    ++m;
+  };
+  insert(first);
+  if (all)
+    for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) insert(agg[col[k]]);
+  return m;
+}
+
+__global__ void k_p_count(int32_t n, const int32_t* rowptr, const int32_t* col, const int32_t* agg, int smoothed,
+                          int32_t* plen, int32_t* scratch, int32_t cap) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  plen[i] = sorted_distinct(agg[i], rowptr, col, agg, i, smoothed != 0, scratch + int64_t(rowptr[i]) + i, cap);
+}
+
+__global__ void k_p_values(int32_t n, const int32_t* rowptr, const int32_t* col, const double* val, const int32_t* agg,
+                           const double* off3, const double* dinv, double omega, const int32_t* prow,
+                           const int32_t* scratch, int32_t* pcol, double* pval) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t e0 = prow[i], e1 = prow[i + 1];
+  const int32_t* cols = scratch + int64_t(rowptr[i]) + i;
+  for (int32_t e = e0; e < e1; ++e) {
+    pcol[e] = cols[e - e0];
+    for (int q = 0; q < 36; ++q) pval[36 * int64_t(e) + q] = 0.0;
+  }
+  auto slot = [&](int32_t c) -> double* {
+    int32_t lo = e0, hi = e1 - 1;
+    while (lo < hi) {
+      const int32_t mid = (lo + hi) >> 1;
+      if (pcol[mid] < c) lo = mid + 1;
+      else hi = mid;
+    }
+    return pval + 36 * int64_t(lo);
+  };
+  double Pt[36];
+  rigid_block(v3at(off3, i), Pt);
+  {
+    double* b = slot(agg[i]);
+    for (int q = 0; q < 36; ++q) b[q] += 1.0 * Pt[q];
+  }
+  if (omega != 0.0) {
+    const double* Di = dinv + 36 * int64_t(i);
+    for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+      const int32_t j = col[k];
+      double Pj[36], T[36], U[36];
+      rigid_block(v3at(off3, j), Pj);
+      mul6(val + 36 * int64_t(k), Pj, T);
+      mul6(Di, T, U);
+      double* b = slot(agg[j]);
+      for (int q = 0; q < 36; ++q) b[q] += -omega * U[q];
+    }
+  }
+}
+
+// build work of the products: 6 |P row col(k)| for every block k of A
+__global__ void k_work_ap(int64_t nnzb, const int32_t* col, const int32_t* prow, unsigned long long* acc) {
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  unsigned long long w = 0;
+  if (k < nnzb) {
+    const int32_t j = col[k];
+    w = 6ull * unsigned(prow[j + 1] - prow[j]);
+  }
+  for (int d = 16; d > 0; d >>= 1) w += __shfl_xor_sync(0xffffffffu, w, d);
+  if ((threadIdx.x & 31) == 0 && w) atomicAdd(acc, w);
+}
+
+// ---- restriction lists (amg.cpp:461-470) ---------------------------------------------------------
+__global__ void k_r_count(int64_t pnnz, const int32_t* pcol, int32_t* cnt) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e < pnnz) atomicAdd(&cnt[pcol[e]], 1);
+}
+
+__global__ void k_r_fill(int32_t n, const int32_t* prow, const int32_t* pcol, const int32_t* rrow, int32_t* cursor,
+                         int32_t* rent_e) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int32_t e = prow[i]; e < prow[i + 1]; ++e) {
+    const int32_t c = pcol[e];
+    rent_e[rrow[c] + atomicAdd(&cursor[c], 1)] = e;
+  }
+}
+
+// per coarse row: entries by P index (= by fine row, then P index), and their fine rows
+__global__ void k_r_sort(int32_t na, const int32_t* rrow, int32_t* rent_e, int32_t* rent_i, const int32_t* erow) {
+  const int32_t a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= na) return;
+  const int32_t e0 = rrow[a], e1 = rrow[a + 1];
+  for (int32_t u = e0 + 1; u < e1; ++u) {
+    const int32_t v = rent_e[u];
+    int32_t c = u - 1;
+    while (c >= e0 && rent_e[c] > v) {
+      rent_e[c + 1] = rent_e[c];
+      --c;
+    }
+    rent_e[c + 1] = v;
+  }
+  for (int32_t u = e0; u < e1; ++u) rent_i[u] = erow[rent_e[u]];
+}
+
+__global__ void k_entry_rows(int32_t n, const int32_t* prow, int32_t* erow) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int32_t e = prow[i]; e < prow[i + 1]; ++e) erow[e] = i;
+}
+
+// ---- Galerkin product (amg.cpp:472-529) ------------------------------------------------------------
+// A P by fine row: distinct coarse columns over (k, e), sorted
+__global__ void k_ap_count(int32_t n, const int32_t* rowptr, const int32_t* col, const int32_t* prow,
+                           const int32_t* pcol, int32_t* aplen, int32_t* scratch, const int64_t* soff, int32_t cap) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int32_t* out = scratch + soff[i];
+  int32_t m = 0;
+  for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+    const int32_t j = col[k];
+    for (int32_t e = prow[j]; e < prow[j + 1]; ++e) {
+      const int32_t c = pcol[e];
+      int32_t p = 0;
+      while (p < m && out[p] < c) ++p;
+      if (p < m && out[p] == c) continue;
+      if (m >= cap) continue;
+      for (int32_t q = m; q > p; --q) out[q] = out[q - 1];
+      out[p] = c;
+      ++m;
+    }
+  }
+  aplen[i] = m;
+}
+
+__global__ void k_ap_values(int32_t n, const int32_t* rowptr, const int32_t* col, const double* val,
+                            const int32_t* prow, const int32_t* pcol, const double* pval, const int32_t* aprow,
+                            const int32_t* scratch, const int64_t* soff, int32_t* apcol, double* apval) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t e0 = aprow[i], e1 = aprow[i + 1];
+  for (int32_t e = e0; e < e1; ++e) {
+    apcol[e] = scratch[soff[i] + (e - e0)];
+    for (int q = 0; q < 36; ++q) apval[36 * int64_t(e) + q] = 0.0;
+  }
+  for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+    const int32_t j = col[k];
+    const double* Aij = val + 36 * int64_t(k);
+    for (int32_t e = prow[j]; e < prow[j + 1]; ++e) {
+      const int32_t c = pcol[e];
+      int32_t lo = e0, hi = e1 - 1;
+      while (lo < hi) {
+        const int32_t mid = (lo + hi) >> 1;
+        if (apcol[mid] < c) lo = mid + 1;
+        else hi = mid;
+      }
+      mul6_add<false>(Aij, pval + 36 * int64_t(e), apval + 36 * int64_t(lo));
+    }
+  }
+}
+
+// build work of P^T (A P): 6 |P row i| |AP row i|
+__global__ void k_work_rap(int32_t n, const int32_t* prow, const int32_t* aprow, unsigned long long* acc) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long w = 0;
+  if (i < n) w = 6ull * unsigned(prow[i + 1] - prow[i]) * unsigned(aprow[i + 1] - aprow[i]);
+  for (int d = 16; d > 0; d >>= 1) w += __shfl_xor_sync(0xffffffffu, w, d);
+  if ((threadIdx.x & 31) == 0 && w) atomicAdd(acc, w);
+}
+
+// coarse row I: distinct columns over its restriction entries' A P rows; diagonal first, then
+// ascending (Bsr6Builder::finish)
+__global__ void k_c_count(int32_t na, const int32_t* rrow, const int32_t* rent_i, const int32_t* aprow,
+                          const int32_t* apcol, int32_t* clen, int32_t* scratch, const int64_t* soff, int32_t cap) {
+  const int32_t I = blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= na) return;
+  int32_t* out = scratch + soff[I];
+  int32_t m = 0;
+  for (int32_t r = rrow[I]; r < rrow[I + 1]; ++r) {
+    const int32_t i = rent_i[r];
+    for (int32_t e = aprow[i]; e < aprow[i + 1]; ++e) {
+      const int32_t c = apcol[e];
+      int32_t p = 0;
+      while (p < m && out[p] < c) ++p;
+      if (p < m && out[p] == c) continue;
+      if (m >= cap) continue;
+      for (int32_t q = m; q > p; --q) out[q] = out[q - 1];
+      out[p] = c;
+      ++m;
+    }
+  }
+  // (the diagonal to the front)
+  int32_t p = 0;
+  while (p < m && out[p] != I) ++p;
+  if (p < m) {
+    for (int32_t q = p; q > 0; --q) out[q] = out[q - 1];
+    out[0] = I;
+    clen[I] = m;
+  } else {
+    for (int32_t q = m; q > 0; --q) out[q] = out[q - 1];
+    out[0] = I;
+    clen[I] = m + 1;
+  }
+}
+
+__global__ void k_c_values(int32_t na, const int32_t* rrow, const int32_t* rent_i, const int32_t* rent_e,
+                           const double* pval, const int32_t* aprow, const int32_t* apcol, const double* apval,
+                           const int32_t* crow, const int32_t* scratch, const int64_t* soff, int32_t* ccol,
+                           double* cval, double scale) {
+  const int32_t I = blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= na) return;
+  const int32_t c0 = crow[I], c1 = crow[I + 1];
+  for (int32_t c = c0; c < c1; ++c) {
+    ccol[c] = scratch[soff[I] + (c - c0)];
+    for (int q = 0; q < 36; ++q) cval[36 * int64_t(c) + q] = 0.0;
+  }
+  for (int32_t r = rrow[I]; r < rrow[I + 1]; ++r) {
+    const int32_t i = rent_i[r];
+    const double* Pi = pval + 36 * int64_t(rent_e[r]);
+    for (int32_t e = aprow[i]; e < aprow[i + 1]; ++e) {
+      const int32_t J = apcol[e];
+      int32_t slot;
+      if (J == I) {
+        slot = c0;
+      } else {
+        int32_t lo = c0 + 1, hi = c1 - 1;
+        while (lo < hi) {
+          const int32_t mid = (lo + hi) >> 1;
+          if (ccol[mid] < J) lo = mid + 1;
+          else hi = mid;
+        }
+        slot = lo;
+      }
+      mul6_add<true>(Pi, apval + 36 * int64_t(e), cval + 36 * int64_t(slot));
+    }
+  }
+  if (scale != 1.0)
+    for (int32_t c = c0; c < c1; ++c)
+      for (int q = 0; q < 36; ++q) cval[36 * int64_t(c) + q] *= scale;
+}
+
+// per-row scratch offsets: sum over a row's products of the candidate counts (an upper bound)
+__global__ void k_ap_bound(int32_t n, const int32_t* rowptr, const int32_t* col, const int32_t* prow, int32_t* bound) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int32_t b = 0;
+  for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) b += prow[col[k] + 1] - prow[col[k]];
+  bound[i] = b;
+}
+
+__global__ void k_c_bound(int32_t na, const int32_t* rrow, const int32_t* rent_i, const int32_t* aprow,
+                          int32_t* bound) {
+  const int32_t I = blockIdx.x * blockDim.x + threadIdx.x;
+  if (I >= na) return;
+  int32_t b = 1;
+  for (int32_t r = rrow[I]; r < rrow[I + 1]; ++r) b += aprow[rent_i[r] + 1] - aprow[rent_i[r]];
+  bound[I] = b;
+}
+
+__global__ void k_i64_offsets(int32_t n, const int32_t* bound, int64_t* off) {
+  // (sequential: small arrays of per-row bounds; one thread)
+  if (blockIdx.x || threadIdx.x) return;
+  int64_t s = 0;
+  for (int32_t i = 0; i < n; ++i) {
+    off[i] = s;
+    s += bound[i];
+  }
+  off[n] = s;
+}
+
+// ---- the coarsest level's dense factor (amg.cpp:535-578) ---------------------------------------
+__global__ void k_dense_fill(int32_t nc, const int32_t* rowptr, const int32_t* col, const double* val, int32_t m,
+                             double* C) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+    const int32_t j = col[k];
+    for (int r = 0; r < 6; ++r)
+      for (int c = 0; c < 6; ++c) C[int64_t(6 * i + r) * m + (6 * j + c)] += val[36 * int64_t(k) + r * 6 + c];
+  }
+}
+
+__global__ void k_dense_dmax(int32_t m, const double* C, double* dmax) {
+  if (blockIdx.x || threadIdx.x) return;
+  double d = 0.0;
+  for (int32_t i = 0; i < m; ++i) d = maxd(d, fabs(C[int64_t(i) * m + i]));
+  *dmax = d;
+}
+
+__global__ void k_chol_diag(int32_t m, int32_t j, double* C, const double* dmax) {
+  if (blockIdx.x || threadIdx.x) return;
+  double d = C[int64_t(j) * m + j];
+  for (int32_t k = 0; k < j; ++k) d -= C[int64_t(j) * m + k] * C[int64_t(j) * m + k];
+  if (!(d > 1e-12 * *dmax)) d = maxd(1e-12 * *dmax, 1e-300);
+  C[int64_t(j) * m + j] = sqrt(d);
+}
+
+__global__ void k_chol_col(int32_t m, int32_t j, double* C) {
+  const int32_t i = j + 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const double s = C[int64_t(j) * m + j];
+  double v = 0.5 * (C[int64_t(i) * m + j] + C[int64_t(j) * m + i]);
+  for (int32_t k = 0; k < j; ++k) v -= C[int64_t(i) * m + k] * C[int64_t(j) * m + k];
+  C[int64_t(i) * m + j] = v / s;
+}
+
+__global__ void k_chol_mirror(int32_t m, double* C) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= int64_t(m) * m) return;
+  const int32_t i = int32_t(t / m), k = int32_t(t % m);
+  if (k > i) C[t] = C[int64_t(k) * m + i];
+}
+
+// ---- host-side steps ---------------------------------------------------------------------------
+
+int copy_to_host(Problem& P, void* dst, const void* src, size_t bytes) {
+  if (bytes == 0) return SVXG_OK;
+  SVXG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, P.stream));
+  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  return SVXG_OK;
+}
+
+int finalize_level(Problem& P, Level& L, bool* ok) {
+  *ok = false;
+  TRY(P.mem.alloc(&L.dinv, size_t(L.A.n) * 36));
+  Tmp<int32_t> fail(P.stream);
+  TRY(fail.alloc(1));
+  SVXG_CUDA(cudaMemsetAsync(fail.p, 0, sizeof(int32_t), P.stream));
+  if (L.A.n > 0) k_dinv<<<nblk(L.A.n), kT, 0, P.stream>>>(L.A.n, L.A.rowptr, L.A.val, L.dinv, fail.p);
+  int32_t f = 0;
+  TRY(copy_to_host(P, &f, fail.p, sizeof(int32_t)));
+  P.amg_build_work += 12 * int64_t(L.A.n);
+  *ok = f == 0;
+  return SVXG_OK;
+}
+
+// estimate_lmax of a level (amg.cpp:256-275), the value the reference computes
+int estimate_lmax(Problem& P, const Level& L, double* out) {
+  const int32_t n = L.A.n;
+  P.amg_build_work += 15 * (L.A.nnzb + n);
+  const int64_t m = 6 * int64_t(n);
+  Tmp<double> v(P.stream), w(P.stream), st(P.stream);
+  TRY(v.alloc(size_t(m)));
+  TRY(w.alloc(size_t(m)));
+  TRY(st.alloc(3));
+  const double init[3] = {1.0, 0.0, 0.0};
+  SVXG_CUDA(cudaMemcpyAsync(st.p, init, sizeof(init), cudaMemcpyHostToDevice, P.stream));
+  k_lmax_init<<<nblk(m), kT, 0, P.stream>>>(m, v.p);
+  for (int it = 0; it < 15; ++it) {
+    k_spmv_exact<<<nblk(m), kT, 0, P.stream>>>(n, L.A.rowptr, L.A.col, L.A.val, v.p, w.p);
+    k_dinv_apply<<<nblk(n), kT, 0, P.stream>>>(n, L.dinv, w.p, v.p);
+    k_seq_norm<<<1, 32, 0, P.stream>>>(m, v.p, st.p + 1);
+    k_lmax_step<<<1, 1, 0, P.stream>>>(st.p);
+    k_lmax_scale<<<nblk(m), kT, 0, P.stream>>>(m, v.p, st.p);
+  }
+  SVXG_CUDA(cudaGetLastError());
+  double h[3];
+  TRY(copy_to_host(P, h, st.p, sizeof(h)));
+  *out = 1.1 * h[0];
+  return SVXG_OK;
+}
+
+// Amg::coarsen (amg.cpp:320-533): appends level l + 1; *made = false when coarsening stops
+int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
+  *made = false;
+  cudaStream_t st = P.stream;
+  const svxg_amg_options& opt = P.opt.amg;
+  const int32_t n = P.lv[l].A.n;
+  const int64_t nnzb = P.lv[l].A.nnzb;
+  {
+    const Bsr& A = P.lv[l].A;
+    (void)A;
+  }
+  Tmp<double> fro(st);
+  Tmp<int32_t> brow(st), agg1(st), flag(st), rank(st), claim(st), undecided(st);
+  Tmp<uint8_t> strong(st), state(st), covered(st);
+  TRY(fro.alloc(size_t(nnzb)));
+  TRY(brow.alloc(size_t(nnzb)));
+  TRY(strong.alloc(size_t(nnzb)));
+  TRY(state.alloc(size_t(n)));
+  TRY(covered.alloc(size_t(n)));
+  TRY(claim.alloc(size_t(n)));
+  TRY(agg1.alloc(size_t(n)));
+  TRY(flag.alloc(size_t(n) + 1));
+  TRY(rank.alloc(size_t(n) + 1));
+  TRY(undecided.alloc(1));
+  Tmp<int32_t> iso(st), noniso(st), isorank(st), alloc(st), allocscan(st), gfirst(st);
+  TRY(iso.alloc(size_t(n) + 1));
+  TRY(noniso.alloc(size_t(n) + 1));
+  TRY(isorank.alloc(size_t(n) + 1));
+  TRY(alloc.alloc(size_t(n) + 1));
+  TRY(allocscan.alloc(size_t(n) + 1));
+  TRY(gfirst.alloc(size_t(n) / 8 + 2));
+  int32_t* agg = nullptr;
+  TRY(P.mem.alloc(&agg, size_t(n)));
+  {
+    const Bsr& A = P.lv[l].A;
+    k_fro_blocks<<<nblk(nnzb), kT, 0, st>>>(nnzb, A.val, fro.p);
+    k_block_rows<<<nblk(n), kT, 0, st>>>(n, A.rowptr, brow.p);
+  }
+  double theta = opt.strength;
+  int32_t na = 0;
+  for (int round = 0;; ++round) {
+    const Bsr& A = P.lv[l].A;
+    k_strong<<<nblk(nnzb), kT, 0, st>>>(nnzb, brow.p, A.col, fro.p, A.rowptr, theta, strong.p);
+    k_mis_init<<<nblk(n), kT, 0, st>>>(n, A.rowptr, state.p, covered.p, claim.p);
+    for (int guard = 0; guard <= n; ++guard) {
+      SVXG_CUDA(cudaMemsetAsync(undecided.p, 0, sizeof(int32_t), st));
+      k_mis_claim<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, claim.p);
+      k_mis_decide<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, covered.p, claim.p, undecided.p);
+      k_mis_cover<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, covered.p, claim.p);
+      int32_t u = 0;
+      TRY(copy_to_host(P, &u, undecided.p, sizeof(int32_t)));
+      if (u == 0) break;
+    }
+    k_root_flags<<<nblk(n), kT, 0, st>>>(n, state.p, flag.p);
+    int32_t na1 = 0;
+    TRY(exclusive_scan_i32(P, flag.p, rank.p, n, &na1));
+    SVXG_CUDA(cudaMemsetAsync(agg1.p, 0xff, sizeof(int32_t) * size_t(n), st));
+    k_agg_pass1<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, rank.p, agg1.p);
+    k_agg_pass2<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, fro.p, agg1.p, agg);
+    k_pass3_flags<<<nblk(n), kT, 0, st>>>(n, A.rowptr, agg, iso.p, noniso.p);
+    TRY(exclusive_scan_i32(P, iso.p, isorank.p, n, nullptr));
+    k_pass3_alloc<<<nblk(n), kT, 0, st>>>(n, iso.p, isorank.p, noniso.p, alloc.p, gfirst.p);
+    int32_t nalloc = 0;
+    TRY(exclusive_scan_i32(P, alloc.p, allocscan.p, n, &nalloc));
+    k_pass3_assign<<<nblk(n), kT, 0, st>>>(n, na1, iso.p, isorank.p, noniso.p, allocscan.p, gfirst.p, agg);
+    SVXG_CUDA(cudaGetLastError());
+    na = na1 + nalloc;
+    if (!opt.reaggregate || round == 3 || 2 * int64_t(na) <= n) break;
+    theta *= 0.5;
+  }
+  if (na >= n || double(na) > 0.85 * n) {
+    P.mem.release(agg);
+    return SVXG_OK;
+  }
+  P.lv.emplace_back();
+  Level& F = P.lv[l];
+  Level& C = P.lv[l + 1];
+  F.parent = agg;
+  C.A.n = na;
+  // coarse positions and offsets
+  {
+    Tmp<int32_t> cnt(st), off(st), cursor(st), members(st);
+    TRY(cnt.alloc(size_t(na) + 1));
+    TRY(off.alloc(size_t(na) + 1));
+    TRY(cursor.alloc(size_t(na) + 1));
+    TRY(members.alloc(size_t(n)));
+    SVXG_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * (size_t(na) + 1), st));
+    SVXG_CUDA(cudaMemsetAsync(cursor.p, 0, sizeof(int32_t) * (size_t(na) + 1), st));
+    k_count_members<<<nblk(n), kT, 0, st>>>(n, agg, cnt.p);
+    TRY(exclusive_scan_i32(P, cnt.p, off.p, int64_t(na) + 1, nullptr));
+    k_fill_members<<<nblk(n), kT, 0, st>>>(n, agg, off.p, cursor.p, members.p);
+    TRY(P.mem.alloc(&C.pos, 3 * size_t(na)));
+    k_coarse_pos<<<nblk(na), kT, 0, st>>>(na, off.p, members.p, F.pos, C.pos);
+  }
+  Tmp<double> off3(st);
+  TRY(off3.alloc(3 * size_t(n)));
+  k_offsets<<<nblk(n), kT, 0, st>>>(n, agg, F.pos, C.pos, off3.p);
+  // prolongation
+  double omega = 0.0;
+  if (smoothed) {
+    double lm = 0.0;
+    TRY(estimate_lmax(P, F, &lm));
+    F.lmax = lm;
+    omega = (4.0 / 3.0) / maxd(1e-300, lm);
+  }
+  {
+    const Bsr& A = F.A;
+    Tmp<int32_t> plen(st), scratch(st);
+    TRY(plen.alloc(size_t(n) + 1));
+    TRY(scratch.alloc(size_t(nnzb) + size_t(n) + 1));
+    SVXG_CUDA(cudaMemsetAsync(plen.p, 0, sizeof(int32_t) * (size_t(n) + 1), st));
+    k_p_count<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, agg, smoothed ? 1 : 0, plen.p, scratch.p, INT_MAX);
+    TRY(P.mem.alloc(&F.prow, size_t(n) + 1));
+    int32_t pnnz = 0;
+    TRY(exclusive_scan_i32(P, plen.p, F.prow, int64_t(n) + 1, &pnnz));
+    F.pnnz = pnnz;
+    TRY(P.mem.alloc(&F.pcol, size_t(pnnz)));
+    TRY(P.mem.alloc(&F.pval, size_t(pnnz) * 36));
+    k_p_values<<<nblk(n, 128), 128, 0, st>>>(n, A.rowptr, A.col, A.val, agg, off3.p, F.dinv, omega, F.prow,
+                                              scratch.p, F.pcol, F.pval);
+  }
+  if (smoothed) P.amg_build_work += 12 * nnzb;
+  {
+    Tmp<unsigned long long> acc(st);
+    TRY(acc.alloc(1));
+    SVXG_CUDA(cudaMemsetAsync(acc.p, 0, sizeof(unsigned long long), st));
+    k_work_ap<<<nblk(nnzb), kT, 0, st>>>(nnzb, F.A.col, F.prow, acc.p);
+    unsigned long long w = 0;
+    TRY(copy_to_host(P, &w, acc.p, sizeof(w)));
+    P.amg_build_work += int64_t(w);
+  }
+  // restriction lists
+  {
+    Tmp<int32_t> cnt(st), cursor(st), erow(st);
+    TRY(cnt.alloc(size_t(na) + 1));
+    TRY(cursor.alloc(size_t(na) + 1));
+    TRY(erow.alloc(size_t(F.pnnz)));
+    SVXG_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * (size_t(na) + 1), st));
+    SVXG_CUDA(cudaMemsetAsync(cursor.p, 0, sizeof(int32_t) * (size_t(na) + 1), st));
+    k_r_count<<<nblk(F.pnnz), kT, 0, st>>>(F.pnnz, F.pcol, cnt.p);
+    TRY(P.mem.alloc(&F.rrow, size_t(na) + 1));
+    TRY(exclusive_scan_i32(P, cnt.p, F.rrow, int64_t(na) + 1, nullptr));
+    TRY(P.mem.alloc(&F.rent_e, size_t(F.pnnz)));
+    TRY(P.mem.alloc(&F.rent_i, size_t(F.pnnz)));
+    k_r_fill<<<nblk(n), kT, 0, st>>>(n, F.prow, F.pcol, F.rrow, cursor.p, F.rent_e);
+    k_entry_rows<<<nblk(n), kT, 0, st>>>(n, F.prow, erow.p);
+    k_r_sort<<<nblk(na), kT, 0, st>>>(na, F.rrow, F.rent_e, F.rent_i, erow.p);
+  }
+  // Galerkin: A P
+  Tmp<int32_t> aprow(st), apcol(st);
+  Tmp<double> apval(st);
+  {
+    Tmp<int32_t> bound(st), scratch(st);
+    Tmp<int64_t> soff(st);
+    TRY(bound.alloc(size_t(n) + 1));
+    TRY(soff.alloc(size_t(n) + 1));
+    k_ap_bound<<<nblk(n), kT, 0, st>>>(n, F.A.rowptr, F.A.col, F.prow, bound.p);
+    k_i64_offsets<<<1, 1, 0, st>>>(n, bound.p, soff.p);
+    int64_t stotal = 0;
+    TRY(copy_to_host(P, &stotal, soff.p + n, sizeof(int64_t)));
+    TRY(scratch.alloc(size_t(stotal) + 1));
+    TRY(aprow.alloc(size_t(n) + 1));
+    Tmp<int32_t> aplen(st);
+    TRY(aplen.alloc(size_t(n) + 1));
+    SVXG_CUDA(cudaMemsetAsync(aplen.p, 0, sizeof(int32_t) * (size_t(n) + 1), st));
+    k_ap_count<<<nblk(n), kT, 0, st>>>(n, F.A.rowptr, F.A.col, F.prow, F.pcol, aplen.p, scratch.p, soff.p, INT_MAX);
+    int32_t apnnz = 0;
+    TRY(exclusive_scan_i32(P, aplen.p, aprow.p, int64_t(n) + 1, &apnnz));
+    TRY(apcol.alloc(size_t(apnnz)));
+    TRY(apval.alloc(size_t(apnnz) * 36));
+    k_ap_values<<<nblk(n, 128), 128, 0, st>>>(n, F.A.rowptr, F.A.col, F.A.val, F.prow, F.pcol, F.pval, aprow.p,
+                                              scratch.p, soff.p, apcol.p, apval.p);
+  }
+  {
+    Tmp<unsigned long long> acc(st);
+    TRY(acc.alloc(1));
+    SVXG_CUDA(cudaMemsetAsync(acc.p, 0, sizeof(unsigned long long), st));
+    k_work_rap<<<nblk(n), kT, 0, st>>>(n, F.prow, aprow.p, acc.p);
+    unsigned long long w = 0;
+    TRY(copy_to_host(P, &w, acc.p, sizeof(w)));
+    P.amg_build_work += int64_t(w);
+  }
+  // Galerkin: P^T (A P) by coarse row
+  {
+    Tmp<int32_t> bound(st), scratch(st), clen(st);
+    Tmp<int64_t> soff(st);
+    TRY(bound.alloc(size_t(na) + 1));
+    TRY(soff.alloc(size_t(na) + 1));
+    k_c_bound<<<nblk(na), kT, 0, st>>>(na, F.rrow, F.rent_i, aprow.p, bound.p);
+    k_i64_offsets<<<1, 1, 0, st>>>(na, bound.p, soff.p);
+    int64_t stotal = 0;
+    TRY(copy_to_host(P, &stotal, soff.p + na, sizeof(int64_t)));
+    TRY(scratch.alloc(size_t(stotal) + 1));
+    TRY(clen.alloc(size_t(na) + 1));
+    SVXG_CUDA(cudaMemsetAsync(clen.p, 0, sizeof(int32_t) * (size_t(na) + 1), st));
+    k_c_count<<<nblk(na), kT, 0, st>>>(na, F.rrow, F.rent_i, aprow.p, apcol.p, clen.p, scratch.p, soff.p, INT_MAX);
+    TRY(P.mem.alloc(&C.A.rowptr, size_t(na) + 1));
+    int32_t cnnz = 0;
+    TRY(exclusive_scan_i32(P, clen.p, C.A.rowptr, int64_t(na) + 1, &cnnz));
+    C.A.nnzb = cnnz;
+    TRY(P.mem.alloc(&C.A.col, size_t(cnnz)));
+    TRY(P.mem.alloc(&C.A.val, size_t(cnnz) * 36));
+    const double scale = (!smoothed && opt.coarse_scale != 1.0) ? opt.coarse_scale : 1.0;
+    k_c_values<<<nblk(na, 128), 128, 0, st>>>(na, F.rrow, F.rent_i, F.rent_e, F.pval, aprow.p, apcol.p, apval.p,
+                                              C.A.rowptr, scratch.p, soff.p, C.A.col, C.A.val, scale);
+  }
+  SVXG_CUDA(cudaGetLastError());
+  bool fin = false;
+  TRY(finalize_level(P, P.lv[l + 1], &fin));
+  if (!fin) {
+    // (coarse level singular: the reference's coarsen returns false after F's P is made)
+    Level& Cx = P.lv.back();
+    P.mem.release(Cx.A.rowptr);
+    P.mem.release(Cx.A.col);
+    P.mem.release(Cx.A.val);
+    P.mem.release(Cx.dinv);
+    P.mem.release(Cx.pos);
+    P.lv.pop_back();
+    return SVXG_OK;
+  }
+  *made = true;
+  return SVXG_OK;
+}
+
+int factor_coarsest(Problem& P) {
+  const Level& L = P.lv.back();
+  if (L.A.n > 4 * P.opt.amg.coarse_max) {
+    P.chol_n = 0;
+    return SVXG_OK;
+  }
+  const int32_t m = 6 * L.A.n;
+  P.chol_n = m;
+  P.amg_build_work += int64_t(m) * m * m / 108;
+  TRY(P.mem.alloc(&P.d_chol, size_t(m) * size_t(m)));
+  cudaStream_t st = P.stream;
+  SVXG_CUDA(cudaMemsetAsync(P.d_chol, 0, sizeof(double) * size_t(m) * size_t(m), st));
+  k_dense_fill<<<nblk(L.A.n), kT, 0, st>>>(L.A.n, L.A.rowptr, L.A.col, L.A.val, m, P.d_chol);
+  Tmp<double> dmax(st);
+  TRY(dmax.alloc(1));
+  k_dense_dmax<<<1, 1, 0, st>>>(m, P.d_chol, dmax.p);
+  for (int32_t j = 0; j < m; ++j) {
+    k_chol_diag<<<1, 1, 0, st>>>(m, j, P.d_chol, dmax.p);
+    if (m - j - 1 > 0) k_chol_col<<<nblk(m - j - 1, 128), 128, 0, st>>>(m, j, P.d_chol);
+  }
+  k_chol_mirror<<<nblk(int64_t(m) * m), kT, 0, st>>>(m, P.d_chol);
+  SVXG_CUDA(cudaGetLastError());
+  return SVXG_OK;
+}
+
+__global__ void k_level0_pos(int32_t n, const svxg_node* nodes, const int32_t* dof, double* pos) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t d = dof[i];
+  if (d < 0) return;
+  pos[3 * int64_t(d)] = nodes[i].c.x;
+  pos[3 * int64_t(d) + 1] = nodes[i].c.y;
+  pos[3 * int64_t(d) + 2] = nodes[i].c.z;
+}
+
+}  // namespace
+
+// Amg::build (amg.cpp:277-318) over K
+int build_hierarchy(Problem& P, int32_t* ok) {
+  *ok = 0;
+  P.lv.clear();
+  P.chol_n = 0;
+  P.amg_work = 0;
+  P.amg_build_work = 0;
+  if (P.nfree == 0) {
+    *ok = 1;
+    return SVXG_OK;
+  }
+  P.lv.emplace_back();
+  {
+    Level& L0 = P.lv[0];
+    L0.A = P.K;  // (level 0's matrix is K itself: shared, not copied)
+    TRY(P.mem.alloc(&L0.pos, 3 * size_t(P.nfree)));
+    k_level0_pos<<<nblk(P.n), kT, 0, P.stream>>>(P.n, P.d_nodes, P.d_dof, L0.pos);
+    bool fin = false;
+    TRY(finalize_level(P, L0, &fin));
+    if (!fin) {
+      P.mem.release(L0.pos);
+      P.mem.release(L0.dinv);
+      P.lv.clear();
+      return SVXG_OK;
+    }
+  }
+  const svxg_amg_options& o = P.opt.amg;
+  const int max_levels = std::min(o.max_levels, 16);
+  while (int(P.lv.size()) < max_levels && P.lv.back().A.n > o.coarse_max) {
+    const Bsr& L = P.lv.back().A;
+    const bool dense = P.lv.size() > 1 && L.nnzb > 80 * int64_t(L.n);
+    if (dense && !o.coarsen_dense) break;
+    bool made = false;
+    TRY(coarsen(P, P.lv.size() - 1, !dense && o.smoothed, &made));
+    if (!made) break;
+    if (dense) break;
+  }
+  TRY(factor_coarsest(P));
+  // work per apply (amg.cpp:306-316)
+  for (size_t l = 0; l < P.lv.size(); ++l) {
+    const bool last = l + 1 == P.lv.size();
+    const int64_t nd = o.dense_work_per_unknown ? P.chol_n : P.chol_n / 6;
+    const int64_t blocks = P.lv[l].A.nnzb;
+    const int64_t coarsest = P.chol_n > 0 ? std::max<int64_t>(blocks, 2 * nd * nd) : 8 * 2 * blocks;
+    const int64_t per = last ? coarsest : blocks * (4 * o.sweeps + 2);
+    int64_t g = 1;
+    for (size_t k = 0; k < l; ++k) g *= o.gamma;
+    P.amg_work += per * g;
+  }
+  TRY(prepare_cycle(P));
+  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  *ok = 1;
+  return SVXG_OK;
+}
+
+}  // namespace svxg

@@ -1,0 +1,196 @@
+// problem.cuh - device state of one stress problem and the launchers each translation unit owns.
+//
+// HBM layout of a problem (all device-resident between calls):
+//   graph:  nodes (AoS svxg_node, 40 B), bonds (AoS svxg_bond, 216 B), material table (8 KB)
+//   K:      BSR of 6x6 blocks: rowptr[nfree+1] i32, col[nnzb] i32, val[36 nnzb] f64 row-major,
+//           each block row contiguous (a warp reads a row's blocks as one stream)
+//   K32:    the same values in f32 (mixed precision)
+//   hierarchy: per level A (BSR f64 for setup, f32 copy for the cycle), D^-1 (f64, f32),
+//           prolongation (BSR by fine row) and restriction (by coarse row) in f32, vectors of
+//           6 per node
+//   run:    x, r, z, p, q (6 nfree f64), the load, scalars of the conjugate-gradient sequence
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "svxg.h"
+
+namespace svxg {
+
+// Thread-local last error message (svxg_last_error).
+void set_error(const std::string& msg);
+
+#define SVXG_CUDA(call)                                                                   \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) {                                                              \
+      ::svxg::set_error(std::string(#call) + ": " + cudaGetErrorString(e_));              \
+      return SVXG_ERR_CUDA;                                                               \
+    }                                                                                     \
+  } while (0)
+
+// Device allocations of a problem (counted against its bytes).
+struct DevArena {
+  std::vector<std::pair<void*, size_t>> live;
+  int64_t bytes = 0;
+  template <class T>
+  int alloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, count * sizeof(T));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+      return e == cudaErrorMemoryAllocation ? SVXG_ERR_NOMEM : SVXG_ERR_CUDA;
+    }
+    live.push_back({q, count * sizeof(T)});
+    bytes += int64_t(count * sizeof(T));
+    *p = static_cast<T*>(q);
+    return SVXG_OK;
+  }
+  template <class T>
+  void release(T*& p) {
+    if (!p) return;
+    for (size_t i = 0; i < live.size(); ++i)
+      if (live[i].first == p) {
+        cudaFree(p);
+        bytes -= int64_t(live[i].second);
+        live[i] = live.back();
+        live.pop_back();
+        break;
+      }
+    p = nullptr;
+  }
+  // [p, p + bytes) inside one live allocation (a host-side guard before copies)
+  bool holds(const void* p, size_t bytes) const {
+    const char* c = static_cast<const char*>(p);
+    for (const auto& e : live) {
+      const char* b = static_cast<const char*>(e.first);
+      if (c >= b && c + bytes <= b + e.second) return true;
+    }
+    return false;
+  }
+  void release_all() {
+    for (auto& e : live) cudaFree(e.first);
+    live.clear();
+    bytes = 0;
+  }
+};
+
+struct Bsr {
+  int32_t n = 0;
+  int64_t nnzb = 0;
+  int32_t* rowptr = nullptr;
+  int32_t* col = nullptr;
+  double* val = nullptr;  // 36 per block, row-major
+  float* val32 = nullptr; // 36 per block, row-major (f32 copy)
+};
+
+// The scalars of a conjugate-gradient run (device memory).
+struct PcgScalars {
+  double rz, bn, target, pq, alpha, beta, rn, rel_res;
+  int32_t iters, converged, breakdown, done;
+  int32_t maxit, pad0;
+  double rr, rz_new;
+};
+
+struct Level {
+  Bsr A;
+  double* dinv = nullptr;    // 36 per node (f64, setup)
+  float* dinv32 = nullptr;   // 36 per node (f32, cycle)
+  int32_t* parent = nullptr; // node -> coarse node
+  double* pos = nullptr;     // 3 per node
+  int32_t* prow = nullptr;   // prolongation by fine row
+  int32_t* pcol = nullptr;
+  double* pval = nullptr;
+  float* pval32 = nullptr;
+  int64_t pnnz = 0;
+  int32_t* rrow = nullptr;   // restriction by coarse row: entries (fine node, P block)
+  int32_t* rent_i = nullptr;
+  int32_t* rent_e = nullptr;
+  double lmax = 0.0;         // lambda_max(D^-1 A) estimate (smoothed prolongation's damping)
+  double cheb_lmax = 0.0;    // the smoother's estimate
+  float* b32 = nullptr;      // cycle vectors, 6 per node (f32)
+  float* x32 = nullptr;
+  float* r32 = nullptr;
+  float* t32 = nullptr;
+  float* u32 = nullptr;
+};
+
+struct Problem {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  DevArena mem;
+  // graph (host copy kept for the in-place updates' bookkeeping)
+  int32_t n = 0, nb = 0;
+  std::vector<svxg_node> h_nodes;
+  std::vector<svxg_bond> h_bonds;
+  std::vector<svxg_material> h_mats;
+  svxg_node* d_nodes = nullptr;
+  svxg_bond* d_bonds = nullptr;
+  svxg_material* d_mats = nullptr;
+  bool have_graph = false;
+  // assembly
+  svxg_stress_options opt{};
+  bool assembled = false, pc_current = false, jacobi_only = false;
+  int64_t assembly_work = 0;
+  int32_t nfree = 0;
+  int32_t* d_dof = nullptr;       // node -> free index (-1 fixed)
+  std::vector<int32_t> h_dof;
+  uint8_t* d_in_k = nullptr;      // per bond
+  Bsr K;
+  double id_scale = 1.0;
+  double* d_jinv = nullptr;       // block-Jacobi inverses (36 per free node)
+  // multigrid
+  std::vector<Level> lv;
+  double* d_chol = nullptr;       // coarsest dense factor (m x m, lower = L, upper = L^T)
+  double* d_cinv = nullptr;       // its inverse L^-1 (lower), for the cycle's coarsest solve
+  double* d_cvec = nullptr;       // coarsest solve's f64 vectors (2 m)
+  int32_t chol_n = 0;
+  int64_t amg_work = 0, amg_build_work = 0;
+  // run state
+  double *d_x = nullptr, *d_r = nullptr, *d_z = nullptr, *d_p = nullptr, *d_q = nullptr, *d_f = nullptr;
+  double* d_un = nullptr;         // node-order u then f (12 n), owned by the C ABI's calls
+  PcgScalars* d_s = nullptr;
+  PcgScalars* h_s = nullptr;      // pinned mirror
+  double* d_partials = nullptr;   // block partial sums
+  unsigned* d_counter = nullptr;  // last-block counters
+  int32_t partial_blocks = 0;
+  bool active = false;
+  int32_t run_iters = 0;
+  // scratch
+  int32_t* d_scan = nullptr;      // scan block sums
+  int64_t scan_cap = 0;
+};
+
+// ---- launchers (one translation unit each) ---------------------------------------------------
+// exact_assemble.cu
+int assemble_matrix(Problem& P);                 // dof, pattern, K, id_scale, identity rows
+int build_jacobi(Problem& P);                    // block-Jacobi inverses
+int remove_bonds_device(Problem& P, const int32_t* bonds, int32_t count);  // sequential, in order
+int set_identity_rows(Problem& P, const int32_t* rows, int32_t count);
+// exact_amg.cu
+int build_hierarchy(Problem& P, int32_t* ok);    // Amg::build on the device
+// solve.cu
+int spmv(Problem& P, const Bsr& A, const double* x, double* y);
+int pcg_begin(Problem& P, const double* f_nodes, const double* u0_nodes);  // device, node order
+int pcg_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res);
+int gather_solution(Problem& P, double* u_nodes);                        // device, node order
+int precondition(Problem& P, const double* r, double* z);
+int free_run(Problem& P);
+// vcycle.cu
+int vcycle(Problem& P, const double* r, double* z);
+int prepare_cycle(Problem& P);
+// exact_judge.cu
+int bond_loads_device(Problem& P, const double* u_nodes, svxg_bond_load* out);
+int utilization_device(Problem& P, const double* u_nodes, double fragility, double* phi, uint8_t* mode,
+                       int32_t* over, int32_t* n_over);
+// scan.cu
+int exclusive_scan_i32(Problem& P, const int32_t* in, int32_t* out, int64_t n, int32_t* total_host);
+
+}  // namespace svxg

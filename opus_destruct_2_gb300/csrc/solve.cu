@@ -1,0 +1,508 @@
+// solve.cu - BSR SpMV and the preconditioned conjugate-gradient sequence on the device.
+//
+// The sequence is the reference's StressProblem::begin / iterate (core/src/stress/stress.cpp:
+// 362-464): the same recurrences, breakdown tests (p.q <= 0, r.z <= 0, non-finite loads) and
+// convergence test (||r|| <= rtol ||f||), with the dots as deterministic two-level reductions
+// (block partial sums, then the last block to finish sums them in block order: no atomics on
+// values, identical run to run). alpha, beta and the flags live on the device; an iteration is
+// four launches and never waits for the host:
+//   1. q = K p with p.q in the epilogue           -> alpha, breakdown
+//   2. x += alpha p, r -= alpha q with r.r        -> convergence
+//   3. z = M^-1 r (block-Jacobi: fused with r.z; multigrid: the V-cycle, then r.z)
+//   4. p = z + beta p
+// Every kernel returns at once when the run is done, so a batch of iterations queued past
+// convergence costs only launches.
+#include <cmath>
+
+#include "problem.cuh"
+
+namespace svxg {
+namespace {
+
+constexpr int kVecT = 256;    // vector kernels: one thread per free node
+constexpr int kSpmvT = 256;   // SpMV: one warp per block row
+constexpr int kRowsPerBlock = kSpmvT / 32;
+
+inline unsigned vec_blocks(int32_t nfree) { return unsigned((nfree + kVecT - 1) / kVecT); }
+inline unsigned spmv_blocks(int32_t n) { return unsigned((n + kRowsPerBlock - 1) / kRowsPerBlock); }
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+  return v;
+}
+
+// Sum of one value per thread over the block (fixed tree); valid in thread 0.
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < NT / 32; ++i) s += sh[i];
+  return s;
+}
+
+// Writes this block's NV partials; returns true in every thread of the last block to finish,
+// after which that block may read all partials.
+template <int NV>
+__device__ __forceinline__ bool publish(const double* vals, double* partials, unsigned* counter) {
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    for (int v = 0; v < NV; ++v) partials[size_t(blockIdx.x) * NV + v] = vals[v];
+    __threadfence();
+    const unsigned t = atomicAdd(counter, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  return last;
+}
+
+// In the last block: the NV totals over all blocks' partials, in block order per thread then a
+// fixed tree; valid in thread 0. Resets the counter.
+template <int NT, int NV>
+__device__ __forceinline__ void gather_totals(const double* partials, unsigned* counter, double* out, double* sh) {
+  __threadfence();
+  for (int v = 0; v < NV; ++v) {
+    double s = 0.0;
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += NT) s += __ldcg(&partials[size_t(b) * NV + v]);
+    out[v] = block_sum<NT>(s, sh);
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
+// ---- SpMV ------------------------------------------------------------------------------------
+// One warp per block row; lanes 6g + r (g < 5) take block g of each group of five and its row r:
+// six consecutive values of the block (16-byte loads) against the column's x (the same six
+// values for the group's six lanes: one broadcast load). The five groups' sums meet in lanes
+// 0-5 by shuffles.
+template <typename V>
+__device__ __forceinline__ double row_dot6(const V* m, const double* x);
+
+template <>
+__device__ __forceinline__ double row_dot6<double>(const double* m, const double* x) {
+  const double2 a = __ldg(reinterpret_cast<const double2*>(m));
+  const double2 b = __ldg(reinterpret_cast<const double2*>(m) + 1);
+  const double2 c = __ldg(reinterpret_cast<const double2*>(m) + 2);
+  const double2 u = __ldg(reinterpret_cast<const double2*>(x));
+  const double2 v = __ldg(reinterpret_cast<const double2*>(x) + 1);
+  const double2 w = __ldg(reinterpret_cast<const double2*>(x) + 2);
+  return a.x * u.x + a.y * u.y + b.x * v.x + b.y * v.y + c.x * w.x + c.y * w.y;
+}
+
+enum Epilogue { kPlain = 0, kDotP = 1 };
+
+template <int EPI>
+__global__ void __launch_bounds__(kSpmvT) k_spmv(int32_t n, const int32_t* __restrict__ rowptr,
+                                                 const int32_t* __restrict__ col, const double* __restrict__ val,
+                                                 const double* __restrict__ x, double* __restrict__ y,
+                                                 double* partials, unsigned* counter, PcgScalars* s) {
+  __shared__ double sh[kSpmvT / 32];
+  if (EPI == kDotP && s->done) return;
+  const int lane = threadIdx.x & 31;
+  const int32_t row = blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5);
+  const int g = lane / 6, r = lane - 6 * (lane / 6);
+  double acc = 0.0;
+  if (row < n) {
+    const int32_t k0 = rowptr[row], k1 = rowptr[row + 1];
+    if (g < 5)
+      for (int32_t k = k0 + g; k < k1; k += 5)
+        acc += row_dot6<double>(val + 36 * int64_t(k) + 6 * r, x + 6 * int64_t(__ldg(col + k)));
+  }
+  const double a1 = __shfl_sync(0xffffffffu, acc, (r + 6) & 31);
+  const double a2 = __shfl_sync(0xffffffffu, acc, (r + 12) & 31);
+  const double a3 = __shfl_sync(0xffffffffu, acc, (r + 18) & 31);
+  const double a4 = __shfl_sync(0xffffffffu, acc, (r + 24) & 31);
+  const double yr = acc + a1 + a2 + a3 + a4;
+  double dp = 0.0;
+  if (row < n && lane < 6) {
+    y[6 * int64_t(row) + lane] = yr;
+    if (EPI == kDotP) dp = x[6 * int64_t(row) + lane] * yr;
+  }
+  if (EPI == kDotP) {
+    const double bs = block_sum<kSpmvT>(dp, sh);
+    if (publish<1>(&bs, partials, counter)) {
+      double tot;
+      gather_totals<kSpmvT, 1>(partials, counter, &tot, sh);
+      if (threadIdx.x == 0) {
+        s->pq = tot;
+        s->iters += 1;
+        if (!(tot > 0)) {
+          s->breakdown = 1;
+          s->done = 1;
+        } else {
+          s->alpha = s->rz / tot;
+        }
+      }
+    }
+  }
+}
+
+// ---- vector kernels (one thread per free node, 6 entries) ---------------------------------------
+
+// r = f - q, partial f.f (begin)
+__global__ void k_begin_r(int32_t nfree, const double* f, const double* q, double* r, double* partials,
+                          unsigned* counter, PcgScalars* s) {
+  __shared__ double sh[kVecT / 32];
+  const int32_t i = blockIdx.x * kVecT + threadIdx.x;
+  double ff = 0.0;
+  if (i < nfree)
+    for (int c = 0; c < 6; ++c) {
+      const double fv = f[6 * int64_t(i) + c];
+      r[6 * int64_t(i) + c] = fv - q[6 * int64_t(i) + c];
+      ff += fv * fv;
+    }
+  const double bs = block_sum<kVecT>(ff, sh);
+  if (publish<1>(&bs, partials, counter)) {
+    double tot;
+    gather_totals<kVecT, 1>(partials, counter, &tot, sh);
+    if (threadIdx.x == 0) s->bn = sqrt(tot);
+  }
+}
+
+// zero x and r when the load is zero or not finite (stress.cpp:389-394)
+__global__ void k_begin_zero(int32_t nfree, double* x, double* r, const PcgScalars* s) {
+  if (s->bn > 0.0) return;
+  const int32_t i = blockIdx.x * kVecT + threadIdx.x;
+  if (i < nfree)
+    for (int c = 0; c < 6; ++c) x[6 * int64_t(i) + c] = r[6 * int64_t(i) + c] = 0.0;
+}
+
+// z = Jinv r (block-Jacobi), and r.z; MODE 0: begin (rz, p = z), 1: iteration (beta)
+template <int MODE>
+__global__ void k_jacobi_rz(int32_t nfree, const double* __restrict__ jinv, const double* __restrict__ r,
+                            double* __restrict__ z, double* p, double* partials, unsigned* counter, PcgScalars* s) {
+  __shared__ double sh[kVecT / 32];
+  if (MODE == 1 && s->done) return;
+  const int32_t i = blockIdx.x * kVecT + threadIdx.x;
+  double rz = 0.0;
+  if (i < nfree) {
+    const double* J = jinv + 36 * int64_t(i);
+    double rv[6];
+    for (int c = 0; c < 6; ++c) rv[c] = r[6 * int64_t(i) + c];
+    for (int a = 0; a < 6; ++a) {
+      double zv = 0.0;
+      for (int c = 0; c < 6; ++c) zv += J[6 * a + c] * rv[c];
+      z[6 * int64_t(i) + a] = zv;
+      if (MODE == 0) p[6 * int64_t(i) + a] = zv;
+      rz += rv[a] * zv;
+    }
+  }
+  const double bs = block_sum<kVecT>(rz, sh);
+  if (publish<1>(&bs, partials, counter)) {
+    double tot;
+    gather_totals<kVecT, 1>(partials, counter, &tot, sh);
+    if (threadIdx.x == 0) {
+      if (MODE == 0) {
+        s->rz = tot;
+      } else if (!(tot > 0)) {
+        s->breakdown = 1;
+        s->done = 1;
+      } else {
+        s->beta = tot / s->rz;
+        s->rz = tot;
+      }
+    }
+  }
+}
+
+// r.z after a multigrid preconditioner; MODE 0: begin (rz, p = z), 1: iteration (beta)
+template <int MODE>
+__global__ void k_rz(int32_t nfree, const double* __restrict__ r, const double* __restrict__ z, double* p,
+                     double* partials, unsigned* counter, PcgScalars* s) {
+  __shared__ double sh[kVecT / 32];
+  if (MODE == 1 && s->done) return;
+  const int32_t i = blockIdx.x * kVecT + threadIdx.x;
+  double rz = 0.0;
+  if (i < nfree)
+    for (int c = 0; c < 6; ++c) {
+      const double zv = z[6 * int64_t(i) + c];
+      rz += r[6 * int64_t(i) + c] * zv;
+      if (MODE == 0) p[6 * int64_t(i) + c] = zv;
+    }
+  const double bs = block_sum<kVecT>(rz, sh);
+  if (publish<1>(&bs, partials, counter)) {
+    double tot;
+    gather_totals<kVecT, 1>(partials, counter, &tot, sh);
+    if (threadIdx.x == 0) {
+      if (MODE == 0) {
+        s->rz = tot;
+      } else if (!(tot > 0)) {
+        s->breakdown = 1;
+        s->done = 1;
+      } else {
+        s->beta = tot / s->rz;
+        s->rz = tot;
+      }
+    }
+  }
+}
+
+// the start of iterate(): ||r||, the target, the non-finite and already-converged exits
+__global__ void k_iter_start(int32_t nfree, const double* r, double rtol, int32_t maxit, double* partials,
+                             unsigned* counter, PcgScalars* s) {
+  __shared__ double sh[kVecT / 32];
+  const int32_t i = blockIdx.x * kVecT + threadIdx.x;
+  double rr = 0.0;
+  if (i < nfree)
+    for (int c = 0; c < 6; ++c) {
+      const double v = r[6 * int64_t(i) + c];
+      rr += v * v;
+    }
+  const double bs = block_sum<kVecT>(rr, sh);
+  if (publish<1>(&bs, partials, counter)) {
+    double tot;
+    gather_totals<kVecT, 1>(partials, counter, &tot, sh);
+    if (threadIdx.x == 0) {
+      const double rn = sqrt(tot);
+      s->rn = rn;
+      s->iters = 0;
+      s->converged = 0;
+      s->breakdown = 0;
+      s->done = 0;
+      s->maxit = maxit;
+      s->target = rtol * s->bn;
+      if (!isfinite(s->bn) || !isfinite(rn)) {
+        s->rel_res = INFINITY;
+        s->breakdown = 1;
+        s->done = 1;
+      } else {
+        s->rel_res = s->bn > 0 ? rn / s->bn : 0.0;
+        if (rn <= s->target || !(s->bn > 0) || nfree == 0 || maxit <= 0) {
+          s->converged = (rn <= s->target || !(s->bn > 0) || nfree == 0) ? 1 : 0;
+          s->done = 1;
+        }
+      }
+    }
+  }
+}
+
+// x += alpha p, r -= alpha q, ||r|| and the convergence test
+__global__ void k_axpy_rr(int32_t nfree, double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
+                          const double* __restrict__ q, double* partials, unsigned* counter, PcgScalars* s) {
+  __shared__ double sh[kVecT / 32];
+  if (s->done) return;
+  const double alpha = s->alpha;
+  const int32_t i = blockIdx.x * kVecT + threadIdx.x;
+  double rr = 0.0;
+  if (i < nfree)
+    for (int c = 0; c < 6; ++c) {
+      const int64_t k = 6 * int64_t(i) + c;
+      x[k] += alpha * p[k];
+      const double rv = r[k] - alpha * q[k];
+      r[k] = rv;
+      rr += rv * rv;
+    }
+  const double bs = block_sum<kVecT>(rr, sh);
+  if (publish<1>(&bs, partials, counter)) {
+    double tot;
+    gather_totals<kVecT, 1>(partials, counter, &tot, sh);
+    if (threadIdx.x == 0) {
+      const double rn = sqrt(tot);
+      s->rn = rn;
+      s->rel_res = rn / s->bn;
+      if (rn <= s->target) {
+        s->converged = 1;
+        s->done = 1;
+      }
+    }
+  }
+}
+
+// p = z + beta p
+__global__ void k_p_update(int32_t nfree, const double* __restrict__ z, double* __restrict__ p, PcgScalars* s) {
+  if (s->done) return;
+  const double beta = s->beta;
+  const int32_t i = blockIdx.x * kVecT + threadIdx.x;
+  if (i < nfree)
+    for (int c = 0; c < 6; ++c) {
+      const int64_t k = 6 * int64_t(i) + c;
+      p[k] = z[k] + beta * p[k];
+    }
+}
+
+// the iteration cap ends a call after a full iteration (the sequence resumes in the next call)
+__global__ void k_mark_cap(PcgScalars* s) {
+  if (threadIdx.x == 0 && !s->done && s->iters >= s->maxit) s->done = 2;
+}
+
+// z = Jinv r alone (the preconditioner's application)
+__global__ void k_jacobi_apply(int32_t nfree, const double* __restrict__ jinv, const double* __restrict__ r,
+                               double* __restrict__ z) {
+  const int32_t i = blockIdx.x * kVecT + threadIdx.x;
+  if (i >= nfree) return;
+  const double* J = jinv + 36 * int64_t(i);
+  for (int a = 0; a < 6; ++a) {
+    double zv = 0.0;
+    for (int c = 0; c < 6; ++c) zv += J[6 * a + c] * r[6 * int64_t(i) + c];
+    z[6 * int64_t(i) + a] = zv;
+  }
+}
+
+// node order <-> free-DOF order
+__global__ void k_scatter_free(int32_t n, const int32_t* dof, const double* nodes6, double* free6) {
+  const int32_t i = blockIdx.x * kVecT + threadIdx.x;
+  if (i >= n) return;
+  const int32_t d = dof[i];
+  if (d < 0) return;
+  for (int c = 0; c < 6; ++c) free6[6 * int64_t(d) + c] = nodes6[6 * int64_t(i) + c];
+}
+
+__global__ void k_gather_nodes(int32_t n, const int32_t* dof, const double* free6, double* nodes6) {
+  const int32_t i = blockIdx.x * kVecT + threadIdx.x;
+  if (i >= n) return;
+  const int32_t d = dof[i];
+  for (int c = 0; c < 6; ++c) nodes6[6 * int64_t(i) + c] = d >= 0 ? free6[6 * int64_t(d) + c] : 0.0;
+}
+
+#define TRY(x)            \
+  do {                    \
+    int e__ = (x);        \
+    if (e__) return e__;  \
+  } while (0)
+
+int ensure_run(Problem& P) {
+  if (P.d_x) return SVXG_OK;
+  const size_t m = 6 * size_t(P.nfree);
+  TRY(P.mem.alloc(&P.d_x, m));
+  TRY(P.mem.alloc(&P.d_r, m));
+  TRY(P.mem.alloc(&P.d_z, m));
+  TRY(P.mem.alloc(&P.d_p, m));
+  TRY(P.mem.alloc(&P.d_q, m));
+  TRY(P.mem.alloc(&P.d_f, m));
+  TRY(P.mem.alloc(&P.d_s, 1));
+  P.partial_blocks = int32_t(std::max(spmv_blocks(P.nfree), vec_blocks(P.nfree))) + 1;
+  TRY(P.mem.alloc(&P.d_partials, size_t(P.partial_blocks) * 4));
+  TRY(P.mem.alloc(&P.d_counter, 4));
+  SVXG_CUDA(cudaMemsetAsync(P.d_counter, 0, 4 * sizeof(unsigned), P.stream));
+  SVXG_CUDA(cudaMemsetAsync(P.d_s, 0, sizeof(PcgScalars), P.stream));
+  if (!P.h_s) SVXG_CUDA(cudaMallocHost(&P.h_s, sizeof(PcgScalars)));
+  return SVXG_OK;
+}
+
+}  // namespace
+
+int spmv(Problem& P, const Bsr& A, const double* x, double* y) {
+  if (A.n == 0) return SVXG_OK;
+  k_spmv<kPlain><<<spmv_blocks(A.n), kSpmvT, 0, P.stream>>>(A.n, A.rowptr, A.col, A.val, x, y, nullptr, nullptr,
+                                                            nullptr);
+  SVXG_CUDA(cudaGetLastError());
+  return SVXG_OK;
+}
+
+int free_run(Problem& P) {
+  P.mem.release(P.d_x);
+  P.mem.release(P.d_r);
+  P.mem.release(P.d_z);
+  P.mem.release(P.d_p);
+  P.mem.release(P.d_q);
+  P.mem.release(P.d_f);
+  P.mem.release(P.d_s);
+  P.mem.release(P.d_partials);
+  P.mem.release(P.d_counter);
+  P.active = false;
+  return SVXG_OK;
+}
+
+int precondition(Problem& P, const double* r, double* z) {
+  if (P.jacobi_only) {
+    if (P.nfree > 0) k_jacobi_apply<<<vec_blocks(P.nfree), kVecT, 0, P.stream>>>(P.nfree, P.d_jinv, r, z);
+    SVXG_CUDA(cudaGetLastError());
+    return SVXG_OK;
+  }
+  return vcycle(P, r, z);
+}
+
+// StressProblem::begin (stress.cpp:362-401); f, u0: device, node order (u0 may be null)
+int pcg_begin(Problem& P, const double* f_nodes, const double* u0_nodes) {
+  TRY(ensure_run(P));
+  const int32_t nf = P.nfree;
+  const size_t m = 6 * size_t(nf);
+  cudaStream_t st = P.stream;
+  SVXG_CUDA(cudaMemsetAsync(P.d_x, 0, m * sizeof(double), st));
+  SVXG_CUDA(cudaMemsetAsync(P.d_s, 0, sizeof(PcgScalars), st));
+  const unsigned nb_nodes = unsigned((P.n + kVecT - 1) / kVecT);
+  if (P.n > 0) {
+    k_scatter_free<<<nb_nodes, kVecT, 0, st>>>(P.n, P.d_dof, f_nodes, P.d_f);
+    if (u0_nodes) k_scatter_free<<<nb_nodes, kVecT, 0, st>>>(P.n, P.d_dof, u0_nodes, P.d_x);
+  }
+  if (nf > 0) {
+    TRY(spmv(P, P.K, P.d_x, P.d_q));
+    k_begin_r<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_f, P.d_q, P.d_r, P.d_partials, P.d_counter, P.d_s);
+    k_begin_zero<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_x, P.d_r, P.d_s);
+    if (P.jacobi_only) {
+      k_jacobi_rz<0><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_jinv, P.d_r, P.d_z, P.d_p, P.d_partials,
+                                                       P.d_counter, P.d_s);
+    } else {
+      TRY(vcycle(P, P.d_r, P.d_z));
+      k_rz<0><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_r, P.d_z, P.d_p, P.d_partials, P.d_counter, P.d_s);
+    }
+  }
+  SVXG_CUDA(cudaGetLastError());
+  P.active = true;
+  P.run_iters = 0;
+  return SVXG_OK;
+}
+
+// StressProblem::iterate (stress.cpp:403-464)
+int pcg_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) {
+  svxg_pcg_result out{};
+  if (!P.active) {
+    if (res) *res = out;
+    return SVXG_OK;
+  }
+  const int32_t nf = P.nfree;
+  cudaStream_t st = P.stream;
+  k_iter_start<<<vec_blocks(std::max(nf, 1)), kVecT, 0, st>>>(nf, P.d_r, rtol, maxit, P.d_partials, P.d_counter,
+                                                             P.d_s);
+  SVXG_CUDA(cudaGetLastError());
+  int32_t queued = 0;
+  int32_t batch = 2;
+  for (;;) {
+    SVXG_CUDA(cudaMemcpyAsync(P.h_s, P.d_s, sizeof(PcgScalars), cudaMemcpyDeviceToHost, st));
+    SVXG_CUDA(cudaStreamSynchronize(st));
+    if (P.h_s->done || queued >= maxit) break;
+    const int32_t todo = std::min(batch, maxit - queued);
+    for (int32_t it = 0; it < todo; ++it) {
+      k_spmv<kDotP><<<spmv_blocks(nf), kSpmvT, 0, st>>>(nf, P.K.rowptr, P.K.col, P.K.val, P.d_p, P.d_q,
+                                                        P.d_partials, P.d_counter, P.d_s);
+      k_axpy_rr<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_x, P.d_r, P.d_p, P.d_q, P.d_partials, P.d_counter, P.d_s);
+      if (P.jacobi_only) {
+        k_jacobi_rz<1><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_jinv, P.d_r, P.d_z, nullptr, P.d_partials,
+                                                         P.d_counter, P.d_s);
+      } else {
+        TRY(vcycle(P, P.d_r, P.d_z));
+        k_rz<1><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_r, P.d_z, nullptr, P.d_partials, P.d_counter, P.d_s);
+      }
+      k_p_update<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_z, P.d_p, P.d_s);
+      k_mark_cap<<<1, 32, 0, st>>>(P.d_s);
+    }
+    SVXG_CUDA(cudaGetLastError());
+    queued += todo;
+    batch = std::min(batch * 2, 32);
+  }
+  out.iters = P.h_s->iters;
+  out.converged = P.h_s->converged;
+  out.breakdown = P.h_s->breakdown;
+  out.rel_res = P.h_s->rel_res;
+  P.run_iters += out.iters;
+  if (out.breakdown && !std::isfinite(out.rel_res)) P.active = false;
+  if (res) *res = out;
+  return SVXG_OK;
+}
+
+int gather_solution(Problem& P, double* u_nodes) {
+  if (P.n == 0) return SVXG_OK;
+  if (!P.d_x) {
+    SVXG_CUDA(cudaMemsetAsync(u_nodes, 0, 6 * size_t(P.n) * sizeof(double), P.stream));
+    return SVXG_OK;
+  }
+  k_gather_nodes<<<unsigned((P.n + kVecT - 1) / kVecT), kVecT, 0, P.stream>>>(P.n, P.d_dof, P.d_x, u_nodes);
+  SVXG_CUDA(cudaGetLastError());
+  return SVXG_OK;
+}
+
+}  // namespace svxg

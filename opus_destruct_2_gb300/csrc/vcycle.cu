@@ -1,0 +1,426 @@
+// vcycle.cu - the multigrid V-cycle on the device, in single precision as the reference's
+// (Amg::make_fast / cycle_f / apply, core/src/solve/amg.cpp:594-731): r (f64) -> f32 at entry,
+// one cycle from zero, z (f32 -> f64) at exit; the coarsest level solved densely in f64.
+//
+// The smoother is the one the reference's options name but its cycle does not implement
+// (AmgOptions::sgs = false: block-Jacobi Chebyshev, core/include/svx/solve/amg.hpp:53-55): a
+// Chebyshev polynomial in D^-1 A on [lmax / 10, lmax] (lmax: the level's power-iteration bound),
+// the same polynomial before and after the coarse correction so the cycle stays symmetric (a
+// valid conjugate-gradient preconditioner). Unlike the reference's hybrid Gauss-Seidel it has no
+// sequential dependence: every step is one warp-per-block-row SpMV with the D^-1 block of the row
+// and the vector updates fused into its epilogue (direction vectors double-buffered; x updated
+// one step late so that no kernel reads a neighbour's x while it is being written).
+//
+// Per level and cycle: pre-smoothing (2 kernels), residual (1), restriction (1, an SpMV over
+// P^T stored by coarse row), prolongation (1, an SpMV over P by fine row, accumulating),
+// post-smoothing (2).
+#include <algorithm>
+#include <cmath>
+
+#include "problem.cuh"
+
+namespace svxg {
+namespace {
+
+constexpr int kT = 256;
+constexpr int kRows = kT / 32;
+inline unsigned nblk(int64_t n, int t = kT) { return unsigned(std::max<int64_t>(1, (n + t - 1) / t)); }
+inline unsigned rblk(int32_t n) { return unsigned(std::max<int32_t>(1, (n + kRows - 1) / kRows)); }
+
+#define TRY(x)            \
+  do {                    \
+    int e__ = (x);        \
+    if (e__) return e__;  \
+  } while (0)
+
+constexpr int kChebDegree = 2;      // smoothing polynomial degree (each side)
+constexpr double kChebRatio = 10.0; // lmax / lmin of the smoothed interval
+constexpr int kCoarseDegree = 8;    // stalled coarsest level: polynomial degree in place of a solve
+
+__global__ void k_cvt(int64_t m, const double* in, float* out) {
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < m) out[k] = float(in[k]);
+}
+
+__global__ void k_widen(int64_t m, const float* in, double* out) {
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < m) out[k] = double(in[k]);
+}
+
+// R (P^T blocks) in restriction order: R_r = P_{rent_e[r]}^T, row-major
+__global__ void k_cvt_transpose(int64_t pnnz, const int32_t* rent_e, const double* pval, float* rval) {
+  const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (r >= pnnz) return;
+  const double* P = pval + 36 * int64_t(rent_e[r]);
+  float* R = rval + 36 * r;
+  for (int a = 0; a < 6; ++a)
+    for (int b = 0; b < 6; ++b) R[a * 6 + b] = float(P[b * 6 + a]);
+}
+
+// Warp-per-row block product in f32: lanes 6g + c (g < 5) take every fifth block of the row
+// and its row c; the row's six sums end in lanes 0-5.
+__device__ __forceinline__ float row_block_sum(int32_t k0, int32_t k1, const int32_t* __restrict__ col,
+                                               const float* __restrict__ val, const float* __restrict__ x) {
+  const int lane = threadIdx.x & 31;
+  const int g = lane / 6, c = lane - 6 * g;
+  float acc = 0.0f;
+  if (g < 5)
+    for (int32_t k = k0 + g; k < k1; k += 5) {
+      const float2* m = reinterpret_cast<const float2*>(val + 36 * int64_t(k) + 6 * c);
+      const float2* xv = reinterpret_cast<const float2*>(x + 6 * int64_t(__ldg(col + k)));
+      const float2 a = __ldg(m), b = __ldg(m + 1), d = __ldg(m + 2);
+      const float2 u = __ldg(xv), v = __ldg(xv + 1), w = __ldg(xv + 2);
+      acc += a.x * u.x + a.y * u.y + b.x * v.x + b.y * v.y + d.x * w.x + d.y * w.y;
+    }
+  const float a1 = __shfl_sync(0xffffffffu, acc, (c + 6) & 31);
+  const float a2 = __shfl_sync(0xffffffffu, acc, (c + 12) & 31);
+  const float a3 = __shfl_sync(0xffffffffu, acc, (c + 18) & 31);
+  const float a4 = __shfl_sync(0xffffffffu, acc, (c + 24) & 31);
+  return acc + a1 + a2 + a3 + a4;
+}
+
+// (D^-1 v)_c for lane c < 6, v held by lanes 0-5
+__device__ __forceinline__ float dinv_row(const float* __restrict__ D, float v, int c) {
+  float s = 0.0f;
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    const float vq = __shfl_sync(0xffffffffu, v, q);
+    if (c < 6) s += __ldg(D + 6 * c + q) * vq;
+  }
+  return s;
+}
+
+enum Mode {
+  kY = 0,        // y = A x
+  kAcc = 1,      // y += A x
+  kStep = 2,     // r = rin - A d; dout = c1 d + c2 D^-1 r; x (= or +=) d [+ dout]
+  kResPend = 3,  // r = rin - A d; x += d
+  kPostStart = 4 // r = b - A x; dout = D^-1 r / theta
+};
+
+struct StepArgs {
+  const float* rin;  // kStep / kResPend: previous residual; kPostStart: b
+  float* r;          // residual out
+  float* dout;       // next direction
+  float* x;          // the smoothed iterate
+  const float* D;    // D^-1 blocks (36 per node)
+  float c1, c2;
+  int x_init;        // kStep: x = d (the first step from zero)
+  int x_last;        // kStep: also add dout (the last step)
+};
+
+template <int MODE>
+__global__ void __launch_bounds__(kT) k_bsr32(int32_t n, const int32_t* __restrict__ rowptr,
+                                              const int32_t* __restrict__ col, const float* __restrict__ val,
+                                              const float* __restrict__ v, float* y, StepArgs s) {
+  const int lane = threadIdx.x & 31;
+  const int32_t row = blockIdx.x * kRows + (threadIdx.x >> 5);
+  if (row >= n) return;  // (whole warps exit together)
+  const float av = row_block_sum(rowptr[row], rowptr[row + 1], col, val, v);
+  const int c = lane;
+  const int64_t o = 6 * int64_t(row) + c;
+  if (MODE == kY) {
+    if (c < 6) y[o] = av;
+  } else if (MODE == kAcc) {
+    if (c < 6) y[o] += av;
+  } else if (MODE == kStep) {
+    const float rv = c < 6 ? s.rin[o] - av : 0.0f;
+    const float z = dinv_row(s.D + 36 * int64_t(row), rv, c);
+    if (c < 6) {
+      const float dprev = v[o];
+      const float dn = s.c1 * dprev + s.c2 * z;
+      s.r[o] = rv;
+      s.dout[o] = dn;
+      float xv = s.x_init ? dprev : s.x[o] + dprev;
+      if (s.x_last) xv += dn;
+      s.x[o] = xv;
+    }
+  } else if (MODE == kResPend) {
+    if (c < 6) {
+      s.r[o] = s.rin[o] - av;
+      s.x[o] += v[o];
+    }
+  } else if (MODE == kPostStart) {
+    const float rv = c < 6 ? s.rin[o] - av : 0.0f;
+    const float z = dinv_row(s.D + 36 * int64_t(row), rv, c);
+    if (c < 6) {
+      s.r[o] = rv;
+      s.dout[o] = s.c2 * z;
+    }
+  }
+}
+
+// d = D^-1 b / theta (the first Chebyshev direction from x = 0); one thread per node
+__global__ void k_cheb_first(int32_t n, const float* __restrict__ D, const float* __restrict__ b, float inv_theta,
+                             float* d) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float* Di = D + 36 * int64_t(i);
+  float bv[6];
+  for (int q = 0; q < 6; ++q) bv[q] = b[6 * int64_t(i) + q];
+  for (int c = 0; c < 6; ++c) {
+    float s = 0.0f;
+    for (int q = 0; q < 6; ++q) s += Di[6 * c + q] * bv[q];
+    d[6 * int64_t(i) + c] = s * inv_theta;
+  }
+}
+
+__global__ void k_add(int64_t m, const float* d, float* x) {
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < m) x[k] += d[k];
+}
+
+// coarsest level: x = L^-T (L^-1 b) in f64 (warp per row, rows of L^-1 and of L^-T)
+__global__ void k_dense_mv(int32_t m, const double* __restrict__ M, const float* __restrict__ b32,
+                           const double* __restrict__ b64, double* y64, float* y32) {
+  const int lane = threadIdx.x & 31;
+  const int32_t row = blockIdx.x * kRows + (threadIdx.x >> 5);
+  if (row >= m) return;
+  double s = 0.0;
+  const double* Mr = M + int64_t(row) * m;
+  for (int32_t k = lane; k < m; k += 32) s += Mr[k] * (b32 ? double(b32[k]) : b64[k]);
+  for (int d = 16; d > 0; d >>= 1) s += __shfl_xor_sync(0xffffffffu, s, d);
+  if (lane == 0) {
+    if (y64) y64[row] = s;
+    if (y32) y32[row] = float(s);
+  }
+}
+
+// L^-1 column by column (forward substitution on the identity), and its transpose
+__global__ void k_tri_inverse(int32_t m, const double* __restrict__ L, double* X, double* XT) {
+  const int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  for (int32_t i = 0; i < j; ++i) {
+    X[int64_t(i) * m + j] = 0.0;
+    XT[int64_t(j) * m + i] = 0.0;
+  }
+  const double xjj = 1.0 / L[int64_t(j) * m + j];
+  X[int64_t(j) * m + j] = xjj;
+  XT[int64_t(j) * m + j] = xjj;
+  for (int32_t i = j + 1; i < m; ++i) {
+    double s = 0.0;
+    for (int32_t k = j; k < i; ++k) s += L[int64_t(i) * m + k] * X[int64_t(k) * m + j];
+    const double xij = -s / L[int64_t(i) * m + i];
+    X[int64_t(i) * m + j] = xij;
+    XT[int64_t(j) * m + i] = xij;
+  }
+}
+
+// power iteration for the smoother's bound where the setup left none (f64, 12 steps)
+__global__ void k_pow_step(int32_t n, const double* dinv, const double* w, double* v) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* D = dinv + 36 * int64_t(i);
+  for (int c = 0; c < 6; ++c) {
+    double s = 0.0;
+    for (int q = 0; q < 6; ++q) s += D[6 * c + q] * w[6 * int64_t(i) + q];
+    v[6 * int64_t(i) + c] = s;
+  }
+}
+
+__global__ void k_norm_scale(int64_t m, double* v, double* nrm) {
+  // one block: norm, then scale
+  __shared__ double sh[kT];
+  double s = 0.0;
+  for (int64_t k = threadIdx.x; k < m; k += blockDim.x) s += v[k] * v[k];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int d = blockDim.x / 2; d > 0; d >>= 1) {
+    if (threadIdx.x < d) sh[threadIdx.x] += sh[threadIdx.x + d];
+    __syncthreads();
+  }
+  const double nv = sqrt(sh[0]);
+  if (threadIdx.x == 0) *nrm = nv;
+  if (nv > 0)
+    for (int64_t k = threadIdx.x; k < m; k += blockDim.x) v[k] /= nv;
+}
+
+__global__ void k_spmv64(int32_t n, const int32_t* rowptr, const int32_t* col, const double* val, const double* x,
+                         double* y) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= 6 * int64_t(n)) return;
+  const int32_t i = int32_t(t / 6);
+  const int r = int(t % 6);
+  double s = 0.0;
+  for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+    for (int q = 0; q < 6; ++q) s += val[36 * int64_t(k) + 6 * r + q] * x[6 * int64_t(col[k]) + q];
+  y[t] = s;
+}
+
+__global__ void k_fill_ones(int64_t m, double* v) {
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < m) v[k] = 1.0 + 0.001 * double(k % 7);
+}
+
+int power_bound(Problem& P, const Level& L, double* out) {
+  const int64_t m = 6 * int64_t(L.A.n);
+  double *v = nullptr, *w = nullptr, *nv = nullptr;
+  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&v), m * sizeof(double), P.stream));
+  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&w), m * sizeof(double), P.stream));
+  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&nv), sizeof(double), P.stream));
+  k_fill_ones<<<nblk(m), kT, 0, P.stream>>>(m, v);
+  for (int it = 0; it < 12; ++it) {
+    k_spmv64<<<nblk(m), kT, 0, P.stream>>>(L.A.n, L.A.rowptr, L.A.col, L.A.val, v, w);
+    k_pow_step<<<nblk(L.A.n), kT, 0, P.stream>>>(L.A.n, L.dinv, w, v);
+    k_norm_scale<<<1, kT, 0, P.stream>>>(m, v, nv);
+  }
+  double h = 0.0;
+  cudaMemcpyAsync(&h, nv, sizeof(double), cudaMemcpyDeviceToHost, P.stream);
+  cudaFreeAsync(v, P.stream);
+  cudaFreeAsync(w, P.stream);
+  cudaFreeAsync(nv, P.stream);
+  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  *out = 1.1 * h;
+  return SVXG_OK;
+}
+
+// Chebyshev coefficients on [lmax / ratio, lmax] (Saad, Iterative Methods, Alg. 12.1)
+struct Cheb {
+  float inv_theta;
+  float c1[16], c2[16];
+};
+
+Cheb chebyshev(double lmax, double ratio, int degree) {
+  Cheb C{};
+  const double lmin = lmax / ratio;
+  const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
+  const double sigma = theta / delta;
+  double rho = 1.0 / sigma;
+  C.inv_theta = float(1.0 / theta);
+  for (int i = 1; i < degree && i < 16; ++i) {
+    const double rn = 1.0 / (2.0 * sigma - rho);
+    C.c1[i] = float(rn * rho);
+    C.c2[i] = float(2.0 * rn / delta);
+    rho = rn;
+  }
+  return C;
+}
+
+// Chebyshev smoothing of A x = b. from_zero: x = p(D^-1 A) D^-1 b; else x += p(D^-1 A) D^-1 (b - A x).
+// Leaves r = b - A x (from_zero, want_residual) for the restriction.
+int smooth(Problem& P, const Level& L, const float* b, float* x, bool from_zero, int degree, double ratio,
+           bool want_residual) {
+  cudaStream_t st = P.stream;
+  const int32_t n = L.A.n;
+  const Cheb C = chebyshev(L.cheb_lmax, ratio, degree);
+  float* d0 = L.t32;
+  float* d1 = L.u32;
+  StepArgs s{};
+  s.D = L.dinv32;
+  if (from_zero) {
+    k_cheb_first<<<nblk(n), kT, 0, st>>>(n, L.dinv32, b, C.inv_theta, d0);
+    s.rin = b;
+  } else {
+    s.rin = b;
+    s.r = L.r32;
+    s.dout = d0;
+    s.c2 = C.inv_theta;
+    k_bsr32<kPostStart><<<rblk(n), kT, 0, st>>>(n, L.A.rowptr, L.A.col, L.A.val32, x, nullptr, s);
+    s.rin = L.r32;
+  }
+  for (int i = 1; i < degree; ++i) {
+    s.r = L.r32;
+    s.dout = d1;
+    s.x = x;
+    s.c1 = C.c1[i];
+    s.c2 = C.c2[i];
+    s.x_init = (from_zero && i == 1) ? 1 : 0;
+    s.x_last = (i == degree - 1 && !(from_zero && want_residual)) ? 1 : 0;
+    k_bsr32<kStep><<<rblk(n), kT, 0, st>>>(n, L.A.rowptr, L.A.col, L.A.val32, d0, nullptr, s);
+    s.rin = L.r32;
+    std::swap(d0, d1);
+  }
+  if (from_zero && want_residual) {
+    // r = r - A d; x += d (the last direction)
+    s.r = L.r32;
+    s.x = x;
+    if (degree == 1) {
+      SVXG_CUDA(cudaMemsetAsync(x, 0, sizeof(float) * 6 * size_t(n), st));
+    }
+    k_bsr32<kResPend><<<rblk(n), kT, 0, st>>>(n, L.A.rowptr, L.A.col, L.A.val32, d0, nullptr, s);
+  } else if (degree == 1) {
+    if (from_zero) {
+      SVXG_CUDA(cudaMemcpyAsync(x, d0, sizeof(float) * 6 * size_t(n), cudaMemcpyDeviceToDevice, st));
+    } else {
+      k_add<<<nblk(6 * int64_t(n)), kT, 0, st>>>(6 * int64_t(n), d0, x);
+    }
+  }
+  return SVXG_OK;
+}
+
+int cycle(Problem& P, size_t l, const float* b, float* x) {
+  cudaStream_t st = P.stream;
+  const Level& L = P.lv[l];
+  const int32_t n = L.A.n;
+  if (l + 1 == P.lv.size()) {
+    if (P.chol_n > 0) {
+      const int32_t m = P.chol_n;
+      k_dense_mv<<<rblk(m), kT, 0, st>>>(m, P.d_cinv, b, nullptr, P.d_cvec, nullptr);
+      k_dense_mv<<<rblk(m), kT, 0, st>>>(m, P.d_cinv + int64_t(m) * m, nullptr, P.d_cvec, nullptr, x);
+      return SVXG_OK;
+    }
+    return smooth(P, L, b, x, true, kCoarseDegree, 30.0, false);
+  }
+  TRY(smooth(P, L, b, x, true, kChebDegree, kChebRatio, true));
+  const Level& C = P.lv[l + 1];
+  StepArgs none{};
+  // restriction: bc = P^T r
+  k_bsr32<kY><<<rblk(C.A.n), kT, 0, st>>>(C.A.n, L.rrow, L.rent_i, L.pval32 + 36 * L.pnnz, L.r32, C.b32, none);
+  TRY(cycle(P, l + 1, C.b32, C.x32));
+  // prolongation: x += P xc
+  k_bsr32<kAcc><<<rblk(n), kT, 0, st>>>(n, L.prow, L.pcol, L.pval32, C.x32, x, none);
+  TRY(smooth(P, L, b, x, false, kChebDegree, kChebRatio, false));
+  return SVXG_OK;
+}
+
+}  // namespace
+
+int prepare_cycle(Problem& P) {
+  cudaStream_t st = P.stream;
+  for (size_t l = 0; l < P.lv.size(); ++l) {
+    Level& L = P.lv[l];
+    const int32_t n = L.A.n;
+    if (!L.A.val32) {
+      TRY(P.mem.alloc(&L.A.val32, 36 * size_t(L.A.nnzb)));
+      k_cvt<<<nblk(36 * L.A.nnzb), kT, 0, st>>>(36 * L.A.nnzb, L.A.val, L.A.val32);
+      if (l == 0) P.K.val32 = L.A.val32;
+    }
+    TRY(P.mem.alloc(&L.dinv32, 36 * size_t(n)));
+    k_cvt<<<nblk(36 * int64_t(n)), kT, 0, st>>>(36 * int64_t(n), L.dinv, L.dinv32);
+    if (L.pnnz > 0 && l + 1 < P.lv.size()) {
+      // P blocks by fine row, then P^T blocks in restriction order
+      TRY(P.mem.alloc(&L.pval32, 72 * size_t(L.pnnz)));
+      k_cvt<<<nblk(36 * L.pnnz), kT, 0, st>>>(36 * L.pnnz, L.pval, L.pval32);
+      k_cvt_transpose<<<nblk(L.pnnz), kT, 0, st>>>(L.pnnz, L.rent_e, L.pval, L.pval32 + 36 * L.pnnz);
+    }
+    for (float** v : {&L.b32, &L.x32, &L.r32, &L.t32, &L.u32}) TRY(P.mem.alloc(v, 6 * size_t(std::max(n, 1))));
+    const bool last = l + 1 == P.lv.size();
+    if (!last || P.chol_n == 0) {
+      if (L.lmax > 0) L.cheb_lmax = L.lmax;
+      else TRY(power_bound(P, L, &L.cheb_lmax));
+    }
+  }
+  if (P.chol_n > 0) {
+    const int32_t m = P.chol_n;
+    TRY(P.mem.alloc(&P.d_cinv, 2 * size_t(m) * size_t(m)));
+    TRY(P.mem.alloc(&P.d_cvec, 2 * size_t(m)));
+    k_tri_inverse<<<nblk(m, 64), 64, 0, st>>>(m, P.d_chol, P.d_cinv, P.d_cinv + int64_t(m) * m);
+  }
+  SVXG_CUDA(cudaGetLastError());
+  return SVXG_OK;
+}
+
+// z = M^-1 r: one V-cycle from zero (Amg::apply)
+int vcycle(Problem& P, const double* r, double* z) {
+  if (P.lv.empty()) return SVXG_OK;
+  cudaStream_t st = P.stream;
+  Level& L0 = P.lv[0];
+  const int64_t m = 6 * int64_t(L0.A.n);
+  k_cvt<<<nblk(m), kT, 0, st>>>(m, r, L0.b32);
+  TRY(cycle(P, 0, L0.b32, L0.x32));
+  k_widen<<<nblk(m), kT, 0, st>>>(m, L0.x32, z);
+  SVXG_CUDA(cudaGetLastError());
+  return SVXG_OK;
+}
+
+}  // namespace svxg

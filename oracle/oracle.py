@@ -21,7 +21,8 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 import build_oracle  # noqa: E402
-from opus_destruct_2_gb300.graph import (LOAD_DTYPE, PcgResult, StressOptions, ptr)  # noqa: E402
+from opus_destruct_2_gb300.graph import (BOND_DTYPE, LOAD_DTYPE, MATERIAL_DTYPE, NODE_DTYPE, PcgResult,  # noqa: E402
+                                         StressOptions, ptr)
 
 c_i32, c_i64, c_f64, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p
 
@@ -119,6 +120,15 @@ def set_threads(n: int) -> None:
         r.svxr_set_threads(int(n))
 
 
+def records(nodes, bonds, mats):
+    """The C record layouts (converted field by field when a caller's arrays are packed)."""
+    n = np.array(nodes, dtype=NODE_DTYPE)
+    b = np.array(bonds, dtype=BOND_DTYPE)
+    m = np.array(mats, dtype=MATERIAL_DTYPE)
+    assert n.dtype.itemsize == 40 and b.dtype.itemsize == 216 and m.dtype.itemsize == 64 and len(m) == 127
+    return n, b, m
+
+
 class Level:
     """One multigrid level in double precision (A, D^-1, aggregates, prolongation)."""
 
@@ -145,9 +155,7 @@ class Port:
 
     def __init__(self, nodes: np.ndarray, bonds: np.ndarray, mats: np.ndarray):
         self.lib = port_lib()
-        self.nodes = np.ascontiguousarray(nodes)
-        self.bonds = np.ascontiguousarray(bonds)
-        self.mats = np.ascontiguousarray(mats)
+        self.nodes, self.bonds, self.mats = records(nodes, bonds, mats)
         self.h = self.lib.svxo_create(ptr(self.nodes), len(nodes), ptr(self.bonds), len(bonds), ptr(self.mats))
 
     def __del__(self):
@@ -259,9 +267,7 @@ class Reference:
         self.lib = reference_lib()
         if self.lib is None:
             raise RuntimeError("the reference is not built on this machine")
-        self.nodes = np.ascontiguousarray(nodes)
-        self.bonds = np.array(bonds)
-        self.mats = np.ascontiguousarray(mats)
+        self.nodes, self.bonds, self.mats = records(nodes, bonds, mats)
 
     def solve(self, f, opt: StressOptions | None = None, u=None, rtol=1e-8, maxit=500, warm=False):
         n = len(self.nodes)

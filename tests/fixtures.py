@@ -68,7 +68,10 @@ def cantilever(n: int, L: float, mass: float):
 
 
 def add_bond(nodes, bonds, A, B, n, p, a):
-    return np.concatenate([bonds, _bonds([bond_record(nodes, A, B, n, p, a)])])
+    out = empty_bonds(len(bonds) + 1)  # (np.concatenate would pack the padded record layout)
+    out[:-1] = bonds
+    out[-1] = bond_record(nodes, A, B, n, p, a)
+    return out
 
 
 def gravity(nodes):
