@@ -1,0 +1,378 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 stress solve on the city-block workload.
+
+One step = one complete stress solve of a structure: K assembled from the bonds, the aggregation
+multigrid built, AMG-preconditioned CG to ||r|| <= rtol ||f|| (cold start), and every bond's
+fibre-stress check with the failure set (the reference's assemble + solve + judge of
+core/src/stress/stress.cpp). The workload is the city block: seeded random towers of 5-40 storeys
+of 0.5 m voxels in four materials (concrete, steel, masonry, wood, each +-20 %), pre-scored into
+fragments; gravity loads; FP64 PCG to rtol 1e-8.
+
+  value   solves/s with the graph resident on the device (device f / u / outputs)
+  e2e     solves/s through the C ABI with host buffers: graph upload, f in, u, phi, modes and
+          the failure list out, every step
+  roofline  the conjugate-gradient SpMV (FP64 K), timed live with CUDA events on the problem's
+          stream over the timed region, against the measured HBM copy bandwidth
+  cpu_baseline  the oracle (a C restatement of the reference's solve, OpenMP) on the host's cores,
+          one solve of the same graph
+
+Launch: python bench.py [--gpus N --steps K --warmup W] (N > 1 under torchrun: one replica per
+GPU, each solving its own seeded city block; value = all ranks' solves / the slowest rank's time).
+--impl reference times the reference's CPU implementation of the path (the oracle port on every
+host thread) on the same workload and prints the same JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (ROOT, os.path.join(ROOT, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "stress solves/sec & p99 latency at rel.resid 1e-6 vs plain FP64 PCG, 1 GB300"
+L2_BYTES = 129 * 2**20
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def measured_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def workload(args, rank: int):
+    from opus_destruct_2_gb300 import synth
+    if args.workload == "city":
+        nodes, bonds, f, mats = synth.city_graph(lots_x=args.lots, lots_y=args.lots, seed=args.seed + rank)
+        desc = (f"city block: {args.lots}x{args.lots} seeded towers of 5-40 storeys, 0.5 m voxels, concrete/steel/"
+                f"masonry/wood +-20%")
+    else:
+        nodes, bonds, f, mats = synth.tower_graph(storeys=10, seed=args.seed + rank)
+        desc = "tower: 10 storeys, 8 x 8 m plan, 0.5 m voxels, concrete E = 30 GPa"
+    return nodes, bonds, f, mats, desc
+
+
+class Clocks:
+    """nvidia-smi samples (200 ms) during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(index)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def run_reference(args, rank: int, world: int):
+    """The reference's CPU implementation of the path: the oracle port, every host thread."""
+    if rank != 0:
+        return
+    import oracle
+    from opus_destruct_2_gb300.graph import StressOptions
+    nodes, bonds, f, mats, desc = workload(args, 0)
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    times = []
+    iters = 0
+    for step in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        P = oracle.Port(nodes, bonds, mats)
+        P.assemble(StressOptions(amg_min_nodes=160))
+        u, res = P.solve(f, rtol=args.rtol, maxit=args.maxit)
+        P.judge(u)
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            times.append(dt)
+        iters = res.iters
+    total = sum(times)
+    value = len(times) / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": desc, "nodes": int(len(nodes)), "bonds": int(len(bonds)), "rtol": args.rtol,
+                   "pcg_iters": int(iters)},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": "each step: one full solve (assemble + multigrid build + PCG + judge) of the "
+                                   "workload graph by the oracle's C restatement of the reference (the reference "
+                                   "tree is not on this machine)"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "p50_ms": 1e3 * float(np.percentile(times, 50)), "p99_ms": 1e3 * float(np.percentile(times, 99)),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(args, nodes, bonds, f, mats) -> dict:
+    import oracle
+    from opus_destruct_2_gb300.graph import StressOptions
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    t0 = time.perf_counter()
+    P = oracle.Port(nodes, bonds, mats)
+    P.assemble(StressOptions(amg_min_nodes=160))
+    u, res = P.solve(f, rtol=args.rtol, maxit=args.maxit)
+    P.judge(u)
+    dt = time.perf_counter() - t0
+    return {"value": 1.0 / dt, "unit": "solves/s", "cores": threads, "kind": "port",
+            "sample": f"one full solve (assemble + multigrid build + PCG to rtol {args.rtol:g} + judge) of the "
+                      f"workload graph by the oracle's C restatement of the reference; {dt:.2f} s, "
+                      f"{res.iters} PCG iterations"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["city", "tower"], default="city")
+    ap.add_argument("--lots", type=int, default=8)
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--rtol", type=float, default=1e-8)
+    ap.add_argument("--maxit", type=int, default=500)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+
+    from opus_destruct_2_gb300 import load_library
+    from opus_destruct_2_gb300.graph import PcgResult, StressOptions, ptr
+
+    L = load_library()
+    L.svxg_launch_count.restype = ctypes.c_int64
+    L.svxg_timer_enable.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+    L.svxg_timer_read.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)]
+    L.svxg_utilization_device.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]
+
+    def check(code):
+        if code < 0:
+            raise RuntimeError(f"svxg error {code}: {L.svxg_last_error().decode()}")
+
+    nodes, bonds, f, mats, desc = workload(args, rank)
+    n, nb = len(nodes), len(bonds)
+    dev = torch.device("cuda", local_rank)
+    h = ctypes.c_void_p()
+    check(L.svxg_problem_create(ctypes.byref(h), local_rank))
+    stream = torch.cuda.ExternalStream(L.svxg_problem_stream(h), device=dev)
+    opt = StressOptions(amg_min_nodes=160)
+    ok = ctypes.c_int32()
+    res = PcgResult()
+    n_over = ctypes.c_int32()
+
+    # device-resident inputs and outputs
+    f_dev = torch.from_numpy(f).to(dev)
+    u_dev = torch.zeros(6 * n, dtype=torch.float64, device=dev)
+    phi_dev = torch.zeros(max(nb, 1), dtype=torch.float64, device=dev)
+    mode_dev = torch.zeros(max(nb, 1), dtype=torch.uint8, device=dev)
+    over_dev = torch.zeros(max(nb, 1), dtype=torch.int32, device=dev)
+    torch.cuda.synchronize()
+    check(L.svxg_set_graph(h, ptr(nodes), n, ptr(bonds), nb, ptr(mats)))
+
+    phases = {"assemble": [], "solve": [], "judge": []}
+
+    def step_device(record=False):
+        t0 = time.perf_counter()
+        check(L.svxg_assemble(h, ctypes.byref(opt), ctypes.byref(ok)))
+        if not ok.value:
+            raise RuntimeError("assemble: singular")
+        t1 = time.perf_counter()
+        check(L.svxg_solve_device(h, ctypes.c_void_p(f_dev.data_ptr()), ctypes.c_void_p(u_dev.data_ptr()), args.rtol,
+                                  args.maxit, 0, ctypes.byref(res)))
+        t2 = time.perf_counter()
+        check(L.svxg_utilization_device(h, 1.0, ctypes.c_void_p(phi_dev.data_ptr()),
+                                        ctypes.c_void_p(mode_dev.data_ptr()), ctypes.c_void_p(over_dev.data_ptr()),
+                                        ctypes.byref(n_over)))
+        torch.cuda.current_stream(dev).synchronize()
+        stream.synchronize()
+        t3 = time.perf_counter()
+        if record:
+            phases["assemble"].append(t1 - t0)
+            phases["solve"].append(t2 - t1)
+            phases["judge"].append(t3 - t2)
+        return t3 - t0
+
+    # host-buffer path (the e2e leg)
+    u_host = np.zeros(6 * n)
+    phi_host = np.zeros(max(nb, 1))
+    mode_host = np.zeros(max(nb, 1), np.uint8)
+    over_host = np.zeros(max(nb, 1), np.int32)
+
+    def step_host():
+        check(L.svxg_set_graph(h, ptr(nodes), n, ptr(bonds), nb, ptr(mats)))
+        check(L.svxg_assemble(h, ctypes.byref(opt), ctypes.byref(ok)))
+        check(L.svxg_solve(h, ptr(f), ptr(u_host), args.rtol, args.maxit, 0, ctypes.byref(res)))
+        check(L.svxg_utilization(h, 1.0, ptr(phi_host), ptr(mode_host), ptr(over_host), len(over_host),
+                                 ctypes.byref(n_over)))
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step_device()
+    # --- timed: device-resident ---
+    barrier()
+    clocks = Clocks(local_rank)
+    launches0 = L.svxg_launch_count()
+    L.svxg_timer_enable(h, 1)
+    tm, tl = ctypes.c_double(), ctypes.c_int64()
+    L.svxg_timer_read(h, ctypes.byref(tm), ctypes.byref(tl))  # (reset)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    lat = []
+    for _ in range(args.steps):
+        lat.append(step_device(record=True))
+    ev1.record(stream)
+    barrier()
+    elapsed = ev0.elapsed_time(ev1) / 1e3
+    launches = L.svxg_launch_count() - launches0
+    L.svxg_timer_read(h, ctypes.byref(tm), ctypes.byref(tl))
+    L.svxg_timer_enable(h, 0)
+    clk = clocks.stop()
+    iters = res.iters
+    info_fail = n_over.value
+    if dist is not None:
+        t = torch.tensor([elapsed], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    # --- timed: end to end through the C ABI with host buffers ---
+    step_host()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_host()
+    barrier()
+    e2e_elapsed = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_elapsed], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_elapsed = float(t.item())
+
+    from opus_destruct_2_gb300 import Info
+    info = Info()
+    check(L.svxg_get_info(h, ctypes.byref(info)))
+    nfree, nnzb = info.nfree, info.matrix_blocks
+    spmv_bytes = nnzb * (36 * 8 + 4) + nfree * (4 + 6 * 8 + 6 * 8)
+    peaks = measured_peaks()
+    achieved = (spmv_bytes * tl.value / (tm.value / 1e3) / 1e9) if tm.value > 0 else 0.0
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "spmv_traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as fh:
+            tj = json.load(fh)
+        if tj.get("nnzb") and tj.get("dram_bytes_per_launch"):
+            traffic = float(tj["dram_bytes_per_launch"]) * nnzb / float(tj["nnzb"])
+
+    if rank != 0:
+        return
+    h2d = nodes.nbytes + bonds.nbytes + mats.nbytes + f.nbytes
+    d2h = u_host.nbytes + 8 * nb + nb + 4 * info_fail
+    value = world * args.steps / elapsed
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "solves/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * elapsed / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": desc, "nodes": int(n), "bonds": int(nb), "dof": int(6 * nfree), "blocks": int(nnzb),
+                   "levels": info.sizes(), "rtol": args.rtol, "pcg_iters": int(iters), "failing_bonds": int(info_fail),
+                   "precision": "fp64 K and CG, f32 V-cycle", "step": "assemble + multigrid build + PCG + judge",
+                   "l2": "inputs larger than L2 (K alone is %.0f MB)" % (nnzb * 288 / 1e6),
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"kernel": "conjugate-gradient SpMV (FP64 BSR 6x6, p.q fused)", "bound": "hbm",
+                     "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"] if peaks["hbm_gbs"] else None,
+                     "peak_source": peaks["source"], "traffic": traffic,
+                     "algorithmic_bytes_per_launch": int(spmv_bytes), "launches": int(tl.value),
+                     "avg_us": 1e3 * tm.value / max(tl.value, 1)},
+        "e2e": {"value": world * args.steps / e2e_elapsed, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+        "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+        "phase_ms": {k: 1e3 * float(np.mean(v)) for k, v in phases.items() if v},
+    }
+    if clk is not None:
+        line["clocks"] = clk
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args, nodes, bonds, f, mats)
+    print(json.dumps(line), flush=True)
+    L.svxg_problem_destroy(h)
+
+
+if __name__ == "__main__":
+    main()

@@ -106,8 +106,19 @@ int svxg_bond_loads(svxg_problem* p, const double* u, svxg_bond_load* out);
 int svxg_utilization(svxg_problem* p, double fragility, double* phi, uint8_t* mode, int32_t* over, int32_t cap,
                      int32_t* n_over);
 
+/* The same at the current solution with device outputs (phi: nb doubles, mode: nb bytes, over:
+ * nb int32 - any may be null); *n_over (host) receives the failure count. */
+int svxg_utilization_device(svxg_problem* p, double fragility, double* phi_dev, uint8_t* mode_dev, int32_t* over_dev,
+                            int32_t* n_over);
+
 /* --- counters ------------------------------------------------------------------------------- */
 int svxg_get_info(svxg_problem* p, svxg_info* info);
+/* Kernel launches made by this library since it was loaded (all problems, all threads). */
+int64_t svxg_launch_count(void);
+/* Live timing of the conjugate-gradient SpMV: CUDA events on the problem's stream around each of
+ * its launches while enabled; read returns their summed duration (ms) and count, and resets. */
+int svxg_timer_enable(svxg_problem* p, int32_t on);
+int svxg_timer_read(svxg_problem* p, double* ms_total, int64_t* launches);
 
 /* --- parity access (tests) ------------------------------------------------------------------ */
 /* K as assembled: call with null arrays for *nfree / *nnzb, then with arrays of those sizes. */
@@ -119,6 +130,9 @@ int svxg_debug_level(svxg_problem* p, int32_t level, int32_t* rowptr, int32_t* c
                      int32_t* parent, int32_t* prow, int32_t* pcol, double* pval, double* pos, double* lmax);
 /* z = M^-1 r and y = K x over the free DOFs (host arrays of 6 nfree). */
 int svxg_debug_precondition(svxg_problem* p, const double* r, double* z);
+/* sqrt of ((0 + v0^2) + v1^2) + ... summed in index order, computed in parallel on the device
+ * (the multigrid setup's exact norm): for checking it against a sequential host loop. */
+int svxg_debug_seq_norm(const double* v, int64_t n, double* out);
 int svxg_debug_apply(svxg_problem* p, const double* x, double* y);
 
 #ifdef __cplusplus

@@ -4,6 +4,7 @@
 // is kept on the host as well so that remove_bond / retire_nodes can pick their bonds and rows
 // as the reference does; every number is computed on the device.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -101,6 +102,11 @@ int upload_bond_flags(Problem& P, int32_t b) {
 
 void set_error(const std::string& msg) { g_error = msg; }
 
+namespace {
+std::atomic<int64_t> g_launches{0};
+}
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
 }  // namespace svxg
 
 using namespace svxg;
@@ -108,6 +114,31 @@ using namespace svxg;
 extern "C" {
 
 const char* svxg_last_error(void) { return g_error.c_str(); }
+
+int64_t svxg_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int svxg_timer_enable(svxg_problem* p, int32_t on) {
+  CHECK_P(p);
+  p->P.timer_on = on != 0;
+  return SVXG_OK;
+}
+
+int svxg_timer_read(svxg_problem* p, double* ms_total, int64_t* launches) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  DeviceScope ds(P.device);
+  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  double tot = 0.0;
+  for (size_t k = 0; k + 1 < 2 * P.timer_used + 1 && k / 2 < P.timer_used; k += 2) {
+    float ms = 0.0f;
+    SVXG_CUDA(cudaEventElapsedTime(&ms, P.timer_events[k], P.timer_events[k + 1]));
+    tot += ms;
+  }
+  if (ms_total) *ms_total = tot;
+  if (launches) *launches = int64_t(P.timer_used);
+  P.timer_used = 0;
+  return SVXG_OK;
+}
 
 int svxg_device_count(void) {
   int n = 0;
@@ -145,6 +176,7 @@ void svxg_problem_destroy(svxg_problem* p) {
   DeviceScope ds(p->P.device);
   cudaStreamSynchronize(p->P.stream);
   p->P.mem.release_all();
+  for (cudaEvent_t e : p->P.timer_events) cudaEventDestroy(e);
   if (p->P.h_s) cudaFreeHost(p->P.h_s);
   cudaStreamDestroy(p->P.stream);
   delete p;
@@ -512,6 +544,21 @@ int svxg_utilization(svxg_problem* p, double fragility, double* phi, uint8_t* mo
   return e;
 }
 
+int svxg_utilization_device(svxg_problem* p, double fragility, double* phi_dev, uint8_t* mode_dev, int32_t* over_dev,
+                            int32_t* n_over) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  DeviceScope ds(P.device);
+  TRY(ensure_node_vectors(P));
+  const size_t m = 6 * size_t(P.n);
+  if (P.d_x && P.assembled) {
+    TRY(gather_solution(P, P.d_un));
+  } else {
+    SVXG_CUDA(cudaMemsetAsync(P.d_un, 0, m * sizeof(double), P.stream));
+  }
+  return utilization_device(P, P.d_un, fragility, phi_dev, mode_dev, over_dev, n_over);
+}
+
 int svxg_get_info(svxg_problem* p, svxg_info* info) {
   CHECK_P(p);
   if (!info) return SVXG_ERR_ARG;
@@ -588,6 +635,17 @@ int svxg_debug_level(svxg_problem* p, int32_t level, int32_t* rowptr, int32_t* c
   TRY(get(pos, L.pos, sizeof(double) * 3 * n));
   if (lmax) *lmax = L.lmax;
   return SVXG_OK;
+}
+
+int svxg_debug_seq_norm(const double* v, int64_t n, double* out) {
+  if (n < 0 || (n > 0 && !v) || !out) return SVXG_ERR_ARG;
+  double* d = nullptr;
+  SVXG_CUDA(cudaMalloc(&d, sizeof(double) * size_t(n + 1)));
+  cudaMemcpy(d, v, sizeof(double) * size_t(n), cudaMemcpyHostToDevice);
+  int e = debug_seq_norm(0, d, n, d + n);
+  if (!e) e = cudaMemcpy(out, d + n, sizeof(double), cudaMemcpyDeviceToHost) == cudaSuccess ? SVXG_OK : SVXG_ERR_CUDA;
+  cudaFree(d);
+  return e;
 }
 
 int svxg_debug_apply(svxg_problem* p, const double* x, double* y) {

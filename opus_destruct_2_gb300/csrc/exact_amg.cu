@@ -22,6 +22,7 @@
 #include <cmath>
 
 #include "blk6.cuh"
+#include "exact_sum.cuh"
 #include "problem.cuh"
 
 namespace svxg {
@@ -94,23 +95,15 @@ __global__ void k_dinv_apply(int32_t n, const double* dinv, const double* w, dou
   if (i < n) mv6(dinv + 36 * int64_t(i), w + 6 * int64_t(i), v + 6 * int64_t(i));
 }
 
-// nv = sqrt(sum of v_k^2 in index order); one warp: lanes square, lane 0 adds in order.
-// lam <- nv and v /= nv happen in k_lmax_scale; a zero or non-finite norm stops the iteration.
-__global__ void k_seq_norm(int64_t m, const double* v, double* out) {
-  __shared__ double sq[32];
-  const int lane = threadIdx.x;
-  double s = 0.0;
-  for (int64_t b = 0; b < m; b += 32) {
-    const int64_t k = b + lane;
-    sq[lane] = k < m ? v[k] * v[k] : 0.0;
-    __syncwarp();
-    if (lane == 0) {
-      const int cnt = int(std::min<int64_t>(32, m - b));
-      for (int q = 0; q < cnt; ++q) s += sq[q];
-    }
-    __syncwarp();
-  }
-  if (lane == 0) out[0] = sqrt(s);
+// nv = sqrt(sum of v_k^2 in index order): the sequential sum's exact bits, computed in parallel
+// (exact_sum.cuh). lam <- nv and v /= nv happen in k_lmax_step / k_lmax_scale; a zero or
+// non-finite norm stops the iteration.
+__global__ void __launch_bounds__(exact::kThreads) k_seq_norm(int64_t m, const double* v, double* out) {
+  const double s = exact::sequential_sum(m, [v](int64_t k) {
+    const double x = v[k];
+    return x * x;
+  });
+  if (threadIdx.x == 0) out[0] = sqrt(s);
 }
 
 // state: [0] = lam, [1] = nv, [2] = stopped
@@ -465,16 +458,28 @@ __global__ void k_ap_count(int32_t n, const int32_t* rowptr, const int32_t* col,
   aplen[i] = m;
 }
 
+// (one warp per row: lane l owns entries l and, for l < 4, 32 + l of every 6x6 product; each
+// entry is summed over q in order and added to its block as mul6_add does - the same additions)
+__device__ __forceinline__ void warp_mul6_add(bool trans, const double* __restrict__ A, const double* __restrict__ B,
+                                              double* C, int lane) {
+  for (int ent = lane; ent < 36; ent += 32) {
+    const int r = ent / 6, c = ent - 6 * (ent / 6);
+    double s = 0.0;
+    for (int q = 0; q < 6; ++q) s += (trans ? A[q * 6 + r] : A[r * 6 + q]) * B[q * 6 + c];
+    C[ent] = C[ent] + s;
+  }
+}
+
 __global__ void k_ap_values(int32_t n, const int32_t* rowptr, const int32_t* col, const double* val,
                             const int32_t* prow, const int32_t* pcol, const double* pval, const int32_t* aprow,
                             const int32_t* scratch, const int64_t* soff, int32_t* apcol, double* apval) {
-  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int32_t i = int32_t((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
   if (i >= n) return;
   const int32_t e0 = aprow[i], e1 = aprow[i + 1];
-  for (int32_t e = e0; e < e1; ++e) {
-    apcol[e] = scratch[soff[i] + (e - e0)];
-    for (int q = 0; q < 36; ++q) apval[36 * int64_t(e) + q] = 0.0;
-  }
+  for (int32_t e = e0 + lane; e < e1; e += 32) apcol[e] = scratch[soff[i] + (e - e0)];
+  for (int64_t q = 36 * int64_t(e0) + lane; q < 36 * int64_t(e1); q += 32) apval[q] = 0.0;
+  __syncwarp();
   for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
     const int32_t j = col[k];
     const double* Aij = val + 36 * int64_t(k);
@@ -486,7 +491,8 @@ __global__ void k_ap_values(int32_t n, const int32_t* rowptr, const int32_t* col
         if (apcol[mid] < c) lo = mid + 1;
         else hi = mid;
       }
-      mul6_add<false>(Aij, pval + 36 * int64_t(e), apval + 36 * int64_t(lo));
+      warp_mul6_add(false, Aij, pval + 36 * int64_t(e), apval + 36 * int64_t(lo), lane);
+      __syncwarp();
     }
   }
 }
@@ -539,13 +545,13 @@ __global__ void k_c_values(int32_t na, const int32_t* rrow, const int32_t* rent_
                            const double* pval, const int32_t* aprow, const int32_t* apcol, const double* apval,
                            const int32_t* crow, const int32_t* scratch, const int64_t* soff, int32_t* ccol,
                            double* cval, double scale) {
-  const int32_t I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int32_t I = int32_t((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
   if (I >= na) return;
   const int32_t c0 = crow[I], c1 = crow[I + 1];
-  for (int32_t c = c0; c < c1; ++c) {
-    ccol[c] = scratch[soff[I] + (c - c0)];
-    for (int q = 0; q < 36; ++q) cval[36 * int64_t(c) + q] = 0.0;
-  }
+  for (int32_t c = c0 + lane; c < c1; c += 32) ccol[c] = scratch[soff[I] + (c - c0)];
+  for (int64_t q = 36 * int64_t(c0) + lane; q < 36 * int64_t(c1); q += 32) cval[q] = 0.0;
+  __syncwarp();
   for (int32_t r = rrow[I]; r < rrow[I + 1]; ++r) {
     const int32_t i = rent_i[r];
     const double* Pi = pval + 36 * int64_t(rent_e[r]);
@@ -563,12 +569,12 @@ __global__ void k_c_values(int32_t na, const int32_t* rrow, const int32_t* rent_
         }
         slot = lo;
       }
-      mul6_add<true>(Pi, apval + 36 * int64_t(e), cval + 36 * int64_t(slot));
+      warp_mul6_add(true, Pi, apval + 36 * int64_t(e), cval + 36 * int64_t(slot), lane);
+      __syncwarp();
     }
   }
   if (scale != 1.0)
-    for (int32_t c = c0; c < c1; ++c)
-      for (int q = 0; q < 36; ++q) cval[36 * int64_t(c) + q] *= scale;
+    for (int64_t q = 36 * int64_t(c0) + lane; q < 36 * int64_t(c1); q += 32) cval[q] *= scale;
 }
 
 // per-row scratch offsets: sum over a row's products of the candidate counts (an upper bound)
@@ -589,15 +595,9 @@ __global__ void k_c_bound(int32_t na, const int32_t* rrow, const int32_t* rent_i
   bound[I] = b;
 }
 
-__global__ void k_i64_offsets(int32_t n, const int32_t* bound, int64_t* off) {
-  // (sequential: small arrays of per-row bounds; one thread)
-  if (blockIdx.x || threadIdx.x) return;
-  int64_t s = 0;
-  for (int32_t i = 0; i < n; ++i) {
-    off[i] = s;
-    s += bound[i];
-  }
-  off[n] = s;
+__global__ void k_widen_offsets(int32_t n, const int32_t* scan32, int64_t* off) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i <= n) off[i] = int64_t(scan32[i]);
 }
 
 // ---- the coarsest level's dense factor (amg.cpp:535-578) ---------------------------------------
@@ -652,13 +652,30 @@ int copy_to_host(Problem& P, void* dst, const void* src, size_t bytes) {
   return SVXG_OK;
 }
 
+// offsets of per-row scratch regions: an exclusive scan of the n bounds (bound[n] = 0)
+int offsets64(Problem& P, const int32_t* bound, int32_t n, int64_t* off, int64_t* total) {
+  int32_t* scan32 = nullptr;
+  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scan32), sizeof(int32_t) * (size_t(n) + 1), P.stream));
+  int32_t t = 0;
+  int e = exclusive_scan_i32(P, bound, scan32, int64_t(n) + 1, &t);
+  if (!e) (k_widen_offsets<<<nblk(int64_t(n) + 1), kT, 0, P.stream>>>(n, scan32, off), SVXG_COUNT_LAUNCH());
+  cudaFreeAsync(scan32, P.stream);
+  if (e) return e;
+  if (t < 0) {
+    set_error("multigrid setup: product scratch beyond 2^31 entries");
+    return SVXG_ERR_NOMEM;
+  }
+  *total = t;
+  return SVXG_OK;
+}
+
 int finalize_level(Problem& P, Level& L, bool* ok) {
   *ok = false;
   TRY(P.mem.alloc(&L.dinv, size_t(L.A.n) * 36));
   Tmp<int32_t> fail(P.stream);
   TRY(fail.alloc(1));
   SVXG_CUDA(cudaMemsetAsync(fail.p, 0, sizeof(int32_t), P.stream));
-  if (L.A.n > 0) k_dinv<<<nblk(L.A.n), kT, 0, P.stream>>>(L.A.n, L.A.rowptr, L.A.val, L.dinv, fail.p);
+  if (L.A.n > 0) (k_dinv<<<nblk(L.A.n), kT, 0, P.stream>>>(L.A.n, L.A.rowptr, L.A.val, L.dinv, fail.p), SVXG_COUNT_LAUNCH());
   int32_t f = 0;
   TRY(copy_to_host(P, &f, fail.p, sizeof(int32_t)));
   P.amg_build_work += 12 * int64_t(L.A.n);
@@ -677,13 +694,13 @@ int estimate_lmax(Problem& P, const Level& L, double* out) {
   TRY(st.alloc(3));
   const double init[3] = {1.0, 0.0, 0.0};
   SVXG_CUDA(cudaMemcpyAsync(st.p, init, sizeof(init), cudaMemcpyHostToDevice, P.stream));
-  k_lmax_init<<<nblk(m), kT, 0, P.stream>>>(m, v.p);
+  (k_lmax_init<<<nblk(m), kT, 0, P.stream>>>(m, v.p), SVXG_COUNT_LAUNCH());
   for (int it = 0; it < 15; ++it) {
-    k_spmv_exact<<<nblk(m), kT, 0, P.stream>>>(n, L.A.rowptr, L.A.col, L.A.val, v.p, w.p);
-    k_dinv_apply<<<nblk(n), kT, 0, P.stream>>>(n, L.dinv, w.p, v.p);
-    k_seq_norm<<<1, 32, 0, P.stream>>>(m, v.p, st.p + 1);
-    k_lmax_step<<<1, 1, 0, P.stream>>>(st.p);
-    k_lmax_scale<<<nblk(m), kT, 0, P.stream>>>(m, v.p, st.p);
+    (k_spmv_exact<<<nblk(m), kT, 0, P.stream>>>(n, L.A.rowptr, L.A.col, L.A.val, v.p, w.p), SVXG_COUNT_LAUNCH());
+    (k_dinv_apply<<<nblk(n), kT, 0, P.stream>>>(n, L.dinv, w.p, v.p), SVXG_COUNT_LAUNCH());
+    (k_seq_norm<<<1, exact::kThreads, 0, P.stream>>>(m, v.p, st.p + 1), SVXG_COUNT_LAUNCH());
+    (k_lmax_step<<<1, 1, 0, P.stream>>>(st.p), SVXG_COUNT_LAUNCH());
+    (k_lmax_scale<<<nblk(m), kT, 0, P.stream>>>(m, v.p, st.p), SVXG_COUNT_LAUNCH());
   }
   SVXG_CUDA(cudaGetLastError());
   double h[3];
@@ -727,36 +744,36 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
   TRY(P.mem.alloc(&agg, size_t(n)));
   {
     const Bsr& A = P.lv[l].A;
-    k_fro_blocks<<<nblk(nnzb), kT, 0, st>>>(nnzb, A.val, fro.p);
-    k_block_rows<<<nblk(n), kT, 0, st>>>(n, A.rowptr, brow.p);
+    (k_fro_blocks<<<nblk(nnzb), kT, 0, st>>>(nnzb, A.val, fro.p), SVXG_COUNT_LAUNCH());
+    (k_block_rows<<<nblk(n), kT, 0, st>>>(n, A.rowptr, brow.p), SVXG_COUNT_LAUNCH());
   }
   double theta = opt.strength;
   int32_t na = 0;
   for (int round = 0;; ++round) {
     const Bsr& A = P.lv[l].A;
-    k_strong<<<nblk(nnzb), kT, 0, st>>>(nnzb, brow.p, A.col, fro.p, A.rowptr, theta, strong.p);
-    k_mis_init<<<nblk(n), kT, 0, st>>>(n, A.rowptr, state.p, covered.p, claim.p);
+    (k_strong<<<nblk(nnzb), kT, 0, st>>>(nnzb, brow.p, A.col, fro.p, A.rowptr, theta, strong.p), SVXG_COUNT_LAUNCH());
+    (k_mis_init<<<nblk(n), kT, 0, st>>>(n, A.rowptr, state.p, covered.p, claim.p), SVXG_COUNT_LAUNCH());
     for (int guard = 0; guard <= n; ++guard) {
       SVXG_CUDA(cudaMemsetAsync(undecided.p, 0, sizeof(int32_t), st));
-      k_mis_claim<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, claim.p);
-      k_mis_decide<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, covered.p, claim.p, undecided.p);
-      k_mis_cover<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, covered.p, claim.p);
+      (k_mis_claim<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, claim.p), SVXG_COUNT_LAUNCH());
+      (k_mis_decide<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, covered.p, claim.p, undecided.p), SVXG_COUNT_LAUNCH());
+      (k_mis_cover<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, covered.p, claim.p), SVXG_COUNT_LAUNCH());
       int32_t u = 0;
       TRY(copy_to_host(P, &u, undecided.p, sizeof(int32_t)));
       if (u == 0) break;
     }
-    k_root_flags<<<nblk(n), kT, 0, st>>>(n, state.p, flag.p);
+    (k_root_flags<<<nblk(n), kT, 0, st>>>(n, state.p, flag.p), SVXG_COUNT_LAUNCH());
     int32_t na1 = 0;
     TRY(exclusive_scan_i32(P, flag.p, rank.p, n, &na1));
     SVXG_CUDA(cudaMemsetAsync(agg1.p, 0xff, sizeof(int32_t) * size_t(n), st));
-    k_agg_pass1<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, rank.p, agg1.p);
-    k_agg_pass2<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, fro.p, agg1.p, agg);
-    k_pass3_flags<<<nblk(n), kT, 0, st>>>(n, A.rowptr, agg, iso.p, noniso.p);
+    (k_agg_pass1<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, rank.p, agg1.p), SVXG_COUNT_LAUNCH());
+    (k_agg_pass2<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, fro.p, agg1.p, agg), SVXG_COUNT_LAUNCH());
+    (k_pass3_flags<<<nblk(n), kT, 0, st>>>(n, A.rowptr, agg, iso.p, noniso.p), SVXG_COUNT_LAUNCH());
     TRY(exclusive_scan_i32(P, iso.p, isorank.p, n, nullptr));
-    k_pass3_alloc<<<nblk(n), kT, 0, st>>>(n, iso.p, isorank.p, noniso.p, alloc.p, gfirst.p);
+    (k_pass3_alloc<<<nblk(n), kT, 0, st>>>(n, iso.p, isorank.p, noniso.p, alloc.p, gfirst.p), SVXG_COUNT_LAUNCH());
     int32_t nalloc = 0;
     TRY(exclusive_scan_i32(P, alloc.p, allocscan.p, n, &nalloc));
-    k_pass3_assign<<<nblk(n), kT, 0, st>>>(n, na1, iso.p, isorank.p, noniso.p, allocscan.p, gfirst.p, agg);
+    (k_pass3_assign<<<nblk(n), kT, 0, st>>>(n, na1, iso.p, isorank.p, noniso.p, allocscan.p, gfirst.p, agg), SVXG_COUNT_LAUNCH());
     SVXG_CUDA(cudaGetLastError());
     na = na1 + nalloc;
     if (!opt.reaggregate || round == 3 || 2 * int64_t(na) <= n) break;
@@ -780,15 +797,15 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     TRY(members.alloc(size_t(n)));
     SVXG_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * (size_t(na) + 1), st));
     SVXG_CUDA(cudaMemsetAsync(cursor.p, 0, sizeof(int32_t) * (size_t(na) + 1), st));
-    k_count_members<<<nblk(n), kT, 0, st>>>(n, agg, cnt.p);
+    (k_count_members<<<nblk(n), kT, 0, st>>>(n, agg, cnt.p), SVXG_COUNT_LAUNCH());
     TRY(exclusive_scan_i32(P, cnt.p, off.p, int64_t(na) + 1, nullptr));
-    k_fill_members<<<nblk(n), kT, 0, st>>>(n, agg, off.p, cursor.p, members.p);
+    (k_fill_members<<<nblk(n), kT, 0, st>>>(n, agg, off.p, cursor.p, members.p), SVXG_COUNT_LAUNCH());
     TRY(P.mem.alloc(&C.pos, 3 * size_t(na)));
-    k_coarse_pos<<<nblk(na), kT, 0, st>>>(na, off.p, members.p, F.pos, C.pos);
+    (k_coarse_pos<<<nblk(na), kT, 0, st>>>(na, off.p, members.p, F.pos, C.pos), SVXG_COUNT_LAUNCH());
   }
   Tmp<double> off3(st);
   TRY(off3.alloc(3 * size_t(n)));
-  k_offsets<<<nblk(n), kT, 0, st>>>(n, agg, F.pos, C.pos, off3.p);
+  (k_offsets<<<nblk(n), kT, 0, st>>>(n, agg, F.pos, C.pos, off3.p), SVXG_COUNT_LAUNCH());
   // prolongation
   double omega = 0.0;
   if (smoothed) {
@@ -803,22 +820,22 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     TRY(plen.alloc(size_t(n) + 1));
     TRY(scratch.alloc(size_t(nnzb) + size_t(n) + 1));
     SVXG_CUDA(cudaMemsetAsync(plen.p, 0, sizeof(int32_t) * (size_t(n) + 1), st));
-    k_p_count<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, agg, smoothed ? 1 : 0, plen.p, scratch.p, INT_MAX);
+    (k_p_count<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, agg, smoothed ? 1 : 0, plen.p, scratch.p, INT_MAX), SVXG_COUNT_LAUNCH());
     TRY(P.mem.alloc(&F.prow, size_t(n) + 1));
     int32_t pnnz = 0;
     TRY(exclusive_scan_i32(P, plen.p, F.prow, int64_t(n) + 1, &pnnz));
     F.pnnz = pnnz;
     TRY(P.mem.alloc(&F.pcol, size_t(pnnz)));
     TRY(P.mem.alloc(&F.pval, size_t(pnnz) * 36));
-    k_p_values<<<nblk(n, 128), 128, 0, st>>>(n, A.rowptr, A.col, A.val, agg, off3.p, F.dinv, omega, F.prow,
-                                              scratch.p, F.pcol, F.pval);
+    (k_p_values<<<nblk(n, 128), 128, 0, st>>>(n, A.rowptr, A.col, A.val, agg, off3.p, F.dinv, omega, F.prow,
+                                              scratch.p, F.pcol, F.pval), SVXG_COUNT_LAUNCH());
   }
   if (smoothed) P.amg_build_work += 12 * nnzb;
   {
     Tmp<unsigned long long> acc(st);
     TRY(acc.alloc(1));
     SVXG_CUDA(cudaMemsetAsync(acc.p, 0, sizeof(unsigned long long), st));
-    k_work_ap<<<nblk(nnzb), kT, 0, st>>>(nnzb, F.A.col, F.prow, acc.p);
+    (k_work_ap<<<nblk(nnzb), kT, 0, st>>>(nnzb, F.A.col, F.prow, acc.p), SVXG_COUNT_LAUNCH());
     unsigned long long w = 0;
     TRY(copy_to_host(P, &w, acc.p, sizeof(w)));
     P.amg_build_work += int64_t(w);
@@ -831,14 +848,14 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     TRY(erow.alloc(size_t(F.pnnz)));
     SVXG_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * (size_t(na) + 1), st));
     SVXG_CUDA(cudaMemsetAsync(cursor.p, 0, sizeof(int32_t) * (size_t(na) + 1), st));
-    k_r_count<<<nblk(F.pnnz), kT, 0, st>>>(F.pnnz, F.pcol, cnt.p);
+    (k_r_count<<<nblk(F.pnnz), kT, 0, st>>>(F.pnnz, F.pcol, cnt.p), SVXG_COUNT_LAUNCH());
     TRY(P.mem.alloc(&F.rrow, size_t(na) + 1));
     TRY(exclusive_scan_i32(P, cnt.p, F.rrow, int64_t(na) + 1, nullptr));
     TRY(P.mem.alloc(&F.rent_e, size_t(F.pnnz)));
     TRY(P.mem.alloc(&F.rent_i, size_t(F.pnnz)));
-    k_r_fill<<<nblk(n), kT, 0, st>>>(n, F.prow, F.pcol, F.rrow, cursor.p, F.rent_e);
-    k_entry_rows<<<nblk(n), kT, 0, st>>>(n, F.prow, erow.p);
-    k_r_sort<<<nblk(na), kT, 0, st>>>(na, F.rrow, F.rent_e, F.rent_i, erow.p);
+    (k_r_fill<<<nblk(n), kT, 0, st>>>(n, F.prow, F.pcol, F.rrow, cursor.p, F.rent_e), SVXG_COUNT_LAUNCH());
+    (k_entry_rows<<<nblk(n), kT, 0, st>>>(n, F.prow, erow.p), SVXG_COUNT_LAUNCH());
+    (k_r_sort<<<nblk(na), kT, 0, st>>>(na, F.rrow, F.rent_e, F.rent_i, erow.p), SVXG_COUNT_LAUNCH());
   }
   // Galerkin: A P
   Tmp<int32_t> aprow(st), apcol(st);
@@ -848,28 +865,28 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     Tmp<int64_t> soff(st);
     TRY(bound.alloc(size_t(n) + 1));
     TRY(soff.alloc(size_t(n) + 1));
-    k_ap_bound<<<nblk(n), kT, 0, st>>>(n, F.A.rowptr, F.A.col, F.prow, bound.p);
-    k_i64_offsets<<<1, 1, 0, st>>>(n, bound.p, soff.p);
+    SVXG_CUDA(cudaMemsetAsync(bound.p, 0, sizeof(int32_t) * (size_t(n) + 1), st));
+    (k_ap_bound<<<nblk(n), kT, 0, st>>>(n, F.A.rowptr, F.A.col, F.prow, bound.p), SVXG_COUNT_LAUNCH());
     int64_t stotal = 0;
-    TRY(copy_to_host(P, &stotal, soff.p + n, sizeof(int64_t)));
+    TRY(offsets64(P, bound.p, n, soff.p, &stotal));
     TRY(scratch.alloc(size_t(stotal) + 1));
     TRY(aprow.alloc(size_t(n) + 1));
     Tmp<int32_t> aplen(st);
     TRY(aplen.alloc(size_t(n) + 1));
     SVXG_CUDA(cudaMemsetAsync(aplen.p, 0, sizeof(int32_t) * (size_t(n) + 1), st));
-    k_ap_count<<<nblk(n), kT, 0, st>>>(n, F.A.rowptr, F.A.col, F.prow, F.pcol, aplen.p, scratch.p, soff.p, INT_MAX);
+    (k_ap_count<<<nblk(n), kT, 0, st>>>(n, F.A.rowptr, F.A.col, F.prow, F.pcol, aplen.p, scratch.p, soff.p, INT_MAX), SVXG_COUNT_LAUNCH());
     int32_t apnnz = 0;
     TRY(exclusive_scan_i32(P, aplen.p, aprow.p, int64_t(n) + 1, &apnnz));
     TRY(apcol.alloc(size_t(apnnz)));
     TRY(apval.alloc(size_t(apnnz) * 36));
-    k_ap_values<<<nblk(n, 128), 128, 0, st>>>(n, F.A.rowptr, F.A.col, F.A.val, F.prow, F.pcol, F.pval, aprow.p,
-                                              scratch.p, soff.p, apcol.p, apval.p);
+    (k_ap_values<<<nblk(32 * int64_t(n), 128), 128, 0, st>>>(n, F.A.rowptr, F.A.col, F.A.val, F.prow, F.pcol, F.pval, aprow.p,
+                                              scratch.p, soff.p, apcol.p, apval.p), SVXG_COUNT_LAUNCH());
   }
   {
     Tmp<unsigned long long> acc(st);
     TRY(acc.alloc(1));
     SVXG_CUDA(cudaMemsetAsync(acc.p, 0, sizeof(unsigned long long), st));
-    k_work_rap<<<nblk(n), kT, 0, st>>>(n, F.prow, aprow.p, acc.p);
+    (k_work_rap<<<nblk(n), kT, 0, st>>>(n, F.prow, aprow.p, acc.p), SVXG_COUNT_LAUNCH());
     unsigned long long w = 0;
     TRY(copy_to_host(P, &w, acc.p, sizeof(w)));
     P.amg_build_work += int64_t(w);
@@ -880,14 +897,14 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     Tmp<int64_t> soff(st);
     TRY(bound.alloc(size_t(na) + 1));
     TRY(soff.alloc(size_t(na) + 1));
-    k_c_bound<<<nblk(na), kT, 0, st>>>(na, F.rrow, F.rent_i, aprow.p, bound.p);
-    k_i64_offsets<<<1, 1, 0, st>>>(na, bound.p, soff.p);
+    SVXG_CUDA(cudaMemsetAsync(bound.p, 0, sizeof(int32_t) * (size_t(na) + 1), st));
+    (k_c_bound<<<nblk(na), kT, 0, st>>>(na, F.rrow, F.rent_i, aprow.p, bound.p), SVXG_COUNT_LAUNCH());
     int64_t stotal = 0;
-    TRY(copy_to_host(P, &stotal, soff.p + na, sizeof(int64_t)));
+    TRY(offsets64(P, bound.p, na, soff.p, &stotal));
     TRY(scratch.alloc(size_t(stotal) + 1));
     TRY(clen.alloc(size_t(na) + 1));
     SVXG_CUDA(cudaMemsetAsync(clen.p, 0, sizeof(int32_t) * (size_t(na) + 1), st));
-    k_c_count<<<nblk(na), kT, 0, st>>>(na, F.rrow, F.rent_i, aprow.p, apcol.p, clen.p, scratch.p, soff.p, INT_MAX);
+    (k_c_count<<<nblk(na), kT, 0, st>>>(na, F.rrow, F.rent_i, aprow.p, apcol.p, clen.p, scratch.p, soff.p, INT_MAX), SVXG_COUNT_LAUNCH());
     TRY(P.mem.alloc(&C.A.rowptr, size_t(na) + 1));
     int32_t cnnz = 0;
     TRY(exclusive_scan_i32(P, clen.p, C.A.rowptr, int64_t(na) + 1, &cnnz));
@@ -895,8 +912,8 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     TRY(P.mem.alloc(&C.A.col, size_t(cnnz)));
     TRY(P.mem.alloc(&C.A.val, size_t(cnnz) * 36));
     const double scale = (!smoothed && opt.coarse_scale != 1.0) ? opt.coarse_scale : 1.0;
-    k_c_values<<<nblk(na, 128), 128, 0, st>>>(na, F.rrow, F.rent_i, F.rent_e, F.pval, aprow.p, apcol.p, apval.p,
-                                              C.A.rowptr, scratch.p, soff.p, C.A.col, C.A.val, scale);
+    (k_c_values<<<nblk(32 * int64_t(na), 128), 128, 0, st>>>(na, F.rrow, F.rent_i, F.rent_e, F.pval, aprow.p, apcol.p, apval.p,
+                                              C.A.rowptr, scratch.p, soff.p, C.A.col, C.A.val, scale), SVXG_COUNT_LAUNCH());
   }
   SVXG_CUDA(cudaGetLastError());
   bool fin = false;
@@ -928,15 +945,15 @@ int factor_coarsest(Problem& P) {
   TRY(P.mem.alloc(&P.d_chol, size_t(m) * size_t(m)));
   cudaStream_t st = P.stream;
   SVXG_CUDA(cudaMemsetAsync(P.d_chol, 0, sizeof(double) * size_t(m) * size_t(m), st));
-  k_dense_fill<<<nblk(L.A.n), kT, 0, st>>>(L.A.n, L.A.rowptr, L.A.col, L.A.val, m, P.d_chol);
+  (k_dense_fill<<<nblk(L.A.n), kT, 0, st>>>(L.A.n, L.A.rowptr, L.A.col, L.A.val, m, P.d_chol), SVXG_COUNT_LAUNCH());
   Tmp<double> dmax(st);
   TRY(dmax.alloc(1));
-  k_dense_dmax<<<1, 1, 0, st>>>(m, P.d_chol, dmax.p);
+  (k_dense_dmax<<<1, 1, 0, st>>>(m, P.d_chol, dmax.p), SVXG_COUNT_LAUNCH());
   for (int32_t j = 0; j < m; ++j) {
-    k_chol_diag<<<1, 1, 0, st>>>(m, j, P.d_chol, dmax.p);
-    if (m - j - 1 > 0) k_chol_col<<<nblk(m - j - 1, 128), 128, 0, st>>>(m, j, P.d_chol);
+    (k_chol_diag<<<1, 1, 0, st>>>(m, j, P.d_chol, dmax.p), SVXG_COUNT_LAUNCH());
+    if (m - j - 1 > 0) (k_chol_col<<<nblk(m - j - 1, 128), 128, 0, st>>>(m, j, P.d_chol), SVXG_COUNT_LAUNCH());
   }
-  k_chol_mirror<<<nblk(int64_t(m) * m), kT, 0, st>>>(m, P.d_chol);
+  (k_chol_mirror<<<nblk(int64_t(m) * m), kT, 0, st>>>(m, P.d_chol), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   return SVXG_OK;
 }
@@ -952,6 +969,13 @@ __global__ void k_level0_pos(int32_t n, const svxg_node* nodes, const int32_t* d
 }
 
 }  // namespace
+
+// sqrt of the sequential sum of squares of n device doubles (the power iteration's norm)
+int debug_seq_norm(cudaStream_t st, const double* v, int64_t n, double* out_dev) {
+  (k_seq_norm<<<1, exact::kThreads, 0, st>>>(n, v, out_dev), SVXG_COUNT_LAUNCH());
+  SVXG_CUDA(cudaGetLastError());
+  return SVXG_OK;
+}
 
 // Amg::build (amg.cpp:277-318) over K
 int build_hierarchy(Problem& P, int32_t* ok) {
@@ -969,7 +993,7 @@ int build_hierarchy(Problem& P, int32_t* ok) {
     Level& L0 = P.lv[0];
     L0.A = P.K;  // (level 0's matrix is K itself: shared, not copied)
     TRY(P.mem.alloc(&L0.pos, 3 * size_t(P.nfree)));
-    k_level0_pos<<<nblk(P.n), kT, 0, P.stream>>>(P.n, P.d_nodes, P.d_dof, L0.pos);
+    (k_level0_pos<<<nblk(P.n), kT, 0, P.stream>>>(P.n, P.d_nodes, P.d_dof, L0.pos), SVXG_COUNT_LAUNCH());
     bool fin = false;
     TRY(finalize_level(P, L0, &fin));
     if (!fin) {

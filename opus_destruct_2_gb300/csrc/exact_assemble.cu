@@ -15,6 +15,7 @@
 //      or empty rows set to id_scale I.
 // No floating-point atomics anywhere: K is identical run to run and equal to the reference's.
 #include "blk6.cuh"
+#include "exact_sum.cuh"
 #include "problem.cuh"
 
 namespace svxg {
@@ -189,18 +190,21 @@ __global__ void k_trace(int32_t nfree, const int32_t* rowptr, const double* val,
   if (id) atomicAdd(nident, 1);
 }
 
-// id_scale (stress.cpp:112-122): the rows' terms summed one after another, in row order
-__global__ void k_id_scale(int32_t nfree, const double* term, double* out) {
-  double tr = 0.0;
-  int32_t cnt = 0;
-  for (int32_t d = 0; d < nfree; ++d) {
+// id_scale (stress.cpp:112-122): the rows' terms summed one after another, in row order (the
+// sequential sum's exact bits, computed in parallel: exact_sum.cuh), over their count
+__global__ void __launch_bounds__(exact::kThreads) k_id_scale(int32_t nfree, const double* term, double* out) {
+  const double tr = exact::sequential_sum(nfree, [term](int64_t d) {
     const double t = term[d];
-    if (t >= 0.0) {
-      tr += t;
-      ++cnt;
-    }
-  }
-  out[0] = cnt ? tr / cnt : 1.0;
+    return t >= 0.0 ? t : 0.0;
+  });
+  __shared__ int32_t cnt;
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  int32_t c = 0;
+  for (int32_t d = threadIdx.x; d < nfree; d += blockDim.x) c += term[d] >= 0.0 ? 1 : 0;
+  atomicAdd(&cnt, c);
+  __syncthreads();
+  if (threadIdx.x == 0) out[0] = cnt ? tr / cnt : 1.0;
 }
 
 // retired and empty rows: id_scale on the diagonal (stress.cpp:123-130)
@@ -328,10 +332,10 @@ int assemble_matrix(Problem& P) {
   TRY(node_of_dof.alloc(size_t(n)));
   P.mem.release(P.d_dof);
   TRY(P.mem.alloc(&P.d_dof, size_t(n)));
-  if (n > 0) k_free_flags<<<blocks_for(n), kT, 0, st>>>(n, P.d_nodes, flags.p);
+  if (n > 0) (k_free_flags<<<blocks_for(n), kT, 0, st>>>(n, P.d_nodes, flags.p), SVXG_COUNT_LAUNCH());
   int32_t nfree = 0;
   TRY(exclusive_scan_i32(P, flags.p, scan.p, n, &nfree));
-  if (n > 0) k_dof<<<blocks_for(n), kT, 0, st>>>(n, P.d_nodes, scan.p, P.d_dof, node_of_dof.p);
+  if (n > 0) (k_dof<<<blocks_for(n), kT, 0, st>>>(n, P.d_nodes, scan.p, P.d_dof, node_of_dof.p), SVXG_COUNT_LAUNCH());
   P.nfree = nfree;
   // 2. incidences
   P.mem.release(P.d_in_k);
@@ -342,19 +346,19 @@ int assemble_matrix(Problem& P) {
   TRY(cursor.alloc(size_t(n) + 1));
   SVXG_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int32_t) * (size_t(n) + 1), st));
   SVXG_CUDA(cudaMemsetAsync(cursor.p, 0, sizeof(int32_t) * (size_t(n) + 1), st));
-  if (nb > 0) k_classify<<<blocks_for(nb), kT, 0, st>>>(nb, P.d_bonds, P.d_nodes, P.d_dof, P.d_in_k, cnt.p);
+  if (nb > 0) (k_classify<<<blocks_for(nb), kT, 0, st>>>(nb, P.d_bonds, P.d_nodes, P.d_dof, P.d_in_k, cnt.p), SVXG_COUNT_LAUNCH());
   int32_t ninc = 0;
   TRY(exclusive_scan_i32(P, cnt.p, off.p, int64_t(n) + 1, &ninc));
   Tmp<uint64_t> by_nbr(st);
   Tmp<uint32_t> by_bond(st);
   TRY(by_nbr.alloc(size_t(ninc)));
   TRY(by_bond.alloc(size_t(ninc)));
-  if (nb > 0) k_fill<<<blocks_for(nb), kT, 0, st>>>(nb, P.d_bonds, P.d_dof, P.d_in_k, off.p, cursor.p, by_nbr.p);
+  if (nb > 0) (k_fill<<<blocks_for(nb), kT, 0, st>>>(nb, P.d_bonds, P.d_dof, P.d_in_k, off.p, cursor.p, by_nbr.p), SVXG_COUNT_LAUNCH());
   // 3. pattern
   Tmp<int32_t> rowlen(st);
   TRY(rowlen.alloc(size_t(nfree) + 1));
   SVXG_CUDA(cudaMemsetAsync(rowlen.p, 0, sizeof(int32_t) * (size_t(nfree) + 1), st));
-  if (n > 0) k_sort_rows<<<blocks_for(n, 128), 128, 0, st>>>(n, P.d_dof, off.p, by_nbr.p, by_bond.p, rowlen.p);
+  if (n > 0) (k_sort_rows<<<blocks_for(n, 128), 128, 0, st>>>(n, P.d_dof, off.p, by_nbr.p, by_bond.p, rowlen.p), SVXG_COUNT_LAUNCH());
   P.mem.release(P.K.rowptr);
   TRY(P.mem.alloc(&P.K.rowptr, size_t(nfree) + 1));
   int32_t nnzb = 0;
@@ -370,13 +374,13 @@ int assemble_matrix(Problem& P) {
   TRY(cstart.alloc(size_t(nnzb)));
   TRY(ccount.alloc(size_t(nnzb)));
   if (nfree > 0)
-    k_columns<<<blocks_for(nfree), kT, 0, st>>>(nfree, node_of_dof.p, off.p, by_nbr.p, P.K.rowptr, P.K.col, cstart.p,
-                                                ccount.p);
+    (k_columns<<<blocks_for(nfree), kT, 0, st>>>(nfree, node_of_dof.p, off.p, by_nbr.p, P.K.rowptr, P.K.col, cstart.p,
+                                                ccount.p), SVXG_COUNT_LAUNCH());
   // 4. values
   if (nnzb > 0)
-    k_block_values<<<blocks_for(nnzb, 128), 128, 0, st>>>(nnzb, nfree, P.K.rowptr, P.K.col, node_of_dof.p, cstart.p,
+    (k_block_values<<<blocks_for(nnzb, 128), 128, 0, st>>>(nnzb, nfree, P.K.rowptr, P.K.col, node_of_dof.p, cstart.p,
                                                           ccount.p, by_nbr.p, by_bond.p, P.d_bonds, P.d_nodes,
-                                                          P.d_mats, P.K.val);
+                                                          P.d_mats, P.K.val), SVXG_COUNT_LAUNCH());
   // 5. id_scale and identity rows
   Tmp<double> term(st), ids(st);
   Tmp<uint8_t> ident(st);
@@ -387,10 +391,10 @@ int assemble_matrix(Problem& P) {
   TRY(ids.alloc(1));
   SVXG_CUDA(cudaMemsetAsync(nident.p, 0, sizeof(int32_t), st));
   if (nfree > 0)
-    k_trace<<<blocks_for(nfree), kT, 0, st>>>(nfree, P.K.rowptr, P.K.val, node_of_dof.p, P.d_nodes, term.p, ident.p,
-                                              nident.p);
-  k_id_scale<<<1, 1, 0, st>>>(nfree, term.p, ids.p);
-  if (nfree > 0) k_identity<<<blocks_for(nfree), kT, 0, st>>>(nfree, P.K.rowptr, ident.p, ids.p, P.K.val);
+    (k_trace<<<blocks_for(nfree), kT, 0, st>>>(nfree, P.K.rowptr, P.K.val, node_of_dof.p, P.d_nodes, term.p, ident.p,
+                                              nident.p), SVXG_COUNT_LAUNCH());
+  (k_id_scale<<<1, exact::kThreads, 0, st>>>(nfree, term.p, ids.p), SVXG_COUNT_LAUNCH());
+  if (nfree > 0) (k_identity<<<blocks_for(nfree), kT, 0, st>>>(nfree, P.K.rowptr, ident.p, ids.p, P.K.val), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   SVXG_CUDA(cudaMemcpyAsync(&P.id_scale, ids.p, sizeof(double), cudaMemcpyDeviceToHost, st));
   P.h_dof.resize(size_t(n));
@@ -406,7 +410,7 @@ int build_jacobi(Problem& P) {
   P.mem.release(P.d_jinv);
   TRY(P.mem.alloc(&P.d_jinv, size_t(P.nfree) * 36));
   if (P.nfree > 0)
-    k_jacobi<<<blocks_for(P.nfree), kT, 0, P.stream>>>(P.nfree, P.K.rowptr, P.K.val, P.id_scale, P.d_jinv);
+    (k_jacobi<<<blocks_for(P.nfree), kT, 0, P.stream>>>(P.nfree, P.K.rowptr, P.K.val, P.id_scale, P.d_jinv), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   return SVXG_OK;
 }
@@ -416,8 +420,8 @@ int remove_bonds_device(Problem& P, const int32_t* list, int32_t count) {
   Tmp<int32_t> d(P.stream);
   TRY(d.alloc(size_t(count)));
   SVXG_CUDA(cudaMemcpyAsync(d.p, list, sizeof(int32_t) * size_t(count), cudaMemcpyHostToDevice, P.stream));
-  k_remove_bonds<<<1, 1, 0, P.stream>>>(d.p, count, P.d_bonds, P.d_in_k, P.d_nodes, P.d_mats, P.d_dof, P.K.rowptr,
-                                        P.K.col, P.K.val, P.d_jinv, P.jacobi_only ? 1 : 0, P.id_scale);
+  (k_remove_bonds<<<1, 1, 0, P.stream>>>(d.p, count, P.d_bonds, P.d_in_k, P.d_nodes, P.d_mats, P.d_dof, P.K.rowptr,
+                                        P.K.col, P.K.val, P.d_jinv, P.jacobi_only ? 1 : 0, P.id_scale), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   SVXG_CUDA(cudaStreamSynchronize(P.stream));
   return SVXG_OK;
@@ -428,8 +432,8 @@ int set_identity_rows(Problem& P, const int32_t* rows, int32_t count) {
   Tmp<int32_t> d(P.stream);
   TRY(d.alloc(size_t(count)));
   SVXG_CUDA(cudaMemcpyAsync(d.p, rows, sizeof(int32_t) * size_t(count), cudaMemcpyHostToDevice, P.stream));
-  k_identity_rows<<<blocks_for(count), kT, 0, P.stream>>>(d.p, count, P.K.rowptr, P.K.val, P.d_jinv,
-                                                         P.jacobi_only ? 1 : 0, P.id_scale);
+  (k_identity_rows<<<blocks_for(count), kT, 0, P.stream>>>(d.p, count, P.K.rowptr, P.K.val, P.d_jinv,
+                                                         P.jacobi_only ? 1 : 0, P.id_scale), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   SVXG_CUDA(cudaStreamSynchronize(P.stream));
   return SVXG_OK;

@@ -47,8 +47,8 @@ __global__ void k_compact(int32_t nb, const int32_t* flag, const int32_t* pos, i
 
 int bond_loads_device(Problem& P, const double* u_nodes, svxg_bond_load* out) {
   if (P.nb == 0) return SVXG_OK;
-  k_judge<<<unsigned((P.nb + kT - 1) / kT), kT, 0, P.stream>>>(P.nb, P.d_bonds, P.d_nodes, P.d_mats, u_nodes, 1.0, out,
-                                                              nullptr, nullptr, nullptr);
+  (k_judge<<<unsigned((P.nb + kT - 1) / kT), kT, 0, P.stream>>>(P.nb, P.d_bonds, P.d_nodes, P.d_mats, u_nodes, 1.0, out,
+                                                              nullptr, nullptr, nullptr), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   return SVXG_OK;
 }
@@ -65,10 +65,10 @@ int utilization_device(Problem& P, const double* u_nodes, double fragility, doub
   SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&flag), sizeof(int32_t) * size_t(P.nb), P.stream));
   SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&pos), sizeof(int32_t) * size_t(P.nb), P.stream));
   const unsigned g = unsigned((P.nb + kT - 1) / kT);
-  k_judge<<<g, kT, 0, P.stream>>>(P.nb, P.d_bonds, P.d_nodes, P.d_mats, u_nodes, fragility, nullptr, phi, mode, flag);
+  (k_judge<<<g, kT, 0, P.stream>>>(P.nb, P.d_bonds, P.d_nodes, P.d_mats, u_nodes, fragility, nullptr, phi, mode, flag), SVXG_COUNT_LAUNCH());
   int32_t total = 0;
   int e = exclusive_scan_i32(P, flag, pos, P.nb, &total);
-  if (!e && over) k_compact<<<g, kT, 0, P.stream>>>(P.nb, flag, pos, over);
+  if (!e && over) (k_compact<<<g, kT, 0, P.stream>>>(P.nb, flag, pos, over), SVXG_COUNT_LAUNCH());
   cudaFreeAsync(flag, P.stream);
   cudaFreeAsync(pos, P.stream);
   if (e) return e;

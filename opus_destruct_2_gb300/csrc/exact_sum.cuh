@@ -1,0 +1,237 @@
+// exact_sum.cuh - the sequential double sum s = ((0 + t_0) + t_1) + ... of nonnegative terms,
+// computed in parallel with the very same result bits.
+//
+// The reference sums some nonnegative sequences one term after another (the power iteration's
+// norm, core/src/solve/amg.cpp:267-268; id_scale, core/src/stress/stress.cpp:112-122). A
+// parallel tree would round differently, so the device reproduces the sequential rounding:
+// while the running sum s stays inside one binade [2^e, 2^(e+1)) (ulp U fixed), s is an
+// integer S times U and every addition fl(s + t) is S + round(t / U), the rounding of t / U to an
+// integer with ties broken to the even result - i.e. by the parity of S. Each term is therefore
+// a pair of integer increments (delta if S is even, delta if S is odd), and pairs compose
+// associatively (the second's choice keyed by the parity after the first): a block-wide scan of
+// pairs gives the running S at every position. The first position where S would leave the
+// binade (S >= 2^53; a term at least 2^(e+1), infinite or NaN also counts) is found by a block
+// minimum; there the addition is done by the hardware (IEEE add), the binade changes and the
+// scan resumes. The sum crosses at most a few dozen binades, so the work stays O(n).
+// Integer arithmetic only, apart from those crossing additions.
+#pragma once
+
+#include <cstdint>
+
+namespace svxg {
+namespace exact {
+
+constexpr int kThreads = 1024;
+constexpr int kItems = 8;
+constexpr int64_t kCap = int64_t(1) << 54;  // saturation: past any binade's room
+
+struct Pair {
+  int64_t d0, d1;  // increments (in ulps) from an even / odd S
+};
+
+__device__ __forceinline__ int64_t sat(int64_t a, int64_t b) {
+  const int64_t s = a + b;
+  return s > kCap ? kCap : s;
+}
+
+// x then y
+__device__ __forceinline__ Pair compose(Pair x, Pair y) {
+  Pair r;
+  r.d0 = sat(x.d0, (x.d0 & 1) ? y.d1 : y.d0);
+  r.d1 = sat(x.d1, (x.d1 & 1) ? y.d0 : y.d1);
+  return r;
+}
+
+// the increment pair of adding t (>= 0) to s = S U with U = 2^uexp; kCap marks a crossing term
+__device__ __forceinline__ Pair term_pair(double t, int uexp) {
+  const uint64_t bits = uint64_t(__double_as_longlong(t));
+  const int E = int((bits >> 52) & 0x7ff);
+  if (E == 0x7ff || (bits >> 63)) return {kCap, kCap};  // inf / NaN (/ negative: not expected)
+  uint64_t m;
+  int et;
+  if (E == 0) {
+    m = bits & ((uint64_t(1) << 52) - 1);
+    et = -1074;
+  } else {
+    m = (bits & ((uint64_t(1) << 52) - 1)) | (uint64_t(1) << 52);
+    et = E - 1075;
+  }
+  if (m == 0) return {0, 0};
+  const int sh = et - uexp;  // t / U = m 2^sh
+  if (sh >= 0) {
+    if (sh > 1) return {kCap, kCap};  // t >= 2^(e+1): a crossing (m >= 2^52 when normal)
+    const uint64_t a = m << sh;
+    if (a >= (uint64_t(1) << 53)) return {kCap, kCap};
+    return {int64_t(a), int64_t(a)};
+  }
+  const int r = -sh;
+  if (r > 60) return {0, 0};  // t / U < 2^-7: rounds to 0 whatever the parity
+  const uint64_t I = m >> r;
+  const uint64_t rem = m & ((uint64_t(1) << r) - 1);
+  const uint64_t half = uint64_t(1) << (r - 1);
+  if (rem < half) return {int64_t(I), int64_t(I)};
+  if (rem > half) return {int64_t(I + 1), int64_t(I + 1)};
+  // a tie: the even result
+  const int64_t Ii = int64_t(I);
+  return {Ii + ((Ii & 1) ? 1 : 0), Ii + ((Ii & 1) ? 0 : 1)};
+}
+
+// s = S 2^uexp, S < 2^53 (normal or subnormal)
+__device__ __forceinline__ void split(double s, int64_t* S, int* uexp) {
+  const uint64_t bits = uint64_t(__double_as_longlong(s));
+  const int E = int((bits >> 52) & 0x7ff);
+  if (E == 0) {
+    *S = int64_t(bits & ((uint64_t(1) << 52) - 1));
+    *uexp = -1074;
+  } else {
+    *S = int64_t((bits & ((uint64_t(1) << 52) - 1)) | (uint64_t(1) << 52));
+    *uexp = E - 1075;
+  }
+}
+
+__device__ __forceinline__ double join(int64_t S, int uexp) {
+  // S < 2^53; uexp = -1074 with S < 2^52 is subnormal
+  if (S < (int64_t(1) << 52)) {
+    // only reachable for uexp = -1074 (a normal start keeps S >= 2^52)
+    return __longlong_as_double((long long)S);
+  }
+  const uint64_t E = uint64_t(uexp + 1075);
+  return __longlong_as_double((long long)((E << 52) | (uint64_t(S) & ((uint64_t(1) << 52) - 1))));
+}
+
+// Block-wide exclusive scan of pairs (kThreads threads); returns the exclusive prefix of this
+// thread's pair and the block total in *tot.
+__device__ inline Pair block_scan(Pair v, Pair* tot) {
+  __shared__ Pair sh[kThreads];
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  // Hillis-Steele inclusive scan
+  for (int d = 1; d < kThreads; d <<= 1) {
+    Pair x = sh[threadIdx.x];
+    if (int(threadIdx.x) >= d) x = compose(sh[threadIdx.x - d], x);
+    __syncthreads();
+    sh[threadIdx.x] = x;
+    __syncthreads();
+  }
+  const Pair incl = sh[threadIdx.x];
+  *tot = sh[kThreads - 1];
+  Pair ex = threadIdx.x ? sh[threadIdx.x - 1] : Pair{0, 0};
+  __syncthreads();
+  (void)incl;
+  return ex;
+}
+
+__device__ __forceinline__ int64_t pick(Pair p, int64_t S) { return (S & 1) ? p.d1 : p.d0; }
+
+// The sequential sum of term(k) for k in [0, n), with term(k) >= 0; one block of kThreads.
+// Term: a callable (int64_t k) -> double.
+template <class Term>
+__device__ inline double sequential_sum(int64_t n, Term term) {
+  __shared__ double s_sh;
+  __shared__ int64_t p_sh;
+  __shared__ int64_t first_sh;
+  if (threadIdx.x == 0) {
+    s_sh = 0.0;
+    p_sh = 0;
+  }
+  __syncthreads();
+  constexpr int64_t kTile = int64_t(kThreads) * kItems;
+  while (true) {
+    const int64_t p = p_sh;
+    const double s = s_sh;
+    __syncthreads();
+    if (p >= n) break;
+    const uint64_t sbits = uint64_t(__double_as_longlong(s));
+    if (((sbits >> 52) & 0x7ff) == 0x7ff) {
+      // s is inf or NaN: NaN if any later term is NaN, else s
+      __shared__ int nan_sh;
+      if (threadIdx.x == 0) nan_sh = 0;
+      __syncthreads();
+      for (int64_t k = p + threadIdx.x; k < n; k += kThreads)
+        if (term(k) != term(k)) nan_sh = 1;
+      __syncthreads();
+      const double r = (nan_sh && s == s) ? __longlong_as_double(0x7ff8000000000000LL) : s;
+      __syncthreads();
+      return r;
+    }
+    if (s == 0.0) {
+      // leading zeros leave s at 0; the first nonzero term becomes s exactly
+      if (threadIdx.x == 0) first_sh = n;
+      __syncthreads();
+      for (int64_t b = p; b < n && first_sh == n; b += kTile) {
+        for (int it = 0; it < kItems; ++it) {
+          const int64_t k = b + int64_t(it) * kThreads + threadIdx.x;
+          if (k < n) {
+            const double t = term(k);
+            if (!(t == 0.0)) atomicMin((unsigned long long*)&first_sh, (unsigned long long)k);
+          }
+        }
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) {
+        if (first_sh < n) {
+          s_sh = 0.0 + term(first_sh);
+          p_sh = first_sh + 1;
+        } else {
+          p_sh = n;
+        }
+      }
+      __syncthreads();
+      continue;
+    }
+    int64_t S;
+    int uexp;
+    split(s, &S, &uexp);
+    // this thread's kItems consecutive terms
+    const int64_t base = p + int64_t(threadIdx.x) * kItems;
+    Pair loc[kItems];
+    Pair acc{0, 0};
+    for (int it = 0; it < kItems; ++it) {
+      const int64_t k = base + it;
+      loc[it] = k < n ? term_pair(term(k), uexp) : Pair{0, 0};
+      acc = compose(acc, loc[it]);
+    }
+    Pair tot;
+    const Pair ex = block_scan(acc, &tot);
+    // the first position where S leaves the binade
+    if (threadIdx.x == 0) first_sh = INT64_MAX;
+    __syncthreads();
+    {
+      int64_t run = sat(S, pick(ex, S));
+      for (int it = 0; it < kItems; ++it) {
+        const int64_t k = base + it;
+        if (k >= n) break;
+        const int64_t nxt = sat(run, pick(loc[it], run));
+        if (nxt >= (int64_t(1) << 53)) {
+          atomicMin((unsigned long long*)&first_sh, (unsigned long long)k);
+          break;
+        }
+        run = nxt;
+      }
+    }
+    __syncthreads();
+    const int64_t firstx = first_sh;
+    const int64_t end = p + kTile < n ? p + kTile : n;
+    if (firstx == INT64_MAX) {
+      if (threadIdx.x == 0) {
+        s_sh = join(sat(S, pick(tot, S)), uexp);
+        p_sh = end;
+      }
+    } else {
+      // S just before the crossing: the thread that owns it replays its prefix
+      const int64_t owner = (firstx - p) / kItems;
+      if (int64_t(threadIdx.x) == owner) {
+        int64_t run = sat(S, pick(ex, S));
+        for (int64_t k = base; k < firstx; ++k) run = sat(run, pick(loc[k - base], run));
+        const double before = join(run, uexp);
+        s_sh = __dadd_rn(before, term(firstx));
+        p_sh = firstx + 1;
+      }
+    }
+    __syncthreads();
+  }
+  return s_sh;
+}
+
+}  // namespace exact
+}  // namespace svxg

@@ -24,6 +24,10 @@ namespace svxg {
 // Thread-local last error message (svxg_last_error).
 void set_error(const std::string& msg);
 
+// Kernel launches made by this library (svxg_launch_count): every launch site counts itself.
+void count_launch();
+#define SVXG_COUNT_LAUNCH() ::svxg::count_launch()
+
 #define SVXG_CUDA(call)                                                                   \
   do {                                                                                    \
     cudaError_t e_ = (call);                                                              \
@@ -163,6 +167,10 @@ struct Problem {
   int32_t partial_blocks = 0;
   bool active = false;
   int32_t run_iters = 0;
+  // live kernel timing (CUDA events around each conjugate-gradient SpMV launch)
+  bool timer_on = false;
+  std::vector<cudaEvent_t> timer_events;
+  size_t timer_used = 0;          // event pairs recorded since the last read
   // scratch
   int32_t* d_scan = nullptr;      // scan block sums
   int64_t scan_cap = 0;
@@ -176,6 +184,7 @@ int remove_bonds_device(Problem& P, const int32_t* bonds, int32_t count);  // se
 int set_identity_rows(Problem& P, const int32_t* rows, int32_t count);
 // exact_amg.cu
 int build_hierarchy(Problem& P, int32_t* ok);    // Amg::build on the device
+int debug_seq_norm(cudaStream_t st, const double* v, int64_t n, double* out_dev);
 // solve.cu
 int spmv(Problem& P, const Bsr& A, const double* x, double* y);
 int pcg_begin(Problem& P, const double* f_nodes, const double* u0_nodes);  // device, node order

@@ -90,9 +90,9 @@ int exclusive_scan_i32(Problem& P, const int32_t* in, int32_t* out, int64_t n, i
     P.scan_cap = ntiles + 1;
   }
   if (n > 0) {
-    k_tile_sums<<<unsigned(ntiles), kScanThreads, 0, P.stream>>>(in, n, P.d_scan);
-    k_scan_sums<<<1, kScanThreads, 0, P.stream>>>(P.d_scan, ntiles);
-    k_tile_scan<<<unsigned(ntiles), kScanThreads, 0, P.stream>>>(in, out, n, P.d_scan);
+    (k_tile_sums<<<unsigned(ntiles), kScanThreads, 0, P.stream>>>(in, n, P.d_scan), SVXG_COUNT_LAUNCH());
+    (k_scan_sums<<<1, kScanThreads, 0, P.stream>>>(P.d_scan, ntiles), SVXG_COUNT_LAUNCH());
+    (k_tile_scan<<<unsigned(ntiles), kScanThreads, 0, P.stream>>>(in, out, n, P.d_scan), SVXG_COUNT_LAUNCH());
   } else {
     SVXG_CUDA(cudaMemsetAsync(P.d_scan, 0, sizeof(int32_t), P.stream));
   }

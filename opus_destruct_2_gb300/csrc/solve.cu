@@ -364,6 +364,19 @@ __global__ void k_gather_nodes(int32_t n, const int32_t* dof, const double* free
     if (e__) return e__;  \
   } while (0)
 
+// an event before (closing = false) or after a timed launch
+int timer_mark(Problem& P, bool closing = false) {
+  const size_t k = 2 * P.timer_used + (closing ? 1 : 0);
+  while (P.timer_events.size() <= k) {
+    cudaEvent_t e;
+    SVXG_CUDA(cudaEventCreate(&e));
+    P.timer_events.push_back(e);
+  }
+  SVXG_CUDA(cudaEventRecord(P.timer_events[k], P.stream));
+  if (closing) ++P.timer_used;
+  return SVXG_OK;
+}
+
 int ensure_run(Problem& P) {
   if (P.d_x) return SVXG_OK;
   const size_t m = 6 * size_t(P.nfree);
@@ -387,8 +400,8 @@ int ensure_run(Problem& P) {
 
 int spmv(Problem& P, const Bsr& A, const double* x, double* y) {
   if (A.n == 0) return SVXG_OK;
-  k_spmv<kPlain><<<spmv_blocks(A.n), kSpmvT, 0, P.stream>>>(A.n, A.rowptr, A.col, A.val, x, y, nullptr, nullptr,
-                                                            nullptr);
+  (k_spmv<kPlain><<<spmv_blocks(A.n), kSpmvT, 0, P.stream>>>(A.n, A.rowptr, A.col, A.val, x, y, nullptr, nullptr,
+                                                            nullptr), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   return SVXG_OK;
 }
@@ -409,7 +422,7 @@ int free_run(Problem& P) {
 
 int precondition(Problem& P, const double* r, double* z) {
   if (P.jacobi_only) {
-    if (P.nfree > 0) k_jacobi_apply<<<vec_blocks(P.nfree), kVecT, 0, P.stream>>>(P.nfree, P.d_jinv, r, z);
+    if (P.nfree > 0) (k_jacobi_apply<<<vec_blocks(P.nfree), kVecT, 0, P.stream>>>(P.nfree, P.d_jinv, r, z), SVXG_COUNT_LAUNCH());
     SVXG_CUDA(cudaGetLastError());
     return SVXG_OK;
   }
@@ -426,19 +439,19 @@ int pcg_begin(Problem& P, const double* f_nodes, const double* u0_nodes) {
   SVXG_CUDA(cudaMemsetAsync(P.d_s, 0, sizeof(PcgScalars), st));
   const unsigned nb_nodes = unsigned((P.n + kVecT - 1) / kVecT);
   if (P.n > 0) {
-    k_scatter_free<<<nb_nodes, kVecT, 0, st>>>(P.n, P.d_dof, f_nodes, P.d_f);
-    if (u0_nodes) k_scatter_free<<<nb_nodes, kVecT, 0, st>>>(P.n, P.d_dof, u0_nodes, P.d_x);
+    (k_scatter_free<<<nb_nodes, kVecT, 0, st>>>(P.n, P.d_dof, f_nodes, P.d_f), SVXG_COUNT_LAUNCH());
+    if (u0_nodes) (k_scatter_free<<<nb_nodes, kVecT, 0, st>>>(P.n, P.d_dof, u0_nodes, P.d_x), SVXG_COUNT_LAUNCH());
   }
   if (nf > 0) {
     TRY(spmv(P, P.K, P.d_x, P.d_q));
-    k_begin_r<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_f, P.d_q, P.d_r, P.d_partials, P.d_counter, P.d_s);
-    k_begin_zero<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_x, P.d_r, P.d_s);
+    (k_begin_r<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_f, P.d_q, P.d_r, P.d_partials, P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
+    (k_begin_zero<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_x, P.d_r, P.d_s), SVXG_COUNT_LAUNCH());
     if (P.jacobi_only) {
-      k_jacobi_rz<0><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_jinv, P.d_r, P.d_z, P.d_p, P.d_partials,
-                                                       P.d_counter, P.d_s);
+      (k_jacobi_rz<0><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_jinv, P.d_r, P.d_z, P.d_p, P.d_partials,
+                                                       P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
     } else {
       TRY(vcycle(P, P.d_r, P.d_z));
-      k_rz<0><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_r, P.d_z, P.d_p, P.d_partials, P.d_counter, P.d_s);
+      (k_rz<0><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_r, P.d_z, P.d_p, P.d_partials, P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
     }
   }
   SVXG_CUDA(cudaGetLastError());
@@ -456,8 +469,8 @@ int pcg_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) {
   }
   const int32_t nf = P.nfree;
   cudaStream_t st = P.stream;
-  k_iter_start<<<vec_blocks(std::max(nf, 1)), kVecT, 0, st>>>(nf, P.d_r, rtol, maxit, P.d_partials, P.d_counter,
-                                                             P.d_s);
+  (k_iter_start<<<vec_blocks(std::max(nf, 1)), kVecT, 0, st>>>(nf, P.d_r, rtol, maxit, P.d_partials, P.d_counter,
+                                                             P.d_s), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   int32_t queued = 0;
   int32_t batch = 2;
@@ -467,18 +480,20 @@ int pcg_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) {
     if (P.h_s->done || queued >= maxit) break;
     const int32_t todo = std::min(batch, maxit - queued);
     for (int32_t it = 0; it < todo; ++it) {
-      k_spmv<kDotP><<<spmv_blocks(nf), kSpmvT, 0, st>>>(nf, P.K.rowptr, P.K.col, P.K.val, P.d_p, P.d_q,
-                                                        P.d_partials, P.d_counter, P.d_s);
-      k_axpy_rr<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_x, P.d_r, P.d_p, P.d_q, P.d_partials, P.d_counter, P.d_s);
+      if (P.timer_on) TRY(timer_mark(P));
+      (k_spmv<kDotP><<<spmv_blocks(nf), kSpmvT, 0, st>>>(nf, P.K.rowptr, P.K.col, P.K.val, P.d_p, P.d_q,
+                                                        P.d_partials, P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
+      if (P.timer_on) TRY(timer_mark(P, true));
+      (k_axpy_rr<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_x, P.d_r, P.d_p, P.d_q, P.d_partials, P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
       if (P.jacobi_only) {
-        k_jacobi_rz<1><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_jinv, P.d_r, P.d_z, nullptr, P.d_partials,
-                                                         P.d_counter, P.d_s);
+        (k_jacobi_rz<1><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_jinv, P.d_r, P.d_z, nullptr, P.d_partials,
+                                                         P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
       } else {
         TRY(vcycle(P, P.d_r, P.d_z));
-        k_rz<1><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_r, P.d_z, nullptr, P.d_partials, P.d_counter, P.d_s);
+        (k_rz<1><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_r, P.d_z, nullptr, P.d_partials, P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
       }
-      k_p_update<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_z, P.d_p, P.d_s);
-      k_mark_cap<<<1, 32, 0, st>>>(P.d_s);
+      (k_p_update<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_z, P.d_p, P.d_s), SVXG_COUNT_LAUNCH());
+      (k_mark_cap<<<1, 32, 0, st>>>(P.d_s), SVXG_COUNT_LAUNCH());
     }
     SVXG_CUDA(cudaGetLastError());
     queued += todo;
@@ -500,7 +515,7 @@ int gather_solution(Problem& P, double* u_nodes) {
     SVXG_CUDA(cudaMemsetAsync(u_nodes, 0, 6 * size_t(P.n) * sizeof(double), P.stream));
     return SVXG_OK;
   }
-  k_gather_nodes<<<unsigned((P.n + kVecT - 1) / kVecT), kVecT, 0, P.stream>>>(P.n, P.d_dof, P.d_x, u_nodes);
+  (k_gather_nodes<<<unsigned((P.n + kVecT - 1) / kVecT), kVecT, 0, P.stream>>>(P.n, P.d_dof, P.d_x, u_nodes), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   return SVXG_OK;
 }

@@ -258,11 +258,11 @@ int power_bound(Problem& P, const Level& L, double* out) {
   SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&v), m * sizeof(double), P.stream));
   SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&w), m * sizeof(double), P.stream));
   SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&nv), sizeof(double), P.stream));
-  k_fill_ones<<<nblk(m), kT, 0, P.stream>>>(m, v);
+  (k_fill_ones<<<nblk(m), kT, 0, P.stream>>>(m, v), SVXG_COUNT_LAUNCH());
   for (int it = 0; it < 12; ++it) {
-    k_spmv64<<<nblk(m), kT, 0, P.stream>>>(L.A.n, L.A.rowptr, L.A.col, L.A.val, v, w);
-    k_pow_step<<<nblk(L.A.n), kT, 0, P.stream>>>(L.A.n, L.dinv, w, v);
-    k_norm_scale<<<1, kT, 0, P.stream>>>(m, v, nv);
+    (k_spmv64<<<nblk(m), kT, 0, P.stream>>>(L.A.n, L.A.rowptr, L.A.col, L.A.val, v, w), SVXG_COUNT_LAUNCH());
+    (k_pow_step<<<nblk(L.A.n), kT, 0, P.stream>>>(L.A.n, L.dinv, w, v), SVXG_COUNT_LAUNCH());
+    (k_norm_scale<<<1, kT, 0, P.stream>>>(m, v, nv), SVXG_COUNT_LAUNCH());
   }
   double h = 0.0;
   cudaMemcpyAsync(&h, nv, sizeof(double), cudaMemcpyDeviceToHost, P.stream);
@@ -308,14 +308,14 @@ int smooth(Problem& P, const Level& L, const float* b, float* x, bool from_zero,
   StepArgs s{};
   s.D = L.dinv32;
   if (from_zero) {
-    k_cheb_first<<<nblk(n), kT, 0, st>>>(n, L.dinv32, b, C.inv_theta, d0);
+    (k_cheb_first<<<nblk(n), kT, 0, st>>>(n, L.dinv32, b, C.inv_theta, d0), SVXG_COUNT_LAUNCH());
     s.rin = b;
   } else {
     s.rin = b;
     s.r = L.r32;
     s.dout = d0;
     s.c2 = C.inv_theta;
-    k_bsr32<kPostStart><<<rblk(n), kT, 0, st>>>(n, L.A.rowptr, L.A.col, L.A.val32, x, nullptr, s);
+    (k_bsr32<kPostStart><<<rblk(n), kT, 0, st>>>(n, L.A.rowptr, L.A.col, L.A.val32, x, nullptr, s), SVXG_COUNT_LAUNCH());
     s.rin = L.r32;
   }
   for (int i = 1; i < degree; ++i) {
@@ -326,7 +326,7 @@ int smooth(Problem& P, const Level& L, const float* b, float* x, bool from_zero,
     s.c2 = C.c2[i];
     s.x_init = (from_zero && i == 1) ? 1 : 0;
     s.x_last = (i == degree - 1 && !(from_zero && want_residual)) ? 1 : 0;
-    k_bsr32<kStep><<<rblk(n), kT, 0, st>>>(n, L.A.rowptr, L.A.col, L.A.val32, d0, nullptr, s);
+    (k_bsr32<kStep><<<rblk(n), kT, 0, st>>>(n, L.A.rowptr, L.A.col, L.A.val32, d0, nullptr, s), SVXG_COUNT_LAUNCH());
     s.rin = L.r32;
     std::swap(d0, d1);
   }
@@ -337,12 +337,12 @@ int smooth(Problem& P, const Level& L, const float* b, float* x, bool from_zero,
     if (degree == 1) {
       SVXG_CUDA(cudaMemsetAsync(x, 0, sizeof(float) * 6 * size_t(n), st));
     }
-    k_bsr32<kResPend><<<rblk(n), kT, 0, st>>>(n, L.A.rowptr, L.A.col, L.A.val32, d0, nullptr, s);
+    (k_bsr32<kResPend><<<rblk(n), kT, 0, st>>>(n, L.A.rowptr, L.A.col, L.A.val32, d0, nullptr, s), SVXG_COUNT_LAUNCH());
   } else if (degree == 1) {
     if (from_zero) {
       SVXG_CUDA(cudaMemcpyAsync(x, d0, sizeof(float) * 6 * size_t(n), cudaMemcpyDeviceToDevice, st));
     } else {
-      k_add<<<nblk(6 * int64_t(n)), kT, 0, st>>>(6 * int64_t(n), d0, x);
+      (k_add<<<nblk(6 * int64_t(n)), kT, 0, st>>>(6 * int64_t(n), d0, x), SVXG_COUNT_LAUNCH());
     }
   }
   return SVXG_OK;
@@ -355,8 +355,8 @@ int cycle(Problem& P, size_t l, const float* b, float* x) {
   if (l + 1 == P.lv.size()) {
     if (P.chol_n > 0) {
       const int32_t m = P.chol_n;
-      k_dense_mv<<<rblk(m), kT, 0, st>>>(m, P.d_cinv, b, nullptr, P.d_cvec, nullptr);
-      k_dense_mv<<<rblk(m), kT, 0, st>>>(m, P.d_cinv + int64_t(m) * m, nullptr, P.d_cvec, nullptr, x);
+      (k_dense_mv<<<rblk(m), kT, 0, st>>>(m, P.d_cinv, b, nullptr, P.d_cvec, nullptr), SVXG_COUNT_LAUNCH());
+      (k_dense_mv<<<rblk(m), kT, 0, st>>>(m, P.d_cinv + int64_t(m) * m, nullptr, P.d_cvec, nullptr, x), SVXG_COUNT_LAUNCH());
       return SVXG_OK;
     }
     return smooth(P, L, b, x, true, kCoarseDegree, 30.0, false);
@@ -365,10 +365,10 @@ int cycle(Problem& P, size_t l, const float* b, float* x) {
   const Level& C = P.lv[l + 1];
   StepArgs none{};
   // restriction: bc = P^T r
-  k_bsr32<kY><<<rblk(C.A.n), kT, 0, st>>>(C.A.n, L.rrow, L.rent_i, L.pval32 + 36 * L.pnnz, L.r32, C.b32, none);
+  (k_bsr32<kY><<<rblk(C.A.n), kT, 0, st>>>(C.A.n, L.rrow, L.rent_i, L.pval32 + 36 * L.pnnz, L.r32, C.b32, none), SVXG_COUNT_LAUNCH());
   TRY(cycle(P, l + 1, C.b32, C.x32));
   // prolongation: x += P xc
-  k_bsr32<kAcc><<<rblk(n), kT, 0, st>>>(n, L.prow, L.pcol, L.pval32, C.x32, x, none);
+  (k_bsr32<kAcc><<<rblk(n), kT, 0, st>>>(n, L.prow, L.pcol, L.pval32, C.x32, x, none), SVXG_COUNT_LAUNCH());
   TRY(smooth(P, L, b, x, false, kChebDegree, kChebRatio, false));
   return SVXG_OK;
 }
@@ -382,16 +382,16 @@ int prepare_cycle(Problem& P) {
     const int32_t n = L.A.n;
     if (!L.A.val32) {
       TRY(P.mem.alloc(&L.A.val32, 36 * size_t(L.A.nnzb)));
-      k_cvt<<<nblk(36 * L.A.nnzb), kT, 0, st>>>(36 * L.A.nnzb, L.A.val, L.A.val32);
+      (k_cvt<<<nblk(36 * L.A.nnzb), kT, 0, st>>>(36 * L.A.nnzb, L.A.val, L.A.val32), SVXG_COUNT_LAUNCH());
       if (l == 0) P.K.val32 = L.A.val32;
     }
     TRY(P.mem.alloc(&L.dinv32, 36 * size_t(n)));
-    k_cvt<<<nblk(36 * int64_t(n)), kT, 0, st>>>(36 * int64_t(n), L.dinv, L.dinv32);
+    (k_cvt<<<nblk(36 * int64_t(n)), kT, 0, st>>>(36 * int64_t(n), L.dinv, L.dinv32), SVXG_COUNT_LAUNCH());
     if (L.pnnz > 0 && l + 1 < P.lv.size()) {
       // P blocks by fine row, then P^T blocks in restriction order
       TRY(P.mem.alloc(&L.pval32, 72 * size_t(L.pnnz)));
-      k_cvt<<<nblk(36 * L.pnnz), kT, 0, st>>>(36 * L.pnnz, L.pval, L.pval32);
-      k_cvt_transpose<<<nblk(L.pnnz), kT, 0, st>>>(L.pnnz, L.rent_e, L.pval, L.pval32 + 36 * L.pnnz);
+      (k_cvt<<<nblk(36 * L.pnnz), kT, 0, st>>>(36 * L.pnnz, L.pval, L.pval32), SVXG_COUNT_LAUNCH());
+      (k_cvt_transpose<<<nblk(L.pnnz), kT, 0, st>>>(L.pnnz, L.rent_e, L.pval, L.pval32 + 36 * L.pnnz), SVXG_COUNT_LAUNCH());
     }
     for (float** v : {&L.b32, &L.x32, &L.r32, &L.t32, &L.u32}) TRY(P.mem.alloc(v, 6 * size_t(std::max(n, 1))));
     const bool last = l + 1 == P.lv.size();
@@ -404,7 +404,7 @@ int prepare_cycle(Problem& P) {
     const int32_t m = P.chol_n;
     TRY(P.mem.alloc(&P.d_cinv, 2 * size_t(m) * size_t(m)));
     TRY(P.mem.alloc(&P.d_cvec, 2 * size_t(m)));
-    k_tri_inverse<<<nblk(m, 64), 64, 0, st>>>(m, P.d_chol, P.d_cinv, P.d_cinv + int64_t(m) * m);
+    (k_tri_inverse<<<nblk(m, 64), 64, 0, st>>>(m, P.d_chol, P.d_cinv, P.d_cinv + int64_t(m) * m), SVXG_COUNT_LAUNCH());
   }
   SVXG_CUDA(cudaGetLastError());
   return SVXG_OK;
@@ -416,9 +416,9 @@ int vcycle(Problem& P, const double* r, double* z) {
   cudaStream_t st = P.stream;
   Level& L0 = P.lv[0];
   const int64_t m = 6 * int64_t(L0.A.n);
-  k_cvt<<<nblk(m), kT, 0, st>>>(m, r, L0.b32);
+  (k_cvt<<<nblk(m), kT, 0, st>>>(m, r, L0.b32), SVXG_COUNT_LAUNCH());
   TRY(cycle(P, 0, L0.b32, L0.x32));
-  k_widen<<<nblk(m), kT, 0, st>>>(m, L0.x32, z);
+  (k_widen<<<nblk(m), kT, 0, st>>>(m, L0.x32, z), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   return SVXG_OK;
 }
