@@ -1,0 +1,171 @@
+// svxg_stress_problem.hpp - C++20 host class with svx::StressProblem's interface over the C ABI.
+//
+// The reference's callers hold a `StressProblem` (core/include/svx/stress/stress.hpp:74-160):
+// public `nodes`, `bonds`, `mats`, then assemble / solve / begin / iterate / current /
+// bond_load / remove_bond / retire_nodes / release and the work counters. This class keeps that
+// shape over include/svxg.h so a host written against the reference reads the same; every number
+// comes from the CUDA library. Records are svxg_node / svxg_bond (byte images of SNode / SBond,
+// include/svxg_types.h); `mats` is a table of SVXG_MAX_MATERIALS resolved entries.
+//
+// Like the reference, callers may change `nodes` and `bonds` between calls: the graph is sent to
+// the device at assemble(), and again before a solve when its contents changed since (which, as
+// assembling again would, drops the assembled operator).
+#pragma once
+
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "svxg.h"
+
+namespace svxg {
+
+class StressProblem {
+ public:
+  std::vector<svxg_node> nodes;
+  std::vector<svxg_bond> bonds;
+  std::vector<svxg_material> mats;  // SVXG_MAX_MATERIALS entries
+
+  explicit StressProblem(int device = 0) {
+    if (svxg_problem_create(&p_, device) != SVXG_OK) throw std::runtime_error(svxg_last_error());
+  }
+  ~StressProblem() { svxg_problem_destroy(p_); }
+  StressProblem(const StressProblem&) = delete;
+  StressProblem& operator=(const StressProblem&) = delete;
+
+  // stress.hpp:83 - K and the preconditioner; false on a singular diagonal
+  bool assemble(const svxg_stress_options& opt = svxg_default_options()) {
+    upload();
+    int32_t ok = 0;
+    check(svxg_assemble(p_, &opt, &ok));
+    pull_flags();
+    return ok != 0;
+  }
+  bool assembled() const { return svxg_assembled(p_) != 0; }
+  void invalidate() { check(svxg_invalidate(p_)); }
+  bool preconditioner_current() const { return svxg_preconditioner_current(p_) != 0; }
+  bool block_jacobi() const { return svxg_block_jacobi(p_) != 0; }
+  int64_t assembly_work() const { return info().assembly_work; }
+  void release() {
+    check(svxg_release(p_));
+    for (auto& b : bonds) b.in_k = 0;
+    sent_bonds_ = bonds;
+  }
+  void remove_bond(int32_t b) {
+    check(svxg_remove_bond(p_, b));
+    pull_flags();
+  }
+  void retire_nodes(const std::vector<int32_t>& list) {
+    check(svxg_retire_nodes(p_, list.data(), int32_t(list.size())));
+    for (int32_t i : list) nodes[size_t(i)].gone = 1;
+    sent_nodes_ = nodes;
+    pull_flags();
+  }
+  int32_t free_nodes() const { return info().nfree; }
+  int64_t matrix_blocks() const { return info().matrix_blocks; }
+  int64_t memory_bytes() const { return info().device_bytes; }
+  int64_t work_per_iteration() const { return info().work_per_iteration; }
+
+  // stress.hpp:122 - f, u: 6 per node; u: warm start in, solution out; maxit < 0: no cap
+  svxg_pcg_result solve(const std::vector<double>& f, std::vector<double>& u, double rtol, int maxit, bool warm) {
+    upload_if_changed();
+    u.resize(6 * nodes.size(), 0.0);
+    svxg_pcg_result r{};
+    check(svxg_solve(p_, f.data(), u.data(), rtol, maxit, warm ? 1 : 0, &r));
+    pull_flags();
+    return r;
+  }
+  void begin(const std::vector<double>& f, const std::vector<double>& u0) {
+    upload_if_changed();
+    check(svxg_begin(p_, f.data(), u0.size() == 6 * nodes.size() ? u0.data() : nullptr));
+  }
+  svxg_pcg_result iterate(int maxit, double rtol) {
+    svxg_pcg_result r{};
+    check(svxg_iterate(p_, maxit, rtol, &r));
+    return r;
+  }
+  bool running() const { return svxg_running(p_) != 0; }
+  void stop() { check(svxg_stop(p_)); }
+  void current(std::vector<double>& u) const {
+    u.assign(6 * nodes.size(), 0.0);
+    check(svxg_current(p_, u.data()));
+  }
+
+  // stress.hpp:132 - one bond's load at u (the device evaluates every bond; see bond_loads)
+  svxg_bond_load bond_load(int32_t b, const std::vector<double>& u) const { return bond_loads(u)[size_t(b)]; }
+  std::vector<svxg_bond_load> bond_loads(const std::vector<double>& u) const {
+    std::vector<svxg_bond_load> out(bonds.size());
+    check(svxg_bond_loads(p_, u.data(), out.data()));
+    return out;
+  }
+  // bond_utilization (stress.hpp:64-66) of every bond at the current solution; failing bonds
+  struct Judgement {
+    std::vector<double> phi;
+    std::vector<uint8_t> mode;
+    std::vector<int32_t> failing;
+  };
+  Judgement judge(double fragility) const {
+    Judgement j;
+    j.phi.resize(bonds.size());
+    j.mode.resize(bonds.size());
+    j.failing.resize(bonds.size() + 1);
+    int32_t n = 0;
+    check(svxg_utilization(p_, fragility, j.phi.data(), j.mode.data(), j.failing.data(), int32_t(j.failing.size()),
+                           &n));
+    j.failing.resize(size_t(n));
+    return j;
+  }
+
+  // stress.hpp:134 - a force F at point `at` on a node with centre c
+  static void add_force(std::vector<double>& f, int32_t node, svxg_v3 c, svxg_v3 F, svxg_v3 at) {
+    double* fi = &f[6 * size_t(node)];
+    fi[0] += F.x;
+    fi[1] += F.y;
+    fi[2] += F.z;
+    const double rx = at.x - c.x, ry = at.y - c.y, rz = at.z - c.z;
+    fi[3] += ry * F.z - rz * F.y;
+    fi[4] += rz * F.x - rx * F.z;
+    fi[5] += rx * F.y - ry * F.x;
+  }
+
+  svxg_info info() const {
+    svxg_info i{};
+    check(svxg_get_info(p_, &i));
+    return i;
+  }
+  svxg_problem* handle() const { return p_; }
+
+ private:
+  static void check(int code) {
+    if (code < 0) throw std::runtime_error(std::string("svxg: ") + svxg_last_error());
+  }
+  void upload() {
+    if (mats.size() != SVXG_MAX_MATERIALS) throw std::runtime_error("svxg: mats needs every material id");
+    check(svxg_set_graph(p_, nodes.data(), int32_t(nodes.size()), bonds.data(), int32_t(bonds.size()), mats.data()));
+    sent_nodes_ = nodes;
+    sent_bonds_ = bonds;
+  }
+  static bool same(const void* a, const void* b, size_t n) { return n == 0 || std::memcmp(a, b, n) == 0; }
+  void upload_if_changed() {
+    if (nodes.size() != sent_nodes_.size() || bonds.size() != sent_bonds_.size() ||
+        !same(nodes.data(), sent_nodes_.data(), nodes.size() * sizeof(svxg_node)) ||
+        !same(bonds.data(), sent_bonds_.data(), bonds.size() * sizeof(svxg_bond)))
+      upload();
+  }
+  void pull_flags() {
+    std::vector<uint8_t> br(bonds.size()), ik(bonds.size());
+    check(svxg_bond_flags(p_, br.data(), ik.data()));
+    for (size_t k = 0; k < bonds.size(); ++k) {
+      bonds[k].broken = br[k];
+      bonds[k].in_k = ik[k];
+    }
+    sent_bonds_ = bonds;
+  }
+  svxg_problem* p_ = nullptr;
+  std::vector<svxg_node> sent_nodes_;
+  std::vector<svxg_bond> sent_bonds_;
+};
+
+}  // namespace svxg

@@ -1,0 +1,171 @@
+// test_adapter.cpp - the C++20 host class (include/svxg_stress_problem.hpp) on the device, with the
+// reference's own test cases written as the reference writes them (tests/core/test_stress.cpp).
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include "svxg_stress_problem.hpp"
+
+namespace {
+
+int failures = 0;
+#define CHECK(c)                                                        \
+  do {                                                                  \
+    if (!(c)) {                                                         \
+      std::printf("FAILED %s:%d: %s\n", __FILE__, __LINE__, #c);        \
+      ++failures;                                                       \
+    }                                                                   \
+  } while (0)
+
+bool approx(double a, double b, double eps) { return std::fabs(a - b) <= eps * std::fmax(std::fabs(a), std::fabs(b)); }
+
+std::vector<svxg_material> materials() {
+  // the presets the cases use: rc (id 0, also every unregistered id) and concrete (id 1)
+  std::vector<svxg_material> m(SVXG_MAX_MATERIALS, svxg_material{30e9, 12.5e9, 2400, 1.2e6, 3.5e6, 30e6, 1.6e6, 0.7});
+  m[1] = svxg_material{28e9, 11.5e9, 2300, 0.8e6, 1.2e6, 25e6, 1.2e6, 0.7};
+  return m;
+}
+
+// test_stress.cpp:14-32
+svxg_bond bond(const svxg::StressProblem& P, int32_t A, int32_t B, svxg_v3 n, svxg_v3 p, double a) {
+  svxg_bond s{};
+  s.a = A;
+  s.b = B;
+  s.ma = s.mb = 1;
+  s.n = n;
+  s.t1 = std::fabs(n.x) > 0.5 ? svxg_v3{0, 1, 0} : svxg_v3{1, 0, 0};
+  s.t2 = {n.y * s.t1.z - n.z * s.t1.y, n.z * s.t1.x - n.x * s.t1.z, n.x * s.t1.y - n.y * s.t1.x};
+  s.area = a * a;
+  s.p = p;
+  s.s1 = s.s2 = a * a * a * a / 12.0;
+  s.c1 = s.c2 = 0.5 * a;
+  s.rmax = std::sqrt(0.5) * a;
+  const svxg_v3 ca = P.nodes[size_t(A)].c;
+  s.la = std::fabs((p.x - ca.x) * n.x + (p.y - ca.y) * n.y + (p.z - ca.z) * n.z);
+  if (B >= 0) {
+    const svxg_v3 cb = P.nodes[size_t(B)].c;
+    s.lb = std::fabs((cb.x - p.x) * n.x + (cb.y - p.y) * n.y + (cb.z - p.z) * n.z);
+  } else {
+    s.lb = s.la;
+  }
+  s.strength = 1.0;
+  s.faces = 16;
+  s.tag = -1;
+  return s;
+}
+
+// test_stress.cpp:35-46
+void cantilever(svxg::StressProblem& P, int n, double L, double mass) {
+  P.mats = materials();
+  for (int i = 0; i < n; ++i) {
+    svxg_node nd{};
+    nd.c = {(i + 0.5) * L, 0, 0};
+    nd.mass = mass;
+    P.nodes.push_back(nd);
+  }
+  P.bonds.push_back(bond(P, 0, -1, {-1, 0, 0}, {0, 0, 0}, L));
+  for (int i = 0; i + 1 < n; ++i) P.bonds.push_back(bond(P, i, i + 1, {1, 0, 0}, {(i + 1) * L, 0, 0}, L));
+}
+
+std::vector<double> gravity(const svxg::StressProblem& P) {
+  std::vector<double> f(6 * P.nodes.size(), 0.0);
+  for (size_t i = 0; i < P.nodes.size(); ++i) f[6 * i + 2] = -9.81 * P.nodes[i].mass;
+  return f;
+}
+
+double shear(const svxg_bond_load& L) { return std::sqrt(L.V1 * L.V1 + L.V2 * L.V2); }
+double moment(const svxg_bond_load& L) { return std::sqrt(L.M1 * L.M1 + L.M2 * L.M2); }
+
+}  // namespace
+
+int main() {
+  {  // test_stress.cpp:59-87: a cantilever carries its weight to the support (statics, exactly)
+    const int n = 12;
+    const double L = 0.5, m = 300.0;
+    svxg::StressProblem P;
+    cantilever(P, n, L, m);
+    svxg_stress_options so = svxg_default_options();
+    so.amg_min_nodes = 4;
+    CHECK(P.assemble(so));
+    std::vector<double> u;
+    const svxg_pcg_result r = P.solve(gravity(P), u, 1e-10, 500, false);
+    CHECK(r.converged);
+    const svxg_bond_load root = P.bond_load(0, u);
+    double W = 0.0, M = 0.0;
+    for (int i = 0; i < n; ++i) {
+      W += 9.81 * m;
+      M += 9.81 * m * (i + 0.5) * L;
+    }
+    CHECK(approx(shear(root), W, 1e-6));
+    CHECK(approx(moment(root), M, 1e-6));
+    CHECK(std::fabs(root.N) < 1e-6 * W);
+    const svxg_bond_load tip = P.bond_load(n - 1, u);
+    CHECK(approx(shear(tip), 9.81 * m, 1e-6));
+    CHECK(approx(moment(tip), 9.81 * m * 0.5 * L, 1e-6));
+    const auto j = P.judge(1.0);
+    CHECK(j.phi[0] > 50.0 * j.phi[size_t(n - 1)]);
+  }
+  {  // test_stress.cpp:154-174: removing a bond in place equals assembling without it
+    svxg::StressProblem A, B;
+    cantilever(A, 10, 0.5, 200.0);
+    cantilever(B, 10, 0.5, 200.0);
+    A.bonds.push_back(bond(A, 6, -1, {0, 0, -1}, {A.nodes[6].c.x, 0, -0.25}, 0.5));
+    B.bonds.push_back(bond(B, 6, -1, {0, 0, -1}, {B.nodes[6].c.x, 0, -0.25}, 0.5));
+    svxg_stress_options so = svxg_default_options();
+    so.amg_min_nodes = 1 << 30;
+    CHECK(A.assemble(so));
+    A.remove_bond(3);
+    B.bonds[3].broken = 1;
+    CHECK(B.assemble(so));
+    std::vector<double> ua, ub;
+    A.solve(gravity(A), ua, 1e-11, 2000, false);
+    B.solve(gravity(B), ub, 1e-11, 2000, false);
+    double err = 0.0, mag = 0.0;
+    for (size_t k = 0; k < ua.size(); ++k) {
+      err = std::fmax(err, std::fabs(ua[k] - ub[k]));
+      mag = std::fmax(mag, std::fabs(ub[k]));
+    }
+    CHECK(err <= 1e-6 * mag);
+    CHECK(A.bonds[3].broken == 1 && A.bonds[3].in_k == 0);
+  }
+  {  // test_stress.cpp:293-305: no answer for non-finite loads, u = 0 for none
+    svxg::StressProblem P;
+    cantilever(P, 6, 0.5, 100.0);
+    CHECK(P.assemble());
+    std::vector<double> u(6 * P.nodes.size(), 1.0), f(6 * P.nodes.size(), 0.0);
+    const svxg_pcg_result r0 = P.solve(f, u, 1e-9, 100, true);
+    CHECK(r0.converged);
+    for (double v : u) CHECK(v == 0.0);
+    f[2] = NAN;
+    const svxg_pcg_result r1 = P.solve(f, u, 1e-9, 100, false);
+    CHECK(!r1.converged);
+    CHECK(r1.breakdown);
+  }
+  {  // begin / iterate: the same conjugate-gradient sequence over several calls
+    svxg::StressProblem P;
+    cantilever(P, 40, 0.5, 100.0);
+    svxg_stress_options so = svxg_default_options();
+    so.amg_min_nodes = 1 << 30;
+    CHECK(P.assemble(so));
+    P.begin(gravity(P), {});
+    int total = 0;
+    svxg_pcg_result r{};
+    for (int t = 0; t < 100 && !r.converged; ++t) {
+      r = P.iterate(3, 1e-10);
+      total += r.iters;
+    }
+    CHECK(r.converged);
+    std::vector<double> u1, u2;
+    P.current(u1);
+    const svxg_pcg_result once = P.solve(gravity(P), u2, 1e-10, 1000, false);
+    CHECK(once.iters == total);
+    double err = 0.0, mag = 0.0;
+    for (size_t k = 0; k < u1.size(); ++k) {
+      err = std::fmax(err, std::fabs(u1[k] - u2[k]));
+      mag = std::fmax(mag, std::fabs(u2[k]));
+    }
+    CHECK(err <= 1e-12 * mag);
+  }
+  std::printf(failures ? "%d failures\n" : "ok\n", failures);
+  return failures ? 1 : 0;
+}

@@ -1,0 +1,64 @@
+"""Writes the golden fixtures under tests/golden/ from the reference itself.
+
+Runs only where the reference tree is present (the reference is compiled from its own sources by
+oracle/build_oracle.py into oracle/_ref/). For each case it stores the input graph and the
+reference StressProblem's outputs: u (solved to rtol 1e-12), the PCG result, the hierarchy and
+work counters, and every bond's load, utilization and mode. tests/test_oracle_golden.py checks the
+oracle against them on any machine, bit for bit.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+for p in (ROOT, os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import fixtures as fx  # noqa: E402
+from opus_destruct_2_gb300 import synth  # noqa: E402
+from opus_destruct_2_gb300.graph import StressOptions, default_materials  # noqa: E402
+from oracle import Reference, reference_lib  # noqa: E402
+
+CASES = {
+    "cantilever12": (lambda: fx.cantilever(12, 0.5, 300.0), dict(amg_min_nodes=4)),
+    "lattice8_amg": (lambda: fx.lattice(8), dict(amg_min_nodes=16)),
+    "lattice8_jacobi": (lambda: fx.lattice(8), dict(amg_min_nodes=1 << 30)),
+    "lattice12_retired": (lambda: fx.lattice(12, keep_z=8, retire_top=True), dict(amg_min_nodes=16)),
+    "tower3": (lambda: synth.tower_graph(storeys=3, seed=3)[:2], dict()),
+    "piece_free": (lambda: synth.piece_graph(400, free=True, seed=31)[:2], dict(amg_min_nodes=0)),
+}
+
+
+def main():
+    if reference_lib() is None:
+        raise SystemExit("the reference is not built here")
+    mats = default_materials()
+    for name, (make, opts) in CASES.items():
+        nodes, bonds = make()
+        f = fx.gravity_live(nodes)
+        opt = StressOptions(**opts)
+        R = Reference(nodes, bonds, mats)
+        r = R.solve(f, opt, rtol=1e-12, maxit=5000)
+        loads, phi, mode = R.judge(r["u"])
+        info = r["info"]
+        np.savez_compressed(
+            os.path.join(HERE, f"{name}.npz"),
+            nodes=nodes, bonds=bonds, mats=mats, f=f, u=r["u"], loads=loads, phi=phi, mode=mode,
+            iters=r["res"].iters, rel_res=r["res"].rel_res, converged=r["res"].converged,
+            level_sizes=np.array(info.sizes(), np.int64), level_blocks=np.array(info.blocks(), np.int64),
+            counters=np.array([info.nfree, info.chol_n, info.matrix_blocks, info.work_per_iteration,
+                               info.assembly_work, info.work_per_apply, info.build_work], np.int64),
+            opts=np.array([opt.amg_min_nodes, opt.amg.smoothed, opt.amg.reaggregate, opt.amg.coarsen_dense],
+                          np.int64))
+        print(name, len(nodes), len(bonds), r["res"], info.sizes())
+
+
+if __name__ == "__main__":
+    main()
