@@ -179,6 +179,7 @@ def main():
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--rtol", type=float, default=1e-8)
     ap.add_argument("--maxit", type=int, default=500)
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -218,7 +219,7 @@ def main():
     h = ctypes.c_void_p()
     check(L.svxg_problem_create(ctypes.byref(h), local_rank))
     stream = torch.cuda.ExternalStream(L.svxg_problem_stream(h), device=dev)
-    opt = StressOptions(amg_min_nodes=160)
+    opt = StressOptions(amg_min_nodes=160, precision=1 if args.precision == "mixed" else 0)
     ok = ctypes.c_int32()
     res = PcgResult()
     n_over = ctypes.c_int32()
@@ -346,11 +347,13 @@ def main():
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64",
+        "dtype": "f64" if args.precision == "fp64" else "f32+f64",
         "data": "synthetic",
         "config": {"workload": desc, "nodes": int(n), "bonds": int(nb), "dof": int(6 * nfree), "blocks": int(nnzb),
                    "levels": info.sizes(), "rtol": args.rtol, "pcg_iters": int(iters), "failing_bonds": int(info_fail),
-                   "precision": "fp64 K and CG, f32 V-cycle", "step": "assemble + multigrid build + PCG + judge",
+                   "precision": ("fp64 K and CG, f32 V-cycle" if args.precision == "fp64" else
+                                 "f32 K SpMV and V-cycle inside fp64 refinement (fp64 residual, dots, coarsest)"),
+                   "step": "assemble + multigrid build + PCG + judge",
                    "l2": "inputs larger than L2 (K alone is %.0f MB)" % (nnzb * 288 / 1e6),
                    "parallelism": f"replicas x{world}"},
         "roofline": {"kernel": "conjugate-gradient SpMV (FP64 BSR 6x6, p.q fused)", "bound": "hbm",

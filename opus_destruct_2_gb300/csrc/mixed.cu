@@ -1,0 +1,310 @@
+// mixed.cu - the mixed-precision solve: FP32 K and FP32 V-cycle inside FP64 iterative refinement.
+//
+//   outer (FP64):  r = f - K x   (K in FP64, the exact residual), stop when ||r|| <= rtol ||f||
+//   inner (FP32):  K32 d = r32 by AMG-preconditioned CG to ||r_in|| <= tol_in ||r32||, from d = 0:
+//                  SpMV and the V-cycle in FP32 (K32 is K rounded to f32, the cycle's own level-0
+//                  operator), dot products accumulated in FP64
+//   update (FP64): x += d
+// FP64 stays where the benchmark spec keeps it: the outer residual, the dots and the coarsest dense
+// factor. The refinement converges to the FP64 solution (its residual is the FP64 K's), so the
+// result meets the same rtol as the plain FP64 solve; each inner iteration reads half the bytes
+// of an FP64 one and issues FP32 arithmetic (GB300's FP64 rate is a small fraction of FP32).
+#include <cmath>
+
+#include "problem.cuh"
+
+namespace svxg {
+namespace {
+
+constexpr int kT = 256;
+constexpr int kRows = kT / 32;
+inline unsigned vblk(int32_t n) { return unsigned((std::max(n, 1) + kT - 1) / kT); }
+inline unsigned rblk(int32_t n) { return unsigned((std::max(n, 1) + kRows - 1) / kRows); }
+
+#define TRY(x)            \
+  do {                    \
+    int e__ = (x);        \
+    if (e__) return e__;  \
+  } while (0)
+
+struct MixedScalars {
+  double rz, pq, alpha, beta, rn_in, target_in, rr;
+  int32_t iters, done, breakdown, pad;
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+  return v;
+}
+
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < int(blockDim.x) / 32; ++i) s += sh[i];
+  return s;
+}
+
+// last-block reduction (as solve.cu): true in every thread of the last block, total in tot
+__device__ __forceinline__ bool reduce_last(double v, double* partials, unsigned* counter, double* tot) {
+  __shared__ double sh[32];
+  __shared__ bool last;
+  const double bs = block_sum(v, sh);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = bs;
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double s = 0.0;
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) s += __ldcg(&partials[b]);
+  const double t = block_sum(s, sh);
+  if (threadIdx.x == 0) {
+    *tot = t;
+    *counter = 0u;
+  }
+  return true;
+}
+
+// y32 = K32 p32 (warp per row), p.y accumulated in f64 -> alpha
+__global__ void __launch_bounds__(kT) k_spmv32_dot(int32_t n, const int32_t* __restrict__ rowptr,
+                                                   const int32_t* __restrict__ col, const float* __restrict__ val,
+                                                   const float* __restrict__ p, float* __restrict__ q,
+                                                   double* partials, unsigned* counter, MixedScalars* s) {
+  if (s->done) return;
+  const int lane = threadIdx.x & 31;
+  const int32_t row = blockIdx.x * kRows + (threadIdx.x >> 5);
+  const int g = lane / 6, c = lane - 6 * (lane / 6);
+  float acc = 0.0f;
+  if (row < n && g < 5) {
+    const int32_t k1 = rowptr[row + 1];
+    for (int32_t k = rowptr[row] + g; k < k1; k += 5) {
+      const float2* m = reinterpret_cast<const float2*>(val + 36 * int64_t(k) + 6 * c);
+      const float2* xv = reinterpret_cast<const float2*>(p + 6 * int64_t(__ldg(col + k)));
+      const float2 a = __ldg(m), b = __ldg(m + 1), d = __ldg(m + 2);
+      const float2 u = __ldg(xv), v = __ldg(xv + 1), w = __ldg(xv + 2);
+      acc += a.x * u.x + a.y * u.y + b.x * v.x + b.y * v.y + d.x * w.x + d.y * w.y;
+    }
+  }
+  const float a1 = __shfl_sync(0xffffffffu, acc, (c + 6) & 31);
+  const float a2 = __shfl_sync(0xffffffffu, acc, (c + 12) & 31);
+  const float a3 = __shfl_sync(0xffffffffu, acc, (c + 18) & 31);
+  const float a4 = __shfl_sync(0xffffffffu, acc, (c + 24) & 31);
+  const float y = acc + a1 + a2 + a3 + a4;
+  double dp = 0.0;
+  if (row < n && lane < 6) {
+    q[6 * int64_t(row) + lane] = y;
+    dp = double(p[6 * int64_t(row) + lane]) * double(y);
+  }
+  double tot;
+  if (reduce_last(dp, partials, counter, &tot) && threadIdx.x == 0) {
+    s->pq = tot;
+    s->iters += 1;
+    if (!(tot > 0)) {
+      s->breakdown = 1;
+      s->done = 1;
+    } else {
+      s->alpha = s->rz / tot;
+    }
+  }
+}
+
+// d += alpha p, r -= alpha q (f32), ||r|| in f64 -> inner convergence
+__global__ void k_axpy32(int32_t nf, float* __restrict__ d, float* __restrict__ r, const float* __restrict__ p,
+                         const float* __restrict__ q, double* partials, unsigned* counter, MixedScalars* s) {
+  if (s->done) return;
+  const float a = float(s->alpha);
+  const int64_t i = int64_t(blockIdx.x) * kT + threadIdx.x;
+  double rr = 0.0;
+  if (i < nf)
+    for (int c = 0; c < 6; ++c) {
+      const int64_t k = 6 * i + c;
+      d[k] += a * p[k];
+      const float rv = r[k] - a * q[k];
+      r[k] = rv;
+      rr += double(rv) * double(rv);
+    }
+  double tot;
+  if (reduce_last(rr, partials, counter, &tot) && threadIdx.x == 0) {
+    s->rn_in = sqrt(tot);
+    if (s->rn_in <= s->target_in) s->done = 1;
+  }
+}
+
+// r.z (f64 accumulation); MODE 0: start (rz, p = z), 1: iteration (beta)
+template <int MODE>
+__global__ void k_rz32(int32_t nf, const float* __restrict__ r, const float* __restrict__ z, float* p, double* partials,
+                       unsigned* counter, MixedScalars* s, int32_t maxit) {
+  if (MODE == 1 && s->done) return;
+  const int64_t i = int64_t(blockIdx.x) * kT + threadIdx.x;
+  double rz = 0.0;
+  if (i < nf)
+    for (int c = 0; c < 6; ++c) {
+      const float zv = z[6 * i + c];
+      rz += double(r[6 * i + c]) * double(zv);
+      if (MODE == 0) p[6 * i + c] = zv;
+    }
+  double tot;
+  if (reduce_last(rz, partials, counter, &tot) && threadIdx.x == 0) {
+    if (MODE == 0) {
+      s->rz = tot;
+      if (!(tot > 0)) {
+        s->breakdown = !(tot == 0.0);
+        s->done = 1;
+      }
+    } else if (!(tot > 0)) {
+      s->breakdown = 1;
+      s->done = 1;
+    } else {
+      s->beta = tot / s->rz;
+      s->rz = tot;
+    }
+    if (MODE == 1 && !s->done && s->iters >= maxit) s->done = 1;
+  }
+}
+
+__global__ void k_p32(int32_t nf, const float* __restrict__ z, float* __restrict__ p, const MixedScalars* s) {
+  if (s->done) return;
+  const float b = float(s->beta);
+  const int64_t i = int64_t(blockIdx.x) * kT + threadIdx.x;
+  if (i < nf)
+    for (int c = 0; c < 6; ++c) p[6 * i + c] = z[6 * i + c] + b * p[6 * i + c];
+}
+
+// outer: r64 = f - q64 (q64 = K x), ||r||^2 -> rr; r32 = f32(r64); inner state reset
+__global__ void k_outer_resid(int32_t nf, const double* __restrict__ f, const double* __restrict__ q,
+                              double* __restrict__ r64, float* __restrict__ r32, float* __restrict__ d,
+                              double* partials, unsigned* counter, MixedScalars* s, double tol_in) {
+  const int64_t i = int64_t(blockIdx.x) * kT + threadIdx.x;
+  double rr = 0.0;
+  if (i < nf)
+    for (int c = 0; c < 6; ++c) {
+      const int64_t k = 6 * i + c;
+      const double rv = f[k] - q[k];
+      r64[k] = rv;
+      r32[k] = float(rv);
+      d[k] = 0.0f;
+      rr += rv * rv;
+    }
+  double tot;
+  if (reduce_last(rr, partials, counter, &tot) && threadIdx.x == 0) {
+    s->rr = tot;
+    s->target_in = tol_in * sqrt(tot);
+    s->done = 0;
+    s->breakdown = 0;
+  }
+}
+
+// x += d (f64 += f32)
+__global__ void k_outer_update(int32_t nf, double* __restrict__ x, const float* __restrict__ d) {
+  const int64_t i = int64_t(blockIdx.x) * kT + threadIdx.x;
+  if (i < nf)
+    for (int c = 0; c < 6; ++c) x[6 * i + c] += double(d[6 * i + c]);
+}
+
+}  // namespace
+
+// The mixed-precision run: x (FP64, free-DOF order, the warm start) and f are P's run vectors.
+int mixed_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) {
+  svxg_pcg_result out{};
+  const int32_t nf = P.nfree;
+  cudaStream_t st = P.stream;
+  const size_t m = 6 * size_t(std::max(nf, 1));
+  if (!P.d_mx) {
+    TRY(P.mem.alloc(&P.d_mx, 5 * m));  // d, r32, z32, p32, q32
+    MixedScalars* ms = nullptr;
+    TRY(P.mem.alloc(&ms, 1));
+    P.d_ms = ms;
+    SVXG_CUDA(cudaMallocHost(&P.h_ms, sizeof(MixedScalars)));
+  }
+  float* d = P.d_mx;
+  float* r32 = d + m;
+  float* z32 = d + 2 * m;
+  float* p32 = d + 3 * m;
+  float* q32 = d + 4 * m;
+  MixedScalars* s = static_cast<MixedScalars*>(P.d_ms);
+  MixedScalars* hs = static_cast<MixedScalars*>(P.h_ms);
+  const double tol_in = 1e-3;
+  double bn = 0.0;
+  {
+    // ||f|| from the begin() scalars
+    SVXG_CUDA(cudaMemcpyAsync(P.h_s, P.d_s, sizeof(PcgScalars), cudaMemcpyDeviceToHost, st));
+    SVXG_CUDA(cudaStreamSynchronize(st));
+    bn = P.h_s->bn;
+  }
+  const double target = rtol * bn;
+  int32_t used = 0;
+  if (!std::isfinite(bn)) {
+    out.rel_res = INFINITY;
+    out.breakdown = 1;
+    P.active = false;
+    if (res) *res = out;
+    return SVXG_OK;
+  }
+  for (int outer = 0; outer < 64; ++outer) {
+    // r = f - K x in FP64
+    TRY(spmv(P, P.K, P.d_x, P.d_q));
+    SVXG_CUDA(cudaMemsetAsync(s, 0, sizeof(MixedScalars), st));
+    (k_outer_resid<<<vblk(nf), kT, 0, st>>>(nf, P.d_f, P.d_q, P.d_r, r32, d, P.d_partials, P.d_counter, s, tol_in),
+     SVXG_COUNT_LAUNCH());
+    SVXG_CUDA(cudaMemcpyAsync(hs, s, sizeof(MixedScalars), cudaMemcpyDeviceToHost, st));
+    SVXG_CUDA(cudaStreamSynchronize(st));
+    const double rn = std::sqrt(hs->rr);
+    out.rel_res = bn > 0 ? rn / bn : 0.0;
+    if (!std::isfinite(rn)) {
+      out.rel_res = INFINITY;
+      out.breakdown = 1;
+      break;
+    }
+    if (rn <= target || !(bn > 0) || nf == 0) {
+      out.converged = 1;
+      break;
+    }
+    if (used >= maxit) break;
+    // inner CG from d = 0: z = M^-1 r32 (the f32 V-cycle), p = z
+    P.cycle_stop = &s->done;
+    TRY(vcycle32(P, r32, z32));
+    (k_rz32<0><<<vblk(nf), kT, 0, st>>>(nf, r32, z32, p32, P.d_partials, P.d_counter, s, maxit - used),
+     SVXG_COUNT_LAUNCH());
+    int32_t queued = 0, batch = 2;
+    for (;;) {
+      SVXG_CUDA(cudaMemcpyAsync(hs, s, sizeof(MixedScalars), cudaMemcpyDeviceToHost, st));
+      SVXG_CUDA(cudaStreamSynchronize(st));
+      if (hs->done || queued >= maxit - used) break;
+      const int32_t todo = std::min(batch, maxit - used - queued);
+      for (int32_t it = 0; it < todo; ++it) {
+        (k_spmv32_dot<<<rblk(nf), kT, 0, st>>>(nf, P.K.rowptr, P.K.col, P.K.val32, p32, q32, P.d_partials,
+                                               P.d_counter, s),
+         SVXG_COUNT_LAUNCH());
+        (k_axpy32<<<vblk(nf), kT, 0, st>>>(nf, d, r32, p32, q32, P.d_partials, P.d_counter, s), SVXG_COUNT_LAUNCH());
+        TRY(vcycle32(P, r32, z32));
+        (k_rz32<1><<<vblk(nf), kT, 0, st>>>(nf, r32, z32, nullptr, P.d_partials, P.d_counter, s, maxit - used),
+         SVXG_COUNT_LAUNCH());
+        (k_p32<<<vblk(nf), kT, 0, st>>>(nf, z32, p32, s), SVXG_COUNT_LAUNCH());
+      }
+      SVXG_CUDA(cudaGetLastError());
+      queued += todo;
+      batch = std::min(batch * 2, 32);
+    }
+    used += hs->iters;
+    (k_outer_update<<<vblk(nf), kT, 0, st>>>(nf, P.d_x, d), SVXG_COUNT_LAUNCH());
+    if (hs->breakdown && hs->iters == 0) {
+      out.breakdown = 1;
+      break;
+    }
+  }
+  P.cycle_stop = nullptr;
+  out.iters = used;
+  P.run_iters += used;
+  if (res) *res = out;
+  return SVXG_OK;
+}
+
+}  // namespace svxg

@@ -162,6 +162,10 @@ struct Problem {
   double* d_un = nullptr;         // node-order u then f (12 n), owned by the C ABI's calls
   PcgScalars* d_s = nullptr;
   PcgScalars* h_s = nullptr;      // pinned mirror
+  const int32_t* cycle_stop = nullptr;  // the running sequence's done flag: cycle kernels return at once when set
+  float* d_mx = nullptr;          // mixed precision: d, r, z, p, q in f32 (5 x 6 nfree)
+  void* d_ms = nullptr;           // mixed precision scalars (device)
+  void* h_ms = nullptr;           // ... pinned mirror
   double* d_partials = nullptr;   // block partial sums
   unsigned* d_counter = nullptr;  // last-block counters
   int32_t partial_blocks = 0;
@@ -194,6 +198,9 @@ int precondition(Problem& P, const double* r, double* z);
 int free_run(Problem& P);
 // vcycle.cu
 int vcycle(Problem& P, const double* r, double* z);
+int vcycle32(Problem& P, const float* r, float* z);
+// mixed.cu
+int mixed_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res);
 int prepare_cycle(Problem& P);
 // exact_judge.cu
 int bond_loads_device(Problem& P, const double* u_nodes, svxg_bond_load* out);

@@ -414,6 +414,12 @@ int free_run(Problem& P) {
   P.mem.release(P.d_q);
   P.mem.release(P.d_f);
   P.mem.release(P.d_s);
+  P.mem.release(P.d_mx);
+  {
+    void* ms = P.d_ms;
+    P.mem.release(ms);
+    P.d_ms = nullptr;
+  }
   P.mem.release(P.d_partials);
   P.mem.release(P.d_counter);
   P.active = false;
@@ -449,6 +455,8 @@ int pcg_begin(Problem& P, const double* f_nodes, const double* u0_nodes) {
     if (P.jacobi_only) {
       (k_jacobi_rz<0><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_jinv, P.d_r, P.d_z, P.d_p, P.d_partials,
                                                        P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
+    } else if (P.opt.precision == SVXG_PRECISION_MIXED) {
+      // (the mixed-precision run starts its own inner sequences from the FP64 residual)
     } else {
       TRY(vcycle(P, P.d_r, P.d_z));
       (k_rz<0><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_r, P.d_z, P.d_p, P.d_partials, P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
@@ -469,6 +477,8 @@ int pcg_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) {
   }
   const int32_t nf = P.nfree;
   cudaStream_t st = P.stream;
+  if (P.opt.precision == SVXG_PRECISION_MIXED && !P.jacobi_only) return mixed_iterate(P, maxit, rtol, res);
+  P.cycle_stop = &P.d_s->done;
   (k_iter_start<<<vec_blocks(std::max(nf, 1)), kVecT, 0, st>>>(nf, P.d_r, rtol, maxit, P.d_partials, P.d_counter,
                                                              P.d_s), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
@@ -499,6 +509,7 @@ int pcg_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) {
     queued += todo;
     batch = std::min(batch * 2, 32);
   }
+  P.cycle_stop = nullptr;
   out.iters = P.h_s->iters;
   out.converged = P.h_s->converged;
   out.breakdown = P.h_s->breakdown;

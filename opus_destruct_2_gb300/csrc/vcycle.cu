@@ -37,12 +37,14 @@ constexpr int kChebDegree = 2;      // smoothing polynomial degree (each side)
 constexpr double kChebRatio = 10.0; // lmax / lmin of the smoothed interval
 constexpr int kCoarseDegree = 8;    // stalled coarsest level: polynomial degree in place of a solve
 
-__global__ void k_cvt(int64_t m, const double* in, float* out) {
+__global__ void k_cvt(int64_t m, const double* in, float* out, const int32_t* stop = nullptr) {
+  if (stop && *stop) return;
   const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k < m) out[k] = float(in[k]);
 }
 
-__global__ void k_widen(int64_t m, const float* in, double* out) {
+__global__ void k_widen(int64_t m, const float* in, double* out, const int32_t* stop) {
+  if (stop && *stop) return;
   const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k < m) out[k] = double(in[k]);
 }
@@ -99,6 +101,7 @@ enum Mode {
 };
 
 struct StepArgs {
+  const int32_t* stop;  // nonzero: the run is over, return at once
   const float* rin;  // kStep / kResPend: previous residual; kPostStart: b
   float* r;          // residual out
   float* dout;       // next direction
@@ -113,6 +116,7 @@ template <int MODE>
 __global__ void __launch_bounds__(kT) k_bsr32(int32_t n, const int32_t* __restrict__ rowptr,
                                               const int32_t* __restrict__ col, const float* __restrict__ val,
                                               const float* __restrict__ v, float* y, StepArgs s) {
+  if (s.stop && *s.stop) return;
   const int lane = threadIdx.x & 31;
   const int32_t row = blockIdx.x * kRows + (threadIdx.x >> 5);
   if (row >= n) return;  // (whole warps exit together)
@@ -152,7 +156,8 @@ __global__ void __launch_bounds__(kT) k_bsr32(int32_t n, const int32_t* __restri
 
 // d = D^-1 b / theta (the first Chebyshev direction from x = 0); one thread per node
 __global__ void k_cheb_first(int32_t n, const float* __restrict__ D, const float* __restrict__ b, float inv_theta,
-                             float* d) {
+                             float* d, const int32_t* stop) {
+  if (stop && *stop) return;
   const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float* Di = D + 36 * int64_t(i);
@@ -165,14 +170,16 @@ __global__ void k_cheb_first(int32_t n, const float* __restrict__ D, const float
   }
 }
 
-__global__ void k_add(int64_t m, const float* d, float* x) {
+__global__ void k_add(int64_t m, const float* d, float* x, const int32_t* stop) {
+  if (stop && *stop) return;
   const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k < m) x[k] += d[k];
 }
 
 // coarsest level: x = L^-T (L^-1 b) in f64 (warp per row, rows of L^-1 and of L^-T)
 __global__ void k_dense_mv(int32_t m, const double* __restrict__ M, const float* __restrict__ b32,
-                           const double* __restrict__ b64, double* y64, float* y32) {
+                           const double* __restrict__ b64, double* y64, float* y32, const int32_t* stop) {
+  if (stop && *stop) return;
   const int lane = threadIdx.x & 31;
   const int32_t row = blockIdx.x * kRows + (threadIdx.x >> 5);
   if (row >= m) return;
@@ -306,9 +313,10 @@ int smooth(Problem& P, const Level& L, const float* b, float* x, bool from_zero,
   float* d0 = L.t32;
   float* d1 = L.u32;
   StepArgs s{};
+  s.stop = P.cycle_stop;
   s.D = L.dinv32;
   if (from_zero) {
-    (k_cheb_first<<<nblk(n), kT, 0, st>>>(n, L.dinv32, b, C.inv_theta, d0), SVXG_COUNT_LAUNCH());
+    (k_cheb_first<<<nblk(n), kT, 0, st>>>(n, L.dinv32, b, C.inv_theta, d0, P.cycle_stop), SVXG_COUNT_LAUNCH());
     s.rin = b;
   } else {
     s.rin = b;
@@ -342,7 +350,7 @@ int smooth(Problem& P, const Level& L, const float* b, float* x, bool from_zero,
     if (from_zero) {
       SVXG_CUDA(cudaMemcpyAsync(x, d0, sizeof(float) * 6 * size_t(n), cudaMemcpyDeviceToDevice, st));
     } else {
-      (k_add<<<nblk(6 * int64_t(n)), kT, 0, st>>>(6 * int64_t(n), d0, x), SVXG_COUNT_LAUNCH());
+      (k_add<<<nblk(6 * int64_t(n)), kT, 0, st>>>(6 * int64_t(n), d0, x, P.cycle_stop), SVXG_COUNT_LAUNCH());
     }
   }
   return SVXG_OK;
@@ -355,8 +363,8 @@ int cycle(Problem& P, size_t l, const float* b, float* x) {
   if (l + 1 == P.lv.size()) {
     if (P.chol_n > 0) {
       const int32_t m = P.chol_n;
-      (k_dense_mv<<<rblk(m), kT, 0, st>>>(m, P.d_cinv, b, nullptr, P.d_cvec, nullptr), SVXG_COUNT_LAUNCH());
-      (k_dense_mv<<<rblk(m), kT, 0, st>>>(m, P.d_cinv + int64_t(m) * m, nullptr, P.d_cvec, nullptr, x), SVXG_COUNT_LAUNCH());
+      (k_dense_mv<<<rblk(m), kT, 0, st>>>(m, P.d_cinv, b, nullptr, P.d_cvec, nullptr, P.cycle_stop), SVXG_COUNT_LAUNCH());
+      (k_dense_mv<<<rblk(m), kT, 0, st>>>(m, P.d_cinv + int64_t(m) * m, nullptr, P.d_cvec, nullptr, x, P.cycle_stop), SVXG_COUNT_LAUNCH());
       return SVXG_OK;
     }
     return smooth(P, L, b, x, true, kCoarseDegree, 30.0, false);
@@ -364,6 +372,7 @@ int cycle(Problem& P, size_t l, const float* b, float* x) {
   TRY(smooth(P, L, b, x, true, kChebDegree, kChebRatio, true));
   const Level& C = P.lv[l + 1];
   StepArgs none{};
+  none.stop = P.cycle_stop;
   // restriction: bc = P^T r
   (k_bsr32<kY><<<rblk(C.A.n), kT, 0, st>>>(C.A.n, L.rrow, L.rent_i, L.pval32 + 36 * L.pnnz, L.r32, C.b32, none), SVXG_COUNT_LAUNCH());
   TRY(cycle(P, l + 1, C.b32, C.x32));
@@ -416,9 +425,17 @@ int vcycle(Problem& P, const double* r, double* z) {
   cudaStream_t st = P.stream;
   Level& L0 = P.lv[0];
   const int64_t m = 6 * int64_t(L0.A.n);
-  (k_cvt<<<nblk(m), kT, 0, st>>>(m, r, L0.b32), SVXG_COUNT_LAUNCH());
+  (k_cvt<<<nblk(m), kT, 0, st>>>(m, r, L0.b32, P.cycle_stop), SVXG_COUNT_LAUNCH());
   TRY(cycle(P, 0, L0.b32, L0.x32));
-  (k_widen<<<nblk(m), kT, 0, st>>>(m, L0.x32, z), SVXG_COUNT_LAUNCH());
+  (k_widen<<<nblk(m), kT, 0, st>>>(m, L0.x32, z, P.cycle_stop), SVXG_COUNT_LAUNCH());
+  SVXG_CUDA(cudaGetLastError());
+  return SVXG_OK;
+}
+
+// the same on f32 vectors (the mixed-precision inner solve): z = M^-1 r
+int vcycle32(Problem& P, const float* r, float* z) {
+  if (P.lv.empty()) return SVXG_OK;
+  TRY(cycle(P, 0, r, z));
   SVXG_CUDA(cudaGetLastError());
   return SVXG_OK;
 }
