@@ -200,6 +200,7 @@ int free_run(Problem& P);
 int vcycle(Problem& P, const double* r, double* z);
 int vcycle32(Problem& P, const float* r, float* z);
 // mixed.cu
+int mixed_begin(Problem& P);
 int mixed_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res);
 int prepare_cycle(Problem& P);
 // exact_judge.cu

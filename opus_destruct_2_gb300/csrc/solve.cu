@@ -456,7 +456,7 @@ int pcg_begin(Problem& P, const double* f_nodes, const double* u0_nodes) {
       (k_jacobi_rz<0><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_jinv, P.d_r, P.d_z, P.d_p, P.d_partials,
                                                        P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
     } else if (P.opt.precision == SVXG_PRECISION_MIXED) {
-      // (the mixed-precision run starts its own inner sequences from the FP64 residual)
+      TRY(mixed_begin(P));
     } else {
       TRY(vcycle(P, P.d_r, P.d_z));
       (k_rz<0><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_r, P.d_z, P.d_p, P.d_partials, P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());

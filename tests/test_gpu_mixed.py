@@ -74,3 +74,25 @@ def test_mixed_failure_set(name):
     assert np.array_equal((phi >= 1.0)[safe], (po >= 1.0)[safe])
     print(f"{name}: failing {int((po >= 1).sum())} bonds, min |phi-1| {np.min(np.abs(po - 1)):.2e}, "
           f"phi error {band:.2e}, {int((~safe).sum())} bonds inside the error band")
+
+
+def test_mixed_cap_and_resume_and_edge_loads():
+    nodes, bonds = fx.lattice(8)
+    f = fx.gravity(nodes)
+    G = StressProblem(nodes, bonds, MATS)
+    assert G.assemble(StressOptions(precision=MIXED, amg_min_nodes=16))
+    G.begin(f)
+    r1 = G.iterate(3, 1e-10)
+    assert r1.iters == 3 and not r1.converged
+    r2 = G.iterate(1000, 1e-10)
+    assert r2.converged
+    u_split = G.current()
+    u_once, r = G.solve(f, rtol=1e-10, maxit=1000)
+    assert r.converged and abs(r.iters - (r1.iters + r2.iters)) <= 2
+    assert relerr(u_split, u_once) <= 1e-8
+    z = np.zeros_like(f)
+    u0, rz = G.solve(z, np.ones_like(f), rtol=1e-9, maxit=100, warm=True)
+    assert rz.converged and np.all(u0 == 0.0)
+    f[5] = np.nan
+    _, rn = G.solve(f, rtol=1e-9, maxit=100)
+    assert rn.breakdown and not rn.converged and np.isinf(rn.rel_res)
