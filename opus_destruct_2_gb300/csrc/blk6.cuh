@@ -98,6 +98,44 @@ SVXG_HD void atbd_add_rigid(V3d ra, const BondStiffness& S, V3d rb, double s, do
     }
 }
 
+// The same as atbd_add_rigid with the products by the rigid blocks' exact zeros and ones left out.
+// Every entry keeps the full loops' sequence of nonzero roundings: a zero product added to a sum
+// leaves its value (x + 0 = x; only a zero's sign can differ), and x * 1 = x, so each result equals
+// atbd_add's value for value (checked entry by entry against the full loops by the tests).
+//   T = D B:      rows 0-2: [Dt, Dt R_b] (R_b the skew block of rb), rows 3-5: [0, Dr]
+//   A^T T:        rows 0-2: T's rows 0-2; row 3 + i: the two nonzero R_a(k, i) T[k] terms in k
+//                 order, then T[3 + i]
+SVXG_HD void atbd_add_rigid_fast(V3d ra, const BondStiffness& S, V3d rb, double s, double* C) {
+  const double* Dt = S.Dt;
+  const double* Dr = S.Dr;
+  double T[36];
+  for (int r = 0; r < 3; ++r) {
+    const double d0 = Dt[r * 3], d1 = Dt[r * 3 + 1], d2 = Dt[r * 3 + 2];
+    T[r * 6 + 0] = d0;
+    T[r * 6 + 1] = d1;
+    T[r * 6 + 2] = d2;
+    T[r * 6 + 3] = d1 * -rb.z + d2 * rb.y;
+    T[r * 6 + 4] = d0 * rb.z + d2 * -rb.x;
+    T[r * 6 + 5] = d0 * -rb.y + d1 * rb.x;
+  }
+  for (int r = 0; r < 3; ++r) {
+    T[(3 + r) * 6 + 0] = 0.0;
+    T[(3 + r) * 6 + 1] = 0.0;
+    T[(3 + r) * 6 + 2] = 0.0;
+    T[(3 + r) * 6 + 3] = Dr[r * 3];
+    T[(3 + r) * 6 + 4] = Dr[r * 3 + 1];
+    T[(3 + r) * 6 + 5] = Dr[r * 3 + 2];
+  }
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 6; ++c) C[r * 6 + c] += s * T[r * 6 + c];
+  for (int c = 0; c < 6; ++c) {
+    const double t0 = T[c], t1 = T[6 + c], t2 = T[12 + c];
+    C[18 + c] += s * ((-ra.z * t1 + ra.y * t2) + T[18 + c]);
+    C[24 + c] += s * ((ra.z * t0 + -ra.x * t2) + T[24 + c]);
+    C[30 + c] += s * ((-ra.y * t0 + ra.x * t1) + T[30 + c]);
+  }
+}
+
 // blk6::inv6 (amg.cpp:105-135): Gauss-Jordan with partial pivoting; false if singular.
 SVXG_HD bool inv6(const double* A, double* Ainv) {
   double M[6][12];

@@ -48,6 +48,8 @@ struct DeviceScope {
   } while (0)
 
 void release_solver(Problem& P) {
+  destroy_loop(P.loop_plain);
+  destroy_loop(P.loop_mixed);
   free_run(P);
   P.mem.release(P.K.rowptr);
   P.mem.release(P.K.col);
@@ -106,6 +108,8 @@ namespace {
 std::atomic<int64_t> g_launches{0};
 }
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void uncount_launches(int64_t n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
+void add_launches(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 }  // namespace svxg
 

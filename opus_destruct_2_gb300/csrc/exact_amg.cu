@@ -636,6 +636,36 @@ __global__ void k_chol_col(int32_t m, int32_t j, double* C) {
   C[int64_t(i) * m + j] = v / s;
 }
 
+// the whole factor in one block: the reference's column loop (amg.cpp:555-573), each column's rows
+// split over the threads (each row's sum over k in the reference's order)
+__global__ void __launch_bounds__(1024) k_chol_block(int32_t m, double* C) {
+  __shared__ double dmax_sh, s_sh;
+  if (threadIdx.x == 0) {
+    double d = 0.0;
+    for (int32_t i = 0; i < m; ++i) d = maxd(d, fabs(C[int64_t(i) * m + i]));
+    dmax_sh = d;
+  }
+  __syncthreads();
+  const double dmax = dmax_sh;
+  for (int32_t j = 0; j < m; ++j) {
+    if (threadIdx.x == 0) {
+      double d = C[int64_t(j) * m + j];
+      for (int32_t k = 0; k < j; ++k) d -= C[int64_t(j) * m + k] * C[int64_t(j) * m + k];
+      if (!(d > 1e-12 * dmax)) d = maxd(1e-12 * dmax, 1e-300);
+      s_sh = sqrt(d);
+      C[int64_t(j) * m + j] = s_sh;
+    }
+    __syncthreads();
+    const double sj = s_sh;
+    for (int32_t i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
+      double v = 0.5 * (C[int64_t(i) * m + j] + C[int64_t(j) * m + i]);
+      for (int32_t k = 0; k < j; ++k) v -= C[int64_t(i) * m + k] * C[int64_t(j) * m + k];
+      C[int64_t(i) * m + j] = v / sj;
+    }
+    __syncthreads();
+  }
+}
+
 __global__ void k_chol_mirror(int32_t m, double* C) {
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= int64_t(m) * m) return;
@@ -732,7 +762,7 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
   TRY(agg1.alloc(size_t(n)));
   TRY(flag.alloc(size_t(n) + 1));
   TRY(rank.alloc(size_t(n) + 1));
-  TRY(undecided.alloc(1));
+  TRY(undecided.alloc(8));
   Tmp<int32_t> iso(st), noniso(st), isorank(st), alloc(st), allocscan(st), gfirst(st);
   TRY(iso.alloc(size_t(n) + 1));
   TRY(noniso.alloc(size_t(n) + 1));
@@ -753,13 +783,21 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     const Bsr& A = P.lv[l].A;
     (k_strong<<<nblk(nnzb), kT, 0, st>>>(nnzb, brow.p, A.col, fro.p, A.rowptr, theta, strong.p), SVXG_COUNT_LAUNCH());
     (k_mis_init<<<nblk(n), kT, 0, st>>>(n, A.rowptr, state.p, covered.p, claim.p), SVXG_COUNT_LAUNCH());
-    for (int guard = 0; guard <= n; ++guard) {
-      SVXG_CUDA(cudaMemsetAsync(undecided.p, 0, sizeof(int32_t), st));
-      (k_mis_claim<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, claim.p), SVXG_COUNT_LAUNCH());
-      (k_mis_decide<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, covered.p, claim.p, undecided.p), SVXG_COUNT_LAUNCH());
-      (k_mis_cover<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, covered.p, claim.p), SVXG_COUNT_LAUNCH());
+    // rounds in batches of kBatch (a round after the last decision changes nothing), one host
+    // read per batch: the last round's count of undecided nodes
+    constexpr int kBatch = 8;
+    for (int guard = 0; guard <= n; guard += kBatch) {
+      SVXG_CUDA(cudaMemsetAsync(undecided.p, 0, sizeof(int32_t) * kBatch, st));
+      for (int b = 0; b < kBatch; ++b) {
+        (k_mis_claim<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, claim.p), SVXG_COUNT_LAUNCH());
+        (k_mis_decide<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, covered.p, claim.p,
+                                              undecided.p + b),
+         SVXG_COUNT_LAUNCH());
+        (k_mis_cover<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, covered.p, claim.p),
+         SVXG_COUNT_LAUNCH());
+      }
       int32_t u = 0;
-      TRY(copy_to_host(P, &u, undecided.p, sizeof(int32_t)));
+      TRY(copy_to_host(P, &u, undecided.p + (kBatch - 1), sizeof(int32_t)));
       if (u == 0) break;
     }
     (k_root_flags<<<nblk(n), kT, 0, st>>>(n, state.p, flag.p), SVXG_COUNT_LAUNCH());
@@ -946,13 +984,7 @@ int factor_coarsest(Problem& P) {
   cudaStream_t st = P.stream;
   SVXG_CUDA(cudaMemsetAsync(P.d_chol, 0, sizeof(double) * size_t(m) * size_t(m), st));
   (k_dense_fill<<<nblk(L.A.n), kT, 0, st>>>(L.A.n, L.A.rowptr, L.A.col, L.A.val, m, P.d_chol), SVXG_COUNT_LAUNCH());
-  Tmp<double> dmax(st);
-  TRY(dmax.alloc(1));
-  (k_dense_dmax<<<1, 1, 0, st>>>(m, P.d_chol, dmax.p), SVXG_COUNT_LAUNCH());
-  for (int32_t j = 0; j < m; ++j) {
-    (k_chol_diag<<<1, 1, 0, st>>>(m, j, P.d_chol, dmax.p), SVXG_COUNT_LAUNCH());
-    if (m - j - 1 > 0) (k_chol_col<<<nblk(m - j - 1, 128), 128, 0, st>>>(m, j, P.d_chol), SVXG_COUNT_LAUNCH());
-  }
+  (k_chol_block<<<1, 1024, 0, st>>>(m, P.d_chol), SVXG_COUNT_LAUNCH());
   (k_chol_mirror<<<nblk(int64_t(m) * m), kT, 0, st>>>(m, P.d_chol), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   return SVXG_OK;

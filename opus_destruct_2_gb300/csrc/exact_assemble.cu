@@ -163,11 +163,11 @@ __global__ void k_block_values(int64_t nnzb, int32_t nfree, const int32_t* rowpt
     const V3d p = v3of(b.p);
     const V3d rs = sub3(p, node_c(nodes, i));
     if (diag) {
-      atbd_add_rigid(rs, S, rs, 1.0, C);
+      atbd_add_rigid_fast(rs, S, rs, 1.0, C);
     } else {
       const int32_t other = side ? b.a : b.b;
       const V3d ro = sub3(p, node_c(nodes, other));
-      atbd_add_rigid(rs, S, ro, -1.0, C);
+      atbd_add_rigid_fast(rs, S, ro, -1.0, C);
     }
   }
   double* out = val + 36 * k;
@@ -258,11 +258,11 @@ __global__ void k_remove_bonds(const int32_t* list, int32_t count, svxg_bond* bo
     const int32_t ib = b.b >= 0 ? dof[b.b] : -1;
     const V3d ra = sub3(p, v3of(nodes[b.a].c));
     const V3d rb = b.b >= 0 ? sub3(p, v3of(nodes[b.b].c)) : V3d{0, 0, 0};
-    if (ia >= 0) atbd_add_rigid(ra, S, ra, -1.0, find_block(rowptr, col, val, ia, ia));
-    if (ib >= 0) atbd_add_rigid(rb, S, rb, -1.0, find_block(rowptr, col, val, ib, ib));
+    if (ia >= 0) atbd_add_rigid_fast(ra, S, ra, -1.0, find_block(rowptr, col, val, ia, ia));
+    if (ib >= 0) atbd_add_rigid_fast(rb, S, rb, -1.0, find_block(rowptr, col, val, ib, ib));
     if (ia >= 0 && ib >= 0) {
-      if (double* k1 = find_block(rowptr, col, val, ia, ib)) atbd_add_rigid(ra, S, rb, 1.0, k1);
-      if (double* k2 = find_block(rowptr, col, val, ib, ia)) atbd_add_rigid(rb, S, ra, 1.0, k2);
+      if (double* k1 = find_block(rowptr, col, val, ia, ib)) atbd_add_rigid_fast(ra, S, rb, 1.0, k1);
+      if (double* k2 = find_block(rowptr, col, val, ib, ia)) atbd_add_rigid_fast(rb, S, ra, 1.0, k2);
     }
     if (jacobi) {
       const int32_t ds[2] = {ia, ib};

@@ -166,11 +166,15 @@ struct Problem {
   float* d_mx = nullptr;          // mixed precision: d, r, z, p, q in f32 (5 x 6 nfree)
   void* d_ms = nullptr;           // mixed precision scalars (device)
   void* h_ms = nullptr;           // ... pinned mirror
+  int32_t mx_maxit = 0;
   double* d_partials = nullptr;   // block partial sums
   unsigned* d_counter = nullptr;  // last-block counters
   int32_t partial_blocks = 0;
   bool active = false;
   int32_t run_iters = 0;
+  // whole-iterate graphs (graphs.cu): built on first use after each assemble
+  void* loop_plain = nullptr;
+  void* loop_mixed = nullptr;
   // live kernel timing (CUDA events around each conjugate-gradient SpMV launch)
   bool timer_on = false;
   std::vector<cudaEvent_t> timer_events;
@@ -207,6 +211,13 @@ int prepare_cycle(Problem& P);
 int bond_loads_device(Problem& P, const double* u_nodes, svxg_bond_load* out);
 int utilization_device(Problem& P, const double* u_nodes, double fragility, double* phi, uint8_t* mode,
                        int32_t* over, int32_t* n_over);
+// graphs.cu
+bool use_graphs();
+int timer_mark(Problem& P, bool closing = false);
+int run_loop(Problem& P, void*& slot, const int32_t* done, int (*body)(Problem&), int64_t* body_launches);
+void destroy_loop(void*& slot);
+void uncount_launches(int64_t n);
+void add_launches(int64_t n);
 // scan.cu
 int exclusive_scan_i32(Problem& P, const int32_t* in, int32_t* out, int64_t n, int32_t* total_host);
 

@@ -13,8 +13,10 @@
 // Every kernel returns at once when the run is done, so a batch of iterations queued past
 // convergence costs only launches.
 #include <cmath>
+#include <cstdlib>
 
 #include "problem.cuh"
+#include "spmv_row.cuh"
 
 namespace svxg {
 namespace {
@@ -104,19 +106,8 @@ __global__ void __launch_bounds__(kSpmvT) k_spmv(int32_t n, const int32_t* __res
   if (EPI == kDotP && s->done) return;
   const int lane = threadIdx.x & 31;
   const int32_t row = blockIdx.x * kRowsPerBlock + (threadIdx.x >> 5);
-  const int g = lane / 6, r = lane - 6 * (lane / 6);
-  double acc = 0.0;
-  if (row < n) {
-    const int32_t k0 = rowptr[row], k1 = rowptr[row + 1];
-    if (g < 5)
-      for (int32_t k = k0 + g; k < k1; k += 5)
-        acc += row_dot6<double>(val + 36 * int64_t(k) + 6 * r, x + 6 * int64_t(__ldg(col + k)));
-  }
-  const double a1 = __shfl_sync(0xffffffffu, acc, (r + 6) & 31);
-  const double a2 = __shfl_sync(0xffffffffu, acc, (r + 12) & 31);
-  const double a3 = __shfl_sync(0xffffffffu, acc, (r + 18) & 31);
-  const double a4 = __shfl_sync(0xffffffffu, acc, (r + 24) & 31);
-  const double yr = acc + a1 + a2 + a3 + a4;
+  const int32_t k0 = row < n ? rowptr[row] : 0, k1 = row < n ? rowptr[row + 1] : 0;
+  const double yr = warp_row_product<double, double, double>(k0, k1, col, val, x);
   double dp = 0.0;
   if (row < n && lane < 6) {
     y[6 * int64_t(row) + lane] = yr;
@@ -364,8 +355,10 @@ __global__ void k_gather_nodes(int32_t n, const int32_t* dof, const double* free
     if (e__) return e__;  \
   } while (0)
 
+}  // namespace
+
 // an event before (closing = false) or after a timed launch
-int timer_mark(Problem& P, bool closing = false) {
+int timer_mark(Problem& P, bool closing) {
   const size_t k = 2 * P.timer_used + (closing ? 1 : 0);
   while (P.timer_events.size() <= k) {
     cudaEvent_t e;
@@ -376,6 +369,8 @@ int timer_mark(Problem& P, bool closing = false) {
   if (closing) ++P.timer_used;
   return SVXG_OK;
 }
+
+namespace {
 
 int ensure_run(Problem& P) {
   if (P.d_x) return SVXG_OK;
@@ -456,7 +451,7 @@ int pcg_begin(Problem& P, const double* f_nodes, const double* u0_nodes) {
       (k_jacobi_rz<0><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_jinv, P.d_r, P.d_z, P.d_p, P.d_partials,
                                                        P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
     } else if (P.opt.precision == SVXG_PRECISION_MIXED) {
-      TRY(mixed_begin(P));
+      // (the mixed run starts each inner sequence from the FP64 residual)
     } else {
       TRY(vcycle(P, P.d_r, P.d_z));
       (k_rz<0><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_r, P.d_z, P.d_p, P.d_partials, P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
@@ -466,6 +461,36 @@ int pcg_begin(Problem& P, const double* f_nodes, const double* u0_nodes) {
   P.active = true;
   P.run_iters = 0;
   return SVXG_OK;
+}
+
+// one iteration of the sequence (stress.cpp:428-461), enqueued on P.stream
+int plain_body(Problem& P) {
+  const int32_t nf = P.nfree;
+  cudaStream_t st = P.stream;
+  if (P.timer_on) TRY(timer_mark(P));
+  (k_spmv<kDotP><<<spmv_blocks(nf), kSpmvT, 0, st>>>(nf, P.K.rowptr, P.K.col, P.K.val, P.d_p, P.d_q, P.d_partials,
+                                                    P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
+  if (P.timer_on) TRY(timer_mark(P, true));
+  (k_axpy_rr<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_x, P.d_r, P.d_p, P.d_q, P.d_partials, P.d_counter, P.d_s),
+   SVXG_COUNT_LAUNCH());
+  if (P.jacobi_only) {
+    (k_jacobi_rz<1><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_jinv, P.d_r, P.d_z, nullptr, P.d_partials, P.d_counter,
+                                                      P.d_s), SVXG_COUNT_LAUNCH());
+  } else {
+    TRY(vcycle(P, P.d_r, P.d_z));
+    (k_rz<1><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_r, P.d_z, nullptr, P.d_partials, P.d_counter, P.d_s),
+     SVXG_COUNT_LAUNCH());
+  }
+  (k_p_update<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_z, P.d_p, P.d_s), SVXG_COUNT_LAUNCH());
+  (k_mark_cap<<<1, 32, 0, st>>>(P.d_s), SVXG_COUNT_LAUNCH());
+  SVXG_CUDA(cudaGetLastError());
+  return SVXG_OK;
+}
+
+// whole iterate() calls as one graph launch (SVXG_NO_GRAPHS=1: host-driven batches instead)
+bool use_graphs() {
+  static const bool on = std::getenv("SVXG_NO_GRAPHS") == nullptr;
+  return on;
 }
 
 // StressProblem::iterate (stress.cpp:403-464)
@@ -482,32 +507,24 @@ int pcg_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) {
   (k_iter_start<<<vec_blocks(std::max(nf, 1)), kVecT, 0, st>>>(nf, P.d_r, rtol, maxit, P.d_partials, P.d_counter,
                                                              P.d_s), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
-  int32_t queued = 0;
-  int32_t batch = 2;
-  for (;;) {
+  if (use_graphs() && !P.timer_on) {  // (the live timer brackets each launch: host-driven then)
+    int64_t per = 0;
+    TRY(run_loop(P, P.loop_plain, &P.d_s->done, plain_body, &per));
     SVXG_CUDA(cudaMemcpyAsync(P.h_s, P.d_s, sizeof(PcgScalars), cudaMemcpyDeviceToHost, st));
     SVXG_CUDA(cudaStreamSynchronize(st));
-    if (P.h_s->done || queued >= maxit) break;
-    const int32_t todo = std::min(batch, maxit - queued);
-    for (int32_t it = 0; it < todo; ++it) {
-      if (P.timer_on) TRY(timer_mark(P));
-      (k_spmv<kDotP><<<spmv_blocks(nf), kSpmvT, 0, st>>>(nf, P.K.rowptr, P.K.col, P.K.val, P.d_p, P.d_q,
-                                                        P.d_partials, P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
-      if (P.timer_on) TRY(timer_mark(P, true));
-      (k_axpy_rr<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_x, P.d_r, P.d_p, P.d_q, P.d_partials, P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
-      if (P.jacobi_only) {
-        (k_jacobi_rz<1><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_jinv, P.d_r, P.d_z, nullptr, P.d_partials,
-                                                         P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
-      } else {
-        TRY(vcycle(P, P.d_r, P.d_z));
-        (k_rz<1><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_r, P.d_z, nullptr, P.d_partials, P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
-      }
-      (k_p_update<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_z, P.d_p, P.d_s), SVXG_COUNT_LAUNCH());
-      (k_mark_cap<<<1, 32, 0, st>>>(P.d_s), SVXG_COUNT_LAUNCH());
+    add_launches(per * std::max<int64_t>(1, P.h_s->iters));
+  } else {
+    int32_t queued = 0;
+    int32_t batch = 2;
+    for (;;) {
+      SVXG_CUDA(cudaMemcpyAsync(P.h_s, P.d_s, sizeof(PcgScalars), cudaMemcpyDeviceToHost, st));
+      SVXG_CUDA(cudaStreamSynchronize(st));
+      if (P.h_s->done || queued >= maxit) break;
+      const int32_t todo = std::min(batch, maxit - queued);
+      for (int32_t it = 0; it < todo; ++it) TRY(plain_body(P));
+      queued += todo;
+      batch = std::min(batch * 2, 32);
     }
-    SVXG_CUDA(cudaGetLastError());
-    queued += todo;
-    batch = std::min(batch * 2, 32);
   }
   P.cycle_stop = nullptr;
   out.iters = P.h_s->iters;

@@ -1,0 +1,73 @@
+// spmv_row.cuh - the warp-per-block-row product of a 6x6 BSR matrix, shared by every SpMV.
+//
+// One warp owns one block row. Lanes 6g + c (g < 5, c < 6) take row c of every fifth block; the
+// row's column indices arrive first, in one coalesced load (lane j holds the j-th block's column,
+// broadcast by shuffles), and each group issues the loads of two blocks (k and k + 5: six
+// 8-byte or 16-byte value loads and six broadcast x loads) before it multiplies, so a row of up
+// to ten blocks costs one dependent round trip after the column indices. The five groups' sums
+// meet in lanes 0-5.
+#pragma once
+
+#include <cstdint>
+
+namespace svxg {
+
+template <typename V>
+struct Vec2;
+template <>
+struct Vec2<float> {
+  using T = float2;
+};
+template <>
+struct Vec2<double> {
+  using T = double2;
+};
+
+// m: row c of a block (6 values), x: the column's 6 values; V and X are float or double
+template <typename V, typename X, typename A>
+__device__ __forceinline__ A dot6(const V* __restrict__ m, const X* __restrict__ x) {
+  using MV = typename Vec2<V>::T;
+  using XV = typename Vec2<X>::T;
+  const MV a = __ldg(reinterpret_cast<const MV*>(m)), b = __ldg(reinterpret_cast<const MV*>(m) + 1),
+           d = __ldg(reinterpret_cast<const MV*>(m) + 2);
+  const XV u = __ldg(reinterpret_cast<const XV*>(x)), v = __ldg(reinterpret_cast<const XV*>(x) + 1),
+           w = __ldg(reinterpret_cast<const XV*>(x) + 2);
+  return A(a.x) * A(u.x) + A(a.y) * A(u.y) + A(b.x) * A(v.x) + A(b.y) * A(v.y) + A(d.x) * A(w.x) + A(d.y) * A(w.y);
+}
+
+// (A x)_row,c in lanes c < 6 (other lanes: garbage); whole warp must call
+template <typename V, typename X, typename A>
+__device__ __forceinline__ A warp_row_product(int32_t k0, int32_t k1, const int32_t* __restrict__ col,
+                                              const V* __restrict__ val, const X* __restrict__ x) {
+  const int lane = threadIdx.x & 31;
+  const int g = lane / 6, c = lane - 6 * (lane / 6);
+  A acc = A(0);
+  for (int32_t base = k0; base < k1; base += 30) {
+    // up to 30 blocks: their columns in one load, then three passes of ten
+    const int32_t nb = (k1 - base) < 30 ? (k1 - base) : 30;
+    const int32_t mycol = lane < nb ? __ldg(col + base + lane) : 0;
+    for (int32_t t = 0; t < nb; t += 10) {
+      const int ia = t + g, ib = t + 5 + g;
+      const int32_t ca = __shfl_sync(0xffffffffu, mycol, ia & 31);
+      const int32_t cb = __shfl_sync(0xffffffffu, mycol, ib & 31);
+      if (g < 5 && ia < nb) {
+        const V* ma = val + 36 * int64_t(base + ia) + 6 * c;
+        if (ib < nb) {
+          const V* mb = val + 36 * int64_t(base + ib) + 6 * c;
+          const A pa = dot6<V, X, A>(ma, x + 6 * int64_t(ca));
+          const A pb = dot6<V, X, A>(mb, x + 6 * int64_t(cb));
+          acc += pa + pb;
+        } else {
+          acc += dot6<V, X, A>(ma, x + 6 * int64_t(ca));
+        }
+      }
+    }
+  }
+  const A a1 = __shfl_sync(0xffffffffu, acc, (c + 6) & 31);
+  const A a2 = __shfl_sync(0xffffffffu, acc, (c + 12) & 31);
+  const A a3 = __shfl_sync(0xffffffffu, acc, (c + 18) & 31);
+  const A a4 = __shfl_sync(0xffffffffu, acc, (c + 24) & 31);
+  return acc + a1 + a2 + a3 + a4;
+}
+
+}  // namespace svxg

@@ -18,6 +18,7 @@
 #include <cmath>
 
 #include "problem.cuh"
+#include "spmv_row.cuh"
 
 namespace svxg {
 namespace {
@@ -63,22 +64,7 @@ __global__ void k_cvt_transpose(int64_t pnnz, const int32_t* rent_e, const doubl
 // and its row c; the row's six sums end in lanes 0-5.
 __device__ __forceinline__ float row_block_sum(int32_t k0, int32_t k1, const int32_t* __restrict__ col,
                                                const float* __restrict__ val, const float* __restrict__ x) {
-  const int lane = threadIdx.x & 31;
-  const int g = lane / 6, c = lane - 6 * g;
-  float acc = 0.0f;
-  if (g < 5)
-    for (int32_t k = k0 + g; k < k1; k += 5) {
-      const float2* m = reinterpret_cast<const float2*>(val + 36 * int64_t(k) + 6 * c);
-      const float2* xv = reinterpret_cast<const float2*>(x + 6 * int64_t(__ldg(col + k)));
-      const float2 a = __ldg(m), b = __ldg(m + 1), d = __ldg(m + 2);
-      const float2 u = __ldg(xv), v = __ldg(xv + 1), w = __ldg(xv + 2);
-      acc += a.x * u.x + a.y * u.y + b.x * v.x + b.y * v.y + d.x * w.x + d.y * w.y;
-    }
-  const float a1 = __shfl_sync(0xffffffffu, acc, (c + 6) & 31);
-  const float a2 = __shfl_sync(0xffffffffu, acc, (c + 12) & 31);
-  const float a3 = __shfl_sync(0xffffffffu, acc, (c + 18) & 31);
-  const float a4 = __shfl_sync(0xffffffffu, acc, (c + 24) & 31);
-  return acc + a1 + a2 + a3 + a4;
+  return warp_row_product<float, float, float>(k0, k1, col, val, x);
 }
 
 // (D^-1 v)_c for lane c < 6, v held by lanes 0-5
