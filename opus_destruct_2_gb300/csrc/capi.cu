@@ -254,6 +254,8 @@ static int assemble_impl(Problem& P, const svxg_stress_options* opt, int32_t* ok
     }
     P.assembly_work += P.amg_build_work;
   }
+  TRY(tune_k64(P));
+  P.sched_k32 = P.jacobi_only || P.lv.empty() ? 0 : P.lv[0].sched_a;  // (K32 is level 0's cycle operator)
   SVXG_CUDA(cudaStreamSynchronize(P.stream));
   P.assembled = true;
   if (ok) *ok = 1;

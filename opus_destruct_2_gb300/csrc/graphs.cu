@@ -40,6 +40,10 @@ void destroy_loop(void*& slot) {
 // Builds (once) and launches the loop graph in `slot`: body() enqueues one iteration on P.stream;
 // `done` is the device flag that ends the loop. Returns the body's launch count in *body_launches.
 int run_loop(Problem& P, void*& slot, const int32_t* done, int (*body)(Problem&), int64_t* body_launches) {
+  if (P.nfree <= 0) {
+    set_error("loop graph: no free DOFs");
+    return SVXG_ERR_STATE;
+  }
   LoopGraph* L = static_cast<LoopGraph*>(slot);
   if (!L) {
     L = new LoopGraph;

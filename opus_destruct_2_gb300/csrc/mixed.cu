@@ -80,17 +80,20 @@ __device__ __forceinline__ bool reduce_last(double v, double* partials, unsigned
 }
 
 // y32 = K32 p32 (warp per row), p.y accumulated in f64 -> alpha
+template <int SCHED>
 __global__ void __launch_bounds__(kT) k_spmv32_dot(int32_t n, const int32_t* __restrict__ rowptr,
                                                    const int32_t* __restrict__ col, const float* __restrict__ val,
                                                    const float* __restrict__ p, float* __restrict__ q,
                                                    double* partials, unsigned* counter, MixedScalars* s) {
   if (s->done) return;
-  const int lane = threadIdx.x & 31;
-  const int32_t row = blockIdx.x * kRows + (threadIdx.x >> 5);
-  const int32_t k0 = row < n ? rowptr[row] : 0, k1 = row < n ? rowptr[row + 1] : 0;
-  const float y = warp_row_product<float, float, float>(k0, k1, col, val, p);
+  int c;
+  bool lane_ok;
+  const int32_t row = sched_row<SCHED>(kRows, &c, &lane_ok);
+  const bool row_ok = row < n;
+  const float y = sched_row_product<SCHED, float, float, float>(row_ok, row, rowptr, col, val, p);
+  const int lane = c;
   double dp = 0.0;
-  if (row < n && lane < 6) {
+  if (row_ok && lane_ok) {
     q[6 * int64_t(row) + lane] = y;
     dp = double(p[6 * int64_t(row) + lane]) * double(y);
   }
@@ -213,9 +216,14 @@ int mixed_body(Problem& P) {
   float* q32 = d + 4 * m;
   MixedScalars* s = static_cast<MixedScalars*>(P.d_ms);
   if (P.timer_on) TRY(timer_mark(P));
-  (k_spmv32_dot<<<rblk(nf), kT, 0, st>>>(nf, P.K.rowptr, P.K.col, P.K.val32, p32, q32, P.d_partials, P.d_counter,
-                                         s),
-   SVXG_COUNT_LAUNCH());
+  if (P.sched_k32 == kGroupRow)
+    (k_spmv32_dot<kGroupRow><<<unsigned((std::max(nf, 1) + 5 * kRows - 1) / (5 * kRows)), kT, 0, st>>>(
+         nf, P.K.rowptr, P.K.col, P.K.val32, p32, q32, P.d_partials, P.d_counter, s),
+     SVXG_COUNT_LAUNCH());
+  else
+    (k_spmv32_dot<kWarpRow><<<rblk(nf), kT, 0, st>>>(nf, P.K.rowptr, P.K.col, P.K.val32, p32, q32, P.d_partials,
+                                                     P.d_counter, s),
+     SVXG_COUNT_LAUNCH());
   if (P.timer_on) TRY(timer_mark(P, true));
   (k_axpy32<<<vblk(nf), kT, 0, st>>>(nf, d, r32, p32, q32, P.d_partials, P.d_counter, s), SVXG_COUNT_LAUNCH());
   TRY(vcycle32(P, r32, z32));
@@ -294,7 +302,11 @@ int mixed_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
     P.cycle_stop = &s->done;
     TRY(vcycle32(P, r32, z32));
     (k_rz32<0><<<vblk(nf), kT, 0, st>>>(nf, r32, z32, p32, P.d_partials, P.d_counter, s), SVXG_COUNT_LAUNCH());
-    if (use_graphs() && !P.timer_on) {
+    SVXG_CUDA(cudaMemcpyAsync(hs, s, sizeof(MixedScalars), cudaMemcpyDeviceToHost, st));
+    SVXG_CUDA(cudaStreamSynchronize(st));
+    if (hs->done) {
+      // (the inner start already broke down or met its target)
+    } else if (use_graphs() && !P.timer_on) {
       int64_t per = 0;
       P.mx_maxit = maxit - used;
       TRY(run_loop(P, P.loop_mixed, &s->done, mixed_body, &per));

@@ -124,6 +124,7 @@ struct Level {
   float* r32 = nullptr;
   float* t32 = nullptr;
   float* u32 = nullptr;
+  int sched_a = 0, sched_p = 0, sched_r = 0;  // row-product schedules (spmv_row.cuh), autotuned
 };
 
 struct Problem {
@@ -150,6 +151,7 @@ struct Problem {
   Bsr K;
   double id_scale = 1.0;
   double* d_jinv = nullptr;       // block-Jacobi inverses (36 per free node)
+  int sched_k64 = 0, sched_k32 = 0;  // K's SpMV schedules (FP64 CG, FP32 inner), autotuned
   // multigrid
   std::vector<Level> lv;
   double* d_chol = nullptr;       // coarsest dense factor (m x m, lower = L, upper = L^T)
@@ -200,6 +202,7 @@ int pcg_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res);
 int gather_solution(Problem& P, double* u_nodes);                        // device, node order
 int precondition(Problem& P, const double* r, double* z);
 int free_run(Problem& P);
+int tune_k64(Problem& P);
 // vcycle.cu
 int vcycle(Problem& P, const double* r, double* z);
 int vcycle32(Problem& P, const float* r, float* z);

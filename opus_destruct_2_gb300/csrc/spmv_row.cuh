@@ -70,4 +70,64 @@ __device__ __forceinline__ A warp_row_product(int32_t k0, int32_t k1, const int3
   return acc + a1 + a2 + a3 + a4;
 }
 
+// Schedules of the row product (the autotuner picks one per operator, see tune.cu):
+//   kWarpRow  one warp per block row, the five lane groups over the row's blocks (long rows)
+//   kGroupRow five block rows per warp, one lane group per row, each lane over its row's blocks
+//             (short rows: five rows in flight per warp)
+enum Sched { kWarpRow = 0, kGroupRow = 1 };
+
+template <int SCHED>
+struct RowMap {
+  static constexpr int kRowsPerWarp = SCHED == kWarpRow ? 1 : 5;
+};
+
+// The warp's rows: row of this lane's group (valid: row < n), component c of its output.
+template <int SCHED>
+__device__ __forceinline__ int32_t sched_row(int rows_per_block_warps, int* c_out, bool* lane_ok) {
+  const int lane = threadIdx.x & 31;
+  const int g = lane / 6;
+  *c_out = lane - 6 * g;
+  const int32_t warp = int32_t(blockIdx.x) * rows_per_block_warps + (threadIdx.x >> 5);
+  if (SCHED == kWarpRow) {
+    *lane_ok = lane < 6;
+    return warp;
+  }
+  *lane_ok = g < 5;
+  return warp * 5 + (g < 5 ? g : 4);
+}
+
+// the row's product for this schedule; in kGroupRow every lane sums its own row's blocks
+template <int SCHED, typename V, typename X, typename A>
+__device__ __forceinline__ A sched_row_product(bool row_ok, int32_t row, const int32_t* __restrict__ rowptr,
+                                               const int32_t* __restrict__ col, const V* __restrict__ val,
+                                               const X* __restrict__ x) {
+  if (SCHED == kWarpRow) {
+    const int32_t k0 = row_ok ? rowptr[row] : 0, k1 = row_ok ? rowptr[row + 1] : 0;
+    return warp_row_product<V, X, A>(k0, k1, col, val, x);
+  }
+  const int lane = threadIdx.x & 31;
+  const int g = lane / 6, c = lane - 6 * g;
+  A acc = A(0);
+  if (row_ok && g < 5) {
+    const int32_t k1 = rowptr[row + 1];
+    int32_t k = rowptr[row];
+    for (; k + 1 < k1; k += 2) {
+      const int32_t ca = __ldg(col + k), cb = __ldg(col + k + 1);
+      const A pa = dot6<V, X, A>(val + 36 * int64_t(k) + 6 * c, x + 6 * int64_t(ca));
+      const A pb = dot6<V, X, A>(val + 36 * int64_t(k + 1) + 6 * c, x + 6 * int64_t(cb));
+      acc += pa + pb;
+    }
+    if (k < k1) acc += dot6<V, X, A>(val + 36 * int64_t(k) + 6 * c, x + 6 * int64_t(__ldg(col + k)));
+  }
+  return acc;
+}
+
+// component q of the row's 6-vector v (held by the row's lanes) - whole warp must call
+template <int SCHED, typename T>
+__device__ __forceinline__ T row_component(T v, int q) {
+  const int lane = threadIdx.x & 31;
+  const int base = SCHED == kWarpRow ? 0 : 6 * ((lane / 6) < 5 ? lane / 6 : 4);
+  return __shfl_sync(0xffffffffu, v, base + q);
+}
+
 }  // namespace svxg

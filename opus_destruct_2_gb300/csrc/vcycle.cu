@@ -67,13 +67,14 @@ __device__ __forceinline__ float row_block_sum(int32_t k0, int32_t k1, const int
   return warp_row_product<float, float, float>(k0, k1, col, val, x);
 }
 
-// (D^-1 v)_c for lane c < 6, v held by lanes 0-5
-__device__ __forceinline__ float dinv_row(const float* __restrict__ D, float v, int c) {
+// (D^-1 v)_c for the row's lane c, v held by the row's six lanes
+template <int SCHED>
+__device__ __forceinline__ float dinv_row(const float* __restrict__ D, float v, int c, bool act) {
   float s = 0.0f;
 #pragma unroll
   for (int q = 0; q < 6; ++q) {
-    const float vq = __shfl_sync(0xffffffffu, v, q);
-    if (c < 6) s += __ldg(D + 6 * c + q) * vq;
+    const float vq = row_component<SCHED>(v, q);
+    if (act) s += __ldg(D + 6 * c + q) * vq;
   }
   return s;
 }
@@ -98,25 +99,27 @@ struct StepArgs {
   int x_last;        // kStep: also add dout (the last step)
 };
 
-template <int MODE>
+template <int MODE, int SCHED>
 __global__ void __launch_bounds__(kT) k_bsr32(int32_t n, const int32_t* __restrict__ rowptr,
                                               const int32_t* __restrict__ col, const float* __restrict__ val,
                                               const float* __restrict__ v, float* y, StepArgs s) {
   if (s.stop && *s.stop) return;
-  const int lane = threadIdx.x & 31;
-  const int32_t row = blockIdx.x * kRows + (threadIdx.x >> 5);
-  if (row >= n) return;  // (whole warps exit together)
-  const float av = row_block_sum(rowptr[row], rowptr[row + 1], col, val, v);
-  const int c = lane;
+  int c;
+  bool lane_ok;
+  const int32_t row = sched_row<SCHED>(kRows, &c, &lane_ok);
+  const bool row_ok = row < n;
+  if (SCHED == kWarpRow && !row_ok) return;  // (whole warps exit together)
+  const float av = sched_row_product<SCHED, float, float, float>(row_ok, row, rowptr, col, val, v);
+  const bool act = lane_ok && row_ok;
   const int64_t o = 6 * int64_t(row) + c;
   if (MODE == kY) {
-    if (c < 6) y[o] = av;
+    if (act) y[o] = av;
   } else if (MODE == kAcc) {
-    if (c < 6) y[o] += av;
+    if (act) y[o] += av;
   } else if (MODE == kStep) {
-    const float rv = c < 6 ? s.rin[o] - av : 0.0f;
-    const float z = dinv_row(s.D + 36 * int64_t(row), rv, c);
-    if (c < 6) {
+    const float rv = act ? s.rin[o] - av : 0.0f;
+    const float z = dinv_row<SCHED>(s.D + 36 * int64_t(row_ok ? row : 0), rv, c, act);
+    if (act) {
       const float dprev = v[o];
       const float dn = s.c1 * dprev + s.c2 * z;
       s.r[o] = rv;
@@ -126,17 +129,29 @@ __global__ void __launch_bounds__(kT) k_bsr32(int32_t n, const int32_t* __restri
       s.x[o] = xv;
     }
   } else if (MODE == kResPend) {
-    if (c < 6) {
+    if (act) {
       s.r[o] = s.rin[o] - av;
       s.x[o] += v[o];
     }
   } else if (MODE == kPostStart) {
-    const float rv = c < 6 ? s.rin[o] - av : 0.0f;
-    const float z = dinv_row(s.D + 36 * int64_t(row), rv, c);
-    if (c < 6) {
+    const float rv = act ? s.rin[o] - av : 0.0f;
+    const float z = dinv_row<SCHED>(s.D + 36 * int64_t(row_ok ? row : 0), rv, c, act);
+    if (act) {
       s.r[o] = rv;
       s.dout[o] = s.c2 * z;
     }
+  }
+}
+
+// launch of a mode with the operator's schedule (grid: one warp per row or per five rows)
+template <int MODE>
+void bsr32(cudaStream_t st, int sched, int32_t n, const int32_t* rowptr, const int32_t* col, const float* val,
+           const float* v, float* y, const StepArgs& s) {
+  if (sched == kGroupRow) {
+    const unsigned g = unsigned(std::max<int64_t>(1, (int64_t(n) + 5 * kRows - 1) / (5 * kRows)));
+    (k_bsr32<MODE, kGroupRow><<<g, kT, 0, st>>>(n, rowptr, col, val, v, y, s), SVXG_COUNT_LAUNCH());
+  } else {
+    (k_bsr32<MODE, kWarpRow><<<rblk(n), kT, 0, st>>>(n, rowptr, col, val, v, y, s), SVXG_COUNT_LAUNCH());
   }
 }
 
@@ -309,7 +324,7 @@ int smooth(Problem& P, const Level& L, const float* b, float* x, bool from_zero,
     s.r = L.r32;
     s.dout = d0;
     s.c2 = C.inv_theta;
-    (k_bsr32<kPostStart><<<rblk(n), kT, 0, st>>>(n, L.A.rowptr, L.A.col, L.A.val32, x, nullptr, s), SVXG_COUNT_LAUNCH());
+    bsr32<kPostStart>(st, L.sched_a, n, L.A.rowptr, L.A.col, L.A.val32, x, nullptr, s);
     s.rin = L.r32;
   }
   for (int i = 1; i < degree; ++i) {
@@ -320,7 +335,7 @@ int smooth(Problem& P, const Level& L, const float* b, float* x, bool from_zero,
     s.c2 = C.c2[i];
     s.x_init = (from_zero && i == 1) ? 1 : 0;
     s.x_last = (i == degree - 1 && !(from_zero && want_residual)) ? 1 : 0;
-    (k_bsr32<kStep><<<rblk(n), kT, 0, st>>>(n, L.A.rowptr, L.A.col, L.A.val32, d0, nullptr, s), SVXG_COUNT_LAUNCH());
+    bsr32<kStep>(st, L.sched_a, n, L.A.rowptr, L.A.col, L.A.val32, d0, nullptr, s);
     s.rin = L.r32;
     std::swap(d0, d1);
   }
@@ -331,7 +346,7 @@ int smooth(Problem& P, const Level& L, const float* b, float* x, bool from_zero,
     if (degree == 1) {
       SVXG_CUDA(cudaMemsetAsync(x, 0, sizeof(float) * 6 * size_t(n), st));
     }
-    (k_bsr32<kResPend><<<rblk(n), kT, 0, st>>>(n, L.A.rowptr, L.A.col, L.A.val32, d0, nullptr, s), SVXG_COUNT_LAUNCH());
+    bsr32<kResPend>(st, L.sched_a, n, L.A.rowptr, L.A.col, L.A.val32, d0, nullptr, s);
   } else if (degree == 1) {
     if (from_zero) {
       SVXG_CUDA(cudaMemcpyAsync(x, d0, sizeof(float) * 6 * size_t(n), cudaMemcpyDeviceToDevice, st));
@@ -360,12 +375,32 @@ int cycle(Problem& P, size_t l, const float* b, float* x) {
   StepArgs none{};
   none.stop = P.cycle_stop;
   // restriction: bc = P^T r
-  (k_bsr32<kY><<<rblk(C.A.n), kT, 0, st>>>(C.A.n, L.rrow, L.rent_i, L.pval32 + 36 * L.pnnz, L.r32, C.b32, none), SVXG_COUNT_LAUNCH());
+  bsr32<kY>(st, L.sched_r, C.A.n, L.rrow, L.rent_i, L.pval32 + 36 * L.pnnz, L.r32, C.b32, none);
   TRY(cycle(P, l + 1, C.b32, C.x32));
   // prolongation: x += P xc
-  (k_bsr32<kAcc><<<rblk(n), kT, 0, st>>>(n, L.prow, L.pcol, L.pval32, C.x32, x, none), SVXG_COUNT_LAUNCH());
+  bsr32<kAcc>(st, L.sched_p, n, L.prow, L.pcol, L.pval32, C.x32, x, none);
   TRY(smooth(P, L, b, x, false, kChebDegree, kChebRatio, false));
   return SVXG_OK;
+}
+
+// times y = A x with both schedules (a launch each to warm, then three) and returns the faster
+int tune_bsr32(cudaStream_t st, int32_t n, const int32_t* rowptr, const int32_t* col, const float* val, const float* x,
+               float* y) {
+  if (n <= 0) return kWarpRow;
+  StepArgs none{};
+  cudaEvent_t e[3];
+  for (auto& ev : e) cudaEventCreate(&ev);
+  float ms[2] = {0, 0};
+  for (int sch = 0; sch < 2; ++sch) {
+    bsr32<kY>(st, sch, n, rowptr, col, val, x, y, none);
+    cudaEventRecord(e[0], st);
+    for (int r = 0; r < 3; ++r) bsr32<kY>(st, sch, n, rowptr, col, val, x, y, none);
+    cudaEventRecord(e[1], st);
+    cudaEventSynchronize(e[1]);
+    cudaEventElapsedTime(&ms[sch], e[0], e[1]);
+  }
+  for (auto& ev : e) cudaEventDestroy(ev);
+  return ms[1] < ms[0] ? kGroupRow : kWarpRow;
 }
 
 }  // namespace
@@ -389,11 +424,20 @@ int prepare_cycle(Problem& P) {
       (k_cvt_transpose<<<nblk(L.pnnz), kT, 0, st>>>(L.pnnz, L.rent_e, L.pval, L.pval32 + 36 * L.pnnz), SVXG_COUNT_LAUNCH());
     }
     for (float** v : {&L.b32, &L.x32, &L.r32, &L.t32, &L.u32}) TRY(P.mem.alloc(v, 6 * size_t(std::max(n, 1))));
+    // the schedule of each of the level's operators: the faster of the two, timed here
+    SVXG_CUDA(cudaMemsetAsync(L.t32, 0, sizeof(float) * 6 * size_t(std::max(n, 1)), st));
+    L.sched_a = tune_bsr32(st, n, L.A.rowptr, L.A.col, L.A.val32, L.t32, L.u32);
     const bool last = l + 1 == P.lv.size();
     if (!last || P.chol_n == 0) {
       if (L.lmax > 0) L.cheb_lmax = L.lmax;
       else TRY(power_bound(P, L, &L.cheb_lmax));
     }
+  }
+  for (size_t l = 0; l + 1 < P.lv.size(); ++l) {
+    Level& L = P.lv[l];
+    const Level& C = P.lv[l + 1];
+    L.sched_p = tune_bsr32(st, L.A.n, L.prow, L.pcol, L.pval32, C.t32, L.u32);
+    L.sched_r = tune_bsr32(st, C.A.n, L.rrow, L.rent_i, L.pval32 + 36 * L.pnnz, L.t32, C.u32);
   }
   if (P.chol_n > 0) {
     const int32_t m = P.chol_n;
