@@ -111,6 +111,21 @@ int svxg_utilization(svxg_problem* p, double fragility, double* phi, uint8_t* mo
 int svxg_utilization_device(svxg_problem* p, double fragility, double* phi_dev, uint8_t* mode_dev, int32_t* over_dev,
                             int32_t* n_over);
 
+/* No counterpart in the reference. The same judge for hosts that cannot let a library allocate
+ * device memory (an engine that owns all of HBM through its own pool, whose frame loop must not
+ * block on cudaMalloc/cudaFree): no problem handle, everything in the caller's device buffers -
+ * the graph (nodes: n, bonds: nb, mats: SVXG_MAX_MATERIALS records), u (6 n doubles, node order),
+ * phi (nb doubles), mode (nb bytes), over (nb int32; phi, mode and over may be null), on `stream`
+ * (a cudaStream_t, null: the legacy default stream) of the current device; *n_over (host) gets
+ * the failure count after the stream synchronizes. Allocates nothing: its scratch is one
+ * 512 KiB array in the library's device image, so at most 16,777,216 bonds (more: SVXG_ERR_ARG).
+ * A device's first call looks that array up (cudaGetSymbolAddress), so make it before any stream
+ * capture. Calls share the array: calls that overlap on the GPU race and must be ordered by the
+ * caller. Node indices and material ids out of range: SVXG_ERR_ARG, those bonds skipped. */
+int svxg_utilization_noalloc(const svxg_node* nodes_dev, int32_t n, const svxg_bond* bonds_dev, int32_t nb,
+                             const svxg_material* mats_dev, const double* u_dev, double fragility, double* phi_dev,
+                             uint8_t* mode_dev, int32_t* over_dev, int32_t* n_over, void* stream);
+
 /* --- counters ------------------------------------------------------------------------------- */
 int svxg_get_info(svxg_problem* p, svxg_info* info);
 /* Kernel launches made by this library since it was loaded (all problems, all threads). */
