@@ -42,7 +42,7 @@ typedef struct svxg_info {
   int64_t matrix_blocks, work_per_iteration, assembly_work, work_per_apply, build_work;
   int64_t device_bytes;     /* what the problem holds on the device now */
   int32_t precision;        /* SVXG_PRECISION_* of the last assemble */
-  int32_t pad;
+  int32_t mixed_fallbacks;  /* mixed-precision solves since then finished in FP64 (FP32 stalled) */
 } svxg_info;
 
 const char* svxg_last_error(void);
@@ -149,6 +149,24 @@ int svxg_debug_precondition(svxg_problem* p, const double* r, double* z);
  * (the multigrid setup's exact norm): for checking it against a sequential host loop. */
 int svxg_debug_seq_norm(const double* v, int64_t n, double* out);
 int svxg_debug_apply(svxg_problem* p, const double* x, double* y);
+
+/* Schedule timings of the last assemble, recorded when the environment sets SVXG_TUNE_LOG=1 or
+ * SVXG_TUNE_LIVE=1 before the library loads (the autotuner's input): per BSR operator its kind
+ * (0: K in FP64, 1: a level's A in FP32, 2: prolongation, 3: restriction), level, block rows,
+ * blocks and the time of three products with each row schedule. Without them the schedules come
+ * from the committed table alone and nothing is timed. */
+typedef struct svxg_tune_entry {
+  int32_t kind, level;
+  int64_t rows, blocks;
+  float ms_warp_row, ms_group_row;
+} svxg_tune_entry;
+int svxg_debug_tune_log(svxg_problem* p, svxg_tune_entry* out, int32_t cap, int32_t* count);
+
+/* The host-side trace of the last assemble and host solve when the environment sets SVXG_TRACE=1
+ * before the library loads (the stream is drained at each mark, so device time lands on the
+ * phase that queued it): lines of "microseconds since the assemble began, since the previous
+ * mark, label". Returns the text's length; writes at most cap - 1 characters and a 0. */
+int svxg_debug_trace(svxg_problem* p, char* out, int32_t cap);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,101 @@
+/* svxg_server.h - many stress solves in flight on one GPU: the serving loop and the batched solve.
+ *
+ * The reference solves many independent graphs at once only on the host: piece checks call
+ * distinct StressProblem objects from pool threads, one graph per thread under SerialScope
+ * (core/src/world/world_pieces.cpp:1460-1463). This is that pattern for a GPU-resident solve,
+ * plus what a request loop needs: admission against an HBM budget, structures kept resident
+ * between requests (K, the multigrid hierarchy and the last displacement stay on the device),
+ * warm-started repeat solves after in-place bond removal, and per-request latency.
+ *
+ * A server owns `workers` host threads (its slots). Each takes the oldest waiting request, runs
+ * it on a problem of its own (its own CUDA stream: the solves of different requests overlap on
+ * the device) and records the result under the request's ticket. A new structure is admitted
+ * when the bytes of the resident structures, of the requests running and of its own estimate
+ * fit in the budget; resident structures no request is using are evicted, least recently used
+ * first, to make room. Results are those of the single-problem entry points (svxg.h) for the
+ * same graph, load and options, bit for bit: every request runs the same kernels in the same
+ * order on its own buffers.
+ */
+#ifndef SVXG_SERVER_H
+#define SVXG_SERVER_H
+
+#include "svxg.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct svxg_server svxg_server;
+
+/* A finished request. 64 bytes. */
+typedef struct svxg_request_result {
+  int64_t ticket;
+  int32_t status;     /* SVXG_OK, or the error of the step that failed */
+  int32_t iters, converged, breakdown;
+  int32_t failing;    /* bonds with phi >= 1 after the solve */
+  int32_t warm;       /* 1: started from the structure's last solution on the device */
+  double rel_res;
+  double queue_ms;    /* submission -> a slot took it */
+  double latency_ms;  /* submission -> result recorded */
+  double pad;
+} svxg_request_result;
+
+/* Counters since creation (or the last reset). 96 bytes. */
+typedef struct svxg_serving_stats {
+  int64_t completed, failed, evictions, admission_waits;
+  int64_t resident, resident_bytes, peak_bytes; /* structures kept, their bytes, peak admitted bytes */
+  int64_t pad;
+  double p50_ms, p99_ms, max_ms; /* request latency */
+  double wall_s;                 /* first submission -> last completion */
+} svxg_serving_stats;
+
+/* A server on `device` with `workers` slots admitting up to `hbm_budget_bytes` of problem memory. */
+int svxg_server_create(svxg_server** out, int device, int64_t hbm_budget_bytes, int32_t workers);
+/* Finishes the requests already submitted, then frees everything. */
+void svxg_server_destroy(svxg_server* s);
+
+/* A solve of a new graph: assemble (options `opt`, null: defaults), solve from zero to `rtol`
+ * (maxit < 0: no cap), judge at `fragility`. The graph, material table and load are copied;
+ * u_out (6 n doubles) and over_out (nb int32: the failing bonds, ascending) may be null, and
+ * must stay valid until the request is waited for. structure >= 0 keeps the problem resident
+ * under that id (replacing an earlier one) for repeat requests. Returns a ticket (> 0) or an
+ * error code (< 0). */
+int64_t svxg_server_submit(svxg_server* s, int64_t structure, const svxg_node* nodes, int32_t n,
+                           const svxg_bond* bonds, int32_t nb, const svxg_material* mats, const double* f,
+                           const svxg_stress_options* opt, double rtol, int32_t maxit, double fragility,
+                           double* u_out, int32_t* over_out);
+
+/* A repeat solve of resident structure `structure`: remove the listed bonds in place (the
+ * reference's remove_bond: K downdated, the preconditioner kept), solve from the structure's last
+ * solution, judge. n: its node count (f: 6 n doubles). A structure evicted or never kept returns
+ * status SVXG_ERR_STATE in its result: submit the graph again. */
+int64_t svxg_server_submit_repeat(svxg_server* s, int64_t structure, const int32_t* remove, int32_t nremove,
+                                  const double* f, int32_t n, double rtol, int32_t maxit, double fragility,
+                                  double* u_out, int32_t* over_out);
+
+/* Blocks until the ticket's request has finished; its result is handed over once. */
+int svxg_server_wait(svxg_server* s, int64_t ticket, svxg_request_result* out);
+/* Blocks until every submitted request has finished. */
+int svxg_server_drain(svxg_server* s);
+int svxg_server_stats(svxg_server* s, svxg_serving_stats* out);
+int svxg_server_reset_stats(svxg_server* s);
+/* The bytes admission reserves for a new structure of n nodes and nb bonds while it runs (its
+ * actual bytes replace the estimate once it is resident). */
+int64_t svxg_server_estimate_bytes(int32_t n, int32_t nb);
+/* Drops a resident structure (no effect while a request uses it: it is dropped afterwards). */
+int svxg_server_forget(svxg_server* s, int64_t structure);
+
+/* The batched solve: `count` independent graphs (arrays of per-graph pointers and sizes; one
+ * material table), each assembled, solved from zero and judged as one request of `s`; returns
+ * when all have finished. u_out and over_out (arrays of per-graph buffers) may be null. */
+int svxg_batch_solve(svxg_server* s, int32_t count, const svxg_node* const* nodes, const int32_t* n,
+                     const svxg_bond* const* bonds, const int32_t* nb, const svxg_material* mats,
+                     const double* const* f, const svxg_stress_options* opt, double rtol, int32_t maxit,
+                     double fragility, double* const* u_out, int32_t* const* over_out,
+                     svxg_request_result* results);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SVXG_SERVER_H */

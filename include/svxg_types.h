@@ -83,8 +83,11 @@ typedef struct svxg_amg_options {
 
 /* Arithmetic of the solve. */
 enum {
-  SVXG_PRECISION_FP64 = 0,  /* FP64 K, FP64 PCG; FP32 V-cycle (as the reference) */
-  SVXG_PRECISION_MIXED = 1  /* FP32 K and V-cycle inside FP64 iterative refinement */
+  SVXG_PRECISION_FP64 = 0,      /* FP64 K, FP64 PCG; FP32 V-cycle (as the reference) */
+  SVXG_PRECISION_MIXED = 1,     /* FP32 K and V-cycle inside FP64 iterative refinement, for
+                                   problems of 4096 free nodes or more (smaller ones are
+                                   latency-bound: they run the FP64 sequence) */
+  SVXG_PRECISION_MIXED_ALL = 2  /* the same at every size */
 };
 
 typedef struct svxg_stress_options {

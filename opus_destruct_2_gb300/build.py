@@ -37,7 +37,7 @@ def _newest(paths: list[str]) -> float:
 
 
 def _headers() -> list[str]:
-    return glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.hpp")) + \
+    return sum((glob.glob(os.path.join(CSRC, pat)) for pat in ("*.cuh", "*.hpp", "*.h")), []) + \
         glob.glob(os.path.join(INCLUDE, "*.h"))
 
 

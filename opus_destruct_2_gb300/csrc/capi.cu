@@ -6,7 +6,10 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <cstdlib>
+#include <mutex>
 #include <new>
 
 #include "problem.cuh"
@@ -111,9 +114,106 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 void uncount_launches(int64_t n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
 void add_launches(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+namespace {
+
+constexpr int kPoolDevices = 64;
+std::mutex g_pool_mu;
+cudaMemPool_t g_pool[kPoolDevices] = {};
+
+// The library's pool on `dev`: it keeps what is freed (no release threshold), and it never makes
+// one stream wait for another to reuse memory (a stream reuses only what its own order, or a
+// finished free, allows), so concurrent problems do not serialize through the allocator.
+cudaError_t library_pool(int dev, cudaMemPool_t* out) {
+  if (dev < 0 || dev >= kPoolDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  if (!g_pool[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    cudaError_t e = cudaMemPoolCreate(&pool, &props);
+    if (e != cudaSuccess) return e;
+    uint64_t keep = UINT64_MAX;
+    int no = 0;
+    e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    if (e == cudaSuccess) e = cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no);
+    if (e != cudaSuccess) {
+      cudaMemPoolDestroy(pool);
+      return e;
+    }
+    g_pool[dev] = pool;
+  }
+  *out = g_pool[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+namespace {
+
+std::atomic<int> g_blocking{[] {
+  const char* v = std::getenv("SVXG_BLOCKING_SYNC");
+  return v && v[0] && v[0] != '0' ? 1 : 0;
+}()};
+
+// one blocking-sync event per host thread (and device)
+struct WaitEvent {
+  cudaEvent_t ev = nullptr;
+  int device = -1;
+  ~WaitEvent() {
+    if (ev) cudaEventDestroy(ev);
+  }
+};
+thread_local WaitEvent t_wait;
+
+}  // namespace
+
+void blocking_waits(bool on) { g_blocking.fetch_add(on ? 1 : -1); }
+
+cudaError_t host_wait(cudaStream_t s) {
+  if (g_blocking.load(std::memory_order_relaxed) <= 0) return cudaStreamSynchronize(s);
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (!t_wait.ev || t_wait.device != dev) {
+    if (t_wait.ev) cudaEventDestroy(t_wait.ev);
+    t_wait.ev = nullptr;
+    e = cudaEventCreateWithFlags(&t_wait.ev, cudaEventBlockingSync | cudaEventDisableTiming);
+    if (e != cudaSuccess) return e;
+    t_wait.device = dev;
+  }
+  e = cudaEventRecord(t_wait.ev, s);
+  if (e != cudaSuccess) return e;
+  return cudaEventSynchronize(t_wait.ev);
+}
+
+cudaError_t pool_malloc_async(void** p, size_t bytes, cudaStream_t s) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  cudaMemPool_t pool = nullptr;
+  e = library_pool(dev, &pool);
+  if (e != cudaSuccess) return e;
+  return cudaMallocFromPoolAsync(p, bytes, pool, s);
+}
+
 }  // namespace svxg
 
 using namespace svxg;
+
+namespace svxg {
+
+int ensure_node_vectors(Problem& P) {
+  if (!P.d_un) TRY(P.mem.alloc(&P.d_un, 12 * size_t(std::max(P.n, 1))));  // u, then f
+  if (!P.mem.holds(P.d_un, 12 * sizeof(double) * size_t(std::max(P.n, 1)))) {
+    set_error("node vectors: buffer does not hold 12 n doubles");
+    return SVXG_ERR_STATE;
+  }
+  return SVXG_OK;
+}
+
+}  // namespace svxg
 
 extern "C" {
 
@@ -131,7 +231,7 @@ int svxg_timer_read(svxg_problem* p, double* ms_total, int64_t* launches) {
   CHECK_P(p);
   Problem& P = p->P;
   DeviceScope ds(P.device);
-  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  SVXG_CUDA(host_wait(P.stream));
   double tot = 0.0;
   for (size_t k = 0; k + 1 < 2 * P.timer_used + 1 && k / 2 < P.timer_used; k += 2) {
     float ms = 0.0f;
@@ -170,6 +270,7 @@ int svxg_problem_create(svxg_problem** out, int device) {
     delete p;
     return SVXG_ERR_CUDA;
   }
+  p->P.mem.stream = p->P.stream;
   p->P.opt = svxg_default_options();
   *out = p;
   return SVXG_OK;
@@ -178,8 +279,10 @@ int svxg_problem_create(svxg_problem** out, int device) {
 void svxg_problem_destroy(svxg_problem* p) {
   if (!p) return;
   DeviceScope ds(p->P.device);
-  cudaStreamSynchronize(p->P.stream);
+  destroy_loop(p->P.loop_plain);
+  destroy_loop(p->P.loop_mixed);
   p->P.mem.release_all();
+  host_wait(p->P.stream);
   for (cudaEvent_t e : p->P.timer_events) cudaEventDestroy(e);
   if (p->P.h_s) cudaFreeHost(p->P.h_s);
   if (p->P.h_ms) cudaFreeHost(p->P.h_ms);
@@ -222,7 +325,7 @@ int svxg_set_graph(svxg_problem* p, const svxg_node* nodes, int32_t n, const svx
   if (nb) SVXG_CUDA(cudaMemcpyAsync(P.d_bonds, bonds, sizeof(svxg_bond) * size_t(nb), cudaMemcpyHostToDevice, P.stream));
   SVXG_CUDA(cudaMemcpyAsync(P.d_mats, mats, sizeof(svxg_material) * SVXG_MAX_MATERIALS, cudaMemcpyHostToDevice,
                             P.stream));
-  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  SVXG_CUDA(host_wait(P.stream));
   P.have_graph = true;
   return SVXG_OK;
 }
@@ -235,9 +338,14 @@ static int assemble_impl(Problem& P, const svxg_stress_options* opt, int32_t* ok
   }
   DeviceScope ds(P.device);
   P.opt = opt ? *opt : svxg_default_options();
+  trace_mark(P, "start", true);
   release_solver(P);
+  P.tune_log.clear();
+  P.mixed_fallbacks = 0;
+  P.host_loops = 0;
   P.pc_current = true;
   TRY(assemble_matrix(P));
+  trace_mark(P, "K assembled");
   P.assembly_work = 0;
   for (const svxg_bond& b : P.h_bonds)
     if (b.in_k) P.assembly_work += 48;
@@ -254,9 +362,10 @@ static int assemble_impl(Problem& P, const svxg_stress_options* opt, int32_t* ok
     }
     P.assembly_work += P.amg_build_work;
   }
+  trace_mark(P, "preconditioner built");
   TRY(tune_k64(P));
   P.sched_k32 = P.jacobi_only || P.lv.empty() ? 0 : P.lv[0].sched_a;  // (K32 is level 0's cycle operator)
-  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  SVXG_CUDA(host_wait(P.stream));
   P.assembled = true;
   if (ok) *ok = 1;
   return SVXG_OK;
@@ -282,7 +391,7 @@ int svxg_block_jacobi(const svxg_problem* p) { return p && p->P.jacobi_only ? 1 
 int svxg_release(svxg_problem* p) {
   CHECK_P(p);
   DeviceScope ds(p->P.device);
-  cudaStreamSynchronize(p->P.stream);
+  host_wait(p->P.stream);
   release_solver(p->P);
   for (svxg_bond& b : p->P.h_bonds) b.in_k = 0;
   return SVXG_OK;
@@ -300,7 +409,7 @@ int svxg_remove_bond(svxg_problem* p, int32_t b) {
   hb.broken = 1;
   if (!P.assembled || !hb.in_k) {
     TRY(upload_bond_flags(P, b));
-    SVXG_CUDA(cudaStreamSynchronize(P.stream));
+    SVXG_CUDA(host_wait(P.stream));
     return SVXG_OK;
   }
   hb.in_k = 0;
@@ -353,7 +462,7 @@ int svxg_retire_nodes(svxg_problem* p, const int32_t* list, int32_t count) {
     }
     TRY(set_identity_rows(P, rows.data(), int32_t(rows.size())));
   }
-  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  SVXG_CUDA(host_wait(P.stream));
   P.active = false;
   return SVXG_OK;
 }
@@ -367,14 +476,6 @@ int svxg_bond_flags(svxg_problem* p, uint8_t* broken, uint8_t* in_k) {
   return SVXG_OK;
 }
 
-static int ensure_node_vectors(Problem& P) {
-  if (!P.d_un) TRY(P.mem.alloc(&P.d_un, 12 * size_t(std::max(P.n, 1))));  // u, then f
-  if (!P.mem.holds(P.d_un, 12 * sizeof(double) * size_t(std::max(P.n, 1)))) {
-    set_error("node vectors: buffer does not hold 12 n doubles");
-    return SVXG_ERR_STATE;
-  }
-  return SVXG_OK;
-}
 
 static int ensure_assembled(Problem& P) {
   if (P.assembled) return SVXG_OK;
@@ -395,17 +496,20 @@ static void failed_result(svxg_pcg_result* res) {
 static int solve_common(Problem& P, const double* f_dev, double* u_dev, double rtol, int32_t maxit, int32_t warm,
                         svxg_pcg_result* res) {
   TRY(pcg_begin(P, f_dev, warm ? u_dev : nullptr));
+  trace_mark(P, "solve: begin");
   TRY(pcg_iterate(P, maxit < 0 ? 100000 : maxit, rtol, res));
+  trace_mark(P, "solve: iterate");
   TRY(gather_solution(P, u_dev));
   P.active = false;
   return SVXG_OK;
 }
 
-int svxg_solve(svxg_problem* p, const double* f, double* u, double rtol, int32_t maxit, int32_t warm,
-               svxg_pcg_result* res) {
-  CHECK_P(p);
-  Problem& P = p->P;
-  if (!f || !u) return SVXG_ERR_ARG;
+}  // extern "C"
+
+namespace svxg {
+
+int solve_nodes_host(Problem& P, const double* f, double* u, double rtol, int32_t maxit, int warm,
+                     svxg_pcg_result* res) {
   DeviceScope ds(P.device);
   const int a = ensure_assembled(P);
   if (a < 0) return a;
@@ -413,16 +517,30 @@ int svxg_solve(svxg_problem* p, const double* f, double* u, double rtol, int32_t
     failed_result(res);
     return SVXG_OK;
   }
+  const bool resident = warm == kWarmResident && P.d_un && P.mem.holds(P.d_un, 12 * sizeof(double) * size_t(P.n));
   TRY(ensure_node_vectors(P));
   const size_t m = 6 * size_t(P.n);
   double* du = P.d_un;
   double* df = P.d_un + m;
   SVXG_CUDA(cudaMemcpyAsync(df, f, m * sizeof(double), cudaMemcpyHostToDevice, P.stream));
-  if (warm) SVXG_CUDA(cudaMemcpyAsync(du, u, m * sizeof(double), cudaMemcpyHostToDevice, P.stream));
-  TRY(solve_common(P, df, du, rtol, maxit, warm, res));
-  SVXG_CUDA(cudaMemcpyAsync(u, du, m * sizeof(double), cudaMemcpyDeviceToHost, P.stream));
-  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  if (warm == kWarmHost) SVXG_CUDA(cudaMemcpyAsync(du, u, m * sizeof(double), cudaMemcpyHostToDevice, P.stream));
+  trace_mark(P, "solve: load copied");
+  TRY(solve_common(P, df, du, rtol, maxit, warm == kWarmHost || resident ? 1 : 0, res));
+  if (u) SVXG_CUDA(cudaMemcpyAsync(u, du, m * sizeof(double), cudaMemcpyDeviceToHost, P.stream));
+  SVXG_CUDA(host_wait(P.stream));
+  trace_mark(P, "solve: u copied back");
   return SVXG_OK;
+}
+
+}  // namespace svxg
+
+extern "C" {
+
+int svxg_solve(svxg_problem* p, const double* f, double* u, double rtol, int32_t maxit, int32_t warm,
+               svxg_pcg_result* res) {
+  CHECK_P(p);
+  if (!f || !u) return SVXG_ERR_ARG;
+  return solve_nodes_host(p->P, f, u, rtol, maxit, warm ? kWarmHost : kCold, res);
 }
 
 int svxg_solve_device(svxg_problem* p, const double* f_dev, double* u_dev, double rtol, int32_t maxit, int32_t warm,
@@ -455,7 +573,7 @@ int svxg_begin(svxg_problem* p, const double* f, const double* u0) {
   SVXG_CUDA(cudaMemcpyAsync(df, f, m * sizeof(double), cudaMemcpyHostToDevice, P.stream));
   if (u0) SVXG_CUDA(cudaMemcpyAsync(du, u0, m * sizeof(double), cudaMemcpyHostToDevice, P.stream));
   TRY(pcg_begin(P, df, u0 ? du : nullptr));
-  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  SVXG_CUDA(host_wait(P.stream));
   return SVXG_OK;
 }
 
@@ -485,7 +603,7 @@ int svxg_current(svxg_problem* p, double* u) {
   TRY(ensure_node_vectors(P));
   TRY(gather_solution(P, P.d_un));
   SVXG_CUDA(cudaMemcpyAsync(u, P.d_un, m * sizeof(double), cudaMemcpyDeviceToHost, P.stream));
-  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  SVXG_CUDA(host_wait(P.stream));
   return SVXG_OK;
 }
 
@@ -504,7 +622,7 @@ int svxg_bond_loads(svxg_problem* p, const double* u, svxg_bond_load* out) {
     SVXG_CUDA(cudaMemsetAsync(P.d_un, 0, m * sizeof(double), P.stream));
   }
   svxg_bond_load* d = nullptr;
-  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d), sizeof(svxg_bond_load) * size_t(std::max(P.nb, 1)), P.stream));
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&d), sizeof(svxg_bond_load) * size_t(std::max(P.nb, 1)), P.stream));
   int e = bond_loads_device(P, P.d_un, d);
   if (!e && P.nb)
     e = cudaMemcpyAsync(out, d, sizeof(svxg_bond_load) * size_t(P.nb), cudaMemcpyDeviceToHost, P.stream) ==
@@ -512,7 +630,7 @@ int svxg_bond_loads(svxg_problem* p, const double* u, svxg_bond_load* out) {
             ? SVXG_OK
             : SVXG_ERR_CUDA;
   cudaFreeAsync(d, P.stream);
-  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  SVXG_CUDA(host_wait(P.stream));
   return e;
 }
 
@@ -532,9 +650,9 @@ int svxg_utilization(svxg_problem* p, double fragility, double* phi, uint8_t* mo
   double* dphi = nullptr;
   uint8_t* dmode = nullptr;
   int32_t* dover = nullptr;
-  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dphi), nb * sizeof(double), P.stream));
-  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dmode), nb, P.stream));
-  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dover), nb * sizeof(int32_t), P.stream));
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&dphi), nb * sizeof(double), P.stream));
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&dmode), nb, P.stream));
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&dover), nb * sizeof(int32_t), P.stream));
   int32_t cnt = 0;
   int e = utilization_device(P, P.d_un, fragility, dphi, dmode, dover, &cnt);
   if (!e && P.nb) {
@@ -546,7 +664,7 @@ int svxg_utilization(svxg_problem* p, double fragility, double* phi, uint8_t* mo
   cudaFreeAsync(dphi, P.stream);
   cudaFreeAsync(dmode, P.stream);
   cudaFreeAsync(dover, P.stream);
-  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  SVXG_CUDA(host_wait(P.stream));
   if (n_over) *n_over = cnt;
   return e;
 }
@@ -564,6 +682,32 @@ int svxg_utilization_device(svxg_problem* p, double fragility, double* phi_dev, 
     SVXG_CUDA(cudaMemsetAsync(P.d_un, 0, m * sizeof(double), P.stream));
   }
   return utilization_device(P, P.d_un, fragility, phi_dev, mode_dev, over_dev, n_over);
+}
+
+int svxg_debug_trace(svxg_problem* p, char* out, int32_t cap) {
+  CHECK_P(p);
+  std::string text;
+  const auto& tr = p->P.trace;
+  for (size_t i = 0; i < tr.size(); ++i) {
+    char line[160];
+    std::snprintf(line, sizeof(line), "%10.1f %10.1f  %s\n", tr[i].second - tr[0].second,
+                  i ? tr[i].second - tr[i - 1].second : 0.0, tr[i].first);
+    text += line;
+  }
+  if (out && cap > 0) {
+    const size_t k = std::min(text.size(), size_t(cap - 1));
+    std::memcpy(out, text.data(), k);
+    out[k] = 0;
+  }
+  return int(text.size());
+}
+
+int svxg_debug_tune_log(svxg_problem* p, svxg_tune_entry* out, int32_t cap, int32_t* count) {
+  CHECK_P(p);
+  const int32_t k = int32_t(p->P.tune_log.size());
+  if (count) *count = k;
+  for (int32_t i = 0; out && i < std::min(k, cap); ++i) out[i] = p->P.tune_log[size_t(i)];
+  return SVXG_OK;
 }
 
 int svxg_get_info(svxg_problem* p, svxg_info* info) {
@@ -587,6 +731,7 @@ int svxg_get_info(svxg_problem* p, svxg_info* info) {
   info->build_work = P.amg_build_work;
   info->device_bytes = P.mem.bytes;
   info->precision = P.opt.precision;
+  info->mixed_fallbacks = P.mixed_fallbacks;
   return SVXG_OK;
 }
 
@@ -666,7 +811,7 @@ int svxg_debug_apply(svxg_problem* p, const double* x, double* y) {
   SVXG_CUDA(cudaMalloc(&dy, (m + 1) * sizeof(double)));
   cudaMemcpy(dx, x, m * sizeof(double), cudaMemcpyHostToDevice);
   int e = spmv(P, P.K, dx, dy);
-  cudaStreamSynchronize(P.stream);
+  host_wait(P.stream);
   if (!e) cudaMemcpy(y, dy, m * sizeof(double), cudaMemcpyDeviceToHost);
   cudaFree(dx);
   cudaFree(dy);
@@ -684,7 +829,7 @@ int svxg_debug_precondition(svxg_problem* p, const double* r, double* z) {
   SVXG_CUDA(cudaMalloc(&dz, (m + 1) * sizeof(double)));
   cudaMemcpy(dr, r, m * sizeof(double), cudaMemcpyHostToDevice);
   int e = precondition(P, dr, dz);
-  cudaStreamSynchronize(P.stream);
+  host_wait(P.stream);
   if (!e) cudaMemcpy(z, dz, m * sizeof(double), cudaMemcpyDeviceToHost);
   cudaFree(dr);
   cudaFree(dz);

@@ -45,10 +45,10 @@ struct Tmp {
   int alloc(size_t n) {
     if (p) cudaFreeAsync(p, s);
     p = nullptr;
-    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&p), (n ? n : 1) * sizeof(T), s);
+    cudaError_t e = pool_malloc_async(reinterpret_cast<void**>(&p), (n ? n : 1) * sizeof(T), s);
     if (e != cudaSuccess) {
       cudaGetLastError();
-      set_error(std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
+      set_error(std::string("device allocation: ") + cudaGetErrorString(e));
       p = nullptr;
       return e == cudaErrorMemoryAllocation ? SVXG_ERR_NOMEM : SVXG_ERR_CUDA;
     }
@@ -74,11 +74,9 @@ __global__ void k_lmax_init(int64_t m, double* v) {
   if (k < m) v[k] = 1.0 + 0.001 * (double)(k % 7);
 }
 
-// y = A x in Bsr6::apply's order: one thread per (row, component), blocks in row order
-__global__ void k_spmv_exact(int32_t n, const int32_t* rowptr, const int32_t* col, const double* val, const double* x,
-                             double* y) {
-  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t >= 6 * int64_t(n)) return;
+// entry t = 6 i + r of A x in Bsr6::apply's order (blocks in row order)
+__device__ __forceinline__ double spmv_exact_entry(int64_t t, const int32_t* rowptr, const int32_t* col,
+                                                   const double* val, const double* x) {
   const int32_t i = int32_t(t / 6);
   const int r = int(t % 6);
   double yr = 0.0;
@@ -87,17 +85,11 @@ __global__ void k_spmv_exact(int32_t n, const int32_t* rowptr, const int32_t* co
     const double* xv = x + 6 * int64_t(col[k]);
     yr += m[0] * xv[0] + m[1] * xv[1] + m[2] * xv[2] + m[3] * xv[3] + m[4] * xv[4] + m[5] * xv[5];
   }
-  y[t] = yr;
-}
-
-__global__ void k_dinv_apply(int32_t n, const double* dinv, const double* w, double* v) {
-  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) mv6(dinv + 36 * int64_t(i), w + 6 * int64_t(i), v + 6 * int64_t(i));
+  return yr;
 }
 
 // nv = sqrt(sum of v_k^2 in index order): the sequential sum's exact bits, computed in parallel
-// (exact_sum.cuh). lam <- nv and v /= nv happen in k_lmax_step / k_lmax_scale; a zero or
-// non-finite norm stops the iteration.
+// (exact_sum.cuh).
 __global__ void __launch_bounds__(exact::kThreads) k_seq_norm(int64_t m, const double* v, double* out) {
   const double s = exact::sequential_sum(m, [v](int64_t k) {
     const double x = v[k];
@@ -107,22 +99,57 @@ __global__ void __launch_bounds__(exact::kThreads) k_seq_norm(int64_t m, const d
 }
 
 // state: [0] = lam, [1] = nv, [2] = stopped
-__global__ void k_lmax_scale(int64_t m, double* v, double* state) {
-  const double nv = state[1];
+// Power iteration, two launches a step: v' = D^-1 (A v) with one thread per entry (the node's six
+// entries of A v meet in shared memory, each in k_spmv_exact's order, then mv6's row), and the
+// exact norm with the step's lam / stop / scaling in the same block (levels of at most
+// kLmaxFusedMax unknowns; larger ones scale in a separate launch).
+constexpr int kApplyNodes = 32;  // nodes per block: 192 threads
+__global__ void __launch_bounds__(6 * kApplyNodes) k_lmax_apply(int32_t n, const int32_t* rowptr, const int32_t* col,
+                                                              const double* val, const double* dinv, const double* v,
+                                                              double* w, const double* state) {
+  __shared__ double y[6 * kApplyNodes];
   if (state[2] != 0.0) return;
-  if (!(nv > 0)) return;
-  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k < m) v[k] /= nv;
+  const int64_t t = int64_t(blockIdx.x) * (6 * kApplyNodes) + threadIdx.x;
+  const bool ok = t < 6 * int64_t(n);
+  y[threadIdx.x] = ok ? spmv_exact_entry(t, rowptr, col, val, v) : 0.0;
+  __syncthreads();
+  if (!ok) return;
+  const int32_t i = int32_t(t / 6);
+  const int r = int(t % 6);
+  const double* x = y + 6 * (threadIdx.x / 6);
+  const double* m = dinv + 36 * int64_t(i) + 6 * r;
+  w[t] = m[0] * x[0] + m[1] * x[1] + m[2] * x[2] + m[3] * x[3] + m[4] * x[4] + m[5] * x[5];
 }
 
-__global__ void k_lmax_step(double* state) {
+// nv = exact sequential norm of w; lam <- nv, or a stop on a zero or non-finite norm; v = w / nv
+// (all in this block when `scale`)
+__global__ void __launch_bounds__(exact::kThreads) k_lmax_norm(int64_t m, const double* w, double* v, double* state,
+                                                              int scale) {
+  __shared__ double nv_sh;
   if (state[2] != 0.0) return;
-  const double nv = state[1];
-  if (!(nv > 0)) {
-    state[2] = 1.0;
-    return;
+  const double s = exact::sequential_sum(m, [w](int64_t k) {
+    const double x = w[k];
+    return x * x;
+  });
+  if (threadIdx.x == 0) {
+    const double nv = sqrt(s);
+    nv_sh = nv;
+    state[1] = nv;
+    if (!(nv > 0)) state[2] = 1.0;
+    else state[0] = nv;
   }
-  state[0] = nv;
+  __syncthreads();
+  const double nv = nv_sh;
+  if (!scale || !(nv > 0)) return;
+  for (int64_t k = threadIdx.x; k < m; k += blockDim.x) v[k] = w[k] / nv;
+}
+
+// v = w / nv for a large level (after k_lmax_norm without scaling)
+__global__ void k_lmax_rescale(int64_t m, const double* w, double* v, const double* state) {
+  const double nv = state[1];
+  if (!(nv > 0) || state[2] != 0.0) return;
+  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (k < m) v[k] = w[k] / nv;
 }
 
 // ---- strength (amg.cpp:324-330) ------------------------------------------------------------------
@@ -541,6 +568,87 @@ __global__ void k_c_count(int32_t na, const int32_t* rrow, const int32_t* rent_i
   }
 }
 
+// The same columns for coarse levels of at most kBitmapCols rows, one warp per coarse row: the
+// row's candidate columns are marked in a bitmap in shared memory, which is then read in column
+// order (the serial insertion above costs the candidates times the row length per thread, and
+// coarse rows are long).
+constexpr int32_t kBitmapCols = 8192;
+constexpr int kBitmapWarps = 4;
+
+// the set bits of bm[0, words) as ascending column indices into out (whole warp); returns the count
+__device__ __forceinline__ int32_t warp_emit_bitmap(const unsigned* bm, int32_t words, int32_t* out, int lane) {
+  int32_t base = 0;
+  for (int32_t q0 = 0; q0 < words; q0 += 32) {
+    const int32_t q = q0 + lane;
+    const unsigned w = q < words ? bm[q] : 0u;
+    const int cnt = __popc(w);
+    int pre = cnt;
+    for (int d = 1; d < 32; d <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, pre, d);
+      if (lane >= d) pre += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, pre, 31);
+    int32_t pos = base + pre - cnt;
+    for (unsigned x = w; x; x &= x - 1) out[pos++] = 32 * q + (__ffs(x) - 1);
+    base += total;
+  }
+  return base;
+}
+__global__ void __launch_bounds__(32 * kBitmapWarps) k_c_count_bitmap(int32_t na, const int32_t* rrow,
+                                                                      const int32_t* rent_i, const int32_t* aprow,
+                                                                      const int32_t* apcol, int32_t* clen,
+                                                                      int32_t* scratch, const int64_t* soff) {
+  __shared__ unsigned bits[kBitmapWarps][kBitmapCols / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int32_t I = int32_t(blockIdx.x) * kBitmapWarps + wid;
+  if (I >= na) return;  // (whole warps leave together)
+  unsigned* bm = bits[wid];
+  const int32_t words = (na + 31) / 32;
+  for (int32_t q = lane; q < words; q += 32) bm[q] = 0u;
+  __syncwarp();
+  for (int32_t r = rrow[I]; r < rrow[I + 1]; ++r) {
+    const int32_t i = rent_i[r];
+    for (int32_t e = aprow[i] + lane; e < aprow[i + 1]; e += 32) {
+      const int32_t c = apcol[e];
+      atomicOr(&bm[c >> 5], 1u << (c & 31));
+    }
+  }
+  __syncwarp();
+  // the diagonal first, then the other columns ascending
+  const bool has_diag = (bm[I >> 5] >> (I & 31)) & 1u;
+  if (has_diag && lane == 0) bm[I >> 5] &= ~(1u << (I & 31));
+  __syncwarp();
+  int32_t* out = scratch + soff[I];
+  if (lane == 0) out[0] = I;
+  const int32_t len = 1 + warp_emit_bitmap(bm, words, out + 1, lane);
+  if (lane == 0) clen[I] = len;
+}
+
+// A P's columns per fine row for levels of at most kBitmapCols coarse nodes (one warp per row)
+__global__ void __launch_bounds__(32 * kBitmapWarps) k_ap_count_bitmap(int32_t n, int32_t na, const int32_t* rowptr,
+                                                                       const int32_t* col, const int32_t* prow,
+                                                                       const int32_t* pcol, int32_t* aplen,
+                                                                       int32_t* scratch, const int64_t* soff) {
+  __shared__ unsigned bits[kBitmapWarps][kBitmapCols / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int32_t i = int32_t(blockIdx.x) * kBitmapWarps + wid;
+  if (i >= n) return;
+  unsigned* bm = bits[wid];
+  const int32_t words = (na + 31) / 32;
+  for (int32_t q = lane; q < words; q += 32) bm[q] = 0u;
+  __syncwarp();
+  for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+    const int32_t j = col[k];
+    for (int32_t e = prow[j] + lane; e < prow[j + 1]; e += 32) {
+      const int32_t c = pcol[e];
+      atomicOr(&bm[c >> 5], 1u << (c & 31));
+    }
+  }
+  __syncwarp();
+  const int32_t len = warp_emit_bitmap(bm, words, scratch + soff[i], lane);
+  if (lane == 0) aplen[i] = len;
+}
+
 __global__ void k_c_values(int32_t na, const int32_t* rrow, const int32_t* rent_i, const int32_t* rent_e,
                            const double* pval, const int32_t* aprow, const int32_t* apcol, const double* apval,
                            const int32_t* crow, const int32_t* scratch, const int64_t* soff, int32_t* ccol,
@@ -572,6 +680,53 @@ __global__ void k_c_values(int32_t na, const int32_t* rrow, const int32_t* rent_
       warp_mul6_add(true, Pi, apval + 36 * int64_t(e), cval + 36 * int64_t(slot), lane);
       __syncwarp();
     }
+  }
+  if (scale != 1.0)
+    for (int64_t q = 36 * int64_t(c0) + lane; q < 36 * int64_t(c1); q += 32) cval[q] *= scale;
+}
+
+// The same for long A P rows (coarse levels): the lanes take distinct entries e of one A P row -
+// distinct columns, so distinct blocks of C - and each computes its whole 6x6 product with
+// warp_mul6_add's additions; restriction entries r stay in order, so every block of C sees the
+// same sequence of additions as in k_c_values.
+__global__ void k_c_values_lanes(int32_t na, const int32_t* rrow, const int32_t* rent_i, const int32_t* rent_e,
+                                 const double* pval, const int32_t* aprow, const int32_t* apcol, const double* apval,
+                                 const int32_t* crow, const int32_t* scratch, const int64_t* soff, int32_t* ccol,
+                                 double* cval, double scale) {
+  const int lane = threadIdx.x & 31;
+  const int32_t I = int32_t((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  if (I >= na) return;
+  const int32_t c0 = crow[I], c1 = crow[I + 1];
+  for (int32_t c = c0 + lane; c < c1; c += 32) ccol[c] = scratch[soff[I] + (c - c0)];
+  for (int64_t q = 36 * int64_t(c0) + lane; q < 36 * int64_t(c1); q += 32) cval[q] = 0.0;
+  __syncwarp();
+  for (int32_t r = rrow[I]; r < rrow[I + 1]; ++r) {
+    const int32_t i = rent_i[r];
+    const double* Pi = pval + 36 * int64_t(rent_e[r]);
+    for (int32_t e = aprow[i] + lane; e < aprow[i + 1]; e += 32) {
+      const int32_t J = apcol[e];
+      int32_t slot;
+      if (J == I) {
+        slot = c0;
+      } else {
+        int32_t lo = c0 + 1, hi = c1 - 1;
+        while (lo < hi) {
+          const int32_t mid = (lo + hi) >> 1;
+          if (ccol[mid] < J) lo = mid + 1;
+          else hi = mid;
+        }
+        slot = lo;
+      }
+      const double* B = apval + 36 * int64_t(e);
+      double* C = cval + 36 * int64_t(slot);
+      for (int ent = 0; ent < 36; ++ent) {
+        const int rr = ent / 6, cc = ent - 6 * (ent / 6);
+        double sacc = 0.0;
+        for (int q = 0; q < 6; ++q) sacc += Pi[q * 6 + rr] * B[q * 6 + cc];
+        C[ent] = C[ent] + sacc;
+      }
+    }
+    __syncwarp();
   }
   if (scale != 1.0)
     for (int64_t q = 36 * int64_t(c0) + lane; q < 36 * int64_t(c1); q += 32) cval[q] *= scale;
@@ -612,80 +767,19 @@ __global__ void k_dense_fill(int32_t nc, const int32_t* rowptr, const int32_t* c
   }
 }
 
-__global__ void k_dense_dmax(int32_t m, const double* C, double* dmax) {
-  if (blockIdx.x || threadIdx.x) return;
-  double d = 0.0;
-  for (int32_t i = 0; i < m; ++i) d = maxd(d, fabs(C[int64_t(i) * m + i]));
-  *dmax = d;
-}
-
-__global__ void k_chol_diag(int32_t m, int32_t j, double* C, const double* dmax) {
-  if (blockIdx.x || threadIdx.x) return;
-  double d = C[int64_t(j) * m + j];
-  for (int32_t k = 0; k < j; ++k) d -= C[int64_t(j) * m + k] * C[int64_t(j) * m + k];
-  if (!(d > 1e-12 * *dmax)) d = maxd(1e-12 * *dmax, 1e-300);
-  C[int64_t(j) * m + j] = sqrt(d);
-}
-
-__global__ void k_chol_col(int32_t m, int32_t j, double* C) {
-  const int32_t i = j + 1 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m) return;
-  const double s = C[int64_t(j) * m + j];
-  double v = 0.5 * (C[int64_t(i) * m + j] + C[int64_t(j) * m + i]);
-  for (int32_t k = 0; k < j; ++k) v -= C[int64_t(i) * m + k] * C[int64_t(j) * m + k];
-  C[int64_t(i) * m + j] = v / s;
-}
-
-// the whole factor in one block: the reference's column loop (amg.cpp:555-573), each column's rows
-// split over the threads (each row's sum over k in the reference's order)
-__global__ void __launch_bounds__(1024) k_chol_block(int32_t m, double* C) {
-  __shared__ double dmax_sh, s_sh;
-  if (threadIdx.x == 0) {
-    double d = 0.0;
-    for (int32_t i = 0; i < m; ++i) d = maxd(d, fabs(C[int64_t(i) * m + i]));
-    dmax_sh = d;
-  }
-  __syncthreads();
-  const double dmax = dmax_sh;
-  for (int32_t j = 0; j < m; ++j) {
-    if (threadIdx.x == 0) {
-      double d = C[int64_t(j) * m + j];
-      for (int32_t k = 0; k < j; ++k) d -= C[int64_t(j) * m + k] * C[int64_t(j) * m + k];
-      if (!(d > 1e-12 * dmax)) d = maxd(1e-12 * dmax, 1e-300);
-      s_sh = sqrt(d);
-      C[int64_t(j) * m + j] = s_sh;
-    }
-    __syncthreads();
-    const double sj = s_sh;
-    for (int32_t i = j + 1 + threadIdx.x; i < m; i += blockDim.x) {
-      double v = 0.5 * (C[int64_t(i) * m + j] + C[int64_t(j) * m + i]);
-      for (int32_t k = 0; k < j; ++k) v -= C[int64_t(i) * m + k] * C[int64_t(j) * m + k];
-      C[int64_t(i) * m + j] = v / sj;
-    }
-    __syncthreads();
-  }
-}
-
-__global__ void k_chol_mirror(int32_t m, double* C) {
-  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t >= int64_t(m) * m) return;
-  const int32_t i = int32_t(t / m), k = int32_t(t % m);
-  if (k > i) C[t] = C[int64_t(k) * m + i];
-}
-
 // ---- host-side steps ---------------------------------------------------------------------------
 
 int copy_to_host(Problem& P, void* dst, const void* src, size_t bytes) {
   if (bytes == 0) return SVXG_OK;
   SVXG_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, P.stream));
-  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  SVXG_CUDA(host_wait(P.stream));
   return SVXG_OK;
 }
 
 // offsets of per-row scratch regions: an exclusive scan of the n bounds (bound[n] = 0)
 int offsets64(Problem& P, const int32_t* bound, int32_t n, int64_t* off, int64_t* total) {
   int32_t* scan32 = nullptr;
-  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&scan32), sizeof(int32_t) * (size_t(n) + 1), P.stream));
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&scan32), sizeof(int32_t) * (size_t(n) + 1), P.stream));
   int32_t t = 0;
   int e = exclusive_scan_i32(P, bound, scan32, int64_t(n) + 1, &t);
   if (!e) (k_widen_offsets<<<nblk(int64_t(n) + 1), kT, 0, P.stream>>>(n, scan32, off), SVXG_COUNT_LAUNCH());
@@ -714,6 +808,7 @@ int finalize_level(Problem& P, Level& L, bool* ok) {
 }
 
 // estimate_lmax of a level (amg.cpp:256-275), the value the reference computes
+constexpr int64_t kLmaxFusedMax = 1 << 17;
 int estimate_lmax(Problem& P, const Level& L, double* out) {
   const int32_t n = L.A.n;
   P.amg_build_work += 15 * (L.A.nnzb + n);
@@ -725,12 +820,13 @@ int estimate_lmax(Problem& P, const Level& L, double* out) {
   const double init[3] = {1.0, 0.0, 0.0};
   SVXG_CUDA(cudaMemcpyAsync(st.p, init, sizeof(init), cudaMemcpyHostToDevice, P.stream));
   (k_lmax_init<<<nblk(m), kT, 0, P.stream>>>(m, v.p), SVXG_COUNT_LAUNCH());
+  const bool fused = m <= kLmaxFusedMax;
+  const unsigned ab = unsigned((m + 6 * kApplyNodes - 1) / (6 * kApplyNodes));
   for (int it = 0; it < 15; ++it) {
-    (k_spmv_exact<<<nblk(m), kT, 0, P.stream>>>(n, L.A.rowptr, L.A.col, L.A.val, v.p, w.p), SVXG_COUNT_LAUNCH());
-    (k_dinv_apply<<<nblk(n), kT, 0, P.stream>>>(n, L.dinv, w.p, v.p), SVXG_COUNT_LAUNCH());
-    (k_seq_norm<<<1, exact::kThreads, 0, P.stream>>>(m, v.p, st.p + 1), SVXG_COUNT_LAUNCH());
-    (k_lmax_step<<<1, 1, 0, P.stream>>>(st.p), SVXG_COUNT_LAUNCH());
-    (k_lmax_scale<<<nblk(m), kT, 0, P.stream>>>(m, v.p, st.p), SVXG_COUNT_LAUNCH());
+    (k_lmax_apply<<<ab, 6 * kApplyNodes, 0, P.stream>>>(n, L.A.rowptr, L.A.col, L.A.val, L.dinv, v.p, w.p, st.p),
+     SVXG_COUNT_LAUNCH());
+    (k_lmax_norm<<<1, exact::kThreads, 0, P.stream>>>(m, w.p, v.p, st.p, fused ? 1 : 0), SVXG_COUNT_LAUNCH());
+    if (!fused) (k_lmax_rescale<<<nblk(m), kT, 0, P.stream>>>(m, w.p, v.p, st.p), SVXG_COUNT_LAUNCH());
   }
   SVXG_CUDA(cudaGetLastError());
   double h[3];
@@ -826,6 +922,7 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
   Level& C = P.lv[l + 1];
   F.parent = agg;
   C.A.n = na;
+  trace_mark(P, "coarsen: aggregated");
   // coarse positions and offsets
   {
     Tmp<int32_t> cnt(st), off(st), cursor(st), members(st);
@@ -844,6 +941,7 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
   Tmp<double> off3(st);
   TRY(off3.alloc(3 * size_t(n)));
   (k_offsets<<<nblk(n), kT, 0, st>>>(n, agg, F.pos, C.pos, off3.p), SVXG_COUNT_LAUNCH());
+  trace_mark(P, "coarsen: positions");
   // prolongation
   double omega = 0.0;
   if (smoothed) {
@@ -878,6 +976,7 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     TRY(copy_to_host(P, &w, acc.p, sizeof(w)));
     P.amg_build_work += int64_t(w);
   }
+  trace_mark(P, "coarsen: prolongation");
   // restriction lists
   {
     Tmp<int32_t> cnt(st), cursor(st), erow(st);
@@ -895,7 +994,9 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     (k_entry_rows<<<nblk(n), kT, 0, st>>>(n, F.prow, erow.p), SVXG_COUNT_LAUNCH());
     (k_r_sort<<<nblk(na), kT, 0, st>>>(na, F.rrow, F.rent_e, F.rent_i, erow.p), SVXG_COUNT_LAUNCH());
   }
+  trace_mark(P, "coarsen: restriction lists");
   // Galerkin: A P
+  int64_t apnnz_total = 0;
   Tmp<int32_t> aprow(st), apcol(st);
   Tmp<double> apval(st);
   {
@@ -912,9 +1013,16 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     Tmp<int32_t> aplen(st);
     TRY(aplen.alloc(size_t(n) + 1));
     SVXG_CUDA(cudaMemsetAsync(aplen.p, 0, sizeof(int32_t) * (size_t(n) + 1), st));
-    (k_ap_count<<<nblk(n), kT, 0, st>>>(n, F.A.rowptr, F.A.col, F.prow, F.pcol, aplen.p, scratch.p, soff.p, INT_MAX), SVXG_COUNT_LAUNCH());
+    if (na <= kBitmapCols)
+      (k_ap_count_bitmap<<<unsigned((n + kBitmapWarps - 1) / kBitmapWarps), 32 * kBitmapWarps, 0, st>>>(
+           n, na, F.A.rowptr, F.A.col, F.prow, F.pcol, aplen.p, scratch.p, soff.p),
+       SVXG_COUNT_LAUNCH());
+    else
+      (k_ap_count<<<nblk(n), kT, 0, st>>>(n, F.A.rowptr, F.A.col, F.prow, F.pcol, aplen.p, scratch.p, soff.p, INT_MAX),
+       SVXG_COUNT_LAUNCH());
     int32_t apnnz = 0;
     TRY(exclusive_scan_i32(P, aplen.p, aprow.p, int64_t(n) + 1, &apnnz));
+    apnnz_total = apnnz;
     TRY(apcol.alloc(size_t(apnnz)));
     TRY(apval.alloc(size_t(apnnz) * 36));
     (k_ap_values<<<nblk(32 * int64_t(n), 128), 128, 0, st>>>(n, F.A.rowptr, F.A.col, F.A.val, F.prow, F.pcol, F.pval, aprow.p,
@@ -929,6 +1037,7 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     TRY(copy_to_host(P, &w, acc.p, sizeof(w)));
     P.amg_build_work += int64_t(w);
   }
+  trace_mark(P, "coarsen: A P");
   // Galerkin: P^T (A P) by coarse row
   {
     Tmp<int32_t> bound(st), scratch(st), clen(st);
@@ -942,18 +1051,35 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     TRY(scratch.alloc(size_t(stotal) + 1));
     TRY(clen.alloc(size_t(na) + 1));
     SVXG_CUDA(cudaMemsetAsync(clen.p, 0, sizeof(int32_t) * (size_t(na) + 1), st));
-    (k_c_count<<<nblk(na), kT, 0, st>>>(na, F.rrow, F.rent_i, aprow.p, apcol.p, clen.p, scratch.p, soff.p, INT_MAX), SVXG_COUNT_LAUNCH());
+    if (na <= kBitmapCols)
+      (k_c_count_bitmap<<<unsigned((na + kBitmapWarps - 1) / kBitmapWarps), 32 * kBitmapWarps, 0, st>>>(
+           na, F.rrow, F.rent_i, aprow.p, apcol.p, clen.p, scratch.p, soff.p),
+       SVXG_COUNT_LAUNCH());
+    else
+      (k_c_count<<<nblk(na), kT, 0, st>>>(na, F.rrow, F.rent_i, aprow.p, apcol.p, clen.p, scratch.p, soff.p, INT_MAX),
+       SVXG_COUNT_LAUNCH());
     TRY(P.mem.alloc(&C.A.rowptr, size_t(na) + 1));
     int32_t cnnz = 0;
     TRY(exclusive_scan_i32(P, clen.p, C.A.rowptr, int64_t(na) + 1, &cnnz));
+    trace_mark(P, "coarsen: coarse pattern");
     C.A.nnzb = cnnz;
     TRY(P.mem.alloc(&C.A.col, size_t(cnnz)));
     TRY(P.mem.alloc(&C.A.val, size_t(cnnz) * 36));
     const double scale = (!smoothed && opt.coarse_scale != 1.0) ? opt.coarse_scale : 1.0;
-    (k_c_values<<<nblk(32 * int64_t(na), 128), 128, 0, st>>>(na, F.rrow, F.rent_i, F.rent_e, F.pval, aprow.p, apcol.p, apval.p,
-                                              C.A.rowptr, scratch.p, soff.p, C.A.col, C.A.val, scale), SVXG_COUNT_LAUNCH());
+    // (A P rows of 6 entries or more on average: the lanes over each row's entries)
+    if (apnnz_total >= 6 * int64_t(n))
+      (k_c_values_lanes<<<nblk(32 * int64_t(na), 128), 128, 0, st>>>(na, F.rrow, F.rent_i, F.rent_e, F.pval, aprow.p,
+                                                                      apcol.p, apval.p, C.A.rowptr, scratch.p, soff.p,
+                                                                      C.A.col, C.A.val, scale),
+       SVXG_COUNT_LAUNCH());
+    else
+      (k_c_values<<<nblk(32 * int64_t(na), 128), 128, 0, st>>>(na, F.rrow, F.rent_i, F.rent_e, F.pval, aprow.p, apcol.p,
+                                                                apval.p, C.A.rowptr, scratch.p, soff.p, C.A.col, C.A.val,
+                                                                scale),
+       SVXG_COUNT_LAUNCH());
   }
   SVXG_CUDA(cudaGetLastError());
+  trace_mark(P, "coarsen: coarse values");
   bool fin = false;
   TRY(finalize_level(P, P.lv[l + 1], &fin));
   if (!fin) {
@@ -984,10 +1110,11 @@ int factor_coarsest(Problem& P) {
   cudaStream_t st = P.stream;
   SVXG_CUDA(cudaMemsetAsync(P.d_chol, 0, sizeof(double) * size_t(m) * size_t(m), st));
   (k_dense_fill<<<nblk(L.A.n), kT, 0, st>>>(L.A.n, L.A.rowptr, L.A.col, L.A.val, m, P.d_chol), SVXG_COUNT_LAUNCH());
-  (k_chol_block<<<1, 1024, 0, st>>>(m, P.d_chol), SVXG_COUNT_LAUNCH());
-  (k_chol_mirror<<<nblk(int64_t(m) * m), kT, 0, st>>>(m, P.d_chol), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
-  return SVXG_OK;
+  // the factor (in place) and the inverse the cycle applies: dense.cu
+  TRY(P.mem.alloc(&P.d_cinv, 2 * size_t(m) * size_t(m)));
+  TRY(P.mem.alloc(&P.d_cvec, 2 * size_t(m)));
+  return dense_factor_inverse(P, m, P.d_chol, P.d_chol, P.d_cinv);
 }
 
 __global__ void k_level0_pos(int32_t n, const svxg_node* nodes, const int32_t* dof, double* pos) {
@@ -1028,6 +1155,7 @@ int build_hierarchy(Problem& P, int32_t* ok) {
     (k_level0_pos<<<nblk(P.n), kT, 0, P.stream>>>(P.n, P.d_nodes, P.d_dof, L0.pos), SVXG_COUNT_LAUNCH());
     bool fin = false;
     TRY(finalize_level(P, L0, &fin));
+    trace_mark(P, "level 0 finalized");
     if (!fin) {
       P.mem.release(L0.pos);
       P.mem.release(L0.dinv);
@@ -1043,10 +1171,12 @@ int build_hierarchy(Problem& P, int32_t* ok) {
     if (dense && !o.coarsen_dense) break;
     bool made = false;
     TRY(coarsen(P, P.lv.size() - 1, !dense && o.smoothed, &made));
+    trace_mark(P, "level coarsened");
     if (!made) break;
     if (dense) break;
   }
   TRY(factor_coarsest(P));
+  trace_mark(P, "coarsest factored");
   // work per apply (amg.cpp:306-316)
   for (size_t l = 0; l < P.lv.size(); ++l) {
     const bool last = l + 1 == P.lv.size();
@@ -1059,7 +1189,7 @@ int build_hierarchy(Problem& P, int32_t* ok) {
     P.amg_work += per * g;
   }
   TRY(prepare_cycle(P));
-  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  SVXG_CUDA(host_wait(P.stream));
   *ok = 1;
   return SVXG_OK;
 }

@@ -300,10 +300,10 @@ struct Tmp {
   cudaStream_t s;
   Tmp(cudaStream_t st) : s(st) {}
   int alloc(size_t n) {
-    cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&p), (n ? n : 1) * sizeof(T), s);
+    cudaError_t e = pool_malloc_async(reinterpret_cast<void**>(&p), (n ? n : 1) * sizeof(T), s);
     if (e != cudaSuccess) {
       cudaGetLastError();
-      set_error(std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
+      set_error(std::string("device allocation: ") + cudaGetErrorString(e));
       p = nullptr;
       return e == cudaErrorMemoryAllocation ? SVXG_ERR_NOMEM : SVXG_ERR_CUDA;
     }
@@ -401,7 +401,7 @@ int assemble_matrix(Problem& P) {
   if (n > 0) SVXG_CUDA(cudaMemcpyAsync(P.h_dof.data(), P.d_dof, sizeof(int32_t) * size_t(n), cudaMemcpyDeviceToHost, st));
   std::vector<uint8_t> ik(static_cast<size_t>(nb));
   if (nb > 0) SVXG_CUDA(cudaMemcpyAsync(ik.data(), P.d_in_k, size_t(nb), cudaMemcpyDeviceToHost, st));
-  SVXG_CUDA(cudaStreamSynchronize(st));
+  SVXG_CUDA(host_wait(st));
   for (int32_t k = 0; k < nb; ++k) P.h_bonds[size_t(k)].in_k = ik[size_t(k)];
   return SVXG_OK;
 }
@@ -423,7 +423,7 @@ int remove_bonds_device(Problem& P, const int32_t* list, int32_t count) {
   (k_remove_bonds<<<1, 1, 0, P.stream>>>(d.p, count, P.d_bonds, P.d_in_k, P.d_nodes, P.d_mats, P.d_dof, P.K.rowptr,
                                         P.K.col, P.K.val, P.d_jinv, P.jacobi_only ? 1 : 0, P.id_scale), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
-  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  SVXG_CUDA(host_wait(P.stream));
   return SVXG_OK;
 }
 
@@ -435,7 +435,7 @@ int set_identity_rows(Problem& P, const int32_t* rows, int32_t count) {
   (k_identity_rows<<<blocks_for(count), kT, 0, P.stream>>>(d.p, count, P.K.rowptr, P.K.val, P.d_jinv,
                                                          P.jacobi_only ? 1 : 0, P.id_scale), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
-  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  SVXG_CUDA(host_wait(P.stream));
   return SVXG_OK;
 }
 

@@ -62,8 +62,8 @@ int utilization_device(Problem& P, const double* u_nodes, double fragility, doub
     return SVXG_OK;
   }
   int32_t *flag = nullptr, *pos = nullptr;
-  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&flag), sizeof(int32_t) * size_t(P.nb), P.stream));
-  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&pos), sizeof(int32_t) * size_t(P.nb), P.stream));
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&flag), sizeof(int32_t) * size_t(P.nb), P.stream));
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&pos), sizeof(int32_t) * size_t(P.nb), P.stream));
   const unsigned g = unsigned((P.nb + kT - 1) / kT);
   (k_judge<<<g, kT, 0, P.stream>>>(P.nb, P.d_bonds, P.d_nodes, P.d_mats, u_nodes, fragility, nullptr, phi, mode, flag), SVXG_COUNT_LAUNCH());
   int32_t total = 0;

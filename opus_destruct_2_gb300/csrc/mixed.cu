@@ -24,6 +24,10 @@ namespace {
 
 constexpr int kT = 256;
 constexpr int kRows = kT / 32;
+// An inner FP32 sequence runs at most kInnerCap iterations; a restart that fails to cut the FP64
+// residual to kMinGain of the previous one hands the run to the FP64 sequence.
+constexpr int32_t kInnerCap = 60;
+constexpr double kMinGain = 0.1;
 inline unsigned vblk(int32_t n) { return unsigned((std::max(n, 1) + kT - 1) / kT); }
 inline unsigned rblk(int32_t n) { return unsigned((std::max(n, 1) + kRows - 1) / kRows); }
 
@@ -261,7 +265,7 @@ int mixed_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
   {
     // ||f|| from the begin() scalars
     SVXG_CUDA(cudaMemcpyAsync(P.h_s, P.d_s, sizeof(PcgScalars), cudaMemcpyDeviceToHost, st));
-    SVXG_CUDA(cudaStreamSynchronize(st));
+    SVXG_CUDA(host_wait(st));
     bn = P.h_s->bn;
   }
   const double target = rtol * bn;
@@ -273,15 +277,17 @@ int mixed_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
     if (res) *res = out;
     return SVXG_OK;
   }
+  double rn_prev = INFINITY;
+  bool fallback = false;
   for (int outer = 0; outer < 64; ++outer) {
     // r = f - K x in FP64
     TRY(spmv(P, P.K, P.d_x, P.d_q));
     SVXG_CUDA(cudaMemsetAsync(s, 0, sizeof(MixedScalars), st));
     (k_outer_resid<<<vblk(nf), kT, 0, st>>>(nf, P.d_f, P.d_q, P.d_r, r32, d, P.d_partials, P.d_counter, s, 1.0,
-                                            maxit - used),
+                                            std::min(maxit - used, kInnerCap)),
      SVXG_COUNT_LAUNCH());
     SVXG_CUDA(cudaMemcpyAsync(hs, s, sizeof(MixedScalars), cudaMemcpyDeviceToHost, st));
-    SVXG_CUDA(cudaStreamSynchronize(st));
+    SVXG_CUDA(host_wait(st));
     const double rn = std::sqrt(hs->rr);
     // the inner target: as deep as f32 allows, no deeper than needed
     const double tol_in = std::max(1e-4, 0.3 * target / std::max(rn, 1e-300));
@@ -298,28 +304,37 @@ int mixed_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
       break;
     }
     if (used >= maxit) break;
+    if (rn > kMinGain * rn_prev) {
+      // the FP32 inner sequence no longer gains a factor 1/kMinGain per restart (an operator too
+      // ill-conditioned for FP32 vectors): finish with the FP64 sequence from this x
+      fallback = true;
+      break;
+    }
+    rn_prev = rn;
     // inner CG from d = 0: z = M^-1 r32 (the f32 V-cycle), p = z
     P.cycle_stop = &s->done;
     TRY(vcycle32(P, r32, z32));
     (k_rz32<0><<<vblk(nf), kT, 0, st>>>(nf, r32, z32, p32, P.d_partials, P.d_counter, s), SVXG_COUNT_LAUNCH());
     SVXG_CUDA(cudaMemcpyAsync(hs, s, sizeof(MixedScalars), cudaMemcpyDeviceToHost, st));
-    SVXG_CUDA(cudaStreamSynchronize(st));
+    SVXG_CUDA(host_wait(st));
     if (hs->done) {
       // (the inner start already broke down or met its target)
-    } else if (use_graphs() && !P.timer_on) {
+    } else if (loop_graph_worth(P, P.loop_mixed)) {
       int64_t per = 0;
-      P.mx_maxit = maxit - used;
+      P.mx_maxit = std::min(maxit - used, kInnerCap);
       TRY(run_loop(P, P.loop_mixed, &s->done, mixed_body, &per));
       SVXG_CUDA(cudaMemcpyAsync(hs, s, sizeof(MixedScalars), cudaMemcpyDeviceToHost, st));
-      SVXG_CUDA(cudaStreamSynchronize(st));
+      SVXG_CUDA(host_wait(st));
       add_launches(per * std::max<int64_t>(1, hs->iters));
     } else {
+      P.host_loops += 1;
       int32_t queued = 0, batch = 2;
       for (;;) {
         SVXG_CUDA(cudaMemcpyAsync(hs, s, sizeof(MixedScalars), cudaMemcpyDeviceToHost, st));
-        SVXG_CUDA(cudaStreamSynchronize(st));
-        if (hs->done || queued >= maxit - used) break;
-        const int32_t todo = std::min(batch, maxit - used - queued);
+        SVXG_CUDA(host_wait(st));
+        const int32_t cap = std::min(maxit - used, kInnerCap);
+        if (hs->done || queued >= cap) break;
+        const int32_t todo = std::min(batch, cap - queued);
         for (int32_t it = 0; it < todo; ++it) TRY(mixed_body(P));
         queued += todo;
         batch = std::min(batch * 2, 32);
@@ -333,6 +348,16 @@ int mixed_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
     }
   }
   P.cycle_stop = nullptr;
+  if (fallback) {
+    svxg_pcg_result f64{};
+    TRY(pcg_restart_fp64(P));
+    TRY(plain_iterate(P, maxit - used, rtol, &f64));
+    f64.iters += used;
+    P.run_iters += used;
+    P.mixed_fallbacks += 1;
+    if (res) *res = f64;
+    return SVXG_OK;
+  }
   out.iters = used;
   P.run_iters += used;
   if (res) *res = out;

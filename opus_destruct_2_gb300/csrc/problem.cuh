@@ -37,8 +37,21 @@ void count_launch();
     }                                                                                     \
   } while (0)
 
-// Device allocations of a problem (counted against its bytes).
+// Stream-ordered device allocation from the library's memory pool of the current device (one
+// per device, created on first use): memory freed by a problem stays in the pool for the next
+// problem, and neither allocation nor release synchronizes the device, so problems on other
+// streams keep running while one is built or torn down.
+cudaError_t pool_malloc_async(void** p, size_t bytes, cudaStream_t s);
+
+// Waits on the host until `s` has drained. Spins (cudaStreamSynchronize) by default; while
+// blocking waits are on - a server with several slots holds them on, so that the slots' host
+// threads sleep instead of competing for cores while their streams run - it sleeps on an event.
+cudaError_t host_wait(cudaStream_t s);
+void blocking_waits(bool on);  // counted: on/off pairs nest
+
+// Device allocations of a problem (counted against its bytes), ordered on its stream.
 struct DevArena {
+  cudaStream_t stream = nullptr;
   std::vector<std::pair<void*, size_t>> live;
   int64_t bytes = 0;
   template <class T>
@@ -46,10 +59,10 @@ struct DevArena {
     *p = nullptr;
     if (count == 0) count = 1;
     void* q = nullptr;
-    cudaError_t e = cudaMalloc(&q, count * sizeof(T));
+    cudaError_t e = pool_malloc_async(&q, count * sizeof(T), stream);
     if (e != cudaSuccess) {
       cudaGetLastError();
-      set_error(std::string("cudaMalloc: ") + cudaGetErrorString(e));
+      set_error(std::string("device allocation: ") + cudaGetErrorString(e));
       return e == cudaErrorMemoryAllocation ? SVXG_ERR_NOMEM : SVXG_ERR_CUDA;
     }
     live.push_back({q, count * sizeof(T)});
@@ -62,7 +75,7 @@ struct DevArena {
     if (!p) return;
     for (size_t i = 0; i < live.size(); ++i)
       if (live[i].first == p) {
-        cudaFree(p);
+        cudaFreeAsync(p, stream);
         bytes -= int64_t(live[i].second);
         live[i] = live.back();
         live.pop_back();
@@ -80,7 +93,7 @@ struct DevArena {
     return false;
   }
   void release_all() {
-    for (auto& e : live) cudaFree(e.first);
+    for (auto& e : live) cudaFreeAsync(e.first, stream);
     live.clear();
     bytes = 0;
   }
@@ -169,11 +182,13 @@ struct Problem {
   void* d_ms = nullptr;           // mixed precision scalars (device)
   void* h_ms = nullptr;           // ... pinned mirror
   int32_t mx_maxit = 0;
+  int32_t mixed_fallbacks = 0;    // mixed runs finished by the FP64 sequence (since assemble)
   double* d_partials = nullptr;   // block partial sums
   unsigned* d_counter = nullptr;  // last-block counters
   int32_t partial_blocks = 0;
   bool active = false;
   int32_t run_iters = 0;
+  int32_t host_loops = 0;         // host-driven iterate() runs since the last assemble
   // whole-iterate graphs (graphs.cu): built on first use after each assemble
   void* loop_plain = nullptr;
   void* loop_mixed = nullptr;
@@ -181,12 +196,27 @@ struct Problem {
   bool timer_on = false;
   std::vector<cudaEvent_t> timer_events;
   size_t timer_used = 0;          // event pairs recorded since the last read
+  // host-side trace of the last assemble and solve (SVXG_TRACE=1): label, microseconds since the
+  // assemble began, with the stream drained at each mark so device time is attributed
+  std::vector<std::pair<const char*, double>> trace;
+  // row-schedule timings of the last assemble (kept only when the environment asks for them)
+  std::vector<svxg_tune_entry> tune_log;
   // scratch
   int32_t* d_scan = nullptr;      // scan block sums
   int64_t scan_cap = 0;
 };
 
+// Marks a point of the host-side trace when SVXG_TRACE=1 (drains the problem's stream first);
+// does nothing otherwise. `restart` begins a new trace.
+void trace_mark(Problem& P, const char* label, bool restart = false);
+
 // ---- launchers (one translation unit each) ---------------------------------------------------
+// capi.cu
+enum WarmStart { kCold = 0, kWarmHost = 1, kWarmResident = 2 };
+// f, u host (6 per node); kWarmResident starts from the problem's last solution, still on the device
+int solve_nodes_host(Problem& P, const double* f, double* u, double rtol, int32_t maxit, int warm,
+                     svxg_pcg_result* res);
+int ensure_node_vectors(Problem& P);
 // exact_assemble.cu
 int assemble_matrix(Problem& P);                 // dof, pattern, K, id_scale, identity rows
 int build_jacobi(Problem& P);                    // block-Jacobi inverses
@@ -195,14 +225,27 @@ int set_identity_rows(Problem& P, const int32_t* rows, int32_t count);
 // exact_amg.cu
 int build_hierarchy(Problem& P, int32_t* ok);    // Amg::build on the device
 int debug_seq_norm(cudaStream_t st, const double* v, int64_t n, double* out_dev);
+// dense.cu: C (m x m, the coarsest operator) -> chol (L, L^T mirrored above; may alias C) and
+// cinv (L^-1, then L^-T), all device, m x m row-major
+int dense_factor_inverse(Problem& P, int32_t m, const double* C, double* chol, double* cinv);
 // solve.cu
 int spmv(Problem& P, const Bsr& A, const double* x, double* y);
 int pcg_begin(Problem& P, const double* f_nodes, const double* u0_nodes);  // device, node order
 int pcg_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res);
+int plain_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res);  // the FP64 sequence
+int pcg_restart_fp64(Problem& P);                 // FP64 sequence restarted from the current x
 int gather_solution(Problem& P, double* u_nodes);                        // device, node order
 int precondition(Problem& P, const double* r, double* z);
 int free_run(Problem& P);
 int tune_k64(Problem& P);
+// tune.cu: the row schedule of a BSR operator (spmv_row.cuh), from the committed table (a pure
+// function of the operator's shape, so results never depend on timing); the timings are taken
+// and logged only when the environment asks (SVXG_TUNE_LOG=1; SVXG_TUNE_LIVE=1 also lets them
+// decide)
+enum OpKind { kOpK64 = 0, kOpA32 = 1, kOpP32 = 2, kOpR32 = 3 };
+int table_sched(int kind, int64_t rows, int64_t blocks);
+bool tune_timing();
+int tune_decide(Problem& P, int kind, int level, int64_t rows, int64_t blocks, float ms_warp, float ms_group);
 // vcycle.cu
 int vcycle(Problem& P, const double* r, double* z);
 int vcycle32(Problem& P, const float* r, float* z);
@@ -216,6 +259,17 @@ int utilization_device(Problem& P, const double* u_nodes, double fragility, doub
                        int32_t* over, int32_t* n_over);
 // graphs.cu
 bool use_graphs();
+constexpr int32_t kGraphMinFree = 4096;
+// Mixed precision runs its FP32 inner sequences for problems of at least kMixedMinFree free nodes;
+// below that a product is latency-bound, FP32 saves nothing and its restarts cost host round
+// trips, so the FP64 sequence runs (with the same FP32 V-cycle)
+constexpr int32_t kMixedMinFree = 4096;
+inline bool mixed_run(const Problem& P) {
+  if (P.jacobi_only) return false;
+  return P.opt.precision == SVXG_PRECISION_MIXED_ALL ||
+         (P.opt.precision == SVXG_PRECISION_MIXED && P.nfree >= kMixedMinFree);
+}
+bool loop_graph_worth(const Problem& P, const void* slot);
 int timer_mark(Problem& P, bool closing = false);
 int run_loop(Problem& P, void*& slot, const int32_t* done, int (*body)(Problem&), int64_t* body_launches);
 void destroy_loop(void*& slot);

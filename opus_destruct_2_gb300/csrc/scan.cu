@@ -99,7 +99,7 @@ int exclusive_scan_i32(Problem& P, const int32_t* in, int32_t* out, int64_t n, i
   SVXG_CUDA(cudaGetLastError());
   if (total_host) {
     SVXG_CUDA(cudaMemcpyAsync(total_host, P.d_scan + ntiles, sizeof(int32_t), cudaMemcpyDeviceToHost, P.stream));
-    SVXG_CUDA(cudaStreamSynchronize(P.stream));
+    SVXG_CUDA(host_wait(P.stream));
   }
   return SVXG_OK;
 }

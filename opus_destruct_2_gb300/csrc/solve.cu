@@ -416,14 +416,15 @@ int spmv(Problem& P, const Bsr& A, const double* x, double* y) {
   return SVXG_OK;
 }
 
-// K's FP64 SpMV schedule: the faster of the two on y = K x (a warm-up launch each, then three)
+// K's FP64 SpMV schedule from the table; with tune timing on, y = K x is also timed with both
+// (a warm-up launch each, then three) and logged
 int tune_k64(Problem& P) {
-  P.sched_k64 = kWarpRow;
-  if (P.nfree <= 0) return SVXG_OK;
+  P.sched_k64 = table_sched(kOpK64, P.nfree, P.K.nnzb);
+  if (P.nfree <= 0 || !tune_timing()) return SVXG_OK;
   const size_t m = 6 * size_t(P.nfree);
   double *x = nullptr, *y = nullptr;
-  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&x), m * sizeof(double), P.stream));
-  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&y), m * sizeof(double), P.stream));
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&x), m * sizeof(double), P.stream));
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&y), m * sizeof(double), P.stream));
   SVXG_CUDA(cudaMemsetAsync(x, 0, m * sizeof(double), P.stream));
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
@@ -442,7 +443,7 @@ int tune_k64(Problem& P) {
   cudaEventDestroy(e1);
   cudaFreeAsync(x, P.stream);
   cudaFreeAsync(y, P.stream);
-  P.sched_k64 = ms[1] < ms[0] ? kGroupRow : kWarpRow;
+  P.sched_k64 = tune_decide(P, kOpK64, 0, P.nfree, P.K.nnzb, ms[0], ms[1]);
   SVXG_CUDA(cudaGetLastError());
   return SVXG_OK;
 }
@@ -496,7 +497,7 @@ int pcg_begin(Problem& P, const double* f_nodes, const double* u0_nodes) {
     if (P.jacobi_only) {
       (k_jacobi_rz<0><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_jinv, P.d_r, P.d_z, P.d_p, P.d_partials,
                                                        P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
-    } else if (P.opt.precision == SVXG_PRECISION_MIXED) {
+    } else if (mixed_run(P)) {
       // (the mixed run starts each inner sequence from the FP64 residual)
     } else {
       TRY(vcycle(P, P.d_r, P.d_z));
@@ -539,6 +540,33 @@ bool use_graphs() {
   return on;
 }
 
+// Whether this iterate() runs as the loop graph in `slot`: once built, always; otherwise only
+// for a problem large enough (kGraphMinFree free nodes) or iterated once already since its
+// assemble. A graph is captured and instantiated per assembled problem, and instantiation is a
+// host-side cost that also serializes concurrent problems, so a small problem solved once is
+// better served by host-driven batches of launches (the live timer also needs those).
+bool loop_graph_worth(const Problem& P, const void* slot) {
+  if (!use_graphs() || P.timer_on) return false;
+  return slot != nullptr || P.nfree >= kGraphMinFree || P.host_loops > 0;
+}
+
+// Restarts the FP64 sequence from the current x (the mixed run's fallback): r = f - K x,
+// z = M^-1 r, p = z, as begin() does after its scatter.
+int pcg_restart_fp64(Problem& P) {
+  const int32_t nf = P.nfree;
+  cudaStream_t st = P.stream;
+  SVXG_CUDA(cudaMemsetAsync(P.d_s, 0, sizeof(PcgScalars), st));
+  if (nf > 0) {
+    TRY(spmv(P, P.K, P.d_x, P.d_q));
+    (k_begin_r<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_f, P.d_q, P.d_r, P.d_partials, P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
+    (k_begin_zero<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_x, P.d_r, P.d_s), SVXG_COUNT_LAUNCH());
+    TRY(vcycle(P, P.d_r, P.d_z));
+    (k_rz<0><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_r, P.d_z, P.d_p, P.d_partials, P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
+  }
+  SVXG_CUDA(cudaGetLastError());
+  return SVXG_OK;
+}
+
 // StressProblem::iterate (stress.cpp:403-464)
 int pcg_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) {
   svxg_pcg_result out{};
@@ -546,29 +574,36 @@ int pcg_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) {
     if (res) *res = out;
     return SVXG_OK;
   }
+  if (mixed_run(P)) return mixed_iterate(P, maxit, rtol, res);
+  return plain_iterate(P, maxit, rtol, res);
+}
+
+// the FP64 sequence from its current state, up to maxit iterations
+int plain_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) {
+  svxg_pcg_result out{};
   const int32_t nf = P.nfree;
   cudaStream_t st = P.stream;
-  if (P.opt.precision == SVXG_PRECISION_MIXED && !P.jacobi_only) return mixed_iterate(P, maxit, rtol, res);
   P.cycle_stop = &P.d_s->done;
   (k_iter_start<<<vec_blocks(std::max(nf, 1)), kVecT, 0, st>>>(nf, P.d_r, rtol, maxit, P.d_partials, P.d_counter,
                                                              P.d_s), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   SVXG_CUDA(cudaMemcpyAsync(P.h_s, P.d_s, sizeof(PcgScalars), cudaMemcpyDeviceToHost, st));
-  SVXG_CUDA(cudaStreamSynchronize(st));
+  SVXG_CUDA(host_wait(st));
   if (P.h_s->done || nf == 0) {
     // (converged, empty or not finite at the start: no iteration)
-  } else if (use_graphs() && !P.timer_on) {  // (the live timer brackets each launch: host-driven then)
+  } else if (loop_graph_worth(P, P.loop_plain)) {
     int64_t per = 0;
     TRY(run_loop(P, P.loop_plain, &P.d_s->done, plain_body, &per));
     SVXG_CUDA(cudaMemcpyAsync(P.h_s, P.d_s, sizeof(PcgScalars), cudaMemcpyDeviceToHost, st));
-    SVXG_CUDA(cudaStreamSynchronize(st));
+    SVXG_CUDA(host_wait(st));
     add_launches(per * std::max<int64_t>(1, P.h_s->iters));
   } else {
+    P.host_loops += 1;
     int32_t queued = 0;
     int32_t batch = 2;
     for (;;) {
       SVXG_CUDA(cudaMemcpyAsync(P.h_s, P.d_s, sizeof(PcgScalars), cudaMemcpyDeviceToHost, st));
-      SVXG_CUDA(cudaStreamSynchronize(st));
+      SVXG_CUDA(host_wait(st));
       if (P.h_s->done || queued >= maxit) break;
       const int32_t todo = std::min(batch, maxit - queued);
       for (int32_t it = 0; it < todo; ++it) TRY(plain_body(P));

@@ -1,0 +1,72 @@
+// tune.cu - the row schedule of every BSR operator, chosen from the committed table.
+//
+// Both schedules of spmv_row.cuh compute every row with the same additions in the same order, but
+// the reductions fused into the conjugate-gradient products group rows by thread block, and the
+// two schedules put different rows in a block. The choice is therefore a fixed function of the
+// operator's shape (mean blocks per row against the bound of sched_table.h), never of a timing,
+// so a problem gives the same bits alone, among other problems, and from one run to the next.
+// The table is fitted offline by opus_destruct_2_gb300/autotune.py from the timings this file
+// records when asked.
+#include <chrono>
+#include <cstdlib>
+
+#include "problem.cuh"
+#include "sched_table.h"
+#include "spmv_row.cuh"
+
+namespace svxg {
+
+namespace {
+int env_level() {
+  const char* live = std::getenv("SVXG_TUNE_LIVE");
+  if (live && live[0] && live[0] != '0') return 2;
+  const char* log = std::getenv("SVXG_TUNE_LOG");
+  return log && log[0] && log[0] != '0' ? 1 : 0;
+}
+const int g_level = env_level();
+}  // namespace
+
+int table_sched(int kind, int64_t rows, int64_t blocks) {
+  if (rows <= 0 || kind < 0 || kind > 3) return kWarpRow;
+  return double(blocks) / double(rows) <= kGroupRowMaxMean[kind] ? kGroupRow : kWarpRow;
+}
+
+bool tune_timing() { return g_level > 0; }
+
+namespace {
+const bool g_trace = [] {
+  const char* v = std::getenv("SVXG_TRACE");
+  return v && v[0] && v[0] != '0';
+}();
+double now_us() {
+  return std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+}  // namespace
+
+void trace_mark(Problem& P, const char* label, bool restart) {
+  if (!g_trace) return;
+  cudaStreamSynchronize(P.stream);
+  const double t = now_us();
+  if (restart || P.trace.empty()) {
+    P.trace.clear();
+    P.trace.emplace_back("start", t);
+    if (restart) return;
+  }
+  P.trace.emplace_back(label, t);
+}
+
+int tune_decide(Problem& P, int kind, int level, int64_t rows, int64_t blocks, float ms_warp, float ms_group) {
+  svxg_tune_entry e{};
+  e.kind = kind;
+  e.level = level;
+  e.rows = rows;
+  e.blocks = blocks;
+  e.ms_warp_row = ms_warp;
+  e.ms_group_row = ms_group;
+  P.tune_log.push_back(e);
+  if (g_level == 2) return ms_group < ms_warp ? kGroupRow : kWarpRow;
+  return table_sched(kind, rows, blocks);
+}
+
+}  // namespace svxg
+

@@ -194,26 +194,6 @@ __global__ void k_dense_mv(int32_t m, const double* __restrict__ M, const float*
   }
 }
 
-// L^-1 column by column (forward substitution on the identity), and its transpose
-__global__ void k_tri_inverse(int32_t m, const double* __restrict__ L, double* X, double* XT) {
-  const int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= m) return;
-  for (int32_t i = 0; i < j; ++i) {
-    X[int64_t(i) * m + j] = 0.0;
-    XT[int64_t(j) * m + i] = 0.0;
-  }
-  const double xjj = 1.0 / L[int64_t(j) * m + j];
-  X[int64_t(j) * m + j] = xjj;
-  XT[int64_t(j) * m + j] = xjj;
-  for (int32_t i = j + 1; i < m; ++i) {
-    double s = 0.0;
-    for (int32_t k = j; k < i; ++k) s += L[int64_t(i) * m + k] * X[int64_t(k) * m + j];
-    const double xij = -s / L[int64_t(i) * m + i];
-    X[int64_t(i) * m + j] = xij;
-    XT[int64_t(j) * m + i] = xij;
-  }
-}
-
 // power iteration for the smoother's bound where the setup left none (f64, 12 steps)
 __global__ void k_pow_step(int32_t n, const double* dinv, const double* w, double* v) {
   const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -263,9 +243,9 @@ __global__ void k_fill_ones(int64_t m, double* v) {
 int power_bound(Problem& P, const Level& L, double* out) {
   const int64_t m = 6 * int64_t(L.A.n);
   double *v = nullptr, *w = nullptr, *nv = nullptr;
-  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&v), m * sizeof(double), P.stream));
-  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&w), m * sizeof(double), P.stream));
-  SVXG_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&nv), sizeof(double), P.stream));
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&v), m * sizeof(double), P.stream));
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&w), m * sizeof(double), P.stream));
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&nv), sizeof(double), P.stream));
   (k_fill_ones<<<nblk(m), kT, 0, P.stream>>>(m, v), SVXG_COUNT_LAUNCH());
   for (int it = 0; it < 12; ++it) {
     (k_spmv64<<<nblk(m), kT, 0, P.stream>>>(L.A.n, L.A.rowptr, L.A.col, L.A.val, v, w), SVXG_COUNT_LAUNCH());
@@ -277,7 +257,7 @@ int power_bound(Problem& P, const Level& L, double* out) {
   cudaFreeAsync(v, P.stream);
   cudaFreeAsync(w, P.stream);
   cudaFreeAsync(nv, P.stream);
-  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  SVXG_CUDA(host_wait(P.stream));
   *out = 1.1 * h;
   return SVXG_OK;
 }
@@ -383,10 +363,11 @@ int cycle(Problem& P, size_t l, const float* b, float* x) {
   return SVXG_OK;
 }
 
-// times y = A x with both schedules (a launch each to warm, then three) and returns the faster
-int tune_bsr32(cudaStream_t st, int32_t n, const int32_t* rowptr, const int32_t* col, const float* val, const float* x,
-               float* y) {
-  if (n <= 0) return kWarpRow;
+// the table's schedule for y = A x (n block rows, `blocks` blocks); with tune timing on, both
+// schedules are also timed (a launch each to warm, then three) and logged
+int tune_bsr32(Problem& P, int kind, int level, int64_t blocks, cudaStream_t st, int32_t n, const int32_t* rowptr,
+               const int32_t* col, const float* val, const float* x, float* y) {
+  if (n <= 0 || !tune_timing()) return table_sched(kind, n, blocks);
   StepArgs none{};
   cudaEvent_t e[3];
   for (auto& ev : e) cudaEventCreate(&ev);
@@ -400,7 +381,7 @@ int tune_bsr32(cudaStream_t st, int32_t n, const int32_t* rowptr, const int32_t*
     cudaEventElapsedTime(&ms[sch], e[0], e[1]);
   }
   for (auto& ev : e) cudaEventDestroy(ev);
-  return ms[1] < ms[0] ? kGroupRow : kWarpRow;
+  return tune_decide(P, kind, level, n, blocks, ms[0], ms[1]);
 }
 
 }  // namespace
@@ -424,9 +405,9 @@ int prepare_cycle(Problem& P) {
       (k_cvt_transpose<<<nblk(L.pnnz), kT, 0, st>>>(L.pnnz, L.rent_e, L.pval, L.pval32 + 36 * L.pnnz), SVXG_COUNT_LAUNCH());
     }
     for (float** v : {&L.b32, &L.x32, &L.r32, &L.t32, &L.u32}) TRY(P.mem.alloc(v, 6 * size_t(std::max(n, 1))));
-    // the schedule of each of the level's operators: the faster of the two, timed here
+    // the schedule of each of the level's operators
     SVXG_CUDA(cudaMemsetAsync(L.t32, 0, sizeof(float) * 6 * size_t(std::max(n, 1)), st));
-    L.sched_a = tune_bsr32(st, n, L.A.rowptr, L.A.col, L.A.val32, L.t32, L.u32);
+    L.sched_a = tune_bsr32(P, kOpA32, int(l), L.A.nnzb, st, n, L.A.rowptr, L.A.col, L.A.val32, L.t32, L.u32);
     const bool last = l + 1 == P.lv.size();
     if (!last || P.chol_n == 0) {
       if (L.lmax > 0) L.cheb_lmax = L.lmax;
@@ -436,14 +417,9 @@ int prepare_cycle(Problem& P) {
   for (size_t l = 0; l + 1 < P.lv.size(); ++l) {
     Level& L = P.lv[l];
     const Level& C = P.lv[l + 1];
-    L.sched_p = tune_bsr32(st, L.A.n, L.prow, L.pcol, L.pval32, C.t32, L.u32);
-    L.sched_r = tune_bsr32(st, C.A.n, L.rrow, L.rent_i, L.pval32 + 36 * L.pnnz, L.t32, C.u32);
-  }
-  if (P.chol_n > 0) {
-    const int32_t m = P.chol_n;
-    TRY(P.mem.alloc(&P.d_cinv, 2 * size_t(m) * size_t(m)));
-    TRY(P.mem.alloc(&P.d_cvec, 2 * size_t(m)));
-    (k_tri_inverse<<<nblk(m, 64), 64, 0, st>>>(m, P.d_chol, P.d_cinv, P.d_cinv + int64_t(m) * m), SVXG_COUNT_LAUNCH());
+    L.sched_p = tune_bsr32(P, kOpP32, int(l), L.pnnz, st, L.A.n, L.prow, L.pcol, L.pval32, C.t32, L.u32);
+    L.sched_r = tune_bsr32(P, kOpR32, int(l), L.pnnz, st, C.A.n, L.rrow, L.rent_i, L.pval32 + 36 * L.pnnz, L.t32,
+                           C.u32);
   }
   SVXG_CUDA(cudaGetLastError());
   return SVXG_OK;

@@ -122,6 +122,11 @@ class AmgOptions(ctypes.Structure):
                 ("reaggregate", ctypes.c_int32)]
 
 
+# StressOptions.precision (svxg_types.h): FP64; mixed for problems of 4096 free nodes or more
+# (smaller ones run the FP64 sequence); mixed at every size
+PRECISION_FP64, PRECISION_MIXED, PRECISION_MIXED_ALL = 0, 1, 2
+
+
 class StressOptions(ctypes.Structure):
     """svx::StressOptions (stress.hpp:68-72) plus the arithmetic of the solve."""
     _fields_ = [("rtol", ctypes.c_double), ("amg", AmgOptions), ("amg_min_nodes", ctypes.c_int32),

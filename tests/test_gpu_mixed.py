@@ -12,7 +12,7 @@ from oracle import Port
 
 pytestmark = pytest.mark.gpu
 MATS = default_materials()
-MIXED = 1
+MIXED = 2  # (mixed at every size: these graphs are below the size where mixed is the default)
 
 CASES = {
     "lattice16": (lambda: fx.lattice(16), dict()),
@@ -96,3 +96,15 @@ def test_mixed_cap_and_resume_and_edge_loads():
     f[5] = np.nan
     _, rn = G.solve(f, rtol=1e-9, maxit=100)
     assert rn.breakdown and not rn.converged and np.isinf(rn.rel_res)
+
+
+def test_mixed_below_its_size_runs_the_fp64_sequence():
+    nodes, bonds = fx.lattice(8)
+    f = fx.gravity_live(nodes)
+    out = {}
+    for prec in (0, 1):
+        G = StressProblem(nodes, bonds, MATS)
+        assert G.assemble(StressOptions(precision=prec, amg_min_nodes=16))
+        out[prec] = G.solve(f, rtol=1e-8, maxit=500)
+    assert out[0][1].iters == out[1][1].iters
+    assert np.array_equal(out[0][0], out[1][0])
