@@ -18,6 +18,8 @@ fragments; gravity loads; FP64 PCG to rtol 1e-8.
 
 Launch: python bench.py [--gpus N --steps K --warmup W] (N > 1 under torchrun: one replica per
 GPU, each solving its own seeded city block; value = all ranks' solves / the slowest rank's time).
+--workload batch | serve runs the batched solve or the serving loop instead (one JSON line with
+solves/s, latency percentiles and the plain FP64 per-request rate on the same requests).
 --impl reference times the reference's CPU implementation of the path (the oracle port on every
 host thread) on the same workload and prints the same JSON line.
 """
@@ -168,13 +170,53 @@ def cpu_baseline(args, nodes, bonds, f, mats) -> dict:
                       f"{res.iters} PCG iterations"}
 
 
+def run_many(args, rank: int, world: int):
+    """The batched solve or the serving loop (opus_destruct_2_gb300/workloads.py) on this GPU."""
+    # (more hardware queues for the server's streams; read when the CUDA context is created)
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+    from opus_destruct_2_gb300 import workloads
+    from opus_destruct_2_gb300.graph import PRECISION_FP64, PRECISION_MIXED
+    prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    if args.workload == "batch":
+        r = workloads.batch(count=args.graphs, workers=args.workers, precision=prec, rtol=1e-6)
+        desc = (f"batch: {args.graphs} fragment graphs, log-normal sizes (median 300, 10-20,000), half free pieces "
+                f"with inertial relief, half ground-supported, gravity + one impact load; rtol 1e-6")
+    else:
+        r = workloads.serve(requests=args.requests, rate=args.rate, workers=args.workers, precision=prec, rtol=1e-6)
+        desc = (f"serve: Poisson stream of {args.requests} requests at {args.rate:g}/s, sizes log-normal (median 500, "
+                f"max 50,000), 30% repeats of recent structures with 1-5% of bonds removed (warm start), 40 GB "
+                f"admission budget; rtol 1e-6")
+    clk = clocks.stop()
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": r["solves_per_s"] * world, "unit": "solves/s", "n_gpus": world, "steps": 1,
+        "warmup": 16, "ms_per_step": 1e3 * r["wall_s"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if prec == PRECISION_FP64 else "f32+f64", "data": "synthetic",
+        "config": {"workload": desc, "workers": args.workers,
+                   "precision": ("fp64" if prec == PRECISION_FP64 else
+                                 "mixed (fp32 inner sequences from 65536 free nodes; fp64 sequence below)")},
+        "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"], args.workload: r,
+        "vs_plain_fp64_per_request": r["solves_per_s"] / r["plain_fp64_per_request_solves_per_s"],
+        "roofline": None,
+    }
+    if clk is not None:
+        line["clocks"] = clk
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["city", "tower"], default="city")
+    ap.add_argument("--workload", choices=["city", "tower", "batch", "serve"], default="city")
+    ap.add_argument("--requests", type=int, default=20000, help="serve: requests in the stream")
+    ap.add_argument("--rate", type=float, default=5000.0, help="serve: Poisson arrival rate (requests/s)")
+    ap.add_argument("--graphs", type=int, default=512, help="batch: graphs")
+    ap.add_argument("--workers", type=int, default=16, help="batch / serve: server slots")
     ap.add_argument("--lots", type=int, default=8)
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--rtol", type=float, default=1e-8)
@@ -190,6 +232,9 @@ def main():
 
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload in ("batch", "serve"):
+        run_many(args, rank, world)
         return
 
     import torch

@@ -85,7 +85,7 @@ typedef struct svxg_amg_options {
 enum {
   SVXG_PRECISION_FP64 = 0,      /* FP64 K, FP64 PCG; FP32 V-cycle (as the reference) */
   SVXG_PRECISION_MIXED = 1,     /* FP32 K and V-cycle inside FP64 iterative refinement, for
-                                   problems of 4096 free nodes or more (smaller ones are
+                                   problems of 65536 free nodes or more (smaller ones are
                                    latency-bound: they run the FP64 sequence) */
   SVXG_PRECISION_MIXED_ALL = 2  /* the same at every size */
 };

@@ -2,9 +2,9 @@
 
 Every BSR product (K in FP64; each level's A, prolongation and restriction in FP32) runs with one
 of two row schedules (csrc/spmv_row.cuh): a warp per block row, or five block rows per warp.
-Both give the same bits row by row, but the conjugate-gradient products fuse a reduction whose
-grouping follows the schedule, so the library takes the schedule from a committed table - a
-function of the operator's mean blocks per row - and never from a timing at run time. This
+The two add a row's blocks in different orders and group the fused reductions of the
+conjugate-gradient products differently, so the library takes the schedule from a committed
+table - a function of the operator's mean blocks per row - and never from a timing at run time. This
 script makes that table: it assembles the workloads below with the library's timing log on
 (SVXG_TUNE_LOG=1, set before the library loads), collects both schedules' times for every
 operator, and for each kind of operator picks the bound on mean blocks per row (five rows per

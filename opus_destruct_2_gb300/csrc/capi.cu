@@ -284,9 +284,11 @@ void svxg_problem_destroy(svxg_problem* p) {
   p->P.mem.release_all();
   host_wait(p->P.stream);
   for (cudaEvent_t e : p->P.timer_events) cudaEventDestroy(e);
-  if (p->P.h_s) cudaFreeHost(p->P.h_s);
-  if (p->P.h_ms) cudaFreeHost(p->P.h_ms);
-  cudaStreamDestroy(p->P.stream);
+  if (!p->P.borrowed) {
+    if (p->P.h_s) cudaFreeHost(p->P.h_s);
+    if (p->P.h_ms) cudaFreeHost(p->P.h_ms);
+    cudaStreamDestroy(p->P.stream);
+  }
   delete p;
 }
 

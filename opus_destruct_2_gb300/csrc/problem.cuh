@@ -143,6 +143,9 @@ struct Level {
 struct Problem {
   int device = 0;
   cudaStream_t stream = nullptr;
+  // stream and pinned mirrors (h_s, h_ms) lent by a server slot for the duration of a request,
+  // not owned: destroy leaves them alone
+  bool borrowed = false;
   DevArena mem;
   // graph (host copy kept for the in-place updates' bookkeeping)
   int32_t n = 0, nb = 0;
@@ -261,9 +264,10 @@ int utilization_device(Problem& P, const double* u_nodes, double fragility, doub
 bool use_graphs();
 constexpr int32_t kGraphMinFree = 4096;
 // Mixed precision runs its FP32 inner sequences for problems of at least kMixedMinFree free nodes;
-// below that a product is latency-bound, FP32 saves nothing and its restarts cost host round
-// trips, so the FP64 sequence runs (with the same FP32 V-cycle)
-constexpr int32_t kMixedMinFree = 4096;
+// below that the products are latency-bound, FP32 saves nothing, and the FP32 Krylov vectors'
+// extra iterations and the restarts' host round trips cost more than they save, so the FP64
+// sequence runs (with the same FP32 V-cycle)
+constexpr int32_t kMixedMinFree = 65536;
 inline bool mixed_run(const Problem& P) {
   if (P.jacobi_only) return false;
   return P.opt.precision == SVXG_PRECISION_MIXED_ALL ||

@@ -14,6 +14,7 @@
 #include <deque>
 #include <list>
 #include <mutex>
+#include <new>
 #include <thread>
 #include <unordered_map>
 #include <unordered_set>
@@ -65,6 +66,56 @@ int64_t estimate_bytes(int64_t n, int64_t nb) {
   return blocks * 36 * 12 * 2 + n * 6 * 8 * 24 + n * 40 + nb * 216 + (int64_t(1) << 20);
 }
 
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int d) {
+    cudaGetDevice(&prev);
+    cudaSetDevice(d);
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+// A slot's CUDA stream and pinned scalar mirrors, lent to whichever problem the slot runs (so a
+// resident structure holds device memory only, not a stream or pinned host memory of its own).
+struct Slot {
+  cudaStream_t stream = nullptr;
+  void* h_s = nullptr;
+  void* h_ms = nullptr;
+  int init() {
+    SVXG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    SVXG_CUDA(cudaMallocHost(&h_s, 256));
+    SVXG_CUDA(cudaMallocHost(&h_ms, 256));
+    return SVXG_OK;
+  }
+  ~Slot() {
+    if (stream) cudaStreamSynchronize(stream);
+    if (h_s) cudaFreeHost(h_s);
+    if (h_ms) cudaFreeHost(h_ms);
+    if (stream) cudaStreamDestroy(stream);
+  }
+  void lend(svxg_problem* p) const {
+    Problem& P = p->P;
+    P.stream = stream;
+    P.mem.stream = stream;
+    P.h_s = static_cast<PcgScalars*>(h_s);
+    P.h_ms = h_ms;
+  }
+};
+
+// a problem without a stream or pinned mirrors of its own (a slot lends them)
+int create_bare(svxg_problem** out, int device) {
+  *out = nullptr;
+  svxg_problem* p = new (std::nothrow) svxg_problem;
+  if (!p) return SVXG_ERR_NOMEM;
+  p->P.device = device;
+  p->P.borrowed = true;
+  p->P.opt = svxg_default_options();
+  *out = p;
+  return SVXG_OK;
+}
+
 }  // namespace
 }  // namespace svxg
 
@@ -93,17 +144,19 @@ struct svxg_server {
   Clock::time_point t_first{}, t_last{};
   bool any = false;
   bool blocking = false;
+  Slot admin;  // (lent to problems released outside a slot: forget, destroy)
 };
 
 namespace {
 
-void evict_locked(svxg_server* S, int64_t need) {
+void evict_locked(svxg_server* S, int64_t need, const Slot& slot) {
   for (auto it = S->lru.begin(); it != S->lru.end() && S->resident_bytes + S->running_bytes + need > S->budget;) {
     auto r = S->resident.find(*it);
     if (r == S->resident.end() || S->running_structures.count(*it)) {
       ++it;
       continue;
     }
+    slot.lend(r->second.p);
     svxg_release(r->second.p);
     S->spare.push_back(r->second.p);
     S->resident_bytes -= r->second.bytes;
@@ -185,7 +238,8 @@ int run_repeat(svxg_problem* p, Request& q, svxg_request_result* res) {
 // A request for structure s waits while another request for s runs: it parks in deferred[s]
 // and goes back to the head of the queue when that request finishes. (A repeat submitted after
 // its structure's first request therefore always finds it resident, unless it was evicted.)
-void release_to_spare_locked(svxg_server* S, std::unordered_map<int64_t, Resident>::iterator it) {
+void release_to_spare_locked(svxg_server* S, std::unordered_map<int64_t, Resident>::iterator it, const Slot& slot) {
+  slot.lend(it->second.p);
   svxg_release(it->second.p);
   S->spare.push_back(it->second.p);
   S->resident_bytes -= it->second.bytes;
@@ -195,6 +249,8 @@ void release_to_spare_locked(svxg_server* S, std::unordered_map<int64_t, Residen
 
 void worker(svxg_server* S) {
   cudaSetDevice(S->device);
+  Slot slot;
+  const int slot_ok = slot.init();
   svxg_problem* own = nullptr;
   for (;;) {
     Request q;
@@ -233,11 +289,11 @@ void worker(svxg_server* S) {
           set_error("request exceeds the server's HBM budget");
           e = SVXG_ERR_NOMEM;
         } else {
-          evict_locked(S, est);
+          evict_locked(S, est, slot);
           if (S->resident_bytes + S->running_bytes + est > S->budget) {
             ++S->admission_waits;
             S->cv_mem.wait(lk, [&] {
-              evict_locked(S, est);
+              evict_locked(S, est, slot);
               return S->resident_bytes + S->running_bytes + est <= S->budget;
             });
           }
@@ -247,7 +303,7 @@ void worker(svxg_server* S) {
           keep = q.structure >= 0;
           if (keep) {
             auto old = S->resident.find(q.structure);  // (resubmitted: the new graph replaces it)
-            if (old != S->resident.end()) release_to_spare_locked(S, old);
+            if (old != S->resident.end()) release_to_spare_locked(S, old, slot);
             if (!S->spare.empty()) {
               p = S->spare.back();
               S->spare.pop_back();
@@ -258,13 +314,17 @@ void worker(svxg_server* S) {
     }
     svxg_request_result res{};
     res.queue_ms = std::chrono::duration<double, std::milli>(Clock::now() - q.submitted).count();
+    if (!e && slot_ok) e = slot_ok;
     if (!e && !p && !keep) {
-      if (!own) e = svxg_problem_create(&own, S->device);
+      if (!own) e = create_bare(&own, S->device);
       p = own;
     } else if (!e && !p) {
-      e = svxg_problem_create(&p, S->device);
+      e = create_bare(&p, S->device);
     }
-    if (!e) e = q.repeat ? run_repeat(p, q, &res) : run_new(p, q, &res);
+    if (!e) {
+      slot.lend(p);
+      e = q.repeat ? run_repeat(p, q, &res) : run_new(p, q, &res);
+    }
     res.status = e;
     {
       std::lock_guard<std::mutex> lk(S->mu);
@@ -275,7 +335,7 @@ void worker(svxg_server* S) {
           const int64_t b = it->second.p->P.mem.bytes;
           S->resident_bytes += b - it->second.bytes;
           it->second.bytes = b;
-          if (it->second.forget || e) release_to_spare_locked(S, it);  // (a failed repeat: dropped)
+          if (it->second.forget || e) release_to_spare_locked(S, it, slot);  // (a failed repeat: dropped)
         }
       } else if (keep && p) {
         if (!e) {
@@ -344,6 +404,14 @@ int svxg_server_create(svxg_server** out, int device, int64_t hbm_budget_bytes, 
   svxg_server* S = new svxg_server;
   S->device = device;
   S->budget = hbm_budget_bytes;
+  {
+    DeviceGuard g(device);
+    const int e = S->admin.init();
+    if (e) {
+      delete S;
+      return e;
+    }
+  }
   S->blocking = workers > 1;
   if (S->blocking) blocking_waits(true);
   for (int32_t i = 0; i < workers; ++i) S->threads.emplace_back(worker, S);
@@ -359,8 +427,14 @@ void svxg_server_destroy(svxg_server* S) {
   }
   S->cv_work.notify_all();
   for (auto& t : S->threads) t.join();
-  for (auto& kv : S->resident) svxg_problem_destroy(kv.second.p);
-  for (svxg_problem* p : S->spare) svxg_problem_destroy(p);
+  for (auto& kv : S->resident) {
+    S->admin.lend(kv.second.p);
+    svxg_problem_destroy(kv.second.p);
+  }
+  for (svxg_problem* p : S->spare) {
+    S->admin.lend(p);
+    svxg_problem_destroy(p);
+  }
   if (S->blocking) blocking_waits(false);
   delete S;
 }
@@ -476,11 +550,7 @@ int svxg_server_forget(svxg_server* S, int64_t structure) {
     it->second.forget = true;
     return SVXG_OK;
   }
-  svxg_release(it->second.p);
-  S->spare.push_back(it->second.p);
-  S->resident_bytes -= it->second.bytes;
-  S->lru.erase(it->second.lru);
-  S->resident.erase(it);
+  release_to_spare_locked(S, it, S->admin);
   S->cv_mem.notify_all();
   return SVXG_OK;
 }

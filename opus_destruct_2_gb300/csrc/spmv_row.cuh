@@ -23,14 +23,7 @@ struct Vec2<double> {
   using T = double2;
 };
 
-__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
-__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
-__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
-
-// m: row c of a block (6 values), x: the column's 6 values; V and X are float or double. One
-// product and five fused multiply-adds in a fixed order (no contraction left to the compiler),
-// so every schedule and every inlining of it computes the same bits.
+// m: row c of a block (6 values), x: the column's 6 values; V and X are float or double
 template <typename V, typename X, typename A>
 __device__ __forceinline__ A dot6(const V* __restrict__ m, const X* __restrict__ x) {
   using MV = typename Vec2<V>::T;
@@ -39,12 +32,7 @@ __device__ __forceinline__ A dot6(const V* __restrict__ m, const X* __restrict__
            d = __ldg(reinterpret_cast<const MV*>(m) + 2);
   const XV u = __ldg(reinterpret_cast<const XV*>(x)), v = __ldg(reinterpret_cast<const XV*>(x) + 1),
            w = __ldg(reinterpret_cast<const XV*>(x) + 2);
-  A r = mul_rn(A(a.x), A(u.x));
-  r = fma_rn(A(a.y), A(u.y), r);
-  r = fma_rn(A(b.x), A(v.x), r);
-  r = fma_rn(A(b.y), A(v.y), r);
-  r = fma_rn(A(d.x), A(w.x), r);
-  return fma_rn(A(d.y), A(w.y), r);
+  return A(a.x) * A(u.x) + A(a.y) * A(u.y) + A(b.x) * A(v.x) + A(b.y) * A(v.y) + A(d.x) * A(w.x) + A(d.y) * A(w.y);
 }
 
 // (A x)_row,c in lanes c < 6 (other lanes: garbage); whole warp must call
@@ -82,7 +70,9 @@ __device__ __forceinline__ A warp_row_product(int32_t k0, int32_t k1, const int3
   return acc + a1 + a2 + a3 + a4;
 }
 
-// Schedules of the row product (the autotuner picks one per operator, see tune.cu):
+// Schedules of the row product (chosen per operator by the table of sched_table.h, tune.cu; the
+// two sum a row's blocks in different orders, so the choice is a fixed function of the operator's
+// shape and never of a timing):
 //   kWarpRow  one warp per block row, the five lane groups over the row's blocks (long rows)
 //   kGroupRow five block rows per warp, one lane group per row, each lane over its row's blocks
 //             (short rows: five rows in flight per warp)
@@ -117,31 +107,21 @@ __device__ __forceinline__ A sched_row_product(bool row_ok, int32_t row, const i
     const int32_t k0 = row_ok ? rowptr[row] : 0, k1 = row_ok ? rowptr[row + 1] : 0;
     return warp_row_product<V, X, A>(k0, k1, col, val, x);
   }
-  // The same additions in the same order as kWarpRow, so both schedules give the same bits:
-  // accumulator q sums the row's blocks j = q (mod 5) as pairs (j, j + 5), j = q, q + 10, ...;
-  // the row is then (((s0 + s1) + s2) + s3) + s4.
   const int lane = threadIdx.x & 31;
   const int g = lane / 6, c = lane - 6 * g;
-  A s[5] = {A(0), A(0), A(0), A(0), A(0)};
+  A acc = A(0);
   if (row_ok && g < 5) {
-    const int32_t k0 = rowptr[row], k1 = rowptr[row + 1];
-    for (int32_t t = k0; t < k1; t += 10) {
-#pragma unroll
-      for (int q = 0; q < 5; ++q) {
-        const int32_t ka = t + q, kb = t + q + 5;
-        if (ka < k1) {
-          const A pa = dot6<V, X, A>(val + 36 * int64_t(ka) + 6 * c, x + 6 * int64_t(__ldg(col + ka)));
-          if (kb < k1) {
-            const A pb = dot6<V, X, A>(val + 36 * int64_t(kb) + 6 * c, x + 6 * int64_t(__ldg(col + kb)));
-            s[q] += pa + pb;
-          } else {
-            s[q] += pa;
-          }
-        }
-      }
+    const int32_t k1 = rowptr[row + 1];
+    int32_t k = rowptr[row];
+    for (; k + 1 < k1; k += 2) {
+      const int32_t ca = __ldg(col + k), cb = __ldg(col + k + 1);
+      const A pa = dot6<V, X, A>(val + 36 * int64_t(k) + 6 * c, x + 6 * int64_t(ca));
+      const A pb = dot6<V, X, A>(val + 36 * int64_t(k + 1) + 6 * c, x + 6 * int64_t(cb));
+      acc += pa + pb;
     }
+    if (k < k1) acc += dot6<V, X, A>(val + 36 * int64_t(k) + 6 * c, x + 6 * int64_t(__ldg(col + k)));
   }
-  return (((s[0] + s[1]) + s[2]) + s[3]) + s[4];
+  return acc;
 }
 
 // component q of the row's 6-vector v (held by the row's lanes) - whole warp must call

@@ -1,10 +1,10 @@
 // tune.cu - the row schedule of every BSR operator, chosen from the committed table.
 //
-// Both schedules of spmv_row.cuh compute every row with the same additions in the same order, but
-// the reductions fused into the conjugate-gradient products group rows by thread block, and the
-// two schedules put different rows in a block. The choice is therefore a fixed function of the
-// operator's shape (mean blocks per row against the bound of sched_table.h), never of a timing,
-// so a problem gives the same bits alone, among other problems, and from one run to the next.
+// The two schedules of spmv_row.cuh add a row's blocks in different orders, and the reductions
+// fused into the conjugate-gradient products group rows by thread block differently. The choice
+// is therefore a fixed function of the operator's shape (mean blocks per row against the bound of
+// sched_table.h), never of a timing, so a problem gives the same bits alone, among other problems,
+// and from one run to the next.
 // The table is fitted offline by opus_destruct_2_gb300/autotune.py from the timings this file
 // records when asked.
 #include <chrono>

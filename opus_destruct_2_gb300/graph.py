@@ -122,7 +122,7 @@ class AmgOptions(ctypes.Structure):
                 ("reaggregate", ctypes.c_int32)]
 
 
-# StressOptions.precision (svxg_types.h): FP64; mixed for problems of 4096 free nodes or more
+# StressOptions.precision (svxg_types.h): FP64; mixed for problems of 65536 free nodes or more
 # (smaller ones run the FP64 sequence); mixed at every size
 PRECISION_FP64, PRECISION_MIXED, PRECISION_MIXED_ALL = 0, 1, 2
 
