@@ -72,6 +72,21 @@ int svxg_block_jacobi(const svxg_problem* p);
  * run state; the graph stays. */
 int svxg_release(svxg_problem* p);
 
+/* StressProblem::reassemble (stress.hpp:110, stress.cpp:178-211) after the caller changed the
+ * public members: the graph given here replaces the problem's, K is built again, the multigrid of
+ * the last assemble keeps preconditioning the nodes it covered, and nodes appended since (free
+ * indices from there on) get their own multigrid over K's appended block (24 nodes or more, when
+ * it builds) or their block-Jacobi inverses, applied additively. Falls back to assemble when
+ * nothing was assembled, the problem is block-Jacobi or free nodes were removed. *ok as assemble. */
+int svxg_reassemble(svxg_problem* p, const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb,
+                    const svxg_material* mats, int32_t* ok);
+/* StressProblem::appended (stress.hpp:114): free nodes the multigrid does not cover. */
+int32_t svxg_appended(const svxg_problem* p);
+/* StressProblem::extend_warm_start (stress.hpp:113, stress.cpp:213-244): u (host, 6 n doubles,
+ * in and out) with nodes first_new.. set from their intact bonds' older neighbours' rigid motion,
+ * averaged over up to four passes, on the device. */
+int svxg_extend_warm_start(svxg_problem* p, double* u, int32_t first_new);
+
 /* StressProblem::remove_bond / retire_nodes (stress.hpp:108-109, stress.cpp:260-310): in-place
  * K downdates that keep the preconditioner. */
 int svxg_remove_bond(svxg_problem* p, int32_t b);

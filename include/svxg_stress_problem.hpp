@@ -63,6 +63,25 @@ class StressProblem {
     sent_nodes_ = nodes;
     pull_flags();
   }
+  // stress.hpp:110 - K again from nodes and bonds as they are now; appended nodes get their own
+  // preconditioner, the old one keeps the rest
+  bool reassemble() {
+    if (mats.size() != SVXG_MAX_MATERIALS) throw std::runtime_error("svxg: mats needs every material id");
+    int32_t ok = 0;
+    check(svxg_reassemble(p_, nodes.data(), int32_t(nodes.size()), bonds.data(), int32_t(bonds.size()), mats.data(),
+                          &ok));
+    sent_nodes_ = nodes;
+    sent_bonds_ = bonds;
+    pull_flags();
+    return ok != 0;
+  }
+  // stress.hpp:113 - appended nodes' warm start from their older neighbours (u: 6 per node)
+  void extend_warm_start(std::vector<double>& u, int32_t first_new_node) {
+    upload_if_changed();
+    if (u.size() != 6 * nodes.size()) return;
+    check(svxg_extend_warm_start(p_, u.data(), first_new_node));
+  }
+  int32_t appended() const { return svxg_appended(p_); }
   int32_t free_nodes() const { return info().nfree; }
   int64_t matrix_blocks() const { return info().matrix_blocks; }
   int64_t memory_bytes() const { return info().device_bytes; }

@@ -73,6 +73,9 @@ def load_library() -> ctypes.CDLL:
         "svxg_set_graph": (c_i32, [c_vp, c_vp, c_i32, c_vp, c_i32, c_vp]),
         "svxg_assemble": (c_i32, [c_vp, c_vp, ctypes.POINTER(c_i32)]),
         "svxg_assembled": (c_i32, [c_vp]),
+        "svxg_reassemble": (c_i32, [c_vp, c_vp, c_i32, c_vp, c_i32, c_vp, ctypes.POINTER(c_i32)]),
+        "svxg_appended": (c_i32, [c_vp]),
+        "svxg_extend_warm_start": (c_i32, [c_vp, c_vp, c_i32]),
         "svxg_invalidate": (c_i32, [c_vp]),
         "svxg_preconditioner_current": (c_i32, [c_vp]),
         "svxg_block_jacobi": (c_i32, [c_vp]),
@@ -174,6 +177,32 @@ class StressProblem:
         _check(self._L.svxg_assemble(self._h, ctypes.byref(opt) if opt is not None else None, ctypes.byref(ok)))
         self._pull_flags()
         return bool(ok.value)
+
+    def reassemble(self) -> bool:
+        """StressProblem::reassemble (stress.cpp:178-211): K again from the current nodes and bonds;
+        nodes appended since the last assemble() get their own preconditioner (their multigrid,
+        or their diagonal blocks), the old one keeps the rest."""
+        self.nodes = np.ascontiguousarray(self.nodes, dtype=NODE_DTYPE)
+        self.bonds = np.ascontiguousarray(self.bonds, dtype=BOND_DTYPE)
+        ok = c_i32(0)
+        _check(self._L.svxg_reassemble(self._h, ptr(self.nodes), len(self.nodes), ptr(self.bonds), len(self.bonds),
+                                       ptr(self.mats), ctypes.byref(ok)))
+        self._pull_flags()
+        return bool(ok.value)
+
+    def appended(self) -> int:
+        """Free nodes the last assemble()'s multigrid does not cover (StressProblem::appended)."""
+        return int(self._L.svxg_appended(self._h))
+
+    def extend_warm_start(self, u, first_new: int):
+        """StressProblem::extend_warm_start (stress.cpp:213-244): u (6 per node) with the nodes from
+        first_new on set from their bonded, older neighbours' motion; returns the new array."""
+        self._sync_graph()
+        out = np.array(u, dtype=np.float64)
+        if out.size != 6 * len(self.nodes):
+            raise ValueError("u: 6 per node")
+        _check(self._L.svxg_extend_warm_start(self._h, ptr(out), int(first_new)))
+        return out
 
     def assembled(self) -> bool:
         return bool(self._L.svxg_assembled(self._h))

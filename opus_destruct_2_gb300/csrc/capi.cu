@@ -54,6 +54,8 @@ void release_solver(Problem& P) {
   destroy_loop(P.loop_plain);
   destroy_loop(P.loop_mixed);
   free_run(P);
+  release_appended(P);
+  P.pc_n = 0;
   P.mem.release(P.K.rowptr);
   P.mem.release(P.K.col);
   P.mem.release(P.K.val);
@@ -294,23 +296,29 @@ void svxg_problem_destroy(svxg_problem* p) {
 
 void* svxg_problem_stream(svxg_problem* p) { return p ? static_cast<void*>(p->P.stream) : nullptr; }
 
-int svxg_set_graph(svxg_problem* p, const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb,
-                   const svxg_material* mats) {
-  CHECK_P(p);
-  Problem& P = p->P;
+}  // extern "C"
+
+namespace svxg {
+
+static int check_graph(const char* who, const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb,
+                       const svxg_material* mats) {
   if (n < 0 || nb < 0 || (n > 0 && !nodes) || (nb > 0 && !bonds) || !mats) {
-    set_error("svxg_set_graph: bad sizes or null arrays");
+    set_error(std::string(who) + ": bad sizes or null arrays");
     return SVXG_ERR_ARG;
   }
   for (int32_t k = 0; k < nb; ++k) {
     const svxg_bond& b = bonds[k];
     if (b.a < 0 || b.a >= n || b.b >= n || b.b == b.a || b.ma >= SVXG_MAX_MATERIALS || b.mb >= SVXG_MAX_MATERIALS) {
-      set_error("svxg_set_graph: bond " + std::to_string(k) + " has a bad node or material");
+      set_error(std::string(who) + ": bond " + std::to_string(k) + " has a bad node or material");
       return SVXG_ERR_ARG;
     }
   }
-  DeviceScope ds(P.device);
-  release_solver(P);
+  return SVXG_OK;
+}
+
+// the graph's device and host copies replaced (the solver is left as it is)
+static int upload_graph(Problem& P, const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb,
+                        const svxg_material* mats) {
   P.mem.release(P.d_nodes);
   P.mem.release(P.d_bonds);
   P.mem.release(P.d_mats);
@@ -330,6 +338,20 @@ int svxg_set_graph(svxg_problem* p, const svxg_node* nodes, int32_t n, const svx
   SVXG_CUDA(host_wait(P.stream));
   P.have_graph = true;
   return SVXG_OK;
+}
+
+}  // namespace svxg
+
+extern "C" {
+
+int svxg_set_graph(svxg_problem* p, const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb,
+                   const svxg_material* mats) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  TRY(check_graph("svxg_set_graph", nodes, n, bonds, nb, mats));
+  DeviceScope ds(P.device);
+  release_solver(P);
+  return upload_graph(P, nodes, n, bonds, nb, mats);
 }
 
 static int assemble_impl(Problem& P, const svxg_stress_options* opt, int32_t* ok) {
@@ -368,6 +390,46 @@ static int assemble_impl(Problem& P, const svxg_stress_options* opt, int32_t* ok
   TRY(tune_k64(P));
   P.sched_k32 = P.jacobi_only || P.lv.empty() ? 0 : P.lv[0].sched_a;  // (K32 is level 0's cycle operator)
   SVXG_CUDA(host_wait(P.stream));
+  P.pc_n = P.jacobi_only ? 0 : P.nfree;
+  P.assembled = true;
+  if (ok) *ok = 1;
+  return SVXG_OK;
+}
+
+// StressProblem::reassemble (stress.cpp:178-211) with the graph replaced by the caller's
+static int reassemble_impl(Problem& P, const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb,
+                           const svxg_material* mats, int32_t* ok) {
+  if (ok) *ok = 0;
+  const svxg_stress_options opt = P.opt;
+  if (!P.assembled || P.jacobi_only || P.lv.empty() || P.pc_n == 0) {
+    release_solver(P);
+    TRY(upload_graph(P, nodes, n, bonds, nb, mats));
+    return assemble_impl(P, &opt, ok);
+  }
+  trace_mark(P, "start", true);
+  // the multigrid stays; its level-0 operator keeps the arrays of the K it was built from
+  destroy_loop(P.loop_plain);
+  destroy_loop(P.loop_mixed);
+  free_run(P);
+  release_appended(P);
+  P.mem.release(P.d_jinv);
+  P.mem.release(P.d_un);
+  if (P.K.val32 && !P.lv.empty() && P.lv[0].A.val32 != P.K.val32) P.mem.release(P.K.val32);
+  P.K = Bsr{};
+  P.assembled = false;
+  P.pc_current = false;
+  TRY(upload_graph(P, nodes, n, bonds, nb, mats));
+  TRY(assemble_matrix(P));
+  if (P.nfree < P.pc_n) {  // (nodes left: the indices moved)
+    release_solver(P);
+    return assemble_impl(P, &opt, ok);
+  }
+  TRY(build_jacobi(P));
+  TRY(build_appended(P));
+  TRY(tune_k64(P));
+  P.sched_k32 = 0;
+  SVXG_CUDA(host_wait(P.stream));
+  trace_mark(P, "reassembled");
   P.assembled = true;
   if (ok) *ok = 1;
   return SVXG_OK;
@@ -376,6 +438,33 @@ static int assemble_impl(Problem& P, const svxg_stress_options* opt, int32_t* ok
 int svxg_assemble(svxg_problem* p, const svxg_stress_options* opt, int32_t* ok) {
   CHECK_P(p);
   return assemble_impl(p->P, opt, ok);
+}
+
+int svxg_reassemble(svxg_problem* p, const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb,
+                    const svxg_material* mats, int32_t* ok) {
+  CHECK_P(p);
+  TRY(check_graph("svxg_reassemble", nodes, n, bonds, nb, mats));
+  DeviceScope ds(p->P.device);
+  return reassemble_impl(p->P, nodes, n, bonds, nb, mats, ok);
+}
+
+int32_t svxg_appended(const svxg_problem* p) {
+  return p && p->P.assembled && !p->P.jacobi_only ? p->P.nfree - p->P.pc_n : 0;
+}
+
+int svxg_extend_warm_start(svxg_problem* p, double* u, int32_t first_new) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  if (!u) return SVXG_ERR_ARG;
+  if (first_new < 0 || first_new >= P.n) return SVXG_OK;
+  DeviceScope ds(P.device);
+  TRY(ensure_node_vectors(P));
+  const size_t m = 6 * size_t(P.n);
+  SVXG_CUDA(cudaMemcpyAsync(P.d_un, u, m * sizeof(double), cudaMemcpyHostToDevice, P.stream));
+  TRY(extend_warm_start_device(P, P.d_un, first_new));
+  SVXG_CUDA(cudaMemcpyAsync(u, P.d_un, m * sizeof(double), cudaMemcpyDeviceToHost, P.stream));
+  SVXG_CUDA(host_wait(P.stream));
+  return SVXG_OK;
 }
 
 int svxg_assembled(const svxg_problem* p) { return p && p->P.assembled ? 1 : 0; }

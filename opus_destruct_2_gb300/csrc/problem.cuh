@@ -159,6 +159,8 @@ struct Problem {
   // assembly
   svxg_stress_options opt{};
   bool assembled = false, pc_current = false, jacobi_only = false;
+  int32_t pc_n = 0;               // free nodes the multigrid covers (nodes appended since: pc_n..nfree)
+  Problem* sub = nullptr;         // the appended nodes' own multigrid (reassemble), owned
   int64_t assembly_work = 0;
   int32_t nfree = 0;
   int32_t* d_dof = nullptr;       // node -> free index (-1 fixed)
@@ -249,6 +251,11 @@ enum OpKind { kOpK64 = 0, kOpA32 = 1, kOpP32 = 2, kOpR32 = 3 };
 int table_sched(int kind, int64_t rows, int64_t blocks);
 bool tune_timing();
 int tune_decide(Problem& P, int kind, int level, int64_t rows, int64_t blocks, float ms_warp, float ms_group);
+// exact_appended.cu (StressProblem::reassemble / extend_warm_start)
+int build_appended(Problem& P);                  // P.sub over K's appended block (>= 24 nodes)
+void release_appended(Problem& P);
+int precondition_amg(Problem& P, const double* r, double* z);  // the multigrid, plus the appended part
+int extend_warm_start_device(Problem& P, double* u_nodes, int32_t first_new);
 // vcycle.cu
 int vcycle(Problem& P, const double* r, double* z);
 int vcycle32(Problem& P, const float* r, float* z);
@@ -269,7 +276,7 @@ constexpr int32_t kGraphMinFree = 4096;
 // sequence runs (with the same FP32 V-cycle)
 constexpr int32_t kMixedMinFree = 65536;
 inline bool mixed_run(const Problem& P) {
-  if (P.jacobi_only) return false;
+  if (P.jacobi_only || P.pc_n < P.nfree || !P.K.val32) return false;
   return P.opt.precision == SVXG_PRECISION_MIXED_ALL ||
          (P.opt.precision == SVXG_PRECISION_MIXED && P.nfree >= kMixedMinFree);
 }

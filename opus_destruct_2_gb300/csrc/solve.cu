@@ -474,7 +474,7 @@ int precondition(Problem& P, const double* r, double* z) {
     SVXG_CUDA(cudaGetLastError());
     return SVXG_OK;
   }
-  return vcycle(P, r, z);
+  return precondition_amg(P, r, z);
 }
 
 // StressProblem::begin (stress.cpp:362-401); f, u0: device, node order (u0 may be null)
@@ -500,7 +500,7 @@ int pcg_begin(Problem& P, const double* f_nodes, const double* u0_nodes) {
     } else if (mixed_run(P)) {
       // (the mixed run starts each inner sequence from the FP64 residual)
     } else {
-      TRY(vcycle(P, P.d_r, P.d_z));
+      TRY(precondition_amg(P, P.d_r, P.d_z));
       (k_rz<0><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_r, P.d_z, P.d_p, P.d_partials, P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
     }
   }
@@ -524,7 +524,7 @@ int plain_body(Problem& P) {
     (k_jacobi_rz<1><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_jinv, P.d_r, P.d_z, nullptr, P.d_partials, P.d_counter,
                                                       P.d_s), SVXG_COUNT_LAUNCH());
   } else {
-    TRY(vcycle(P, P.d_r, P.d_z));
+    TRY(precondition_amg(P, P.d_r, P.d_z));
     (k_rz<1><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_r, P.d_z, nullptr, P.d_partials, P.d_counter, P.d_s),
      SVXG_COUNT_LAUNCH());
   }
@@ -560,7 +560,7 @@ int pcg_restart_fp64(Problem& P) {
     TRY(spmv(P, P.K, P.d_x, P.d_q));
     (k_begin_r<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_f, P.d_q, P.d_r, P.d_partials, P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
     (k_begin_zero<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_x, P.d_r, P.d_s), SVXG_COUNT_LAUNCH());
-    TRY(vcycle(P, P.d_r, P.d_z));
+    TRY(precondition_amg(P, P.d_r, P.d_z));
     (k_rz<0><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_r, P.d_z, P.d_p, P.d_partials, P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
   }
   SVXG_CUDA(cudaGetLastError());

@@ -96,6 +96,7 @@ def reference_lib() -> ctypes.CDLL | None:
         lib.svxr_solve.argtypes = [c_vp, c_i32, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_f64, c_i32, c_i32, c_vp, c_vp,
                                    c_vp, c_vp]
         lib.svxr_judge.argtypes = [c_vp, c_i32, c_vp, c_i32, c_vp, c_vp, c_f64, c_vp, c_vp, c_vp, c_vp]
+        lib.svxr_extend_warm_start.argtypes = [c_vp, c_i32, c_vp, c_i32, c_vp, c_vp, c_i32]
         lib.svxr_utilization.restype = c_f64
         lib.svxr_utilization.argtypes = [c_vp, c_vp, c_f64, c_vp, c_vp]
         lib.svxr_matrix.restype = c_i32
@@ -260,6 +261,47 @@ class Port:
         return y
 
 
+def extend_warm_start(nodes, bonds, u, first_new: int):
+    """StressProblem::extend_warm_start (core/src/stress/stress.cpp:213-244), restated: nodes from
+    first_new on take the mean rigid transfer (u_a + th_a x (x_c - x_a)) of their intact bonds'
+    known neighbours, for up to four passes, bonds in index order. Returns the new u."""
+    n = len(nodes)
+    u = np.array(u, dtype=np.float64)
+    if first_new >= n or u.size != 6 * n:
+        return u
+    c = [(float(x), float(y), float(z)) for x, y, z in zip(nodes["c"]["x"], nodes["c"]["y"], nodes["c"]["z"])]
+    known = [i < first_new and not nodes["gone"][i] for i in range(n)]
+    for _ in range(4):
+        acc = [[0.0] * 6 for _ in range(n)]
+        w = [0.0] * n
+        for a, b, broken in zip(bonds["a"], bonds["b"], bonds["broken"]):
+            a, b = int(a), int(b)
+            if broken or b < 0:
+                continue
+            for src, dst in ((a, b), (b, a)):
+                if known[src] and not known[dst] and dst >= first_new:
+                    r = (c[dst][0] - c[src][0], c[dst][1] - c[src][1], c[dst][2] - c[src][2])
+                    th = (u[6 * src + 3], u[6 * src + 4], u[6 * src + 5])
+                    t = (th[1] * r[2] - th[2] * r[1], th[2] * r[0] - th[0] * r[2], th[0] * r[1] - th[1] * r[0])
+                    for q in range(3):
+                        acc[dst][q] += u[6 * src + q] + t[q]
+                    for q in range(3, 6):
+                        acc[dst][q] += u[6 * src + q]
+                    w[dst] += 1.0
+                    break
+        changed = False
+        for i in range(first_new, n):
+            if known[i] or w[i] == 0.0:
+                continue
+            for q in range(6):
+                u[6 * i + q] = acc[i][q] / w[i]
+            known[i] = True
+            changed = True
+        if not changed:
+            break
+    return u
+
+
 class Reference:
     """The reference's own StressProblem, compiled from its sources (see ref_shim.cpp)."""
 
@@ -280,6 +322,12 @@ class Reference:
                                  int(warm), ctypes.byref(res), ctypes.byref(info), ctypes.byref(ta),
                                  ctypes.byref(ts))
         return dict(ok=bool(ok), u=u, res=res, info=info, t_assemble=ta.value, t_solve=ts.value)
+
+    def extend_warm_start(self, u, first_new: int):
+        out = np.array(u, dtype=np.float64)
+        self.lib.svxr_extend_warm_start(ptr(self.nodes), len(self.nodes), ptr(self.bonds), len(self.bonds),
+                                        ptr(self.mats), ptr(out), int(first_new))
+        return out
 
     def judge(self, u, fragility=1.0):
         nb = len(self.bonds)

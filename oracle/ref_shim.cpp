@@ -184,6 +184,20 @@ int svxr_solve(const svxg_node* nodes, int32_t n, svxg_bond* bonds, int32_t nb, 
   return ok ? 1 : 0;
 }
 
+// StressProblem::extend_warm_start (core/src/stress/stress.cpp:213-244) of u (6 per node, in
+// and out) for nodes first_new and up.
+void svxr_extend_warm_start(const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb,
+                            const svxg_material* mats, double* u, int32_t first_new) {
+  MaterialTable table;
+  fill_materials(table, mats);
+  StressProblem P;
+  P.mats = &table;
+  fill_problem(P, nodes, n, bonds, nb);
+  std::vector<f64> uv(u, u + 6 * size_t(n));
+  P.extend_warm_start(uv, first_new);
+  std::memcpy(u, uv.data(), sizeof(double) * 6 * size_t(n));
+}
+
 // The judge's per-bond work: bond_load and bond_utilization (core/src/stress/stress.cpp:477-502,
 // :23-57) of every bond at u (6 per node).
 void svxr_judge(const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb, const svxg_material* mats,

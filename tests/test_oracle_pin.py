@@ -78,3 +78,21 @@ def test_matrix_and_hierarchy_bit_identical(name, make, opts, rtol):
             assert np.array_equal(getattr(A, k), getattr(B, k)), k
         assert A.lmax.value == B.lmax.value
     assert np.array_equal(P2.chol(), chol)
+
+
+def test_extend_warm_start_bit_identical():
+    """The oracle's extend_warm_start (stress.cpp:213-244) against the reference's, on a lattice
+    whose top layers were appended, from a seeded displacement of the older nodes."""
+    from oracle import extend_warm_start
+    from test_gpu_reassemble import appended_case
+    for n, top in ((6, 2), (8, 1)):
+        _, _, nodes, bonds, n_old = appended_case(n, top)
+        rng = np.random.default_rng(n)
+        u = np.zeros(6 * len(nodes))
+        u[:6 * n_old] = rng.normal(size=6 * n_old) * 1e-3
+        bonds = bonds.copy()
+        bonds["broken"][rng.choice(len(bonds), size=len(bonds) // 10, replace=False)] = 1
+        a = extend_warm_start(nodes, bonds, u, n_old)
+        b = Reference(nodes, bonds, MATS).extend_warm_start(u, n_old)
+        assert np.array_equal(a, b)
+        assert np.any(a[6 * n_old:] != 0.0)
