@@ -144,6 +144,128 @@ __global__ void __launch_bounds__(exact::kThreads) k_lmax_norm(int64_t m, const 
   for (int64_t k = threadIdx.x; k < m; k += blockDim.x) v[k] = w[k] / nv;
 }
 
+// The exact norm of a large vector over many blocks. Chunks of kChunk terms: (1) each chunk's
+// approximate sum (any order); (2) per chunk, the approximate sum before it predicts the binade the
+// sequential sum is in over the chunk; when the chunk's start and end lie safely inside one binade,
+// the chunk's composed increment pair in that binade is computed; (3) one block walks the chunks in
+// order with the exact running sum: a chunk whose pair was made for the sum's actual binade and
+// that does not carry it out of the binade is added in one step, any other chunk term by term
+// (exact::sequential_sum_from). The predictions only choose the path: every step is exact.
+constexpr int64_t kChunk = int64_t(exact::kThreads) * exact::kItems;
+constexpr int32_t kNoPair = -100000;
+
+__global__ void __launch_bounds__(256) k_norm_chunk_sum(int64_t m, const double* w, double* csum, const double* state) {
+  __shared__ double sh[256];
+  if (state[2] != 0.0) return;
+  const int64_t a = int64_t(blockIdx.x) * kChunk, b = a + kChunk < m ? a + kChunk : m;
+  double s = 0.0;
+  for (int64_t k = a + threadIdx.x; k < b; k += 256) s += w[k] * w[k];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int d = 128; d > 0; d >>= 1) {
+    if (int(threadIdx.x) < d) sh[threadIdx.x] += sh[threadIdx.x + d];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) csum[blockIdx.x] = sh[0];
+}
+
+__global__ void __launch_bounds__(exact::kThreads) k_norm_chunk_pair(int64_t m, int32_t nchunk, const double* w,
+                                                                     const double* csum, exact::Pair* cpair,
+                                                                     int32_t* cuexp, const double* state) {
+  __shared__ double sh[exact::kThreads];
+  if (state[2] != 0.0) return;
+  const int32_t c = blockIdx.x;
+  double s = 0.0;
+  for (int32_t j = threadIdx.x; j < c; j += exact::kThreads) s += csum[j];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int d = exact::kThreads / 2; d > 0; d >>= 1) {
+    if (int(threadIdx.x) < d) sh[threadIdx.x] += sh[threadIdx.x + d];
+    __syncthreads();
+  }
+  const double before = sh[0], after = sh[0] + csum[c];
+  const double lo = before * (1.0 - 1e-8), hi = after * (1.0 + 1e-8);
+  int64_t S;
+  int ulo = 0, uhi = 1;
+  const bool finite = lo > 0.0 && hi < 1e300;
+  if (finite) {
+    exact::split(lo, &S, &ulo);
+    exact::split(hi, &S, &uhi);
+  }
+  if (!finite || ulo != uhi || ulo == -1074) {
+    if (threadIdx.x == 0) cuexp[c] = kNoPair;
+    return;
+  }
+  const int64_t a = int64_t(c) * kChunk, base = a + int64_t(threadIdx.x) * exact::kItems;
+  const int64_t b = a + kChunk < m ? a + kChunk : m;
+  exact::Pair acc{0, 0};
+  for (int it = 0; it < exact::kItems; ++it) {
+    const int64_t k = base + it;
+    if (k < b) {
+      const double x = w[k];
+      acc = exact::compose(acc, exact::term_pair(x * x, ulo));
+    }
+  }
+  exact::Pair tot;
+  exact::block_scan(acc, &tot);
+  if (threadIdx.x == 0) {
+    cpair[c] = tot;
+    cuexp[c] = ulo;
+  }
+}
+
+__global__ void __launch_bounds__(exact::kThreads) k_norm_walk(int64_t m, int32_t nchunk, const double* w,
+                                                               const exact::Pair* cpair, const int32_t* cuexp,
+                                                               double* state) {
+  __shared__ double s_sh;
+  __shared__ int32_t c_sh;
+  if (state[2] != 0.0) return;
+  if (threadIdx.x == 0) {
+    s_sh = 0.0;
+    c_sh = 0;
+  }
+  __syncthreads();
+  for (;;) {
+    if (threadIdx.x == 0) {
+      double s = s_sh;
+      int32_t c = c_sh;
+      while (c < nchunk && cuexp[c] != kNoPair && s > 0.0 && s < 1e300) {
+        int64_t S;
+        int ue;
+        exact::split(s, &S, &ue);
+        if (ue != cuexp[c]) break;
+        const int64_t S2 = exact::sat(S, exact::pick(cpair[c], S));
+        if (S2 >= (int64_t(1) << 53)) break;
+        s = exact::join(S2, ue);
+        ++c;
+      }
+      s_sh = s;
+      c_sh = c;
+    }
+    __syncthreads();
+    const int32_t c = c_sh;
+    const double s0 = s_sh;
+    __syncthreads();
+    if (c >= nchunk) break;
+    const int64_t a = int64_t(c) * kChunk, b = a + kChunk < m ? a + kChunk : m;
+    const double s1 = exact::sequential_sum_from(s0, a, b, [w](int64_t k) {
+      const double x = w[k];
+      return x * x;
+    });
+    if (threadIdx.x == 0) {
+      s_sh = s1;
+      c_sh = c + 1;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double nv = sqrt(s_sh);
+    state[1] = nv;
+    if (!(nv > 0)) state[2] = 1.0;
+    else state[0] = nv;
+  }
+}
+
 // v = w / nv for a large level (after k_lmax_norm without scaling)
 __global__ void k_lmax_rescale(int64_t m, const double* w, double* v, const double* state) {
   const double nv = state[1];
@@ -822,11 +944,27 @@ int estimate_lmax(Problem& P, const Level& L, double* out) {
   (k_lmax_init<<<nblk(m), kT, 0, P.stream>>>(m, v.p), SVXG_COUNT_LAUNCH());
   const bool fused = m <= kLmaxFusedMax;
   const unsigned ab = unsigned((m + 6 * kApplyNodes - 1) / (6 * kApplyNodes));
+  const int32_t nchunk = int32_t((m + kChunk - 1) / kChunk);
+  Tmp<double> csum(P.stream);
+  Tmp<exact::Pair> cpair(P.stream);
+  Tmp<int32_t> cuexp(P.stream);
+  if (!fused) {
+    TRY(csum.alloc(size_t(nchunk)));
+    TRY(cpair.alloc(size_t(nchunk)));
+    TRY(cuexp.alloc(size_t(nchunk)));
+  }
   for (int it = 0; it < 15; ++it) {
     (k_lmax_apply<<<ab, 6 * kApplyNodes, 0, P.stream>>>(n, L.A.rowptr, L.A.col, L.A.val, L.dinv, v.p, w.p, st.p),
      SVXG_COUNT_LAUNCH());
-    (k_lmax_norm<<<1, exact::kThreads, 0, P.stream>>>(m, w.p, v.p, st.p, fused ? 1 : 0), SVXG_COUNT_LAUNCH());
-    if (!fused) (k_lmax_rescale<<<nblk(m), kT, 0, P.stream>>>(m, w.p, v.p, st.p), SVXG_COUNT_LAUNCH());
+    if (fused) {
+      (k_lmax_norm<<<1, exact::kThreads, 0, P.stream>>>(m, w.p, v.p, st.p, 1), SVXG_COUNT_LAUNCH());
+      continue;
+    }
+    (k_norm_chunk_sum<<<unsigned(nchunk), 256, 0, P.stream>>>(m, w.p, csum.p, st.p), SVXG_COUNT_LAUNCH());
+    (k_norm_chunk_pair<<<unsigned(nchunk), exact::kThreads, 0, P.stream>>>(m, nchunk, w.p, csum.p, cpair.p, cuexp.p,
+                                                                          st.p), SVXG_COUNT_LAUNCH());
+    (k_norm_walk<<<1, exact::kThreads, 0, P.stream>>>(m, nchunk, w.p, cpair.p, cuexp.p, st.p), SVXG_COUNT_LAUNCH());
+    (k_lmax_rescale<<<nblk(m), kT, 0, P.stream>>>(m, w.p, v.p, st.p), SVXG_COUNT_LAUNCH());
   }
   SVXG_CUDA(cudaGetLastError());
   double h[3];
@@ -1129,10 +1267,34 @@ __global__ void k_level0_pos(int32_t n, const svxg_node* nodes, const int32_t* d
 
 }  // namespace
 
-// sqrt of the sequential sum of squares of n device doubles (the power iteration's norm)
+__global__ void k_state_norm_out(const double* state, double* out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *out = state[1];
+}
+
+// sqrt of the sequential sum of squares of n device doubles (the power iteration's norm), by the
+// path estimate_lmax takes for a vector of that length
 int debug_seq_norm(cudaStream_t st, const double* v, int64_t n, double* out_dev) {
-  (k_seq_norm<<<1, exact::kThreads, 0, st>>>(n, v, out_dev), SVXG_COUNT_LAUNCH());
+  if (n <= kLmaxFusedMax) {
+    (k_seq_norm<<<1, exact::kThreads, 0, st>>>(n, v, out_dev), SVXG_COUNT_LAUNCH());
+    SVXG_CUDA(cudaGetLastError());
+    return SVXG_OK;
+  }
+  const int32_t nchunk = int32_t((n + kChunk - 1) / kChunk);
+  Tmp<double> csum(st), state(st);
+  Tmp<exact::Pair> cpair(st);
+  Tmp<int32_t> cuexp(st);
+  TRY(csum.alloc(size_t(nchunk)));
+  TRY(cpair.alloc(size_t(nchunk)));
+  TRY(cuexp.alloc(size_t(nchunk)));
+  TRY(state.alloc(3));
+  SVXG_CUDA(cudaMemsetAsync(state.p, 0, 3 * sizeof(double), st));
+  (k_norm_chunk_sum<<<unsigned(nchunk), 256, 0, st>>>(n, v, csum.p, state.p), SVXG_COUNT_LAUNCH());
+  (k_norm_chunk_pair<<<unsigned(nchunk), exact::kThreads, 0, st>>>(n, nchunk, v, csum.p, cpair.p, cuexp.p, state.p),
+   SVXG_COUNT_LAUNCH());
+  (k_norm_walk<<<1, exact::kThreads, 0, st>>>(n, nchunk, v, cpair.p, cuexp.p, state.p), SVXG_COUNT_LAUNCH());
+  (k_state_norm_out<<<1, 32, 0, st>>>(state.p, out_dev), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
+  SVXG_CUDA(host_wait(st));
   return SVXG_OK;
 }
 

@@ -99,40 +99,57 @@ __device__ __forceinline__ double join(int64_t S, int uexp) {
   return __longlong_as_double((long long)((E << 52) | (uint64_t(S) & ((uint64_t(1) << 52) - 1))));
 }
 
-// Block-wide exclusive scan of pairs (kThreads threads); returns the exclusive prefix of this
-// thread's pair and the block total in *tot.
-__device__ inline Pair block_scan(Pair v, Pair* tot) {
-  __shared__ Pair sh[kThreads];
-  sh[threadIdx.x] = v;
-  __syncthreads();
-  // Hillis-Steele inclusive scan
-  for (int d = 1; d < kThreads; d <<= 1) {
-    Pair x = sh[threadIdx.x];
-    if (int(threadIdx.x) >= d) x = compose(sh[threadIdx.x - d], x);
-    __syncthreads();
-    sh[threadIdx.x] = x;
-    __syncthreads();
+__device__ __forceinline__ Pair shfl_up_pair(Pair v, int d) {
+  Pair u;
+  u.d0 = __shfl_up_sync(0xffffffffu, v.d0, d);
+  u.d1 = __shfl_up_sync(0xffffffffu, v.d1, d);
+  return u;
+}
+
+// inclusive scan of the warp's pairs (whole warp)
+__device__ __forceinline__ Pair warp_scan(Pair v) {
+  const int lane = threadIdx.x & 31;
+  for (int d = 1; d < 32; d <<= 1) {
+    const Pair u = shfl_up_pair(v, d);
+    if (lane >= d) v = compose(u, v);
   }
-  const Pair incl = sh[threadIdx.x];
-  *tot = sh[kThreads - 1];
-  Pair ex = threadIdx.x ? sh[threadIdx.x - 1] : Pair{0, 0};
+  return v;
+}
+
+// Block-wide exclusive scan of pairs (kThreads threads): warps scan by shuffles, then the warps'
+// totals; returns the exclusive prefix of this thread's pair and the block total in *tot.
+__device__ inline Pair block_scan(Pair v, Pair* tot) {
+  __shared__ Pair wsum[kThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const Pair incl = warp_scan(v);
+  Pair ex_w = shfl_up_pair(incl, 1);
+  if (lane == 0) ex_w = Pair{0, 0};
+  if (lane == 31) wsum[w] = incl;
   __syncthreads();
-  (void)incl;
-  return ex;
+  if (w == 0) {
+    const Pair x = warp_scan(wsum[lane]);  // (kThreads / 32 == 32 warps)
+    wsum[lane] = x;
+  }
+  __syncthreads();
+  const Pair before = w ? wsum[w - 1] : Pair{0, 0};
+  *tot = wsum[kThreads / 32 - 1];
+  __syncthreads();
+  return compose(before, ex_w);
 }
 
 __device__ __forceinline__ int64_t pick(Pair p, int64_t S) { return (S & 1) ? p.d1 : p.d0; }
 
-// The sequential sum of term(k) for k in [0, n), with term(k) >= 0; one block of kThreads.
-// Term: a callable (int64_t k) -> double.
+// The sequential sum s0 + term(a) + ... + term(n - 1), added one by one from s0 (>= 0), with
+// term(k) >= 0; one block of kThreads. Term: a callable (int64_t k) -> double. Every thread gets
+// the result.
 template <class Term>
-__device__ inline double sequential_sum(int64_t n, Term term) {
+__device__ inline double sequential_sum_from(double s0, int64_t a, int64_t n, Term term) {
   __shared__ double s_sh;
   __shared__ int64_t p_sh;
   __shared__ int64_t first_sh;
   if (threadIdx.x == 0) {
-    s_sh = 0.0;
-    p_sh = 0;
+    s_sh = s0;
+    p_sh = a;
   }
   __syncthreads();
   constexpr int64_t kTile = int64_t(kThreads) * kItems;
@@ -230,7 +247,15 @@ __device__ inline double sequential_sum(int64_t n, Term term) {
     }
     __syncthreads();
   }
-  return s_sh;
+  const double r = s_sh;
+  __syncthreads();
+  return r;
+}
+
+// The sequential sum of term(k) for k in [0, n) from 0.
+template <class Term>
+__device__ inline double sequential_sum(int64_t n, Term term) {
+  return sequential_sum_from(0.0, 0, n, term);
 }
 
 }  // namespace exact

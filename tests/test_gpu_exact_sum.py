@@ -1,6 +1,7 @@
 """The device's parallel reproduction of a sequential double sum (the multigrid setup's norm,
 core/src/solve/amg.cpp:267-268) against the sequential loop itself: bit for bit, on magnitudes
-spread over 80 binades, exact ties, subnormals, zeros, and non-finite terms."""
+spread over 80 binades, exact ties, subnormals, zeros, and non-finite terms - in one block for
+shorter vectors and by chunks over many blocks for vectors past 131,072 terms."""
 import ctypes
 import math
 
@@ -34,6 +35,10 @@ CASES = {
     "tiny": lambda r: r.random(30_000) * 1e-160,
     "zeros_first": lambda r: np.concatenate([np.zeros(20_000), r.normal(size=20_000)]),
     "power_iteration": lambda r: r.normal(size=1_131_000) * 1e-3,
+    "wide_many_chunks": lambda r: np.exp(r.uniform(-90, 90, 400_000)),
+    "ties_many_chunks": lambda r: np.sqrt((r.integers(0, 8, 300_000) * 0.5) * 2.0 ** r.integers(-3, 3, 300_000)),
+    "growing_many_chunks": lambda r: np.arange(1, 500_001, dtype=np.float64) ** 0.5 * r.uniform(0.9, 1.1, 500_000),
+    "zeros_then_chunks": lambda r: np.concatenate([np.zeros(150_000), r.normal(size=150_000)]),
     "single": lambda r: np.array([3.0]),
     "empty": lambda r: np.zeros(0),
 }
@@ -46,9 +51,10 @@ def test_sequential_norm_bits(name):
     assert (a == b) or (math.isnan(a) and math.isnan(b)), (a, b)
 
 
-def test_non_finite_terms():
-    v = np.ones(10_000)
-    v[5000] = np.inf
+@pytest.mark.parametrize("n", [10_000, 300_000])
+def test_non_finite_terms(n):
+    v = np.ones(n)
+    v[n // 2] = np.inf
     assert dev_norm(v) == math.inf
-    v[7000] = np.nan
+    v[n // 2 + 2000] = np.nan
     assert math.isnan(dev_norm(v))
