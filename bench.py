@@ -114,6 +114,17 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(x: float, dist, device) -> float:
+    """The largest x over the ranks (the slowest rank's time); x itself without a process group.
+    `device`: where the collective's tensor lives (a CUDA device for NCCL, the CPU for gloo)."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args, rank: int, world: int):
     """The reference's CPU implementation of the path: the oracle port, every host thread."""
     if rank != 0:
@@ -339,10 +350,7 @@ def main():
     clk = clocks.stop()
     iters = res.iters
     info_fail = n_over.value
-    if dist is not None:
-        t = torch.tensor([elapsed], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+    elapsed = max_over_ranks(elapsed, dist, dev)
     # --- roofline: the same solves again, each CG SpMV launch bracketed by CUDA events on the
     # problem's stream (the library then drives iterations from the host instead of one graph) ---
     tm, tl = ctypes.c_double(), ctypes.c_int64()
@@ -361,10 +369,7 @@ def main():
         step_host()
     barrier()
     e2e_elapsed = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_elapsed], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_elapsed = float(t.item())
+    e2e_elapsed = max_over_ranks(e2e_elapsed, dist, dev)
 
     from opus_destruct_2_gb300 import Info
     info = Info()
