@@ -646,6 +646,128 @@ __global__ void k_ap_values(int32_t n, const int32_t* rowptr, const int32_t* col
   }
 }
 
+// The same A P rows, accumulated in shared memory when a row has at most kAccSlots blocks (the
+// row's blocks are read-modify-written once per product; in shared memory that round trip is
+// short): each lane keeps its row of A_ik in registers across the k's P entries and adds, for
+// every entry of a product, the same sum in the same order as warp_mul6_add. Longer rows go
+// through global memory as in k_ap_values.
+constexpr int kAccSlots = 40;
+constexpr int kAccWarps = 4;
+__global__ void __launch_bounds__(32 * kAccWarps) k_ap_values_acc(int32_t n, const int32_t* rowptr, const int32_t* col,
+                                                                  const double* val, const int32_t* prow,
+                                                                  const int32_t* pcol, const double* pval,
+                                                                  const int32_t* aprow, const int32_t* scratch,
+                                                                  const int64_t* soff, int32_t* apcol, double* apval) {
+  __shared__ double acc_sh[kAccWarps][kAccSlots * 36];
+  __shared__ int32_t col_sh[kAccWarps][kAccSlots];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int32_t i = int32_t(blockIdx.x) * kAccWarps + wid;
+  if (i >= n) return;
+  const int32_t e0 = aprow[i], e1 = aprow[i + 1], len = e1 - e0;
+  const bool local = len <= kAccSlots;
+  double* acc = local ? acc_sh[wid] : apval + 36 * int64_t(e0);
+  const int32_t* cols = local ? col_sh[wid] : apcol + e0;
+  for (int32_t e = lane; e < len; e += 32) {
+    const int32_t c = scratch[soff[i] + e];
+    apcol[e0 + e] = c;
+    if (local) col_sh[wid][e] = c;
+  }
+  for (int32_t q = lane; q < 36 * len; q += 32) acc[q] = 0.0;
+  __syncwarp();
+  const int r0 = lane / 6, c0 = lane - 6 * (lane / 6);  // entry lane
+  const int r1 = (lane + 32) / 6, c1 = (lane + 32) - 6 * ((lane + 32) / 6);  // entry lane + 32 (lanes < 4)
+  for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+    const int32_t j = col[k];
+    const double* A = val + 36 * int64_t(k);
+    double a0[6], a1[6];
+    for (int q = 0; q < 6; ++q) {
+      a0[q] = A[r0 * 6 + q];
+      a1[q] = lane < 4 ? A[r1 * 6 + q] : 0.0;
+    }
+    for (int32_t e = prow[j]; e < prow[j + 1]; ++e) {
+      const int32_t cc = pcol[e];
+      int32_t lo = 0, hi = len - 1;
+      while (lo < hi) {
+        const int32_t mid = (lo + hi) >> 1;
+        if (cols[mid] < cc) lo = mid + 1;
+        else hi = mid;
+      }
+      const double* B = pval + 36 * int64_t(e);
+      double s0 = 0.0;
+      for (int q = 0; q < 6; ++q) s0 += a0[q] * B[q * 6 + c0];
+      double* C = acc + 36 * int64_t(lo);
+      C[lane] = C[lane] + s0;
+      if (lane < 4) {
+        double s1 = 0.0;
+        for (int q = 0; q < 6; ++q) s1 += a1[q] * B[q * 6 + c1];
+        C[lane + 32] = C[lane + 32] + s1;
+      }
+      __syncwarp();
+    }
+  }
+  if (local)
+    for (int32_t q = lane; q < 36 * len; q += 32) apval[36 * int64_t(e0) + q] = acc[q];
+}
+
+// The coarse rows in the same way (k_c_values_lanes' lanes over an A P row's entries), with the
+// coarse row accumulated in shared memory when it has at most kAccSlots blocks.
+__global__ void __launch_bounds__(32 * kAccWarps) k_c_values_acc(int32_t na, const int32_t* rrow, const int32_t* rent_i,
+                                                                 const int32_t* rent_e, const double* pval,
+                                                                 const int32_t* aprow, const int32_t* apcol,
+                                                                 const double* apval, const int32_t* crow,
+                                                                 const int32_t* scratch, const int64_t* soff,
+                                                                 int32_t* ccol, double* cval, double scale) {
+  __shared__ double acc_sh[kAccWarps][kAccSlots * 36];
+  __shared__ int32_t col_sh[kAccWarps][kAccSlots];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int32_t I = int32_t(blockIdx.x) * kAccWarps + wid;
+  if (I >= na) return;
+  const int32_t c0 = crow[I], c1 = crow[I + 1], len = c1 - c0;
+  const bool local = len <= kAccSlots;
+  double* acc = local ? acc_sh[wid] : cval + 36 * int64_t(c0);
+  const int32_t* cols = local ? col_sh[wid] : ccol + c0;
+  for (int32_t c = lane; c < len; c += 32) {
+    const int32_t v = scratch[soff[I] + c];
+    ccol[c0 + c] = v;
+    if (local) col_sh[wid][c] = v;
+  }
+  for (int32_t q = lane; q < 36 * len; q += 32) acc[q] = 0.0;
+  __syncwarp();
+  for (int32_t r = rrow[I]; r < rrow[I + 1]; ++r) {
+    const int32_t i = rent_i[r];
+    const double* Pi = pval + 36 * int64_t(rent_e[r]);
+    for (int32_t e = aprow[i] + lane; e < aprow[i + 1]; e += 32) {
+      const int32_t J = apcol[e];
+      int32_t slot;
+      if (J == I) {
+        slot = 0;
+      } else {
+        int32_t lo = 1, hi = len - 1;
+        while (lo < hi) {
+          const int32_t mid = (lo + hi) >> 1;
+          if (cols[mid] < J) lo = mid + 1;
+          else hi = mid;
+        }
+        slot = lo;
+      }
+      const double* B = apval + 36 * int64_t(e);
+      double* C = acc + 36 * int64_t(slot);
+      for (int ent = 0; ent < 36; ++ent) {
+        const int rr = ent / 6, cc = ent - 6 * (ent / 6);
+        double sacc = 0.0;
+        for (int q = 0; q < 6; ++q) sacc += Pi[q * 6 + rr] * B[q * 6 + cc];
+        C[ent] = C[ent] + sacc;
+      }
+    }
+    __syncwarp();
+  }
+  if (scale != 1.0)
+    for (int32_t q = lane; q < 36 * len; q += 32) acc[q] *= scale;
+  __syncwarp();
+  if (local)
+    for (int32_t q = lane; q < 36 * len; q += 32) cval[36 * int64_t(c0) + q] = acc[q];
+}
+
 // build work of P^T (A P): 6 |P row i| |AP row i|
 __global__ void k_work_rap(int32_t n, const int32_t* prow, const int32_t* aprow, unsigned long long* acc) {
   const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1163,8 +1285,9 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     apnnz_total = apnnz;
     TRY(apcol.alloc(size_t(apnnz)));
     TRY(apval.alloc(size_t(apnnz) * 36));
-    (k_ap_values<<<nblk(32 * int64_t(n), 128), 128, 0, st>>>(n, F.A.rowptr, F.A.col, F.A.val, F.prow, F.pcol, F.pval, aprow.p,
-                                              scratch.p, soff.p, apcol.p, apval.p), SVXG_COUNT_LAUNCH());
+    (k_ap_values_acc<<<unsigned((n + kAccWarps - 1) / kAccWarps), 32 * kAccWarps, 0, st>>>(
+         n, F.A.rowptr, F.A.col, F.A.val, F.prow, F.pcol, F.pval, aprow.p, scratch.p, soff.p, apcol.p, apval.p),
+     SVXG_COUNT_LAUNCH());
   }
   {
     Tmp<unsigned long long> acc(st);
@@ -1206,9 +1329,9 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     const double scale = (!smoothed && opt.coarse_scale != 1.0) ? opt.coarse_scale : 1.0;
     // (A P rows of 6 entries or more on average: the lanes over each row's entries)
     if (apnnz_total >= 6 * int64_t(n))
-      (k_c_values_lanes<<<nblk(32 * int64_t(na), 128), 128, 0, st>>>(na, F.rrow, F.rent_i, F.rent_e, F.pval, aprow.p,
-                                                                      apcol.p, apval.p, C.A.rowptr, scratch.p, soff.p,
-                                                                      C.A.col, C.A.val, scale),
+      (k_c_values_acc<<<unsigned((na + kAccWarps - 1) / kAccWarps), 32 * kAccWarps, 0, st>>>(
+           na, F.rrow, F.rent_i, F.rent_e, F.pval, aprow.p, apcol.p, apval.p, C.A.rowptr, scratch.p, soff.p, C.A.col,
+           C.A.val, scale),
        SVXG_COUNT_LAUNCH());
     else
       (k_c_values<<<nblk(32 * int64_t(na), 128), 128, 0, st>>>(na, F.rrow, F.rent_i, F.rent_e, F.pval, aprow.p, apcol.p,
