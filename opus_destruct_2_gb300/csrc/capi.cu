@@ -99,9 +99,12 @@ void release_solver(Problem& P) {
 }
 
 int upload_bond_flags(Problem& P, int32_t b) {
-  // (broken and in_k of one bond, host copy -> device)
-  SVXG_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(P.d_bonds + b) + offsetof(svxg_bond, broken),
-                            &P.h_bonds[size_t(b)].broken, 2, cudaMemcpyHostToDevice, P.stream));
+  // (broken and in_k of one bond -> the device record; synchronous: the bytes are on the stack)
+  const uint8_t flags[2] = {P.h_broken[size_t(b)], P.h_in_k[size_t(b)]};
+  static_assert(offsetof(svxg_bond, in_k) == offsetof(svxg_bond, broken) + 1, "flag bytes adjacent");
+  SVXG_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(P.d_bonds + b) + offsetof(svxg_bond, broken), flags, 2,
+                            cudaMemcpyHostToDevice, P.stream));
+  SVXG_CUDA(host_wait(P.stream));
   return SVXG_OK;
 }
 
@@ -326,7 +329,15 @@ static int upload_graph(Problem& P, const svxg_node* nodes, int32_t n, const svx
   P.n = n;
   P.nb = nb;
   P.h_nodes.assign(nodes, nodes + n);
-  P.h_bonds.assign(bonds, bonds + nb);
+  P.h_bond_ab.resize(2 * size_t(nb));
+  P.h_broken.resize(size_t(nb));
+  P.h_in_k.resize(size_t(nb));
+  for (int32_t k = 0; k < nb; ++k) {
+    P.h_bond_ab[2 * size_t(k)] = bonds[k].a;
+    P.h_bond_ab[2 * size_t(k) + 1] = bonds[k].b;
+    P.h_broken[size_t(k)] = bonds[k].broken;
+    P.h_in_k[size_t(k)] = bonds[k].in_k;
+  }
   P.h_mats.assign(mats, mats + SVXG_MAX_MATERIALS);
   TRY(P.mem.alloc(&P.d_nodes, size_t(n)));
   TRY(P.mem.alloc(&P.d_bonds, size_t(nb)));
@@ -371,8 +382,7 @@ static int assemble_impl(Problem& P, const svxg_stress_options* opt, int32_t* ok
   TRY(assemble_matrix(P));
   trace_mark(P, "K assembled");
   P.assembly_work = 0;
-  for (const svxg_bond& b : P.h_bonds)
-    if (b.in_k) P.assembly_work += 48;
+  P.assembly_work = 48 * int64_t(std::count(P.h_in_k.begin(), P.h_in_k.end(), uint8_t(1)));
   P.jacobi_only = P.nfree < P.opt.amg_min_nodes;
   if (P.jacobi_only) {
     TRY(build_jacobi(P));
@@ -484,7 +494,7 @@ int svxg_release(svxg_problem* p) {
   DeviceScope ds(p->P.device);
   host_wait(p->P.stream);
   release_solver(p->P);
-  for (svxg_bond& b : p->P.h_bonds) b.in_k = 0;
+  std::fill(p->P.h_in_k.begin(), p->P.h_in_k.end(), uint8_t(0));
   return SVXG_OK;
 }
 
@@ -496,14 +506,13 @@ int svxg_remove_bond(svxg_problem* p, int32_t b) {
     return SVXG_ERR_ARG;
   }
   DeviceScope ds(P.device);
-  svxg_bond& hb = P.h_bonds[size_t(b)];
-  hb.broken = 1;
-  if (!P.assembled || !hb.in_k) {
+  P.h_broken[size_t(b)] = 1;
+  if (!P.assembled || !P.h_in_k[size_t(b)]) {
     TRY(upload_bond_flags(P, b));
     SVXG_CUDA(host_wait(P.stream));
     return SVXG_OK;
   }
-  hb.in_k = 0;
+  P.h_in_k[size_t(b)] = 0;
   TRY(remove_bonds_device(P, &b, 1));
   if (!P.jacobi_only) P.pc_current = false;
   P.active = false;
@@ -530,11 +539,11 @@ int svxg_retire_nodes(svxg_problem* p, const int32_t* list, int32_t count) {
   }
   std::vector<int32_t> rm;
   for (int32_t b = 0; b < P.nb; ++b) {
-    svxg_bond& B = P.h_bonds[size_t(b)];
-    if (!(now[size_t(B.a)] || (B.b >= 0 && now[size_t(B.b)]))) continue;
-    B.broken = 1;
-    if (P.assembled && B.in_k) {
-      B.in_k = 0;
+    const int32_t ba = P.h_bond_ab[2 * size_t(b)], bb = P.h_bond_ab[2 * size_t(b) + 1];
+    if (!(now[size_t(ba)] || (bb >= 0 && now[size_t(bb)]))) continue;
+    P.h_broken[size_t(b)] = 1;
+    if (P.assembled && P.h_in_k[size_t(b)]) {
+      P.h_in_k[size_t(b)] = 0;
       rm.push_back(b);
       if (!P.jacobi_only) P.pc_current = false;
     } else {
@@ -561,8 +570,8 @@ int svxg_retire_nodes(svxg_problem* p, const int32_t* list, int32_t count) {
 int svxg_bond_flags(svxg_problem* p, uint8_t* broken, uint8_t* in_k) {
   CHECK_P(p);
   for (int32_t k = 0; k < p->P.nb; ++k) {
-    if (broken) broken[k] = p->P.h_bonds[size_t(k)].broken;
-    if (in_k) in_k[k] = p->P.h_bonds[size_t(k)].in_k;
+    if (broken) broken[k] = p->P.h_broken[size_t(k)];
+    if (in_k) in_k[k] = p->P.h_in_k[size_t(k)];
   }
   return SVXG_OK;
 }

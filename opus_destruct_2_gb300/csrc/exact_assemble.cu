@@ -337,6 +337,7 @@ int assemble_matrix(Problem& P) {
   TRY(exclusive_scan_i32(P, flags.p, scan.p, n, &nfree));
   if (n > 0) (k_dof<<<blocks_for(n), kT, 0, st>>>(n, P.d_nodes, scan.p, P.d_dof, node_of_dof.p), SVXG_COUNT_LAUNCH());
   P.nfree = nfree;
+  trace_mark(P, "assemble: DOF numbering");
   // 2. incidences
   P.mem.release(P.d_in_k);
   TRY(P.mem.alloc(&P.d_in_k, size_t(nb)));
@@ -354,6 +355,7 @@ int assemble_matrix(Problem& P) {
   TRY(by_nbr.alloc(size_t(ninc)));
   TRY(by_bond.alloc(size_t(ninc)));
   if (nb > 0) (k_fill<<<blocks_for(nb), kT, 0, st>>>(nb, P.d_bonds, P.d_dof, P.d_in_k, off.p, cursor.p, by_nbr.p), SVXG_COUNT_LAUNCH());
+  trace_mark(P, "assemble: incidences");
   // 3. pattern
   Tmp<int32_t> rowlen(st);
   TRY(rowlen.alloc(size_t(nfree) + 1));
@@ -376,11 +378,13 @@ int assemble_matrix(Problem& P) {
   if (nfree > 0)
     (k_columns<<<blocks_for(nfree), kT, 0, st>>>(nfree, node_of_dof.p, off.p, by_nbr.p, P.K.rowptr, P.K.col, cstart.p,
                                                 ccount.p), SVXG_COUNT_LAUNCH());
+  trace_mark(P, "assemble: pattern");
   // 4. values
   if (nnzb > 0)
     (k_block_values<<<blocks_for(nnzb, 128), 128, 0, st>>>(nnzb, nfree, P.K.rowptr, P.K.col, node_of_dof.p, cstart.p,
                                                           ccount.p, by_nbr.p, by_bond.p, P.d_bonds, P.d_nodes,
                                                           P.d_mats, P.K.val), SVXG_COUNT_LAUNCH());
+  trace_mark(P, "assemble: block values");
   // 5. id_scale and identity rows
   Tmp<double> term(st), ids(st);
   Tmp<uint8_t> ident(st);
@@ -399,10 +403,9 @@ int assemble_matrix(Problem& P) {
   SVXG_CUDA(cudaMemcpyAsync(&P.id_scale, ids.p, sizeof(double), cudaMemcpyDeviceToHost, st));
   P.h_dof.resize(size_t(n));
   if (n > 0) SVXG_CUDA(cudaMemcpyAsync(P.h_dof.data(), P.d_dof, sizeof(int32_t) * size_t(n), cudaMemcpyDeviceToHost, st));
-  std::vector<uint8_t> ik(static_cast<size_t>(nb));
-  if (nb > 0) SVXG_CUDA(cudaMemcpyAsync(ik.data(), P.d_in_k, size_t(nb), cudaMemcpyDeviceToHost, st));
+  P.h_in_k.resize(static_cast<size_t>(nb));
+  if (nb > 0) SVXG_CUDA(cudaMemcpyAsync(P.h_in_k.data(), P.d_in_k, size_t(nb), cudaMemcpyDeviceToHost, st));
   SVXG_CUDA(host_wait(st));
-  for (int32_t k = 0; k < nb; ++k) P.h_bonds[size_t(k)].in_k = ik[size_t(k)];
   return SVXG_OK;
 }
 

@@ -23,6 +23,7 @@ namespace exact {
 
 constexpr int kThreads = 1024;
 constexpr int kItems = 8;
+constexpr int kQuietRounds = 4;  // warp rounds without a crossing before block rounds resume
 constexpr int64_t kCap = int64_t(1) << 54;  // saturation: past any binade's room
 
 struct Pair {
@@ -147,15 +148,18 @@ __device__ inline double sequential_sum_from(double s0, int64_t a, int64_t n, Te
   __shared__ double s_sh;
   __shared__ int64_t p_sh;
   __shared__ int64_t first_sh;
+  __shared__ int quiet_sh;  // warp rounds in a row without a crossing
   if (threadIdx.x == 0) {
     s_sh = s0;
     p_sh = a;
+    quiet_sh = 0;
   }
   __syncthreads();
   constexpr int64_t kTile = int64_t(kThreads) * kItems;
   while (true) {
     const int64_t p = p_sh;
     const double s = s_sh;
+    const bool warp_round = quiet_sh < kQuietRounds;
     __syncthreads();
     if (p >= n) break;
     const uint64_t sbits = uint64_t(__double_as_longlong(s));
@@ -199,6 +203,40 @@ __device__ inline double sequential_sum_from(double s0, int64_t a, int64_t n, Te
     int64_t S;
     int uexp;
     split(s, &S, &uexp);
+    if (warp_round) {
+      // While crossings come close together (a small running sum: the start, after a crossing),
+      // one warp takes 32 terms a round, which costs far less than a block round.
+      if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        const int64_t k = p + lane;
+        const double t = k < n ? term(k) : 0.0;
+        const Pair pr = k < n ? term_pair(t, uexp) : Pair{0, 0};
+        const Pair incl = warp_scan(pr);
+        Pair ex = shfl_up_pair(incl, 1);
+        if (lane == 0) ex = Pair{0, 0};
+        const int64_t run = sat(S, pick(ex, S));
+        const bool cross = k < n && sat(run, pick(pr, run)) >= (int64_t(1) << 53);
+        const unsigned m = __ballot_sync(0xffffffffu, cross);
+        if (m == 0) {
+          Pair tot;
+          tot.d0 = __shfl_sync(0xffffffffu, incl.d0, 31);
+          tot.d1 = __shfl_sync(0xffffffffu, incl.d1, 31);
+          if (lane == 0) {
+            s_sh = join(sat(S, pick(tot, S)), uexp);
+            p_sh = p + 32 < n ? p + 32 : n;
+            quiet_sh = quiet_sh + 1;
+          }
+        } else {
+          if (lane == __ffs(m) - 1) {
+            s_sh = __dadd_rn(join(run, uexp), t);
+            p_sh = k + 1;
+          }
+          if (lane == 0) quiet_sh = 0;
+        }
+      }
+      __syncthreads();
+      continue;
+    }
     // this thread's kItems consecutive terms
     const int64_t base = p + int64_t(threadIdx.x) * kItems;
     Pair loc[kItems];
@@ -243,6 +281,7 @@ __device__ inline double sequential_sum_from(double s0, int64_t a, int64_t n, Te
         const double before = join(run, uexp);
         s_sh = __dadd_rn(before, term(firstx));
         p_sh = firstx + 1;
+        quiet_sh = 0;  // (crossings come in runs: warp rounds until it is quiet again)
       }
     }
     __syncthreads();

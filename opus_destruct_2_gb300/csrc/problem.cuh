@@ -150,7 +150,10 @@ struct Problem {
   // graph (host copy kept for the in-place updates' bookkeeping)
   int32_t n = 0, nb = 0;
   std::vector<svxg_node> h_nodes;
-  std::vector<svxg_bond> h_bonds;
+  // per bond: its nodes (a, b) and its flags as the problem keeps them (the 216-byte records
+  // themselves live on the device only: a host pass over them costs milliseconds on large graphs)
+  std::vector<int32_t> h_bond_ab;
+  std::vector<uint8_t> h_broken, h_in_k;
   std::vector<svxg_material> h_mats;
   svxg_node* d_nodes = nullptr;
   svxg_bond* d_bonds = nullptr;
