@@ -1,13 +1,15 @@
-// dense.cu - the coarsest level's dense factor and its inverse, tiled over many SMs.
+// dense.cu - the coarsest level's dense factor and its inverse, spread over many SMs.
 //
 // Restates factor_coarsest (core/src/solve/amg.cpp:535-578): the coarsest operator (m x m, m =
 // 6 n_c <= 1152) is symmetrized, factored as L L^T with the pivot floor max(1e-12 dmax, 1e-300),
-// and the cycle's coarsest solve (amg.cpp:580-592) applies L^-T L^-1. Here the factor is a
-// right-looking blocked Cholesky on 32 x 32 tiles (per step: the diagonal tile in one CTA, the
-// panel and the trailing update one CTA per tile), and L^-1 is built by tile diagonals
-// (X_ij = -L_ii^-1 sum_k L_ik X_kj, all tiles of one diagonal at once); the cycle then needs two
-// dense products instead of two sequential substitutions. FP64 throughout. The matrix is padded
-// to a multiple of 32 with identity rows, which leaves the factor of the m x m block unchanged.
+// and the cycle's coarsest solve (amg.cpp:580-592) applies L^-T L^-1. The factor is a right-looking
+// blocked Cholesky on 16 x 16 tiles (per step: the diagonal tile in one CTA, the panel and the
+// trailing update one CTA per tile - small tiles, because an SM retires about one FP64 operation
+// a cycle, so a tile's product is the step's critical path); L^-1 is then formed column by column,
+// one warp per column (forward substitution on the identity, each step's dot product across the
+// lanes), all columns at once. The cycle applies two dense products instead of two sequential
+// substitutions. FP64 throughout. The matrix is padded to a multiple of 16 with identity rows,
+// which leaves the factor of the m x m block unchanged.
 #include <cmath>
 
 #include "problem.cuh"
@@ -15,8 +17,10 @@
 namespace svxg {
 namespace {
 
-constexpr int TB = 32;    // tile side
-constexpr int kDT = 256;  // threads per tile CTA: row t / 8, columns 4 (t % 8) .. + 3
+constexpr int TB = 16;    // tile side
+constexpr int kDT = 256;  // threads per tile CTA: entry (t / 16, t % 16)
+constexpr int kMaxM = 1152;
+constexpr int kInvWarps = 4;
 
 inline unsigned gblk(int64_t n, int t) { return unsigned((std::max<int64_t>(n, 1) + t - 1) / t); }
 
@@ -50,18 +54,8 @@ __global__ void k_dense_dmax(int32_t m, const double* __restrict__ C, double* dm
 
 __device__ __forceinline__ void load_tile(double (*S)[TB + 1], const double* __restrict__ D, int32_t mp, int32_t ti,
                                           int32_t tj) {
-  for (int e = threadIdx.x; e < TB * TB; e += kDT) {
-    const int r = e / TB, c = e % TB;
-    S[r][c] = D[int64_t(ti * TB + r) * mp + tj * TB + c];
-  }
-}
-
-__device__ __forceinline__ void store_tile(double* __restrict__ D, int32_t mp, int32_t ti, int32_t tj,
-                                           double (*S)[TB + 1]) {
-  for (int e = threadIdx.x; e < TB * TB; e += kDT) {
-    const int r = e / TB, c = e % TB;
-    D[int64_t(ti * TB + r) * mp + tj * TB + c] = S[r][c];
-  }
+  const int r = threadIdx.x / TB, c = threadIdx.x % TB;
+  S[r][c] = D[int64_t(ti * TB + r) * mp + tj * TB + c];
 }
 
 // step k, diagonal tile: L_kk (into D) and L_kk^-1 (into W + k * TB * TB, row-major, zero above)
@@ -69,12 +63,12 @@ __global__ void __launch_bounds__(kDT) k_potrf(int32_t k, int32_t mp, double* D,
   __shared__ double A[TB][TB + 1], X[TB][TB + 1];
   load_tile(A, D, mp, k, k);
   __syncthreads();
-  const double floor_v = fmax(1e-12 * *dmax_p, 1e-300);
+  const double dm = *dmax_p;
   for (int j = 0; j < TB; ++j) {
     if (threadIdx.x == 0) {
       double d = A[j][j];
       for (int q = 0; q < j; ++q) d -= A[j][q] * A[j][q];
-      if (!(d > 1e-12 * *dmax_p)) d = floor_v;
+      if (!(d > 1e-12 * dm)) d = fmax(1e-12 * dm, 1e-300);
       A[j][j] = sqrt(d);
     }
     __syncthreads();
@@ -86,9 +80,8 @@ __global__ void __launch_bounds__(kDT) k_potrf(int32_t k, int32_t mp, double* D,
     }
     __syncthreads();
   }
-  // zero above the diagonal, then the inverse column by column (forward substitution)
-  for (int e = threadIdx.x; e < TB * TB; e += kDT) {
-    const int r = e / TB, c = e % TB;
+  {
+    const int r = threadIdx.x / TB, c = threadIdx.x % TB;
     if (c > r) A[r][c] = 0.0;
     X[r][c] = 0.0;
   }
@@ -103,9 +96,9 @@ __global__ void __launch_bounds__(kDT) k_potrf(int32_t k, int32_t mp, double* D,
     }
   }
   __syncthreads();
-  store_tile(D, mp, k, k, A);
-  double* Wk = W + int64_t(k) * TB * TB;
-  for (int e = threadIdx.x; e < TB * TB; e += kDT) Wk[e] = X[e / TB][e % TB];
+  const int r = threadIdx.x / TB, c = threadIdx.x % TB;
+  D[int64_t(k * TB + r) * mp + k * TB + c] = A[r][c];
+  W[int64_t(k) * TB * TB + threadIdx.x] = X[r][c];
 }
 
 // step k, panel: L_ik = A_ik L_kk^-T for i = k + 1 + blockIdx.x
@@ -113,17 +106,12 @@ __global__ void __launch_bounds__(kDT) k_trsm(int32_t k, int32_t mp, double* D, 
   __shared__ double A[TB][TB + 1], X[TB][TB + 1];
   const int32_t i = k + 1 + int32_t(blockIdx.x);
   load_tile(A, D, mp, i, k);
-  const double* Wk = W + int64_t(k) * TB * TB;
-  for (int e = threadIdx.x; e < TB * TB; e += kDT) X[e / TB][e % TB] = Wk[e];
+  const int r = threadIdx.x / TB, c = threadIdx.x % TB;
+  X[r][c] = W[int64_t(k) * TB * TB + threadIdx.x];
   __syncthreads();
-  const int r = threadIdx.x / 8, c0 = 4 * (threadIdx.x % 8);
-  double out[4];
-  for (int u = 0; u < 4; ++u) {
-    double s = 0.0;
-    for (int q = 0; q < TB; ++q) s += A[r][q] * X[c0 + u][q];
-    out[u] = s;
-  }
-  for (int u = 0; u < 4; ++u) D[int64_t(i * TB + r) * mp + k * TB + c0 + u] = out[u];
+  double s = 0.0;
+  for (int q = 0; q < TB; ++q) s += A[r][q] * X[c][q];
+  D[int64_t(i * TB + r) * mp + k * TB + c] = s;
 }
 
 // step k, trailing update: D_ij -= L_ik L_jk^T over the tiles k < j <= i (one CTA each)
@@ -138,74 +126,68 @@ __global__ void __launch_bounds__(kDT) k_syrk(int32_t k, int32_t mp, double* D) 
   load_tile(A, D, mp, i, k);
   load_tile(B, D, mp, j, k);
   __syncthreads();
-  const int r = threadIdx.x / 8, c0 = 4 * (threadIdx.x % 8);
-  for (int u = 0; u < 4; ++u) {
+  const int r = threadIdx.x / TB, c = threadIdx.x % TB;
+  double s = 0.0;
+  for (int q = 0; q < TB; ++q) s += A[r][q] * B[c][q];
+  D[int64_t(i * TB + r) * mp + j * TB + c] -= s;
+}
+
+// L^-1 column j (one warp): x_j = 1 / L_jj, x_i = -(sum_{j<=q<i} L_iq x_q) / L_ii; written to
+// cinv (L^-1, row-major m x m) and its transpose after it
+__global__ void __launch_bounds__(32 * kInvWarps) k_inv_cols(int32_t m, int32_t mp, const double* __restrict__ D,
+                                                             double* cinv) {
+  __shared__ double x_sh[kInvWarps][kMaxM];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int32_t j = int32_t(blockIdx.x) * kInvWarps + w;
+  if (j >= m) return;
+  double* x = x_sh[w];
+  double* X = cinv;
+  double* XT = cinv + int64_t(m) * m;
+  for (int32_t i = lane; i < j; i += 32) {
+    X[int64_t(i) * m + j] = 0.0;
+    XT[int64_t(j) * m + i] = 0.0;
+  }
+  if (lane == 0) x[j] = 1.0 / D[int64_t(j) * mp + j];
+  __syncwarp();
+  for (int32_t i = j + 1; i < m; ++i) {
+    const double* Li = D + int64_t(i) * mp;
     double s = 0.0;
-    for (int q = 0; q < TB; ++q) s += A[r][q] * B[c0 + u][q];
-    D[int64_t(i * TB + r) * mp + j * TB + c0 + u] -= s;
+    for (int32_t q = j + lane; q < i; q += 32) s += Li[q] * x[q];
+    for (int d = 16; d > 0; d >>= 1) s += __shfl_xor_sync(0xffffffffu, s, d);
+    if (lane == 0) x[i] = -s / Li[i];
+    __syncwarp();
+  }
+  for (int32_t i = j + lane; i < m; i += 32) {
+    X[int64_t(i) * m + j] = x[i];
+    XT[int64_t(j) * m + i] = x[i];
   }
 }
 
-// X_jj = L_jj^-1 (all diagonal tiles)
-__global__ void __launch_bounds__(kDT) k_inv_diag(int32_t mp, const double* __restrict__ W, double* X) {
-  const int32_t j = blockIdx.x;
-  const double* Wj = W + int64_t(j) * TB * TB;
-  for (int e = threadIdx.x; e < TB * TB; e += kDT) X[int64_t(j * TB + e / TB) * mp + j * TB + e % TB] = Wj[e];
-}
-
-// diagonal d of X = L^-1: X_ij = -L_ii^-1 sum_{k=j}^{i-1} L_ik X_kj, i = j + d, j = blockIdx.x
-__global__ void __launch_bounds__(kDT) k_inv_step(int32_t d, int32_t mp, const double* __restrict__ D,
-                                                  const double* __restrict__ W, double* X) {
-  __shared__ double A[TB][TB + 1], B[TB][TB + 1];
-  const int32_t j = blockIdx.x, i = j + d;
-  const int r = threadIdx.x / 8, c0 = 4 * (threadIdx.x % 8);
-  double s[4] = {0.0, 0.0, 0.0, 0.0};
-  for (int32_t k = j; k < i; ++k) {
-    load_tile(A, D, mp, i, k);
-    load_tile(B, X, mp, k, j);
-    __syncthreads();
-    for (int u = 0; u < 4; ++u)
-      for (int q = 0; q < TB; ++q) s[u] += A[r][q] * B[q][c0 + u];
-    __syncthreads();
-  }
-  // B = S, A = L_ii^-1; X_ij = -A B
-  for (int u = 0; u < 4; ++u) B[r][c0 + u] = s[u];
-  const double* Wi = W + int64_t(i) * TB * TB;
-  for (int e = threadIdx.x; e < TB * TB; e += kDT) A[e / TB][e % TB] = Wi[e];
-  __syncthreads();
-  for (int u = 0; u < 4; ++u) {
-    double v = 0.0;
-    for (int q = 0; q < TB; ++q) v += A[r][q] * B[q][c0 + u];
-    X[int64_t(i * TB + r) * mp + j * TB + c0 + u] = -v;
-  }
-}
-
-// the m x m results: chol = L below and on the diagonal, L^T above; cinv = X, then X^T
-__global__ void k_dense_unpad(int32_t m, int32_t mp, const double* __restrict__ D, const double* __restrict__ X,
-                              double* chol, double* cinv) {
+// chol = L below and on the diagonal, L^T above (m x m)
+__global__ void k_dense_unpad(int32_t m, int32_t mp, const double* __restrict__ D, double* chol) {
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (t >= int64_t(m) * m) return;
   const int32_t i = int32_t(t / m), j = int32_t(t % m);
   chol[t] = i >= j ? D[int64_t(i) * mp + j] : D[int64_t(j) * mp + i];
-  const double x = i >= j ? X[int64_t(i) * mp + j] : 0.0;
-  cinv[t] = x;
-  cinv[int64_t(m) * m + int64_t(j) * m + i] = x;
 }
 
 }  // namespace
 
-// C (m x m, row-major, the coarsest operator as filled) -> P.d_chol (L with L^T mirrored above) and
-// P.d_cinv (L^-1, then L^-T) - both m x m, allocated by the caller
+// C (m x m, row-major, the coarsest operator as filled) -> chol (L with L^T mirrored above) and
+// cinv (L^-1, then L^-T) - both m x m, allocated by the caller; chol may alias C
 int dense_factor_inverse(Problem& P, int32_t m, const double* C, double* chol, double* cinv) {
   if (m <= 0) return SVXG_OK;
+  if (m > kMaxM) {
+    set_error("coarsest factor: more than 1152 unknowns");
+    return SVXG_ERR_ARG;
+  }
   cudaStream_t st = P.stream;
   const int32_t T = (m + TB - 1) / TB, mp = T * TB;
-  double *D = nullptr, *X = nullptr, *W = nullptr, *dmax = nullptr;
+  double *D = nullptr, *W = nullptr, *dmax = nullptr;
   const size_t dd = size_t(mp) * size_t(mp);
   SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&D), dd * sizeof(double), st));
   int e = SVXG_OK;
-  if (pool_malloc_async(reinterpret_cast<void**>(&X), dd * sizeof(double), st) != cudaSuccess ||
-      pool_malloc_async(reinterpret_cast<void**>(&W), size_t(T) * TB * TB * sizeof(double), st) != cudaSuccess ||
+  if (pool_malloc_async(reinterpret_cast<void**>(&W), size_t(T) * TB * TB * sizeof(double), st) != cudaSuccess ||
       pool_malloc_async(reinterpret_cast<void**>(&dmax), sizeof(double), st) != cudaSuccess) {
     cudaGetLastError();
     set_error("coarsest factor: device allocation failed");
@@ -222,16 +204,15 @@ int dense_factor_inverse(Problem& P, int32_t m, const double* C, double* chol, d
         (k_syrk<<<unsigned(int64_t(rest) * (rest + 1) / 2), kDT, 0, st>>>(k, mp, D), SVXG_COUNT_LAUNCH());
       }
     }
-    if (cudaMemsetAsync(X, 0, dd * sizeof(double), st) != cudaSuccess) e = SVXG_ERR_CUDA;
-    (k_inv_diag<<<unsigned(T), kDT, 0, st>>>(mp, W, X), SVXG_COUNT_LAUNCH());
-    for (int32_t d = 1; d < T; ++d) (k_inv_step<<<unsigned(T - d), kDT, 0, st>>>(d, mp, D, W, X), SVXG_COUNT_LAUNCH());
-    (k_dense_unpad<<<gblk(int64_t(m) * m, 256), 256, 0, st>>>(m, mp, D, X, chol, cinv), SVXG_COUNT_LAUNCH());
+    (k_inv_cols<<<unsigned((m + kInvWarps - 1) / kInvWarps), 32 * kInvWarps, 0, st>>>(m, mp, D, cinv),
+     SVXG_COUNT_LAUNCH());
+    (k_dense_unpad<<<gblk(int64_t(m) * m, 256), 256, 0, st>>>(m, mp, D, chol), SVXG_COUNT_LAUNCH());
     if (cudaGetLastError() != cudaSuccess) {
       set_error("coarsest factor: kernel launch failed");
       e = SVXG_ERR_CUDA;
     }
   }
-  for (void* q : {static_cast<void*>(D), static_cast<void*>(X), static_cast<void*>(W), static_cast<void*>(dmax)})
+  for (void* q : {static_cast<void*>(D), static_cast<void*>(W), static_cast<void*>(dmax)})
     if (q) cudaFreeAsync(q, st);
   return e;
 }

@@ -1207,6 +1207,7 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
   if (smoothed) {
     double lm = 0.0;
     TRY(estimate_lmax(P, F, &lm));
+    trace_mark(P, "coarsen: lmax");
     F.lmax = lm;
     omega = (4.0 / 3.0) / maxd(1e-300, lm);
   }

@@ -172,6 +172,8 @@ int build_appended(Problem& P) {
   if (!e) e = S->mem.alloc(&len, size_t(na) + 1);
   int32_t snnz = 0;
   if (!e) {
+    // (len[na] = 0: the scan's total is then the block count)
+    if (cudaMemsetAsync(len, 0, sizeof(int32_t) * (size_t(na) + 1), st) != cudaSuccess) e = SVXG_ERR_CUDA;
     (k_sub_count<<<nblk(na), kT, 0, st>>>(na, P.pc_n, P.K.rowptr, P.K.col, len), SVXG_COUNT_LAUNCH());
     e = exclusive_scan_i32(P, len, S->K.rowptr, int64_t(na) + 1, &snnz);
   }
