@@ -61,6 +61,7 @@ __device__ __forceinline__ void load_tile(double (*S)[TB + 1], const double* __r
 // step k, diagonal tile: L_kk (into D) and L_kk^-1 (into W + k * TB * TB, row-major, zero above)
 __global__ void __launch_bounds__(kDT) k_potrf(int32_t k, int32_t mp, double* D, double* W, const double* dmax_p) {
   __shared__ double A[TB][TB + 1], X[TB][TB + 1];
+  __shared__ double rdiag[TB];  // 1 / L_jj (one division a column; an FP64 division is many operations)
   load_tile(A, D, mp, k, k);
   __syncthreads();
   const double dm = *dmax_p;
@@ -70,29 +71,29 @@ __global__ void __launch_bounds__(kDT) k_potrf(int32_t k, int32_t mp, double* D,
       for (int q = 0; q < j; ++q) d -= A[j][q] * A[j][q];
       if (!(d > 1e-12 * dm)) d = fmax(1e-12 * dm, 1e-300);
       A[j][j] = sqrt(d);
+      rdiag[j] = 1.0 / A[j][j];
     }
     __syncthreads();
     const int i = j + 1 + int(threadIdx.x);
     if (i < TB) {
       double v = A[i][j];
       for (int q = 0; q < j; ++q) v -= A[i][q] * A[j][q];
-      A[i][j] = v / A[j][j];
+      A[i][j] = v * rdiag[j];
     }
     __syncthreads();
   }
   {
     const int r = threadIdx.x / TB, c = threadIdx.x % TB;
     if (c > r) A[r][c] = 0.0;
-    X[r][c] = 0.0;
+    X[r][c] = r == c ? rdiag[r] : 0.0;
   }
   __syncthreads();
   if (threadIdx.x < TB) {
     const int c = threadIdx.x;
-    X[c][c] = 1.0 / A[c][c];
     for (int i = c + 1; i < TB; ++i) {
       double s = 0.0;
       for (int q = c; q < i; ++q) s += A[i][q] * X[q][c];
-      X[i][c] = -s / A[i][i];
+      X[i][c] = -s * rdiag[i];
     }
   }
   __syncthreads();
@@ -132,10 +133,17 @@ __global__ void __launch_bounds__(kDT) k_syrk(int32_t k, int32_t mp, double* D) 
   D[int64_t(i * TB + r) * mp + j * TB + c] -= s;
 }
 
+// rd = 1 / L_ii
+__global__ void k_rdiag(int32_t m, int32_t mp, const double* __restrict__ D, double* rd) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) rd[i] = 1.0 / D[int64_t(i) * mp + i];
+}
+
 // L^-1 column j (one warp): x_j = 1 / L_jj, x_i = -(sum_{j<=q<i} L_iq x_q) / L_ii; written to
 // cinv (L^-1, row-major m x m) and its transpose after it
+
 __global__ void __launch_bounds__(32 * kInvWarps) k_inv_cols(int32_t m, int32_t mp, const double* __restrict__ D,
-                                                             double* cinv) {
+                                                             const double* __restrict__ rd, double* cinv) {
   __shared__ double x_sh[kInvWarps][kMaxM];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int32_t j = int32_t(blockIdx.x) * kInvWarps + w;
@@ -147,14 +155,14 @@ __global__ void __launch_bounds__(32 * kInvWarps) k_inv_cols(int32_t m, int32_t 
     X[int64_t(i) * m + j] = 0.0;
     XT[int64_t(j) * m + i] = 0.0;
   }
-  if (lane == 0) x[j] = 1.0 / D[int64_t(j) * mp + j];
+  if (lane == 0) x[j] = rd[j];
   __syncwarp();
   for (int32_t i = j + 1; i < m; ++i) {
     const double* Li = D + int64_t(i) * mp;
     double s = 0.0;
     for (int32_t q = j + lane; q < i; q += 32) s += Li[q] * x[q];
     for (int d = 16; d > 0; d >>= 1) s += __shfl_xor_sync(0xffffffffu, s, d);
-    if (lane == 0) x[i] = -s / Li[i];
+    if (lane == 0) x[i] = -s * rd[i];
     __syncwarp();
   }
   for (int32_t i = j + lane; i < m; i += 32) {
@@ -183,12 +191,13 @@ int dense_factor_inverse(Problem& P, int32_t m, const double* C, double* chol, d
   }
   cudaStream_t st = P.stream;
   const int32_t T = (m + TB - 1) / TB, mp = T * TB;
-  double *D = nullptr, *W = nullptr, *dmax = nullptr;
+  double *D = nullptr, *W = nullptr, *dmax = nullptr, *rd = nullptr;
   const size_t dd = size_t(mp) * size_t(mp);
   SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&D), dd * sizeof(double), st));
   int e = SVXG_OK;
   if (pool_malloc_async(reinterpret_cast<void**>(&W), size_t(T) * TB * TB * sizeof(double), st) != cudaSuccess ||
-      pool_malloc_async(reinterpret_cast<void**>(&dmax), sizeof(double), st) != cudaSuccess) {
+      pool_malloc_async(reinterpret_cast<void**>(&dmax), sizeof(double), st) != cudaSuccess ||
+      pool_malloc_async(reinterpret_cast<void**>(&rd), size_t(m) * sizeof(double), st) != cudaSuccess) {
     cudaGetLastError();
     set_error("coarsest factor: device allocation failed");
     e = SVXG_ERR_NOMEM;
@@ -204,7 +213,8 @@ int dense_factor_inverse(Problem& P, int32_t m, const double* C, double* chol, d
         (k_syrk<<<unsigned(int64_t(rest) * (rest + 1) / 2), kDT, 0, st>>>(k, mp, D), SVXG_COUNT_LAUNCH());
       }
     }
-    (k_inv_cols<<<unsigned((m + kInvWarps - 1) / kInvWarps), 32 * kInvWarps, 0, st>>>(m, mp, D, cinv),
+    (k_rdiag<<<gblk(m, 256), 256, 0, st>>>(m, mp, D, rd), SVXG_COUNT_LAUNCH());
+    (k_inv_cols<<<unsigned((m + kInvWarps - 1) / kInvWarps), 32 * kInvWarps, 0, st>>>(m, mp, D, rd, cinv),
      SVXG_COUNT_LAUNCH());
     (k_dense_unpad<<<gblk(int64_t(m) * m, 256), 256, 0, st>>>(m, mp, D, chol), SVXG_COUNT_LAUNCH());
     if (cudaGetLastError() != cudaSuccess) {
@@ -212,7 +222,7 @@ int dense_factor_inverse(Problem& P, int32_t m, const double* C, double* chol, d
       e = SVXG_ERR_CUDA;
     }
   }
-  for (void* q : {static_cast<void*>(D), static_cast<void*>(W), static_cast<void*>(dmax)})
+  for (void* q : {static_cast<void*>(D), static_cast<void*>(W), static_cast<void*>(dmax), static_cast<void*>(rd)})
     if (q) cudaFreeAsync(q, st);
   return e;
 }

@@ -91,10 +91,11 @@ __device__ __forceinline__ double spmv_exact_entry(int64_t t, const int32_t* row
 // nv = sqrt(sum of v_k^2 in index order): the sequential sum's exact bits, computed in parallel
 // (exact_sum.cuh).
 __global__ void __launch_bounds__(exact::kThreads) k_seq_norm(int64_t m, const double* v, double* out) {
-  const double s = exact::sequential_sum(m, [v](int64_t k) {
+  const auto sq = [v](int64_t k) {
     const double x = v[k];
     return x * x;
-  });
+  };
+  const double s = blockDim.x == 32 ? exact::warp_sequential_sum_from(0.0, 0, m, sq) : exact::sequential_sum(m, sq);
   if (threadIdx.x == 0) out[0] = sqrt(s);
 }
 
@@ -122,15 +123,16 @@ __global__ void __launch_bounds__(6 * kApplyNodes) k_lmax_apply(int32_t n, const
 }
 
 // nv = exact sequential norm of w; lam <- nv, or a stop on a zero or non-finite norm; v = w / nv
-// (all in this block when `scale`)
+// (all in this block when `scale`). Launched with 32 threads, one warp does the sum (short w).
 __global__ void __launch_bounds__(exact::kThreads) k_lmax_norm(int64_t m, const double* w, double* v, double* state,
                                                               int scale) {
   __shared__ double nv_sh;
   if (state[2] != 0.0) return;
-  const double s = exact::sequential_sum(m, [w](int64_t k) {
+  const auto sq = [w](int64_t k) {
     const double x = w[k];
     return x * x;
-  });
+  };
+  const double s = blockDim.x == 32 ? exact::warp_sequential_sum_from(0.0, 0, m, sq) : exact::sequential_sum(m, sq);
   if (threadIdx.x == 0) {
     const double nv = sqrt(s);
     nv_sh = nv;
@@ -768,6 +770,71 @@ __global__ void __launch_bounds__(32 * kAccWarps) k_c_values_acc(int32_t na, con
     for (int32_t q = lane; q < 36 * len; q += 32) cval[36 * int64_t(c0) + q] = acc[q];
 }
 
+// The same for levels with few coarse rows (too few warps to fill the GPU): a block per coarse
+// row, whose threads take (A P entry, group of nine of the 36 entries) items of one restriction
+// entry at a time, with a barrier between restriction entries - every entry of C still sees its
+// additions in the same order.
+constexpr int kRowT = 128;
+constexpr int32_t kFewRows = 2432;  // (16 warps on each of 152 SMs)
+__global__ void __launch_bounds__(kRowT) k_c_values_rows(int32_t na, const int32_t* rrow, const int32_t* rent_i,
+                                                         const int32_t* rent_e, const double* pval,
+                                                         const int32_t* aprow, const int32_t* apcol,
+                                                         const double* apval, const int32_t* crow,
+                                                         const int32_t* scratch, const int64_t* soff, int32_t* ccol,
+                                                         double* cval, double scale) {
+  __shared__ double acc_sh[kAccSlots * 36];
+  __shared__ int32_t col_sh[kAccSlots];
+  const int32_t I = blockIdx.x;
+  if (I >= na) return;
+  const int32_t c0 = crow[I], c1 = crow[I + 1], len = c1 - c0;
+  const bool local = len <= kAccSlots;
+  double* acc = local ? acc_sh : cval + 36 * int64_t(c0);
+  const int32_t* cols = local ? col_sh : ccol + c0;
+  for (int32_t c = threadIdx.x; c < len; c += kRowT) {
+    const int32_t v = scratch[soff[I] + c];
+    ccol[c0 + c] = v;
+    if (local) col_sh[c] = v;
+  }
+  for (int32_t q = threadIdx.x; q < 36 * len; q += kRowT) acc[q] = 0.0;
+  __syncthreads();
+  for (int32_t r = rrow[I]; r < rrow[I + 1]; ++r) {
+    const int32_t i = rent_i[r];
+    const double* Pi = pval + 36 * int64_t(rent_e[r]);
+    const int32_t e0 = aprow[i], ne = aprow[i + 1] - e0;
+    for (int32_t item = threadIdx.x; item < 4 * ne; item += kRowT) {
+      const int32_t e = e0 + item / 4;
+      const int g = item % 4;
+      const int32_t J = apcol[e];
+      int32_t slot;
+      if (J == I) {
+        slot = 0;
+      } else {
+        int32_t lo = 1, hi = len - 1;
+        while (lo < hi) {
+          const int32_t mid = (lo + hi) >> 1;
+          if (cols[mid] < J) lo = mid + 1;
+          else hi = mid;
+        }
+        slot = lo;
+      }
+      const double* B = apval + 36 * int64_t(e);
+      double* C = acc + 36 * int64_t(slot);
+      for (int ent = 9 * g; ent < 9 * g + 9; ++ent) {
+        const int rr = ent / 6, cc = ent - 6 * (ent / 6);
+        double sacc = 0.0;
+        for (int q = 0; q < 6; ++q) sacc += Pi[q * 6 + rr] * B[q * 6 + cc];
+        C[ent] = C[ent] + sacc;
+      }
+    }
+    __syncthreads();
+  }
+  if (scale != 1.0)
+    for (int32_t q = threadIdx.x; q < 36 * len; q += kRowT) acc[q] *= scale;
+  __syncthreads();
+  if (local)
+    for (int32_t q = threadIdx.x; q < 36 * len; q += kRowT) cval[36 * int64_t(c0) + q] = acc[q];
+}
+
 // build work of P^T (A P): 6 |P row i| |AP row i|
 __global__ void k_work_rap(int32_t n, const int32_t* prow, const int32_t* aprow, unsigned long long* acc) {
   const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1000,15 +1067,16 @@ __global__ void k_widen_offsets(int32_t n, const int32_t* scan32, int64_t* off) 
 }
 
 // ---- the coarsest level's dense factor (amg.cpp:535-578) ---------------------------------------
+// one thread per (row, entry of a 6x6 block): a row's columns are distinct, so each entry of C is
+// written once over the zeroed matrix
 __global__ void k_dense_fill(int32_t nc, const int32_t* rowptr, const int32_t* col, const double* val, int32_t m,
                              double* C) {
-  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= nc) return;
-  for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
-    const int32_t j = col[k];
-    for (int r = 0; r < 6; ++r)
-      for (int c = 0; c < 6; ++c) C[int64_t(6 * i + r) * m + (6 * j + c)] += val[36 * int64_t(k) + r * 6 + c];
-  }
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= 36 * int64_t(nc)) return;
+  const int32_t i = int32_t(t / 36);
+  const int e = int(t % 36), r = e / 6, c = e % 6;
+  for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+    C[int64_t(6 * i + r) * m + (6 * col[k] + c)] += val[36 * int64_t(k) + e];
 }
 
 // ---- host-side steps ---------------------------------------------------------------------------
@@ -1079,7 +1147,8 @@ int estimate_lmax(Problem& P, const Level& L, double* out) {
     (k_lmax_apply<<<ab, 6 * kApplyNodes, 0, P.stream>>>(n, L.A.rowptr, L.A.col, L.A.val, L.dinv, v.p, w.p, st.p),
      SVXG_COUNT_LAUNCH());
     if (fused) {
-      (k_lmax_norm<<<1, exact::kThreads, 0, P.stream>>>(m, w.p, v.p, st.p, 1), SVXG_COUNT_LAUNCH());
+      (k_lmax_norm<<<1, m <= exact::kWarpSumMax ? 32 : exact::kThreads, 0, P.stream>>>(m, w.p, v.p, st.p, 1),
+       SVXG_COUNT_LAUNCH());
       continue;
     }
     (k_norm_chunk_sum<<<unsigned(nchunk), 256, 0, P.stream>>>(m, w.p, csum.p, st.p), SVXG_COUNT_LAUNCH());
@@ -1329,7 +1398,12 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     TRY(P.mem.alloc(&C.A.val, size_t(cnnz) * 36));
     const double scale = (!smoothed && opt.coarse_scale != 1.0) ? opt.coarse_scale : 1.0;
     // (A P rows of 6 entries or more on average: the lanes over each row's entries)
-    if (apnnz_total >= 6 * int64_t(n))
+    if (na < kFewRows)
+      (k_c_values_rows<<<unsigned(na), kRowT, 0, st>>>(na, F.rrow, F.rent_i, F.rent_e, F.pval, aprow.p, apcol.p,
+                                                        apval.p, C.A.rowptr, scratch.p, soff.p, C.A.col, C.A.val,
+                                                        scale),
+       SVXG_COUNT_LAUNCH());
+    else if (apnnz_total >= 6 * int64_t(n))
       (k_c_values_acc<<<unsigned((na + kAccWarps - 1) / kAccWarps), 32 * kAccWarps, 0, st>>>(
            na, F.rrow, F.rent_i, F.rent_e, F.pval, aprow.p, apcol.p, apval.p, C.A.rowptr, scratch.p, soff.p, C.A.col,
            C.A.val, scale),
@@ -1371,7 +1445,8 @@ int factor_coarsest(Problem& P) {
   TRY(P.mem.alloc(&P.d_chol, size_t(m) * size_t(m)));
   cudaStream_t st = P.stream;
   SVXG_CUDA(cudaMemsetAsync(P.d_chol, 0, sizeof(double) * size_t(m) * size_t(m), st));
-  (k_dense_fill<<<nblk(L.A.n), kT, 0, st>>>(L.A.n, L.A.rowptr, L.A.col, L.A.val, m, P.d_chol), SVXG_COUNT_LAUNCH());
+  (k_dense_fill<<<nblk(36 * int64_t(L.A.n)), kT, 0, st>>>(L.A.n, L.A.rowptr, L.A.col, L.A.val, m, P.d_chol),
+   SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   // the factor (in place) and the inverse the cycle applies: dense.cu
   TRY(P.mem.alloc(&P.d_cinv, 2 * size_t(m) * size_t(m)));
@@ -1399,7 +1474,7 @@ __global__ void k_state_norm_out(const double* state, double* out) {
 // path estimate_lmax takes for a vector of that length
 int debug_seq_norm(cudaStream_t st, const double* v, int64_t n, double* out_dev) {
   if (n <= kLmaxFusedMax) {
-    (k_seq_norm<<<1, exact::kThreads, 0, st>>>(n, v, out_dev), SVXG_COUNT_LAUNCH());
+    (k_seq_norm<<<1, n <= exact::kWarpSumMax ? 32 : exact::kThreads, 0, st>>>(n, v, out_dev), SVXG_COUNT_LAUNCH());
     SVXG_CUDA(cudaGetLastError());
     return SVXG_OK;
   }

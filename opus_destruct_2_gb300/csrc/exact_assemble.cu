@@ -193,10 +193,13 @@ __global__ void k_trace(int32_t nfree, const int32_t* rowptr, const double* val,
 // id_scale (stress.cpp:112-122): the rows' terms summed one after another, in row order (the
 // sequential sum's exact bits, computed in parallel: exact_sum.cuh), over their count
 __global__ void __launch_bounds__(exact::kThreads) k_id_scale(int32_t nfree, const double* term, double* out) {
-  const double tr = exact::sequential_sum(nfree, [term](int64_t d) {
+  const auto f = [term](int64_t d) {
     const double t = term[d];
     return t >= 0.0 ? t : 0.0;
-  });
+  };
+  // (one warp for a short sum: launched with 32 threads)
+  const double tr = blockDim.x == 32 ? exact::warp_sequential_sum_from(0.0, 0, nfree, f)
+                                     : exact::sequential_sum(nfree, f);
   __shared__ int32_t cnt;
   if (threadIdx.x == 0) cnt = 0;
   __syncthreads();
@@ -397,7 +400,8 @@ int assemble_matrix(Problem& P) {
   if (nfree > 0)
     (k_trace<<<blocks_for(nfree), kT, 0, st>>>(nfree, P.K.rowptr, P.K.val, node_of_dof.p, P.d_nodes, term.p, ident.p,
                                               nident.p), SVXG_COUNT_LAUNCH());
-  (k_id_scale<<<1, exact::kThreads, 0, st>>>(nfree, term.p, ids.p), SVXG_COUNT_LAUNCH());
+  (k_id_scale<<<1, nfree <= exact::kWarpSumMax ? 32 : exact::kThreads, 0, st>>>(nfree, term.p, ids.p),
+   SVXG_COUNT_LAUNCH());
   if (nfree > 0) (k_identity<<<blocks_for(nfree), kT, 0, st>>>(nfree, P.K.rowptr, ident.p, ids.p, P.K.val), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   SVXG_CUDA(cudaMemcpyAsync(&P.id_scale, ids.p, sizeof(double), cudaMemcpyDeviceToHost, st));

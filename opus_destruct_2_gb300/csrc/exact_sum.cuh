@@ -24,6 +24,7 @@ namespace exact {
 constexpr int kThreads = 1024;
 constexpr int kItems = 8;
 constexpr int kQuietRounds = 4;  // warp rounds without a crossing before block rounds resume
+constexpr int64_t kWarpSumMax = 4096;  // sums of at most this many terms go to one warp
 constexpr int64_t kCap = int64_t(1) << 54;  // saturation: past any binade's room
 
 struct Pair {
@@ -289,6 +290,62 @@ __device__ inline double sequential_sum_from(double s0, int64_t a, int64_t n, Te
   const double r = s_sh;
   __syncthreads();
   return r;
+}
+
+// The same by one warp (the only threads that call it), for short sequences: rounds of 32 terms
+// with no block-wide barrier. Every lane gets the result.
+template <class Term>
+__device__ inline double warp_sequential_sum_from(double s, int64_t p, int64_t n, Term term) {
+  const int lane = threadIdx.x & 31;
+  while (p < n) {
+    const uint64_t sbits = uint64_t(__double_as_longlong(s));
+    if (((sbits >> 52) & 0x7ff) == 0x7ff) {
+      // s is inf or NaN: NaN if any later term is NaN, else s
+      bool nan = false;
+      for (int64_t k = p + lane; k < n; k += 32) nan |= term(k) != term(k);
+      const bool any = __any_sync(0xffffffffu, nan);
+      return (any && s == s) ? __longlong_as_double(0x7ff8000000000000LL) : s;
+    }
+    if (s == 0.0) {
+      // leading zeros leave s at 0; the first nonzero term becomes s exactly
+      const int64_t k = p + lane;
+      const double t = k < n ? term(k) : 0.0;
+      const unsigned m = __ballot_sync(0xffffffffu, k < n && !(t == 0.0));
+      if (m == 0) {
+        p = p + 32;
+        continue;
+      }
+      const int f = __ffs(m) - 1;
+      s = 0.0 + __shfl_sync(0xffffffffu, t, f);
+      p = p + f + 1;
+      continue;
+    }
+    int64_t S;
+    int uexp;
+    split(s, &S, &uexp);
+    const int64_t k = p + lane;
+    const double t = k < n ? term(k) : 0.0;
+    const Pair pr = k < n ? term_pair(t, uexp) : Pair{0, 0};
+    const Pair incl = warp_scan(pr);
+    Pair ex = shfl_up_pair(incl, 1);
+    if (lane == 0) ex = Pair{0, 0};
+    const int64_t run = sat(S, pick(ex, S));
+    const bool cross = k < n && sat(run, pick(pr, run)) >= (int64_t(1) << 53);
+    const unsigned m = __ballot_sync(0xffffffffu, cross);
+    if (m == 0) {
+      Pair tot;
+      tot.d0 = __shfl_sync(0xffffffffu, incl.d0, 31);
+      tot.d1 = __shfl_sync(0xffffffffu, incl.d1, 31);
+      s = join(sat(S, pick(tot, S)), uexp);
+      p = p + 32;
+    } else {
+      const int f = __ffs(m) - 1;
+      const double before = __shfl_sync(0xffffffffu, join(run, uexp), f);
+      s = __dadd_rn(before, __shfl_sync(0xffffffffu, t, f));
+      p = p + f + 1;
+    }
+  }
+  return s;
 }
 
 // The sequential sum of term(k) for k in [0, n) from 0.

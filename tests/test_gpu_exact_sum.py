@@ -1,7 +1,8 @@
 """The device's parallel reproduction of a sequential double sum (the multigrid setup's norm,
 core/src/solve/amg.cpp:267-268) against the sequential loop itself: bit for bit, on magnitudes
 spread over 80 binades, exact ties, subnormals, zeros, and non-finite terms - in one block for
-shorter vectors and by chunks over many blocks for vectors past 131,072 terms."""
+shorter vectors (one warp up to 4096 terms) and by chunks over many blocks for vectors past
+131,072 terms."""
 import ctypes
 import math
 
@@ -39,6 +40,11 @@ CASES = {
     "ties_many_chunks": lambda r: np.sqrt((r.integers(0, 8, 300_000) * 0.5) * 2.0 ** r.integers(-3, 3, 300_000)),
     "growing_many_chunks": lambda r: np.arange(1, 500_001, dtype=np.float64) ** 0.5 * r.uniform(0.9, 1.1, 500_000),
     "zeros_then_chunks": lambda r: np.concatenate([np.zeros(150_000), r.normal(size=150_000)]),
+    "wide_short": lambda r: np.exp(r.uniform(-90, 90, 3000)),
+    "ties_short": lambda r: np.sqrt((r.integers(0, 8, 4096) * 0.5) * 2.0 ** r.integers(-3, 3, 4096)),
+    "zeros_first_short": lambda r: np.concatenate([np.zeros(1000), r.normal(size=1000)]),
+    "all_zero_short": lambda r: np.zeros(500),
+    "subnormal_short": lambda r: r.random(2000) * 1e-160,
     "single": lambda r: np.array([3.0]),
     "empty": lambda r: np.zeros(0),
 }
@@ -51,10 +57,10 @@ def test_sequential_norm_bits(name):
     assert (a == b) or (math.isnan(a) and math.isnan(b)), (a, b)
 
 
-@pytest.mark.parametrize("n", [10_000, 300_000])
+@pytest.mark.parametrize("n", [2_000, 10_000, 300_000])
 def test_non_finite_terms(n):
     v = np.ones(n)
     v[n // 2] = np.inf
     assert dev_norm(v) == math.inf
-    v[n // 2 + 2000] = np.nan
+    v[n // 2 + n // 8] = np.nan
     assert math.isnan(dev_norm(v))
