@@ -350,6 +350,50 @@ __global__ void k_mis_cover(int32_t n, const int32_t* rowptr, const int32_t* col
     if (strong[k]) covered[col[k]] = 1;
 }
 
+// All the rounds of a smaller level in one block (claim, decide, cover as above, a block barrier
+// between them; the rounds end when a decide leaves no node undecided), instead of three launches
+// a round and a host read every few rounds.
+constexpr int32_t kMisSmall = 8192;
+__global__ void __launch_bounds__(1024) k_mis_small(int32_t n, const int32_t* rowptr, const int32_t* col,
+                                                    const uint8_t* strong, uint8_t* state, uint8_t* covered,
+                                                    int32_t* claim) {
+  for (int32_t round = 0; round <= n; ++round) {
+    for (int32_t i = threadIdx.x; i < n; i += blockDim.x) {
+      if (state[i] != 0) continue;
+      atomicMin(&claim[i], i);
+      for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+        if (strong[k]) atomicMin(&claim[col[k]], i);
+    }
+    __syncthreads();
+    int und = 0;
+    for (int32_t i = threadIdx.x; i < n; i += blockDim.x) {
+      if (state[i] != 0) continue;
+      bool cov = covered[i] != 0;
+      bool mine = claim[i] == i;
+      for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+        if (strong[k]) {
+          const int32_t x = col[k];
+          cov = cov || covered[x] != 0;
+          mine = mine && claim[x] == i;
+        }
+      if (cov) state[i] = 2;
+      else if (mine) state[i] = 3;
+      else und = 1;
+    }
+    const int any = __syncthreads_or(und);
+    for (int32_t i = threadIdx.x; i < n; i += blockDim.x) {
+      claim[i] = INT_MAX;
+      if (state[i] != 3) continue;
+      state[i] = 1;
+      covered[i] = 1;
+      for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+        if (strong[k]) covered[col[k]] = 1;
+    }
+    __syncthreads();
+    if (!any) break;
+  }
+}
+
 __global__ void k_root_flags(int32_t n, const uint8_t* state, int32_t* flag) {
   const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) flag[i] = state[i] == 1 ? 1 : 0;
@@ -1211,7 +1255,9 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     // rounds in batches of kBatch (a round after the last decision changes nothing), one host
     // read per batch: the last round's count of undecided nodes
     constexpr int kBatch = 8;
-    for (int guard = 0; guard <= n; guard += kBatch) {
+    if (n <= kMisSmall)
+      (k_mis_small<<<1, 1024, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, covered.p, claim.p), SVXG_COUNT_LAUNCH());
+    for (int guard = 0; n > kMisSmall && guard <= n; guard += kBatch) {
       SVXG_CUDA(cudaMemsetAsync(undecided.p, 0, sizeof(int32_t) * kBatch, st));
       for (int b = 0; b < kBatch; ++b) {
         (k_mis_claim<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, claim.p), SVXG_COUNT_LAUNCH());

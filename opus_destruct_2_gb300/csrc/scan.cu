@@ -80,6 +80,24 @@ __global__ void k_tile_scan(const int32_t* in, int32_t* out, int64_t n, const in
   }
 }
 
+// one block for short arrays (at most one tile): out and the total (sums[0]) in one launch
+__global__ void k_scan_one_tile(const int32_t* in, int32_t* out, int64_t n, int32_t* sums) {
+  const int64_t base = int64_t(threadIdx.x) * kScanItems;
+  int32_t v[kScanItems];
+  int32_t s = 0;
+  for (int k = 0; k < kScanItems; ++k) {
+    v[k] = (base + k < n) ? in[base + k] : 0;
+    s += v[k];
+  }
+  int32_t total;
+  int32_t run = block_excl(s, &total);
+  for (int k = 0; k < kScanItems; ++k) {
+    if (base + k < n) out[base + k] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == 0) sums[1] = total;
+}
+
 }  // namespace
 
 int exclusive_scan_i32(Problem& P, const int32_t* in, int32_t* out, int64_t n, int32_t* total_host) {
@@ -89,7 +107,9 @@ int exclusive_scan_i32(Problem& P, const int32_t* in, int32_t* out, int64_t n, i
     if (int e = P.mem.alloc(&P.d_scan, size_t(ntiles + 1))) return e;
     P.scan_cap = ntiles + 1;
   }
-  if (n > 0) {
+  if (n > 0 && ntiles == 1) {
+    (k_scan_one_tile<<<1, kScanThreads, 0, P.stream>>>(in, out, n, P.d_scan), SVXG_COUNT_LAUNCH());
+  } else if (n > 0) {
     (k_tile_sums<<<unsigned(ntiles), kScanThreads, 0, P.stream>>>(in, n, P.d_scan), SVXG_COUNT_LAUNCH());
     (k_scan_sums<<<1, kScanThreads, 0, P.stream>>>(P.d_scan, ntiles), SVXG_COUNT_LAUNCH());
     (k_tile_scan<<<unsigned(ntiles), kScanThreads, 0, P.stream>>>(in, out, n, P.d_scan), SVXG_COUNT_LAUNCH());
