@@ -510,6 +510,119 @@ int pcg_begin(Problem& P, const double* f_nodes, const double* u0_nodes) {
   return SVXG_OK;
 }
 
+// A whole block-Jacobi iterate() in one block, for the small problems the reference preconditions
+// by their diagonal blocks: each iteration's steps in order (q = K p with p.q and alpha, the x and r
+// update with ||r|| and the convergence test, z = Jinv r with r.z and beta, the p update, the cap),
+// with the same breakdown and stopping rules and the same device scalars as the launches of
+// plain_body; block barriers stand for the kernel boundaries, and the dot products are block
+// trees (fixed order).
+constexpr int kJacobiBlockT = 1024;
+constexpr int32_t kJacobiBlockMax = 4096;
+
+__device__ __forceinline__ double block_tree_sum(double v, double* sh) {
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int d = kJacobiBlockT / 2; d > 0; d >>= 1) {
+    if (int(threadIdx.x) < d) sh[threadIdx.x] += sh[threadIdx.x + d];
+    __syncthreads();
+  }
+  const double t = sh[0];
+  __syncthreads();
+  return t;
+}
+
+__global__ void __launch_bounds__(kJacobiBlockT) k_jacobi_pcg_block(int32_t nf, const int32_t* __restrict__ rowptr,
+                                                                    const int32_t* __restrict__ col,
+                                                                    const double* __restrict__ val,
+                                                                    const double* __restrict__ jinv, double* x,
+                                                                    double* r, double* z, double* p, double* q,
+                                                                    PcgScalars* s) {
+  __shared__ double sh[kJacobiBlockT];
+  const int64_t m = 6 * int64_t(nf);
+  for (int32_t guard = 0; guard <= s->maxit; ++guard) {
+    __syncthreads();
+    if (s->done) break;
+    // q = K p, p.q
+    double pq = 0.0;
+    for (int64_t t = threadIdx.x; t < m; t += kJacobiBlockT) {
+      const int32_t i = int32_t(t / 6);
+      const int c = int(t % 6);
+      double y = 0.0;
+      for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
+        const double* a = val + 36 * int64_t(k) + 6 * c;
+        const double* v = p + 6 * int64_t(col[k]);
+        y += a[0] * v[0] + a[1] * v[1] + a[2] * v[2] + a[3] * v[3] + a[4] * v[4] + a[5] * v[5];
+      }
+      q[t] = y;
+      pq += p[t] * y;
+    }
+    pq = block_tree_sum(pq, sh);
+    if (threadIdx.x == 0) {
+      s->pq = pq;
+      s->iters += 1;
+      if (!(pq > 0)) {
+        s->breakdown = 1;
+        s->done = 1;
+      } else {
+        s->alpha = s->rz / pq;
+      }
+    }
+    __syncthreads();
+    if (s->done) break;
+    // x += alpha p, r -= alpha q, ||r||
+    const double alpha = s->alpha;
+    double rr = 0.0;
+    for (int64_t t = threadIdx.x; t < m; t += kJacobiBlockT) {
+      x[t] += alpha * p[t];
+      const double rv = r[t] - alpha * q[t];
+      r[t] = rv;
+      rr += rv * rv;
+    }
+    rr = block_tree_sum(rr, sh);
+    if (threadIdx.x == 0) {
+      const double rn = sqrt(rr);
+      s->rn = rn;
+      s->rel_res = rn / s->bn;
+      if (rn <= s->target) {
+        s->converged = 1;
+        s->done = 1;
+      }
+    }
+    __syncthreads();
+    if (s->done) break;
+    // z = Jinv r, r.z, beta
+    double rz = 0.0;
+    for (int32_t i = threadIdx.x; i < nf; i += kJacobiBlockT) {
+      const double* J = jinv + 36 * int64_t(i);
+      double rv[6];
+      for (int c = 0; c < 6; ++c) rv[c] = r[6 * int64_t(i) + c];
+      for (int a = 0; a < 6; ++a) {
+        double zv = 0.0;
+        for (int c = 0; c < 6; ++c) zv += J[6 * a + c] * rv[c];
+        z[6 * int64_t(i) + a] = zv;
+        rz += rv[a] * zv;
+      }
+    }
+    rz = block_tree_sum(rz, sh);
+    if (threadIdx.x == 0) {
+      if (!(rz > 0)) {
+        s->breakdown = 1;
+        s->done = 1;
+      } else {
+        s->beta = rz / s->rz;
+        s->rz = rz;
+      }
+    }
+    __syncthreads();
+    if (s->done) break;
+    // p = z + beta p; the cap
+    const double beta = s->beta;
+    for (int64_t t = threadIdx.x; t < m; t += kJacobiBlockT) p[t] = z[t] + beta * p[t];
+    __syncthreads();
+    if (threadIdx.x == 0 && !s->done && s->iters >= s->maxit) s->done = 2;
+  }
+}
+
 // one iteration of the sequence (stress.cpp:428-461), enqueued on P.stream
 int plain_body(Problem& P) {
   const int32_t nf = P.nfree;
@@ -591,6 +704,13 @@ int plain_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
   SVXG_CUDA(host_wait(st));
   if (P.h_s->done || nf == 0) {
     // (converged, empty or not finite at the start: no iteration)
+  } else if (P.jacobi_only && nf <= kJacobiBlockMax && !P.timer_on) {
+    (k_jacobi_pcg_block<<<1, kJacobiBlockT, 0, st>>>(nf, P.K.rowptr, P.K.col, P.K.val, P.d_jinv, P.d_x, P.d_r, P.d_z,
+                                                      P.d_p, P.d_q, P.d_s),
+     SVXG_COUNT_LAUNCH());
+    SVXG_CUDA(cudaGetLastError());
+    SVXG_CUDA(cudaMemcpyAsync(P.h_s, P.d_s, sizeof(PcgScalars), cudaMemcpyDeviceToHost, st));
+    SVXG_CUDA(host_wait(st));
   } else if (loop_graph_worth(P, P.loop_plain)) {
     int64_t per = 0;
     TRY(run_loop(P, P.loop_plain, &P.d_s->done, plain_body, &per));
