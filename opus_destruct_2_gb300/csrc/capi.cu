@@ -88,6 +88,12 @@ void release_solver(Problem& P) {
   }
   P.mem.release(P.d_cinv);
   P.mem.release(P.d_cvec);
+  P.mem.release(P.d_cinv32);
+  {
+    char* bd = static_cast<char*>(P.d_bdesc);
+    P.mem.release(bd);
+    P.d_bdesc = nullptr;
+  }
   P.lv.clear();
   P.chol_n = 0;
   P.amg_work = P.amg_build_work = 0;
@@ -174,7 +180,16 @@ thread_local WaitEvent t_wait;
 
 }  // namespace
 
-void blocking_waits(bool on) { g_blocking.fetch_add(on ? 1 : -1); }
+// SVXG_BLOCKING_SYNC=0 keeps spinning waits even under a server (=1 forces sleeping waits)
+const int g_blocking_env = [] {
+  const char* v = std::getenv("SVXG_BLOCKING_SYNC");
+  return v && v[0] ? (v[0] == '0' ? 0 : 1) : -1;
+}();
+
+void blocking_waits(bool on) {
+  if (g_blocking_env == 0) return;
+  g_blocking.fetch_add(on ? 1 : -1);
+}
 
 cudaError_t host_wait(cudaStream_t s) {
   if (g_blocking.load(std::memory_order_relaxed) <= 0) return cudaStreamSynchronize(s);

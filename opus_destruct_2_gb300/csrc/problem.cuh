@@ -197,6 +197,8 @@ struct Problem {
   bool active = false;
   int32_t run_iters = 0;
   int32_t host_loops = 0;         // host-driven iterate() runs since the last assemble
+  void* d_bdesc = nullptr;        // block_solve.cu: the levels' descriptor of a small problem
+  float* d_cinv32 = nullptr;      // ... and its coarsest inverse in f32
   // whole-iterate graphs (graphs.cu): built on first use after each assemble
   void* loop_plain = nullptr;
   void* loop_mixed = nullptr;
@@ -254,6 +256,10 @@ enum OpKind { kOpK64 = 0, kOpA32 = 1, kOpP32 = 2, kOpR32 = 3 };
 int table_sched(int kind, int64_t rows, int64_t blocks);
 bool tune_timing();
 int tune_decide(Problem& P, int kind, int level, int64_t rows, int64_t blocks, float ms_warp, float ms_group);
+// block_solve.cu: a small problem's AMG iterate() in one block launch
+constexpr int32_t kBlockSolveMax = 1536;
+bool block_solve_fits(const Problem& P);
+int block_iterate(Problem& P);
 // exact_appended.cu (StressProblem::reassemble / extend_warm_start)
 int build_appended(Problem& P);                  // P.sub over K's appended block (>= 24 nodes)
 void release_appended(Problem& P);

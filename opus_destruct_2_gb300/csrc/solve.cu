@@ -711,6 +711,10 @@ int plain_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
     SVXG_CUDA(cudaGetLastError());
     SVXG_CUDA(cudaMemcpyAsync(P.h_s, P.d_s, sizeof(PcgScalars), cudaMemcpyDeviceToHost, st));
     SVXG_CUDA(host_wait(st));
+  } else if (block_solve_fits(P)) {
+    TRY(block_iterate(P));
+    SVXG_CUDA(cudaMemcpyAsync(P.h_s, P.d_s, sizeof(PcgScalars), cudaMemcpyDeviceToHost, st));
+    SVXG_CUDA(host_wait(st));
   } else if (loop_graph_worth(P, P.loop_plain)) {
     int64_t per = 0;
     TRY(run_loop(P, P.loop_plain, &P.d_s->done, plain_body, &per));
