@@ -157,7 +157,8 @@ def serve(requests: int = 20000, rate: float = 5000.0, repeat_share: float = 0.3
     dof = np.array([6 * len(geoms[p[2]][0]) for p in plan])
     near10k = (dof >= 8000) & (dof <= 12000)
     plain_reqs = [geoms[p[2]] for p in plan]
-    plain_rate, plain_lat = plain_per_request(plain_reqs, mats, rtol, maxit, plain_sample)
+    plain_rate, plain_lat = (plain_per_request(plain_reqs, mats, rtol, maxit, plain_sample) if plain_sample > 0
+                             else (float("nan"), np.array([np.nan])))
     return {
         "solves_per_s": float(ok.sum()) / wall, "wall_s": wall, "submit_s": submit_s,
         "requests": requests, "offered_rate": rate, "completed": int(ok.sum()),
