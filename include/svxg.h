@@ -141,6 +141,26 @@ int svxg_utilization_noalloc(const svxg_node* nodes_dev, int32_t n, const svxg_b
                              const svxg_material* mats_dev, const double* u_dev, double fragility, double* phi_dev,
                              uint8_t* mode_dev, int32_t* over_dev, int32_t* n_over, void* stream);
 
+/* --- the judge's break rounds ---------------------------------------------------------------- */
+/* Replaces World::Impl::judge's cascade of one structure (core/src/world/world.cpp:1162-1277)
+ * with its solve restarts (world.cpp:1041-1110) and detach_unsupported (world.cpp:1371-1458), on
+ * this problem: solve (warm from u, at most o->maxit iterations; unconverged solves restart as
+ * the world restarts them), judge every intact bond under lerp(judged, L, dif) while a shock is
+ * on, break the round's worst bonds (thr = max(1, band x max phi), at least the worst quarter,
+ * at most max_breaks_per_round) with remove_bond, retire what no support holds (their loads and
+ * motion become zero), and again, until no bond is over strength or max_rounds rounds broke
+ * bonds. opt: assemble()'s options (null: the last ones; a restart on a rebuilt preconditioner
+ * sets amg_min_nodes = 0 as the world does); o: null for the defaults.
+ * f: the load (6 n, host; not changed), u: the warm start in and the last solution out (6 n).
+ * judged / judged_has: the bonds' last steady loads and whether they have one (nb each, in and
+ * out; both null: none). phi: the last judgement's utilizations (nb, broken bonds 0), or null.
+ * broken: the bonds the rounds broke, in order (up to broken_cap); retired: the nodes retired, in
+ * order (up to retired_cap); res: counts and the final status (SVXG_CASCADE_*). The problem's
+ * bonds and nodes are left broken and retired as the reference's would be (svxg_bond_flags). */
+int svxg_cascade(svxg_problem* p, const svxg_stress_options* opt, const svxg_cascade_options* o, const double* f,
+                 double* u, svxg_bond_load* judged, uint8_t* judged_has, double* phi, int32_t* broken,
+                 int32_t broken_cap, int32_t* retired, int32_t retired_cap, svxg_cascade_result* res);
+
 /* --- counters ------------------------------------------------------------------------------- */
 int svxg_get_info(svxg_problem* p, svxg_info* info);
 /* Kernel launches made by this library since it was loaded (all problems, all threads). */

@@ -112,6 +112,64 @@ typedef struct svxg_bond_load {
 
 enum { SVXG_FAIL_NONE = 0, SVXG_FAIL_TENSION = 1, SVXG_FAIL_CRUSH = 2, SVXG_FAIL_SHEAR = 3 };
 
+/* The judge's break rounds of one structure: World::Impl::judge (core/src/world/world.cpp:1162-1277)
+ * with the solve restarts of World::Impl's tick (world.cpp:1041-1110) and detach_unsupported
+ * (world.cpp:1371-1458, graph_components world_internal.hpp:660-705). Defaults: WorldConfig and
+ * WorldParams (core/include/svx/world/world.hpp:116, :140-153). */
+typedef struct svxg_cascade_options {
+  double rtol;                  /* stress_rtol, 3e-3 */
+  double fragility;             /* 1 */
+  double dif;                   /* dynamic increase factor of a sudden load change, 1.5 */
+  double break_band;            /* a round breaks phi >= max(1, band x max phi), 0.85 */
+  int32_t max_breaks_per_round; /* 256 (at most 65536 here) */
+  int32_t max_rounds;           /* 400 */
+  int32_t maxit;                /* iterations of a solve before it restarts, 120 (world.cpp:1074) */
+  int32_t solve_restarts;       /* unconverged restarts in a row before the structure is left, 60 */
+  int32_t rebuild_after;        /* a converged solve longer than this rebuilds a stale
+                                   preconditioner before the next one, 60 (world.cpp:1109) */
+  int32_t shock;                /* 1: the first judgement blends from the judged loads (a sudden
+                                   load change), as every judgement after a round of breaks does */
+  int32_t detach;               /* 1: after a round, parts no longer held by a support retire */
+  int32_t pad;
+} svxg_cascade_options;
+
+enum {
+  SVXG_CASCADE_SETTLED = 0,    /* a judgement found no bond at or over its strength */
+  SVXG_CASCADE_MAX_ROUNDS = 1, /* max_rounds rounds broke bonds, and some are still over */
+  SVXG_CASCADE_ABANDONED = 2,  /* solve_restarts restarts in a row did not converge */
+  SVXG_CASCADE_BREAKDOWN = 3,  /* a solve broke down (not positive definite, or non-finite) */
+  SVXG_CASCADE_SINGULAR = 4    /* assemble() found a singular diagonal */
+};
+
+typedef struct svxg_cascade_result {
+  int32_t status;         /* SVXG_CASCADE_* */
+  int32_t rounds;         /* rounds that broke bonds */
+  int32_t bonds_broken;   /* by the rounds (bonds of retired nodes not counted) */
+  int32_t nodes_retired;
+  int32_t solves;
+  int32_t restarts;       /* unconverged solves restarted, in all */
+  int64_t pcg_iters;
+  double max_utilization; /* of the last judgement */
+  double rel_res;         /* of the last solve */
+} svxg_cascade_result;
+
+static inline svxg_cascade_options svxg_default_cascade_options(void) {
+  svxg_cascade_options o;
+  o.rtol = 3e-3;
+  o.fragility = 1.0;
+  o.dif = 1.5;
+  o.break_band = 0.85;
+  o.max_breaks_per_round = 256;
+  o.max_rounds = 400;
+  o.maxit = 120;
+  o.solve_restarts = 60;
+  o.rebuild_after = 60;
+  o.shock = 0;
+  o.detach = 1;
+  o.pad = 0;
+  return o;
+}
+
 /* Defaults of the reference's option records. */
 static inline svxg_stress_options svxg_default_options(void) {
   svxg_stress_options o;

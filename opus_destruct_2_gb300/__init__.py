@@ -17,11 +17,11 @@ import sys
 import numpy as np
 
 from . import build as _build
-from .graph import (BOND_DTYPE, LOAD_DTYPE, MATERIAL_DTYPE, NODE_DTYPE, PcgResult, StressOptions, default_materials,
-                    ptr)
+from .graph import (BOND_DTYPE, LOAD_DTYPE, MATERIAL_DTYPE, NODE_DTYPE, CascadeOptions, CascadeResult, PcgResult,
+                    StressOptions, default_materials, ptr)
 
 __all__ = ["StressProblem", "StressOptions", "PcgResult", "Info", "load_library", "default_materials",
-           "NODE_DTYPE", "BOND_DTYPE", "SvxgError"]
+           "NODE_DTYPE", "BOND_DTYPE", "SvxgError", "CascadeOptions", "CascadeResult"]
 
 c_i32, c_i64, c_f64, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p
 
@@ -105,6 +105,7 @@ def load_library() -> ctypes.CDLL:
         "svxg_utilization_device": (c_i32, [c_vp, c_f64, c_vp, c_vp, c_vp, ctypes.POINTER(c_i32)]),
         "svxg_timer_enable": (c_i32, [c_vp, c_i32]),
         "svxg_timer_read": (c_i32, [c_vp, ctypes.POINTER(c_f64), ctypes.POINTER(c_i64)]),
+        "svxg_cascade": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp, c_i32, c_vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -273,6 +274,38 @@ class StressProblem:
 
     def bond_load(self, b: int, u) -> np.ndarray:
         return self.bond_loads(u)[b]
+
+    def cascade(self, f, u=None, options: CascadeOptions | None = None, opt: StressOptions | None = None,
+                judged=None, has=None):
+        """The judge's break rounds of this structure (World::Impl::judge,
+        core/src/world/world.cpp:1162-1277, with the tick's solve restarts and
+        detach_unsupported): solve, judge, break the round's worst bonds, retire what no support
+        holds, again until nothing is over strength. Returns (u, CascadeResult, extras) with
+        extras = dict(broken=[bonds in the order broken], retired=[nodes in the order retired],
+        phi=last utilizations, judged=LOAD_DTYPE records, has=uint8 flags). The problem's bonds and
+        nodes are left broken and retired (self.bonds / self.nodes follow)."""
+        self._sync_graph()
+        n, nb = len(self.nodes), len(self.bonds)
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        if f.size != 6 * n:
+            raise ValueError("f: 6 per node")
+        u = np.zeros(6 * n) if u is None else np.array(u, dtype=np.float64)
+        judged = np.zeros(nb, LOAD_DTYPE) if judged is None else np.array(judged, dtype=LOAD_DTYPE)
+        has = np.zeros(nb, np.uint8) if has is None else np.array(has, dtype=np.uint8)
+        phi = np.zeros(max(nb, 1))
+        broken = np.zeros(max(nb, 1), np.int32)
+        retired = np.zeros(max(n, 1), np.int32)
+        res = CascadeResult()
+        o = CascadeOptions() if options is None else options
+        _check(self._L.svxg_cascade(self._h, ctypes.byref(opt) if opt is not None else None, ctypes.byref(o),
+                                    ptr(f), ptr(u), ptr(judged), ptr(has), ptr(phi), ptr(broken), len(broken),
+                                    ptr(retired), len(retired), ctypes.byref(res)))
+        rl = retired[:min(res.nodes_retired, len(retired))].copy()
+        self.nodes["gone"][rl] = 1
+        self._pull_flags()
+        extras = dict(broken=broken[:min(res.bonds_broken, len(broken))].tolist(), retired=rl.tolist(),
+                      phi=phi[:nb].copy(), judged=judged, has=has)
+        return u, res, extras
 
     def utilization(self, fragility: float = 1.0):
         """(phi, mode, failing bond indices) at the current solution."""

@@ -88,6 +88,8 @@ void release_solver(Problem& P) {
   }
   P.mem.release(P.d_cinv);
   P.mem.release(P.d_cvec);
+  P.mem.release(P.d_rm_head);
+  P.rm_head_cap = 0;
   P.mem.release(P.d_cinv32);
   {
     char* bd = static_cast<char*>(P.d_bdesc);
@@ -949,6 +951,170 @@ int svxg_debug_precondition(svxg_problem* p, const double* r, double* z) {
   cudaFree(dr);
   cudaFree(dz);
   return e;
+}
+
+
+// The judge's break rounds of one structure (World::Impl::judge, core/src/world/world.cpp:1162-1277;
+// the solve restarts of the tick, world.cpp:1041-1110; detach_unsupported, world.cpp:1371-1458).
+// Everything per bond and per node runs on the device; the host reads the round's counts.
+int svxg_cascade(svxg_problem* p, const svxg_stress_options* opt, const svxg_cascade_options* co, const double* f,
+                 double* u, svxg_bond_load* judged, uint8_t* judged_has, double* phi, int32_t* broken,
+                 int32_t broken_cap, int32_t* retired, int32_t retired_cap, svxg_cascade_result* res) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  if (!res || (P.n > 0 && (!f || !u)) || ((judged == nullptr) != (judged_has == nullptr)) || broken_cap < 0 ||
+      retired_cap < 0) {
+    set_error("svxg_cascade: bad arguments");
+    return SVXG_ERR_ARG;
+  }
+  std::memset(res, 0, sizeof(*res));
+  if (!P.have_graph) {
+    set_error("svxg_cascade: no graph");
+    return SVXG_ERR_STATE;
+  }
+  const svxg_cascade_options o = co ? *co : svxg_default_cascade_options();
+  const int32_t max_breaks = std::max(1, o.max_breaks_per_round);  // (as world.cpp:61 clamps it)
+  DeviceScope ds(P.device);
+  const svxg_stress_options base = opt ? *opt : P.opt;
+  svxg_stress_options multigrid_opt = base;
+  multigrid_opt.amg_min_nodes = 0;  // (a structure restarted on a rebuilt preconditioner: world.cpp:1030)
+  CascadeScratch S;
+  TRY(cascade_alloc(P, S, max_breaks));
+  struct Free {
+    CascadeScratch& s;
+    ~Free() { cascade_free(s); }
+  } free_scratch{S};
+  const size_t m6 = 6 * size_t(P.n);
+  cudaStream_t st = P.stream;
+  if (m6) {
+    SVXG_CUDA(cudaMemcpyAsync(S.f, f, m6 * sizeof(double), cudaMemcpyHostToDevice, st));
+    SVXG_CUDA(cudaMemcpyAsync(S.u, u, m6 * sizeof(double), cudaMemcpyHostToDevice, st));
+  }
+  if (P.nb > 0) {
+    if (judged) {
+      SVXG_CUDA(cudaMemcpyAsync(S.judged, judged, sizeof(svxg_bond_load) * size_t(P.nb), cudaMemcpyHostToDevice, st));
+      SVXG_CUDA(cudaMemcpyAsync(S.has, judged_has, size_t(P.nb), cudaMemcpyHostToDevice, st));
+    } else {
+      SVXG_CUDA(cudaMemsetAsync(S.has, 0, size_t(P.nb), st));
+    }
+    SVXG_CUDA(cudaMemsetAsync(S.phi, 0, sizeof(double) * size_t(P.nb), st));
+  }
+  bool shock = o.shock != 0, multigrid = false;
+  int32_t restarts = 0;
+  std::vector<int32_t> hb, hr;
+  CascadeState hs{};
+  auto read_state = [&]() -> int {
+    SVXG_CUDA(cudaMemcpyAsync(&hs, S.st, sizeof(hs), cudaMemcpyDeviceToHost, st));
+    SVXG_CUDA(host_wait(st));
+    return SVXG_OK;
+  };
+  for (;;) {
+    if (!P.assembled) {
+      int32_t ok = 0;
+      TRY(assemble_impl(P, multigrid ? &multigrid_opt : &base, &ok));
+      if (!ok) {
+        res->status = SVXG_CASCADE_SINGULAR;
+        break;
+      }
+    }
+    if (m6) SVXG_CUDA(cudaMemcpyAsync(S.u0, S.u, m6 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    svxg_pcg_result r{};
+    TRY(solve_common(P, S.f, S.u, o.rtol, o.maxit, 1, &r));
+    res->solves += 1;
+    res->pcg_iters += r.iters;
+    res->rel_res = r.rel_res;
+    if (r.breakdown) {
+      if (m6) SVXG_CUDA(cudaMemcpyAsync(S.u, S.u0, m6 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      res->status = SVXG_CASCADE_BREAKDOWN;
+      break;
+    }
+    if (!r.converged) {
+      // world.cpp:1070-1093: keep the iterate unless it diverged; rebuild a stale or block-Jacobi
+      // preconditioner; a current one that diverged starts again from rest
+      const bool rebuild = !(P.assembled && P.pc_current) || P.jacobi_only;
+      const bool diverging = !(r.rel_res < 10.0);
+      if (diverging && m6) SVXG_CUDA(cudaMemcpyAsync(S.u, S.u0, m6 * sizeof(double), cudaMemcpyDeviceToDevice, st));
+      if (rebuild) {
+        P.assembled = false;
+        P.active = false;
+        multigrid = true;
+      } else if (diverging && m6) {
+        SVXG_CUDA(cudaMemsetAsync(S.u, 0, m6 * sizeof(double), st));
+      }
+      ++restarts;
+      ++res->restarts;
+      if (restarts >= o.solve_restarts) {
+        res->status = SVXG_CASCADE_ABANDONED;
+        break;
+      }
+      continue;
+    }
+    restarts = 0;
+    if (r.iters > o.rebuild_after && (!(P.assembled && P.pc_current) || P.jacobi_only)) {
+      P.assembled = false;  // (world.cpp:1109: the next solve rebuilds it)
+      P.active = false;
+    }
+    TRY(cascade_judge(P, S, o.fragility, o.dif, shock && o.dif != 1.0 ? 1 : 0, o.break_band, max_breaks));
+    TRY(read_state());
+    {
+      double mx = 0.0;
+      std::memcpy(&mx, &hs.maxphi_bits, sizeof(mx));
+      res->max_utilization = mx;
+    }
+    if (hs.m == 0) {
+      res->status = SVXG_CASCADE_SETTLED;
+      break;
+    }
+    if (res->rounds >= o.max_rounds) {
+      res->status = SVXG_CASCADE_MAX_ROUNDS;
+      break;
+    }
+    if (hs.K <= 0) {
+      set_error("svxg_cascade: round selection failed");
+      return SVXG_ERR_STATE;
+    }
+    const size_t old = hb.size();
+    hb.resize(old + size_t(hs.K));
+    SVXG_CUDA(cudaMemcpyAsync(hb.data() + old, S.sel, sizeof(int32_t) * size_t(hs.K), cudaMemcpyDeviceToHost, st));
+    TRY(remove_bonds_list(P, S.sel, nullptr, hs.K, S.st));
+    res->bonds_broken += hs.K;
+    res->rounds += 1;
+    shock = true;
+    if (o.detach) {
+      TRY(cascade_find_loose(P, S));
+      TRY(read_state());
+      if (hs.r > 0) {
+        TRY(cascade_retire(P, S, hs.r));
+        const size_t o2 = hr.size();
+        hr.resize(o2 + size_t(hs.r));
+        SVXG_CUDA(cudaMemcpyAsync(hr.data() + o2, S.nlist, sizeof(int32_t) * size_t(hs.r), cudaMemcpyDeviceToHost,
+                                  st));
+        res->nodes_retired += hs.r;
+      }
+    }
+    TRY(read_state());
+    if (P.assembled && !P.jacobi_only && (hs.any_in_k || hs.r_dof)) P.pc_current = false;
+    P.active = false;
+  }
+  // results, and the host's copies of the flags the rounds changed
+  if (m6) SVXG_CUDA(cudaMemcpyAsync(u, S.u, m6 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (P.nb > 0) {
+    if (judged) {
+      SVXG_CUDA(cudaMemcpyAsync(judged, S.judged, sizeof(svxg_bond_load) * size_t(P.nb), cudaMemcpyDeviceToHost, st));
+      SVXG_CUDA(cudaMemcpyAsync(judged_has, S.has, size_t(P.nb), cudaMemcpyDeviceToHost, st));
+    }
+    if (phi) SVXG_CUDA(cudaMemcpyAsync(phi, S.phi, sizeof(double) * size_t(P.nb), cudaMemcpyDeviceToHost, st));
+    TRY(cascade_bond_flags(P, S));
+    P.h_broken.resize(size_t(P.nb));
+    P.h_in_k.resize(size_t(P.nb));
+    SVXG_CUDA(cudaMemcpyAsync(P.h_broken.data(), S.broken8, size_t(P.nb), cudaMemcpyDeviceToHost, st));
+    SVXG_CUDA(cudaMemcpyAsync(P.h_in_k.data(), S.in_k8, size_t(P.nb), cudaMemcpyDeviceToHost, st));
+  }
+  SVXG_CUDA(host_wait(st));
+  for (int32_t i : hr) P.h_nodes[size_t(i)].gone = 1;
+  for (size_t k = 0; k < hb.size() && k < size_t(broken_cap); ++k) broken[k] = hb[k];
+  for (size_t k = 0; k < hr.size() && k < size_t(retired_cap); ++k) retired[k] = hr[k];
+  return SVXG_OK;
 }
 
 }  // extern "C"

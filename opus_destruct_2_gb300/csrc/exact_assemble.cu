@@ -422,11 +422,19 @@ int build_jacobi(Problem& P) {
   return SVXG_OK;
 }
 
+// up to this many bonds, one thread removes them one after another (one launch)
+constexpr int32_t kSequentialRemoveMax = 4;
+
 int remove_bonds_device(Problem& P, const int32_t* list, int32_t count) {
   if (count <= 0) return SVXG_OK;
   Tmp<int32_t> d(P.stream);
   TRY(d.alloc(size_t(count)));
   SVXG_CUDA(cudaMemcpyAsync(d.p, list, sizeof(int32_t) * size_t(count), cudaMemcpyHostToDevice, P.stream));
+  if (count > kSequentialRemoveMax) {  // (many: every block's chain in parallel, the same bits)
+    TRY(remove_bonds_list(P, d.p, nullptr, count, nullptr));
+    SVXG_CUDA(host_wait(P.stream));
+    return SVXG_OK;
+  }
   (k_remove_bonds<<<1, 1, 0, P.stream>>>(d.p, count, P.d_bonds, P.d_in_k, P.d_nodes, P.d_mats, P.d_dof, P.K.rowptr,
                                         P.K.col, P.K.val, P.d_jinv, P.jacobi_only ? 1 : 0, P.id_scale), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());

@@ -214,6 +214,8 @@ struct Problem {
   // scratch
   int32_t* d_scan = nullptr;      // scan block sums
   int64_t scan_cap = 0;
+  int32_t* d_rm_head = nullptr;   // exact_cascade.cu: a chain head per block of K (-1 between calls)
+  int64_t rm_head_cap = 0;
 };
 
 // Marks a point of the host-side trace when SVXG_TRACE=1 (drains the problem's stream first);
@@ -297,5 +299,46 @@ void uncount_launches(int64_t n);
 void add_launches(int64_t n);
 // scan.cu
 int exclusive_scan_i32(Problem& P, const int32_t* in, int32_t* out, int64_t n, int32_t* total_host);
+const int32_t* scan_total_device(const Problem& P, int64_t n);  // the last scan's total (device)
+// exact_cascade.cu: the judge's break rounds (the host loop: svxg_cascade, capi.cu)
+struct CascadeState {  // device; the host reads it once or twice a round
+  int32_t m;          // bonds at or over strength
+  int32_t K;          // bonds the round breaks
+  int32_t n_thr;      // bonds at or over the round's threshold
+  int32_t any_in_k;   // a removed bond was in K
+  int32_t r;          // nodes no support holds
+  int32_t rb;         // bonds of those nodes
+  int32_t r_dof;      // a retired node had a free DOF
+  int32_t pad;
+  double top;         // the largest phi over strength
+  unsigned long long maxphi_bits;  // the largest phi of the judgement
+};
+struct CascadeScratch {
+  char* base = nullptr;
+  cudaStream_t stream = nullptr;
+  CascadeState* st = nullptr;
+  double *u = nullptr, *f = nullptr, *u0 = nullptr;  // node order, 6 per node
+  svxg_bond_load* judged = nullptr;
+  uint8_t* has = nullptr;
+  double* phi = nullptr;
+  int32_t *flag = nullptr, *pos = nullptr, *over = nullptr, *sel = nullptr, *blist = nullptr;
+  int32_t* parent = nullptr;
+  uint8_t *held = nullptr, *now = nullptr;
+  int32_t *nlist = nullptr, *npos = nullptr;
+  unsigned long long* gphi = nullptr;
+  int32_t* gb = nullptr;
+  int64_t gcap = 0;
+  uint8_t *broken8 = nullptr, *in_k8 = nullptr;
+};
+int cascade_alloc(Problem& P, CascadeScratch& S, int32_t max_breaks);
+void cascade_free(CascadeScratch& S);
+int cascade_judge(Problem& P, CascadeScratch& S, double fragility, double dif, int blend, double band,
+                  int32_t max_breaks);
+int cascade_find_loose(Problem& P, CascadeScratch& S);
+int cascade_retire(Problem& P, CascadeScratch& S, int32_t r);
+int cascade_bond_flags(Problem& P, CascadeScratch& S);
+// StressProblem::remove_bond of a device list of distinct bonds, in list order (count: *count_dev
+// if given, else bound); unassembled: the bonds only break
+int remove_bonds_list(Problem& P, const int32_t* list, const int32_t* count_dev, int32_t bound, CascadeState* st);
 
 }  // namespace svxg

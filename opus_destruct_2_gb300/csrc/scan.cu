@@ -124,4 +124,8 @@ int exclusive_scan_i32(Problem& P, const int32_t* in, int32_t* out, int64_t n, i
   return SVXG_OK;
 }
 
+const int32_t* scan_total_device(const Problem& P, int64_t n) {
+  return P.d_scan + (n + kScanTile - 1) / kScanTile;
+}
+
 }  // namespace svxg

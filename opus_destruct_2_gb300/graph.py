@@ -158,5 +158,39 @@ class PcgResult(ctypes.Structure):
                 f"breakdown={bool(self.breakdown)})")
 
 
+class CascadeOptions(ctypes.Structure):
+    """svxg_cascade_options: the judge's break rounds of one structure (World::Impl::judge,
+    core/src/world/world.cpp:1162-1277); defaults from WorldConfig/WorldParams (world.hpp)."""
+    _fields_ = [("rtol", ctypes.c_double), ("fragility", ctypes.c_double), ("dif", ctypes.c_double),
+                ("break_band", ctypes.c_double), ("max_breaks_per_round", ctypes.c_int32),
+                ("max_rounds", ctypes.c_int32), ("maxit", ctypes.c_int32), ("solve_restarts", ctypes.c_int32),
+                ("rebuild_after", ctypes.c_int32), ("shock", ctypes.c_int32), ("detach", ctypes.c_int32),
+                ("pad", ctypes.c_int32)]
+
+    def __init__(self, **kw):
+        super().__init__()
+        self.rtol, self.fragility, self.dif, self.break_band = 3e-3, 1.0, 1.5, 0.85
+        self.max_breaks_per_round, self.max_rounds, self.maxit = 256, 400, 120
+        self.solve_restarts, self.rebuild_after, self.shock, self.detach = 60, 60, 0, 1
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+
+# svxg_cascade_result.status
+CASCADE_SETTLED, CASCADE_MAX_ROUNDS, CASCADE_ABANDONED, CASCADE_BREAKDOWN, CASCADE_SINGULAR = 0, 1, 2, 3, 4
+
+
+class CascadeResult(ctypes.Structure):
+    """svxg_cascade_result."""
+    _fields_ = [("status", ctypes.c_int32), ("rounds", ctypes.c_int32), ("bonds_broken", ctypes.c_int32),
+                ("nodes_retired", ctypes.c_int32), ("solves", ctypes.c_int32), ("restarts", ctypes.c_int32),
+                ("pcg_iters", ctypes.c_int64), ("max_utilization", ctypes.c_double), ("rel_res", ctypes.c_double)]
+
+    def __repr__(self) -> str:
+        return (f"CascadeResult(status={self.status}, rounds={self.rounds}, broken={self.bonds_broken}, "
+                f"retired={self.nodes_retired}, solves={self.solves}, restarts={self.restarts}, "
+                f"iters={self.pcg_iters}, max_phi={self.max_utilization:.4g}, rel_res={self.rel_res:.3e})")
+
+
 def ptr(a: np.ndarray | None):
     return None if a is None else ctypes.c_void_p(a.ctypes.data)

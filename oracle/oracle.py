@@ -75,6 +75,10 @@ def port_lib() -> ctypes.CDLL:
         lib.svxo_apply_k.argtypes = [c_vp, c_vp, c_vp]
         lib.svxo_set_threads.argtypes = [ctypes.c_int]
         lib.svxo_seq_sum.restype = c_f64
+        lib.svxo_utilization_many.argtypes = [c_vp, c_vp, c_f64, c_vp, c_vp]
+        lib.svxo_invalidate.argtypes = [c_vp]
+        lib.svxo_assembled.argtypes = [c_vp]
+        lib.svxo_preconditioner_current.argtypes = [c_vp]
         lib.svxo_seq_sum.argtypes = [c_vp, c_i64]
         _port = lib
     return _port
@@ -110,6 +114,18 @@ def reference_lib() -> ctypes.CDLL | None:
         lib.svxr_hier_get.argtypes = [c_vp, c_i32] + [c_vp] * 10
         lib.svxr_hier_free.argtypes = [c_vp]
         lib.svxr_set_threads.argtypes = [ctypes.c_int]
+        lib.svxr_p_create.restype = c_vp
+        lib.svxr_p_create.argtypes = [c_vp, c_i32, c_vp, c_i32, c_vp]
+        for name in ("destroy", "assembled", "invalidate", "preconditioner_current", "block_jacobi"):
+            getattr(lib, "svxr_p_" + name).argtypes = [c_vp]
+        lib.svxr_p_assemble.argtypes = [c_vp, c_vp]
+        lib.svxr_p_solve.argtypes = [c_vp, c_vp, c_vp, c_f64, c_i32, c_i32, c_vp]
+        lib.svxr_p_remove_bond.argtypes = [c_vp, c_i32]
+        lib.svxr_p_retire_nodes.argtypes = [c_vp, c_vp, c_i32]
+        lib.svxr_p_bond_flags.argtypes = [c_vp, c_vp, c_vp]
+        lib.svxr_p_judge.argtypes = [c_vp, c_vp, c_f64, c_vp, c_vp, c_vp]
+        lib.svxr_p_utilization_many.argtypes = [c_vp, c_vp, c_f64, c_vp, c_vp]
+        lib.svxr_p_matrix.argtypes = [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]
         _ref = lib
     return _ref
 
@@ -204,6 +220,26 @@ class Port:
         i = Info()
         self.lib.svxo_get_info(self.h, ctypes.byref(i))
         return i
+
+    def assembled(self) -> bool:
+        return bool(self.lib.svxo_assembled(self.h))
+
+    def invalidate(self):
+        self.lib.svxo_invalidate(self.h)
+
+    def preconditioner_current(self) -> bool:
+        return bool(self.lib.svxo_preconditioner_current(self.h))
+
+    def block_jacobi(self) -> bool:
+        return bool(self.info().block_jacobi)
+
+    def utilization_many(self, loads, fragility=1.0):
+        """bond_utilization of every bond under `loads` (one record per bond)."""
+        loads = np.ascontiguousarray(loads, dtype=LOAD_DTYPE)
+        phi = np.zeros(len(self.bonds))
+        mode = np.zeros(len(self.bonds), np.uint8)
+        self.lib.svxo_utilization_many(self.h, ptr(loads), fragility, ptr(phi), ptr(mode))
+        return phi, mode
 
     def bond_flags(self):
         br = np.zeros(len(self.bonds), np.uint8)
@@ -380,3 +416,245 @@ class Reference:
         L = np.ascontiguousarray(load)
         phi = self.lib.svxr_utilization(ptr(b), ptr(L), fragility, ptr(self.mats), ctypes.byref(mode))
         return phi, mode.value
+
+
+class RefProblem:
+    """One of the reference's own StressProblem kept between calls (ref_shim.cpp), with Port's
+    methods, so that the break rounds below run on the reference itself."""
+
+    def __init__(self, nodes, bonds, mats):
+        self.lib = reference_lib()
+        if self.lib is None:
+            raise RuntimeError("the reference is not built on this machine")
+        self.nodes, self.bonds, self.mats = records(nodes, bonds, mats)
+        self.h = self.lib.svxr_p_create(ptr(self.nodes), len(self.nodes), ptr(self.bonds), len(self.bonds),
+                                        ptr(self.mats))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.svxr_p_destroy(self.h)
+            self.h = None
+
+    def assemble(self, opt: StressOptions | None = None) -> bool:
+        return bool(self.lib.svxr_p_assemble(self.h, ctypes.byref(opt) if opt is not None else None))
+
+    def assembled(self) -> bool:
+        return bool(self.lib.svxr_p_assembled(self.h))
+
+    def invalidate(self):
+        self.lib.svxr_p_invalidate(self.h)
+
+    def preconditioner_current(self) -> bool:
+        return bool(self.lib.svxr_p_preconditioner_current(self.h))
+
+    def block_jacobi(self) -> bool:
+        return bool(self.lib.svxr_p_block_jacobi(self.h))
+
+    def solve(self, f, u=None, rtol=1e-8, maxit=500, warm=False):
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        u = np.zeros(6 * len(self.nodes)) if u is None else np.array(u, dtype=np.float64)
+        res = PcgResult()
+        self.lib.svxr_p_solve(self.h, ptr(f), ptr(u), rtol, maxit, int(warm), ctypes.byref(res))
+        return u, res
+
+    def remove_bond(self, b):
+        self.lib.svxr_p_remove_bond(self.h, int(b))
+
+    def retire_nodes(self, lst):
+        a = np.ascontiguousarray(lst, dtype=np.int32)
+        self.lib.svxr_p_retire_nodes(self.h, ptr(a), len(a))
+
+    def bond_flags(self):
+        br = np.zeros(len(self.bonds), np.uint8)
+        ik = np.zeros(len(self.bonds), np.uint8)
+        self.lib.svxr_p_bond_flags(self.h, ptr(br), ptr(ik))
+        return br, ik
+
+    def judge(self, u, fragility=1.0):
+        nb = len(self.bonds)
+        loads = np.zeros(nb, LOAD_DTYPE)
+        phi = np.zeros(nb)
+        mode = np.zeros(nb, np.uint8)
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        self.lib.svxr_p_judge(self.h, ptr(u), fragility, ptr(loads), ptr(phi), ptr(mode))
+        return loads, phi, mode
+
+    def utilization_many(self, loads, fragility=1.0):
+        loads = np.ascontiguousarray(loads, dtype=LOAD_DTYPE)
+        phi = np.zeros(len(self.bonds))
+        mode = np.zeros(len(self.bonds), np.uint8)
+        self.lib.svxr_p_utilization_many(self.h, ptr(loads), fragility, ptr(phi), ptr(mode))
+        return phi, mode
+
+    def matrix(self):
+        nf, nz = c_i32(), c_i64()
+        self.lib.svxr_p_matrix(self.h, ctypes.byref(nf), ctypes.byref(nz), None, None, None)
+        rowptr = np.zeros(nf.value + 1, np.int32)
+        col = np.zeros(nz.value, np.int32)
+        val = np.zeros((nz.value, 6, 6))
+        self.lib.svxr_p_matrix(self.h, ctypes.byref(nf), ctypes.byref(nz), ptr(rowptr), ptr(col), ptr(val))
+        return dict(nfree=nf.value, rowptr=rowptr, col=col, val=val)
+
+
+# ---- the judge's break rounds (restated) ---------------------------------------------------------
+
+LOAD_FIELDS = ("N", "V1", "V2", "T", "M1", "M2")
+
+
+def supported_nodes(n: int, bonds, broken, gone=None) -> np.ndarray:
+    """graph_components (core/src/world/world_internal.hpp:660-705) as detach_unsupported seeds it
+    (core/src/world/world.cpp:1371-1377): component 0 is every node reachable over intact
+    node-to-node bonds from a node with an intact support bond. Returns a bool per node (True:
+    in component 0). `gone` is not read: a node retired before has no intact bond left."""
+    from scipy.sparse import coo_matrix
+    from scipy.sparse.csgraph import connected_components
+    a = np.asarray(bonds["a"], dtype=np.int64)
+    b = np.asarray(bonds["b"], dtype=np.int64)
+    live = np.asarray(broken) == 0
+    seed = np.zeros(n, bool)
+    seed[a[live & (b < 0)]] = True
+    e = live & (b >= 0)
+    if n == 0:
+        return seed
+    g = coo_matrix((np.ones(int(e.sum()), np.int8), (a[e], b[e])), shape=(n, n))
+    _, lab = connected_components(g, directed=False)
+    held = np.zeros(lab.max() + 1, bool)
+    held[lab[seed]] = True
+    return held[lab]
+
+
+def select_breaks(over_b, over_phi, band: float, max_breaks: int) -> list[int]:
+    """The bonds one round breaks (core/src/world/world.cpp:1219-1271): `over` sorted by phi
+    descending then index ascending; thr = max(1, band x max phi); the loop takes bonds while
+    phi >= thr or fewer than the quota max(1, (m + 3) / 4) are taken, at most max_breaks."""
+    m = len(over_b)
+    order = np.lexsort((over_b, -over_phi))
+    ob, op = over_b[order], over_phi[order]
+    top = float(op[0])
+    x = band * top
+    thr = x if 1.0 < x else 1.0
+    quota = max(1, (m + 3) // 4)
+    out = []
+    for k in range(m):
+        if (op[k] < thr and k >= quota) or len(out) >= max_breaks:
+            break
+        out.append(int(ob[k]))
+    return out
+
+
+def cascade(P, f, u, o, opt: StressOptions | None = None, judged=None, has=None):
+    """The judge's break rounds of one structure, on a problem with Port's methods (Port: the C
+    restatement; RefProblem: the reference itself). Each round:
+
+      1. assemble if needed (after a restart on a stale preconditioner: amg_min_nodes = 0, the
+         structure's multigrid flag, world.cpp:1030), then solve warm from u with at most o.maxit
+         iterations (world.cpp:1041-1050). Breakdown: stop (status BREAKDOWN, u as it started).
+         Not converged: restart as world.cpp:1070-1093 (keep the iterate unless it diverged,
+         rel_res >= 10; rebuild the preconditioner if it is stale or block-Jacobi, else a diverged
+         one starts from rest); o.solve_restarts in a row: stop (ABANDONED).
+      2. converged after more than o.rebuild_after iterations on a stale preconditioner (or a
+         block-Jacobi one): rebuild before the next solve (world.cpp:1109).
+      3. judge (world.cpp:1162-1201): every intact bond's load L; its utilization under
+         lerp(judged, L, dif) if a shock is on, dif != 1 and the bond was judged before, else
+         under L; judged := L. No bond at or over 1, or o.max_rounds rounds done: stop.
+      4. break the bonds select_breaks() picks, in that order, with remove_bond (world.cpp:1258-1270);
+         a shock is on from now on.
+      5. o.detach: retire every node not held by a support (world.cpp:1371-1458), zero their
+         loads and motion (world.cpp:1460-1478).
+
+    Returns a dict: u, f, judged, has, broken (in order), retired (in order), per_round (bonds
+    broken per round), phi (last judgement), and the svxg_cascade_result fields."""
+    n = len(P.nodes)
+    nb = len(P.bonds)
+    f = np.array(f, dtype=np.float64)
+    u = np.array(u, dtype=np.float64)
+    judged = np.zeros(nb, LOAD_DTYPE) if judged is None else np.array(judged, dtype=LOAD_DTYPE)
+    has = np.zeros(nb, np.uint8) if has is None else np.array(has, dtype=np.uint8)
+    gone = np.array(P.nodes["gone"], dtype=np.uint8)
+    opt = StressOptions() if opt is None else opt
+    opt_mg = StressOptions()
+    ctypes.memmove(ctypes.byref(opt_mg), ctypes.byref(opt), ctypes.sizeof(StressOptions))
+    opt_mg.amg_min_nodes = 0
+    shock = bool(o.shock)
+    multigrid = False
+    restarts = 0
+    out = dict(status=0, rounds=0, bonds_broken=0, nodes_retired=0, solves=0, restarts=0, pcg_iters=0,
+               max_utilization=0.0, rel_res=0.0, broken=[], retired=[], per_round=[], phi=np.zeros(nb))
+    while True:
+        if not P.assembled() and not P.assemble(opt_mg if multigrid else opt):
+            out["status"] = 4
+            break
+        u0 = u.copy()
+        u, r = P.solve(f, u, o.rtol, o.maxit, True)
+        out["solves"] += 1
+        out["pcg_iters"] += r.iters
+        out["rel_res"] = r.rel_res
+        if r.breakdown:
+            u = u0
+            out["status"] = 3
+            break
+        if not r.converged:
+            rebuild = (not P.preconditioner_current()) or P.block_jacobi()
+            diverging = not (r.rel_res < 10.0)
+            if diverging:
+                u = u0
+            if rebuild:
+                P.invalidate()
+                multigrid = True
+            elif diverging:
+                u = np.zeros_like(u)
+            restarts += 1
+            out["restarts"] += 1
+            if restarts >= o.solve_restarts:
+                out["status"] = 2
+                break
+            continue
+        restarts = 0
+        if r.iters > o.rebuild_after and ((not P.preconditioner_current()) or P.block_jacobi()):
+            P.invalidate()
+        broken, _ = P.bond_flags()
+        live = broken == 0
+        loads, _, _ = P.judge(u, o.fragility)
+        le = loads.copy()
+        if shock and o.dif != 1.0:
+            w = live & (has != 0)
+            for k in LOAD_FIELDS:
+                le[k][w] = judged[k][w] + o.dif * (loads[k][w] - judged[k][w])
+        phi, _ = P.utilization_many(le, o.fragility)
+        judged[live] = loads[live]
+        has[live] = 1
+        phi = np.where(live, phi, 0.0)
+        out["phi"] = phi
+        mx = 0.0
+        for v in phi[live]:
+            mx = v if mx < v else mx
+        out["max_utilization"] = float(mx)
+        over = np.nonzero(live & (phi >= 1.0))[0]
+        if len(over) == 0:
+            out["status"] = 0
+            break
+        if out["rounds"] >= o.max_rounds:
+            out["status"] = 1
+            break
+        sel = select_breaks(over, phi[over], o.break_band, o.max_breaks_per_round)
+        for b in sel:
+            P.remove_bond(b)
+        out["broken"].extend(sel)
+        out["per_round"].append(len(sel))
+        out["bonds_broken"] += len(sel)
+        out["rounds"] += 1
+        shock = True
+        if o.detach:
+            broken, _ = P.bond_flags()
+            held = supported_nodes(n, P.bonds, broken)
+            ret = np.nonzero(~held & (gone == 0))[0].astype(np.int32)
+            if len(ret):
+                P.retire_nodes(ret)
+                gone[ret] = 1
+                for q in range(6):
+                    f[6 * ret + q] = 0.0
+                    u[6 * ret + q] = 0.0
+                out["retired"].extend(int(i) for i in ret)
+                out["nodes_retired"] += len(ret)
+    out.update(u=u, f=f, judged=judged, has=has)
+    return out

@@ -356,4 +356,96 @@ void svxr_hier_get(void* hp, int32_t l, int32_t* rowptr, int32_t* col, double* v
 
 void svxr_hier_free(void* hp) { delete static_cast<Hier*>(hp); }
 
+
+// ---- one problem kept between calls (the judge's break rounds drive it: remove_bond,
+// retire_nodes and solve on the same K, as World::Impl::judge does, core/src/world/world.cpp:1162-1277)
+
+struct RefProblem {
+  MaterialTable table;
+  StressProblem P;
+};
+
+void* svxr_p_create(const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb, const svxg_material* mats) {
+  RefProblem* h = new RefProblem;
+  fill_materials(h->table, mats);
+  h->P.mats = &h->table;
+  fill_problem(h->P, nodes, n, bonds, nb);
+  return h;
+}
+
+void svxr_p_destroy(void* h) { delete static_cast<RefProblem*>(h); }
+
+int svxr_p_assemble(void* h, const svxg_stress_options* o) { return static_cast<RefProblem*>(h)->P.assemble(options(o)) ? 1 : 0; }
+int svxr_p_assembled(void* h) { return static_cast<RefProblem*>(h)->P.assembled() ? 1 : 0; }
+void svxr_p_invalidate(void* h) { static_cast<RefProblem*>(h)->P.invalidate(); }
+int svxr_p_preconditioner_current(void* h) { return static_cast<RefProblem*>(h)->P.preconditioner_current() ? 1 : 0; }
+int svxr_p_block_jacobi(void* h) { return static_cast<RefProblem*>(h)->P.block_jacobi() ? 1 : 0; }
+
+void svxr_p_solve(void* h, const double* f, double* u, double rtol, int32_t maxit, int32_t warm, svxg_pcg_result* res) {
+  StressProblem& P = static_cast<RefProblem*>(h)->P;
+  const size_t m = 6 * P.nodes.size();
+  std::vector<f64> fv(f, f + m), uv(u, u + m);
+  const PcgResult r = P.solve(fv, uv, rtol, maxit, warm != 0);
+  std::memcpy(u, uv.data(), sizeof(double) * m);
+  res->iters = r.iters;
+  res->converged = r.converged;
+  res->breakdown = r.breakdown;
+  res->rel_res = r.rel_res;
+}
+
+void svxr_p_remove_bond(void* h, int32_t b) { static_cast<RefProblem*>(h)->P.remove_bond(b); }
+
+void svxr_p_retire_nodes(void* h, const int32_t* list, int32_t count) {
+  static_cast<RefProblem*>(h)->P.retire_nodes(std::vector<i32>(list, list + count));
+}
+
+void svxr_p_bond_flags(void* h, uint8_t* broken, uint8_t* in_k) {
+  const StressProblem& P = static_cast<RefProblem*>(h)->P;
+  for (size_t k = 0; k < P.bonds.size(); ++k) {
+    if (broken) broken[k] = P.bonds[k].broken ? 1 : 0;
+    if (in_k) in_k[k] = P.bonds[k].in_k ? 1 : 0;
+  }
+}
+
+void svxr_p_judge(void* h, const double* u, double fragility, svxg_bond_load* loads, double* phi, uint8_t* mode) {
+  RefProblem* R = static_cast<RefProblem*>(h);
+  const StressProblem& P = R->P;
+  std::vector<f64> uv(u, u + 6 * P.nodes.size());
+  for (size_t k = 0; k < P.bonds.size(); ++k) {
+    const BondLoad L = P.bond_load(static_cast<i32>(k), uv);
+    FailMode m = FailMode::None;
+    const f64 ph = bond_utilization(P.bonds[k], L, fragility, R->table, &m);
+    if (loads) loads[k] = svxg_bond_load{L.N, L.V1, L.V2, L.T, L.M1, L.M2};
+    if (phi) phi[k] = ph;
+    if (mode) mode[k] = static_cast<uint8_t>(m);
+  }
+}
+
+// bond_utilization of every bond of the problem under the given loads (one per bond)
+void svxr_p_utilization_many(void* h, const svxg_bond_load* loads, double fragility, double* phi, uint8_t* mode) {
+  RefProblem* R = static_cast<RefProblem*>(h);
+  const StressProblem& P = R->P;
+  for (size_t k = 0; k < P.bonds.size(); ++k) {
+    BondLoad l;
+    l.N = loads[k].N;
+    l.V1 = loads[k].V1;
+    l.V2 = loads[k].V2;
+    l.T = loads[k].T;
+    l.M1 = loads[k].M1;
+    l.M2 = loads[k].M2;
+    FailMode m = FailMode::None;
+    phi[k] = bond_utilization(P.bonds[k], l, fragility, R->table, &m);
+    if (mode) mode[k] = static_cast<uint8_t>(m);
+  }
+}
+
+void svxr_p_matrix(void* h, int32_t* nfree, int64_t* nnzb, int32_t* rowptr, int32_t* col, double* val) {
+  const StressProblem& P = static_cast<RefProblem*>(h)->P;
+  *nfree = P.K_.n;
+  *nnzb = static_cast<int64_t>(P.K_.col.size());
+  if (rowptr) std::memcpy(rowptr, P.K_.rowptr.data(), sizeof(int32_t) * P.K_.rowptr.size());
+  if (col) std::memcpy(col, P.K_.col.data(), sizeof(int32_t) * P.K_.col.size());
+  if (val) std::memcpy(val, P.K_.val.data(), sizeof(double) * P.K_.val.size());
+}
+
 }  // extern "C"

@@ -1473,6 +1473,24 @@ void svxo_judge(const svxo_problem* P, const double* u, double fragility, svxg_b
   }
 }
 
+/* bond_utilization of every bond of the problem under the given loads (one per bond) */
+void svxo_utilization_many(const svxo_problem* P, const svxg_bond_load* loads, double fragility, double* phi,
+                           uint8_t* mode) {
+  for (int32_t k = 0; k < P->nb; ++k) {
+    uint8_t md = 0;
+    phi[k] = utilization(&P->bonds[k], &loads[k], fragility, P->mats, &md);
+    if (mode) mode[k] = md;
+  }
+}
+
+/* StressProblem::invalidate / assembled / preconditioner_current (stress.hpp:83-91) */
+void svxo_invalidate(svxo_problem* P) {
+  P->assembled = 0;
+  P->active = 0;
+}
+int svxo_assembled(const svxo_problem* P) { return P->assembled; }
+int svxo_preconditioner_current(const svxo_problem* P) { return P->assembled && P->pc_current; }
+
 void svxo_get_info(const svxo_problem* P, svxo_info* info) {
   memset(info, 0, sizeof(*info));
   info->nfree = P->nfree;

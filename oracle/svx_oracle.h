@@ -61,6 +61,14 @@ void svxo_judge(const svxo_problem* P, const double* u, double fragility, svxg_b
 double svxo_utilization(const svxg_bond* b, const svxg_bond_load* L, double fragility, const svxg_material* mats,
                         uint8_t* mode);
 
+/* bond_utilization of every bond under the given loads (one per bond). */
+void svxo_utilization_many(const svxo_problem* P, const svxg_bond_load* loads, double fragility, double* phi,
+                           uint8_t* mode);
+/* StressProblem::invalidate / assembled / preconditioner_current (stress.hpp:83-91). */
+void svxo_invalidate(svxo_problem* P);
+int svxo_assembled(const svxo_problem* P);
+int svxo_preconditioner_current(const svxo_problem* P);
+
 /* K (after svxo_assemble). rowptr: nfree + 1, col: nnzb, val: 36 nnzb, dof: n. */
 void svxo_matrix_dims(const svxo_problem* P, int32_t* nfree, int64_t* nnzb);
 void svxo_matrix(const svxo_problem* P, int32_t* dof, int32_t* rowptr, int32_t* col, double* val, double* id_scale);

@@ -7,6 +7,10 @@ work counters, and every bond's load, utilization and mode. tests/test_oracle_go
 oracle against them on any machine, bit for bit.
 
     python tests/golden/make_golden.py
+
+It also writes tests/golden/cascade/*.npz: the judge's break rounds of tests/cascade_cases.py
+run on the reference's own StressProblem (tests/test_oracle_golden.py checks the oracle's
+cascade against them bit for bit).
 """
 from __future__ import annotations
 
@@ -60,5 +64,32 @@ def main():
         print(name, len(nodes), len(bonds), r["res"], info.sizes())
 
 
+def cascades():
+    """tests/golden/cascade/<case>.npz: the break rounds of tests/cascade_cases.py run on the
+    reference's own StressProblem (oracle.RefProblem): inputs and every output."""
+    import cascade_cases as cc
+    from oracle import RefProblem, cascade
+    out_dir = os.path.join(HERE, "cascade")
+    os.makedirs(out_dir, exist_ok=True)
+    for name, (nodes, bonds, mats, f, ko, so, judged, has) in cc.cases().items():
+        R = RefProblem(nodes, bonds, mats)
+        o = cc.options(ko)
+        r = cascade(R, f, np.zeros(6 * len(nodes)), o, cc.stress_options(so), judged, has)
+        okeys = sorted(ko)
+        skeys = sorted(so)
+        np.savez_compressed(
+            os.path.join(out_dir, f"{name}.npz"), nodes=nodes, bonds=bonds, mats=mats, f=f,
+            judged_in=judged if judged is not None else np.zeros(0), has_in=has if has is not None else np.zeros(0),
+            okeys=np.array(okeys), ovals=np.array([float(ko[k]) for k in okeys]),
+            skeys=np.array(skeys, dtype=str), svals=np.array([float(so[k]) for k in skeys]),
+            u=r["u"], phi=r["phi"], judged=r["judged"], has=r["has"], broken=np.array(r["broken"], np.int32),
+            retired=np.array(r["retired"], np.int32), per_round=np.array(r["per_round"], np.int32),
+            counts=np.array([r["status"], r["rounds"], r["bonds_broken"], r["nodes_retired"], r["solves"],
+                             r["restarts"], r["pcg_iters"]], np.int64),
+            max_utilization=r["max_utilization"])
+        print("cascade", name, r["status"], r["rounds"], r["bonds_broken"], r["nodes_retired"])
+
+
 if __name__ == "__main__":
     main()
+    cascades()

@@ -29,3 +29,45 @@ def test_oracle_matches_reference_golden(path):
             i.build_work] == list(g["counters"])
     loads, phi, mode = P.judge(g["u"])
     assert np.array_equal(loads, g["loads"]) and np.array_equal(phi, g["phi"]) and np.array_equal(mode, g["mode"])
+
+
+import cascade_cases as cc  # noqa: E402
+from oracle import cascade  # noqa: E402
+
+CASCADE_FILES = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "cascade", "*.npz")))
+
+
+@pytest.mark.parametrize("path", CASCADE_FILES, ids=[os.path.basename(p)[:-4] for p in CASCADE_FILES])
+def test_oracle_cascade_matches_reference_golden(path):
+    """The break rounds on the C restatement against the same rounds run on the reference's own
+    StressProblem (golden/make_golden.py): bit for bit."""
+    nodes, bonds, mats, f, ko, so, judged, has, exp = cc.load_golden(path)
+    P = Port(nodes, bonds, mats)
+    r = cascade(P, f, np.zeros(6 * len(nodes)), cc.options(ko), cc.stress_options(so), judged, has)
+    for k in ("status", "rounds", "bonds_broken", "nodes_retired", "solves", "restarts", "pcg_iters", "broken",
+              "retired", "per_round", "max_utilization"):
+        assert r[k] == exp[k], k
+    assert np.array_equal(r["u"], exp["u"]) and np.array_equal(r["phi"], exp["phi"])
+    assert r["judged"].tobytes() == exp["judged"].tobytes() and np.array_equal(r["has"], exp["has"])
+
+
+def test_select_breaks_rules():
+    """The round's selection (world.cpp:1219-1271) on hand-made over-strength lists: phi
+    descending, index ascending on ties; everything at or over max(1, band x max); at least the
+    worst quarter; at most max_breaks."""
+    from oracle import select_breaks
+    b = np.array([3, 7, 9, 12, 20, 21, 30, 31], np.int64)
+    phi = np.array([1.2, 2.0, 1.0, 2.0, 1.9, 1.05, 1.1, 1.71])
+    # thr = max(1, 0.85 x 2.0) = 1.7: 7, 12 (ties by index), 20, 31
+    assert select_breaks(b, phi, 0.85, 256) == [7, 12, 20, 31]
+    assert select_breaks(b, phi, 0.85, 3) == [7, 12, 20]
+    # band 0.99: thr 1.98 -> 2 bonds, but the quota is (8 + 3) / 4 = 2
+    assert select_breaks(b, phi, 0.99, 256) == [7, 12]
+    # band 0.5: thr max(1, 1.0) = 1 -> every one
+    assert select_breaks(b, phi, 0.5, 256) == [7, 12, 20, 31, 3, 30, 21, 9]
+    # one over: one break
+    assert select_breaks(np.array([5]), np.array([1.0]), 0.85, 256) == [5]
+    # quota above the band: 9 over, thr picks 1, quota (9 + 3) / 4 = 3
+    b9 = np.arange(9)
+    p9 = np.array([1.0, 1.0, 5.0, 1.1, 1.2, 1.0, 1.0, 1.0, 1.3])
+    assert select_breaks(b9, p9, 0.85, 256) == [2, 8, 4]

@@ -96,3 +96,28 @@ def test_extend_warm_start_bit_identical():
         b = Reference(nodes, bonds, MATS).extend_warm_start(u, n_old)
         assert np.array_equal(a, b)
         assert np.any(a[6 * n_old:] != 0.0)
+
+
+import cascade_cases as cc  # noqa: E402
+from oracle import RefProblem, cascade  # noqa: E402
+
+CASCADES = cc.cases()
+
+
+@pytest.mark.parametrize("name", list(CASCADES), ids=list(CASCADES))
+def test_cascade_bit_identical(name):
+    """The break rounds (oracle.cascade) on the C restatement and on the reference's own
+    StressProblem: the same bonds broken in the same order, the same nodes retired, the same u,
+    judged loads and utilizations, bit for bit."""
+    nodes, bonds, mats, f, ko, so, judged, has = CASCADES[name]
+    out = []
+    for cls in (Port, RefProblem):
+        P = cls(nodes, bonds, mats)
+        out.append(cascade(P, f, np.zeros(6 * len(nodes)), cc.options(ko), cc.stress_options(so), judged, has))
+    a, b = out
+    assert a["rounds"] > 0 or a["bonds_broken"] == 0
+    for k in ("status", "rounds", "bonds_broken", "nodes_retired", "solves", "restarts", "pcg_iters", "broken",
+              "retired", "per_round", "max_utilization"):
+        assert a[k] == b[k], k
+    assert np.array_equal(a["u"], b["u"]) and np.array_equal(a["phi"], b["phi"])
+    assert a["judged"].tobytes() == b["judged"].tobytes() and np.array_equal(a["has"], b["has"])
