@@ -20,6 +20,7 @@ Launch: python bench.py [--gpus N --steps K --warmup W] (N > 1 under torchrun: o
 GPU, each solving its own seeded city block; value = all ranks' solves / the slowest rank's time).
 --workload batch | serve runs the batched solve or the serving loop instead (one JSON line with
 solves/s, latency percentiles and the plain FP64 per-request rate on the same requests).
+--workload cascade runs the judge's break rounds of the city block (svxg_cascade) per step.
 --impl reference times the reference's CPU implementation of the path (the oracle port on every
 host thread) on the same workload and prints the same JSON line.
 """
@@ -225,13 +226,93 @@ def run_many(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
+def run_cascade(args, rank: int, world: int):
+    """The judge's break rounds of the city block (svxg_cascade): one step = assemble + every round
+    (solve warm, judge, break, retire what falls) until nothing is over strength, from the same
+    intact city each step, through the C ABI with host buffers. value = solves/s inside the
+    cascade; the CPU baseline runs the oracle's restatement of the same rounds (bounded: the first
+    rounds) on the host's cores and must break the same bonds."""
+    import torch
+    from opus_destruct_2_gb300 import StressProblem, load_library
+    from opus_destruct_2_gb300.graph import CascadeOptions, StressOptions
+    if world > 1:
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    L = load_library()
+    from opus_destruct_2_gb300 import synth
+    nodes, bonds, f, mats = synth.city_graph(lots_x=args.lots, lots_y=args.lots, seed=args.seed + rank)
+    opt = StressOptions()
+    o = CascadeOptions(rtol=args.rtol, fragility=args.fragility, maxit=args.maxit)
+
+    def step():
+        G = StressProblem(nodes, bonds, mats)
+        t0 = time.perf_counter()
+        if not G.assemble(opt):
+            raise RuntimeError("assemble: singular")
+        u, res, ex = G.cascade(f, options=o, opt=opt)
+        return time.perf_counter() - t0, res, ex
+
+    for _ in range(args.warmup):
+        step()
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    launches0 = L.svxg_launch_count()
+    walls, last = [], None
+    for _ in range(args.steps):
+        w, res, ex = step()
+        walls.append(w)
+        last = (res, ex)
+    launches = L.svxg_launch_count() - launches0
+    clk = clocks.stop()
+    res, ex = last
+    wall = max(walls)
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:
+        import oracle
+        oracle.set_threads(os.cpu_count() or 1)
+        rounds = 2
+        P = oracle.Port(nodes, bonds, mats)
+        t0 = time.perf_counter()
+        P.assemble(opt)
+        ro = oracle.cascade(P, f, np.zeros(6 * len(nodes)), CascadeOptions(rtol=args.rtol, fragility=args.fragility,
+                                                                            maxit=args.maxit, max_rounds=rounds), opt)
+        tc = time.perf_counter() - t0
+        k = len(ro["broken"])
+        cpu = {"value": ro["solves"] / tc, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"assemble + the first {rounds} rounds ({ro['solves']} solves, {k} bonds) of the same "
+                         f"cascade, oracle restatement (C, OpenMP)",
+               "wall_s": tc, "same_breaks_as_device": ex["broken"][:k] == ro["broken"]}
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": world * res.solves / wall, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"cascade: judge break rounds of the {args.lots}x{args.lots} city block (seeded towers "
+                               f"of 5-40 storeys, four materials), gravity, fragility {args.fragility:g}, rtol "
+                               f"{args.rtol:g}, {args.maxit} iterations a solve, world defaults (band 0.85, 256 "
+                               f"breaks a round, rebuild after 60 iterations on a stale preconditioner)",
+                   "nodes": int(len(nodes)), "bonds": int(len(bonds)),
+                   "step": "assemble + the whole cascade, host buffers in and out"},
+        "cascade": {"status": int(res.status), "rounds": int(res.rounds), "bonds_broken": int(res.bonds_broken),
+                    "nodes_retired": int(res.nodes_retired), "solves": int(res.solves),
+                    "restarts": int(res.restarts), "pcg_iters": int(res.pcg_iters),
+                    "ms_per_round": 1e3 * wall / max(1, res.rounds), "walls_s": walls},
+        "roofline": None, "gpu_launches": int(launches / max(1, args.steps)),
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    if clk is not None:
+        line["clocks"] = clk
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["city", "tower", "batch", "serve"], default="city")
+    ap.add_argument("--workload", choices=["city", "tower", "batch", "serve", "cascade"], default="city")
+    ap.add_argument("--fragility", type=float, default=1.0, help="cascade: strength divisor")
     ap.add_argument("--requests", type=int, default=20000, help="serve: requests in the stream")
     ap.add_argument("--rate", type=float, default=5000.0, help="serve: Poisson arrival rate (requests/s)")
     ap.add_argument("--graphs", type=int, default=512, help="batch: graphs")
@@ -254,6 +335,9 @@ def main():
         return
     if args.workload in ("batch", "serve"):
         run_many(args, rank, world)
+        return
+    if args.workload == "cascade":
+        run_cascade(args, rank, world)
         return
 
     import torch
