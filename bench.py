@@ -305,13 +305,103 @@ def run_cascade(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
+def run_sections(args, rank: int, world: int):
+    """Graph construction from voxels: the city block's bonds from its voxel-face interfaces
+    (svxg_build_bonds: SecAcc::finish_lattice + section_strengths on the device). One step = every
+    bond of the city; value = bonds/s with the interfaces resident (CUDA events on the launching
+    stream), e2e = bonds/s through the C ABI with host arrays in and out; the CPU baseline is the
+    oracle's restatement (one thread) on the same interfaces, which must give the same bytes."""
+    import torch
+    from opus_destruct_2_gb300 import build_bonds, load_library, synth
+    from opus_destruct_2_gb300.graph import BOND_DTYPE
+    L = load_library()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    nodes, _, _, mats = synth.city_graph(lots_x=args.lots, lots_y=args.lots, seed=args.seed + rank)
+    secs, faces = synth.last_sections()
+    nb, nf = len(secs), len(faces)
+    t = {k: torch.from_numpy(np.frombuffer(v.tobytes(), np.uint8).copy()).to(dev)
+         for k, v in dict(nodes=nodes, secs=secs, faces=faces, mats=mats).items()}
+    out = torch.zeros(nb * BOND_DTYPE.itemsize, dtype=torch.uint8, device=dev)
+    flush = torch.empty(2 * L2_BYTES, dtype=torch.uint8, device=dev)
+    st = torch.cuda.current_stream(dev)
+
+    def launch():
+        rc = L.svxg_build_bonds_device(ctypes.c_void_p(t["nodes"].data_ptr()), len(nodes),
+                                       ctypes.c_void_p(t["secs"].data_ptr()), nb, ctypes.c_void_p(t["faces"].data_ptr()),
+                                       nf, ctypes.c_void_p(t["mats"].data_ptr()), ctypes.c_void_p(out.data_ptr()), None,
+                                       ctypes.c_void_p(st.cuda_stream))
+        if rc:
+            raise RuntimeError(L.svxg_last_error().decode())
+
+    for _ in range(args.warmup):
+        launch()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    launches0 = L.svxg_launch_count()
+    ms = []
+    for _ in range(args.steps):
+        flush.zero_()  # (L2 flushed between steps)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        launch()
+        e1.record(st)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    launches = L.svxg_launch_count() - launches0
+    clk = clocks.stop()
+    kernel_ms = statistics.median(ms)
+    got = np.frombuffer(out.cpu().numpy().tobytes(), dtype=BOND_DTYPE)
+    # end to end: host arrays in and out
+    build_bonds(nodes, secs, faces, mats)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        built = build_bonds(nodes, secs, faces, mats)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    cpu = None
+    if not args.no_cpu_baseline:
+        import oracle
+        t0 = time.perf_counter()
+        want = oracle.build_bonds(nodes, secs, faces, mats)
+        tc = time.perf_counter() - t0
+        same = all(np.ascontiguousarray(got[k]).tobytes() == np.ascontiguousarray(want[k]).tobytes()
+                   for k in BOND_DTYPE.names)
+        cpu = {"value": nb / tc, "unit": "bonds/s", "cores": 1, "kind": "port",
+               "sample": "every bond of the same city, oracle restatement (C, one thread)", "same_bytes": bool(same)}
+    algo = nb * (56 + BOND_DTYPE.itemsize + 2 * 40) + nf * 20
+    peaks = measured_peaks()
+    achieved = algo / (kernel_ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": nb / (kernel_ms / 1e3), "unit": "bonds/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"sections: the bonds of the {args.lots}x{args.lots} city block from its voxel-face "
+                               f"interfaces (SecAcc::finish_lattice + section_strengths), L2 flushed between steps",
+                   "bonds": int(nb), "faces": int(nf)},
+        "e2e": {"value": nb / e2e_s, "unit": "bonds/s", "h2d_bytes_per_step": int(nodes.nbytes + secs.nbytes +
+                                                                                   faces.nbytes + mats.nbytes),
+                "d2h_bytes_per_step": int(built.nbytes)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs"), "unit": "GB/s",
+                     "frac": achieved / peaks["hbm_gbs"] if peaks.get("hbm_gbs") else None, "traffic": None,
+                     "algorithmic_bytes": int(algo)},
+        "gpu_launches": int(launches / max(1, args.steps)),
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    if clk is not None:
+        line["clocks"] = clk
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["city", "tower", "batch", "serve", "cascade"], default="city")
+    ap.add_argument("--workload", choices=["city", "tower", "batch", "serve", "cascade", "sections"], default="city")
     ap.add_argument("--fragility", type=float, default=1.0, help="cascade: strength divisor")
     ap.add_argument("--requests", type=int, default=20000, help="serve: requests in the stream")
     ap.add_argument("--rate", type=float, default=5000.0, help="serve: Poisson arrival rate (requests/s)")
@@ -338,6 +428,9 @@ def main():
         return
     if args.workload == "cascade":
         run_cascade(args, rank, world)
+        return
+    if args.workload == "sections":
+        run_sections(args, rank, world)
         return
 
     import torch

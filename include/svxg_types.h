@@ -112,6 +112,36 @@ typedef struct svxg_bond_load {
 
 enum { SVXG_FAIL_NONE = 0, SVXG_FAIL_TENSION = 1, SVXG_FAIL_CRUSH = 2, SVXG_FAIL_SHEAR = 3 };
 
+/* A bond's interface before it is a bond: the world's accumulator of the voxel faces two
+ * fragments share (all axes), or of one fragment's faces on a support along one axis
+ * (SecHead / SecAcc, core/src/world/world_internal.hpp:106-128). Its faces are
+ * faces[first_face .. first_face + faces). */
+typedef struct svxg_section {
+  int32_t a, b;          /* nodes; b < 0: a support */
+  int64_t first_face;
+  int32_t faces;
+  uint8_t axis;          /* a support's face axis (0..2) */
+  int8_t sign;           /* a support's side of a: the normal from a to the support is sign e_axis */
+  uint8_t ma, mb;        /* materials of the two sides (a support's: its own) */
+  uint8_t sectioned;     /* 1: strengths from the faces' voxels (section_strengths) */
+  uint8_t pad[7];
+  double h;              /* voxel size of the faces' lattice (m) */
+  double strength_a, strength_b;  /* the two sides' strength multipliers */
+} svxg_section;
+
+/* One voxel face of an interface: the face between voxel (x, y, z) of the lattice and its
+ * +axis neighbour; sign +1 when a is on the lower side. The two voxels as the world stores them
+ * (core/include/svx/world/grid.hpp:27-38: 0 air, else material id + 1 in the low 7 bits) and
+ * their damage (0 intact .. 255 no strength left). */
+typedef struct svxg_face {
+  int32_t x, y, z;
+  uint8_t axis;
+  int8_t sign;
+  uint8_t vox_lo, vox_hi;
+  uint8_t damage_lo, damage_hi;
+  uint8_t pad[2];
+} svxg_face;
+
 /* The judge's break rounds of one structure: World::Impl::judge (core/src/world/world.cpp:1162-1277)
  * with the solve restarts of World::Impl's tick (world.cpp:1041-1110) and detach_unsupported
  * (world.cpp:1371-1458, graph_components world_internal.hpp:660-705). Defaults: WorldConfig and

@@ -21,7 +21,7 @@ from .graph import (BOND_DTYPE, LOAD_DTYPE, MATERIAL_DTYPE, NODE_DTYPE, CascadeO
                     StressOptions, default_materials, ptr)
 
 __all__ = ["StressProblem", "StressOptions", "PcgResult", "Info", "load_library", "default_materials",
-           "NODE_DTYPE", "BOND_DTYPE", "SvxgError", "CascadeOptions", "CascadeResult"]
+           "NODE_DTYPE", "BOND_DTYPE", "SvxgError", "CascadeOptions", "CascadeResult", "build_bonds"]
 
 c_i32, c_i64, c_f64, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p
 
@@ -106,6 +106,8 @@ def load_library() -> ctypes.CDLL:
         "svxg_timer_enable": (c_i32, [c_vp, c_i32]),
         "svxg_timer_read": (c_i32, [c_vp, ctypes.POINTER(c_f64), ctypes.POINTER(c_i64)]),
         "svxg_cascade": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp, c_i32, c_vp]),
+        "svxg_build_bonds": (c_i32, [c_vp, c_i32, c_vp, c_i32, c_vp, c_i64, c_vp, c_vp]),
+        "svxg_build_bonds_device": (c_i32, [c_vp, c_i32, c_vp, c_i32, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -120,6 +122,22 @@ def _check(code: int) -> int:
         msg = load_library().svxg_last_error()
         raise SvxgError(code, msg.decode() if msg else "")
     return code
+
+
+def build_bonds(nodes, secs, faces, mats=None) -> np.ndarray:
+    """The bonds of voxel-face interfaces on the GPU (SecAcc::finish_lattice + section_strengths,
+    core/src/world/world_internal.hpp:133-232, :370-399): bond k from secs[k] (SECTION_DTYPE) and
+    its faces (FACE_DTYPE). Returns BOND_DTYPE records."""
+    from .graph import FACE_DTYPE, SECTION_DTYPE
+    L = load_library()
+    nodes = np.ascontiguousarray(nodes, dtype=NODE_DTYPE)
+    secs = np.ascontiguousarray(secs, dtype=SECTION_DTYPE)
+    faces = np.ascontiguousarray(faces, dtype=FACE_DTYPE)
+    mats = np.ascontiguousarray(default_materials() if mats is None else mats, dtype=MATERIAL_DTYPE)
+    out = np.zeros(len(secs), BOND_DTYPE)
+    _check(L.svxg_build_bonds(ptr(nodes), len(nodes), ptr(secs), len(secs), ptr(faces), len(faces), ptr(mats),
+                              ptr(out)))
+    return out
 
 
 class StressProblem:

@@ -1117,4 +1117,79 @@ int svxg_cascade(svxg_problem* p, const svxg_stress_options* opt, const svxg_cas
   return SVXG_OK;
 }
 
+
+// SecAcc::finish_lattice + section_strengths (core/src/world/world_internal.hpp:133-232,
+// :370-399) on the device: host arrays in and out.
+int svxg_build_bonds(const svxg_node* nodes, int32_t n, const svxg_section* secs, int32_t nb, const svxg_face* faces,
+                     int64_t nf, const svxg_material* mats, svxg_bond* out) {
+  if (n < 0 || nb < 0 || nf < 0 || (nb > 0 && (!nodes || !secs || !mats || !out)) || (nf > 0 && !faces)) {
+    set_error("svxg_build_bonds: bad arguments");
+    return SVXG_ERR_ARG;
+  }
+  for (int32_t k = 0; k < nb; ++k) {
+    const svxg_section& S = secs[k];
+    if (S.a < 0 || S.a >= n || S.b >= n || S.faces < 0 || S.first_face < 0 || S.first_face + S.faces > nf ||
+        (S.b < 0 && S.axis > 2)) {
+      set_error("svxg_build_bonds: section " + std::to_string(k) + " out of range");
+      return SVXG_ERR_ARG;
+    }
+  }
+  for (int64_t f = 0; f < nf; ++f)
+    if (faces[f].axis > 2) {
+      set_error("svxg_build_bonds: face axis out of range");
+      return SVXG_ERR_ARG;
+    }
+  if (nb == 0) return SVXG_OK;
+  int dev = 0;
+  SVXG_CUDA(cudaGetDevice(&dev));
+  DeviceScope ds(dev);
+  cudaStream_t st = cudaStreamPerThread;
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+  const size_t bn = up(sizeof(svxg_node) * size_t(std::max(n, 1))), bs = up(sizeof(svxg_section) * size_t(nb)),
+               bf = up(sizeof(svxg_face) * size_t(std::max<int64_t>(nf, 1))),
+               bm = up(sizeof(svxg_material) * SVXG_MAX_MATERIALS), bo = up(sizeof(svxg_bond) * size_t(nb));
+  char* base = nullptr;
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&base), bn + bs + bf + bm + bo + 256, st));
+  svxg_node* dn = reinterpret_cast<svxg_node*>(base);
+  svxg_section* dsec = reinterpret_cast<svxg_section*>(base + bn);
+  svxg_face* dfc = reinterpret_cast<svxg_face*>(base + bn + bs);
+  svxg_material* dm = reinterpret_cast<svxg_material*>(base + bn + bs + bf);
+  svxg_bond* dout = reinterpret_cast<svxg_bond*>(base + bn + bs + bf + bm);
+  int32_t* dbad = reinterpret_cast<int32_t*>(base + bn + bs + bf + bm + bo);
+  int e = SVXG_OK;
+  int32_t bad = 0;
+  do {
+    if (n > 0 && cudaMemcpyAsync(dn, nodes, sizeof(svxg_node) * size_t(n), cudaMemcpyHostToDevice, st)) break;
+    if (cudaMemcpyAsync(dsec, secs, sizeof(svxg_section) * size_t(nb), cudaMemcpyHostToDevice, st)) break;
+    if (nf > 0 && cudaMemcpyAsync(dfc, faces, sizeof(svxg_face) * size_t(nf), cudaMemcpyHostToDevice, st)) break;
+    if (cudaMemcpyAsync(dm, mats, sizeof(svxg_material) * SVXG_MAX_MATERIALS, cudaMemcpyHostToDevice, st)) break;
+    if (cudaMemsetAsync(dbad, 0, sizeof(int32_t), st)) break;
+    e = build_bonds_device(dn, n, dsec, nb, dfc, nf, dm, dout, dbad, st);
+    if (e) break;
+    if (cudaMemcpyAsync(out, dout, sizeof(svxg_bond) * size_t(nb), cudaMemcpyDeviceToHost, st)) break;
+    if (cudaMemcpyAsync(&bad, dbad, sizeof(int32_t), cudaMemcpyDeviceToHost, st)) break;
+  } while (0);
+  cudaError_t ce = cudaGetLastError();
+  cudaFreeAsync(base, st);
+  SVXG_CUDA(host_wait(st));
+  if (e) return e;
+  if (ce != cudaSuccess) {
+    set_error(std::string("svxg_build_bonds: ") + cudaGetErrorString(ce));
+    return SVXG_ERR_CUDA;
+  }
+  return bad ? SVXG_ERR_ARG : SVXG_OK;
+}
+
+int svxg_build_bonds_device(const svxg_node* nodes_dev, int32_t n, const svxg_section* secs_dev, int32_t nb,
+                            const svxg_face* faces_dev, int64_t nf, const svxg_material* mats_dev, svxg_bond* out_dev,
+                            int32_t* n_bad_dev, void* stream) {
+  if (n < 0 || nb < 0 || nf < 0 || (nb > 0 && (!nodes_dev || !secs_dev || !mats_dev || !out_dev)) ||
+      (nf > 0 && !faces_dev)) {
+    set_error("svxg_build_bonds_device: bad arguments");
+    return SVXG_ERR_ARG;
+  }
+  return build_bonds_device(nodes_dev, n, secs_dev, nb, faces_dev, nf, mats_dev, out_dev, n_bad_dev,
+                            static_cast<cudaStream_t>(stream));
+}
+
 }  // extern "C"

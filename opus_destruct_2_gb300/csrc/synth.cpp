@@ -62,6 +62,9 @@ struct Graph {
   std::vector<svxg_node> nodes;
   std::vector<svxg_bond> bonds;
   std::vector<double> f;
+  // the same bonds as interfaces of voxel faces (the section-geometry path)
+  std::vector<svxg_section> secs;
+  std::vector<svxg_face> faces;
 };
 
 // Tower frame: storeys of `hs` voxels, slabs `ts` thick, a perimeter wall two voxels thick with
@@ -441,6 +444,83 @@ void fragment(const Grid& G, const MatProps& M, Rng& R, Graph& g) {
   }
   for (auto& v : per)
     for (auto& s : v) g.bonds.push_back(s);
+  // The interfaces of the same bonds (in the same order) as the world accumulates them: every
+  // face two fragments share, of any axis, in scan order; a grounded fragment's faces on the
+  // ground below it. Voxel damage: one voxel in eight, 1-200, from its own seeded stream (the
+  // graph's stream is left as it was).
+  const int ix0 = int(std::lround(G.ox / kVoxel)), iy0 = int(std::lround(G.oy / kVoxel));
+  Rng D(0x5EC7u ^ (uint64_t(uint32_t(base)) << 20) ^ (uint64_t(G.nx) << 8) ^ uint64_t(G.nz));
+  std::vector<uint8_t> dmg(nvox, 0);
+  for (size_t v = 0; v < nvox; ++v)
+    if (G.occ[v] && D.integer(0, 7) == 0) dmg[v] = uint8_t(D.integer(1, 200));
+  const uint8_t vox = uint8_t(G.mat + 1);
+  const uint8_t rock_vox = uint8_t((5 + 1) | 0x80);  // (rock, anchored)
+  std::vector<std::vector<svxg_face>> sup(static_cast<size_t>(nf));
+  std::map<std::pair<int32_t, int32_t>, std::vector<svxg_face>> acc;
+  for (int z = 0; z < G.nz; ++z)
+    for (int y = 0; y < G.ny; ++y)
+      for (int x = 0; x < G.nx; ++x) {
+        const size_t v = G.at(x, y, z);
+        const int32_t a = frag[v];
+        if (a < 0) continue;
+        if (z == 0 && G.grounded) {
+          svxg_face fc;
+          std::memset(&fc, 0, sizeof(fc));
+          fc.x = x + ix0;
+          fc.y = y + iy0;
+          fc.z = -1;
+          fc.axis = 2;
+          fc.sign = -1;
+          fc.vox_lo = rock_vox;
+          fc.vox_hi = vox;
+          fc.damage_hi = dmg[v];
+          sup[size_t(a)].push_back(fc);
+        }
+        for (int ax = 0; ax < 3; ++ax) {
+          const int p = x + (ax == 0), q = y + (ax == 1), r = z + (ax == 2);
+          if (!G.on(p, q, r)) continue;
+          const size_t w = G.at(p, q, r);
+          const int32_t b = frag[w];
+          if (b == a) continue;
+          svxg_face fc;
+          std::memset(&fc, 0, sizeof(fc));
+          fc.x = x + ix0;
+          fc.y = y + iy0;
+          fc.z = z;
+          fc.axis = uint8_t(ax);
+          fc.sign = a < b ? 1 : -1;
+          fc.vox_lo = vox;
+          fc.vox_hi = vox;
+          fc.damage_lo = dmg[v];
+          fc.damage_hi = dmg[w];
+          acc[a < b ? std::make_pair(a, b) : std::make_pair(b, a)].push_back(fc);
+        }
+      }
+  auto emit = [&](int32_t a, int32_t b, const std::vector<svxg_face>& fs) {
+    svxg_section sc;
+    std::memset(&sc, 0, sizeof(sc));
+    sc.a = base + a;
+    sc.b = b >= 0 ? base + b : -1;
+    sc.first_face = int64_t(g.faces.size());
+    sc.faces = int32_t(fs.size());
+    sc.axis = 2;
+    sc.sign = -1;
+    sc.ma = G.mat;
+    sc.mb = b >= 0 ? G.mat : uint8_t(5);
+    sc.sectioned = 1;
+    sc.h = kVoxel;
+    sc.strength_a = 1.0;
+    sc.strength_b = b >= 0 ? 1.0 : 1e9;  // (the anchored side never governs)
+    g.secs.push_back(sc);
+    g.faces.insert(g.faces.end(), fs.begin(), fs.end());
+  };
+  {
+    auto it = acc.begin();
+    for (int32_t a = 0; a < nf; ++a) {
+      if (!sup[size_t(a)].empty()) emit(a, -1, sup[size_t(a)]);
+      for (; it != acc.end() && it->first.first == a; ++it) emit(a, it->first.second, it->second);
+    }
+  }
 }
 
 // Loads of a free piece: its rigid acceleration under gravity and the impact taken out of every
@@ -588,6 +668,15 @@ void svxs_get(void* hp, svxg_node* nodes, svxg_bond* bonds, double* f) {
   if (nodes) std::memcpy(nodes, g.nodes.data(), sizeof(svxg_node) * g.nodes.size());
   if (bonds) std::memcpy(bonds, g.bonds.data(), sizeof(svxg_bond) * g.bonds.size());
   if (f) std::memcpy(f, g.f.data(), sizeof(double) * g.f.size());
+}
+
+int32_t svxs_num_sections(void* hp) { return int32_t(static_cast<Handle*>(hp)->g.secs.size()); }
+int64_t svxs_num_faces(void* hp) { return int64_t(static_cast<Handle*>(hp)->g.faces.size()); }
+
+void svxs_get_sections(void* hp, svxg_section* secs, svxg_face* faces) {
+  const Graph& g = static_cast<Handle*>(hp)->g;
+  if (secs) std::memcpy(secs, g.secs.data(), sizeof(svxg_section) * g.secs.size());
+  if (faces) std::memcpy(faces, g.faces.data(), sizeof(svxg_face) * g.faces.size());
 }
 
 void svxs_free(void* hp) { delete static_cast<Handle*>(hp); }

@@ -18,8 +18,8 @@ import os
 import numpy as np
 
 from . import build as _build
-from .graph import (BOND_DTYPE, CONCRETE, MASONRY, NODE_DTYPE, RC, STEEL, WOOD, default_materials, ptr,
-                    register_material)
+from .graph import (BOND_DTYPE, CONCRETE, FACE_DTYPE, MASONRY, NODE_DTYPE, RC, SECTION_DTYPE, STEEL, WOOD,
+                    default_materials, ptr, register_material)
 
 
 class _Mat(ctypes.Structure):
@@ -46,6 +46,10 @@ def lib() -> ctypes.CDLL:
         L.svxs_num_bonds.argtypes = [vp]
         L.svxs_get.argtypes = [vp, vp, vp, vp]
         L.svxs_free.argtypes = [vp]
+        L.svxs_num_sections.argtypes = [vp]
+        L.svxs_num_faces.restype = ctypes.c_int64
+        L.svxs_num_faces.argtypes = [vp]
+        L.svxs_get_sections.argtypes = [vp, vp, vp]
         _lib = L
     return _lib
 
@@ -56,6 +60,9 @@ def _mat(table: np.ndarray, mid: int) -> _Mat:
                 float(m["friction"]), mid, 0)
 
 
+_last_sections = None
+
+
 def _take(h):
     L = lib()
     n, nb = L.svxs_num_nodes(h), L.svxs_num_bonds(h)
@@ -63,8 +70,19 @@ def _take(h):
     bonds = np.zeros(nb, BOND_DTYPE)
     f = np.zeros(6 * n)
     L.svxs_get(h, ptr(nodes), ptr(bonds), ptr(f))
+    global _last_sections
+    secs = np.zeros(L.svxs_num_sections(h), SECTION_DTYPE)
+    faces = np.zeros(L.svxs_num_faces(h), FACE_DTYPE)
+    L.svxs_get_sections(h, ptr(secs), ptr(faces))
+    _last_sections = (secs, faces)
     L.svxs_free(h)
     return nodes, bonds, f
+
+
+def last_sections():
+    """The interfaces (SECTION_DTYPE, FACE_DTYPE) of the graph the last generator call made: its
+    bonds' voxel faces, one section per bond in the same order."""
+    return _last_sections
 
 
 def tower_graph(storeys: int = 10, wx: int = 16, wy: int = 16, seed: int = 1, material: int = RC):

@@ -68,6 +68,7 @@ def build_reference(force: bool = False) -> str | None:
     os.makedirs(objdir, exist_ok=True)
     flags = ["g++", "-std=c++20", "-O3", "-DNDEBUG", "-ffp-contract=off", "-fno-fast-math", "-fno-exceptions",
              "-fno-rtti", "-fPIC", "-pthread", "-I", os.path.join(REFERENCE, "core", "include"),
+             "-I", os.path.join(REFERENCE, "core", "src", "world"),
              "-I", os.path.join(ROOT, "include")]
     objs = []
     jobs = []

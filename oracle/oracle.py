@@ -76,6 +76,7 @@ def port_lib() -> ctypes.CDLL:
         lib.svxo_set_threads.argtypes = [ctypes.c_int]
         lib.svxo_seq_sum.restype = c_f64
         lib.svxo_utilization_many.argtypes = [c_vp, c_vp, c_f64, c_vp, c_vp]
+        lib.svxo_build_bonds.argtypes = [c_vp, c_vp, c_i32, c_vp, c_vp, c_vp]
         lib.svxo_invalidate.argtypes = [c_vp]
         lib.svxo_assembled.argtypes = [c_vp]
         lib.svxo_preconditioner_current.argtypes = [c_vp]
@@ -114,6 +115,7 @@ def reference_lib() -> ctypes.CDLL | None:
         lib.svxr_hier_get.argtypes = [c_vp, c_i32] + [c_vp] * 10
         lib.svxr_hier_free.argtypes = [c_vp]
         lib.svxr_set_threads.argtypes = [ctypes.c_int]
+        lib.svxr_build_bonds.argtypes = [c_vp, c_vp, c_i32, c_vp, c_vp, c_vp]
         lib.svxr_p_create.restype = c_vp
         lib.svxr_p_create.argtypes = [c_vp, c_i32, c_vp, c_i32, c_vp]
         for name in ("destroy", "assembled", "invalidate", "preconditioner_current", "block_jacobi"):
@@ -416,6 +418,27 @@ class Reference:
         L = np.ascontiguousarray(load)
         phi = self.lib.svxr_utilization(ptr(b), ptr(L), fragility, ptr(self.mats), ctypes.byref(mode))
         return phi, mode.value
+
+
+def build_bonds(nodes, secs, faces, mats, reference: bool = False):
+    """The bonds of the interfaces `secs` (SECTION_DTYPE) over `faces` (FACE_DTYPE):
+    SecAcc::finish_lattice + section_strengths (core/src/world/world_internal.hpp:133-232,
+    :370-399). reference=False: the C restatement; True: the reference's own header code
+    (ref_shim.cpp)."""
+    from opus_destruct_2_gb300.graph import FACE_DTYPE, SECTION_DTYPE
+    nodes = np.ascontiguousarray(nodes, dtype=NODE_DTYPE)
+    secs = np.ascontiguousarray(secs, dtype=SECTION_DTYPE)
+    faces = np.ascontiguousarray(faces, dtype=FACE_DTYPE)
+    mats = np.ascontiguousarray(mats, dtype=MATERIAL_DTYPE)
+    out = np.zeros(len(secs), BOND_DTYPE)
+    if reference:
+        lib = reference_lib()
+        if lib is None:
+            raise RuntimeError("the reference is not built on this machine")
+        lib.svxr_build_bonds(ptr(nodes), ptr(secs), len(secs), ptr(faces), ptr(mats), ptr(out))
+    else:
+        port_lib().svxo_build_bonds(ptr(nodes), ptr(secs), len(secs), ptr(faces), ptr(mats), ptr(out))
+    return out
 
 
 class RefProblem:

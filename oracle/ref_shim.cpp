@@ -19,7 +19,10 @@
 
 #include <chrono>
 #include <cstring>
+#include <map>
 #include <vector>
+
+#include "world_internal.hpp"  // (SecAcc, section_strengths: header-only, core/src/world)
 
 #include "svxg_types.h"
 
@@ -356,6 +359,76 @@ void svxr_hier_get(void* hp, int32_t l, int32_t* rowptr, int32_t* col, double* v
 
 void svxr_hier_free(void* hp) { delete static_cast<Hier*>(hp); }
 
+
+// ---- section geometry: the world's own SecAcc::finish_lattice and section_strengths
+// (core/src/world/world_internal.hpp:133-232, :370-399) on the given interfaces, bond k from
+// secs[k], as World::Impl builds its bonds (core/src/world/world.cpp:839-850)
+
+static svxg_v3 to3(const V3& v) { return svxg_v3{v.x, v.y, v.z}; }
+
+void svxr_build_bonds(const svxg_node* nodes, const svxg_section* secs, int32_t nb, const svxg_face* faces,
+                      const svxg_material* mats, svxg_bond* out) {
+  MaterialTable table;
+  fill_materials(table, mats);
+  for (int32_t k = 0; k < nb; ++k) {
+    const svxg_section& S = secs[k];
+    world_detail::SecAcc A;
+    A.a = S.a;
+    A.b = S.b;
+    A.axis = S.axis;
+    A.sign = S.sign;
+    A.mb = static_cast<MaterialId>(S.mb);
+    A.grid = 0;
+    A.strength_b = S.strength_b;
+    std::map<IVec3, world_detail::VoxelAt> vox;  // (the voxels either side of each face)
+    for (int32_t f = 0; f < S.faces; ++f) {
+      const svxg_face& F = faces[S.first_face + f];
+      IVec3 q{F.x, F.y, F.z};
+      A.faces.push_back(q);
+      A.fax.push_back(F.axis);
+      A.fsg.push_back(F.sign);
+      vox[q] = world_detail::VoxelAt{F.vox_lo, F.damage_lo};
+      q[F.axis] += 1;
+      vox[q] = world_detail::VoxelAt{F.vox_hi, F.damage_hi};
+    }
+    const V3 ca = v3(nodes[S.a].c);
+    V3 cbv{};
+    if (S.b >= 0) cbv = v3(nodes[S.b].c);
+    SBond B = A.finish_lattice(S.h, ca, S.b >= 0 ? &cbv : nullptr, static_cast<MaterialId>(S.ma), S.strength_a);
+    if (S.sectioned)
+      world_detail::section_strengths(table, A.faces.data(), A.fax.data(), A.faces.size(),
+                                      [&](const IVec3& p) { return vox[p]; }, B);
+    svxg_bond& o = out[k];
+    std::memset(&o, 0, sizeof(o));
+    o.a = B.a;
+    o.b = B.b;
+    o.broken = B.broken ? 1 : 0;
+    o.in_k = B.in_k ? 1 : 0;
+    o.ma = static_cast<uint8_t>(B.ma);
+    o.mb = static_cast<uint8_t>(B.mb);
+    o.sectioned = B.sectioned ? 1 : 0;
+    o.n = to3(B.n);
+    o.t1 = to3(B.t1);
+    o.t2 = to3(B.t2);
+    o.area = B.area;
+    o.p = to3(B.p);
+    o.s1 = B.s1;
+    o.s2 = B.s2;
+    o.c1 = B.c1;
+    o.c2 = B.c2;
+    o.rmax = B.rmax;
+    o.la = B.la;
+    o.lb = B.lb;
+    o.strength = B.strength;
+    o.ft = B.ft;
+    o.fb = B.fb;
+    o.fc = B.fc;
+    o.coh = B.coh;
+    o.mu = B.mu;
+    o.faces = B.faces;
+    o.tag = k;
+  }
+}
 
 // ---- one problem kept between calls (the judge's break rounds drive it: remove_bond,
 // retire_nodes and solve on the same K, as World::Impl::judge does, core/src/world/world.cpp:1162-1277)

@@ -1433,6 +1433,168 @@ double svxo_utilization(const svxg_bond* b, const svxg_bond_load* L, double frag
   return utilization(b, L, fragility, mats, mode);
 }
 
+/* ----------------------------------------------------------------------------------------------
+ * Section geometry: SecAcc::finish_lattice (core/src/world/world_internal.hpp:133-232) and
+ * section_strengths (world_internal.hpp:370-399), bond by bond, as World::Impl builds its bonds
+ * (core/src/world/world.cpp:839-850).
+ * -------------------------------------------------------------------------------------------- */
+
+static v3 v3_scale(v3 a, double s) { v3 r = {a.x * s, a.y * s, a.z * s}; return r; }
+static v3 v3_normalized(v3 a) { /* vec.hpp:47-50 */
+  const double n = sqrt(v3_dot(a, a));
+  if (n > 0) return v3_scale(a, 1.0 / n);
+  v3 z = {0, 0, 0};
+  return z;
+}
+static void v3_addc(v3* a, int i, double v) {
+  if (i == 0) a->x += v;
+  else if (i == 1) a->y += v;
+  else a->z += v;
+}
+static void frame_of(v3 n, v3* t1, v3* t2) { /* world_internal.hpp:64-69 */
+  const double ax = fabs(n.x), ay = fabs(n.y), az = fabs(n.z);
+  v3 e = {0, 0, 1};
+  if (ax <= ay && ax <= az) { e.x = 1; e.z = 0; }
+  else if (ay <= az) { e.y = 1; e.z = 0; }
+  *t1 = v3_normalized(v3_cross(n, e));
+  *t2 = v3_cross(n, *t1);
+}
+static v3 face_centre(const svxg_face* F, double h) {
+  v3 x = {h * F->x, h * F->y, h * F->z};
+  v3_addc(&x, F->axis, 0.5 * h);
+  return x;
+}
+static const svxg_material* vox_material(const svxg_material* mats, uint8_t a, uint8_t b) {
+  /* grid.hpp:33-36: a side that is air takes the other's material */
+  const int id = (a != 0 ? (a & 0x7F) : (b & 0x7F)) - 1;
+  return &mats[id >= 0 && id < SVXG_MAX_MATERIALS ? id : 0];
+}
+
+void svxo_build_bonds(const svxg_node* nodes, const svxg_section* secs, int32_t nb, const svxg_face* faces,
+                      const svxg_material* mats, svxg_bond* out) {
+  for (int32_t k = 0; k < nb; ++k) {
+    const svxg_section* S = &secs[k];
+    const svxg_face* F = faces + S->first_face;
+    const int32_t nf = S->faces;
+    svxg_bond B;
+    memset(&B, 0, sizeof(B));
+    B.a = S->a;
+    B.b = S->b;
+    B.ma = S->ma;
+    B.mb = S->mb;
+    B.faces = nf;
+    const double h = S->h, A1 = h * h;
+    const v3 ca = v3_of(nodes[S->a].c);
+    const int has_b = S->b >= 0;
+    const v3 cb = has_b ? v3_of(nodes[S->b].c) : ca;
+    v3 n = {0, 0, 0};
+    if (has_b) {
+      for (int32_t f = 0; f < nf; ++f) v3_addc(&n, F[f].axis, (double)F[f].sign);
+      if (v3_dot(n, n) < 1e-12) n = v3_sub(cb, ca);
+      if (v3_dot(n, n) < 1e-12) { n.x = 0; n.y = 0; n.z = 1; }
+      n = v3_normalized(n);
+    } else {
+      v3_addc(&n, S->axis, (double)S->sign);
+    }
+    v3 t1, t2;
+    frame_of(n, &t1, &t2);
+    double W = 0.0;
+    v3 pc = {0, 0, 0};
+    for (int32_t f = 0; f < nf; ++f) {
+      const v3 x = face_centre(&F[f], h);
+      const double w = A1 * MAXD(0.05, fabs(v3_at(n, F[f].axis)));
+      W += w;
+      pc.x += x.x * w;
+      pc.y += x.y * w;
+      pc.z += x.z * w;
+    }
+    pc = v3_scale(pc, 1.0 / W);
+    {
+      double s11 = 0.0, s22 = 0.0, s12 = 0.0;
+      for (int32_t f = 0; f < nf; ++f) {
+        const v3 d = v3_sub(face_centre(&F[f], h), pc);
+        const double w = A1 * MAXD(0.05, fabs(v3_at(n, F[f].axis)));
+        const double y1 = v3_dot(d, t1), y2 = v3_dot(d, t2);
+        s11 += w * y1 * y1;
+        s22 += w * y2 * y2;
+        s12 += w * y1 * y2;
+      }
+      if (fabs(s12) > 1e-9 * (s11 + s22)) {
+        const double half = 0.5 * (s11 - s22);
+        const double l1 = 0.5 * (s11 + s22) + sqrt(half * half + s12 * s12);
+        double e1 = s12, e2 = l1 - s11;
+        if (fabs(l1 - s22) > fabs(e2)) {
+          e1 = l1 - s22;
+          e2 = s12;
+        }
+        const double en = sqrt(e1 * e1 + e2 * e2);
+        if (en > 0.0) {
+          e1 /= en;
+          e2 /= en;
+          const v3 u1 = {t1.x * e1 + t2.x * e2, t1.y * e1 + t2.y * e2, t1.z * e1 + t2.z * e2};
+          const v3 u2 = {t2.x * e1 - t1.x * e2, t2.y * e1 - t1.y * e2, t2.z * e1 - t1.z * e2};
+          t1 = u1;
+          t2 = u2;
+        }
+      }
+    }
+    B.n.x = n.x; B.n.y = n.y; B.n.z = n.z;
+    B.t1.x = t1.x; B.t1.y = t1.y; B.t1.z = t1.z;
+    B.t2.x = t2.x; B.t2.y = t2.y; B.t2.z = t2.z;
+    B.p.x = pc.x; B.p.y = pc.y; B.p.z = pc.z;
+    B.area = MAXD(W, 0.25 * nf * A1);
+    double s1 = 0.0, s2 = 0.0, m1 = 0.0, m2 = 0.0;
+    for (int32_t f = 0; f < nf; ++f) {
+      const v3 d = v3_sub(face_centre(&F[f], h), pc);
+      const double w = A1 * MAXD(0.05, fabs(v3_at(n, F[f].axis)));
+      const double y1 = v3_dot(d, t1), y2 = v3_dot(d, t2);
+      s1 += w * y1 * y1;
+      s2 += w * y2 * y2;
+      m1 = MAXD(m1, fabs(y1));
+      m2 = MAXD(m2, fabs(y2));
+    }
+    B.s1 = s1 + B.area * A1 / 12.0;
+    B.s2 = s2 + B.area * A1 / 12.0;
+    B.c1 = m1 + 0.5 * h;
+    B.c2 = m2 + 0.5 * h;
+    B.rmax = sqrt(B.c1 * B.c1 + B.c2 * B.c2);
+    if (has_b) {
+      const v3 d = v3_sub(cb, ca);
+      const double L = MAXD(MAXD(fabs(v3_dot(d, n)), 0.5 * sqrt(v3_dot(d, d))), 0.5 * h);
+      const double x = v3_dot(v3_sub(pc, ca), n), lo = 0.1 * L, hi = 0.9 * L;
+      B.la = x < lo ? lo : (hi < x ? hi : x);
+      B.lb = L - B.la;
+    } else {
+      B.la = MAXD(0.25 * h, v3_dot(v3_sub(pc, ca), n));
+      B.lb = 0.5 * h;
+    }
+    B.strength = MIND(S->strength_a, S->strength_b);
+    if (S->sectioned && nf > 0) {
+      double ft = 0, fb = 0, fc = 0, coh = 0, mu = 0;
+      for (int32_t f = 0; f < nf; ++f) {
+        const svxg_material* A = vox_material(mats, F[f].vox_lo, F[f].vox_hi);
+        const svxg_material* M = vox_material(mats, F[f].vox_hi, F[f].vox_lo);
+        const int dm = F[f].damage_lo > F[f].damage_hi ? F[f].damage_lo : F[f].damage_hi;
+        const double cond = MAXD(1e-6, 1.0 - (double)dm / 255.0);
+        ft += cond * MIND(A->ft, M->ft);
+        fb += cond * MIND(A->fb, M->fb);
+        fc += cond * MIND(A->fc, M->fc);
+        coh += cond * MIND(A->cohesion, M->cohesion);
+        mu += MIND(A->friction, M->friction);
+      }
+      const double w = 1.0 / (double)nf;
+      B.sectioned = 1;
+      B.ft = (float)(ft * w);
+      B.fb = (float)(fb * w);
+      B.fc = (float)(fc * w);
+      B.coh = (float)(coh * w);
+      B.mu = (float)(mu * w);
+    }
+    B.tag = k;
+    out[k] = B;
+  }
+}
+
 /* StressProblem::bond_load, stress.cpp:477-502 */
 static svxg_bond_load bond_load(const svxo_problem* P, int32_t bi, const double* u) {
   const svxg_bond* b = &P->bonds[bi];

@@ -69,6 +69,11 @@ void svxo_invalidate(svxo_problem* P);
 int svxo_assembled(const svxo_problem* P);
 int svxo_preconditioner_current(const svxo_problem* P);
 
+/* The bonds of the given interfaces: SecAcc::finish_lattice + section_strengths
+ * (core/src/world/world_internal.hpp:133-232, :370-399), bond k from secs[k]. */
+void svxo_build_bonds(const svxg_node* nodes, const svxg_section* secs, int32_t nb, const svxg_face* faces,
+                      const svxg_material* mats, svxg_bond* out);
+
 /* K (after svxo_assemble). rowptr: nfree + 1, col: nnzb, val: 36 nnzb, dof: n. */
 void svxo_matrix_dims(const svxo_problem* P, int32_t* nfree, int64_t* nnzb);
 void svxo_matrix(const svxo_problem* P, int32_t* dof, int32_t* rowptr, int32_t* col, double* val, double* id_scale);

@@ -120,3 +120,11 @@ def lattice(n: int, L: float = 0.4, keep_z: int | None = None, retire_top: bool 
                     lst.append(bond_record(nodes, idx(x, y, z), idx(x, y, z + 1), (0.0, 0.0, 1.0),
                                            (cc[0], cc[1], cc[2] + 0.5 * L), L))
     return nodes, _bonds(lst)
+
+
+def same_records(a, b) -> bool:
+    """Field by field, bit for bit (the padding between fields is not compared: numpy does not
+    keep it through save/load)."""
+    if a.dtype.names != b.dtype.names or len(a) != len(b):
+        return False
+    return all(np.ascontiguousarray(a[k]).tobytes() == np.ascontiguousarray(b[k]).tobytes() for k in a.dtype.names)

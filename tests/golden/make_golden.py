@@ -10,7 +10,8 @@ oracle against them on any machine, bit for bit.
 
 It also writes tests/golden/cascade/*.npz: the judge's break rounds of tests/cascade_cases.py
 run on the reference's own StressProblem (tests/test_oracle_golden.py checks the oracle's
-cascade against them bit for bit).
+cascade against them bit for bit), and tests/golden/sections/*.npz: voxel-face interfaces and the
+bonds the reference's section geometry makes of them.
 """
 from __future__ import annotations
 
@@ -90,6 +91,28 @@ def cascades():
         print("cascade", name, r["status"], r["rounds"], r["bonds_broken"], r["nodes_retired"])
 
 
+def sections():
+    """tests/golden/sections/<case>.npz: interfaces of tests/section_cases.py (the small ones) and
+    the bonds the reference's own SecAcc::finish_lattice + section_strengths make of them."""
+    import section_cases as sc
+    from oracle import build_bonds
+    out_dir = os.path.join(HERE, "sections")
+    os.makedirs(out_dir, exist_ok=True)
+    for name in ("tower2", "piece", "handmade"):
+        if name == "tower2":
+            nodes, _, _, mats = synth.tower_graph(2, seed=5)
+            secs, faces = synth.last_sections()
+        elif name == "piece":
+            nodes, secs, faces, mats = sc.generated("piece")
+        else:
+            nodes, secs, faces, mats = sc.handmade()
+        bonds = build_bonds(nodes, secs, faces, mats, reference=True)
+        np.savez_compressed(os.path.join(out_dir, f"{name}.npz"), nodes=nodes, secs=secs, faces=faces, mats=mats,
+                            bonds=bonds)
+        print("sections", name, len(secs), len(faces))
+
+
 if __name__ == "__main__":
     main()
     cascades()
+    sections()

@@ -32,6 +32,7 @@ def test_oracle_matches_reference_golden(path):
 
 
 import cascade_cases as cc  # noqa: E402
+import fixtures as fx  # noqa: E402
 from oracle import cascade  # noqa: E402
 
 CASCADE_FILES = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "cascade", "*.npz")))
@@ -71,3 +72,16 @@ def test_select_breaks_rules():
     b9 = np.arange(9)
     p9 = np.array([1.0, 1.0, 5.0, 1.1, 1.2, 1.0, 1.0, 1.0, 1.3])
     assert select_breaks(b9, p9, 0.85, 256) == [2, 8, 4]
+
+
+SECTION_FILES = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "sections", "*.npz")))
+
+
+@pytest.mark.parametrize("path", SECTION_FILES, ids=[os.path.basename(p)[:-4] for p in SECTION_FILES])
+def test_oracle_sections_match_reference_golden(path):
+    """Section geometry of the C restatement against the bonds the reference's own
+    SecAcc::finish_lattice + section_strengths made of the same interfaces: bit for bit."""
+    from oracle import build_bonds
+    g = np.load(path)
+    out = build_bonds(g["nodes"], g["secs"], g["faces"], g["mats"])
+    assert fx.same_records(out, g["bonds"])

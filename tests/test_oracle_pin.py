@@ -121,3 +121,19 @@ def test_cascade_bit_identical(name):
         assert a[k] == b[k], k
     assert np.array_equal(a["u"], b["u"]) and np.array_equal(a["phi"], b["phi"])
     assert a["judged"].tobytes() == b["judged"].tobytes() and np.array_equal(a["has"], b["has"])
+
+
+import section_cases as scases  # noqa: E402
+from oracle import build_bonds  # noqa: E402
+
+SECTIONS = scases.cases()
+
+
+@pytest.mark.parametrize("name", list(SECTIONS), ids=list(SECTIONS))
+def test_build_bonds_bit_identical(name):
+    """Section geometry (SecAcc::finish_lattice + section_strengths) of the C restatement against
+    the reference's own header code on the same interfaces, bit for bit."""
+    nodes, secs, faces, mats = SECTIONS[name]
+    a = build_bonds(nodes, secs, faces, mats)
+    b = build_bonds(nodes, secs, faces, mats, reference=True)
+    assert fx.same_records(a, b)
