@@ -183,6 +183,64 @@ typedef struct svxg_cascade_result {
   double rel_res;         /* of the last solve */
 } svxg_cascade_result;
 
+/* A loose piece's break rounds within one substep: World::Impl::body_stress_run's rounds
+ * (core/src/world/world_pieces.cpp:614-808) on its load (inertial relief and point forces, built
+ * by the caller). Defaults: WorldConfig (core/include/svx/world/world.hpp:150, :165-176, :269). */
+typedef struct svxg_piece_options {
+  double rtol;                  /* body_stress_rtol, 1e-2 */
+  double fragility;             /* 1 */
+  double break_band;            /* 0.85 */
+  double round_fraction;        /* impact_round_fraction: a round breaks at least this fraction
+                                   of the bonds over strength, 0.25 */
+  double energy;                /* what the impact dissipates (J); < 0: a resting load, no limit */
+  double fracture_energy;       /* x the materials' fracture energies, 1 */
+  double crush_energy;          /* crushing a bond costs this x its fracture energy, 20 */
+  double chip_fraction;         /* parts lighter than this x the piece are chips, 0.04 */
+  int32_t maxit;                /* body_stress_maxit, 60 */
+  int32_t rounds;               /* impact_rounds, 8 */
+  int32_t max_breaks_per_round; /* 256 */
+  int32_t pad;
+} svxg_piece_options;
+
+enum {
+  SVXG_PIECE_SETTLED = 0,      /* a round found no bond at or over its strength */
+  SVXG_PIECE_ENERGY = 1,       /* the impact's energy could not pay for the next crack */
+  SVXG_PIECE_APART = 2,        /* the piece came apart (a part heavier than a chip) */
+  SVXG_PIECE_LAST_ROUND = 3,   /* the last round broke bonds */
+  SVXG_PIECE_SOLVE_FAILED = 4, /* a solve did not converge even on a rebuilt preconditioner */
+  SVXG_PIECE_NO_PIN = 5,       /* bonds broke but the piece has no pinned node to split from */
+  SVXG_PIECE_SINGULAR = 6      /* assemble() found a singular diagonal */
+};
+
+typedef struct svxg_piece_result {
+  int32_t status;          /* SVXG_PIECE_* */
+  int32_t checks;          /* rounds solved and judged */
+  int32_t bonds_broken;
+  int32_t chips;           /* chip nodes retired (their loads moved to the piece) */
+  int32_t pcg_iters;
+  int32_t rebuilt;         /* the preconditioner was rebuilt once */
+  double spent;            /* fracture energy paid */
+  double first_max_utilization;  /* the first round's largest phi (the body's last_phi) */
+  double max_utilization;  /* the last round's */
+} svxg_piece_result;
+
+static inline svxg_piece_options svxg_default_piece_options(void) {
+  svxg_piece_options o;
+  o.rtol = 1e-2;
+  o.fragility = 1.0;
+  o.break_band = 0.85;
+  o.round_fraction = 0.25;
+  o.energy = -1.0;
+  o.fracture_energy = 1.0;
+  o.crush_energy = 20.0;
+  o.chip_fraction = 0.04;
+  o.maxit = 60;
+  o.rounds = 8;
+  o.max_breaks_per_round = 256;
+  o.pad = 0;
+  return o;
+}
+
 static inline svxg_cascade_options svxg_default_cascade_options(void) {
   svxg_cascade_options o;
   o.rtol = 3e-3;

@@ -202,5 +202,49 @@ class CascadeResult(ctypes.Structure):
                 f"iters={self.pcg_iters}, max_phi={self.max_utilization:.4g}, rel_res={self.rel_res:.3e})")
 
 
+class PieceOptions(ctypes.Structure):
+    """svxg_piece_options: a loose piece's break rounds within a substep (World::Impl::body_stress_run,
+    core/src/world/world_pieces.cpp:614-808); defaults from WorldConfig (world.hpp)."""
+    _fields_ = [("rtol", ctypes.c_double), ("fragility", ctypes.c_double), ("break_band", ctypes.c_double),
+                ("round_fraction", ctypes.c_double), ("energy", ctypes.c_double), ("fracture_energy", ctypes.c_double),
+                ("crush_energy", ctypes.c_double), ("chip_fraction", ctypes.c_double), ("maxit", ctypes.c_int32),
+                ("rounds", ctypes.c_int32), ("max_breaks_per_round", ctypes.c_int32), ("pad", ctypes.c_int32)]
+
+    def __init__(self, **kw):
+        super().__init__()
+        self.rtol, self.fragility, self.break_band, self.round_fraction = 1e-2, 1.0, 0.85, 0.25
+        self.energy, self.fracture_energy, self.crush_energy, self.chip_fraction = -1.0, 1.0, 20.0, 0.04
+        self.maxit, self.rounds, self.max_breaks_per_round = 60, 8, 256
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+
+# svxg_piece_result.status
+(PIECE_SETTLED, PIECE_ENERGY, PIECE_APART, PIECE_LAST_ROUND, PIECE_SOLVE_FAILED, PIECE_NO_PIN,
+ PIECE_SINGULAR) = range(7)
+
+
+class PieceResult(ctypes.Structure):
+    """svxg_piece_result."""
+    _fields_ = [("status", ctypes.c_int32), ("checks", ctypes.c_int32), ("bonds_broken", ctypes.c_int32),
+                ("chips", ctypes.c_int32), ("pcg_iters", ctypes.c_int32), ("rebuilt", ctypes.c_int32),
+                ("spent", ctypes.c_double), ("first_max_utilization", ctypes.c_double),
+                ("max_utilization", ctypes.c_double)]
+
+    def __repr__(self) -> str:
+        return (f"PieceResult(status={self.status}, checks={self.checks}, broken={self.bonds_broken}, "
+                f"chips={self.chips}, iters={self.pcg_iters}, spent={self.spent:.4g}, "
+                f"max_phi={self.max_utilization:.4g})")
+
+
+def default_fracture_energies() -> np.ndarray:
+    """Gf (J/m^2) per material id, SVXG_MAX_MATERIALS entries, as the reference's preset table
+    holds them (MaterialTable::reset, core/src/material/material.cpp:72-93); ids never registered
+    resolve to id 0's, as the table's lookup does (material.hpp:97-100)."""
+    gf = np.full(127, 2000.0)
+    gf[:12] = [2000.0, 400.0, 1e6, 120.0, 20.0, 600.0, 2000.0, 6000.0, 120.0, 4.0, 50000.0, 2e5]
+    return gf
+
+
 def ptr(a: np.ndarray | None):
     return None if a is None else ctypes.c_void_p(a.ctypes.data)

@@ -9,6 +9,7 @@ Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import 
 from __future__ import annotations
 
 import ctypes
+import math
 import os
 import sys
 
@@ -77,6 +78,7 @@ def port_lib() -> ctypes.CDLL:
         lib.svxo_seq_sum.restype = c_f64
         lib.svxo_utilization_many.argtypes = [c_vp, c_vp, c_f64, c_vp, c_vp]
         lib.svxo_build_bonds.argtypes = [c_vp, c_vp, c_i32, c_vp, c_vp, c_vp]
+        lib.svxo_set_broken.argtypes = [c_vp, c_i32, ctypes.c_int]
         lib.svxo_invalidate.argtypes = [c_vp]
         lib.svxo_assembled.argtypes = [c_vp]
         lib.svxo_preconditioner_current.argtypes = [c_vp]
@@ -123,6 +125,7 @@ def reference_lib() -> ctypes.CDLL | None:
         lib.svxr_p_assemble.argtypes = [c_vp, c_vp]
         lib.svxr_p_solve.argtypes = [c_vp, c_vp, c_vp, c_f64, c_i32, c_i32, c_vp]
         lib.svxr_p_remove_bond.argtypes = [c_vp, c_i32]
+        lib.svxr_p_set_broken.argtypes = [c_vp, c_i32, ctypes.c_int]
         lib.svxr_p_retire_nodes.argtypes = [c_vp, c_vp, c_i32]
         lib.svxr_p_bond_flags.argtypes = [c_vp, c_vp, c_vp]
         lib.svxr_p_judge.argtypes = [c_vp, c_vp, c_f64, c_vp, c_vp, c_vp]
@@ -217,6 +220,9 @@ class Port:
     def retire_nodes(self, lst):
         a = np.ascontiguousarray(lst, dtype=np.int32)
         self.lib.svxo_retire_nodes(self.h, ptr(a), len(a))
+
+    def set_broken(self, b, v):
+        self.lib.svxo_set_broken(self.h, int(b), int(bool(v)))
 
     def info(self) -> Info:
         i = Info()
@@ -487,6 +493,9 @@ class RefProblem:
         a = np.ascontiguousarray(lst, dtype=np.int32)
         self.lib.svxr_p_retire_nodes(self.h, ptr(a), len(a))
 
+    def set_broken(self, b, v):
+        self.lib.svxr_p_set_broken(self.h, int(b), int(bool(v)))
+
     def bond_flags(self):
         br = np.zeros(len(self.bonds), np.uint8)
         ik = np.zeros(len(self.bonds), np.uint8)
@@ -680,4 +689,221 @@ def cascade(P, f, u, o, opt: StressOptions | None = None, judged=None, has=None)
                 out["retired"].extend(int(i) for i in ret)
                 out["nodes_retired"] += len(ret)
     out.update(u=u, f=f, judged=judged, has=has)
+    return out
+
+
+# ---- a loose piece's break rounds (restated) -----------------------------------------------------
+
+CRUSH = 2  # FailMode::Crush (svxg_types.h SVXG_FAIL_CRUSH)
+
+
+def _cross(a, b):
+    return (a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0])
+
+
+def pin_components(n: int, bonds, broken, pin: int):
+    """graph_components (core/src/world/world_internal.hpp:660-705) seeded by the pinned node:
+    component 0 holds every node reachable from it over intact node-to-node bonds, the others are
+    numbered from 1 in node order. Returns (labels, count)."""
+    from scipy.sparse import coo_matrix
+    from scipy.sparse.csgraph import connected_components
+    a = np.asarray(bonds["a"], dtype=np.int64)
+    b = np.asarray(bonds["b"], dtype=np.int64)
+    e = (np.asarray(broken) == 0) & (b >= 0)
+    g = coo_matrix((np.ones(int(e.sum()), np.int8), (a[e], b[e])), shape=(n, n))
+    _, lab = connected_components(g, directed=False)
+    comp = np.full(n, -1, np.int64)
+    comp[lab == lab[pin]] = 0
+    nc = 1
+    for i in range(n):
+        if comp[i] < 0:
+            comp[lab == lab[i]] = nc
+            nc += 1
+    return comp, nc
+
+
+def piece_rounds(P, f, u, o, gf, opt: StressOptions | None = None):
+    """A loose piece's break rounds within one substep (World::Impl::body_stress_run,
+    core/src/world/world_pieces.cpp:614-808) on a problem with Port's methods, load f given (its
+    inertial relief and point forces), warm start u. Each round: solve (at most o.maxit
+    iterations; a failed solve after the first round rebuilds the preconditioner once, then
+    gives up); judge every intact bond whose node a is not retired; break the worst (phi >=
+    max(1, band x max phi), at least ceil(round_fraction x m), at most max_breaks), each crack paid
+    from o.energy when it is >= 0 (crushing costs crush_energy x more); stop when the energy runs
+    out, nothing broke or it was the last round; else split from the pinned node: a part heavier
+    than chip_fraction x the piece ends the rounds (the piece came apart), lighter parts (chips)
+    pass their load to the nodes they broke from and retire. gf: Gf per material id.
+    Returns a dict with u, f, broken (in order), modes (of those), chips (in order) and the
+    svxg_piece_result fields."""
+    n, nb = len(P.nodes), len(P.bonds)
+    f = np.array(f, dtype=np.float64)
+    u = np.array(u, dtype=np.float64)
+    gone = np.array(P.nodes["gone"], dtype=np.uint8)
+    fixed = np.array(P.nodes["fixed"], dtype=np.uint8)
+    mass = np.array(P.nodes["mass"], dtype=np.float64)
+    c = [(float(x), float(y), float(z)) for x, y, z in zip(P.nodes["c"]["x"], P.nodes["c"]["y"], P.nodes["c"]["z"])]
+    body_mass = 0.0
+    for i in range(n):
+        if not gone[i]:
+            body_mass += float(mass[i])
+    base = StressOptions() if opt is None else opt
+    so = StressOptions()
+    ctypes.memmove(ctypes.byref(so), ctypes.byref(base), ctypes.sizeof(StressOptions))
+    so.rtol = o.rtol
+    so.amg_min_nodes = 0
+    out = dict(status=0, checks=0, bonds_broken=0, chips=0, pcg_iters=0, rebuilt=0, spent=0.0,
+               first_max_utilization=0.0, max_utilization=0.0, broken=[], modes=[], chip_nodes=[])
+    if not P.assembled() and not P.assemble(so):
+        out["status"] = 6
+        out.update(u=u, f=f)
+        return out
+    impact = o.energy >= 0.0
+    rounds = max(1, o.rounds)
+    spent = 0.0
+    rebuilt = False
+    a_of = np.asarray(P.bonds["a"], np.int64)
+    b_of = np.asarray(P.bonds["b"], np.int64)
+    area = np.asarray(P.bonds["area"], np.float64)
+    strength = np.asarray(P.bonds["strength"], np.float64)
+    ma, mb = np.asarray(P.bonds["ma"]), np.asarray(P.bonds["mb"])
+    for rnd in range(rounds):
+        u, r = P.solve(f, u, o.rtol, o.maxit, True)
+        if not r.converged and (r.breakdown or r.rel_res > 5.0 * o.rtol) and rnd > 0 and not rebuilt:
+            rebuilt = True
+            out["rebuilt"] = 1
+            P.invalidate()
+            if P.assemble(so):
+                u, r = P.solve(f, u, o.rtol, o.maxit, True)
+        if not r.converged and (r.breakdown or r.rel_res > 5.0 * o.rtol):
+            P.invalidate()
+            u = np.zeros_like(u)
+            out["status"] = 4
+            break
+        out["checks"] += 1
+        out["pcg_iters"] += r.iters
+        broken, _ = P.bond_flags()
+        _, phi, mode = P.judge(u, o.fragility)
+        live = (broken == 0) & (gone[a_of] == 0)
+        mx = 0.0
+        for v in phi[live]:
+            mx = v if mx < v else mx
+        if rnd == 0:
+            out["first_max_utilization"] = float(mx)
+        out["max_utilization"] = float(mx)
+        over = np.nonzero(live & (phi >= 1.0))[0]
+        if len(over) == 0:
+            out["status"] = 0
+            break
+        order = np.lexsort((over, -phi[over]))
+        ob, op = over[order], phi[over][order]
+        x = o.break_band * float(op[0])
+        thr = x if 1.0 < x else 1.0
+        quota = int(math.ceil(o.round_fraction * float(len(over))))
+        sel = []
+        poor = False
+        for q in range(len(ob)):
+            k = int(ob[q])
+            if (op[q] < thr and q >= quota) or len(sel) >= o.max_breaks_per_round:
+                break
+            if impact:
+                crush = o.crush_energy if mode[k] == CRUSH else 1.0
+                g1, g2 = float(gf[ma[k]]), float(gf[mb[k]])
+                cost = o.fracture_energy * crush * float(area[k]) * (g2 if g2 < g1 else g1) * float(strength[k])
+                if spent + cost > o.energy:
+                    poor = True
+                    break
+                spent += cost
+            sel.append(k)
+        for k in sel:
+            P.remove_bond(k)
+        out["broken"].extend(sel)
+        out["modes"].extend(int(mode[k]) for k in sel)
+        out["bonds_broken"] += len(sel)
+        out["spent"] = spent
+        if poor or not sel or rnd + 1 == rounds:
+            out["status"] = 1 if poor else (0 if not sel else 3)
+            break
+        pin = -1
+        for i in range(n):
+            if fixed[i]:
+                pin = i
+        if pin < 0:
+            out["status"] = 5
+            break
+        broken, _ = P.bond_flags()
+        comp, nc = pin_components(n, P.bonds, broken, pin)
+        if nc <= 1:
+            continue
+        cmass = [0.0] * nc
+        for i in range(n):
+            if not gone[i]:
+                cmass[comp[i]] += float(mass[i])
+        if any(cmass[k] > o.chip_fraction * body_mass for k in range(1, nc)):
+            out["status"] = 2
+            break
+        # chips (world_pieces.cpp:752-808)
+        attach = [[] for _ in range(nc)]
+        for k in range(nb):
+            if not broken[k] or b_of[k] < 0:
+                continue
+            ca, cb = comp[a_of[k]], comp[b_of[k]]
+            if ca > 0 and cb == 0 and not gone[b_of[k]]:
+                attach[ca].append(int(b_of[k]))
+            if cb > 0 and ca == 0 and not gone[a_of[k]]:
+                attach[cb].append(int(a_of[k]))
+        cF = [[0.0, 0.0, 0.0] for _ in range(nc)]
+        cM = [[0.0, 0.0, 0.0] for _ in range(nc)]
+        chip_nodes = []
+        for i in range(n):
+            ci = comp[i]
+            if ci == 0 or gone[i]:
+                continue
+            chip_nodes.append(i)
+            A = attach[ci]
+            if not A:
+                best, bj = 1e300, -1
+                for j in range(n):
+                    if comp[j] != 0 or gone[j]:
+                        continue
+                    d = (c[j][0] - c[i][0], c[j][1] - c[i][1], c[j][2] - c[i][2])
+                    d2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2]
+                    if d2 < best:
+                        best, bj = d2, j
+                if bj < 0:
+                    continue
+                A.append(bj)
+            Fi = (float(f[6 * i]), float(f[6 * i + 1]), float(f[6 * i + 2]))
+            for q in range(3):
+                cF[ci][q] += Fi[q]
+            t = _cross(c[i], Fi)
+            Mi = (float(f[6 * i + 3]) + t[0], float(f[6 * i + 4]) + t[1], float(f[6 * i + 5]) + t[2])
+            for q in range(3):
+                cM[ci][q] += Mi[q]
+            f[6 * i:6 * i + 6] = 0.0
+        for ci in range(1, nc):
+            A = sorted(set(attach[ci]))
+            if not A:
+                continue
+            w = 1.0 / float(len(A))
+            Fj = (cF[ci][0] * w, cF[ci][1] * w, cF[ci][2] * w)
+            Mr = list(cM[ci])
+            for j in A:
+                t = _cross(c[j], Fj)
+                Mr = [Mr[0] - t[0], Mr[1] - t[1], Mr[2] - t[2]]
+            Mj = (Mr[0] * w, Mr[1] * w, Mr[2] * w)
+            for j in A:
+                for q in range(3):
+                    f[6 * j + q] += Fj[q]
+                    f[6 * j + 3 + q] += Mj[q]
+        inner = [k for k in range(nb) if not broken[k] and b_of[k] >= 0 and comp[a_of[k]] > 0
+                 and comp[a_of[k]] == comp[b_of[k]]]
+        P.retire_nodes(chip_nodes)
+        for k in inner:
+            P.set_broken(k, False)
+        for i in chip_nodes:
+            gone[i] = 1
+            u[6 * i:6 * i + 6] = 0.0
+        out["chip_nodes"].extend(chip_nodes)
+        out["chips"] += len(chip_nodes)
+    out.update(u=u, f=f)
     return out

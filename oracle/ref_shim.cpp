@@ -467,6 +467,7 @@ void svxr_p_solve(void* h, const double* f, double* u, double rtol, int32_t maxi
 }
 
 void svxr_p_remove_bond(void* h, int32_t b) { static_cast<RefProblem*>(h)->P.remove_bond(b); }
+void svxr_p_set_broken(void* h, int32_t b, int v) { static_cast<RefProblem*>(h)->P.bonds[size_t(b)].broken = v != 0; }
 
 void svxr_p_retire_nodes(void* h, const int32_t* list, int32_t count) {
   static_cast<RefProblem*>(h)->P.retire_nodes(std::vector<i32>(list, list + count));

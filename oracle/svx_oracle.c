@@ -1645,6 +1645,10 @@ void svxo_utilization_many(const svxo_problem* P, const svxg_bond_load* loads, d
   }
 }
 
+/* A caller writing bonds[b].broken (the public member), as the piece rounds do for a chip's inner
+ * bonds after retiring it (core/src/world/world_pieces.cpp:800-802). */
+void svxo_set_broken(svxo_problem* P, int32_t b, int v) { P->bonds[b].broken = (uint8_t)(v != 0); }
+
 /* StressProblem::invalidate / assembled / preconditioner_current (stress.hpp:83-91) */
 void svxo_invalidate(svxo_problem* P) {
   P->assembled = 0;

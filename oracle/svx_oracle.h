@@ -64,6 +64,8 @@ double svxo_utilization(const svxg_bond* b, const svxg_bond_load* L, double frag
 /* bond_utilization of every bond under the given loads (one per bond). */
 void svxo_utilization_many(const svxo_problem* P, const svxg_bond_load* loads, double fragility, double* phi,
                            uint8_t* mode);
+/* bonds[b].broken = v (a caller's write to the public member). */
+void svxo_set_broken(svxo_problem* P, int32_t b, int v);
 /* StressProblem::invalidate / assembled / preconditioner_current (stress.hpp:83-91). */
 void svxo_invalidate(svxo_problem* P);
 int svxo_assembled(const svxo_problem* P);

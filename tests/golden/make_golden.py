@@ -11,7 +11,8 @@ oracle against them on any machine, bit for bit.
 It also writes tests/golden/cascade/*.npz: the judge's break rounds of tests/cascade_cases.py
 run on the reference's own StressProblem (tests/test_oracle_golden.py checks the oracle's
 cascade against them bit for bit), and tests/golden/sections/*.npz: voxel-face interfaces and the
-bonds the reference's section geometry makes of them.
+bonds the reference's section geometry makes of them, and tests/golden/pieces/*.npz: loose pieces'
+break rounds run on the reference's own StressProblem.
 """
 from __future__ import annotations
 
@@ -112,7 +113,30 @@ def sections():
         print("sections", name, len(secs), len(faces))
 
 
+def pieces():
+    """tests/golden/pieces/<case>.npz: the break rounds of tests/piece_cases.py run on the
+    reference's own StressProblem (oracle.RefProblem): inputs and outputs."""
+    import piece_cases as pc
+    from oracle import RefProblem, piece_rounds
+    out_dir = os.path.join(HERE, "pieces")
+    os.makedirs(out_dir, exist_ok=True)
+    for name in pc.CASES:
+        nodes, bonds, mats, f, ko, gf = pc.case(name)
+        r = piece_rounds(RefProblem(nodes, bonds, mats), f, np.zeros(6 * len(nodes)), pc.options(ko), gf)
+        okeys = sorted(ko)
+        np.savez_compressed(
+            os.path.join(out_dir, f"{name}.npz"), nodes=nodes, bonds=bonds, mats=mats, f=f, gf=gf,
+            okeys=np.array(okeys), ovals=np.array([float(ko[k]) for k in okeys]), u=r["u"], f_out=r["f"],
+            broken=np.array(r["broken"], np.int32), modes=np.array(r["modes"], np.int32),
+            chip_nodes=np.array(r["chip_nodes"], np.int32),
+            counts=np.array([r["status"], r["checks"], r["bonds_broken"], r["chips"], r["pcg_iters"], r["rebuilt"]],
+                            np.int64),
+            reals=np.array([r["spent"], r["first_max_utilization"], r["max_utilization"]]))
+        print("piece", name, r["status"], r["checks"], r["bonds_broken"], r["chips"])
+
+
 if __name__ == "__main__":
     main()
     cascades()
     sections()
+    pieces()

@@ -85,3 +85,21 @@ def test_oracle_sections_match_reference_golden(path):
     g = np.load(path)
     out = build_bonds(g["nodes"], g["secs"], g["faces"], g["mats"])
     assert fx.same_records(out, g["bonds"])
+
+
+import piece_cases as pc  # noqa: E402
+from oracle import piece_rounds  # noqa: E402
+
+PIECE_FILES = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "pieces", "*.npz")))
+
+
+@pytest.mark.parametrize("path", PIECE_FILES, ids=[os.path.basename(p)[:-4] for p in PIECE_FILES])
+def test_oracle_piece_rounds_match_reference_golden(path):
+    """A piece's break rounds on the C restatement against the same rounds run on the reference's
+    own StressProblem (golden/make_golden.py): bit for bit."""
+    nodes, bonds, mats, f, ko, gf, exp = pc.load_golden(path)
+    r = piece_rounds(Port(nodes, bonds, mats), f, np.zeros(6 * len(nodes)), pc.options(ko), gf)
+    for k in ("status", "checks", "bonds_broken", "chips", "pcg_iters", "rebuilt", "spent", "first_max_utilization",
+              "max_utilization", "broken", "modes", "chip_nodes"):
+        assert r[k] == exp[k], k
+    assert np.array_equal(r["u"], exp["u"]) and np.array_equal(r["f"], exp["f"])

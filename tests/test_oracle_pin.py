@@ -137,3 +137,24 @@ def test_build_bonds_bit_identical(name):
     a = build_bonds(nodes, secs, faces, mats)
     b = build_bonds(nodes, secs, faces, mats, reference=True)
     assert fx.same_records(a, b)
+
+
+import piece_cases as pcases  # noqa: E402
+from oracle import piece_rounds  # noqa: E402
+
+
+@pytest.mark.parametrize("name", list(pcases.CASES), ids=list(pcases.CASES))
+def test_piece_rounds_bit_identical(name):
+    """A piece's break rounds (oracle.piece_rounds) on the C restatement and on the reference's own
+    StressProblem: the same bonds broken in order with their modes, the same chips, the same u
+    and moved loads, bit for bit."""
+    nodes, bonds, mats, f, ko, gf = pcases.case(name)
+    out = []
+    for cls in (Port, RefProblem):
+        P = cls(nodes, bonds, mats)
+        out.append(piece_rounds(P, f, np.zeros(6 * len(nodes)), pcases.options(ko), gf))
+    a, b = out
+    for k in ("status", "checks", "bonds_broken", "chips", "pcg_iters", "rebuilt", "spent", "first_max_utilization",
+              "max_utilization", "broken", "modes", "chip_nodes"):
+        assert a[k] == b[k], k
+    assert np.array_equal(a["u"], b["u"]) and np.array_equal(a["f"], b["f"])
