@@ -179,6 +179,26 @@ int svxg_cascade(svxg_problem* p, const svxg_stress_options* opt, const svxg_cas
                  double* u, svxg_bond_load* judged, uint8_t* judged_has, double* phi, int32_t* broken,
                  int32_t broken_cap, int32_t* retired, int32_t retired_cap, svxg_cascade_result* res);
 
+/* Replaces World::Impl::body_stress_run's break rounds of a loose piece within one substep
+ * (core/src/world/world_pieces.cpp:614-808), on this problem: f (6 n, in and out) is the piece's
+ * load - its inertial relief and point forces, built by the caller (add_force) - and comes back
+ * with the chips' loads moved onto the piece; u (6 n) the warm start in, the last solution out.
+ * Each round solves (o->maxit iterations at o->rtol; after the first round a failed solve
+ * rebuilds the preconditioner once, then the rounds stop with u = 0), judges every intact bond
+ * whose node a is not retired, breaks the worst (phi >= max(1, band x max phi), at least
+ * ceil(round_fraction x over), at most max_breaks_per_round), each crack paid from o->energy when
+ * it is >= 0 at fracture_energy x (crush_energy if it crushes) x area x min(Gf) x strength, and
+ * stops when the energy runs out, nothing broke or it was the last round; otherwise the piece
+ * splits from its pinned node (the last node with `fixed`): a part heavier than chip_fraction x
+ * the piece ends the rounds, lighter parts (chips) pass their net force and moment on to the
+ * nodes they broke from and retire. gf: fracture energy per material (SVXG_MAX_MATERIALS; null:
+ * the reference presets'). opt: assemble()'s options (null: the last ones; the piece is
+ * assembled with rtol = o->rtol, amg_min_nodes = 0 as the world does). broken / modes: the bonds
+ * broken, in order, and their failure modes (up to broken_cap); chips: the chip nodes retired. */
+int svxg_piece_rounds(svxg_problem* p, const svxg_stress_options* opt, const svxg_piece_options* o, const double* gf,
+                      double* f, double* u, int32_t* broken, uint8_t* modes, int32_t broken_cap, int32_t* chips,
+                      int32_t chips_cap, svxg_piece_result* res);
+
 /* --- counters ------------------------------------------------------------------------------- */
 int svxg_get_info(svxg_problem* p, svxg_info* info);
 /* Kernel launches made by this library since it was loaded (all problems, all threads). */

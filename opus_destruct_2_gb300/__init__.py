@@ -18,10 +18,11 @@ import numpy as np
 
 from . import build as _build
 from .graph import (BOND_DTYPE, LOAD_DTYPE, MATERIAL_DTYPE, NODE_DTYPE, CascadeOptions, CascadeResult, PcgResult,
-                    StressOptions, default_materials, ptr)
+                    PieceOptions, PieceResult, StressOptions, default_materials, ptr)
 
 __all__ = ["StressProblem", "StressOptions", "PcgResult", "Info", "load_library", "default_materials",
-           "NODE_DTYPE", "BOND_DTYPE", "SvxgError", "CascadeOptions", "CascadeResult", "build_bonds"]
+           "NODE_DTYPE", "BOND_DTYPE", "SvxgError", "CascadeOptions", "CascadeResult", "build_bonds",
+           "PieceOptions", "PieceResult"]
 
 c_i32, c_i64, c_f64, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p
 
@@ -107,6 +108,7 @@ def load_library() -> ctypes.CDLL:
         "svxg_timer_read": (c_i32, [c_vp, ctypes.POINTER(c_f64), ctypes.POINTER(c_i64)]),
         "svxg_cascade": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp, c_i32, c_vp]),
         "svxg_build_bonds": (c_i32, [c_vp, c_i32, c_vp, c_i32, c_vp, c_i64, c_vp, c_vp]),
+        "svxg_piece_rounds": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp, c_i32, c_vp]),
         "svxg_build_bonds_device": (c_i32, [c_vp, c_i32, c_vp, c_i32, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
     }
     for name, (res, args) in sig.items():
@@ -324,6 +326,34 @@ class StressProblem:
         extras = dict(broken=broken[:min(res.bonds_broken, len(broken))].tolist(), retired=rl.tolist(),
                       phi=phi[:nb].copy(), judged=judged, has=has)
         return u, res, extras
+
+    def piece_rounds(self, f, u=None, options: PieceOptions | None = None, gf=None, opt: StressOptions | None = None):
+        """A loose piece's break rounds within one substep (World::Impl::body_stress_run,
+        core/src/world/world_pieces.cpp:614-808). f: the piece's load (inertial relief and point
+        forces). Returns (u, f with the chips' loads moved, PieceResult, extras) with extras =
+        dict(broken=[bonds in the order broken], modes=[their failure modes], chips=[chip nodes
+        retired]); the problem's bonds and nodes are left broken and retired."""
+        from .graph import default_fracture_energies
+        self._sync_graph()
+        n, nb = len(self.nodes), len(self.bonds)
+        f = np.array(f, dtype=np.float64)
+        if f.size != 6 * n:
+            raise ValueError("f: 6 per node")
+        u = np.zeros(6 * n) if u is None else np.array(u, dtype=np.float64)
+        gf = np.ascontiguousarray(default_fracture_energies() if gf is None else gf, dtype=np.float64)
+        broken = np.zeros(max(nb, 1), np.int32)
+        modes = np.zeros(max(nb, 1), np.uint8)
+        chips = np.zeros(max(n, 1), np.int32)
+        res = PieceResult()
+        o = PieceOptions() if options is None else options
+        _check(self._L.svxg_piece_rounds(self._h, ctypes.byref(opt) if opt is not None else None, ctypes.byref(o),
+                                         ptr(gf), ptr(f), ptr(u), ptr(broken), ptr(modes), len(broken), ptr(chips),
+                                         len(chips), ctypes.byref(res)))
+        cl = chips[:min(res.chips, len(chips))].copy()
+        self.nodes["gone"][cl] = 1
+        self._pull_flags()
+        k = min(res.bonds_broken, len(broken))
+        return u, f, res, dict(broken=broken[:k].tolist(), modes=modes[:k].tolist(), chips=cl.tolist())
 
     def utilization(self, fragility: float = 1.0):
         """(phi, mode, failing bond indices) at the current solution."""

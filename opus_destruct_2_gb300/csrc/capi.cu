@@ -1054,7 +1054,7 @@ int svxg_cascade(svxg_problem* p, const svxg_stress_options* opt, const svxg_cas
       P.assembled = false;  // (world.cpp:1109: the next solve rebuilds it)
       P.active = false;
     }
-    TRY(cascade_judge(P, S, o.fragility, o.dif, shock && o.dif != 1.0 ? 1 : 0, o.break_band, max_breaks));
+    TRY(cascade_judge(P, S, o.fragility, o.dif, shock && o.dif != 1.0 ? 1 : 0, o.break_band, max_breaks, BreakRule{}));
     TRY(read_state());
     {
       double mx = 0.0;
@@ -1190,6 +1190,299 @@ int svxg_build_bonds_device(const svxg_node* nodes_dev, int32_t n, const svxg_se
   }
   return build_bonds_device(nodes_dev, n, secs_dev, nb, faces_dev, nf, mats_dev, out_dev, n_bad_dev,
                             static_cast<cudaStream_t>(stream));
+}
+
+
+// A loose piece's break rounds within one substep (World::Impl::body_stress_run,
+// core/src/world/world_pieces.cpp:614-808). Per round the device solves, judges, picks and pays
+// for the breaks and removes them; the host reads the round's counts and, when the piece splits
+// from its pinned node, sorts its parts (their nodes are few) and moves the chips' loads.
+int svxg_piece_rounds(svxg_problem* p, const svxg_stress_options* opt, const svxg_piece_options* po, const double* gf,
+                      double* f, double* u, int32_t* broken, uint8_t* modes, int32_t broken_cap, int32_t* chips,
+                      int32_t chips_cap, svxg_piece_result* res) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  if (!res || (P.n > 0 && (!f || !u)) || broken_cap < 0 || chips_cap < 0) {
+    set_error("svxg_piece_rounds: bad arguments");
+    return SVXG_ERR_ARG;
+  }
+  std::memset(res, 0, sizeof(*res));
+  if (!P.have_graph) {
+    set_error("svxg_piece_rounds: no graph");
+    return SVXG_ERR_STATE;
+  }
+  const svxg_piece_options o = po ? *po : svxg_default_piece_options();
+  const int32_t max_breaks = std::max(0, o.max_breaks_per_round);
+  DeviceScope ds(P.device);
+  svxg_stress_options so = opt ? *opt : P.opt;
+  so.rtol = o.rtol;
+  so.amg_min_nodes = 0;  // (small pieces: the coarsest level is the whole graph, solved exactly)
+  CascadeScratch S;
+  TRY(cascade_alloc(P, S, std::max(1, max_breaks)));
+  struct Free {
+    CascadeScratch& s;
+    ~Free() { cascade_free(s); }
+  } free_scratch{S};
+  const int32_t n = P.n, nb = P.nb;
+  const size_t m6 = 6 * size_t(n);
+  cudaStream_t st = P.stream;
+  std::vector<double> gfh(SVXG_MAX_MATERIALS, 2000.0);
+  if (gf) std::copy(gf, gf + SVXG_MAX_MATERIALS, gfh.begin());
+  SVXG_CUDA(cudaMemcpyAsync(S.gf, gfh.data(), sizeof(double) * SVXG_MAX_MATERIALS, cudaMemcpyHostToDevice, st));
+  if (m6) {
+    SVXG_CUDA(cudaMemcpyAsync(S.f, f, m6 * sizeof(double), cudaMemcpyHostToDevice, st));
+    SVXG_CUDA(cudaMemcpyAsync(S.u, u, m6 * sizeof(double), cudaMemcpyHostToDevice, st));
+  }
+  if (nb > 0) SVXG_CUDA(cudaMemsetAsync(S.phi, 0, sizeof(double) * size_t(nb), st));
+  std::vector<int32_t> hb, hc;
+  std::vector<uint8_t> hm;
+  CascadeState hs{};
+  auto read_state = [&]() -> int {
+    SVXG_CUDA(cudaMemcpyAsync(&hs, S.st, sizeof(hs), cudaMemcpyDeviceToHost, st));
+    SVXG_CUDA(host_wait(st));
+    return SVXG_OK;
+  };
+  double body_mass = 0.0;
+  for (int32_t i = 0; i < n; ++i)
+    if (!P.h_nodes[size_t(i)].gone) body_mass += P.h_nodes[size_t(i)].mass;
+  BreakRule rule;
+  rule.fraction = std::max(0.0, o.round_fraction);
+  rule.energy = o.energy;
+  rule.fracture_energy = o.fracture_energy;
+  rule.crush_energy = o.crush_energy;
+  rule.gf = S.gf;
+  const bool impact = o.energy >= 0.0;
+  const int32_t rounds = std::max(1, o.rounds);
+  bool rebuilt = false;
+  double spent = 0.0;
+  if (!P.assembled) {
+    int32_t ok = 0;
+    TRY(assemble_impl(P, &so, &ok));
+    if (!ok) {
+      res->status = SVXG_PIECE_SINGULAR;
+      return SVXG_OK;
+    }
+  }
+  res->status = SVXG_PIECE_SETTLED;
+  for (int32_t round = 0; round < rounds; ++round) {
+    svxg_pcg_result r{};
+    TRY(solve_common(P, S.f, S.u, o.rtol, o.maxit, 1, &r));
+    const auto failed = [&](const svxg_pcg_result& x) {
+      return !x.converged && (x.breakdown || x.rel_res > 5.0 * o.rtol);
+    };
+    if (failed(r) && round > 0 && !rebuilt) {
+      // (the multigrid of the intact piece is stale after the breaks and the chips: rebuilt once)
+      rebuilt = true;
+      res->rebuilt = 1;
+      P.assembled = false;
+      P.active = false;
+      int32_t ok = 0;
+      TRY(assemble_impl(P, &so, &ok));
+      if (ok) TRY(solve_common(P, S.f, S.u, o.rtol, o.maxit, 1, &r));
+    }
+    if (failed(r)) {
+      P.assembled = false;
+      P.active = false;
+      if (m6) SVXG_CUDA(cudaMemsetAsync(S.u, 0, m6 * sizeof(double), st));
+      res->status = SVXG_PIECE_SOLVE_FAILED;
+      break;
+    }
+    res->checks += 1;
+    res->pcg_iters += r.iters;
+    rule.spent = spent;
+    TRY(cascade_judge(P, S, o.fragility, 1.0, 0, o.break_band, std::max(1, max_breaks), rule));
+    TRY(read_state());
+    {
+      double mx = 0.0;
+      std::memcpy(&mx, &hs.maxphi_bits, sizeof(mx));
+      if (round == 0) res->first_max_utilization = mx;
+      res->max_utilization = mx;
+    }
+    if (hs.m == 0) {
+      res->status = SVXG_PIECE_SETTLED;
+      break;
+    }
+    // (max_breaks 0: the reference's loop takes none)
+    const int32_t k = max_breaks == 0 ? 0 : hs.K;
+    const bool poor = max_breaks == 0 ? false : hs.poor != 0;
+    if (k < 0) {
+      set_error("svxg_piece_rounds: round selection failed");
+      return SVXG_ERR_STATE;
+    }
+    if (impact && max_breaks > 0) spent = hs.spent;
+    if (k > 0) {
+      const size_t old = hb.size();
+      hb.resize(old + size_t(k));
+      hm.resize(old + size_t(k));
+      TRY(cascade_gather_modes(P, S, k));
+      SVXG_CUDA(cudaMemcpyAsync(hb.data() + old, S.sel, sizeof(int32_t) * size_t(k), cudaMemcpyDeviceToHost, st));
+      SVXG_CUDA(cudaMemcpyAsync(hm.data() + old, S.selmode, size_t(k), cudaMemcpyDeviceToHost, st));
+      TRY(remove_bonds_list(P, S.sel, nullptr, k, S.st));
+      res->bonds_broken += k;
+    }
+    res->spent = spent;
+    if (poor || k == 0 || round + 1 == rounds) {
+      res->status = poor ? SVXG_PIECE_ENERGY : (k == 0 ? SVXG_PIECE_SETTLED : SVXG_PIECE_LAST_ROUND);
+      break;
+    }
+    int32_t pin = -1;
+    for (int32_t i = 0; i < n; ++i)
+      if (P.h_nodes[size_t(i)].fixed) pin = i;
+    if (pin < 0) {
+      res->status = SVXG_PIECE_NO_PIN;
+      break;
+    }
+    // the parts: graph_components seeded by the pin (world_internal.hpp:660-705), component 0 the
+    // pin's, the others numbered from 1 in node order (each root is its part's smallest node)
+    TRY(cascade_roots(P, S));
+    std::vector<int32_t> root(static_cast<size_t>(n));
+    std::vector<uint8_t> brk(static_cast<size_t>(nb));
+    SVXG_CUDA(cudaMemcpyAsync(root.data(), S.parent, sizeof(int32_t) * size_t(n), cudaMemcpyDeviceToHost, st));
+    TRY(cascade_bond_flags(P, S));
+    if (nb > 0) SVXG_CUDA(cudaMemcpyAsync(brk.data(), S.broken8, size_t(nb), cudaMemcpyDeviceToHost, st));
+    SVXG_CUDA(host_wait(st));
+    std::vector<int32_t> comp(static_cast<size_t>(n), -1), number(static_cast<size_t>(n), -1);
+    int32_t nc = 1;
+    for (int32_t i = 0; i < n; ++i) {
+      const int32_t rt = root[size_t(i)];
+      if (rt == root[size_t(pin)]) {
+        comp[size_t(i)] = 0;
+      } else {
+        if (number[size_t(rt)] < 0) number[size_t(rt)] = nc++;
+        comp[size_t(i)] = number[size_t(rt)];
+      }
+    }
+    if (nc <= 1) continue;
+    std::vector<double> cmass(static_cast<size_t>(nc), 0.0);
+    for (int32_t i = 0; i < n; ++i)
+      if (!P.h_nodes[size_t(i)].gone) cmass[size_t(comp[size_t(i)])] += P.h_nodes[size_t(i)].mass;
+    bool apart = false;
+    for (int32_t c = 1; c < nc; ++c)
+      if (cmass[size_t(c)] > o.chip_fraction * body_mass) apart = true;
+    if (apart) {
+      res->status = SVXG_PIECE_APART;
+      break;
+    }
+    // chips pass their net load on to the nodes they broke from (world_pieces.cpp:752-797)
+    std::vector<double> fh(m6);
+    if (m6) SVXG_CUDA(cudaMemcpyAsync(fh.data(), S.f, m6 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SVXG_CUDA(host_wait(st));
+    std::vector<std::vector<int32_t>> attach(static_cast<size_t>(nc));
+    for (int32_t b = 0; b < nb; ++b) {
+      const int32_t ba = P.h_bond_ab[2 * size_t(b)], bb = P.h_bond_ab[2 * size_t(b) + 1];
+      if (!brk[size_t(b)] || bb < 0) continue;
+      const int32_t ca = comp[size_t(ba)], cb = comp[size_t(bb)];
+      if (ca > 0 && cb == 0 && !P.h_nodes[size_t(bb)].gone) attach[size_t(ca)].push_back(bb);
+      if (cb > 0 && ca == 0 && !P.h_nodes[size_t(ba)].gone) attach[size_t(cb)].push_back(ba);
+    }
+    auto cross = [](const double* a, const double* b, double* o3) {
+      o3[0] = a[1] * b[2] - a[2] * b[1];
+      o3[1] = a[2] * b[0] - a[0] * b[2];
+      o3[2] = a[0] * b[1] - a[1] * b[0];
+    };
+    std::vector<double> cF(3 * size_t(nc), 0.0), cM(3 * size_t(nc), 0.0);
+    std::vector<int32_t> chip_nodes;
+    for (int32_t i = 0; i < n; ++i) {
+      const int32_t c = comp[size_t(i)];
+      if (c == 0 || P.h_nodes[size_t(i)].gone) continue;
+      chip_nodes.push_back(i);
+      auto& A = attach[size_t(c)];
+      const svxg_v3& ci = P.h_nodes[size_t(i)].c;
+      if (A.empty()) {
+        double best = 1e300;
+        int32_t bj = -1;
+        for (int32_t j = 0; j < n; ++j) {
+          if (comp[size_t(j)] != 0 || P.h_nodes[size_t(j)].gone) continue;
+          const svxg_v3& cj = P.h_nodes[size_t(j)].c;
+          const double dx = cj.x - ci.x, dy = cj.y - ci.y, dz = cj.z - ci.z;
+          const double d = dx * dx + dy * dy + dz * dz;
+          if (d < best) {
+            best = d;
+            bj = j;
+          }
+        }
+        if (bj < 0) continue;
+        A.push_back(bj);
+      }
+      double* fi = &fh[6 * size_t(i)];
+      const double Fi[3] = {fi[0], fi[1], fi[2]};
+      const double cc[3] = {ci.x, ci.y, ci.z};
+      double t[3];
+      cross(cc, Fi, t);
+      for (int q = 0; q < 3; ++q) cF[3 * size_t(c) + q] += Fi[q];
+      const double Mi[3] = {fi[3] + t[0], fi[4] + t[1], fi[5] + t[2]};
+      for (int q = 0; q < 3; ++q) cM[3 * size_t(c) + q] += Mi[q];
+      for (int q = 0; q < 6; ++q) fi[q] = 0.0;
+    }
+    for (int32_t c = 1; c < nc; ++c) {
+      auto& A = attach[size_t(c)];
+      if (A.empty()) continue;
+      std::sort(A.begin(), A.end());
+      A.erase(std::unique(A.begin(), A.end()), A.end());
+      const double w = 1.0 / static_cast<double>(A.size());
+      const double Fj[3] = {cF[3 * size_t(c)] * w, cF[3 * size_t(c) + 1] * w, cF[3 * size_t(c) + 2] * w};
+      double Mr[3] = {cM[3 * size_t(c)], cM[3 * size_t(c) + 1], cM[3 * size_t(c) + 2]};
+      for (int32_t j : A) {
+        const svxg_v3& cj = P.h_nodes[size_t(j)].c;
+        const double cc[3] = {cj.x, cj.y, cj.z};
+        double t[3];
+        cross(cc, Fj, t);
+        for (int q = 0; q < 3; ++q) Mr[q] = Mr[q] - t[q];
+      }
+      const double Mj[3] = {Mr[0] * w, Mr[1] * w, Mr[2] * w};
+      for (int32_t j : A) {
+        double* fj = &fh[6 * size_t(j)];
+        for (int q = 0; q < 3; ++q) {
+          fj[q] += Fj[q];
+          fj[3 + q] += Mj[q];
+        }
+      }
+    }
+    // (a chip holds together: its own bonds leave K but keep their topology)
+    std::vector<int32_t> inner;
+    for (int32_t b = 0; b < nb; ++b) {
+      const int32_t ba = P.h_bond_ab[2 * size_t(b)], bb = P.h_bond_ab[2 * size_t(b) + 1];
+      if (!brk[size_t(b)] && bb >= 0 && comp[size_t(ba)] > 0 && comp[size_t(ba)] == comp[size_t(bb)]) inner.push_back(b);
+    }
+    if (m6) SVXG_CUDA(cudaMemcpyAsync(S.f, fh.data(), m6 * sizeof(double), cudaMemcpyHostToDevice, st));
+    const int32_t r_count = int32_t(chip_nodes.size());
+    if (r_count > 0) {
+      SVXG_CUDA(cudaMemcpyAsync(S.nlist, chip_nodes.data(), sizeof(int32_t) * size_t(r_count), cudaMemcpyHostToDevice,
+                                st));
+      SVXG_CUDA(cudaMemcpyAsync(&S.st->r, &r_count, sizeof(int32_t), cudaMemcpyHostToDevice, st));
+      TRY(cascade_retire(P, S, r_count));
+      if (!inner.empty()) {
+        SVXG_CUDA(cudaMemcpyAsync(S.blist, inner.data(), sizeof(int32_t) * inner.size(), cudaMemcpyHostToDevice, st));
+        TRY(unbreak_list(P, S.blist, int32_t(inner.size())));
+      }
+      for (int32_t i : chip_nodes) P.h_nodes[size_t(i)].gone = 1;
+      hc.insert(hc.end(), chip_nodes.begin(), chip_nodes.end());
+      res->chips += r_count;
+    }
+    TRY(read_state());
+    if (P.assembled && !P.jacobi_only && (hs.any_in_k || hs.r_dof)) P.pc_current = false;
+    P.active = false;
+  }
+  if (P.assembled && !P.jacobi_only && !hb.empty()) P.pc_current = false;
+  if (m6) {
+    SVXG_CUDA(cudaMemcpyAsync(u, S.u, m6 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SVXG_CUDA(cudaMemcpyAsync(f, S.f, m6 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  }
+  if (nb > 0) {
+    TRY(cascade_bond_flags(P, S));
+    P.h_broken.resize(size_t(nb));
+    P.h_in_k.resize(size_t(nb));
+    SVXG_CUDA(cudaMemcpyAsync(P.h_broken.data(), S.broken8, size_t(nb), cudaMemcpyDeviceToHost, st));
+    SVXG_CUDA(cudaMemcpyAsync(P.h_in_k.data(), S.in_k8, size_t(nb), cudaMemcpyDeviceToHost, st));
+  }
+  SVXG_CUDA(host_wait(st));
+  for (size_t t = 0; t < hb.size() && t < size_t(broken_cap); ++t) {
+    if (broken) broken[t] = hb[t];
+    if (modes) modes[t] = hm[t];
+  }
+  for (size_t t = 0; t < hc.size() && t < size_t(chips_cap); ++t)
+    if (chips) chips[t] = hc[t];
+  return SVXG_OK;
 }
 
 }  // extern "C"

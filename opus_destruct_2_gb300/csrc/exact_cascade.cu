@@ -46,11 +46,11 @@ unsigned grid_for(int64_t n, int t = kT) { return unsigned((n + t - 1) / t); }
 
 __global__ void k_cascade_judge(int32_t nb, const svxg_bond* __restrict__ bonds, const svxg_node* __restrict__ nodes,
                                 const svxg_material* __restrict__ mats, const double* __restrict__ u,
-                                double fragility, double dif, int blend, svxg_bond_load* judged, uint8_t* has,
-                                double* phi, int32_t* flag, CascadeState* st) {
+                                double fragility, double dif, int blend, int skip_gone_a, svxg_bond_load* judged,
+                                uint8_t* has, double* phi, uint8_t* mode, int32_t* flag, CascadeState* st) {
   const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   double ph = 0.0;
-  if (k < nb && !bonds[k].broken) {
+  if (k < nb && !bonds[k].broken && !(skip_gone_a && nodes[bonds[k].a].gone)) {
     const svxg_bond b = bonds[k];
     const svxg_node& na = nodes[b.a];
     const double* ua = na.fixed ? nullptr : u + 6 * int64_t(b.a);
@@ -63,7 +63,7 @@ __global__ void k_cascade_judge(int32_t nb, const svxg_bond* __restrict__ bonds,
     }
     const svxg_bond_load L = bond_load(b, mats, v3of(na.c), ua, cb, ub);
     svxg_bond_load Le = L;
-    if (blend && has[k]) {
+    if (blend && judged && has[k]) {
       const svxg_bond_load J = judged[k];
       Le.N = J.N + dif * (L.N - J.N);
       Le.V1 = J.V1 + dif * (L.V1 - J.V1);
@@ -74,8 +74,11 @@ __global__ void k_cascade_judge(int32_t nb, const svxg_bond* __restrict__ bonds,
     }
     uint8_t m = 0;
     ph = bond_utilization(b, Le, fragility, mats, &m);
-    judged[k] = L;
-    has[k] = 1;
+    if (judged) {
+      judged[k] = L;
+      has[k] = 1;
+    }
+    if (mode) mode[k] = m;
     phi[k] = ph;
     flag[k] = ph >= 1.0 ? 1 : 0;
   } else if (k < nb) {
@@ -158,7 +161,8 @@ __device__ int32_t block_sum_i(int32_t v, int32_t* red) {
 // bonds the round breaks, in the order the reference breaks them. gphi/gb: sort scratch of
 // gcap entries (a power of two >= K) for rounds that break more than kSelShared bonds.
 __global__ void __launch_bounds__(kSelT) k_cascade_select(const int32_t* over, const double* phi, double band,
-                                                          int32_t max_breaks, int32_t* sel,
+                                                          int32_t max_breaks, BreakRule rule, const svxg_bond* bonds,
+                                                          const uint8_t* mode, int32_t* sel,
                                                           unsigned long long* gphi, int32_t* gb, int64_t gcap,
                                                           CascadeState* st) {
   __shared__ double redd[32];
@@ -184,8 +188,12 @@ __global__ void __launch_bounds__(kSelT) k_cascade_select(const int32_t* over, c
   int32_t c = 0;
   for (int32_t i = threadIdx.x; i < m; i += blockDim.x) c += phi[over[i]] >= thr ? 1 : 0;
   const int32_t n_thr = block_sum_i(c, redi);
-  const int32_t quota = max(1, int32_t((int64_t(m) + 3) / 4));
-  const int32_t take = max(n_thr, quota);
+  // the quota: a structure's round, at least the worst quarter (world.cpp:1258); a piece's, at
+  // least ceil(fraction x m) (world_pieces.cpp:666)
+  int64_t quota = rule.fraction < 0.0 ? max(int64_t(1), (int64_t(m) + 3) / 4)
+                                      : static_cast<int64_t>(ceil(rule.fraction * static_cast<double>(m)));
+  if (quota > m) quota = m;
+  const int32_t take = max(n_thr, int32_t(quota));
   const int32_t K = min(max_breaks, take);
   // the K-th largest key, digit by digit from the top (12 bytes; keys are distinct)
   u128 prefix = 0;
@@ -262,7 +270,27 @@ __global__ void __launch_bounds__(kSelT) k_cascade_select(const int32_t* over, c
   }
   for (int32_t i = threadIdx.x; i < K; i += blockDim.x) sel[i] = kb[i];
   if (threadIdx.x == 0) {
-    st->K = K;
+    // an impact pays for its cracks in order: the first it cannot pay for ends the round
+    // (world_pieces.cpp:672-683)
+    int32_t keep = K, poor = 0;
+    double spent = rule.spent;
+    if (rule.energy >= 0.0) {
+      for (int32_t t = 0; t < K; ++t) {
+        const svxg_bond& B = bonds[kb[t]];
+        const double crush = mode[kb[t]] == SVXG_FAIL_CRUSH ? rule.crush_energy : 1.0;
+        const double g1 = rule.gf[B.ma], g2 = rule.gf[B.mb];
+        const double cost = rule.fracture_energy * crush * B.area * mind(g1, g2) * B.strength;
+        if (spent + cost > rule.energy) {
+          keep = t;
+          poor = 1;
+          break;
+        }
+        spent += cost;
+      }
+    }
+    st->K = keep;
+    st->poor = poor;
+    st->spent = spent;
     st->top = top;
     st->n_thr = n_thr;
   }
@@ -466,6 +494,18 @@ __global__ void k_mark_broken(const int32_t* list, const int32_t* count_dev, int
   if (t < count) bonds[list[t]].broken = 1;
 }
 
+__global__ void k_gather_modes(const int32_t* sel, int32_t count, const uint8_t* mode, uint8_t* out) {
+  const int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < count) out[t] = mode[sel[t]];
+}
+
+// bonds[list[t]].broken = 0: a caller's write to the public member (a chip's inner bonds keep
+// their topology after the chip retires, world_pieces.cpp:800-802); in_k stays as it is
+__global__ void k_unbreak(const int32_t* list, int32_t count, svxg_bond* bonds) {
+  const int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < count) bonds[list[t]].broken = 0;
+}
+
 __global__ void k_copy_flags(int32_t nb, const svxg_bond* bonds, const uint8_t* in_k_dev, uint8_t* broken,
                              uint8_t* in_k) {
   const int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -530,7 +570,8 @@ int cascade_alloc(Problem& P, CascadeScratch& S, int32_t max_breaks) {
   S.gcap = p2 > kSelShared ? p2 : 0;
   const size_t bytes = 256 * 40 + sizeof(CascadeState) + 3 * 6 * n * sizeof(double) + nb * sizeof(svxg_bond_load) +
                        nb * (1 + sizeof(double) + 4 * sizeof(int32_t)) + nf * sizeof(int32_t) + n * (2 + 3 * sizeof(int32_t)) +
-                       size_t(S.gcap) * (sizeof(unsigned long long) + sizeof(int32_t)) + 2 * nb;
+                       size_t(S.gcap) * (sizeof(unsigned long long) + sizeof(int32_t)) + 4 * nb +
+                       sizeof(double) * SVXG_MAX_MATERIALS;
   SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&S.base), bytes, P.stream));
   S.stream = P.stream;
   char* c = S.base;
@@ -555,6 +596,9 @@ int cascade_alloc(Problem& P, CascadeScratch& S, int32_t max_breaks) {
   S.gb = carve<int32_t>(c, size_t(std::max<int64_t>(S.gcap, 1)));
   S.broken8 = carve<uint8_t>(c, nb);
   S.in_k8 = carve<uint8_t>(c, nb);
+  S.mode = carve<uint8_t>(c, nb);
+  S.selmode = carve<uint8_t>(c, nb);
+  S.gf = carve<double>(c, SVXG_MAX_MATERIALS);
   return SVXG_OK;
 }
 
@@ -564,17 +608,19 @@ void cascade_free(CascadeScratch& S) {
 }
 
 int cascade_judge(Problem& P, CascadeScratch& S, double fragility, double dif, int blend, double band,
-                  int32_t max_breaks) {
+                  int32_t max_breaks, const BreakRule& rule) {
   SVXG_CUDA(cudaMemsetAsync(S.st, 0, sizeof(CascadeState), P.stream));
   if (P.nb == 0) return SVXG_OK;
   const unsigned g = grid_for(P.nb);
-  (k_cascade_judge<<<g, kT, 0, P.stream>>>(P.nb, P.d_bonds, P.d_nodes, P.d_mats, S.u, fragility, dif, blend, S.judged,
-                                           S.has, S.phi, S.flag, S.st), SVXG_COUNT_LAUNCH());
+  const bool piece = rule.fraction >= 0.0;  // (pieces: no judged loads; bonds of retired nodes skipped; modes kept)
+  (k_cascade_judge<<<g, kT, 0, P.stream>>>(P.nb, P.d_bonds, P.d_nodes, P.d_mats, S.u, fragility, dif, blend,
+                                           piece ? 1 : 0, piece ? nullptr : S.judged, S.has, S.phi, S.mode, S.flag,
+                                           S.st), SVXG_COUNT_LAUNCH());
   TRY(exclusive_scan_i32(P, S.flag, S.pos, P.nb, nullptr));
   (k_scatter_flagged<<<g, kT, 0, P.stream>>>(P.nb, S.flag, S.pos, S.over), SVXG_COUNT_LAUNCH());
   (k_take_count<<<1, 1, 0, P.stream>>>(scan_total_device(P, P.nb), &S.st->m), SVXG_COUNT_LAUNCH());
-  (k_cascade_select<<<1, kSelT, 0, P.stream>>>(S.over, S.phi, band, max_breaks, S.sel, S.gphi, S.gb, S.gcap, S.st),
-   SVXG_COUNT_LAUNCH());
+  (k_cascade_select<<<1, kSelT, 0, P.stream>>>(S.over, S.phi, band, max_breaks, rule, P.d_bonds, S.mode, S.sel, S.gphi,
+                                               S.gb, S.gcap, S.st), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   return SVXG_OK;
 }
@@ -617,6 +663,31 @@ int cascade_retire(Problem& P, CascadeScratch& S, int32_t r) {
 int cascade_bond_flags(Problem& P, CascadeScratch& S) {
   if (P.nb == 0) return SVXG_OK;
   (k_copy_flags<<<grid_for(P.nb), kT, 0, P.stream>>>(P.nb, P.d_bonds, P.d_in_k, S.broken8, S.in_k8), SVXG_COUNT_LAUNCH());
+  SVXG_CUDA(cudaGetLastError());
+  return SVXG_OK;
+}
+
+// union-find roots of the intact node-to-node bonds (each node's component's smallest index)
+int cascade_roots(Problem& P, CascadeScratch& S) {
+  if (P.n == 0) return SVXG_OK;
+  const unsigned gn = grid_for(P.n), gb = grid_for(std::max(P.nb, 1));
+  (k_cc_init<<<gn, kT, 0, P.stream>>>(P.n, S.parent, S.held, S.now), SVXG_COUNT_LAUNCH());
+  if (P.nb > 0) (k_cc_hook<<<gb, kT, 0, P.stream>>>(P.nb, P.d_bonds, S.parent), SVXG_COUNT_LAUNCH());
+  (k_cc_flatten<<<gn, kT, 0, P.stream>>>(P.n, S.parent), SVXG_COUNT_LAUNCH());
+  SVXG_CUDA(cudaGetLastError());
+  return SVXG_OK;
+}
+
+int cascade_gather_modes(Problem& P, CascadeScratch& S, int32_t count) {
+  if (count <= 0) return SVXG_OK;
+  (k_gather_modes<<<grid_for(count), kT, 0, P.stream>>>(S.sel, count, S.mode, S.selmode), SVXG_COUNT_LAUNCH());
+  SVXG_CUDA(cudaGetLastError());
+  return SVXG_OK;
+}
+
+int unbreak_list(Problem& P, const int32_t* list_dev, int32_t count) {
+  if (count <= 0) return SVXG_OK;
+  (k_unbreak<<<grid_for(count), kT, 0, P.stream>>>(list_dev, count, P.d_bonds), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   return SVXG_OK;
 }

@@ -316,6 +316,18 @@ struct CascadeState {  // device; the host reads it once or twice a round
   int32_t pad;
   double top;         // the largest phi over strength
   unsigned long long maxphi_bits;  // the largest phi of the judgement
+  double spent;       // fracture energy paid so far (pieces)
+  int32_t poor;       // the energy ran out this round (pieces)
+  int32_t pad2;
+};
+// How a round picks its breaks: a structure's (fraction < 0: at least the worst quarter, no
+// energy) or a piece's (at least ceil(fraction x m); energy >= 0: cracks paid from it)
+struct BreakRule {
+  double fraction = -1.0;
+  double energy = -1.0;
+  double spent = 0.0;
+  double fracture_energy = 1.0, crush_energy = 20.0;
+  const double* gf = nullptr;  // device, Gf per material
 };
 struct CascadeScratch {
   char* base = nullptr;
@@ -333,11 +345,16 @@ struct CascadeScratch {
   int32_t* gb = nullptr;
   int64_t gcap = 0;
   uint8_t *broken8 = nullptr, *in_k8 = nullptr;
+  uint8_t *mode = nullptr, *selmode = nullptr;
+  double* gf = nullptr;
 };
 int cascade_alloc(Problem& P, CascadeScratch& S, int32_t max_breaks);
 void cascade_free(CascadeScratch& S);
 int cascade_judge(Problem& P, CascadeScratch& S, double fragility, double dif, int blend, double band,
-                  int32_t max_breaks);
+                  int32_t max_breaks, const BreakRule& rule);
+int cascade_roots(Problem& P, CascadeScratch& S);
+int cascade_gather_modes(Problem& P, CascadeScratch& S, int32_t count);
+int unbreak_list(Problem& P, const int32_t* list_dev, int32_t count);
 int cascade_find_loose(Problem& P, CascadeScratch& S);
 int cascade_retire(Problem& P, CascadeScratch& S, int32_t r);
 int cascade_bond_flags(Problem& P, CascadeScratch& S);
