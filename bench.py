@@ -226,6 +226,56 @@ def run_many(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
+def run_pieces(args, rank: int, world: int):
+    """A substep's loose pieces through their break rounds (svxg_batch_piece_rounds) on this GPU:
+    value = pieces/s; beside it one piece after another on one problem, and the oracle's
+    restatement of the rounds on the host's cores over a sample of the same pieces."""
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+    from opus_destruct_2_gb300 import workloads
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    r = workloads.pieces(count=args.graphs, workers=args.workers)
+    clk = clocks.stop()
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        import oracle
+        from opus_destruct_2_gb300 import synth
+        from opus_destruct_2_gb300.graph import PieceOptions, default_fracture_energies, default_materials
+        oracle.set_threads(os.cpu_count() or 1)
+        sizes = synth.lognormal_sizes(args.graphs, 300, 10, 20000, seed=5)
+        rng = np.random.default_rng(6)
+        mats, gf = default_materials(), default_fracture_energies()
+        done, t0 = 0, time.perf_counter()
+        for k, sz in enumerate(sizes):
+            imp = float(10 ** rng.uniform(4.0, 6.0)) * 20.0
+            nodes, bonds, f, _ = synth.piece_graph(int(sz), free=True, seed=5 * 100003 + k, impact=imp)
+            oracle.piece_rounds(oracle.Port(nodes, bonds, mats), f, np.zeros(6 * len(nodes)), PieceOptions(), gf)
+            done += 1
+            if time.perf_counter() - t0 > 20.0:
+                break
+        tc = time.perf_counter() - t0
+        cpu = {"value": done / tc, "unit": "pieces/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"the first {done} pieces of the same substep, one after another, oracle restatement "
+                         f"(C, OpenMP; piece generation included)"}
+    line = {
+        "metric": METRIC, "value": r["pieces_per_s"] * world, "unit": "pieces/s", "n_gpus": world, "steps": 1,
+        "warmup": 32, "ms_per_step": 1e3 * r["wall_s"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"pieces: {args.graphs} free pieces of log-normal size (median 300 fragments, "
+                               f"10-20,000), inertial relief plus one impact each, break rounds at the world's "
+                               f"settings (rtol 1e-2, 60 iterations, 8 rounds, resting loads)",
+                   "workers": args.workers},
+        "pieces": r, "vs_plain_per_piece": r["pieces_per_s"] / r["plain_per_piece_pieces_per_s"],
+        "roofline": None,
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    if clk is not None:
+        line["clocks"] = clk
+    print(json.dumps(line), flush=True)
+
+
 def run_cascade(args, rank: int, world: int):
     """The judge's break rounds of the city block (svxg_cascade): one step = assemble + every round
     (solve warm, judge, break, retire what falls) until nothing is over strength, from the same
@@ -401,7 +451,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["city", "tower", "batch", "serve", "cascade", "sections"], default="city")
+    ap.add_argument("--workload", choices=["city", "tower", "batch", "serve", "cascade", "sections", "pieces"],
+                    default="city")
     ap.add_argument("--fragility", type=float, default=1.0, help="cascade: strength divisor")
     ap.add_argument("--requests", type=int, default=20000, help="serve: requests in the stream")
     ap.add_argument("--rate", type=float, default=5000.0, help="serve: Poisson arrival rate (requests/s)")
@@ -425,6 +476,9 @@ def main():
         return
     if args.workload in ("batch", "serve"):
         run_many(args, rank, world)
+        return
+    if args.workload == "pieces":
+        run_pieces(args, rank, world)
         return
     if args.workload == "cascade":
         run_cascade(args, rank, world)

@@ -94,6 +94,19 @@ int svxg_batch_solve(svxg_server* s, int32_t count, const svxg_node* const* node
                      double fragility, double* const* u_out, int32_t* const* over_out,
                      svxg_request_result* results);
 
+/* A substep's loose pieces (World::Impl::body_stress_run for each, core/src/world/world_pieces.cpp
+ * :614-808, which the reference runs one piece per pool thread): `count` pieces, each its own
+ * graph with its load f[i] (6 n[i], in and out: the chips' loads move), warm start and result in
+ * u[i] (may be null: from rest, not returned), run through svxg_piece_rounds as requests of `s`
+ * (all in flight at once over its slots). broken_out / modes_out (nb[i] entries each) and
+ * chips_out (n[i]) may be null; piece_results and results (count entries) may be null. */
+int svxg_batch_piece_rounds(svxg_server* s, int32_t count, const svxg_node* const* nodes, const int32_t* n,
+                            const svxg_bond* const* bonds, const int32_t* nb, const svxg_material* mats,
+                            const double* gf, double* const* f, double* const* u, const svxg_stress_options* opt,
+                            const svxg_piece_options* po, int32_t* const* broken_out, uint8_t* const* modes_out,
+                            int32_t* const* chips_out, svxg_piece_result* piece_results,
+                            svxg_request_result* results);
+
 #ifdef __cplusplus
 }
 #endif

@@ -46,7 +46,7 @@ def synth_library(force: bool = False) -> str:
     src = os.path.join(CSRC, "synth.cpp")
     if force or not os.path.exists(out) or _newest([src] + _headers()) > os.path.getmtime(out):
         os.makedirs(LIBDIR, exist_ok=True)
-        _run(["g++", "-std=c++20", "-O2", "-fPIC", "-shared", "-I", INCLUDE, src, "-o", out])
+        _run(["g++", "-std=c++20", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-I", INCLUDE, src, "-o", out])
     return out
 
 
@@ -66,14 +66,16 @@ def cuda_library(force: bool = False, verbose_ptxas: bool = False) -> str:
         o = os.path.join(objdir, os.path.basename(s) + ".o")
         objs.append(o)
         if s.endswith(".cu"):
-            cmd = [NVCC, *ARCH, "-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC,
+            # (host code without contraction either: the same host arithmetic on x86 and Arm)
+            cmd = [NVCC, *ARCH, "-std=c++20", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I", INCLUDE,
+                   "-I", CSRC,
                    "--expt-relaxed-constexpr", "-c", s, "-o", o]
             if os.path.basename(s).startswith("exact_"):
                 cmd.insert(1, "-fmad=false")  # (bit-exact setup arithmetic: no contraction)
             if verbose_ptxas:
                 cmd.insert(1, "-Xptxas=-v")
         else:
-            cmd = ["g++", "-std=c++20", "-O2", "-fPIC", "-I", INCLUDE, "-I", CSRC, "-c", s, "-o", o]
+            cmd = ["g++", "-std=c++20", "-O2", "-ffp-contract=off", "-fPIC", "-I", INCLUDE, "-I", CSRC, "-c", s, "-o", o]
         jobs.append(cmd)
     with ThreadPoolExecutor(max_workers=max(1, min(8, len(jobs)))) as ex:
         list(ex.map(_run, jobs))

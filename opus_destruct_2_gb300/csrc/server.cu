@@ -49,6 +49,16 @@ struct Request {
   double* u_out = nullptr;
   int32_t* over_out = nullptr;
   Clock::time_point submitted;
+  // a loose piece's break rounds instead of one solve and judgement (svxg_piece_rounds)
+  bool piece = false;
+  svxg_piece_options po{};
+  std::vector<double> gf;
+  std::vector<double> u0;
+  double* f_out = nullptr;
+  int32_t* broken_out = nullptr;
+  uint8_t* modes_out = nullptr;
+  int32_t* chips_out = nullptr;
+  svxg_piece_result* piece_out = nullptr;
 };
 
 struct Resident {
@@ -188,9 +198,29 @@ int judge_into(svxg_problem* p, const Request& q, svxg_request_result* res) {
   return e;
 }
 
+int run_piece(svxg_problem* p, Request& q, svxg_request_result* res) {
+  std::vector<double> u(6 * size_t(q.n), 0.0);
+  if (!q.u0.empty()) u = q.u0;
+  svxg_piece_result pr{};
+  const int32_t nb = int32_t(q.bonds.size());
+  const int e = svxg_piece_rounds(p, &q.opt, &q.po, q.gf.data(), q.f.data(), u.data(), q.broken_out, q.modes_out,
+                                  q.broken_out || q.modes_out ? nb : 0, q.chips_out, q.chips_out ? q.n : 0, &pr);
+  if (e) return e;
+  if (q.u_out) std::copy(u.begin(), u.end(), q.u_out);
+  if (q.f_out) std::copy(q.f.begin(), q.f.end(), q.f_out);
+  if (q.piece_out) *q.piece_out = pr;
+  res->iters = pr.pcg_iters;
+  res->converged = pr.status != SVXG_PIECE_SOLVE_FAILED && pr.status != SVXG_PIECE_SINGULAR;
+  res->breakdown = pr.status == SVXG_PIECE_SINGULAR;
+  res->failing = pr.bonds_broken;
+  res->rel_res = 0.0;
+  return SVXG_OK;
+}
+
 int run_new(svxg_problem* p, Request& q, svxg_request_result* res) {
   int e = svxg_set_graph(p, q.nodes.data(), q.n, q.bonds.data(), int32_t(q.bonds.size()), q.mats.data());
   if (e) return e;
+  if (q.piece) return run_piece(p, q, res);
   int32_t ok = 0;
   e = svxg_assemble(p, &q.opt, &ok);
   if (e) return e;
@@ -569,6 +599,59 @@ int svxg_batch_solve(svxg_server* S, int32_t count, const svxg_node* const* node
   for (int32_t i = 0; i < count; ++i) {
     t[size_t(i)] = svxg_server_submit(S, -1, nodes[i], n[i], bonds[i], nb[i], mats, f[i], opt, rtol, maxit, fragility,
                                       u_out ? u_out[i] : nullptr, over_out ? over_out[i] : nullptr);
+    if (t[size_t(i)] < 0) {
+      err = int(t[size_t(i)]);
+      break;
+    }
+  }
+  for (int32_t i = 0; i < count; ++i) {
+    if (t[size_t(i)] <= 0) break;
+    svxg_request_result r{};
+    const int e = svxg_server_wait(S, t[size_t(i)], &r);
+    if (e && !err) err = e;
+    if (results) results[i] = r;
+  }
+  return err;
+}
+
+
+int svxg_batch_piece_rounds(svxg_server* S, int32_t count, const svxg_node* const* nodes, const int32_t* n,
+                            const svxg_bond* const* bonds, const int32_t* nb, const svxg_material* mats,
+                            const double* gf, double* const* f, double* const* u, const svxg_stress_options* opt,
+                            const svxg_piece_options* po, int32_t* const* broken_out, uint8_t* const* modes_out,
+                            int32_t* const* chips_out, svxg_piece_result* piece_results,
+                            svxg_request_result* results) {
+  if (!S || count < 0 || (count > 0 && (!nodes || !n || !bonds || !nb || !f || !mats))) {
+    set_error("svxg_batch_piece_rounds: bad arguments");
+    return SVXG_ERR_ARG;
+  }
+  std::vector<int64_t> t(size_t(count), 0);
+  int err = SVXG_OK;
+  for (int32_t i = 0; i < count; ++i) {
+    if (n[i] < 0 || nb[i] < 0 || (n[i] > 0 && (!nodes[i] || !f[i])) || (nb[i] > 0 && !bonds[i])) {
+      err = SVXG_ERR_ARG;
+      set_error("svxg_batch_piece_rounds: bad piece");
+      break;
+    }
+    Request q;
+    q.n = n[i];
+    q.nodes.assign(nodes[i], nodes[i] + n[i]);
+    q.bonds.assign(bonds[i], bonds[i] + nb[i]);
+    q.mats.assign(mats, mats + SVXG_MAX_MATERIALS);
+    q.f.assign(f[i], f[i] + 6 * size_t(n[i]));
+    if (u && u[i]) q.u0.assign(u[i], u[i] + 6 * size_t(n[i]));
+    q.opt = opt ? *opt : svxg_default_options();
+    q.po = po ? *po : svxg_default_piece_options();
+    q.gf.assign(SVXG_MAX_MATERIALS, 2000.0);
+    if (gf) q.gf.assign(gf, gf + SVXG_MAX_MATERIALS);
+    q.piece = true;
+    q.u_out = u ? u[i] : nullptr;
+    q.f_out = f[i];
+    q.broken_out = broken_out ? broken_out[i] : nullptr;
+    q.modes_out = modes_out ? modes_out[i] : nullptr;
+    q.chips_out = chips_out ? chips_out[i] : nullptr;
+    q.piece_out = piece_results ? &piece_results[i] : nullptr;
+    t[size_t(i)] = submit(S, std::move(q));
     if (t[size_t(i)] < 0) {
       err = int(t[size_t(i)]);
       break;

@@ -15,7 +15,8 @@ import ctypes
 import numpy as np
 
 from . import SvxgError, _check, load_library
-from .graph import BOND_DTYPE, MATERIAL_DTYPE, NODE_DTYPE, StressOptions, ptr
+from .graph import (BOND_DTYPE, MATERIAL_DTYPE, NODE_DTYPE, PieceOptions, PieceResult, StressOptions,
+                    default_fracture_energies, ptr)
 
 c_i32, c_i64, c_f64, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p
 
@@ -55,6 +56,8 @@ def _bind():
         "svxg_server_estimate_bytes": (c_i64, [c_i32, c_i32]),
         "svxg_batch_solve": (c_i32, [c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_f64, c_i32, c_f64,
                                      c_vp, c_vp, c_vp]),
+        "svxg_batch_piece_rounds": (c_i32, [c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                            c_vp, c_vp, c_vp, c_vp, c_vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -178,6 +181,41 @@ class Server:
                                         ctypes.byref(opt) if opt is not None else None, float(rtol), int(maxit),
                                         float(fragility), up, None, res))
         return list(res)[:k], us
+
+
+    def batch_piece_rounds(self, pieces, mats, options: PieceOptions | None = None, gf=None,
+                           opt: StressOptions | None = None, want_lists: bool = False):
+        """A substep's loose pieces: each (nodes, bonds, f) through its break rounds
+        (svxg_piece_rounds), all in flight at once. Returns (PieceResults, RequestResults, u
+        per piece, f per piece with the chips' loads moved, lists) with lists = [dict(broken,
+        modes, chips)] when want_lists."""
+        gs = [_graph(*g) for g in pieces]
+        k = len(gs)
+        mats = np.ascontiguousarray(mats, dtype=MATERIAL_DTYPE)
+        gf = np.ascontiguousarray(default_fracture_energies() if gf is None else gf, dtype=np.float64)
+        P = c_vp * max(k, 1)
+        nodes = P(*[ptr(g[0]) for g in gs])
+        bonds = P(*[ptr(g[1]) for g in gs])
+        fs = [np.array(g[2], dtype=np.float64) for g in gs]
+        us = [np.zeros(6 * len(g[0])) for g in gs]
+        n = np.array([len(g[0]) for g in gs] or [0], np.int32)
+        nb = np.array([len(g[1]) for g in gs] or [0], np.int32)
+        br = [np.zeros(max(len(g[1]), 1), np.int32) for g in gs] if want_lists else None
+        md = [np.zeros(max(len(g[1]), 1), np.uint8) for g in gs] if want_lists else None
+        ch = [np.zeros(max(len(g[0]), 1), np.int32) for g in gs] if want_lists else None
+        pres = (PieceResult * max(k, 1))()
+        res = (RequestResult * max(k, 1))()
+        o = PieceOptions() if options is None else options
+        _check(self._L.svxg_batch_piece_rounds(
+            self._h, k, nodes, ptr(n), bonds, ptr(nb), ptr(mats), ptr(gf), P(*[ptr(x) for x in fs]),
+            P(*[ptr(x) for x in us]), ctypes.byref(opt) if opt is not None else None, ctypes.byref(o),
+            P(*[ptr(x) for x in br]) if want_lists else None, P(*[ptr(x) for x in md]) if want_lists else None,
+            P(*[ptr(x) for x in ch]) if want_lists else None, pres, res))
+        lists = None
+        if want_lists:
+            lists = [dict(broken=br[i][:pres[i].bonds_broken].tolist(), modes=md[i][:pres[i].bonds_broken].tolist(),
+                          chips=ch[i][:pres[i].chips].tolist()) for i in range(k)]
+        return list(pres)[:k], list(res)[:k], us, fs, lists
 
 
 __all__ = ["Server", "estimate_bytes", "RequestResult", "ServingStats", "SvxgError"]

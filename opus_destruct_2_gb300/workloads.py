@@ -93,6 +93,47 @@ def batch(count: int = 512, workers: int = 16, precision: int = PRECISION_MIXED,
     }
 
 
+def pieces(count: int = 512, workers: int = 16, seed: int = 5, plain_sample: int = 64, impact_scale: float = 20.0):
+    """A substep's loose pieces through their break rounds (svxg_batch_piece_rounds): the batched
+    workload's piece sizes (log-normal, median 300 fragments, 10-20,000), every piece free with
+    inertial-relief loads and one impact of log-uniform 1e4-1e6 N scaled by `impact_scale` (so
+    that most pieces crack), the world's settings (rtol 1e-2, 60 iterations, 8 rounds), resting
+    loads (no energy limit). Reports pieces/s beside one piece after another on one problem."""
+    from .graph import PieceOptions
+    sizes = synth.lognormal_sizes(count, 300, 10, 20000, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    ps = []
+    for k, sz in enumerate(sizes):
+        imp = float(10 ** rng.uniform(4.0, 6.0)) * impact_scale
+        nodes, bonds, f, _ = synth.piece_graph(int(sz), free=True, seed=seed * 100003 + k, impact=imp)
+        ps.append((nodes, bonds, f))
+    mats = default_materials()
+    o = PieceOptions()
+    with Server(workers=workers, budget=40 << 30) as S:
+        S.batch_piece_rounds(ps[:min(32, count)], mats, options=o)  # (warm-up)
+        S.reset_stats()
+        t0 = time.perf_counter()
+        pres, res, _, _, _ = S.batch_piece_rounds(ps, mats, options=o)
+        wall = time.perf_counter() - t0
+        st = S.stats()
+    # one piece after another on one problem (the plain per-request path), on a sample
+    lim = min(plain_sample, count)
+    t0 = time.perf_counter()
+    for nodes, bonds, f in ps[:lim]:
+        G = StressProblem(nodes, bonds, mats)
+        G.piece_rounds(f, options=o)
+        del G
+    plain = lim / (time.perf_counter() - t0)
+    return {
+        "pieces_per_s": count / wall, "wall_s": wall, "p50_ms": st.p50_ms, "p99_ms": st.p99_ms, "pieces": count,
+        "nodes": int(sum(len(p[0]) for p in ps)), "bonds_broken": int(sum(r.bonds_broken for r in pres)),
+        "chips": int(sum(r.chips for r in pres)), "rounds": int(sum(r.checks for r in pres)),
+        "statuses": {str(s_): int(sum(1 for r in pres if r.status == s_)) for s_ in range(7)},
+        "failed_requests": int(sum(1 for r in res if r.status != 0)), "workers": workers,
+        "plain_per_piece_pieces_per_s": plain, "plain_sample": lim,
+    }
+
+
 def serve(requests: int = 20000, rate: float = 5000.0, repeat_share: float = 0.3, pool: int = 1500,
           workers: int = 16, precision: int = PRECISION_MIXED, rtol: float = 1e-6, maxit: int = 2000,
           budget: int = 40 << 30, seed: int = 11, plain_sample: int = 300):

@@ -59,3 +59,23 @@ def test_piece_nothing_over():
     u, f_out, res, ex = G.piece_rounds(f * 1e-3, options=pc.options(ko), gf=gf)
     assert res.status == 0 and res.checks == 1 and ex["broken"] == [] and res.spent == 0.0
     assert np.array_equal(f_out, f * 1e-3)
+
+
+def test_batch_piece_rounds_match_one_by_one():
+    """The same pieces through the server, all in flight at once: each piece's rounds as when it
+    runs alone (tight solves: the same bonds, chips and moved loads)."""
+    from opus_destruct_2_gb300.server import Server
+    names = list(pc.CASES)
+    cases = [pc.case(nm) for nm in names]
+    o = pc.options(cases[0][4])
+    with Server(workers=4) as S:
+        pres, res, us, fs, lists = S.batch_piece_rounds([(c[0], c[1], c[3]) for c in cases], cases[0][2], options=o,
+                                                        gf=cases[0][5], want_lists=True)
+    for i, (nodes, bonds, mats, f, ko, gf) in enumerate(cases):
+        assert res[i].status == 0
+        G = StressProblem(nodes, bonds, mats)
+        u, f_out, r1, ex = G.piece_rounds(f, options=o, gf=gf)
+        assert pres[i].status == r1.status and pres[i].bonds_broken == r1.bonds_broken
+        assert lists[i]["broken"] == ex["broken"] and lists[i]["chips"] == ex["chips"]
+        assert np.array_equal(fs[i], f_out)
+        assert relerr(us[i], u) <= 1e-8
