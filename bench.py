@@ -226,6 +226,20 @@ def run_many(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
+def _cpu_piece_init():
+    import oracle
+    oracle.set_threads(1)
+
+
+def _cpu_piece_run(job) -> int:
+    import oracle
+    from opus_destruct_2_gb300.graph import PieceOptions, default_fracture_energies, default_materials
+    nodes, bonds, f = job
+    oracle.piece_rounds(oracle.Port(nodes, bonds, default_materials()), f, np.zeros(6 * len(nodes)), PieceOptions(),
+                        default_fracture_energies())
+    return 1
+
+
 def run_pieces(args, rank: int, world: int):
     """A substep's loose pieces through their break rounds (svxg_batch_piece_rounds) on this GPU:
     value = pieces/s; beside it one piece after another on one problem, and the oracle's
@@ -239,25 +253,26 @@ def run_pieces(args, rank: int, world: int):
         return
     cpu = None
     if not args.no_cpu_baseline:
-        import oracle
+        # the reference's arrangement for small pieces: one piece per thread, all cores at once
+        # (world_pieces.cpp:1460-1463) - here one single-threaded oracle process per core
+        import multiprocessing as mp
         from opus_destruct_2_gb300 import synth
-        from opus_destruct_2_gb300.graph import PieceOptions, default_fracture_energies, default_materials
-        oracle.set_threads(os.cpu_count() or 1)
         sizes = synth.lognormal_sizes(args.graphs, 300, 10, 20000, seed=5)
         rng = np.random.default_rng(6)
-        mats, gf = default_materials(), default_fracture_energies()
-        done, t0 = 0, time.perf_counter()
+        jobs = []
         for k, sz in enumerate(sizes):
             imp = float(10 ** rng.uniform(4.0, 6.0)) * 20.0
             nodes, bonds, f, _ = synth.piece_graph(int(sz), free=True, seed=5 * 100003 + k, impact=imp)
-            oracle.piece_rounds(oracle.Port(nodes, bonds, mats), f, np.zeros(6 * len(nodes)), PieceOptions(), gf)
-            done += 1
-            if time.perf_counter() - t0 > 20.0:
-                break
-        tc = time.perf_counter() - t0
-        cpu = {"value": done / tc, "unit": "pieces/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"the first {done} pieces of the same substep, one after another, oracle restatement "
-                         f"(C, OpenMP; piece generation included)"}
+            jobs.append((nodes, bonds, f))
+        cores = os.cpu_count() or 1
+        with mp.get_context("spawn").Pool(cores, initializer=_cpu_piece_init) as pool:
+            pool.map(_cpu_piece_run, jobs[:cores])  # (workers up)
+            t0 = time.perf_counter()
+            done = sum(pool.imap_unordered(_cpu_piece_run, jobs, chunksize=1))
+            tc = time.perf_counter() - t0
+        cpu = {"value": done / tc, "unit": "pieces/s", "cores": cores, "kind": "port",
+               "sample": f"all {done} pieces of the same substep, one single-threaded oracle process per core "
+                         f"(the reference's one piece per pool thread)"}
     line = {
         "metric": METRIC, "value": r["pieces_per_s"] * world, "unit": "pieces/s", "n_gpus": world, "steps": 1,
         "warmup": 32, "ms_per_step": 1e3 * r["wall_s"], "higher_is_better": True, "scaling": "weak",
