@@ -131,15 +131,31 @@ namespace {
 
 constexpr int kPoolDevices = 64;
 std::mutex g_pool_mu;
-cudaMemPool_t g_pool[kPoolDevices] = {};
 
 // The library's pool on `dev`: it keeps what is freed (no release threshold), and it never makes
 // one stream wait for another to reuse memory (a stream reuses only what its own order, or a
 // finished free, allows), so concurrent problems do not serialize through the allocator.
+// One pool per device and host thread: concurrent problems on other threads (a server's slots)
+// allocate and free without contending for one pool's lock. Memory freed by a thread returns to
+// the pool of the thread that allocated it.
+struct ThreadPools {
+  cudaMemPool_t pool[kPoolDevices] = {};
+  ~ThreadPools() {
+    // (outstanding allocations keep a destroyed pool's memory until they are freed)
+    for (cudaMemPool_t& p : pool)
+      if (p) cudaMemPoolDestroy(p);
+  }
+};
+thread_local ThreadPools t_pools;
+
 cudaError_t library_pool(int dev, cudaMemPool_t* out) {
   if (dev < 0 || dev >= kPoolDevices) return cudaErrorInvalidDevice;
+  if (t_pools.pool[dev]) {
+    *out = t_pools.pool[dev];
+    return cudaSuccess;
+  }
   std::lock_guard<std::mutex> lk(g_pool_mu);
-  if (!g_pool[dev]) {
+  {
     cudaMemPoolProps props = {};
     props.allocType = cudaMemAllocationTypePinned;
     props.location.type = cudaMemLocationTypeDevice;
@@ -155,9 +171,9 @@ cudaError_t library_pool(int dev, cudaMemPool_t* out) {
       cudaMemPoolDestroy(pool);
       return e;
     }
-    g_pool[dev] = pool;
+    t_pools.pool[dev] = pool;
   }
-  *out = g_pool[dev];
+  *out = t_pools.pool[dev];
   return cudaSuccess;
 }
 
