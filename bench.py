@@ -395,8 +395,8 @@ def run_sections(args, rank: int, world: int):
     def launch():
         rc = L.svxg_build_bonds_device(ctypes.c_void_p(t["nodes"].data_ptr()), len(nodes),
                                        ctypes.c_void_p(t["secs"].data_ptr()), nb, ctypes.c_void_p(t["faces"].data_ptr()),
-                                       nf, ctypes.c_void_p(t["mats"].data_ptr()), ctypes.c_void_p(out.data_ptr()), None,
-                                       ctypes.c_void_p(st.cuda_stream))
+                                       nf, None, 0, None, 0, 2, ctypes.c_void_p(t["mats"].data_ptr()),
+                                       ctypes.c_void_p(out.data_ptr()), None, ctypes.c_void_p(st.cuda_stream))
         if rc:
             raise RuntimeError(L.svxg_last_error().decode())
 
@@ -434,7 +434,7 @@ def run_sections(args, rank: int, world: int):
                    for k in BOND_DTYPE.names)
         cpu = {"value": nb / tc, "unit": "bonds/s", "cores": 1, "kind": "port",
                "sample": "every bond of the same city, oracle restatement (C, one thread)", "same_bytes": bool(same)}
-    algo = nb * (56 + BOND_DTYPE.itemsize + 2 * 40) + nf * 20
+    algo = nb * (64 + BOND_DTYPE.itemsize + 2 * 40) + nf * 20
     peaks = measured_peaks()
     achieved = algo / (kernel_ms / 1e3) / 1e9
     line = {
@@ -442,7 +442,8 @@ def run_sections(args, rank: int, world: int):
         "warmup": args.warmup, "ms_per_step": kernel_ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"sections: the bonds of the {args.lots}x{args.lots} city block from its voxel-face "
-                               f"interfaces (SecAcc::finish_lattice + section_strengths), L2 flushed between steps",
+                               f"interfaces (SecAcc::finish, the lattice path: one grid, no junction samples + "
+                               f"section_strengths), L2 flushed between steps",
                    "bonds": int(nb), "faces": int(nf)},
         "e2e": {"value": nb / e2e_s, "unit": "bonds/s", "h2d_bytes_per_step": int(nodes.nbytes + secs.nbytes +
                                                                                    faces.nbytes + mats.nbytes),

@@ -142,22 +142,29 @@ int svxg_utilization_noalloc(const svxg_node* nodes_dev, int32_t n, const svxg_b
                              uint8_t* mode_dev, int32_t* over_dev, int32_t* n_over, void* stream);
 
 /* --- bonds from voxel faces -------------------------------------------------------------------- */
-/* Replaces SecAcc::finish_lattice + section_strengths (core/src/world/world_internal.hpp:133-232,
- * :370-399), the section geometry World::Impl runs for every bond it makes
- * (core/src/world/world.cpp:839-850): bond k of out from secs[k] and its faces - the interface
- * normal and frame, the faces' projected centroid, principal axes, area, s1/s2, c1/c2/rmax, the
- * spring lengths la/lb, the strength multiplier (min of the two sides') and, where sectioned, the
- * section strengths from the faces' voxels and damage (materials: SVXG_MAX_MATERIALS records).
- * Bit for bit the reference's. Host arrays (nodes: n, secs: nb, faces: nf, out: nb); a section
- * whose indices lie outside the arrays: SVXG_ERR_ARG before anything runs. */
+/* Replaces SecAcc::finish (finish_lattice / finish_general) + section_strengths /
+ * section_strengths_general (core/src/world/world_internal.hpp:130-441), the section geometry
+ * World::Impl runs for every bond it makes (core/src/world/world.cpp:839-850): bond k of out from
+ * secs[k], its faces and its junction samples - the interface normal and frame, the elements'
+ * projected centroid, principal axes, area, s1/s2, c1/c2/rmax, the spring lengths la/lb, the
+ * strength multiplier (min of the two sides') and, where sectioned, the section strengths from
+ * the voxels and damage either side of each face and sample (materials: SVXG_MAX_MATERIALS
+ * records). A section without samples on an identity lattice takes finish_lattice, any other
+ * finish_general, as the reference's dispatch does. lats (nl, indexed by a section's grid and a
+ * sample's vg) may be null with nl = 0 when no section has samples (every lattice the
+ * identity); a section's h is its faces' lattice's voxel size; samples: junction samples per face
+ * edge. Bit for bit the reference's. Host arrays (nodes: n, secs: nb, faces: nf, juncs: nj, out:
+ * nb); anything out of range: SVXG_ERR_ARG before anything runs. */
 int svxg_build_bonds(const svxg_node* nodes, int32_t n, const svxg_section* secs, int32_t nb, const svxg_face* faces,
-                     int64_t nf, const svxg_material* mats, svxg_bond* out);
+                     int64_t nf, const svxg_junction* juncs, int64_t nj, const svxg_lattice* lats, int32_t nl,
+                     int32_t samples, const svxg_material* mats, svxg_bond* out);
 /* The same over device arrays on `stream` (a cudaStream_t; null: the legacy default stream),
- * allocating nothing; a section out of range becomes a broken empty bond and counts in *n_bad_dev
- * (device int32, may be null). */
+ * allocating nothing; a section with anything out of range becomes a broken empty bond and
+ * counts in *n_bad_dev (device int32, may be null). */
 int svxg_build_bonds_device(const svxg_node* nodes_dev, int32_t n, const svxg_section* secs_dev, int32_t nb,
-                            const svxg_face* faces_dev, int64_t nf, const svxg_material* mats_dev, svxg_bond* out_dev,
-                            int32_t* n_bad_dev, void* stream);
+                            const svxg_face* faces_dev, int64_t nf, const svxg_junction* juncs_dev, int64_t nj,
+                            const svxg_lattice* lats_dev, int32_t nl, int32_t samples, const svxg_material* mats_dev,
+                            svxg_bond* out_dev, int32_t* n_bad_dev, void* stream);
 
 /* --- the judge's break rounds ---------------------------------------------------------------- */
 /* Replaces World::Impl::judge's cascade of one structure (core/src/world/world.cpp:1162-1277)

@@ -113,9 +113,10 @@ typedef struct svxg_bond_load {
 enum { SVXG_FAIL_NONE = 0, SVXG_FAIL_TENSION = 1, SVXG_FAIL_CRUSH = 2, SVXG_FAIL_SHEAR = 3 };
 
 /* A bond's interface before it is a bond: the world's accumulator of the voxel faces two
- * fragments share (all axes), or of one fragment's faces on a support along one axis
- * (SecHead / SecAcc, core/src/world/world_internal.hpp:106-128). Its faces are
- * faces[first_face .. first_face + faces). */
+ * fragments share (all axes), or of one fragment's faces on a support along one axis, and of the
+ * junction samples where it meets another grid (SecHead / SecAcc,
+ * core/src/world/world_internal.hpp:106-128). Its faces are faces[first_face .. + faces), its
+ * junction samples junctions[first_junction .. + junctions). 64 bytes. */
 typedef struct svxg_section {
   int32_t a, b;          /* nodes; b < 0: a support */
   int64_t first_face;
@@ -124,7 +125,10 @@ typedef struct svxg_section {
   int8_t sign;           /* a support's side of a: the normal from a to the support is sign e_axis */
   uint8_t ma, mb;        /* materials of the two sides (a support's: its own) */
   uint8_t sectioned;     /* 1: strengths from the faces' voxels (section_strengths) */
-  uint8_t pad[7];
+  uint8_t pad;
+  uint16_t grid;         /* the lattice of its faces (index into the lattice table; 0 without one) */
+  int32_t junctions;
+  int64_t first_junction;
   double h;              /* voxel size of the faces' lattice (m) */
   double strength_a, strength_b;  /* the two sides' strength multipliers */
 } svxg_section;
@@ -132,7 +136,7 @@ typedef struct svxg_section {
 /* One voxel face of an interface: the face between voxel (x, y, z) of the lattice and its
  * +axis neighbour; sign +1 when a is on the lower side. The two voxels as the world stores them
  * (core/include/svx/world/grid.hpp:27-38: 0 air, else material id + 1 in the low 7 bits) and
- * their damage (0 intact .. 255 no strength left). */
+ * their damage (0 intact .. 255 no strength left). 20 bytes. */
 typedef struct svxg_face {
   int32_t x, y, z;
   uint8_t axis;
@@ -141,6 +145,30 @@ typedef struct svxg_face {
   uint8_t damage_lo, damage_hi;
   uint8_t pad[2];
 } svxg_face;
+
+/* A lattice in the frame the bonds are made in (LatticeXf, core/include/svx/phys/rigid.hpp:85-95):
+ * x_frame = off + R x_lattice unless identity. 112 bytes. */
+typedef struct svxg_lattice {
+  double off[3];
+  double R[9];           /* row-major */
+  double h;              /* its voxel size (m) */
+  uint8_t identity;
+  uint8_t pad[7];
+} svxg_lattice;
+
+/* A junction sample (JSample, world_internal.hpp:71-79): sample `sub` of face `face` (axis x 2
+ * + 1 for the +axis face) of voxel v of lattice vg lands in voxel o of lattice og (kind 1: in
+ * the unknown world - it holds what reaches into it); sign +1 when the face normal points from a
+ * towards b (or out of a, to a support); weight its share of the face (the samples of both sides
+ * count half each). The two voxels and their damage as the faces'. 40 bytes. */
+typedef struct svxg_junction {
+  int32_t v[3], o[3];
+  uint16_t vg, og;
+  uint8_t face, sub, kind;
+  int8_t sign;
+  float weight;
+  uint8_t vox_v, vox_o, damage_v, damage_o;
+} svxg_junction;
 
 /* The judge's break rounds of one structure: World::Impl::judge (core/src/world/world.cpp:1162-1277)
  * with the solve restarts of World::Impl's tick (world.cpp:1041-1110) and detach_unsupported

@@ -107,9 +107,11 @@ def load_library() -> ctypes.CDLL:
         "svxg_timer_enable": (c_i32, [c_vp, c_i32]),
         "svxg_timer_read": (c_i32, [c_vp, ctypes.POINTER(c_f64), ctypes.POINTER(c_i64)]),
         "svxg_cascade": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp, c_i32, c_vp]),
-        "svxg_build_bonds": (c_i32, [c_vp, c_i32, c_vp, c_i32, c_vp, c_i64, c_vp, c_vp]),
+        "svxg_build_bonds": (c_i32, [c_vp, c_i32, c_vp, c_i32, c_vp, c_i64, c_vp, c_i64, c_vp, c_i32, c_i32, c_vp,
+                                     c_vp]),
         "svxg_piece_rounds": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp, c_i32, c_vp]),
-        "svxg_build_bonds_device": (c_i32, [c_vp, c_i32, c_vp, c_i32, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
+        "svxg_build_bonds_device": (c_i32, [c_vp, c_i32, c_vp, c_i32, c_vp, c_i64, c_vp, c_i64, c_vp, c_i32, c_i32,
+                                            c_vp, c_vp, c_vp, c_vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -126,19 +128,23 @@ def _check(code: int) -> int:
     return code
 
 
-def build_bonds(nodes, secs, faces, mats=None) -> np.ndarray:
-    """The bonds of voxel-face interfaces on the GPU (SecAcc::finish_lattice + section_strengths,
-    core/src/world/world_internal.hpp:133-232, :370-399): bond k from secs[k] (SECTION_DTYPE) and
-    its faces (FACE_DTYPE). Returns BOND_DTYPE records."""
-    from .graph import FACE_DTYPE, SECTION_DTYPE
+def build_bonds(nodes, secs, faces, mats=None, junctions=None, lattices=None, samples: int = 2) -> np.ndarray:
+    """The bonds of voxel-face interfaces on the GPU (SecAcc::finish + section_strengths(_general),
+    core/src/world/world_internal.hpp:130-441): bond k from secs[k] (SECTION_DTYPE), its faces
+    (FACE_DTYPE) and junction samples (JUNCTION_DTYPE), with the lattices (LATTICE_DTYPE) of the
+    faces and samples. Returns BOND_DTYPE records."""
+    from .graph import FACE_DTYPE, JUNCTION_DTYPE, LATTICE_DTYPE, SECTION_DTYPE
     L = load_library()
     nodes = np.ascontiguousarray(nodes, dtype=NODE_DTYPE)
     secs = np.ascontiguousarray(secs, dtype=SECTION_DTYPE)
     faces = np.ascontiguousarray(faces, dtype=FACE_DTYPE)
     mats = np.ascontiguousarray(default_materials() if mats is None else mats, dtype=MATERIAL_DTYPE)
+    js = None if junctions is None else np.ascontiguousarray(junctions, dtype=JUNCTION_DTYPE)
+    ls = None if lattices is None else np.ascontiguousarray(lattices, dtype=LATTICE_DTYPE)
     out = np.zeros(len(secs), BOND_DTYPE)
-    _check(L.svxg_build_bonds(ptr(nodes), len(nodes), ptr(secs), len(secs), ptr(faces), len(faces), ptr(mats),
-                              ptr(out)))
+    _check(L.svxg_build_bonds(ptr(nodes), len(nodes), ptr(secs), len(secs), ptr(faces), len(faces), ptr(js),
+                              0 if js is None else len(js), ptr(ls), 0 if ls is None else len(ls), int(samples),
+                              ptr(mats), ptr(out)))
     return out
 
 

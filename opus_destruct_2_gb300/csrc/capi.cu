@@ -1134,18 +1134,23 @@ int svxg_cascade(svxg_problem* p, const svxg_stress_options* opt, const svxg_cas
 }
 
 
-// SecAcc::finish_lattice + section_strengths (core/src/world/world_internal.hpp:133-232,
-// :370-399) on the device: host arrays in and out.
+// SecAcc::finish + section_strengths(_general) (core/src/world/world_internal.hpp:130-441) on
+// the device: host arrays in and out.
 int svxg_build_bonds(const svxg_node* nodes, int32_t n, const svxg_section* secs, int32_t nb, const svxg_face* faces,
-                     int64_t nf, const svxg_material* mats, svxg_bond* out) {
-  if (n < 0 || nb < 0 || nf < 0 || (nb > 0 && (!nodes || !secs || !mats || !out)) || (nf > 0 && !faces)) {
+                     int64_t nf, const svxg_junction* juncs, int64_t nj, const svxg_lattice* lats, int32_t nl,
+                     int32_t samples, const svxg_material* mats, svxg_bond* out) {
+  if (n < 0 || nb < 0 || nf < 0 || nj < 0 || nl < 0 || samples < 1 ||
+      (nb > 0 && (!nodes || !secs || !mats || !out)) || (nf > 0 && !faces) || (nj > 0 && !juncs) ||
+      (nl > 0 && !lats)) {
     set_error("svxg_build_bonds: bad arguments");
     return SVXG_ERR_ARG;
   }
   for (int32_t k = 0; k < nb; ++k) {
     const svxg_section& S = secs[k];
     if (S.a < 0 || S.a >= n || S.b >= n || S.faces < 0 || S.first_face < 0 || S.first_face + S.faces > nf ||
-        (S.b < 0 && S.axis > 2)) {
+        (S.b < 0 && S.axis > 2) || S.junctions < 0 ||
+        (S.junctions > 0 && (S.first_junction < 0 || S.first_junction + S.junctions > nj)) ||
+        (nl == 0 ? S.junctions != 0 : int32_t(S.grid) >= nl)) {
       set_error("svxg_build_bonds: section " + std::to_string(k) + " out of range");
       return SVXG_ERR_ARG;
     }
@@ -1153,6 +1158,11 @@ int svxg_build_bonds(const svxg_node* nodes, int32_t n, const svxg_section* secs
   for (int64_t f = 0; f < nf; ++f)
     if (faces[f].axis > 2) {
       set_error("svxg_build_bonds: face axis out of range");
+      return SVXG_ERR_ARG;
+    }
+  for (int64_t j = 0; j < nj; ++j)
+    if (juncs[j].vg >= nl || juncs[j].face >= 6) {
+      set_error("svxg_build_bonds: junction sample out of range");
       return SVXG_ERR_ARG;
     }
   if (nb == 0) return SVXG_OK;
@@ -1163,24 +1173,38 @@ int svxg_build_bonds(const svxg_node* nodes, int32_t n, const svxg_section* secs
   auto up = [](size_t b) { return (b + 255) / 256 * 256; };
   const size_t bn = up(sizeof(svxg_node) * size_t(std::max(n, 1))), bs = up(sizeof(svxg_section) * size_t(nb)),
                bf = up(sizeof(svxg_face) * size_t(std::max<int64_t>(nf, 1))),
+               bj = up(sizeof(svxg_junction) * size_t(std::max<int64_t>(nj, 1))),
+               bl = up(sizeof(svxg_lattice) * size_t(std::max(nl, 1))),
                bm = up(sizeof(svxg_material) * SVXG_MAX_MATERIALS), bo = up(sizeof(svxg_bond) * size_t(nb));
   char* base = nullptr;
-  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&base), bn + bs + bf + bm + bo + 256, st));
-  svxg_node* dn = reinterpret_cast<svxg_node*>(base);
-  svxg_section* dsec = reinterpret_cast<svxg_section*>(base + bn);
-  svxg_face* dfc = reinterpret_cast<svxg_face*>(base + bn + bs);
-  svxg_material* dm = reinterpret_cast<svxg_material*>(base + bn + bs + bf);
-  svxg_bond* dout = reinterpret_cast<svxg_bond*>(base + bn + bs + bf + bm);
-  int32_t* dbad = reinterpret_cast<int32_t*>(base + bn + bs + bf + bm + bo);
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&base), bn + bs + bf + bj + bl + bm + bo + 256, st));
+  char* c = base;
+  svxg_node* dn = reinterpret_cast<svxg_node*>(c);
+  c += bn;
+  svxg_section* dsec = reinterpret_cast<svxg_section*>(c);
+  c += bs;
+  svxg_face* dfc = reinterpret_cast<svxg_face*>(c);
+  c += bf;
+  svxg_junction* djs = reinterpret_cast<svxg_junction*>(c);
+  c += bj;
+  svxg_lattice* dl = reinterpret_cast<svxg_lattice*>(c);
+  c += bl;
+  svxg_material* dm = reinterpret_cast<svxg_material*>(c);
+  c += bm;
+  svxg_bond* dout = reinterpret_cast<svxg_bond*>(c);
+  c += bo;
+  int32_t* dbad = reinterpret_cast<int32_t*>(c);
   int e = SVXG_OK;
   int32_t bad = 0;
   do {
     if (n > 0 && cudaMemcpyAsync(dn, nodes, sizeof(svxg_node) * size_t(n), cudaMemcpyHostToDevice, st)) break;
     if (cudaMemcpyAsync(dsec, secs, sizeof(svxg_section) * size_t(nb), cudaMemcpyHostToDevice, st)) break;
     if (nf > 0 && cudaMemcpyAsync(dfc, faces, sizeof(svxg_face) * size_t(nf), cudaMemcpyHostToDevice, st)) break;
+    if (nj > 0 && cudaMemcpyAsync(djs, juncs, sizeof(svxg_junction) * size_t(nj), cudaMemcpyHostToDevice, st)) break;
+    if (nl > 0 && cudaMemcpyAsync(dl, lats, sizeof(svxg_lattice) * size_t(nl), cudaMemcpyHostToDevice, st)) break;
     if (cudaMemcpyAsync(dm, mats, sizeof(svxg_material) * SVXG_MAX_MATERIALS, cudaMemcpyHostToDevice, st)) break;
     if (cudaMemsetAsync(dbad, 0, sizeof(int32_t), st)) break;
-    e = build_bonds_device(dn, n, dsec, nb, dfc, nf, dm, dout, dbad, st);
+    e = build_bonds_device(dn, n, dsec, nb, dfc, nf, djs, nj, dl, nl, samples, dm, dout, dbad, st);
     if (e) break;
     if (cudaMemcpyAsync(out, dout, sizeof(svxg_bond) * size_t(nb), cudaMemcpyDeviceToHost, st)) break;
     if (cudaMemcpyAsync(&bad, dbad, sizeof(int32_t), cudaMemcpyDeviceToHost, st)) break;
@@ -1197,17 +1221,18 @@ int svxg_build_bonds(const svxg_node* nodes, int32_t n, const svxg_section* secs
 }
 
 int svxg_build_bonds_device(const svxg_node* nodes_dev, int32_t n, const svxg_section* secs_dev, int32_t nb,
-                            const svxg_face* faces_dev, int64_t nf, const svxg_material* mats_dev, svxg_bond* out_dev,
-                            int32_t* n_bad_dev, void* stream) {
-  if (n < 0 || nb < 0 || nf < 0 || (nb > 0 && (!nodes_dev || !secs_dev || !mats_dev || !out_dev)) ||
-      (nf > 0 && !faces_dev)) {
+                            const svxg_face* faces_dev, int64_t nf, const svxg_junction* juncs_dev, int64_t nj,
+                            const svxg_lattice* lats_dev, int32_t nl, int32_t samples, const svxg_material* mats_dev,
+                            svxg_bond* out_dev, int32_t* n_bad_dev, void* stream) {
+  if (n < 0 || nb < 0 || nf < 0 || nj < 0 || nl < 0 || samples < 1 ||
+      (nb > 0 && (!nodes_dev || !secs_dev || !mats_dev || !out_dev)) || (nf > 0 && !faces_dev) ||
+      (nj > 0 && !juncs_dev) || (nl > 0 && !lats_dev)) {
     set_error("svxg_build_bonds_device: bad arguments");
     return SVXG_ERR_ARG;
   }
-  return build_bonds_device(nodes_dev, n, secs_dev, nb, faces_dev, nf, mats_dev, out_dev, n_bad_dev,
-                            static_cast<cudaStream_t>(stream));
+  return build_bonds_device(nodes_dev, n, secs_dev, nb, faces_dev, nf, juncs_dev, nj, lats_dev, nl, samples, mats_dev,
+                            out_dev, n_bad_dev, static_cast<cudaStream_t>(stream));
 }
-
 
 // A loose piece's break rounds within one substep (World::Impl::body_stress_run,
 // core/src/world/world_pieces.cpp:614-808). Per round the device solves, judges, picks and pays

@@ -300,7 +300,8 @@ void add_launches(int64_t n);
 // exact_sections.cu: the bonds of voxel-face interfaces (bad: device counter of sections whose
 // indices lie outside the arrays, or null)
 int build_bonds_device(const svxg_node* nodes, int32_t n, const svxg_section* secs, int32_t nb, const svxg_face* faces,
-                       int64_t nf, const svxg_material* mats, svxg_bond* out, int32_t* bad, cudaStream_t st);
+                       int64_t nf, const svxg_junction* juncs, int64_t nj, const svxg_lattice* lats, int32_t nl,
+                       int32_t samples, const svxg_material* mats, svxg_bond* out, int32_t* bad, cudaStream_t st);
 // scan.cu
 int exclusive_scan_i32(Problem& P, const int32_t* in, int32_t* out, int64_t n, int32_t* total_host);
 const int32_t* scan_total_device(const Problem& P, int64_t n);  // the last scan's total (device)

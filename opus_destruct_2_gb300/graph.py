@@ -43,15 +43,23 @@ MATERIAL_DTYPE = np.dtype(
      ("cohesion", "<f8"), ("friction", "<f8")]
 )
 
-# svxg_section / svxg_face (svxg_types.h): a bond's interface of voxel faces, before it is a bond
+# svxg_section / svxg_face / svxg_lattice / svxg_junction (svxg_types.h): a bond's interface of
+# voxel faces and junction samples, before it is a bond
 SECTION_DTYPE = np.dtype(
     [("a", "<i4"), ("b", "<i4"), ("first_face", "<i8"), ("faces", "<i4"), ("axis", "u1"), ("sign", "i1"),
-     ("ma", "u1"), ("mb", "u1"), ("sectioned", "u1"), ("pad", "u1", (7,)), ("h", "<f8"), ("strength_a", "<f8"),
-     ("strength_b", "<f8")])
+     ("ma", "u1"), ("mb", "u1"), ("sectioned", "u1"), ("pad", "u1"), ("grid", "<u2"), ("junctions", "<i4"),
+     ("first_junction", "<i8"), ("h", "<f8"), ("strength_a", "<f8"), ("strength_b", "<f8")])
 FACE_DTYPE = np.dtype(
     [("x", "<i4"), ("y", "<i4"), ("z", "<i4"), ("axis", "u1"), ("sign", "i1"), ("vox_lo", "u1"), ("vox_hi", "u1"),
      ("damage_lo", "u1"), ("damage_hi", "u1"), ("pad", "u1", (2,))])
-assert SECTION_DTYPE.itemsize == 56 and FACE_DTYPE.itemsize == 20
+LATTICE_DTYPE = np.dtype([("off", "<f8", (3,)), ("R", "<f8", (9,)), ("h", "<f8"), ("identity", "u1"),
+                          ("pad", "u1", (7,))])
+JUNCTION_DTYPE = np.dtype(
+    [("v", "<i4", (3,)), ("o", "<i4", (3,)), ("vg", "<u2"), ("og", "<u2"), ("face", "u1"), ("sub", "u1"),
+     ("kind", "u1"), ("sign", "i1"), ("weight", "<f4"), ("vox_v", "u1"), ("vox_o", "u1"), ("damage_v", "u1"),
+     ("damage_o", "u1")])
+assert (SECTION_DTYPE.itemsize, FACE_DTYPE.itemsize, LATTICE_DTYPE.itemsize, JUNCTION_DTYPE.itemsize) == \
+    (64, 20, 112, 40)
 
 LOAD_DTYPE = np.dtype([("N", "<f8"), ("V1", "<f8"), ("V2", "<f8"), ("T", "<f8"), ("M1", "<f8"), ("M2", "<f8")])
 

@@ -77,7 +77,7 @@ def port_lib() -> ctypes.CDLL:
         lib.svxo_set_threads.argtypes = [ctypes.c_int]
         lib.svxo_seq_sum.restype = c_f64
         lib.svxo_utilization_many.argtypes = [c_vp, c_vp, c_f64, c_vp, c_vp]
-        lib.svxo_build_bonds.argtypes = [c_vp, c_vp, c_i32, c_vp, c_vp, c_vp]
+        lib.svxo_build_bonds.argtypes = [c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp]
         lib.svxo_set_broken.argtypes = [c_vp, c_i32, ctypes.c_int]
         lib.svxo_invalidate.argtypes = [c_vp]
         lib.svxo_assembled.argtypes = [c_vp]
@@ -117,7 +117,7 @@ def reference_lib() -> ctypes.CDLL | None:
         lib.svxr_hier_get.argtypes = [c_vp, c_i32] + [c_vp] * 10
         lib.svxr_hier_free.argtypes = [c_vp]
         lib.svxr_set_threads.argtypes = [ctypes.c_int]
-        lib.svxr_build_bonds.argtypes = [c_vp, c_vp, c_i32, c_vp, c_vp, c_vp]
+        lib.svxr_build_bonds.argtypes = [c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_i32, c_i32, c_vp, c_vp]
         lib.svxr_p_create.restype = c_vp
         lib.svxr_p_create.argtypes = [c_vp, c_i32, c_vp, c_i32, c_vp]
         for name in ("destroy", "assembled", "invalidate", "preconditioner_current", "block_jacobi"):
@@ -426,24 +426,29 @@ class Reference:
         return phi, mode.value
 
 
-def build_bonds(nodes, secs, faces, mats, reference: bool = False):
-    """The bonds of the interfaces `secs` (SECTION_DTYPE) over `faces` (FACE_DTYPE):
-    SecAcc::finish_lattice + section_strengths (core/src/world/world_internal.hpp:133-232,
-    :370-399). reference=False: the C restatement; True: the reference's own header code
-    (ref_shim.cpp)."""
-    from opus_destruct_2_gb300.graph import FACE_DTYPE, SECTION_DTYPE
+def build_bonds(nodes, secs, faces, mats, reference: bool = False, junctions=None, lattices=None,
+                samples: int = 2):
+    """The bonds of the interfaces `secs` (SECTION_DTYPE) over `faces` (FACE_DTYPE) and, where
+    given, `junctions` (JUNCTION_DTYPE) and `lattices` (LATTICE_DTYPE): SecAcc::finish +
+    section_strengths(_general) (core/src/world/world_internal.hpp:130-441). reference=False: the
+    C restatement; True: the reference's own header code (ref_shim.cpp)."""
+    from opus_destruct_2_gb300.graph import FACE_DTYPE, JUNCTION_DTYPE, LATTICE_DTYPE, SECTION_DTYPE
     nodes = np.ascontiguousarray(nodes, dtype=NODE_DTYPE)
     secs = np.ascontiguousarray(secs, dtype=SECTION_DTYPE)
     faces = np.ascontiguousarray(faces, dtype=FACE_DTYPE)
     mats = np.ascontiguousarray(mats, dtype=MATERIAL_DTYPE)
+    js = None if junctions is None else np.ascontiguousarray(junctions, dtype=JUNCTION_DTYPE)
+    ls = None if lattices is None else np.ascontiguousarray(lattices, dtype=LATTICE_DTYPE)
     out = np.zeros(len(secs), BOND_DTYPE)
     if reference:
         lib = reference_lib()
         if lib is None:
             raise RuntimeError("the reference is not built on this machine")
-        lib.svxr_build_bonds(ptr(nodes), ptr(secs), len(secs), ptr(faces), ptr(mats), ptr(out))
+        lib.svxr_build_bonds(ptr(nodes), ptr(secs), len(secs), ptr(faces), ptr(js), ptr(ls),
+                             0 if ls is None else len(ls), int(samples), ptr(mats), ptr(out))
     else:
-        port_lib().svxo_build_bonds(ptr(nodes), ptr(secs), len(secs), ptr(faces), ptr(mats), ptr(out))
+        port_lib().svxo_build_bonds(ptr(nodes), ptr(secs), len(secs), ptr(faces), ptr(js), ptr(ls), int(samples),
+                                    ptr(mats), ptr(out))
     return out
 
 

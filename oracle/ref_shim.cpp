@@ -367,9 +367,19 @@ void svxr_hier_free(void* hp) { delete static_cast<Hier*>(hp); }
 static svxg_v3 to3(const V3& v) { return svxg_v3{v.x, v.y, v.z}; }
 
 void svxr_build_bonds(const svxg_node* nodes, const svxg_section* secs, int32_t nb, const svxg_face* faces,
+                      const svxg_junction* juncs, const svxg_lattice* lats, int32_t nl, int32_t samples,
                       const svxg_material* mats, svxg_bond* out) {
   MaterialTable table;
   fill_materials(table, mats);
+  std::vector<LatticeXf> xfs(size_t(std::max(nl, 1)));
+  for (int32_t g = 0; g < nl; ++g) {
+    LatticeXf& X = xfs[size_t(g)];
+    X.off = V3{lats[g].off[0], lats[g].off[1], lats[g].off[2]};
+    for (int q = 0; q < 9; ++q) X.R.m[size_t(q)] = lats[g].R[q];
+    for (int r = 0; r < 3; ++r)
+      for (int c = 0; c < 3; ++c) X.Rt.m[size_t(3 * r + c)] = lats[g].R[3 * c + r];
+    X.identity = lats[g].identity != 0;
+  }
   for (int32_t k = 0; k < nb; ++k) {
     const svxg_section& S = secs[k];
     world_detail::SecAcc A;
@@ -378,26 +388,52 @@ void svxr_build_bonds(const svxg_node* nodes, const svxg_section* secs, int32_t 
     A.axis = S.axis;
     A.sign = S.sign;
     A.mb = static_cast<MaterialId>(S.mb);
-    A.grid = 0;
+    A.grid = S.grid;
     A.strength_b = S.strength_b;
-    std::map<IVec3, world_detail::VoxelAt> vox;  // (the voxels either side of each face)
+    // (the voxels either side of each face and sample, by lattice)
+    std::map<std::pair<uint16_t, IVec3>, world_detail::VoxelAt> vox;
     for (int32_t f = 0; f < S.faces; ++f) {
       const svxg_face& F = faces[S.first_face + f];
       IVec3 q{F.x, F.y, F.z};
       A.faces.push_back(q);
       A.fax.push_back(F.axis);
       A.fsg.push_back(F.sign);
-      vox[q] = world_detail::VoxelAt{F.vox_lo, F.damage_lo};
+      vox[{S.grid, q}] = world_detail::VoxelAt{F.vox_lo, F.damage_lo};
       q[F.axis] += 1;
-      vox[q] = world_detail::VoxelAt{F.vox_hi, F.damage_hi};
+      vox[{S.grid, q}] = world_detail::VoxelAt{F.vox_hi, F.damage_hi};
+    }
+    for (int32_t j = 0; j < S.junctions; ++j) {
+      const svxg_junction& J = juncs[S.first_junction + j];
+      world_detail::JSample js;
+      js.v = IVec3{J.v[0], J.v[1], J.v[2]};
+      js.o = IVec3{J.o[0], J.o[1], J.o[2]};
+      js.vg = J.vg;
+      js.og = J.og;
+      js.face = J.face;
+      js.sub = J.sub;
+      js.kind = J.kind;
+      A.js.push_back(js);
+      A.jsg.push_back(J.sign);
+      A.jw.push_back(J.weight);
+      vox[{J.vg, js.v}] = world_detail::VoxelAt{J.vox_v, J.damage_v};
+      if (J.kind != world_detail::kJunctionUnknown) vox[{J.og, js.o}] = world_detail::VoxelAt{J.vox_o, J.damage_o};
     }
     const V3 ca = v3(nodes[S.a].c);
     V3 cbv{};
     if (S.b >= 0) cbv = v3(nodes[S.b].c);
-    SBond B = A.finish_lattice(S.h, ca, S.b >= 0 ? &cbv : nullptr, static_cast<MaterialId>(S.ma), S.strength_a);
-    if (S.sectioned)
-      world_detail::section_strengths(table, A.faces.data(), A.fax.data(), A.faces.size(),
-                                      [&](const IVec3& p) { return vox[p]; }, B);
+    const LatticeXf ident{};
+    auto hx = [&](int g) { return nl > 0 ? lats[g].h : S.h; };
+    auto xf = [&](int g) -> const LatticeXf& { return nl > 0 ? xfs[size_t(g)] : ident; };
+    SBond B = A.finish(hx, xf, samples, ca, S.b >= 0 ? &cbv : nullptr, static_cast<MaterialId>(S.ma), S.strength_a);
+    if (S.sectioned) {
+      if (A.js.empty())
+        world_detail::section_strengths(table, A.faces.data(), A.fax.data(), A.faces.size(),
+                                        [&](const IVec3& p) { return vox[{S.grid, p}]; }, B);
+      else
+        world_detail::section_strengths_general(
+            table, S.grid, A.faces.data(), A.fax.data(), A.faces.size(), A.js.data(), A.js.size(),
+            [&](uint16_t g, const IVec3& p) { return vox[{g, p}]; }, B, samples);
+    }
     svxg_bond& o = out[k];
     std::memset(&o, 0, sizeof(o));
     o.a = B.a;

@@ -1470,10 +1470,224 @@ static const svxg_material* vox_material(const svxg_material* mats, uint8_t a, u
   return &mats[id >= 0 && id < SVXG_MAX_MATERIALS ? id : 0];
 }
 
+/* LatticeXf::to / dir_to (rigid.hpp:91-93) with M3 * V3 (vec.hpp:63-66) */
+static v3 xf_dir(const svxg_lattice* X, v3 d) {
+  if (!X || X->identity) return d;
+  const double* R = X->R;
+  v3 r = {R[0] * d.x + R[1] * d.y + R[2] * d.z, R[3] * d.x + R[4] * d.y + R[5] * d.z,
+          R[6] * d.x + R[7] * d.y + R[8] * d.z};
+  return r;
+}
+static v3 xf_to(const svxg_lattice* X, v3 s) {
+  if (!X || X->identity) return s;
+  const v3 r = xf_dir(X, s);
+  v3 o = {X->off[0] + r.x, X->off[1] + r.y, X->off[2] + r.z};
+  return o;
+}
+/* junction_point (world_internal.hpp:94-103) with push 0 */
+static v3 junction_point(const int32_t* v, int face, int sub, int32_t S, double h) {
+  const int a = face >> 1, a1 = (a + 1) % 3, a2 = (a + 2) % 3;
+  const double sg = (face & 1) ? 1.0 : -1.0;
+  const int i = sub / S, j = sub % S;
+  v3 s = {h * v[0], h * v[1], h * v[2]};
+  v3_addc(&s, a, sg * (0.5 * h + 0.0));
+  v3_addc(&s, a1, ((i + 0.5) / (double)S - 0.5) * h);
+  v3_addc(&s, a2, ((j + 0.5) / (double)S - 0.5) * h);
+  return s;
+}
+
+/* SecAcc::finish_general (world_internal.hpp:237-352) and section_strengths_general
+ * (world_internal.hpp:404-441): faces of a placed lattice and junction samples, each a small
+ * square at a point with a normal, projected onto the plane normal to their mean normal. */
+static svxg_bond finish_general(const svxg_node* nodes, const svxg_section* S, const svxg_face* F,
+                                const svxg_junction* J, const svxg_lattice* lats, int32_t Sj,
+                                const svxg_material* mats) {
+  svxg_bond B;
+  memset(&B, 0, sizeof(B));
+  B.a = S->a;
+  B.b = S->b;
+  B.ma = S->ma;
+  B.mb = S->mb;
+  const int32_t nf = S->faces, nj = S->junctions, ne = nf + nj;
+  B.faces = ne;
+  v3* xs = (v3*)malloc(sizeof(v3) * (size_t)(ne > 0 ? ne : 1));
+  v3* nk = (v3*)malloc(sizeof(v3) * (size_t)(ne > 0 ? ne : 1));
+  double* ar = (double*)malloc(sizeof(double) * (size_t)(ne > 0 ? ne : 1));
+  double* sd = (double*)malloc(sizeof(double) * (size_t)(ne > 0 ? ne : 1));
+  double* ws = (double*)malloc(sizeof(double) * (size_t)(ne > 0 ? ne : 1));
+  const double h = S->h, A1 = h * h;
+  const svxg_lattice* X = lats ? &lats[S->grid] : NULL;
+  for (int32_t k = 0; k < nf; ++k) {
+    v3 x = {h * F[k].x, h * F[k].y, h * F[k].z};
+    v3_addc(&x, F[k].axis, 0.5 * h);
+    xs[k] = xf_to(X, x);
+    v3 n0 = {0, 0, 0};
+    v3_addc(&n0, F[k].axis, (double)F[k].sign);
+    nk[k] = xf_dir(X, n0);
+    ar[k] = A1;
+    sd[k] = h;
+  }
+  for (int32_t q = 0; q < nj; ++q) {
+    const svxg_junction* s = &J[q];
+    const svxg_lattice* Xs = &lats[s->vg];
+    const double hs = Xs->h, sj = hs / (double)(Sj > 1 ? Sj : 1);
+    const int32_t k = nf + q;
+    xs[k] = xf_to(Xs, junction_point(s->v, s->face, s->sub, Sj, hs));
+    v3 fn = {0, 0, 0};
+    v3_addc(&fn, s->face >> 1, (s->face & 1) ? 1.0 : -1.0);
+    nk[k] = v3_scale(xf_dir(Xs, fn), (double)s->sign);
+    ar[k] = sj * sj * (double)s->weight;
+    sd[k] = sj;
+  }
+  double atot = 0.0;
+  for (int32_t k = 0; k < ne; ++k) atot += ar[k];
+  const v3 ca = v3_of(nodes[S->a].c);
+  const int has_b = S->b >= 0;
+  const v3 cb = has_b ? v3_of(nodes[S->b].c) : ca;
+  v3 n = {0, 0, 0};
+  if (has_b || nj) {
+    for (int32_t k = 0; k < ne; ++k) {
+      const v3 t = v3_scale(nk[k], ar[k]);
+      n.x += t.x;
+      n.y += t.y;
+      n.z += t.z;
+    }
+    const double tiny = 1e-12 * atot * atot;
+    if (v3_dot(n, n) <= tiny && has_b) n = v3_sub(cb, ca);
+    if (v3_dot(n, n) <= tiny) { n.x = 0; n.y = 0; n.z = 1; }
+    n = v3_normalized(n);
+  } else {
+    v3 e = {0, 0, 0};
+    v3_addc(&e, S->axis, (double)S->sign);
+    n = xf_dir(X, e);
+  }
+  v3 t1, t2;
+  frame_of(n, &t1, &t2);
+  double W = 0.0;
+  v3 pc = {0, 0, 0};
+  for (int32_t k = 0; k < ne; ++k) {
+    ws[k] = ar[k] * MAXD(0.05, fabs(v3_dot(n, nk[k])));
+    W += ws[k];
+    pc.x += xs[k].x * ws[k];
+    pc.y += xs[k].y * ws[k];
+    pc.z += xs[k].z * ws[k];
+  }
+  pc = v3_scale(pc, 1.0 / W);
+  {
+    double s11 = 0.0, s22 = 0.0, s12 = 0.0;
+    for (int32_t k = 0; k < ne; ++k) {
+      const v3 d = v3_sub(xs[k], pc);
+      const double y1 = v3_dot(d, t1), y2 = v3_dot(d, t2);
+      s11 += ws[k] * y1 * y1;
+      s22 += ws[k] * y2 * y2;
+      s12 += ws[k] * y1 * y2;
+    }
+    if (fabs(s12) > 1e-9 * (s11 + s22)) {
+      const double half = 0.5 * (s11 - s22);
+      const double l1 = 0.5 * (s11 + s22) + sqrt(half * half + s12 * s12);
+      double e1 = s12, e2 = l1 - s11;
+      if (fabs(l1 - s22) > fabs(e2)) {
+        e1 = l1 - s22;
+        e2 = s12;
+      }
+      const double en = sqrt(e1 * e1 + e2 * e2);
+      if (en > 0.0) {
+        e1 /= en;
+        e2 /= en;
+        const v3 u1 = {t1.x * e1 + t2.x * e2, t1.y * e1 + t2.y * e2, t1.z * e1 + t2.z * e2};
+        const v3 u2 = {t2.x * e1 - t1.x * e2, t2.y * e1 - t1.y * e2, t2.z * e1 - t1.z * e2};
+        t1 = u1;
+        t2 = u2;
+      }
+    }
+  }
+  B.n.x = n.x; B.n.y = n.y; B.n.z = n.z;
+  B.t1.x = t1.x; B.t1.y = t1.y; B.t1.z = t1.z;
+  B.t2.x = t2.x; B.t2.y = t2.y; B.t2.z = t2.z;
+  B.p.x = pc.x; B.p.y = pc.y; B.p.z = pc.z;
+  B.area = MAXD(W, 0.25 * atot);
+  double s1 = 0.0, s2 = 0.0, m1 = 0.0, m2 = 0.0, own = 0.0;
+  for (int32_t k = 0; k < ne; ++k) {
+    const v3 d = v3_sub(xs[k], pc);
+    const double y1 = v3_dot(d, t1), y2 = v3_dot(d, t2);
+    s1 += ws[k] * y1 * y1;
+    s2 += ws[k] * y2 * y2;
+    m1 = MAXD(m1, fabs(y1) + 0.5 * sd[k]);
+    m2 = MAXD(m2, fabs(y2) + 0.5 * sd[k]);
+    own += ws[k] * sd[k] * sd[k];
+  }
+  own /= W;
+  B.s1 = s1 + B.area * own / 12.0;
+  B.s2 = s2 + B.area * own / 12.0;
+  B.c1 = m1;
+  B.c2 = m2;
+  B.rmax = sqrt(B.c1 * B.c1 + B.c2 * B.c2);
+  if (has_b) {
+    const v3 d = v3_sub(cb, ca);
+    const double L = MAXD(MAXD(fabs(v3_dot(d, n)), 0.5 * sqrt(v3_dot(d, d))), 0.5 * h);
+    const double x = v3_dot(v3_sub(pc, ca), n), lo = 0.1 * L, hi = 0.9 * L;
+    B.la = x < lo ? lo : (hi < x ? hi : x);
+    B.lb = L - B.la;
+  } else {
+    B.la = MAXD(0.25 * h, v3_dot(v3_sub(pc, ca), n));
+    B.lb = 0.5 * h;
+  }
+  B.strength = MIND(S->strength_a, S->strength_b);
+  if (S->sectioned) {
+    double ft = 0, fb = 0, fc = 0, coh = 0, mu = 0, wsum = 0;
+    const double sw = 1.0 / (double)(Sj * Sj > 1 ? Sj * Sj : 1);
+    for (int32_t k = 0; k < ne; ++k) {
+      uint8_t va, vb, da, db;
+      double w;
+      if (k < nf) {
+        va = F[k].vox_lo; vb = F[k].vox_hi; da = F[k].damage_lo; db = F[k].damage_hi;
+        w = 1.0;
+      } else {
+        const svxg_junction* s = &J[k - nf];
+        va = s->vox_v; da = s->damage_v;
+        if (s->kind == 1) { vb = va; db = da; } else { vb = s->vox_o; db = s->damage_o; }
+        w = sw * (double)1.0f;
+      }
+      const svxg_material* A = vox_material(mats, va, vb);
+      const svxg_material* M = vox_material(mats, vb, va);
+      const int dm = da > db ? da : db;
+      const double cond = MAXD(1e-6, 1.0 - (double)dm / 255.0);
+      ft += w * cond * MIND(A->ft, M->ft);
+      fb += w * cond * MIND(A->fb, M->fb);
+      fc += w * cond * MIND(A->fc, M->fc);
+      coh += w * cond * MIND(A->cohesion, M->cohesion);
+      mu += w * MIND(A->friction, M->friction);
+      wsum += w;
+    }
+    if (ne > 0 && wsum > 0.0) {
+      const double w = 1.0 / wsum;
+      B.sectioned = 1;
+      B.ft = (float)(ft * w);
+      B.fb = (float)(fb * w);
+      B.fc = (float)(fc * w);
+      B.coh = (float)(coh * w);
+      B.mu = (float)(mu * w);
+    }
+  }
+  free(xs);
+  free(nk);
+  free(ar);
+  free(sd);
+  free(ws);
+  return B;
+}
+
 void svxo_build_bonds(const svxg_node* nodes, const svxg_section* secs, int32_t nb, const svxg_face* faces,
+                      const svxg_junction* juncs, const svxg_lattice* lats, int32_t samples,
                       const svxg_material* mats, svxg_bond* out) {
   for (int32_t k = 0; k < nb; ++k) {
     const svxg_section* S = &secs[k];
+    if (S->junctions > 0 || (lats && !lats[S->grid].identity)) {  /* SecAcc::finish (world_internal.hpp:130-133) */
+      out[k] = finish_general(nodes, S, faces + S->first_face, juncs ? juncs + S->first_junction : NULL, lats,
+                              samples, mats);
+      out[k].tag = k;
+      continue;
+    }
     const svxg_face* F = faces + S->first_face;
     const int32_t nf = S->faces;
     svxg_bond B;

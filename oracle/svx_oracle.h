@@ -71,9 +71,13 @@ void svxo_invalidate(svxo_problem* P);
 int svxo_assembled(const svxo_problem* P);
 int svxo_preconditioner_current(const svxo_problem* P);
 
-/* The bonds of the given interfaces: SecAcc::finish_lattice + section_strengths
- * (core/src/world/world_internal.hpp:133-232, :370-399), bond k from secs[k]. */
+/* The bonds of the given interfaces: SecAcc::finish (finish_lattice / finish_general) +
+ * section_strengths / section_strengths_general (core/src/world/world_internal.hpp:130-441),
+ * bond k from secs[k]; lattices (by section grid and sample vg) and junctions may be NULL when
+ * no section has junction samples and every faces' lattice is the identity; samples: junction
+ * samples per face edge. */
 void svxo_build_bonds(const svxg_node* nodes, const svxg_section* secs, int32_t nb, const svxg_face* faces,
+                      const svxg_junction* juncs, const svxg_lattice* lats, int32_t samples,
                       const svxg_material* mats, svxg_bond* out);
 
 /* K (after svxo_assemble). rowptr: nfree + 1, col: nnzb, val: 36 nnzb, dof: n. */

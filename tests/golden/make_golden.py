@@ -99,18 +99,23 @@ def sections():
     from oracle import build_bonds
     out_dir = os.path.join(HERE, "sections")
     os.makedirs(out_dir, exist_ok=True)
-    for name in ("tower2", "piece", "handmade"):
+    from opus_destruct_2_gb300.graph import JUNCTION_DTYPE, LATTICE_DTYPE
+    for name in ("tower2", "piece", "handmade", "general"):
+        js, lats = np.zeros(0, JUNCTION_DTYPE), np.zeros(0, LATTICE_DTYPE)
         if name == "tower2":
             nodes, _, _, mats = synth.tower_graph(2, seed=5)
             secs, faces = synth.last_sections()
         elif name == "piece":
             nodes, secs, faces, mats = sc.generated("piece")
-        else:
+        elif name == "handmade":
             nodes, secs, faces, mats = sc.handmade()
-        bonds = build_bonds(nodes, secs, faces, mats, reference=True)
+        else:
+            nodes, secs, faces, js, lats, mats = sc.general(4, count=120)
+        bonds = build_bonds(nodes, secs, faces, mats, reference=True, junctions=js if len(js) else None,
+                            lattices=lats if len(lats) else None)
         np.savez_compressed(os.path.join(out_dir, f"{name}.npz"), nodes=nodes, secs=secs, faces=faces, mats=mats,
-                            bonds=bonds)
-        print("sections", name, len(secs), len(faces))
+                            junctions=js, lattices=lats, bonds=bonds)
+        print("sections", name, len(secs), len(faces), len(js))
 
 
 def pieces():

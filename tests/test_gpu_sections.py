@@ -1,6 +1,6 @@
 """Bonds from voxel-face interfaces on the device (svxg_build_bonds, through the C ABI) against
-the oracle's restatement of SecAcc::finish_lattice + section_strengths
-(core/src/world/world_internal.hpp:133-232, :370-399), itself pinned bit for bit to the
+the oracle's restatement of SecAcc::finish (finish_lattice / finish_general) + section_strengths
+(_general) (core/src/world/world_internal.hpp:130-441), itself pinned bit for bit to the
 reference's own header code (test_oracle_pin.py, golden/sections/). Bar: bit for bit, every field
 of every bond (integer and floating point: the same operations in the same order, no
 contraction)."""
@@ -24,6 +24,16 @@ def test_build_bonds_bit_exact(name):
     nodes, secs, faces, mats = CASES[name]
     got = build_bonds(nodes, secs, faces, mats)
     want = oracle.build_bonds(nodes, secs, faces, mats)
+    assert fx.same_records(got, want)
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_build_bonds_general_bit_exact(seed):
+    """Placed lattices and junction samples between lattices (finish_general,
+    section_strengths_general), mixed with lattice sections: bit for bit the oracle's."""
+    nodes, secs, faces, js, lats, mats = sc.general(seed)
+    got = build_bonds(nodes, secs, faces, mats, junctions=js, lattices=lats)
+    want = oracle.build_bonds(nodes, secs, faces, mats, junctions=js, lattices=lats)
     assert fx.same_records(got, want)
 
 
@@ -55,7 +65,7 @@ def test_build_bonds_device_counts_bad_sections():
     L = load_library()
     rc = L.svxg_build_bonds_device(ctypes.c_void_p(t["nodes"].data_ptr()), len(nodes),
                                    ctypes.c_void_p(t["secs"].data_ptr()), len(secs),
-                                   ctypes.c_void_p(t["faces"].data_ptr()), len(faces),
+                                   ctypes.c_void_p(t["faces"].data_ptr()), len(faces), None, 0, None, 0, 2,
                                    ctypes.c_void_p(t["mats"].data_ptr()), ctypes.c_void_p(out.data_ptr()),
                                    ctypes.c_void_p(nbad.data_ptr()), None)
     assert rc == 0

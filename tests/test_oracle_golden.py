@@ -83,7 +83,9 @@ def test_oracle_sections_match_reference_golden(path):
     SecAcc::finish_lattice + section_strengths made of the same interfaces: bit for bit."""
     from oracle import build_bonds
     g = np.load(path)
-    out = build_bonds(g["nodes"], g["secs"], g["faces"], g["mats"])
+    js, lats = g["junctions"], g["lattices"]
+    out = build_bonds(g["nodes"], g["secs"], g["faces"], g["mats"], junctions=js if len(js) else None,
+                      lattices=lats if len(lats) else None)
     assert fx.same_records(out, g["bonds"])
 
 

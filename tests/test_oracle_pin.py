@@ -129,6 +129,16 @@ from oracle import build_bonds  # noqa: E402
 SECTIONS = scases.cases()
 
 
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_build_bonds_general_bit_identical(seed):
+    """finish_general + section_strengths_general (placed lattices, junction samples) of the C
+    restatement against the reference's own header code, bit for bit."""
+    nodes, secs, faces, js, lats, mats = scases.general(seed)
+    a = build_bonds(nodes, secs, faces, mats, junctions=js, lattices=lats)
+    b = build_bonds(nodes, secs, faces, mats, reference=True, junctions=js, lattices=lats)
+    assert fx.same_records(a, b)
+
+
 @pytest.mark.parametrize("name", list(SECTIONS), ids=list(SECTIONS))
 def test_build_bonds_bit_identical(name):
     """Section geometry (SecAcc::finish_lattice + section_strengths) of the C restatement against
