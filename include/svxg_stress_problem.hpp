@@ -149,6 +149,65 @@ class StressProblem {
     fi[5] += rx * F.y - ry * F.x;
   }
 
+  // World::Impl::judge's break rounds of this structure (svxg_cascade): nodes and bonds are left
+  // retired and broken as the reference's world leaves them. judged / judged_has: the steady loads
+  // per bond, in and out (both empty: none yet; then they are filled).
+  struct Cascade {
+    svxg_cascade_result result{};
+    std::vector<int32_t> broken, retired;
+    std::vector<double> phi;
+  };
+  Cascade cascade(const std::vector<double>& f, std::vector<double>& u,
+                  const svxg_cascade_options& o = svxg_default_cascade_options(),
+                  std::vector<svxg_bond_load>* judged = nullptr, std::vector<uint8_t>* judged_has = nullptr) {
+    upload_if_changed();
+    Cascade c;
+    u.resize(6 * nodes.size(), 0.0);
+    c.broken.resize(bonds.size() + 1);
+    c.retired.resize(nodes.size() + 1);
+    c.phi.resize(bonds.size() + 1);
+    if (judged && judged_has) {
+      judged->resize(bonds.size());
+      judged_has->resize(bonds.size(), 0);
+    }
+    check(svxg_cascade(p_, nullptr, &o, f.data(), u.data(), judged && judged_has ? judged->data() : nullptr,
+                       judged && judged_has ? judged_has->data() : nullptr, c.phi.data(), c.broken.data(),
+                       int32_t(c.broken.size()), c.retired.data(), int32_t(c.retired.size()), &c.result));
+    c.broken.resize(size_t(c.result.bonds_broken));
+    c.retired.resize(size_t(c.result.nodes_retired));
+    c.phi.resize(bonds.size());
+    for (int32_t i : c.retired) nodes[size_t(i)].gone = 1;
+    sent_nodes_ = nodes;
+    pull_flags();
+    return c;
+  }
+
+  // World::Impl::body_stress_run's break rounds of this piece (svxg_piece_rounds): f is its load
+  // and comes back with the chips' loads moved; gf: fracture energy per material (null: presets).
+  struct PieceRounds {
+    svxg_piece_result result{};
+    std::vector<int32_t> broken, chips;
+    std::vector<uint8_t> modes;
+  };
+  PieceRounds piece_rounds(std::vector<double>& f, std::vector<double>& u,
+                           const svxg_piece_options& o = svxg_default_piece_options(), const double* gf = nullptr) {
+    upload_if_changed();
+    PieceRounds r;
+    u.resize(6 * nodes.size(), 0.0);
+    r.broken.resize(bonds.size() + 1);
+    r.modes.resize(bonds.size() + 1);
+    r.chips.resize(nodes.size() + 1);
+    check(svxg_piece_rounds(p_, nullptr, &o, gf, f.data(), u.data(), r.broken.data(), r.modes.data(),
+                            int32_t(r.broken.size()), r.chips.data(), int32_t(r.chips.size()), &r.result));
+    r.broken.resize(size_t(r.result.bonds_broken));
+    r.modes.resize(size_t(r.result.bonds_broken));
+    r.chips.resize(size_t(r.result.chips));
+    for (int32_t i : r.chips) nodes[size_t(i)].gone = 1;
+    sent_nodes_ = nodes;
+    pull_flags();
+    return r;
+  }
+
   svxg_info info() const {
     svxg_info i{};
     check(svxg_get_info(p_, &i));
@@ -186,5 +245,21 @@ class StressProblem {
   std::vector<svxg_node> sent_nodes_;
   std::vector<svxg_bond> sent_bonds_;
 };
+
+// SecAcc::finish + section_strengths(_general) of every interface (svxg_build_bonds): bond k of
+// the result from secs[k].
+inline std::vector<svxg_bond> build_bonds(const std::vector<svxg_node>& nodes, const std::vector<svxg_section>& secs,
+                                          const std::vector<svxg_face>& faces,
+                                          const std::vector<svxg_material>& mats,
+                                          const std::vector<svxg_junction>& junctions = {},
+                                          const std::vector<svxg_lattice>& lattices = {}, int32_t samples = 2) {
+  std::vector<svxg_bond> out(secs.size());
+  const int e = svxg_build_bonds(nodes.data(), int32_t(nodes.size()), secs.data(), int32_t(secs.size()), faces.data(),
+                                 int64_t(faces.size()), junctions.empty() ? nullptr : junctions.data(),
+                                 int64_t(junctions.size()), lattices.empty() ? nullptr : lattices.data(),
+                                 int32_t(lattices.size()), samples, mats.data(), out.data());
+  if (e < 0) throw std::runtime_error(std::string("svxg: ") + svxg_last_error());
+  return out;
+}
 
 }  // namespace svxg

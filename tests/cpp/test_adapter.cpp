@@ -166,6 +166,58 @@ int main() {
     }
     CHECK(err <= 1e-12 * mag);
   }
+  {
+    // the judge's break rounds: an overloaded cantilever breaks at its support, and the part that
+    // no support holds retires (then nothing is left over strength)
+    svxg::StressProblem P;
+    cantilever(P, 8, 0.5, 2.0e5);
+    CHECK(P.assemble());
+    std::vector<double> u;
+    svxg_cascade_options o = svxg_default_cascade_options();
+    o.rtol = 1e-10;
+    o.maxit = 1000;
+    const auto c = P.cascade(gravity(P), u, o);
+    CHECK(c.result.status == SVXG_CASCADE_SETTLED);
+    CHECK(c.result.rounds >= 1 && !c.broken.empty() && c.broken[0] == 0);
+    CHECK(int(c.retired.size()) == 8);
+    CHECK(P.bonds[0].broken == 1);
+    for (const svxg_node& nd : P.nodes) CHECK(nd.gone == 1);
+  }
+  {
+    // a piece's break rounds on the same cantilever pinned at its root: rounds run, loads move
+    svxg::StressProblem P;
+    cantilever(P, 8, 0.5, 2.0e5);
+    P.bonds.erase(P.bonds.begin());  // (no support: a free piece, pinned at node 0)
+    P.nodes[0].fixed = 1;
+    std::vector<double> f = gravity(P), u;
+    svxg_piece_options o = svxg_default_piece_options();
+    o.rtol = 1e-10;
+    o.maxit = 1000;
+    const auto r = P.piece_rounds(f, u, o);
+    CHECK(r.result.checks >= 1);
+    CHECK(r.broken.size() == r.modes.size());
+    CHECK(r.result.status != SVXG_PIECE_SOLVE_FAILED && r.result.status != SVXG_PIECE_SINGULAR);
+  }
+  {
+    // bonds from voxel faces: two voxels side by side (lattice voxel i centred at h i), one face
+    std::vector<svxg_node> nodes(2);
+    nodes[0].c = {0.0, 0.0, 0.0};
+    nodes[1].c = {0.5, 0.0, 0.0};
+    svxg_section sec{};
+    sec.a = 0;
+    sec.b = 1;
+    sec.faces = 1;
+    sec.sectioned = 1;
+    sec.h = 0.5;
+    sec.strength_a = sec.strength_b = 1.0;
+    svxg_face fc{};
+    fc.axis = 0;
+    fc.sign = 1;
+    fc.vox_lo = fc.vox_hi = 2;  // (material 1 on both sides)
+    const auto b = svxg::build_bonds(nodes, {sec}, {fc}, materials());
+    CHECK(b.size() == 1 && b[0].n.x == 1.0 && b[0].area == 0.25 && b[0].la == 0.25 && b[0].lb == 0.25);
+    CHECK(b[0].sectioned == 1 && b[0].faces == 1);
+  }
   std::printf(failures ? "%d failures\n" : "ok\n", failures);
   return failures ? 1 : 0;
 }
