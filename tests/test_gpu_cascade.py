@@ -171,3 +171,34 @@ def test_retire_many_nodes_bit_exact(jacobi):
     u, r = G.solve(f, rtol=1e-11, maxit=4000)
     uo, _ = O.solve(f, rtol=1e-11, maxit=4000)
     assert r.converged and relerr(u, uo) <= 1e-6
+
+
+# (detach = 0 is left out: the parts the rounds cut off then float, K is singular and where a solve
+# of an inconsistent singular system breaks down depends on rounding, not on the reference's rules)
+@pytest.mark.parametrize("over", [dict(max_breaks_per_round=1, max_rounds=12), dict(break_band=1.0),
+                                  dict(max_rounds=3), dict(dif=1.0, shock=1)],
+                         ids=["one_a_round", "band_1", "three_rounds", "no_blend"])
+def test_cascade_options_match_oracle(over):
+    """The rounds' options as the reference's world config varies them: the same bonds broken in
+    order, the same nodes retired, the same ending."""
+    name = "tower_f9" if "dif" not in over else "tower_f7_shock"
+    G, O, ro, u, res, ex = run_both(name, **over)
+    assert res.status == ro["status"] and res.rounds == ro["rounds"]
+    assert ex["broken"] == ro["broken"] and ex["retired"] == ro["retired"]
+    assert relerr(u, ro["u"]) <= 1e-6
+
+
+def test_cascade_mixed_precision_problem():
+    """A problem assembled for mixed precision at every size: its solves (FP32 inner sequences,
+    FP64 refinement, K downdated in FP64 only) reach the same tight tolerance, so the rounds are
+    the oracle's."""
+    nodes, bonds, mats, f, ko, so, judged, has = CASES["tower_f9"]
+    kw = dict(ko, **TIGHT)
+    O = oracle.Port(nodes, bonds, mats)
+    ro = oracle.cascade(O, f, np.zeros(6 * len(nodes)), CascadeOptions(**kw), StressOptions(**so))
+    G = StressProblem(nodes, bonds, mats)
+    mixed = StressOptions(precision=2, **so)
+    assert G.assemble(mixed)
+    u, res, ex = G.cascade(f, options=CascadeOptions(**kw), opt=mixed)
+    assert res.status == ro["status"] and ex["broken"] == ro["broken"] and ex["retired"] == ro["retired"]
+    assert relerr(u, ro["u"]) <= 1e-6

@@ -79,3 +79,18 @@ def test_batch_piece_rounds_match_one_by_one():
         assert lists[i]["broken"] == ex["broken"] and lists[i]["chips"] == ex["chips"]
         assert np.array_equal(fs[i], f_out)
         assert relerr(us[i], u) <= 1e-8
+
+
+@pytest.mark.parametrize("over", [dict(rounds=1), dict(max_breaks_per_round=1), dict(energy=0.0),
+                                  dict(round_fraction=1.0), dict(break_band=1.0, energy=5000.0)],
+                         ids=["one_round", "one_a_round", "no_energy", "all_over", "band_energy"])
+def test_piece_options_match_oracle(over):
+    nodes, bonds, mats, f, ko, gf = pc.case("many_chips")
+    o = pc.options(dict(ko, **over))
+    ro = oracle.piece_rounds(oracle.Port(nodes, bonds, mats), f, np.zeros(6 * len(nodes)), o, gf)
+    G = StressProblem(nodes, bonds, mats)
+    u, f_out, res, ex = G.piece_rounds(f, options=o, gf=gf)
+    assert res.status == ro["status"] and res.checks == ro["checks"]
+    assert ex["broken"] == ro["broken"] and ex["modes"] == ro["modes"] and ex["chips"] == ro["chip_nodes"]
+    assert res.spent == ro["spent"] and np.array_equal(f_out, ro["f"])
+    assert relerr(u, ro["u"]) <= 1e-6
