@@ -226,6 +226,18 @@ cudaError_t host_wait(cudaStream_t s) {
   return cudaEventSynchronize(t_wait.ev);
 }
 
+// The calling thread's pool on the current device keeps at most `keep` bytes it is not using
+// (a server slot calls this after each request, so one large request does not leave its peak
+// reserved for good).
+void pool_trim(size_t keep) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kPoolDevices) {
+    cudaGetLastError();
+    return;
+  }
+  if (t_pools.pool[dev]) cudaMemPoolTrimTo(t_pools.pool[dev], keep);
+}
+
 cudaError_t pool_malloc_async(void** p, size_t bytes, cudaStream_t s) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);

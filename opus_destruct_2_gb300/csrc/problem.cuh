@@ -42,6 +42,8 @@ void count_launch();
 // problem, and neither allocation nor release synchronizes the device, so problems on other
 // streams keep running while one is built or torn down.
 cudaError_t pool_malloc_async(void** p, size_t bytes, cudaStream_t s);
+// The calling thread's pool (current device) keeps at most `keep` unused bytes.
+void pool_trim(size_t keep);
 
 // Waits on the host until `s` has drained. Spins (cudaStreamSynchronize) by default; while
 // blocking waits are on - a server with several slots holds them on, so that the slots' host

@@ -395,6 +395,7 @@ void worker(svxg_server* S) {
       S->cv_mem.notify_all();
     }
     record(S, q, res);
+    pool_trim(size_t(1) << 30);  // (this slot's pool keeps at most 1 GiB it is not using)
   }
   if (own) svxg_problem_destroy(own);
 }
