@@ -394,6 +394,72 @@ __global__ void __launch_bounds__(1024) k_mis_small(int32_t n, const int32_t* ro
   }
 }
 
+// The remaining rounds of a long level once few nodes are undecided, in one block over the list
+// of those nodes (the same claim, decide and cover; decided nodes take no part in a round, so
+// the rounds are the full-width ones). Claims are reset on every entry a round wrote.
+__global__ void __launch_bounds__(1024) k_mis_tail(const int32_t* list, int32_t m, const int32_t* rowptr,
+                                                   const int32_t* col, const uint8_t* strong, uint8_t* state,
+                                                   uint8_t* covered, int32_t* claim) {
+  for (int32_t round = 0; round <= m; ++round) {
+    for (int32_t t = threadIdx.x; t < m; t += blockDim.x) {
+      const int32_t i = list[t];
+      if (state[i] != 0) continue;
+      atomicMin(&claim[i], i);
+      for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+        if (strong[k]) atomicMin(&claim[col[k]], i);
+    }
+    __syncthreads();
+    int und = 0;
+    for (int32_t t = threadIdx.x; t < m; t += blockDim.x) {
+      const int32_t i = list[t];
+      if (state[i] != 0) continue;
+      bool cov = covered[i] != 0;
+      bool mine = claim[i] == i;
+      for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+        if (strong[k]) {
+          const int32_t x = col[k];
+          cov = cov || covered[x] != 0;
+          mine = mine && claim[x] == i;
+        }
+      if (cov) state[i] = 2;
+      else if (mine) state[i] = 3;
+      else und = 1;
+    }
+    const int any = __syncthreads_or(und);
+    for (int32_t t = threadIdx.x; t < m; t += blockDim.x) {
+      const int32_t i = list[t];
+      claim[i] = INT_MAX;
+      for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+        if (strong[k]) claim[col[k]] = INT_MAX;
+    }
+    __syncthreads();
+    for (int32_t t = threadIdx.x; t < m; t += blockDim.x) {
+      const int32_t i = list[t];
+      if (state[i] != 3) continue;
+      state[i] = 1;
+      covered[i] = 1;
+      for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+        if (strong[k]) covered[col[k]] = 1;
+    }
+    __syncthreads();
+    if (!any) break;
+  }
+}
+
+// (a round of one block over the list costs about what three grid-wide launches cost once the
+// list is this short)
+constexpr int32_t kMisTail = 1024;
+
+__global__ void k_undecided_flags(int32_t n, const uint8_t* state, int32_t* flag) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) flag[i] = state[i] == 0 ? 1 : 0;
+}
+
+__global__ void k_list_flagged(int32_t n, const int32_t* flag, const int32_t* pos, int32_t* out) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && flag[i]) out[pos[i]] = i;
+}
+
 __global__ void k_root_flags(int32_t n, const uint8_t* state, int32_t* flag) {
   const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) flag[i] = state[i] == 1 ? 1 : 0;
@@ -1270,6 +1336,16 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
       int32_t u = 0;
       TRY(copy_to_host(P, &u, undecided.p + (kBatch - 1), sizeof(int32_t)));
       if (u == 0) break;
+      if (u <= kMisTail) {
+        // (the long tail of rounds over the few nodes left: one block launch)
+        (k_undecided_flags<<<nblk(n), kT, 0, st>>>(n, state.p, flag.p), SVXG_COUNT_LAUNCH());
+        int32_t m = 0;
+        TRY(exclusive_scan_i32(P, flag.p, rank.p, n, &m));
+        (k_list_flagged<<<nblk(n), kT, 0, st>>>(n, flag.p, rank.p, agg1.p), SVXG_COUNT_LAUNCH());
+        (k_mis_tail<<<1, 1024, 0, st>>>(agg1.p, m, A.rowptr, A.col, strong.p, state.p, covered.p, claim.p),
+         SVXG_COUNT_LAUNCH());
+        break;
+      }
     }
     (k_root_flags<<<nblk(n), kT, 0, st>>>(n, state.p, flag.p), SVXG_COUNT_LAUNCH());
     int32_t na1 = 0;

@@ -28,6 +28,9 @@ CASES = {
     "tower10": (lambda: synth.tower_graph(storeys=10, seed=1)[:2], dict()),
     "piece_free": (lambda: synth.piece_graph(600, free=True, seed=21)[:2], dict(amg_min_nodes=0)),
     "piece_grounded": (lambda: synth.piece_graph(900, free=False, seed=22)[:2], dict(amg_min_nodes=0)),
+    # levels of more than 8192 nodes: aggregation rounds across the grid, then the one-block tail
+    "lattice24": (lambda: fx.lattice(24), dict()),
+    "city3": (lambda: synth.city_graph(lots_x=3, lots_y=3, seed=2)[:2], dict()),
 }
 
 
