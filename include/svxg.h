@@ -91,6 +91,10 @@ int svxg_extend_warm_start(svxg_problem* p, double* u, int32_t first_new);
  * K downdates that keep the preconditioner. */
 int svxg_remove_bond(svxg_problem* p, int32_t b);
 int svxg_retire_nodes(svxg_problem* p, const int32_t* list, int32_t count);
+/* remove_bond of each listed bond, in list order (the reference's loop of calls, e.g. a judge
+ * round's breaks, world.cpp:1258-1270), with one device pass and one wait: K's blocks get the
+ * same subtractions in the same order. */
+int svxg_remove_bonds(svxg_problem* p, const int32_t* list, int32_t count);
 /* The bonds' in_k / broken flags as the problem keeps them (the reference writes them into the
  * caller's bonds). Either pointer may be null. */
 int svxg_bond_flags(svxg_problem* p, uint8_t* broken, uint8_t* in_k);

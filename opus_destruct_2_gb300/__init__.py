@@ -83,6 +83,7 @@ def load_library() -> ctypes.CDLL:
         "svxg_release": (c_i32, [c_vp]),
         "svxg_remove_bond": (c_i32, [c_vp, c_i32]),
         "svxg_retire_nodes": (c_i32, [c_vp, c_vp, c_i32]),
+        "svxg_remove_bonds": (c_i32, [c_vp, c_vp, c_i32]),
         "svxg_bond_flags": (c_i32, [c_vp, c_vp, c_vp]),
         "svxg_solve": (c_i32, [c_vp, c_vp, c_vp, c_f64, c_i32, c_i32, c_vp]),
         "svxg_solve_device": (c_i32, [c_vp, c_vp, c_vp, c_f64, c_i32, c_i32, c_vp]),
@@ -249,6 +250,12 @@ class StressProblem:
 
     def remove_bond(self, b: int):
         _check(self._L.svxg_remove_bond(self._h, int(b)))
+        self._pull_flags()
+
+    def remove_bonds(self, lst):
+        """remove_bond of each listed bond in order, in one device pass."""
+        a = np.ascontiguousarray(lst, dtype=np.int32)
+        _check(self._L.svxg_remove_bonds(self._h, ptr(a), len(a)))
         self._pull_flags()
 
     def retire_nodes(self, lst):

@@ -564,6 +564,38 @@ int svxg_remove_bond(svxg_problem* p, int32_t b) {
   return SVXG_OK;
 }
 
+// remove_bond of each listed bond in list order, with one device pass and one wait
+int svxg_remove_bonds(svxg_problem* p, const int32_t* list, int32_t count) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  if (count <= 0) return SVXG_OK;
+  if (!list) return SVXG_ERR_ARG;
+  for (int32_t t = 0; t < count; ++t)
+    if (list[t] < 0 || list[t] >= P.nb) {
+      set_error("svxg_remove_bonds: no such bond");
+      return SVXG_ERR_ARG;
+    }
+  DeviceScope ds(P.device);
+  std::vector<int32_t> rm;
+  rm.reserve(size_t(count));
+  for (int32_t t = 0; t < count; ++t) {
+    const int32_t b = list[t];
+    P.h_broken[size_t(b)] = 1;
+    if (!P.assembled || !P.h_in_k[size_t(b)]) {
+      TRY(upload_bond_flags(P, b));  // (not in K: the bond only breaks)
+      continue;
+    }
+    P.h_in_k[size_t(b)] = 0;  // (a repeat of the bond later in the list is then a no-op, as the reference's)
+    rm.push_back(b);
+  }
+  if (!rm.empty()) {
+    TRY(remove_bonds_device(P, rm.data(), int32_t(rm.size())));
+    if (!P.jacobi_only) P.pc_current = false;
+  }
+  P.active = false;
+  return SVXG_OK;
+}
+
 int svxg_retire_nodes(svxg_problem* p, const int32_t* list, int32_t count) {
   CHECK_P(p);
   Problem& P = p->P;

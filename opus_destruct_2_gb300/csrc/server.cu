@@ -250,8 +250,8 @@ int run_repeat(svxg_problem* p, Request& q, svxg_request_result* res) {
     set_error("repeat request: node count differs from the resident structure's");
     return SVXG_ERR_ARG;
   }
-  for (int32_t b : q.remove) {
-    const int e = svxg_remove_bond(p, b);
+  if (!q.remove.empty()) {
+    const int e = svxg_remove_bonds(p, q.remove.data(), int32_t(q.remove.size()));
     if (e) return e;
   }
   svxg_pcg_result r{};

@@ -202,3 +202,26 @@ def test_cascade_mixed_precision_problem():
     u, res, ex = G.cascade(f, options=CascadeOptions(**kw), opt=mixed)
     assert res.status == ro["status"] and ex["broken"] == ro["broken"] and ex["retired"] == ro["retired"]
     assert relerr(u, ro["u"]) <= 1e-6
+
+
+@pytest.mark.parametrize("jacobi", [False, True], ids=["amg", "jacobi"])
+def test_remove_bonds_list_bit_exact(jacobi):
+    """remove_bonds (one device pass) of a list with repeats and bonds sharing nodes: K and the
+    flags as the oracle's remove_bond calls in the same order."""
+    nodes, bonds = fx.lattice(7)
+    mats = default_materials()
+    opt = StressOptions(amg_min_nodes=1 << 30 if jacobi else 16)
+    G = StressProblem(nodes, bonds, mats)
+    O = oracle.Port(nodes, bonds, mats)
+    assert G.assemble(opt) and O.assemble(opt)
+    rng = np.random.default_rng(5)
+    lst = rng.choice(len(bonds), size=60, replace=False).astype(np.int32)
+    lst = np.concatenate([lst, lst[:5]])  # (repeats: no-ops)
+    G.remove_bonds(lst)
+    for b in lst:
+        O.remove_bond(int(b))
+    a, b = G.debug_matrix(), O.matrix()
+    assert np.array_equal(a["val"], b["val"])
+    br, ik = O.bond_flags()
+    assert np.array_equal(G.bonds["broken"], br) and np.array_equal(G.bonds["in_k"], ik)
+    assert G.preconditioner_current() == O.preconditioner_current()
