@@ -1,0 +1,75 @@
+"""The city block at its full size (the plain-FP64-at-scale configuration: 187,893 fragments,
+452,741 bonds, 1.13 M DOF) against the oracle, on the device.
+
+Bars: K and the whole multigrid hierarchy's integer structure (level sizes, blocks,
+prolongation sizes, work counters) bit for bit; u within 1e-6 relative for the FP64 solve and
+1e-5 for the mixed-precision one (FP32 K and V-cycle inside FP64 refinement), both solved to
+rel. residual 1e-10; the set of failing bonds identical; the device's residual, recomputed on the
+host from the device's own K, at the requested tolerance."""
+import numpy as np
+import pytest
+
+import oracle
+from opus_destruct_2_gb300 import StressProblem, synth
+from opus_destruct_2_gb300.graph import PRECISION_MIXED_ALL, StressOptions
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def city():
+    nodes, bonds, f, mats = synth.city_graph(lots_x=8, lots_y=8, seed=2)
+    O = oracle.Port(nodes, bonds, mats)
+    assert O.assemble(StressOptions())
+    uo, ro = O.solve(f, rtol=1e-10, maxit=2000)
+    assert ro.converged
+    _, phi_o, _ = O.judge(uo)
+    return dict(nodes=nodes, bonds=bonds, f=f, mats=mats, O=O, uo=uo, failing=np.nonzero(phi_o >= 1.0)[0])
+
+
+def relerr(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+def residual(G, u, f):
+    """||f - K u|| / ||f|| over the free DOFs with the device's own K (host arithmetic)."""
+    m = G.debug_matrix()
+    dof, rowptr, col, val = m["dof"], m["rowptr"], m["col"], m["val"]
+    nf = m["nfree"]
+    x = np.zeros((nf, 6))
+    b = np.zeros((nf, 6))
+    free = dof >= 0
+    x[dof[free]] = u.reshape(-1, 6)[free]
+    b[dof[free]] = f.reshape(-1, 6)[free]
+    rows = np.repeat(np.arange(nf), np.diff(rowptr))
+    y = np.zeros((nf, 6))
+    np.add.at(y, rows, np.einsum("kij,kj->ki", val, x[col]))
+    return float(np.linalg.norm(b - y) / np.linalg.norm(b))
+
+
+def test_city_block_fp64(city):
+    G = StressProblem(city["nodes"], city["bonds"], city["mats"])
+    assert G.assemble(StressOptions())
+    gi, oi = G.info(), city["O"].info()
+    assert gi.sizes() == oi.sizes() and gi.blocks() == oi.blocks()
+    for k in ("nfree", "chol_n", "matrix_blocks", "work_per_iteration", "assembly_work", "work_per_apply",
+              "build_work"):
+        assert getattr(gi, k) == getattr(oi, k), k
+    a, b = G.debug_matrix(), city["O"].matrix()
+    assert np.array_equal(a["rowptr"], b["rowptr"]) and np.array_equal(a["col"], b["col"])
+    assert np.array_equal(a["val"], b["val"])
+    u, r = G.solve(city["f"], rtol=1e-10, maxit=2000)
+    assert r.converged and relerr(u, city["uo"]) <= 1e-6
+    assert residual(G, u, city["f"]) <= 1e-10 * 1.01
+    phi, _, failing = G.utilization(1.0)
+    assert np.array_equal(np.sort(failing), city["failing"])
+
+
+def test_city_block_mixed(city):
+    G = StressProblem(city["nodes"], city["bonds"], city["mats"])
+    assert G.assemble(StressOptions(precision=PRECISION_MIXED_ALL))
+    u, r = G.solve(city["f"], rtol=1e-10, maxit=4000)
+    assert r.converged and relerr(u, city["uo"]) <= 1e-5
+    assert residual(G, u, city["f"]) <= 1e-10 * 1.01
+    _, _, failing = G.utilization(1.0)
+    assert np.array_equal(np.sort(failing), city["failing"])
