@@ -4,12 +4,14 @@
 //   inner (FP32):  K32 d = r32 by AMG-preconditioned CG to ||r_in|| <= tol_in ||r32||, from d = 0
 //                  (tol_in = max(1e-4, 0.3 rtol ||f|| / ||r||): as few outer steps as f32 allows):
 //                  SpMV and the V-cycle in FP32 (K32 is K rounded to f32, the cycle's own level-0
-//                  operator), dot products accumulated in FP64
+//                  operator), dot products with exact products and double-float partial sums,
+//                  returned in FP64 (FF below)
 //   update (FP64): x += d
-// FP64 stays where the benchmark spec keeps it: the outer residual, the dots and the coarsest dense
-// factor. The refinement converges to the FP64 solution (its residual is the FP64 K's), so the
-// result meets the same rtol as the plain FP64 solve; each inner iteration reads half the bytes
-// of an FP64 one and issues FP32 arithmetic (GB300's FP64 rate is a small fraction of FP32).
+// FP64 (or its double-float equal in the dots) stays in the outer residual, the dots and the
+// coarsest dense factor. The refinement converges to the FP64 solution (its residual is the FP64
+// K's), so the result meets the same rtol as the plain FP64 solve; each inner iteration reads half
+// the bytes of an FP64 one and issues FP32 arithmetic (GB300's FP64 rate is a small fraction of
+// FP32).
 // Restarting the inner sequence at each outer step costs iterations (its Krylov space is lost),
 // but a single f32 sequence with reliable updates does not converge on slender structures:
 // f32 Krylov vectors lose conjugacy when the condition number times 2^-24 approaches 1. Each
@@ -29,7 +31,6 @@ constexpr int kRows = kT / 32;
 constexpr int32_t kInnerCap = 60;
 constexpr double kMinGain = 0.1;
 inline unsigned vblk(int32_t n) { return unsigned((std::max(n, 1) + kT - 1) / kT); }
-inline unsigned rblk(int32_t n) { return unsigned((std::max(n, 1) + kRows - 1) / kRows); }
 
 #define TRY(x)            \
   do {                    \
@@ -60,6 +61,104 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
   return s;
 }
 
+// Double-float sums for the inner dots. A pair (hi, lo) of floats, read as hi + lo, carries about
+// 48 significant bits, and the product of two floats is exact in it; summing in pairs issues FP32
+// instructions, where an FP64 sum of the same terms issues FP64 ones, which GB300 runs at a small
+// fraction of the FP32 rate (in the fused SpMV the FP64 reduction, not the memory, set the time).
+// The methods are published ones:
+//   a thread's terms:    Dot2 (Ogita, Rump and Oishi, "Accurate sum and dot product", SIAM J. Sci.
+//                        Comput. 26 (2005), Alg. 5.3): TwoProduct by FMA, TwoSum of the high parts,
+//                        the rounding errors summed beside them;
+//   combining partials:  the accurate double-word addition (Joldes, Muller and Popescu, "Tight and
+//                        rigorous error bounds for basic building blocks of double-word arithmetic",
+//                        ACM TOMS 44 (2017), Alg. 6), relative error below 3u^2.
+// The explicitly rounded intrinsics are never contracted into FMAs, which the error-free
+// transformations need. The sums are combined in a fixed order: results are the same bits on every
+// run, and the total is returned as an FP64 value.
+struct FF {
+  float hi, lo;
+};
+
+__device__ __forceinline__ FF two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return FF{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+
+__device__ __forceinline__ FF fast_two_sum(float a, float b) {  // |a| >= |b| or a == 0
+  const float s = __fadd_rn(a, b);
+  return FF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+// Dot2 step: acc.hi the running sum of the products' high parts, acc.lo the sum of the errors
+__device__ __forceinline__ void dot2_add(FF& acc, float x, float y) {
+  const float h = __fmul_rn(x, y);
+  const float r = __fmaf_rn(x, y, -h);
+  const FF t = two_sum(acc.hi, h);
+  acc.hi = t.hi;
+  acc.lo = __fadd_rn(acc.lo, __fadd_rn(t.lo, r));
+}
+
+// a Dot2 accumulator as a normalised double-float value
+__device__ __forceinline__ FF dot2_value(FF acc) { return two_sum(acc.hi, acc.lo); }
+
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  FF s = two_sum(a.hi, b.hi);
+  const FF t = two_sum(a.lo, b.lo);
+  s = fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
+  return fast_two_sum(s.hi, __fadd_rn(s.lo, t.lo));
+}
+
+// lanes xor-combined from `first` down (16: the whole warp; 4: lanes 0-7)
+__device__ __forceinline__ FF ff_warp_sum(FF v, int first) {
+  for (int d = first; d > 0; d >>= 1)
+    v = ff_add(v, FF{__shfl_xor_sync(0xffffffffu, v.hi, d), __shfl_xor_sync(0xffffffffu, v.lo, d)});
+  return v;
+}
+
+// the block's sum in thread 0
+__device__ __forceinline__ FF ff_block_sum(FF v, float2* sh, int first) {
+  v = ff_warp_sum(v, first);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sh[w] = make_float2(v.hi, v.lo);
+  __syncthreads();
+  FF s{0.0f, 0.0f};
+  if (w == 0) {
+    if (lane < int(blockDim.x) / 32) s = FF{sh[lane].x, sh[lane].y};
+    s = ff_warp_sum(s, 16);
+  }
+  return s;
+}
+
+// last-block reduction of double-float partials (stored as float pairs in the FP64 partials
+// buffer); true in every thread of the last block, the FP64 total in tot
+__device__ __forceinline__ bool reduce_last_ff(FF v, int first, double* partials, unsigned* counter, double* tot) {
+  __shared__ float2 sh[32];
+  __shared__ bool last;
+  float2* pp = reinterpret_cast<float2*>(partials);
+  const FF bs = ff_block_sum(v, sh, first);
+  if (threadIdx.x == 0) {
+    pp[blockIdx.x] = make_float2(bs.hi, bs.lo);
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  FF s{0.0f, 0.0f};
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+    const float2 x = __ldcg(&pp[b]);
+    s = ff_add(s, FF{x.x, x.y});
+  }
+  const FF t = ff_block_sum(s, sh, 16);
+  if (threadIdx.x == 0) {
+    *tot = double(t.hi) + double(t.lo);
+    *counter = 0u;
+  }
+  return true;
+}
+
 // last-block reduction (as solve.cu): true in every thread of the last block, total in tot
 __device__ __forceinline__ bool reduce_last(double v, double* partials, unsigned* counter, double* tot) {
   __shared__ double sh[32];
@@ -83,26 +182,40 @@ __device__ __forceinline__ bool reduce_last(double v, double* partials, unsigned
   return true;
 }
 
-// y32 = K32 p32 (warp per row), p.y accumulated in f64 -> alpha
+// y32 = K32 p32, p.y in double-float -> alpha. Each warp takes kDotSteps row steps (the block's
+// warps on consecutive warp indices at every step), so the block reduction and the wait on the
+// partials' fence and counter are paid once per kDotSteps steps (measured on the city block: 1 step
+// 48 us, 2 steps 42, 4 steps 40, 8 steps 44, the last with a partial last wave).
+constexpr int kDotSteps = 4;
+template <int SCHED>
+inline unsigned spmv_dot_blocks(int32_t n) {
+  const int64_t per = int64_t(kRows) * kDotSteps * RowMap<SCHED>::kRowsPerWarp;
+  return unsigned((std::max<int64_t>(n, 1) + per - 1) / per);
+}
+
 template <int SCHED>
 __global__ void __launch_bounds__(kT) k_spmv32_dot(int32_t n, const int32_t* __restrict__ rowptr,
                                                    const int32_t* __restrict__ col, const float* __restrict__ val,
                                                    const float* __restrict__ p, float* __restrict__ q,
                                                    double* partials, unsigned* counter, MixedScalars* s) {
   if (s->done) return;
-  int c;
-  bool lane_ok;
-  const int32_t row = sched_row<SCHED>(kRows, &c, &lane_ok);
-  const bool row_ok = row < n;
-  const float y = sched_row_product<SCHED, float, float, float>(row_ok, row, rowptr, col, val, p);
-  const int lane = c;
-  double dp = 0.0;
-  if (row_ok && lane_ok) {
-    q[6 * int64_t(row) + lane] = y;
-    dp = double(p[6 * int64_t(row) + lane]) * double(y);
+  FF acc{0.0f, 0.0f};
+  for (int j = 0; j < kDotSteps; ++j) {
+    int c;
+    bool lane_ok;
+    const int32_t warp = (int32_t(blockIdx.x) * kDotSteps + j) * kRows + (threadIdx.x >> 5);
+    const int32_t row = sched_row_of<SCHED>(warp, &c, &lane_ok);
+    const bool row_ok = row < n;
+    if (SCHED == kWarpRow && !row_ok) break;  // (warp-uniform; the warp's rows only grow)
+    const float y = sched_row_product<SCHED, float, float, float>(row_ok, row, rowptr, col, val, p);
+    if (row_ok && lane_ok) {
+      q[6 * int64_t(row) + c] = y;
+      dot2_add(acc, p[6 * int64_t(row) + c], y);
+    }
   }
+  // kWarpRow: only lanes 0-5 hold terms
   double tot;
-  if (reduce_last(dp, partials, counter, &tot) && threadIdx.x == 0) {
+  if (reduce_last_ff(dot2_value(acc), SCHED == kWarpRow ? 4 : 16, partials, counter, &tot) && threadIdx.x == 0) {
     s->pq = tot;
     s->iters += 1;
     if (!(tot > 0)) {
@@ -114,23 +227,23 @@ __global__ void __launch_bounds__(kT) k_spmv32_dot(int32_t n, const int32_t* __r
   }
 }
 
-// d += alpha p, r -= alpha q (f32), ||r|| in f64 -> inner convergence
+// d += alpha p, r -= alpha q (f32), ||r|| -> inner convergence
 __global__ void k_axpy32(int32_t nf, float* __restrict__ d, float* __restrict__ r, const float* __restrict__ p,
                          const float* __restrict__ q, double* partials, unsigned* counter, MixedScalars* s) {
   if (s->done) return;
   const float a = float(s->alpha);
   const int64_t i = int64_t(blockIdx.x) * kT + threadIdx.x;
-  double rr = 0.0;
+  FF rr{0.0f, 0.0f};
   if (i < nf)
     for (int c = 0; c < 6; ++c) {
       const int64_t k = 6 * i + c;
       d[k] += a * p[k];
       const float rv = r[k] - a * q[k];
       r[k] = rv;
-      rr += double(rv) * double(rv);
+      dot2_add(rr, rv, rv);
     }
   double tot;
-  if (reduce_last(rr, partials, counter, &tot) && threadIdx.x == 0) {
+  if (reduce_last_ff(dot2_value(rr), 16, partials, counter, &tot) && threadIdx.x == 0) {
     s->rn_in = sqrt(tot);
     if (s->rn_in <= s->target_in) s->done = 1;
   }
@@ -142,15 +255,15 @@ __global__ void k_rz32(int32_t nf, const float* __restrict__ r, const float* __r
                        unsigned* counter, MixedScalars* s) {
   if (MODE == 1 && s->done) return;
   const int64_t i = int64_t(blockIdx.x) * kT + threadIdx.x;
-  double rz = 0.0;
+  FF rz{0.0f, 0.0f};
   if (i < nf)
     for (int c = 0; c < 6; ++c) {
       const float zv = z[6 * i + c];
-      rz += double(r[6 * i + c]) * double(zv);
+      dot2_add(rz, r[6 * i + c], zv);
       if (MODE == 0) p[6 * i + c] = zv;
     }
   double tot;
-  if (reduce_last(rz, partials, counter, &tot) && threadIdx.x == 0) {
+  if (reduce_last_ff(dot2_value(rz), 16, partials, counter, &tot) && threadIdx.x == 0) {
     if (MODE == 0) {
       s->rz = tot;
       if (!(tot > 0)) {
@@ -221,12 +334,12 @@ int mixed_body(Problem& P) {
   MixedScalars* s = static_cast<MixedScalars*>(P.d_ms);
   if (P.timer_on) TRY(timer_mark(P));
   if (P.sched_k32 == kGroupRow)
-    (k_spmv32_dot<kGroupRow><<<unsigned((std::max(nf, 1) + 5 * kRows - 1) / (5 * kRows)), kT, 0, st>>>(
-         nf, P.K.rowptr, P.K.col, P.K.val32, p32, q32, P.d_partials, P.d_counter, s),
+    (k_spmv32_dot<kGroupRow><<<spmv_dot_blocks<kGroupRow>(nf), kT, 0, st>>>(nf, P.K.rowptr, P.K.col, P.K.val32, p32,
+                                                                          q32, P.d_partials, P.d_counter, s),
      SVXG_COUNT_LAUNCH());
   else
-    (k_spmv32_dot<kWarpRow><<<rblk(nf), kT, 0, st>>>(nf, P.K.rowptr, P.K.col, P.K.val32, p32, q32, P.d_partials,
-                                                     P.d_counter, s),
+    (k_spmv32_dot<kWarpRow><<<spmv_dot_blocks<kWarpRow>(nf), kT, 0, st>>>(nf, P.K.rowptr, P.K.col, P.K.val32, p32,
+                                                                        q32, P.d_partials, P.d_counter, s),
      SVXG_COUNT_LAUNCH());
   if (P.timer_on) TRY(timer_mark(P, true));
   (k_axpy32<<<vblk(nf), kT, 0, st>>>(nf, d, r32, p32, q32, P.d_partials, P.d_counter, s), SVXG_COUNT_LAUNCH());
@@ -258,7 +371,6 @@ int mixed_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
   float* r32 = d + m;
   float* z32 = d + 2 * m;
   float* p32 = d + 3 * m;
-  float* q32 = d + 4 * m;
   MixedScalars* s = static_cast<MixedScalars*>(P.d_ms);
   MixedScalars* hs = static_cast<MixedScalars*>(P.h_ms);
   double bn = 0.0;

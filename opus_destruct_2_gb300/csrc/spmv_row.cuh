@@ -85,17 +85,22 @@ struct RowMap {
 
 // The warp's rows: row of this lane's group (valid: row < n), component c of its output.
 template <int SCHED>
-__device__ __forceinline__ int32_t sched_row(int rows_per_block_warps, int* c_out, bool* lane_ok) {
+__device__ __forceinline__ int32_t sched_row_of(int32_t warp, int* c_out, bool* lane_ok) {
   const int lane = threadIdx.x & 31;
   const int g = lane / 6;
   *c_out = lane - 6 * g;
-  const int32_t warp = int32_t(blockIdx.x) * rows_per_block_warps + (threadIdx.x >> 5);
   if (SCHED == kWarpRow) {
     *lane_ok = lane < 6;
     return warp;
   }
   *lane_ok = g < 5;
   return warp * 5 + (g < 5 ? g : 4);
+}
+
+// the block's warps take consecutive warp indices
+template <int SCHED>
+__device__ __forceinline__ int32_t sched_row(int rows_per_block_warps, int* c_out, bool* lane_ok) {
+  return sched_row_of<SCHED>(int32_t(blockIdx.x) * rows_per_block_warps + (threadIdx.x >> 5), c_out, lane_ok);
 }
 
 // the row's product for this schedule; in kGroupRow every lane sums its own row's blocks
