@@ -22,6 +22,7 @@
 #include <cmath>
 
 #include "blk6.cuh"
+#include "exact_runs.cuh"
 #include "exact_sum.cuh"
 #include "problem.cuh"
 
@@ -88,22 +89,10 @@ __device__ __forceinline__ double spmv_exact_entry(int64_t t, const int32_t* row
   return yr;
 }
 
-// nv = sqrt(sum of v_k^2 in index order): the sequential sum's exact bits, computed in parallel
-// (exact_sum.cuh).
-__global__ void __launch_bounds__(exact::kThreads) k_seq_norm(int64_t m, const double* v, double* out) {
-  const auto sq = [v](int64_t k) {
-    const double x = v[k];
-    return x * x;
-  };
-  const double s = blockDim.x == 32 ? exact::warp_sequential_sum_from(0.0, 0, m, sq) : exact::sequential_sum(m, sq);
-  if (threadIdx.x == 0) out[0] = sqrt(s);
-}
-
 // state: [0] = lam, [1] = nv, [2] = stopped
-// Power iteration, two launches a step: v' = D^-1 (A v) with one thread per entry (the node's six
-// entries of A v meet in shared memory, each in k_spmv_exact's order, then mv6's row), and the
-// exact norm with the step's lam / stop / scaling in the same block (levels of at most
-// kLmaxFusedMax unknowns; larger ones scale in a separate launch).
+// Power iteration step: v' = D^-1 (A v) with one thread per entry (the node's six entries of A v
+// meet in shared memory, each in Bsr6::apply's order, then mv6's row), then the exact norm with
+// the step's lam / stop / scaling (launch_norm).
 constexpr int kApplyNodes = 32;  // nodes per block: 192 threads
 __global__ void __launch_bounds__(6 * kApplyNodes) k_lmax_apply(int32_t n, const int32_t* rowptr, const int32_t* col,
                                                               const double* val, const double* dinv, const double* v,
@@ -122,44 +111,49 @@ __global__ void __launch_bounds__(6 * kApplyNodes) k_lmax_apply(int32_t n, const
   w[t] = m[0] * x[0] + m[1] * x[1] + m[2] * x[2] + m[3] * x[3] + m[4] * x[4] + m[5] * x[5];
 }
 
-// nv = exact sequential norm of w; lam <- nv, or a stop on a zero or non-finite norm; v = w / nv
-// (all in this block when `scale`). Launched with 32 threads, one warp does the sum (short w).
-__global__ void __launch_bounds__(exact::kThreads) k_lmax_norm(int64_t m, const double* w, double* v, double* state,
-                                                              int scale) {
-  __shared__ double nv_sh;
-  if (state[2] != 0.0) return;
-  const auto sq = [w](int64_t k) {
+// The exact norm: sqrt of the sequential sum of w_k^2 (amg.cpp:267-268: the reference's
+// v[i] * v[i], one rounding each) by predicted binade runs (exact_runs.cuh). Vectors of at most
+// exact::kTile terms take one block (k_norm_small, with the scaling v = w / nv); longer ones a
+// tile per block: approximate tile sums, each tile's segments, one block's ordered walk, then
+// the scaling.
+struct SqTerm {
+  const double* w;
+  __device__ __forceinline__ double operator()(int64_t k) const {
     const double x = w[k];
     return x * x;
-  };
-  const double s = blockDim.x == 32 ? exact::warp_sequential_sum_from(0.0, 0, m, sq) : exact::sequential_sum(m, sq);
+  }
+};
+
+// state[0] = lam <- nv, state[1] = nv; a zero or non-finite norm stops the iteration
+__device__ __forceinline__ void set_norm(double* state, double nv) {
+  state[1] = nv;
+  if (!(nv > 0)) state[2] = 1.0;
+  else state[0] = nv;
+}
+
+__global__ void __launch_bounds__(exact::kThreads) k_norm_small(int64_t m, const double* w, double* v,
+                                                               exact::Seg* rec, int32_t* cnt, double* state) {
+  __shared__ double nv_sh;
+  if (state[2] != 0.0) return;
+  const int32_t n = exact::build_segments(0, m, 0.0, SqTerm{w}, rec);
+  if (threadIdx.x == 0) cnt[0] = n > exact::kTileSegs ? -1 : n;
+  __syncthreads();
+  const double s = exact::walk_segments(1, cnt, rec, m, SqTerm{w});
   if (threadIdx.x == 0) {
-    const double nv = sqrt(s);
-    nv_sh = nv;
-    state[1] = nv;
-    if (!(nv > 0)) state[2] = 1.0;
-    else state[0] = nv;
+    nv_sh = sqrt(s);
+    set_norm(state, nv_sh);
   }
   __syncthreads();
   const double nv = nv_sh;
-  if (!scale || !(nv > 0)) return;
-  for (int64_t k = threadIdx.x; k < m; k += blockDim.x) v[k] = w[k] / nv;
+  if (!v || !(nv > 0)) return;
+  for (int64_t k = threadIdx.x; k < m; k += exact::kThreads) v[k] = w[k] / nv;
 }
 
-// The exact norm of a large vector over many blocks. Chunks of kChunk terms: (1) each chunk's
-// approximate sum (any order); (2) per chunk, the approximate sum before it predicts the binade the
-// sequential sum is in over the chunk; when the chunk's start and end lie safely inside one binade,
-// the chunk's composed increment pair in that binade is computed; (3) one block walks the chunks in
-// order with the exact running sum: a chunk whose pair was made for the sum's actual binade and
-// that does not carry it out of the binade is added in one step, any other chunk term by term
-// (exact::sequential_sum_from). The predictions only choose the path: every step is exact.
-constexpr int64_t kChunk = int64_t(exact::kThreads) * exact::kItems;
-constexpr int32_t kNoPair = -100000;
-
-__global__ void __launch_bounds__(256) k_norm_chunk_sum(int64_t m, const double* w, double* csum, const double* state) {
+// tile sums (any order: the predictions' approximate prefix)
+__global__ void __launch_bounds__(256) k_norm_tile_sum(int64_t m, const double* w, double* tsum, const double* state) {
   __shared__ double sh[256];
   if (state[2] != 0.0) return;
-  const int64_t a = int64_t(blockIdx.x) * kChunk, b = a + kChunk < m ? a + kChunk : m;
+  const int64_t a = int64_t(blockIdx.x) * exact::kTile, b = a + exact::kTile < m ? a + exact::kTile : m;
   double s = 0.0;
   for (int64_t k = a + threadIdx.x; k < b; k += 256) s += w[k] * w[k];
   sh[threadIdx.x] = s;
@@ -168,112 +162,65 @@ __global__ void __launch_bounds__(256) k_norm_chunk_sum(int64_t m, const double*
     if (int(threadIdx.x) < d) sh[threadIdx.x] += sh[threadIdx.x + d];
     __syncthreads();
   }
-  if (threadIdx.x == 0) csum[blockIdx.x] = sh[0];
+  if (threadIdx.x == 0) tsum[blockIdx.x] = sh[0];
 }
 
-__global__ void __launch_bounds__(exact::kThreads) k_norm_chunk_pair(int64_t m, int32_t nchunk, const double* w,
-                                                                     const double* csum, exact::Pair* cpair,
-                                                                     int32_t* cuexp, const double* state) {
-  __shared__ double sh[exact::kThreads];
+// tile c's segments (c = this block)
+__global__ void __launch_bounds__(exact::kThreads) k_norm_segments(int64_t m, const double* w, const double* tsum,
+                                                                  exact::Seg* rec, int32_t* cnt, const double* state) {
   if (state[2] != 0.0) return;
   const int32_t c = blockIdx.x;
-  double s = 0.0;
-  for (int32_t j = threadIdx.x; j < c; j += exact::kThreads) s += csum[j];
-  sh[threadIdx.x] = s;
-  __syncthreads();
-  for (int d = exact::kThreads / 2; d > 0; d >>= 1) {
-    if (int(threadIdx.x) < d) sh[threadIdx.x] += sh[threadIdx.x + d];
-    __syncthreads();
-  }
-  const double before = sh[0], after = sh[0] + csum[c];
-  const double lo = before * (1.0 - 1e-8), hi = after * (1.0 + 1e-8);
-  int64_t S;
-  int ulo = 0, uhi = 1;
-  const bool finite = lo > 0.0 && hi < 1e300;
-  if (finite) {
-    exact::split(lo, &S, &ulo);
-    exact::split(hi, &S, &uhi);
-  }
-  if (!finite || ulo != uhi || ulo == -1074) {
-    if (threadIdx.x == 0) cuexp[c] = kNoPair;
-    return;
-  }
-  const int64_t a = int64_t(c) * kChunk, base = a + int64_t(threadIdx.x) * exact::kItems;
-  const int64_t b = a + kChunk < m ? a + kChunk : m;
-  exact::Pair acc{0, 0};
-  for (int it = 0; it < exact::kItems; ++it) {
-    const int64_t k = base + it;
-    if (k < b) {
-      const double x = w[k];
-      acc = exact::compose(acc, exact::term_pair(x * x, ulo));
-    }
-  }
-  exact::Pair tot;
-  exact::block_scan(acc, &tot);
-  if (threadIdx.x == 0) {
-    cpair[c] = tot;
-    cuexp[c] = ulo;
-  }
+  double before = 0.0;
+  for (int32_t j = threadIdx.x; j < c; j += exact::kThreads) before += tsum[j];
+  before = exact::block_sum_approx(before);
+  const int64_t a = int64_t(c) * exact::kTile, b = a + exact::kTile < m ? a + exact::kTile : m;
+  const int32_t n = exact::build_segments(a, b, before, SqTerm{w}, rec + int64_t(c) * exact::kTileSegs);
+  if (threadIdx.x == 0) cnt[c] = n > exact::kTileSegs ? -1 : n;
 }
 
-__global__ void __launch_bounds__(exact::kThreads) k_norm_walk(int64_t m, int32_t nchunk, const double* w,
-                                                               const exact::Pair* cpair, const int32_t* cuexp,
-                                                               double* state) {
-  __shared__ double s_sh;
-  __shared__ int32_t c_sh;
+__global__ void __launch_bounds__(exact::kThreads) k_norm_walk(int64_t m, int32_t ntile, const double* w,
+                                                              const exact::Seg* rec, const int32_t* cnt,
+                                                              double* state) {
   if (state[2] != 0.0) return;
-  if (threadIdx.x == 0) {
-    s_sh = 0.0;
-    c_sh = 0;
-  }
-  __syncthreads();
-  for (;;) {
-    if (threadIdx.x == 0) {
-      double s = s_sh;
-      int32_t c = c_sh;
-      while (c < nchunk && cuexp[c] != kNoPair && s > 0.0 && s < 1e300) {
-        int64_t S;
-        int ue;
-        exact::split(s, &S, &ue);
-        if (ue != cuexp[c]) break;
-        const int64_t S2 = exact::sat(S, exact::pick(cpair[c], S));
-        if (S2 >= (int64_t(1) << 53)) break;
-        s = exact::join(S2, ue);
-        ++c;
-      }
-      s_sh = s;
-      c_sh = c;
-    }
-    __syncthreads();
-    const int32_t c = c_sh;
-    const double s0 = s_sh;
-    __syncthreads();
-    if (c >= nchunk) break;
-    const int64_t a = int64_t(c) * kChunk, b = a + kChunk < m ? a + kChunk : m;
-    const double s1 = exact::sequential_sum_from(s0, a, b, [w](int64_t k) {
-      const double x = w[k];
-      return x * x;
-    });
-    if (threadIdx.x == 0) {
-      s_sh = s1;
-      c_sh = c + 1;
-    }
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    const double nv = sqrt(s_sh);
-    state[1] = nv;
-    if (!(nv > 0)) state[2] = 1.0;
-    else state[0] = nv;
-  }
+  const double s = exact::walk_segments(ntile, cnt, rec, m, SqTerm{w});
+  if (threadIdx.x == 0) set_norm(state, sqrt(s));
 }
 
-// v = w / nv for a large level (after k_lmax_norm without scaling)
-__global__ void k_lmax_rescale(int64_t m, const double* w, double* v, const double* state) {
+// v = w / nv for a long vector (after k_norm_walk)
+__global__ void k_norm_rescale(int64_t m, const double* w, double* v, const double* state) {
   const double nv = state[1];
   if (!(nv > 0) || state[2] != 0.0) return;
   const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k < m) v[k] = w[k] / nv;
+}
+
+// scratch of the exact norm of vectors of m terms
+struct NormScratch {
+  Tmp<double> tsum;
+  Tmp<exact::Seg> rec;
+  Tmp<int32_t> cnt;
+  int32_t ntile = 0;
+  explicit NormScratch(cudaStream_t st) : tsum(st), rec(st), cnt(st) {}
+  int alloc(int64_t m) {
+    ntile = int32_t(std::max<int64_t>(1, (m + exact::kTile - 1) / exact::kTile));
+    TRY(tsum.alloc(size_t(ntile)));
+    TRY(rec.alloc(size_t(ntile) * exact::kTileSegs));
+    return cnt.alloc(size_t(ntile));
+  }
+};
+
+// The exact norm of w into state (lam, nv, stopped), and v = w / nv when v is given.
+int launch_norm(cudaStream_t st, int64_t m, const double* w, double* v, double* state, NormScratch& S) {
+  if (m <= exact::kTile) {
+    (k_norm_small<<<1, exact::kThreads, 0, st>>>(m, w, v, S.rec.p, S.cnt.p, state), SVXG_COUNT_LAUNCH());
+    return SVXG_OK;
+  }
+  const unsigned nt = unsigned(S.ntile);
+  (k_norm_tile_sum<<<nt, 256, 0, st>>>(m, w, S.tsum.p, state), SVXG_COUNT_LAUNCH());
+  (k_norm_segments<<<nt, exact::kThreads, 0, st>>>(m, w, S.tsum.p, S.rec.p, S.cnt.p, state), SVXG_COUNT_LAUNCH());
+  (k_norm_walk<<<1, exact::kThreads, 0, st>>>(m, S.ntile, w, S.rec.p, S.cnt.p, state), SVXG_COUNT_LAUNCH());
+  if (v) (k_norm_rescale<<<nblk(m), kT, 0, st>>>(m, w, v, state), SVXG_COUNT_LAUNCH());
+  return SVXG_OK;
 }
 
 // ---- strength (amg.cpp:324-330) ------------------------------------------------------------------
@@ -1230,42 +1177,24 @@ int finalize_level(Problem& P, Level& L, bool* ok) {
 }
 
 // estimate_lmax of a level (amg.cpp:256-275), the value the reference computes
-constexpr int64_t kLmaxFusedMax = 1 << 17;
 int estimate_lmax(Problem& P, const Level& L, double* out) {
   const int32_t n = L.A.n;
   P.amg_build_work += 15 * (L.A.nnzb + n);
   const int64_t m = 6 * int64_t(n);
   Tmp<double> v(P.stream), w(P.stream), st(P.stream);
+  NormScratch ns(P.stream);
   TRY(v.alloc(size_t(m)));
   TRY(w.alloc(size_t(m)));
   TRY(st.alloc(3));
+  TRY(ns.alloc(m));
   const double init[3] = {1.0, 0.0, 0.0};
   SVXG_CUDA(cudaMemcpyAsync(st.p, init, sizeof(init), cudaMemcpyHostToDevice, P.stream));
   (k_lmax_init<<<nblk(m), kT, 0, P.stream>>>(m, v.p), SVXG_COUNT_LAUNCH());
-  const bool fused = m <= kLmaxFusedMax;
   const unsigned ab = unsigned((m + 6 * kApplyNodes - 1) / (6 * kApplyNodes));
-  const int32_t nchunk = int32_t((m + kChunk - 1) / kChunk);
-  Tmp<double> csum(P.stream);
-  Tmp<exact::Pair> cpair(P.stream);
-  Tmp<int32_t> cuexp(P.stream);
-  if (!fused) {
-    TRY(csum.alloc(size_t(nchunk)));
-    TRY(cpair.alloc(size_t(nchunk)));
-    TRY(cuexp.alloc(size_t(nchunk)));
-  }
   for (int it = 0; it < 15; ++it) {
     (k_lmax_apply<<<ab, 6 * kApplyNodes, 0, P.stream>>>(n, L.A.rowptr, L.A.col, L.A.val, L.dinv, v.p, w.p, st.p),
      SVXG_COUNT_LAUNCH());
-    if (fused) {
-      (k_lmax_norm<<<1, m <= exact::kWarpSumMax ? 32 : exact::kThreads, 0, P.stream>>>(m, w.p, v.p, st.p, 1),
-       SVXG_COUNT_LAUNCH());
-      continue;
-    }
-    (k_norm_chunk_sum<<<unsigned(nchunk), 256, 0, P.stream>>>(m, w.p, csum.p, st.p), SVXG_COUNT_LAUNCH());
-    (k_norm_chunk_pair<<<unsigned(nchunk), exact::kThreads, 0, P.stream>>>(m, nchunk, w.p, csum.p, cpair.p, cuexp.p,
-                                                                          st.p), SVXG_COUNT_LAUNCH());
-    (k_norm_walk<<<1, exact::kThreads, 0, P.stream>>>(m, nchunk, w.p, cpair.p, cuexp.p, st.p), SVXG_COUNT_LAUNCH());
-    (k_lmax_rescale<<<nblk(m), kT, 0, P.stream>>>(m, w.p, v.p, st.p), SVXG_COUNT_LAUNCH());
+    TRY(launch_norm(P.stream, m, w.p, v.p, st.p, ns));
   }
   SVXG_CUDA(cudaGetLastError());
   double h[3];
@@ -1595,24 +1524,12 @@ __global__ void k_state_norm_out(const double* state, double* out) {
 // sqrt of the sequential sum of squares of n device doubles (the power iteration's norm), by the
 // path estimate_lmax takes for a vector of that length
 int debug_seq_norm(cudaStream_t st, const double* v, int64_t n, double* out_dev) {
-  if (n <= kLmaxFusedMax) {
-    (k_seq_norm<<<1, n <= exact::kWarpSumMax ? 32 : exact::kThreads, 0, st>>>(n, v, out_dev), SVXG_COUNT_LAUNCH());
-    SVXG_CUDA(cudaGetLastError());
-    return SVXG_OK;
-  }
-  const int32_t nchunk = int32_t((n + kChunk - 1) / kChunk);
-  Tmp<double> csum(st), state(st);
-  Tmp<exact::Pair> cpair(st);
-  Tmp<int32_t> cuexp(st);
-  TRY(csum.alloc(size_t(nchunk)));
-  TRY(cpair.alloc(size_t(nchunk)));
-  TRY(cuexp.alloc(size_t(nchunk)));
+  Tmp<double> state(st);
+  NormScratch ns(st);
   TRY(state.alloc(3));
+  TRY(ns.alloc(n));
   SVXG_CUDA(cudaMemsetAsync(state.p, 0, 3 * sizeof(double), st));
-  (k_norm_chunk_sum<<<unsigned(nchunk), 256, 0, st>>>(n, v, csum.p, state.p), SVXG_COUNT_LAUNCH());
-  (k_norm_chunk_pair<<<unsigned(nchunk), exact::kThreads, 0, st>>>(n, nchunk, v, csum.p, cpair.p, cuexp.p, state.p),
-   SVXG_COUNT_LAUNCH());
-  (k_norm_walk<<<1, exact::kThreads, 0, st>>>(n, nchunk, v, cpair.p, cuexp.p, state.p), SVXG_COUNT_LAUNCH());
+  TRY(launch_norm(st, n, v, nullptr, state.p, ns));
   (k_state_norm_out<<<1, 32, 0, st>>>(state.p, out_dev), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   SVXG_CUDA(host_wait(st));
