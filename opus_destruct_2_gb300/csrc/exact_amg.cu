@@ -678,38 +678,13 @@ __device__ __forceinline__ void warp_mul6_add(bool trans, const double* __restri
   }
 }
 
-__global__ void k_ap_values(int32_t n, const int32_t* rowptr, const int32_t* col, const double* val,
-                            const int32_t* prow, const int32_t* pcol, const double* pval, const int32_t* aprow,
-                            const int32_t* scratch, const int64_t* soff, int32_t* apcol, double* apval) {
-  const int lane = threadIdx.x & 31;
-  const int32_t i = int32_t((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
-  if (i >= n) return;
-  const int32_t e0 = aprow[i], e1 = aprow[i + 1];
-  for (int32_t e = e0 + lane; e < e1; e += 32) apcol[e] = scratch[soff[i] + (e - e0)];
-  for (int64_t q = 36 * int64_t(e0) + lane; q < 36 * int64_t(e1); q += 32) apval[q] = 0.0;
-  __syncwarp();
-  for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
-    const int32_t j = col[k];
-    const double* Aij = val + 36 * int64_t(k);
-    for (int32_t e = prow[j]; e < prow[j + 1]; ++e) {
-      const int32_t c = pcol[e];
-      int32_t lo = e0, hi = e1 - 1;
-      while (lo < hi) {
-        const int32_t mid = (lo + hi) >> 1;
-        if (apcol[mid] < c) lo = mid + 1;
-        else hi = mid;
-      }
-      warp_mul6_add(false, Aij, pval + 36 * int64_t(e), apval + 36 * int64_t(lo), lane);
-      __syncwarp();
-    }
-  }
-}
-
 // The same A P rows, accumulated in shared memory when a row has at most kAccSlots blocks (the
 // row's blocks are read-modify-written once per product; in shared memory that round trip is
-// short): each lane keeps its row of A_ik in registers across the k's P entries and adds, for
-// every entry of a product, the same sum in the same order as warp_mul6_add. Longer rows go
-// through global memory as in k_ap_values.
+// short). For each block A_ik of the row, the products with the blocks of P's row k are spread
+// over the lanes as (P entry, output entry) items: GB300 issues FP64 instructions for whole warps,
+// so the lanes are kept busy rather than one lane per output entry (36 entries: a pass of 32 and
+// a pass of 4). Every output entry receives the same sums in the same order as warp_mul6_add:
+// the k's in row order, each entry one 6-term sum. Longer rows go through global memory.
 constexpr int kAccSlots = 40;
 constexpr int kAccWarps = 4;
 __global__ void __launch_bounds__(32 * kAccWarps) k_ap_values_acc(int32_t n, const int32_t* rowptr, const int32_t* col,
@@ -719,6 +694,7 @@ __global__ void __launch_bounds__(32 * kAccWarps) k_ap_values_acc(int32_t n, con
                                                                   const int64_t* soff, int32_t* apcol, double* apval) {
   __shared__ double acc_sh[kAccWarps][kAccSlots * 36];
   __shared__ int32_t col_sh[kAccWarps][kAccSlots];
+  __shared__ int32_t slot_sh[kAccWarps][32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int32_t i = int32_t(blockIdx.x) * kAccWarps + wid;
   if (i >= n) return;
@@ -733,33 +709,30 @@ __global__ void __launch_bounds__(32 * kAccWarps) k_ap_values_acc(int32_t n, con
   }
   for (int32_t q = lane; q < 36 * len; q += 32) acc[q] = 0.0;
   __syncwarp();
-  const int r0 = lane / 6, c0 = lane - 6 * (lane / 6);  // entry lane
-  const int r1 = (lane + 32) / 6, c1 = (lane + 32) - 6 * ((lane + 32) / 6);  // entry lane + 32 (lanes < 4)
   for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
     const int32_t j = col[k];
     const double* A = val + 36 * int64_t(k);
-    double a0[6], a1[6];
-    for (int q = 0; q < 6; ++q) {
-      a0[q] = A[r0 * 6 + q];
-      a1[q] = lane < 4 ? A[r1 * 6 + q] : 0.0;
-    }
-    for (int32_t e = prow[j]; e < prow[j + 1]; ++e) {
-      const int32_t cc = pcol[e];
-      int32_t lo = 0, hi = len - 1;
-      while (lo < hi) {
-        const int32_t mid = (lo + hi) >> 1;
-        if (cols[mid] < cc) lo = mid + 1;
-        else hi = mid;
+    for (int32_t pb = prow[j]; pb < prow[j + 1]; pb += 32) {
+      const int32_t np = prow[j + 1] - pb < 32 ? prow[j + 1] - pb : 32;
+      if (lane < np) {
+        const int32_t cc = pcol[pb + lane];
+        int32_t lo = 0, hi = len - 1;
+        while (lo < hi) {
+          const int32_t mid = (lo + hi) >> 1;
+          if (cols[mid] < cc) lo = mid + 1;
+          else hi = mid;
+        }
+        slot_sh[wid][lane] = lo;
       }
-      const double* B = pval + 36 * int64_t(e);
-      double s0 = 0.0;
-      for (int q = 0; q < 6; ++q) s0 += a0[q] * B[q * 6 + c0];
-      double* C = acc + 36 * int64_t(lo);
-      C[lane] = C[lane] + s0;
-      if (lane < 4) {
-        double s1 = 0.0;
-        for (int q = 0; q < 6; ++q) s1 += a1[q] * B[q * 6 + c1];
-        C[lane + 32] = C[lane + 32] + s1;
+      __syncwarp();
+      for (int32_t it = lane; it < 36 * np; it += 32) {
+        const int32_t el = it / 36, ent = it - 36 * el;
+        const int r = ent / 6, c = ent - 6 * r;
+        const double* B = pval + 36 * int64_t(pb + el);
+        double s0 = 0.0;
+        for (int q = 0; q < 6; ++q) s0 += A[r * 6 + q] * B[q * 6 + c];
+        double* C = acc + 36 * int64_t(slot_sh[wid][el]) + ent;
+        *C = *C + s0;
       }
       __syncwarp();
     }
@@ -768,8 +741,10 @@ __global__ void __launch_bounds__(32 * kAccWarps) k_ap_values_acc(int32_t n, con
     for (int32_t q = lane; q < 36 * len; q += 32) apval[36 * int64_t(e0) + q] = acc[q];
 }
 
-// The coarse rows in the same way (k_c_values_lanes' lanes over an A P row's entries), with the
-// coarse row accumulated in shared memory when it has at most kAccSlots blocks.
+// The coarse rows C = P^T (A P) in the same way: a warp per coarse row, accumulated in shared
+// memory when it has at most kAccSlots blocks. For each restriction entry (fine row i, block P_iI)
+// the blocks of A P's row i are taken 32 at a time and their (block, C entry) items spread over
+// the lanes; each C entry receives one 6-term sum per restriction entry, in restriction order.
 __global__ void __launch_bounds__(32 * kAccWarps) k_c_values_acc(int32_t na, const int32_t* rrow, const int32_t* rent_i,
                                                                  const int32_t* rent_e, const double* pval,
                                                                  const int32_t* aprow, const int32_t* apcol,
@@ -778,6 +753,7 @@ __global__ void __launch_bounds__(32 * kAccWarps) k_c_values_acc(int32_t na, con
                                                                  int32_t* ccol, double* cval, double scale) {
   __shared__ double acc_sh[kAccWarps][kAccSlots * 36];
   __shared__ int32_t col_sh[kAccWarps][kAccSlots];
+  __shared__ int32_t slot_sh[kAccWarps][32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int32_t I = int32_t(blockIdx.x) * kAccWarps + wid;
   if (I >= na) return;
@@ -795,30 +771,36 @@ __global__ void __launch_bounds__(32 * kAccWarps) k_c_values_acc(int32_t na, con
   for (int32_t r = rrow[I]; r < rrow[I + 1]; ++r) {
     const int32_t i = rent_i[r];
     const double* Pi = pval + 36 * int64_t(rent_e[r]);
-    for (int32_t e = aprow[i] + lane; e < aprow[i + 1]; e += 32) {
-      const int32_t J = apcol[e];
-      int32_t slot;
-      if (J == I) {
-        slot = 0;
-      } else {
-        int32_t lo = 1, hi = len - 1;
-        while (lo < hi) {
-          const int32_t mid = (lo + hi) >> 1;
-          if (cols[mid] < J) lo = mid + 1;
-          else hi = mid;
+    for (int32_t eb = aprow[i]; eb < aprow[i + 1]; eb += 32) {
+      const int32_t ne = aprow[i + 1] - eb < 32 ? aprow[i + 1] - eb : 32;
+      if (lane < ne) {
+        const int32_t J = apcol[eb + lane];
+        int32_t slot;
+        if (J == I) {
+          slot = 0;
+        } else {
+          int32_t lo = 1, hi = len - 1;
+          while (lo < hi) {
+            const int32_t mid = (lo + hi) >> 1;
+            if (cols[mid] < J) lo = mid + 1;
+            else hi = mid;
+          }
+          slot = lo;
         }
-        slot = lo;
+        slot_sh[wid][lane] = slot;
       }
-      const double* B = apval + 36 * int64_t(e);
-      double* C = acc + 36 * int64_t(slot);
-      for (int ent = 0; ent < 36; ++ent) {
-        const int rr = ent / 6, cc = ent - 6 * (ent / 6);
+      __syncwarp();
+      for (int32_t it = lane; it < 36 * ne; it += 32) {
+        const int32_t el = it / 36, ent = it - 36 * el;
+        const int rr = ent / 6, cc = ent - 6 * rr;
+        const double* B = apval + 36 * int64_t(eb + el);
         double sacc = 0.0;
         for (int q = 0; q < 6; ++q) sacc += Pi[q * 6 + rr] * B[q * 6 + cc];
-        C[ent] = C[ent] + sacc;
+        double* C = acc + 36 * int64_t(slot_sh[wid][el]) + ent;
+        *C = *C + sacc;
       }
+      __syncwarp();
     }
-    __syncwarp();
   }
   if (scale != 1.0)
     for (int32_t q = lane; q < 36 * len; q += 32) acc[q] *= scale;
@@ -1048,53 +1030,6 @@ __global__ void k_c_values(int32_t na, const int32_t* rrow, const int32_t* rent_
       warp_mul6_add(true, Pi, apval + 36 * int64_t(e), cval + 36 * int64_t(slot), lane);
       __syncwarp();
     }
-  }
-  if (scale != 1.0)
-    for (int64_t q = 36 * int64_t(c0) + lane; q < 36 * int64_t(c1); q += 32) cval[q] *= scale;
-}
-
-// The same for long A P rows (coarse levels): the lanes take distinct entries e of one A P row -
-// distinct columns, so distinct blocks of C - and each computes its whole 6x6 product with
-// warp_mul6_add's additions; restriction entries r stay in order, so every block of C sees the
-// same sequence of additions as in k_c_values.
-__global__ void k_c_values_lanes(int32_t na, const int32_t* rrow, const int32_t* rent_i, const int32_t* rent_e,
-                                 const double* pval, const int32_t* aprow, const int32_t* apcol, const double* apval,
-                                 const int32_t* crow, const int32_t* scratch, const int64_t* soff, int32_t* ccol,
-                                 double* cval, double scale) {
-  const int lane = threadIdx.x & 31;
-  const int32_t I = int32_t((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
-  if (I >= na) return;
-  const int32_t c0 = crow[I], c1 = crow[I + 1];
-  for (int32_t c = c0 + lane; c < c1; c += 32) ccol[c] = scratch[soff[I] + (c - c0)];
-  for (int64_t q = 36 * int64_t(c0) + lane; q < 36 * int64_t(c1); q += 32) cval[q] = 0.0;
-  __syncwarp();
-  for (int32_t r = rrow[I]; r < rrow[I + 1]; ++r) {
-    const int32_t i = rent_i[r];
-    const double* Pi = pval + 36 * int64_t(rent_e[r]);
-    for (int32_t e = aprow[i] + lane; e < aprow[i + 1]; e += 32) {
-      const int32_t J = apcol[e];
-      int32_t slot;
-      if (J == I) {
-        slot = c0;
-      } else {
-        int32_t lo = c0 + 1, hi = c1 - 1;
-        while (lo < hi) {
-          const int32_t mid = (lo + hi) >> 1;
-          if (ccol[mid] < J) lo = mid + 1;
-          else hi = mid;
-        }
-        slot = lo;
-      }
-      const double* B = apval + 36 * int64_t(e);
-      double* C = cval + 36 * int64_t(slot);
-      for (int ent = 0; ent < 36; ++ent) {
-        const int rr = ent / 6, cc = ent - 6 * (ent / 6);
-        double sacc = 0.0;
-        for (int q = 0; q < 6; ++q) sacc += Pi[q * 6 + rr] * B[q * 6 + cc];
-        C[ent] = C[ent] + sacc;
-      }
-    }
-    __syncwarp();
   }
   if (scale != 1.0)
     for (int64_t q = 36 * int64_t(c0) + lane; q < 36 * int64_t(c1); q += 32) cval[q] *= scale;
