@@ -522,8 +522,6 @@ __global__ void k_offsets(int32_t n, const int32_t* agg, const double* fpos, con
   for (int c = 0; c < 3; ++c) off3[3 * int64_t(i) + c] = fpos[3 * int64_t(i) + c] - cpos[3 * int64_t(a) + c];
 }
 
-__device__ __forceinline__ V3d v3at(const double* p, int64_t i) { return {p[3 * i], p[3 * i + 1], p[3 * i + 2]}; }
-
 // ---- prolongation (amg.cpp:405-452) ----------------------------------------------------------------
 // distinct coarse columns of fine row i: agg[i] and agg[col k] (all k when smoothed)
 __device__ int32_t sorted_distinct(int32_t first, const int32_t* rowptr, const int32_t* col, const int32_t* agg,
@@ -551,44 +549,94 @@ __global__ void k_p_count(int32_t n, const int32_t* rowptr, const int32_t* col, 
   plen[i] = sorted_distinct(agg[i], rowptr, col, agg, i, smoothed != 0, scratch + int64_t(rowptr[i]) + i, cap);
 }
 
-__global__ void k_p_values(int32_t n, const int32_t* rowptr, const int32_t* col, const double* val, const int32_t* agg,
-                           const double* off3, const double* dinv, double omega, const int32_t* prow,
-                           const int32_t* scratch, int32_t* pcol, double* pval) {
-  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int32_t e0 = prow[i], e1 = prow[i + 1];
-  const int32_t* cols = scratch + int64_t(rowptr[i]) + i;
-  for (int32_t e = e0; e < e1; ++e) {
-    pcol[e] = cols[e - e0];
-    for (int q = 0; q < 36; ++q) pval[36 * int64_t(e) + q] = 0.0;
+// rigid_block(r)[q][c] (blk6.cuh) with r = off3 row j, the same values without the array
+__device__ __forceinline__ double rigid_entry(const double* off3, int32_t j, int q, int c) {
+  if (q == c) return 1.0;
+  const double* r = off3 + 3 * int64_t(j);
+  switch (q * 6 + c) {
+    case 4: return r[2];
+    case 5: return -r[1];
+    case 9: return -r[2];
+    case 11: return r[0];
+    case 15: return r[1];
+    case 16: return -r[0];
+    default: return 0.0;
   }
-  auto slot = [&](int32_t c) -> double* {
-    int32_t lo = e0, hi = e1 - 1;
+}
+
+// The smoothed prolongation rows (amg.cpp:405-452), a warp per fine row i, its P blocks in
+// shared memory when it has at most kPSlots of them. The row's own aggregate block gets
+// rigid_block(off_i); then, for the row's neighbours k in chunks of kPNb, T_k = A_ik rigid_block
+// (off_j) and U_k = D_i^-1 T_k with the (k, entry) items spread over the lanes (GB300 issues FP64
+// instructions for whole warps), and the block of aggregate agg[j] adds -omega U_k, neighbour by
+// neighbour. Every entry gets the reference's sums (mul6's 6-term sums, the axpy) in its order.
+constexpr int kPNb = 8;
+constexpr int kPSlots = 16;
+constexpr int kPWarps = 4;
+__global__ void __launch_bounds__(32 * kPWarps) k_p_values(int32_t n, const int32_t* rowptr, const int32_t* col,
+                                                           const double* val, const int32_t* agg, const double* off3,
+                                                           const double* dinv, double omega, const int32_t* prow,
+                                                           const int32_t* scratch, int32_t* pcol, double* pval) {
+  __shared__ double t_sh[kPWarps][kPNb * 36], u_sh[kPWarps][kPNb * 36];
+  __shared__ double acc_sh[kPWarps][kPSlots * 36];
+  __shared__ int32_t slot_sh[kPWarps][kPNb];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int32_t i = int32_t(blockIdx.x) * kPWarps + wid;
+  if (i >= n) return;
+  const int32_t e0 = prow[i], len = prow[i + 1] - e0;
+  const int32_t* cols = scratch + int64_t(rowptr[i]) + i;
+  for (int32_t e = lane; e < len; e += 32) pcol[e0 + e] = cols[e];
+  const bool local = len <= kPSlots;
+  double* acc = local ? acc_sh[wid] : pval + 36 * int64_t(e0);
+  for (int32_t q = lane; q < 36 * len; q += 32) acc[q] = 0.0;
+  const auto find = [&](int32_t c) {
+    int32_t lo = 0, hi = len - 1;
     while (lo < hi) {
       const int32_t mid = (lo + hi) >> 1;
-      if (pcol[mid] < c) lo = mid + 1;
+      if (cols[mid] < c) lo = mid + 1;
       else hi = mid;
     }
-    return pval + 36 * int64_t(lo);
+    return lo;
   };
-  double Pt[36];
-  rigid_block(v3at(off3, i), Pt);
+  __syncwarp();
   {
-    double* b = slot(agg[i]);
-    for (int q = 0; q < 36; ++q) b[q] += 1.0 * Pt[q];
+    double* b = acc + 36 * int64_t(find(agg[i]));
+    for (int q = lane; q < 36; q += 32) b[q] = b[q] + 1.0 * rigid_entry(off3, i, q / 6, q % 6);
   }
+  __syncwarp();
   if (omega != 0.0) {
     const double* Di = dinv + 36 * int64_t(i);
-    for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) {
-      const int32_t j = col[k];
-      double Pj[36], T[36], U[36];
-      rigid_block(v3at(off3, j), Pj);
-      mul6(val + 36 * int64_t(k), Pj, T);
-      mul6(Di, T, U);
-      double* b = slot(agg[j]);
-      for (int q = 0; q < 36; ++q) b[q] += -omega * U[q];
+    for (int32_t kb = rowptr[i]; kb < rowptr[i + 1]; kb += kPNb) {
+      const int32_t nk = rowptr[i + 1] - kb < kPNb ? rowptr[i + 1] - kb : kPNb;
+      if (lane < nk) slot_sh[wid][lane] = find(agg[col[kb + lane]]);
+      for (int32_t it = lane; it < 36 * nk; it += 32) {
+        const int32_t kl = it / 36, ent = it - 36 * kl;
+        const int r = ent / 6, c = ent - 6 * r;
+        const double* A = val + 36 * int64_t(kb + kl);
+        const int32_t j = col[kb + kl];
+        double s = 0.0;
+        for (int q = 0; q < 6; ++q) s += A[r * 6 + q] * rigid_entry(off3, j, q, c);
+        t_sh[wid][it] = s;
+      }
+      __syncwarp();
+      for (int32_t it = lane; it < 36 * nk; it += 32) {
+        const int32_t kl = it / 36, ent = it - 36 * kl;
+        const int r = ent / 6, c = ent - 6 * r;
+        const double* T = t_sh[wid] + 36 * kl;
+        double s = 0.0;
+        for (int q = 0; q < 6; ++q) s += Di[r * 6 + q] * T[q * 6 + c];
+        u_sh[wid][it] = s;
+      }
+      __syncwarp();
+      for (int32_t kl = 0; kl < nk; ++kl) {
+        double* b = acc + 36 * int64_t(slot_sh[wid][kl]);
+        for (int q = lane; q < 36; q += 32) b[q] = b[q] + -omega * u_sh[wid][36 * kl + q];
+        __syncwarp();
+      }
     }
   }
+  if (local)
+    for (int32_t q = lane; q < 36 * len; q += 32) pval[36 * int64_t(e0) + q] = acc[q];
 }
 
 // build work of the products: 6 |P row col(k)| for every block k of A
@@ -1279,7 +1327,7 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     F.pnnz = pnnz;
     TRY(P.mem.alloc(&F.pcol, size_t(pnnz)));
     TRY(P.mem.alloc(&F.pval, size_t(pnnz) * 36));
-    (k_p_values<<<nblk(n, 128), 128, 0, st>>>(n, A.rowptr, A.col, A.val, agg, off3.p, F.dinv, omega, F.prow,
+    (k_p_values<<<unsigned((n + kPWarps - 1) / kPWarps), 32 * kPWarps, 0, st>>>(n, A.rowptr, A.col, A.val, agg, off3.p, F.dinv, omega, F.prow,
                                               scratch.p, F.pcol, F.pval), SVXG_COUNT_LAUNCH());
   }
   if (smoothed) P.amg_build_work += 12 * nnzb;
