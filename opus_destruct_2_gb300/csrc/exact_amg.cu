@@ -111,6 +111,46 @@ __global__ void __launch_bounds__(6 * kApplyNodes) k_lmax_apply(int32_t n, const
   w[t] = m[0] * x[0] + m[1] * x[1] + m[2] * x[2] + m[3] * x[3] + m[4] * x[4] + m[5] * x[5];
 }
 
+// The same step for shorter levels with longer rows, a warp per node: the six-term products of
+// the row's blocks (entry, block items over the lanes, chunks of kApplyChunk blocks) first, then
+// lanes 0-5 add them in block order - the same sums as spmv_exact_entry - and D^-1 (A v).
+constexpr int kApplyChunk = 16;
+constexpr int kApplyWarps = 4;
+constexpr int32_t kApplyRowsMax = 16384;  // levels up to this many nodes take the warp-per-node form
+__global__ void __launch_bounds__(32 * kApplyWarps) k_lmax_apply_rows(int32_t n, const int32_t* rowptr,
+                                                                      const int32_t* col, const double* val,
+                                                                      const double* dinv, const double* v, double* w,
+                                                                      const double* state) {
+  __shared__ double d_sh[kApplyWarps][6 * kApplyChunk];
+  __shared__ double y_sh[kApplyWarps][6];
+  if (state[2] != 0.0) return;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int32_t i = int32_t(blockIdx.x) * kApplyWarps + wid;
+  if (i >= n) return;
+  double yr = 0.0;
+  for (int32_t kb = rowptr[i]; kb < rowptr[i + 1]; kb += kApplyChunk) {
+    const int32_t nk = rowptr[i + 1] - kb < kApplyChunk ? rowptr[i + 1] - kb : kApplyChunk;
+    for (int32_t it = lane; it < 6 * nk; it += 32) {
+      const int32_t kl = it / 6;
+      const int r = it - 6 * kl;
+      const double* m = val + 36 * int64_t(kb + kl) + 6 * r;
+      const double* xv = v + 6 * int64_t(col[kb + kl]);
+      d_sh[wid][it] = m[0] * xv[0] + m[1] * xv[1] + m[2] * xv[2] + m[3] * xv[3] + m[4] * xv[4] + m[5] * xv[5];
+    }
+    __syncwarp();
+    if (lane < 6)
+      for (int32_t kl = 0; kl < nk; ++kl) yr += d_sh[wid][6 * kl + lane];
+    __syncwarp();
+  }
+  if (lane < 6) y_sh[wid][lane] = yr;
+  __syncwarp();
+  if (lane < 6) {
+    const double* x = y_sh[wid];
+    const double* m = dinv + 36 * int64_t(i) + 6 * lane;
+    w[6 * int64_t(i) + lane] = m[0] * x[0] + m[1] * x[1] + m[2] * x[2] + m[3] * x[3] + m[4] * x[4] + m[5] * x[5];
+  }
+}
+
 // The exact norm: sqrt of the sequential sum of w_k^2 (amg.cpp:267-268: the reference's
 // v[i] * v[i], one rounding each) by predicted binade runs (exact_runs.cuh). Vectors of at most
 // exact::kTile terms take one block (k_norm_small, with the scaling v = w / nv); longer ones a
@@ -1175,8 +1215,13 @@ int estimate_lmax(Problem& P, const Level& L, double* out) {
   (k_lmax_init<<<nblk(m), kT, 0, P.stream>>>(m, v.p), SVXG_COUNT_LAUNCH());
   const unsigned ab = unsigned((m + 6 * kApplyNodes - 1) / (6 * kApplyNodes));
   for (int it = 0; it < 15; ++it) {
-    (k_lmax_apply<<<ab, 6 * kApplyNodes, 0, P.stream>>>(n, L.A.rowptr, L.A.col, L.A.val, L.dinv, v.p, w.p, st.p),
-     SVXG_COUNT_LAUNCH());
+    if (n <= kApplyRowsMax)
+      (k_lmax_apply_rows<<<unsigned((n + kApplyWarps - 1) / kApplyWarps), 32 * kApplyWarps, 0, P.stream>>>(
+           n, L.A.rowptr, L.A.col, L.A.val, L.dinv, v.p, w.p, st.p),
+       SVXG_COUNT_LAUNCH());
+    else
+      (k_lmax_apply<<<ab, 6 * kApplyNodes, 0, P.stream>>>(n, L.A.rowptr, L.A.col, L.A.val, L.dinv, v.p, w.p, st.p),
+       SVXG_COUNT_LAUNCH());
     TRY(launch_norm(P.stream, m, w.p, v.p, st.p, ns));
   }
   SVXG_CUDA(cudaGetLastError());

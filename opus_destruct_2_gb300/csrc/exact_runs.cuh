@@ -2,8 +2,8 @@
 // by predicted binade runs.
 //
 // An approximate prefix sum, taken in any order, places every partial sum of the sequence in
-// its binade up to a relative margin (kMargin: the sequential sum of k terms is within k 2^-53 of
-// the exact one, the approximate prefix far closer). Terms whose partial sums before and after
+// its binade up to a relative margin (about 1.5e-8: the sequential sum of k terms is within
+// k 2^-53 of the exact one, the approximate prefix far closer). Terms whose partial sums before and after
 // lie safely inside one binade form runs; the increment pairs of a run's terms (exact_sum.cuh:
 // integer additions in the binade's ulps, ties keyed by parity) compose into one pair in
 // parallel. A term at which the binade may change is a single, added by the hardware. One thread
@@ -25,7 +25,6 @@ namespace exact {
 
 constexpr int64_t kTile = int64_t(kThreads) * kItems;  // terms per tile (one block)
 constexpr int32_t kTileSegs = 1024;                     // segment records per tile
-constexpr double kMargin = 1e-8;
 constexpr int32_t kSkipCode = 100000;    // zeros before the first nonzero term: no change
 constexpr int32_t kSingleCode = 100001;  // one term, added by the hardware
 constexpr int32_t kRangeCode = 100002;   // a tile summed term by term (walk only)
@@ -103,17 +102,21 @@ __device__ inline double block_sum_approx(double v) {
   return y;
 }
 
-// a term's segment code from the approximate sums before (pe) and after (pi) it
+// A term's segment code from the approximate sums before (pe) and after (pi) it, by integer
+// tests on their bits (the FP64 pipe is the scarce one): a run code when both are normal, in
+// one binade, and at least about 1.5e-8 of it inside (mantissa fractions above kLowGuard and below
+// the top by kHighGuard, in ulps of 2^52), else a single.
+constexpr uint64_t kMant = (uint64_t(1) << 52) - 1;
+constexpr uint64_t kLowGuard = uint64_t(1) << 26;   // 1.5e-8 of the binade's bottom
+constexpr uint64_t kHighGuard = uint64_t(1) << 27;  // 1.5e-8 of its top
 __device__ __forceinline__ int32_t seg_code(double t, double pe, double pi) {
-  if (t == 0.0 && pi == 0.0) return kSkipCode;
-  const double lo = pe * (1.0 - kMargin), hi = pi * (1.0 + kMargin);
-  if (!(lo > 0.0) || !(hi < 1e300)) return kSingleCode;  // (also NaN)
-  int64_t S;
-  int ulo, uhi;
-  split(lo, &S, &ulo);
-  split(hi, &S, &uhi);
-  if (ulo != uhi || ulo == -1074) return kSingleCode;
-  return ulo;
+  const uint64_t bt = uint64_t(__double_as_longlong(t));
+  const uint64_t be = uint64_t(__double_as_longlong(pe)), bi = uint64_t(__double_as_longlong(pi));
+  if ((bt | bi) == 0) return kSkipCode;  // (+0 + +0: zeros before the first nonzero term)
+  const uint64_t ee = be >> 52, ei = bi >> 52;  // (a sign bit makes these large)
+  if (ee == 0 || ee >= 0x7fe || ei != ee) return kSingleCode;
+  if ((be & kMant) < kLowGuard || (bi & kMant) > kMant - kHighGuard) return kSingleCode;
+  return int32_t(ee) - 1075;
 }
 
 // segmented scan element: f = a segment starts inside, v = the pairs since the last start,
