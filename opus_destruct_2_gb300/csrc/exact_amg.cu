@@ -287,12 +287,14 @@ __global__ void k_strong(int64_t nnzb, const int32_t* brow, const int32_t* col, 
 
 // ---- pass 1: the lexicographically first independent set, in rounds ---------------------------
 // state: 0 undecided, 1 root, 2 non-root (isolated rows start as non-roots: amg.cpp:340)
-__global__ void k_mis_init(int32_t n, const int32_t* rowptr, uint8_t* state, uint8_t* covered, int32_t* claim) {
+__global__ void k_mis_init(int32_t n, const int32_t* rowptr, uint8_t* state, uint8_t* covered, int32_t* claim,
+                           int32_t* claim2) {
   const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   state[i] = (rowptr[i + 1] - rowptr[i] <= 1) ? 2 : 0;
   covered[i] = 0;
   claim[i] = INT_MAX;
+  claim2[i] = INT_MAX;
 }
 
 __global__ void k_mis_claim(int32_t n, const int32_t* rowptr, const int32_t* col, const uint8_t* strong,
@@ -325,16 +327,27 @@ __global__ void k_mis_decide(int32_t n, const int32_t* rowptr, const int32_t* co
   }
 }
 
-__global__ void k_mis_cover(int32_t n, const int32_t* rowptr, const int32_t* col, const uint8_t* strong,
-                            uint8_t* state, uint8_t* covered, int32_t* claim) {
+// The cover of round r and the claims of round r + 1 in one launch, the claims double-buffered:
+// round r's (claim_done) are reset while round r + 1's go to claim_next (reset by the previous
+// such launch). A node decided in round r keeps a nonzero state, so only the still undecided
+// claim.
+__global__ void k_mis_cover_claim(int32_t n, const int32_t* rowptr, const int32_t* col, const uint8_t* strong,
+                                  uint8_t* state, uint8_t* covered, int32_t* claim_done, int32_t* claim_next) {
   const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  claim[i] = INT_MAX;
-  if (state[i] != 3) return;
-  state[i] = 1;
-  covered[i] = 1;
+  claim_done[i] = INT_MAX;
+  const uint8_t si = state[i];
+  if (si == 3) {
+    state[i] = 1;
+    covered[i] = 1;
+    for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+      if (strong[k]) covered[col[k]] = 1;
+    return;
+  }
+  if (si != 0) return;
+  atomicMin(&claim_next[i], i);
   for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
-    if (strong[k]) covered[col[k]] = 1;
+    if (strong[k]) atomicMin(&claim_next[col[k]], i);
 }
 
 // All the rounds of a smaller level in one block (claim, decide, cover as above, a block barrier
@@ -1243,7 +1256,7 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     (void)A;
   }
   Tmp<double> fro(st);
-  Tmp<int32_t> brow(st), agg1(st), flag(st), rank(st), claim(st), undecided(st);
+  Tmp<int32_t> brow(st), agg1(st), flag(st), rank(st), claim(st), claim2(st), undecided(st);
   Tmp<uint8_t> strong(st), state(st), covered(st);
   TRY(fro.alloc(size_t(nnzb)));
   TRY(brow.alloc(size_t(nnzb)));
@@ -1251,6 +1264,7 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
   TRY(state.alloc(size_t(n)));
   TRY(covered.alloc(size_t(n)));
   TRY(claim.alloc(size_t(n)));
+  TRY(claim2.alloc(size_t(n)));
   TRY(agg1.alloc(size_t(n)));
   TRY(flag.alloc(size_t(n) + 1));
   TRY(rank.alloc(size_t(n) + 1));
@@ -1274,21 +1288,26 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
   for (int round = 0;; ++round) {
     const Bsr& A = P.lv[l].A;
     (k_strong<<<nblk(nnzb), kT, 0, st>>>(nnzb, brow.p, A.col, fro.p, A.rowptr, theta, strong.p), SVXG_COUNT_LAUNCH());
-    (k_mis_init<<<nblk(n), kT, 0, st>>>(n, A.rowptr, state.p, covered.p, claim.p), SVXG_COUNT_LAUNCH());
+    (k_mis_init<<<nblk(n), kT, 0, st>>>(n, A.rowptr, state.p, covered.p, claim.p, claim2.p), SVXG_COUNT_LAUNCH());
     // rounds in batches of kBatch (a round after the last decision changes nothing), one host
-    // read per batch: the last round's count of undecided nodes
+    // read per batch: the last round's count of undecided nodes; two launches a round (decide,
+    // then cover + the next round's claims)
     constexpr int kBatch = 8;
+    int32_t* cur = claim.p;
+    int32_t* nxt = claim2.p;
     if (n <= kMisSmall)
       (k_mis_small<<<1, 1024, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, covered.p, claim.p), SVXG_COUNT_LAUNCH());
+    else
+      (k_mis_claim<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, cur), SVXG_COUNT_LAUNCH());
     for (int guard = 0; n > kMisSmall && guard <= n; guard += kBatch) {
       SVXG_CUDA(cudaMemsetAsync(undecided.p, 0, sizeof(int32_t) * kBatch, st));
       for (int b = 0; b < kBatch; ++b) {
-        (k_mis_claim<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, claim.p), SVXG_COUNT_LAUNCH());
-        (k_mis_decide<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, covered.p, claim.p,
+        (k_mis_decide<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, covered.p, cur,
                                               undecided.p + b),
          SVXG_COUNT_LAUNCH());
-        (k_mis_cover<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, covered.p, claim.p),
+        (k_mis_cover_claim<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, strong.p, state.p, covered.p, cur, nxt),
          SVXG_COUNT_LAUNCH());
+        std::swap(cur, nxt);
       }
       int32_t u = 0;
       TRY(copy_to_host(P, &u, undecided.p + (kBatch - 1), sizeof(int32_t)));
@@ -1299,7 +1318,7 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
         int32_t m = 0;
         TRY(exclusive_scan_i32(P, flag.p, rank.p, n, &m));
         (k_list_flagged<<<nblk(n), kT, 0, st>>>(n, flag.p, rank.p, agg1.p), SVXG_COUNT_LAUNCH());
-        (k_mis_tail<<<1, 1024, 0, st>>>(agg1.p, m, A.rowptr, A.col, strong.p, state.p, covered.p, claim.p),
+        (k_mis_tail<<<1, 1024, 0, st>>>(agg1.p, m, A.rowptr, A.col, strong.p, state.p, covered.p, cur),
          SVXG_COUNT_LAUNCH());
         break;
       }
