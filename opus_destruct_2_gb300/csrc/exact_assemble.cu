@@ -134,21 +134,36 @@ __global__ void k_columns(int32_t nfree, const int32_t* node_of_dof, const int32
 __device__ __forceinline__ V3d node_c(const svxg_node* nodes, int32_t i) { return v3of(nodes[i].c); }
 
 // one thread per block: its contributions in bond order (stress.cpp:94-109)
+// DIAG: a thread per row, its diagonal block (the row's first: every bond of the node); else a
+// thread per block, the off-diagonal ones (one bond each, as a rule). The two kinds take separate
+// launches: a diagonal block sums several bonds, and mixed in one warp it would hold the warp's
+// other lanes idle on the FP64 pipe.
+template <bool DIAG>
 __global__ void k_block_values(int64_t nnzb, int32_t nfree, const int32_t* rowptr, const int32_t* col,
                                const int32_t* node_of_dof, const int32_t* cstart, const int32_t* ccount,
                                const uint64_t* by_nbr, const uint32_t* by_bond, const svxg_bond* bonds,
                                const svxg_node* nodes, const svxg_material* mats, double* val) {
-  const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k >= nnzb) return;
-  // the block's row: binary search in rowptr
-  int32_t lo = 0, hi = nfree - 1;
-  while (lo < hi) {
-    const int32_t mid = (lo + hi + 1) >> 1;
-    if (rowptr[mid] <= k) lo = mid;
-    else hi = mid - 1;
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  int32_t d;
+  int64_t k;
+  if (DIAG) {
+    if (t >= nfree) return;
+    d = int32_t(t);
+    k = rowptr[d];
+  } else {
+    if (t >= nnzb) return;
+    k = t;
+    // the block's row: binary search in rowptr
+    int32_t lo = 0, hi = nfree - 1;
+    while (lo < hi) {
+      const int32_t mid = (lo + hi + 1) >> 1;
+      if (rowptr[mid] <= k) lo = mid;
+      else hi = mid - 1;
+    }
+    d = lo;
+    if (rowptr[d] == k) return;  // (the diagonal: the DIAG launch)
   }
-  const int32_t d = lo;
-  const bool diag = rowptr[d] == k;
+  const bool diag = DIAG;
   const int32_t i = node_of_dof[d];
   double C[36];
   for (int q = 0; q < 36; ++q) C[q] = 0.0;
@@ -383,10 +398,14 @@ int assemble_matrix(Problem& P) {
                                                 ccount.p), SVXG_COUNT_LAUNCH());
   trace_mark(P, "assemble: pattern");
   // 4. values
-  if (nnzb > 0)
-    (k_block_values<<<blocks_for(nnzb, 128), 128, 0, st>>>(nnzb, nfree, P.K.rowptr, P.K.col, node_of_dof.p, cstart.p,
-                                                          ccount.p, by_nbr.p, by_bond.p, P.d_bonds, P.d_nodes,
-                                                          P.d_mats, P.K.val), SVXG_COUNT_LAUNCH());
+  if (nnzb > 0) {
+    (k_block_values<true><<<blocks_for(nfree, 128), 128, 0, st>>>(nnzb, nfree, P.K.rowptr, P.K.col, node_of_dof.p,
+                                                                 cstart.p, ccount.p, by_nbr.p, by_bond.p, P.d_bonds,
+                                                                 P.d_nodes, P.d_mats, P.K.val), SVXG_COUNT_LAUNCH());
+    (k_block_values<false><<<blocks_for(nnzb, 128), 128, 0, st>>>(nnzb, nfree, P.K.rowptr, P.K.col, node_of_dof.p,
+                                                                  cstart.p, ccount.p, by_nbr.p, by_bond.p, P.d_bonds,
+                                                                  P.d_nodes, P.d_mats, P.K.val), SVXG_COUNT_LAUNCH());
+  }
   trace_mark(P, "assemble: block values");
   // 5. id_scale and identity rows
   Tmp<double> term(st), ids(st);
