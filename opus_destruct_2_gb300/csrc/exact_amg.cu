@@ -602,6 +602,14 @@ __global__ void k_p_count(int32_t n, const int32_t* rowptr, const int32_t* col, 
   plen[i] = sorted_distinct(agg[i], rowptr, col, agg, i, smoothed != 0, scratch + int64_t(rowptr[i]) + i, cap);
 }
 
+// 0.0 + x without an FP64 operation: x, with -0.0 made +0.0 (the reference's sums start at +0.0;
+// the first addition changes nothing else for a finite or infinite x), by an integer test on the
+// bits - the FP64 pipe bounds the products below
+__device__ __forceinline__ double plus_zero(double x) {
+  const long long b = __double_as_longlong(x);
+  return __longlong_as_double(b == (long long)0x8000000000000000ULL ? 0LL : b);
+}
+
 // rigid_block(r)[q][c] (blk6.cuh) with r = off3 row j, the same values without the array
 __device__ __forceinline__ double rigid_entry(const double* off3, int32_t j, int q, int c) {
   if (q == c) return 1.0;
@@ -617,12 +625,29 @@ __device__ __forceinline__ double rigid_entry(const double* off3, int32_t j, int
   }
 }
 
+// (A rigid_block(r))[row][c]: mul6's sum over q with the rigid block's zero terms left out and
+// its unit terms as plain additions. A zero product added to a sum that starts at +0.0 leaves it
+// unchanged (the sum is never -0.0) when A is finite, and x * 1.0 is x: the same bits as the
+// full sum for finite K, with 4 of its 12 FP64 operations at most.
+__device__ __forceinline__ double a_rigid_entry(const double* A, int row, int c, const double* r) {
+  const double* a = A + 6 * row;
+  switch (c) {
+    case 0:
+    case 1:
+    case 2: return plus_zero(a[c]);
+    case 3: return (plus_zero(a[1] * -r[2]) + a[2] * r[1]) + a[3];
+    case 4: return (plus_zero(a[0] * r[2]) + a[2] * -r[0]) + a[4];
+    default: return (plus_zero(a[0] * -r[1]) + a[1] * r[0]) + a[5];
+  }
+}
+
 // The smoothed prolongation rows (amg.cpp:405-452), a warp per fine row i, its P blocks in
 // shared memory when it has at most kPSlots of them. The row's own aggregate block gets
 // rigid_block(off_i); then, for the row's neighbours k in chunks of kPNb, T_k = A_ik rigid_block
 // (off_j) and U_k = D_i^-1 T_k with the (k, entry) items spread over the lanes (GB300 issues FP64
 // instructions for whole warps), and the block of aggregate agg[j] adds -omega U_k, neighbour by
-// neighbour. Every entry gets the reference's sums (mul6's 6-term sums, the axpy) in its order.
+// neighbour. Every entry gets the reference's sums (mul6's 6-term sums, the axpy) in its order;
+// T's sums skip the rigid block's zero terms (a_rigid_entry).
 constexpr int kPNb = 8;
 constexpr int kPSlots = 16;
 constexpr int kPWarps = 4;
@@ -665,19 +690,15 @@ __global__ void __launch_bounds__(32 * kPWarps) k_p_values(int32_t n, const int3
       for (int32_t it = lane; it < 36 * nk; it += 32) {
         const int32_t kl = it / 36, ent = it - 36 * kl;
         const int r = ent / 6, c = ent - 6 * r;
-        const double* A = val + 36 * int64_t(kb + kl);
-        const int32_t j = col[kb + kl];
-        double s = 0.0;
-        for (int q = 0; q < 6; ++q) s += A[r * 6 + q] * rigid_entry(off3, j, q, c);
-        t_sh[wid][it] = s;
+        t_sh[wid][it] = a_rigid_entry(val + 36 * int64_t(kb + kl), r, c, off3 + 3 * int64_t(col[kb + kl]));
       }
       __syncwarp();
       for (int32_t it = lane; it < 36 * nk; it += 32) {
         const int32_t kl = it / 36, ent = it - 36 * kl;
         const int r = ent / 6, c = ent - 6 * r;
         const double* T = t_sh[wid] + 36 * kl;
-        double s = 0.0;
-        for (int q = 0; q < 6; ++q) s += Di[r * 6 + q] * T[q * 6 + c];
+        double s = plus_zero(Di[r * 6] * T[c]);
+        for (int q = 1; q < 6; ++q) s += Di[r * 6 + q] * T[q * 6 + c];
         u_sh[wid][it] = s;
       }
       __syncwarp();
@@ -830,8 +851,8 @@ __global__ void __launch_bounds__(32 * kAccWarps) k_ap_values_acc(int32_t n, con
         const int32_t el = it / 36, ent = it - 36 * el;
         const int r = ent / 6, c = ent - 6 * r;
         const double* B = pval + 36 * int64_t(pb + el);
-        double s0 = 0.0;
-        for (int q = 0; q < 6; ++q) s0 += A[r * 6 + q] * B[q * 6 + c];
+        double s0 = plus_zero(A[r * 6] * B[c]);
+        for (int q = 1; q < 6; ++q) s0 += A[r * 6 + q] * B[q * 6 + c];
         double* C = acc + 36 * int64_t(slot_sh[wid][el]) + ent;
         *C = *C + s0;
       }
@@ -895,8 +916,8 @@ __global__ void __launch_bounds__(32 * kAccWarps) k_c_values_acc(int32_t na, con
         const int32_t el = it / 36, ent = it - 36 * el;
         const int rr = ent / 6, cc = ent - 6 * rr;
         const double* B = apval + 36 * int64_t(eb + el);
-        double sacc = 0.0;
-        for (int q = 0; q < 6; ++q) sacc += Pi[q * 6 + rr] * B[q * 6 + cc];
+        double sacc = plus_zero(Pi[rr] * B[cc]);
+        for (int q = 1; q < 6; ++q) sacc += Pi[q * 6 + rr] * B[q * 6 + cc];
         double* C = acc + 36 * int64_t(slot_sh[wid][el]) + ent;
         *C = *C + sacc;
       }
@@ -961,8 +982,8 @@ __global__ void __launch_bounds__(kRowT) k_c_values_rows(int32_t na, const int32
       double* C = acc + 36 * int64_t(slot);
       for (int ent = 9 * g; ent < 9 * g + 9; ++ent) {
         const int rr = ent / 6, cc = ent - 6 * (ent / 6);
-        double sacc = 0.0;
-        for (int q = 0; q < 6; ++q) sacc += Pi[q * 6 + rr] * B[q * 6 + cc];
+        double sacc = plus_zero(Pi[rr] * B[cc]);
+        for (int q = 1; q < 6; ++q) sacc += Pi[q * 6 + rr] * B[q * 6 + cc];
         C[ent] = C[ent] + sacc;
       }
     }
