@@ -178,7 +178,36 @@ __global__ void __launch_bounds__(exact::kThreads) k_norm_small(int64_t m, const
   const int32_t n = exact::build_segments(0, m, 0.0, SqTerm{w}, rec);
   if (threadIdx.x == 0) cnt[0] = n > exact::kTileSegs ? -1 : n;
   __syncthreads();
-  const double s = exact::walk_segments(1, cnt, rec, m, SqTerm{w});
+  const double s = exact::walk_segments(0.0, 0, 1, cnt, rec, m, SqTerm{w});
+  if (threadIdx.x == 0) {
+    nv_sh = sqrt(s);
+    set_norm(state, nv_sh);
+  }
+  __syncthreads();
+  const double nv = nv_sh;
+  if (!v || !(nv > 0)) return;
+  for (int64_t k = threadIdx.x; k < m; k += exact::kThreads) v[k] = w[k] / nv;
+}
+
+// a vector of a few tiles in one block, tile after tile: each tile's segments, then the walk over
+// them from the running sum (a launch instead of four: small requests are launch-bound)
+constexpr int64_t kNormLoopMax = 8 * exact::kTile;
+__global__ void __launch_bounds__(exact::kThreads) k_norm_loop(int64_t m, const double* w, double* v,
+                                                              exact::Seg* rec, int32_t* cnt, double* state) {
+  __shared__ double nv_sh;
+  if (state[2] != 0.0) return;
+  double s = 0.0, before = 0.0;
+  const int32_t ntile = int32_t((m + exact::kTile - 1) / exact::kTile);
+  for (int32_t c = 0; c < ntile; ++c) {
+    const int64_t a = int64_t(c) * exact::kTile, b = a + exact::kTile < m ? a + exact::kTile : m;
+    double tile = 0.0;
+    const int32_t n = exact::build_segments(a, b, before, SqTerm{w}, rec, &tile);
+    if (threadIdx.x == 0) cnt[0] = n > exact::kTileSegs ? -1 : n;
+    __syncthreads();
+    s = exact::walk_segments(s, c, 1, cnt, rec, m, SqTerm{w});
+    if (!(s < INFINITY)) break;  // (the walk has looked at every later term)
+    before += tile;
+  }
   if (threadIdx.x == 0) {
     nv_sh = sqrt(s);
     set_norm(state, nv_sh);
@@ -222,7 +251,7 @@ __global__ void __launch_bounds__(exact::kThreads) k_norm_walk(int64_t m, int32_
                                                               const exact::Seg* rec, const int32_t* cnt,
                                                               double* state) {
   if (state[2] != 0.0) return;
-  const double s = exact::walk_segments(ntile, cnt, rec, m, SqTerm{w});
+  const double s = exact::walk_segments(0.0, 0, ntile, cnt, rec, m, SqTerm{w});
   if (threadIdx.x == 0) set_norm(state, sqrt(s));
 }
 
@@ -253,6 +282,10 @@ struct NormScratch {
 int launch_norm(cudaStream_t st, int64_t m, const double* w, double* v, double* state, NormScratch& S) {
   if (m <= exact::kTile) {
     (k_norm_small<<<1, exact::kThreads, 0, st>>>(m, w, v, S.rec.p, S.cnt.p, state), SVXG_COUNT_LAUNCH());
+    return SVXG_OK;
+  }
+  if (m <= kNormLoopMax) {
+    (k_norm_loop<<<1, exact::kThreads, 0, st>>>(m, w, v, S.rec.p, S.cnt.p, state), SVXG_COUNT_LAUNCH());
     return SVXG_OK;
   }
   const unsigned nt = unsigned(S.ntile);

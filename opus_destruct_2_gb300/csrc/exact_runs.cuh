@@ -146,9 +146,10 @@ __device__ __forceinline__ Pair seg_pair(double t, int32_t code) {
 
 // The segments of terms [a, b) (b - a <= kTile; before: the approximate sum of the terms
 // before a), in order, to out[0, kTileSegs); returns their count in every thread (more than
-// kTileSegs: only counted).
+// kTileSegs: only counted), and the tile's approximate sum in *tile_total when given.
 template <class Term>
-__device__ int32_t build_segments(int64_t a, int64_t b, double before, Term term, Seg* out) {
+__device__ int32_t build_segments(int64_t a, int64_t b, double before, Term term, Seg* out,
+                                  double* tile_total = nullptr) {
   __shared__ int32_t first_code[kThreads / 32], last_code[kThreads / 32];
   __shared__ SegScan wsc[kThreads / 32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -161,6 +162,7 @@ __device__ int32_t build_segments(int64_t a, int64_t b, double before, Term term
     own += t[it];
   }
   double pe = before + block_excl_approx(own);
+  if (tile_total) *tile_total = block_sum_approx(own);
   int32_t code[kItems];
 #pragma unroll
   for (int it = 0; it < kItems; ++it) {
@@ -239,19 +241,20 @@ __device__ int32_t build_segments(int64_t a, int64_t b, double before, Term term
   return total;
 }
 
-// The sequential sum from 0 over the segments of tiles [0, ntile): tile c's cnt[c] records at
-// rec + c kTileSegs, or, for cnt[c] < 0, its terms [c kTile, min((c + 1) kTile, m)) term by term.
-// Every thread gets the result.
+// The sequential sum from s0 over the segments of tiles tile0 + [0, ntile): tile tile0 + i's
+// cnt[i] records at rec + i kTileSegs, or, for cnt[i] < 0, its terms term by term. Every thread
+// gets the result (after a non-finite partial sum: the final one, all later terms looked at).
 constexpr int kWalkBatch = 512;
 template <class Term>
-__device__ double walk_segments(int32_t ntile, const int32_t* cnt, const Seg* rec, int64_t m, Term term) {
+__device__ double walk_segments(double s0, int32_t tile0, int32_t ntile, const int32_t* cnt, const Seg* rec,
+                                int64_t m, Term term) {
   __shared__ Seg batch[kWalkBatch];
   __shared__ int32_t woff[kThreads + 1];
   __shared__ double s_sh;
   __shared__ int32_t j_sh, act_sh;
   __shared__ int64_t fa_sh, fb_sh;
   if (threadIdx.x == 0) {
-    s_sh = 0.0;
+    s_sh = s0;
     act_sh = 0;
   }
   __syncthreads();
@@ -277,7 +280,7 @@ __device__ double walk_segments(int32_t ntile, const int32_t* cnt, const Seg* re
         const int32_t c = c0 + lo;
         const int32_t n = cnt[c];
         if (n < 0) {
-          const int64_t ta = int64_t(c) * kTile, tb = ta + kTile < m ? ta + kTile : m;
+          const int64_t ta = int64_t(tile0 + c) * kTile, tb = ta + kTile < m ? ta + kTile : m;
           batch[threadIdx.x] = Seg{Pair{0, 0}, 0.0, ta, int32_t(tb - ta), kRangeCode};
         } else {
           batch[threadIdx.x] = rec[int64_t(c) * kTileSegs + (g - woff[lo])];
