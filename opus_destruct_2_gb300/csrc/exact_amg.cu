@@ -218,6 +218,81 @@ __global__ void __launch_bounds__(exact::kThreads) k_norm_loop(int64_t m, const 
   for (int64_t k = threadIdx.x; k < m; k += exact::kThreads) v[k] = w[k] / nv;
 }
 
+// the same terms read through L2 (a block reading other blocks' writes of the same launch)
+struct SqTermCG {
+  const double* w;
+  __device__ __forceinline__ double operator()(int64_t k) const {
+    const double x = __ldcg(w + k);
+    return x * x;
+  }
+};
+
+// A power iteration step of a level of at most exact::kTile unknowns in one launch: the warps
+// apply D^-1 A v a node each (k_lmax_apply_rows' sums), and the last block to finish takes the
+// exact norm and the scaling (k_norm_small's) - one launch a step instead of two, for the small
+// problems whose setup is bound by launches.
+constexpr int kStepChunk = 8;
+__global__ void __launch_bounds__(exact::kThreads) k_lmax_step_small(int32_t n, const int32_t* rowptr,
+                                                                    const int32_t* col, const double* val,
+                                                                    const double* dinv, double* v, double* w,
+                                                                    exact::Seg* rec, int32_t* cnt, unsigned* counter,
+                                                                    double* state) {
+  __shared__ double d_sh[exact::kThreads / 32][6 * kStepChunk];
+  __shared__ double y_sh[exact::kThreads / 32][6];
+  __shared__ bool last;
+  __shared__ double nv_sh;
+  if (state[2] != 0.0) return;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int32_t i = int32_t(blockIdx.x) * (exact::kThreads / 32) + wid;
+  if (i < n) {
+    double yr = 0.0;
+    for (int32_t kb = rowptr[i]; kb < rowptr[i + 1]; kb += kStepChunk) {
+      const int32_t nk = rowptr[i + 1] - kb < kStepChunk ? rowptr[i + 1] - kb : kStepChunk;
+      for (int32_t it = lane; it < 6 * nk; it += 32) {
+        const int32_t kl = it / 6;
+        const int r = it - 6 * kl;
+        const double* m = val + 36 * int64_t(kb + kl) + 6 * r;
+        const double* xv = v + 6 * int64_t(col[kb + kl]);
+        d_sh[wid][it] = m[0] * xv[0] + m[1] * xv[1] + m[2] * xv[2] + m[3] * xv[3] + m[4] * xv[4] + m[5] * xv[5];
+      }
+      __syncwarp();
+      if (lane < 6)
+        for (int32_t kl = 0; kl < nk; ++kl) yr += d_sh[wid][6 * kl + lane];
+      __syncwarp();
+    }
+    if (lane < 6) y_sh[wid][lane] = yr;
+    __syncwarp();
+    if (lane < 6) {
+      const double* x = y_sh[wid];
+      const double* m = dinv + 36 * int64_t(i) + 6 * lane;
+      w[6 * int64_t(i) + lane] = m[0] * x[0] + m[1] * x[1] + m[2] * x[2] + m[3] * x[3] + m[4] * x[4] + m[5] * x[5];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // (every block has read v and written w: the last one may rescale v)
+  const int64_t mm = 6 * int64_t(n);
+  const int32_t ns = exact::build_segments(0, mm, 0.0, SqTermCG{w}, rec);
+  if (threadIdx.x == 0) cnt[0] = ns > exact::kTileSegs ? -1 : ns;
+  __syncthreads();
+  const double sum = exact::walk_segments(0.0, 0, 1, cnt, rec, mm, SqTermCG{w});
+  if (threadIdx.x == 0) {
+    nv_sh = sqrt(sum);
+    set_norm(state, nv_sh);
+    *counter = 0u;
+  }
+  __syncthreads();
+  const double nv = nv_sh;
+  if (!(nv > 0)) return;
+  for (int64_t k = threadIdx.x; k < mm; k += exact::kThreads) v[k] = __ldcg(w + k) / nv;
+}
+
 // tile sums (any order: the predictions' approximate prefix)
 __global__ void __launch_bounds__(256) k_norm_tile_sum(int64_t m, const double* w, double* tsum, const double* state) {
   __shared__ double sh[256];
@@ -1281,7 +1356,17 @@ int estimate_lmax(Problem& P, const Level& L, double* out) {
   SVXG_CUDA(cudaMemcpyAsync(st.p, init, sizeof(init), cudaMemcpyHostToDevice, P.stream));
   (k_lmax_init<<<nblk(m), kT, 0, P.stream>>>(m, v.p), SVXG_COUNT_LAUNCH());
   const unsigned ab = unsigned((m + 6 * kApplyNodes - 1) / (6 * kApplyNodes));
-  for (int it = 0; it < 15; ++it) {
+  if (m <= exact::kTile) {
+    Tmp<unsigned> counter(P.stream);
+    TRY(counter.alloc(1));
+    SVXG_CUDA(cudaMemsetAsync(counter.p, 0, sizeof(unsigned), P.stream));
+    const unsigned sb = unsigned((n + exact::kThreads / 32 - 1) / (exact::kThreads / 32));
+    for (int it = 0; it < 15; ++it)
+      (k_lmax_step_small<<<sb, exact::kThreads, 0, P.stream>>>(n, L.A.rowptr, L.A.col, L.A.val, L.dinv, v.p, w.p,
+                                                               ns.rec.p, ns.cnt.p, counter.p, st.p),
+       SVXG_COUNT_LAUNCH());
+  }
+  for (int it = 0; m > exact::kTile && it < 15; ++it) {
     if (n <= kApplyRowsMax)
       (k_lmax_apply_rows<<<unsigned((n + kApplyWarps - 1) / kApplyWarps), 32 * kApplyWarps, 0, P.stream>>>(
            n, L.A.rowptr, L.A.col, L.A.val, L.dinv, v.p, w.p, st.p),
