@@ -429,7 +429,7 @@ __global__ void k_mis_decide(int32_t n, const int32_t* rowptr, const int32_t* co
   if (cov) {
     state[i] = 2;
   } else if (mine) {
-    state[i] = 3;  // (a root of this round: covers in k_mis_cover)
+    state[i] = 3;  // (a root of this round: covers in k_mis_cover_claim)
   } else {
     atomicAdd(undecided, 1);
   }
