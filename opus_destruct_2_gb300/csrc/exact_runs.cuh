@@ -3,8 +3,8 @@
 //
 // An approximate prefix sum, taken in any order, places every partial sum of the sequence in
 // its binade up to a relative margin (about 1.5e-8: the sequential sum of k terms is within
-// k 2^-53 of the exact one, the approximate prefix far closer). Terms whose partial sums before and after
-// lie safely inside one binade form runs; the increment pairs of a run's terms (exact_sum.cuh:
+// k 2^-53 of the exact one, the approximate prefix far closer). Terms whose partial sums before
+// and after lie safely inside one binade form runs; the increment pairs of a run's terms (exact_sum.cuh:
 // integer additions in the binade's ulps, ties keyed by parity) compose into one pair in
 // parallel. A term at which the binade may change is a single, added by the hardware. One thread
 // then walks the segments in order with the exact running sum: a run is applied in one step when
@@ -104,8 +104,8 @@ __device__ inline double block_sum_approx(double v) {
 
 // A term's segment code from the approximate sums before (pe) and after (pi) it, by integer
 // tests on their bits (the FP64 pipe is the scarce one): a run code when both are normal, in
-// one binade, and at least about 1.5e-8 of it inside (mantissa fractions above kLowGuard and below
-// the top by kHighGuard, in ulps of 2^52), else a single.
+// one binade, and at least about 1.5e-8 of it inside (mantissa fractions above kLowGuard and
+// below the top by kHighGuard, in ulps of 2^52), else a single.
 constexpr uint64_t kMant = (uint64_t(1) << 52) - 1;
 constexpr uint64_t kLowGuard = uint64_t(1) << 26;   // 1.5e-8 of the binade's bottom
 constexpr uint64_t kHighGuard = uint64_t(1) << 27;  // 1.5e-8 of its top
