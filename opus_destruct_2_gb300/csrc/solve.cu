@@ -134,10 +134,62 @@ __global__ void __launch_bounds__(kSpmvT) k_spmv(int32_t n, const int32_t* __res
   }
 }
 
+// The CG product with its fused p.q: each warp takes kDotSteps row steps (the block's warps on
+// consecutive warp indices at every step) before the block's reduction, whose FP64 shuffle tree
+// and partials counter a block otherwise pays every 8 (or 40) rows - GB300's FP64 pipe bounds
+// this kernel, and the counter's wait holds the block's warps.
+constexpr int kDotSteps = 4;
+template <int SCHED>
+__global__ void __launch_bounds__(kSpmvT) k_spmv_dot(int32_t n, const int32_t* __restrict__ rowptr,
+                                                     const int32_t* __restrict__ col, const double* __restrict__ val,
+                                                     const double* __restrict__ x, double* __restrict__ y,
+                                                     double* partials, unsigned* counter, PcgScalars* s) {
+  __shared__ double sh[kSpmvT / 32];
+  if (s->done) return;
+  double dp = 0.0;
+  for (int j = 0; j < kDotSteps; ++j) {
+    int c;
+    bool lane_ok;
+    const int32_t warp = (int32_t(blockIdx.x) * kDotSteps + j) * kRowsPerBlock + (threadIdx.x >> 5);
+    const int32_t row = sched_row_of<SCHED>(warp, &c, &lane_ok);
+    const bool row_ok = row < n;
+    if (SCHED == kWarpRow && !row_ok) break;  // (warp-uniform; the warp's rows only grow)
+    const double yr = sched_row_product<SCHED, double, double, double>(row_ok, row, rowptr, col, val, x);
+    if (row_ok && lane_ok) {
+      y[6 * int64_t(row) + c] = yr;
+      dp += x[6 * int64_t(row) + c] * yr;
+    }
+  }
+  const double bs = block_sum<kSpmvT>(dp, sh);
+  if (publish<1>(&bs, partials, counter)) {
+    double tot;
+    gather_totals<kSpmvT, 1>(partials, counter, &tot, sh);
+    if (threadIdx.x == 0) {
+      s->pq = tot;
+      s->iters += 1;
+      if (!(tot > 0)) {
+        s->breakdown = 1;
+        s->done = 1;
+      } else {
+        s->alpha = s->rz / tot;
+      }
+    }
+  }
+}
+
 template <int EPI>
 void launch_spmv(cudaStream_t st, int sched, int32_t n, const int32_t* rowptr, const int32_t* col, const double* val,
                  const double* x, double* y, double* partials, unsigned* counter, PcgScalars* s) {
-  if (sched == kGroupRow) {
+  if (EPI == kDotP) {
+    const int per = kRowsPerBlock * kDotSteps * (sched == kGroupRow ? 5 : 1);
+    const unsigned g = unsigned((std::max(n, 1) + per - 1) / per);
+    if (sched == kGroupRow)
+      (k_spmv_dot<kGroupRow><<<g, kSpmvT, 0, st>>>(n, rowptr, col, val, x, y, partials, counter, s),
+       SVXG_COUNT_LAUNCH());
+    else
+      (k_spmv_dot<kWarpRow><<<g, kSpmvT, 0, st>>>(n, rowptr, col, val, x, y, partials, counter, s),
+       SVXG_COUNT_LAUNCH());
+  } else if (sched == kGroupRow) {
     const unsigned g = unsigned((std::max(n, 1) + 5 * kRowsPerBlock - 1) / (5 * kRowsPerBlock));
     (k_spmv<EPI, kGroupRow><<<g, kSpmvT, 0, st>>>(n, rowptr, col, val, x, y, partials, counter, s),
      SVXG_COUNT_LAUNCH());
