@@ -43,6 +43,8 @@ typedef struct svxg_info {
   int64_t device_bytes;     /* what the problem holds on the device now */
   int32_t precision;        /* SVXG_PRECISION_* of the last assemble */
   int32_t mixed_fallbacks;  /* mixed-precision solves since then finished in FP64 (FP32 stalled) */
+  int64_t graph_bytes;      /* of device_bytes: the graph's copy (nodes, bonds, materials); the rest
+                               is what svxg_release frees (StressProblem::solver_bytes) */
 } svxg_info;
 
 const char* svxg_last_error(void);
@@ -138,9 +140,11 @@ int svxg_utilization_device(svxg_problem* p, double fragility, double* phi_dev, 
  * (a cudaStream_t, null: the legacy default stream) of the current device; *n_over (host) gets
  * the failure count after the stream synchronizes. Allocates nothing: its scratch is one
  * 512 KiB array in the library's device image, so at most 16,777,216 bonds (more: SVXG_ERR_ARG).
- * A device's first call looks that array up (cudaGetSymbolAddress), so make it before any stream
- * capture. Calls share the array: calls that overlap on the GPU race and must be ordered by the
- * caller. Node indices and material ids out of range: SVXG_ERR_ARG, those bonds skipped. */
+ * A device's first call looks that array up (cudaGetSymbolAddress) and keeps its address for the
+ * life of the process, so make it before any stream capture, and do not call this after a
+ * cudaDeviceReset of that device. Each call synchronizes `stream` before it returns (it reads the
+ * count back). Calls share the array: calls that overlap on the GPU race and must be ordered by
+ * the caller. Node indices and material ids out of range: SVXG_ERR_ARG, those bonds skipped. */
 int svxg_utilization_noalloc(const svxg_node* nodes_dev, int32_t n, const svxg_bond* bonds_dev, int32_t nb,
                              const svxg_material* mats_dev, const double* u_dev, double fragility, double* phi_dev,
                              uint8_t* mode_dev, int32_t* over_dev, int32_t* n_over, void* stream);
@@ -218,6 +222,14 @@ int64_t svxg_launch_count(void);
  * its launches while enabled; read returns their summed duration (ms) and count, and resets. */
 int svxg_timer_enable(svxg_problem* p, int32_t on);
 int svxg_timer_read(svxg_problem* p, double* ms_total, int64_t* launches);
+/* The conjugate-gradient SpMV timed alone: `reps` back-to-back launches of the kernel an iteration
+ * runs on the assembled K (q = K p with p.q fused; precision SVXG_PRECISION_FP64: the FP64 K,
+ * otherwise the mixed sequence's FP32 K), each doing its work, CUDA events on the problem's
+ * stream; *ms_per_launch their mean. The problem's run state is not touched. */
+int svxg_time_spmv(svxg_problem* p, int32_t precision, int32_t reps, double* ms_per_launch);
+/* This GPU's FP64 fused multiply-add throughput (TFLOP/s, 2 per FMA), measured by independent FMA
+ * chains over every SM: the ceiling of the FP64-issue-bound kernels. */
+int svxg_measure_fp64_rate(int device, double* tflops);
 
 /* --- parity access (tests) ------------------------------------------------------------------ */
 /* K as assembled: call with null arrays for *nfree / *nnzb, then with arrays of those sizes. */

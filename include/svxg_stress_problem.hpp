@@ -10,17 +10,28 @@
 // Like the reference, callers may change `nodes` and `bonds` between calls: the graph is sent to
 // the device at assemble(), and again before a solve when its contents changed since (which, as
 // assembling again would, drops the assembled operator).
+//
+// Errors follow the reference's contract, which is built without exceptions (CMakeLists.txt:248,
+// -fno-exceptions): nothing here throws. A failed library call leaves its message in error()
+// (and svxg_last_error()); assemble() then returns false, solve() / iterate() a result with
+// breakdown set and rel_res = inf (the reference's answer for an unassembled problem,
+// stress.cpp:349-354), and the other members leave their outputs empty or zero. A problem whose
+// device could not be set up (ok() false) fails every call that way.
 #pragma once
 
 #include <cmath>
 #include <cstring>
-#include <stdexcept>
 #include <string>
 #include <vector>
 
 #include "svxg.h"
 
 namespace svxg {
+
+// What a byte count counts (svx::Bytes, core/include/svx/base/mem.hpp:14): Held - what the
+// problem holds (host vectors' capacities, device allocations); Used - what it uses (host vectors'
+// elements; the device side is allocated to size, so both count the same there).
+enum class Bytes : uint8_t { Held, Used };
 
 class StressProblem {
  public:
@@ -29,36 +40,45 @@ class StressProblem {
   std::vector<svxg_material> mats;  // SVXG_MAX_MATERIALS entries
 
   explicit StressProblem(int device = 0) {
-    if (svxg_problem_create(&p_, device) != SVXG_OK) throw std::runtime_error(svxg_last_error());
+    if (svxg_problem_create(&p_, device) != SVXG_OK) {
+      p_ = nullptr;
+      note_error();
+    }
   }
-  ~StressProblem() { svxg_problem_destroy(p_); }
+  ~StressProblem() {
+    if (p_) svxg_problem_destroy(p_);
+  }
   StressProblem(const StressProblem&) = delete;
   StressProblem& operator=(const StressProblem&) = delete;
 
-  // stress.hpp:83 - K and the preconditioner; false on a singular diagonal
+  // whether the device side exists; the message of the last failed call
+  bool ok() const { return p_ != nullptr; }
+  const std::string& error() const { return error_; }
+
+  // stress.hpp:83 - K and the preconditioner; false on a singular diagonal or a failed call
   bool assemble(const svxg_stress_options& opt = svxg_default_options()) {
-    upload();
+    if (!upload()) return false;
     int32_t ok = 0;
-    check(svxg_assemble(p_, &opt, &ok));
+    if (!check(svxg_assemble(p_, &opt, &ok))) return false;
     pull_flags();
     return ok != 0;
   }
-  bool assembled() const { return svxg_assembled(p_) != 0; }
+  bool assembled() const { return p_ && svxg_assembled(p_) == 1; }
   void invalidate() { check(svxg_invalidate(p_)); }
-  bool preconditioner_current() const { return svxg_preconditioner_current(p_) != 0; }
-  bool block_jacobi() const { return svxg_block_jacobi(p_) != 0; }
+  bool preconditioner_current() const { return p_ && svxg_preconditioner_current(p_) == 1; }
+  bool block_jacobi() const { return p_ && svxg_block_jacobi(p_) == 1; }
   int64_t assembly_work() const { return info().assembly_work; }
   void release() {
-    check(svxg_release(p_));
+    if (!check(svxg_release(p_))) return;
     for (auto& b : bonds) b.in_k = 0;
     sent_bonds_ = bonds;
+    ++generation_;
   }
   void remove_bond(int32_t b) {
-    check(svxg_remove_bond(p_, b));
-    pull_flags();
+    if (check(svxg_remove_bond(p_, b))) pull_flags();
   }
   void retire_nodes(const std::vector<int32_t>& list) {
-    check(svxg_retire_nodes(p_, list.data(), int32_t(list.size())));
+    if (!check(svxg_retire_nodes(p_, list.data(), int32_t(list.size())))) return;
     for (int32_t i : list) nodes[size_t(i)].gone = 1;
     sent_nodes_ = nodes;
     pull_flags();
@@ -66,59 +86,96 @@ class StressProblem {
   // stress.hpp:110 - K again from nodes and bonds as they are now; appended nodes get their own
   // preconditioner, the old one keeps the rest
   bool reassemble() {
-    if (mats.size() != SVXG_MAX_MATERIALS) throw std::runtime_error("svxg: mats needs every material id");
+    if (!mats_complete()) return false;
     int32_t ok = 0;
-    check(svxg_reassemble(p_, nodes.data(), int32_t(nodes.size()), bonds.data(), int32_t(bonds.size()), mats.data(),
-                          &ok));
+    if (!check(svxg_reassemble(p_, nodes.data(), int32_t(nodes.size()), bonds.data(), int32_t(bonds.size()),
+                               mats.data(), &ok)))
+      return false;
     sent_nodes_ = nodes;
     sent_bonds_ = bonds;
     pull_flags();
     return ok != 0;
   }
   // stress.hpp:113 - appended nodes' warm start from their older neighbours (u: 6 per node)
-  void extend_warm_start(std::vector<double>& u, int32_t first_new_node) {
-    upload_if_changed();
-    if (u.size() != 6 * nodes.size()) return;
+  void extend_warm_start(std::vector<double>& u, int32_t first_new_node) const {
+    if (!upload_if_changed() || u.size() != 6 * nodes.size()) return;
     check(svxg_extend_warm_start(p_, u.data(), first_new_node));
   }
-  int32_t appended() const { return svxg_appended(p_); }
+  int32_t appended() const { return p_ ? svxg_appended(p_) : 0; }
   int32_t free_nodes() const { return info().nfree; }
   int64_t matrix_blocks() const { return info().matrix_blocks; }
-  int64_t memory_bytes() const { return info().device_bytes; }
+  // stress.hpp:116-117 - the graph's records and the solver; of those, what release() frees
+  int64_t memory_bytes(Bytes kind = Bytes::Held) const {
+    const svxg_info i = info();
+    return host_bytes(nodes, kind) + host_bytes(bonds, kind) + host_bytes(mats, kind) + i.device_bytes;
+  }
+  int64_t solver_bytes(Bytes kind = Bytes::Held) const {
+    (void)kind;
+    const svxg_info i = info();
+    return i.device_bytes - i.graph_bytes;
+  }
   int64_t work_per_iteration() const { return info().work_per_iteration; }
 
   // stress.hpp:122 - f, u: 6 per node; u: warm start in, solution out; maxit < 0: no cap
   svxg_pcg_result solve(const std::vector<double>& f, std::vector<double>& u, double rtol, int maxit, bool warm) {
-    upload_if_changed();
     u.resize(6 * nodes.size(), 0.0);
+    if (f.size() != 6 * nodes.size()) {
+      error_ = "svxg: f needs 6 entries per node";
+      return failed();
+    }
+    if (!upload_if_changed()) return failed();
     svxg_pcg_result r{};
-    check(svxg_solve(p_, f.data(), u.data(), rtol, maxit, warm ? 1 : 0, &r));
+    if (!check(svxg_solve(p_, f.data(), u.data(), rtol, maxit, warm ? 1 : 0, &r))) return failed();
     pull_flags();
     return r;
   }
   void begin(const std::vector<double>& f, const std::vector<double>& u0) {
-    upload_if_changed();
+    if (f.size() != 6 * nodes.size()) {
+      error_ = "svxg: f needs 6 entries per node";
+      return;
+    }
+    if (!upload_if_changed()) return;
     check(svxg_begin(p_, f.data(), u0.size() == 6 * nodes.size() ? u0.data() : nullptr));
   }
   svxg_pcg_result iterate(int maxit, double rtol) {
     svxg_pcg_result r{};
-    check(svxg_iterate(p_, maxit, rtol, &r));
+    if (!check(svxg_iterate(p_, maxit, rtol, &r))) return failed();
     return r;
   }
-  bool running() const { return svxg_running(p_) != 0; }
+  bool running() const { return p_ && svxg_running(p_) == 1; }
   void stop() { check(svxg_stop(p_)); }
   void current(std::vector<double>& u) const {
     u.assign(6 * nodes.size(), 0.0);
     check(svxg_current(p_, u.data()));
   }
 
-  // stress.hpp:132 - one bond's load at u (the device evaluates every bond; see bond_loads)
-  svxg_bond_load bond_load(int32_t b, const std::vector<double>& u) const { return bond_loads(u)[size_t(b)]; }
+  // stress.hpp:132 - one bond's load at u. The reference's callers ask bond by bond at one u
+  // (world.cpp:1174, :1238, :1927; world_io.cpp:98, :122); the device evaluates every bond at once,
+  // so the loads of the last u asked for are kept here and served while the two nodes a bond reads
+  // (u of its ends) are unchanged and no call changed the graph since: one device pass per
+  // distinct u, O(1) host work per call. Changes callers make to `nodes` / `bonds` themselves are
+  // seen by the next device pass (a new u, or bond_loads()).
+  svxg_bond_load bond_load(int32_t b, const std::vector<double>& u) const {
+    if (b < 0 || size_t(b) >= bonds.size() || u.size() != 6 * nodes.size()) return svxg_bond_load{};
+    if (!cache_serves(b, u)) {
+      cache_.loads = bond_loads(u);
+      cache_.u = u;
+      cache_.generation = generation_;
+      cache_.valid = cache_.loads.size() == bonds.size();
+      ++cache_.device_passes;
+      if (!cache_.valid) return svxg_bond_load{};
+    }
+    return cache_.loads[size_t(b)];
+  }
+  // every bond's load at u, one device pass
   std::vector<svxg_bond_load> bond_loads(const std::vector<double>& u) const {
+    if (u.size() != 6 * nodes.size() || !upload_if_changed()) return {};
     std::vector<svxg_bond_load> out(bonds.size());
-    check(svxg_bond_loads(p_, u.data(), out.data()));
+    if (!check(svxg_bond_loads(p_, u.data(), out.data()))) return {};
     return out;
   }
+  // device passes bond_load() has made (for callers checking the per-u cache)
+  int64_t bond_load_passes() const { return cache_.device_passes; }
   // bond_utilization (stress.hpp:64-66) of every bond at the current solution; failing bonds
   struct Judgement {
     std::vector<double> phi;
@@ -131,8 +188,9 @@ class StressProblem {
     j.mode.resize(bonds.size());
     j.failing.resize(bonds.size() + 1);
     int32_t n = 0;
-    check(svxg_utilization(p_, fragility, j.phi.data(), j.mode.data(), j.failing.data(), int32_t(j.failing.size()),
-                           &n));
+    if (!check(svxg_utilization(p_, fragility, j.phi.data(), j.mode.data(), j.failing.data(),
+                                int32_t(j.failing.size()), &n)))
+      return Judgement{};
     j.failing.resize(size_t(n));
     return j;
   }
@@ -160,9 +218,12 @@ class StressProblem {
   Cascade cascade(const std::vector<double>& f, std::vector<double>& u,
                   const svxg_cascade_options& o = svxg_default_cascade_options(),
                   std::vector<svxg_bond_load>* judged = nullptr, std::vector<uint8_t>* judged_has = nullptr) {
-    upload_if_changed();
     Cascade c;
     u.resize(6 * nodes.size(), 0.0);
+    if (f.size() != 6 * nodes.size() || !upload_if_changed()) {
+      c.result.status = SVXG_ERR_ARG;
+      return c;
+    }
     c.broken.resize(bonds.size() + 1);
     c.retired.resize(nodes.size() + 1);
     c.phi.resize(bonds.size() + 1);
@@ -170,9 +231,14 @@ class StressProblem {
       judged->resize(bonds.size());
       judged_has->resize(bonds.size(), 0);
     }
-    check(svxg_cascade(p_, nullptr, &o, f.data(), u.data(), judged && judged_has ? judged->data() : nullptr,
-                       judged && judged_has ? judged_has->data() : nullptr, c.phi.data(), c.broken.data(),
-                       int32_t(c.broken.size()), c.retired.data(), int32_t(c.retired.size()), &c.result));
+    const int e = svxg_cascade(p_, nullptr, &o, f.data(), u.data(), judged && judged_has ? judged->data() : nullptr,
+                               judged && judged_has ? judged_has->data() : nullptr, c.phi.data(), c.broken.data(),
+                               int32_t(c.broken.size()), c.retired.data(), int32_t(c.retired.size()), &c.result);
+    if (!check(e)) {
+      c = Cascade{};
+      c.result.status = e;
+      return c;
+    }
     c.broken.resize(size_t(c.result.bonds_broken));
     c.retired.resize(size_t(c.result.nodes_retired));
     c.phi.resize(bonds.size());
@@ -191,14 +257,22 @@ class StressProblem {
   };
   PieceRounds piece_rounds(std::vector<double>& f, std::vector<double>& u,
                            const svxg_piece_options& o = svxg_default_piece_options(), const double* gf = nullptr) {
-    upload_if_changed();
     PieceRounds r;
     u.resize(6 * nodes.size(), 0.0);
+    if (f.size() != 6 * nodes.size() || !upload_if_changed()) {
+      r.result.status = SVXG_ERR_ARG;
+      return r;
+    }
     r.broken.resize(bonds.size() + 1);
     r.modes.resize(bonds.size() + 1);
     r.chips.resize(nodes.size() + 1);
-    check(svxg_piece_rounds(p_, nullptr, &o, gf, f.data(), u.data(), r.broken.data(), r.modes.data(),
-                            int32_t(r.broken.size()), r.chips.data(), int32_t(r.chips.size()), &r.result));
+    const int e = svxg_piece_rounds(p_, nullptr, &o, gf, f.data(), u.data(), r.broken.data(), r.modes.data(),
+                                    int32_t(r.broken.size()), r.chips.data(), int32_t(r.chips.size()), &r.result);
+    if (!check(e)) {
+      r = PieceRounds{};
+      r.result.status = e;
+      return r;
+    }
     r.broken.resize(size_t(r.result.bonds_broken));
     r.modes.resize(size_t(r.result.bonds_broken));
     r.chips.resize(size_t(r.result.chips));
@@ -216,34 +290,87 @@ class StressProblem {
   svxg_problem* handle() const { return p_; }
 
  private:
-  static void check(int code) {
-    if (code < 0) throw std::runtime_error(std::string("svxg: ") + svxg_last_error());
+  // false (and the message kept) for a failed call; a missing device side fails every call
+  bool check(int code) const {
+    if (!p_) {
+      if (error_.empty()) error_ = "svxg: no device problem";
+      return false;
+    }
+    if (code >= 0) return true;
+    note_error();
+    return false;
   }
-  void upload() {
-    if (mats.size() != SVXG_MAX_MATERIALS) throw std::runtime_error("svxg: mats needs every material id");
-    check(svxg_set_graph(p_, nodes.data(), int32_t(nodes.size()), bonds.data(), int32_t(bonds.size()), mats.data()));
+  void note_error() const { error_ = std::string("svxg: ") + svxg_last_error(); }
+  static svxg_pcg_result failed() {
+    svxg_pcg_result r{};
+    r.breakdown = 1;
+    r.rel_res = INFINITY;
+    return r;
+  }
+  bool mats_complete() const {
+    if (mats.size() == SVXG_MAX_MATERIALS) return true;
+    error_ = "svxg: mats needs every material id";
+    return false;
+  }
+  template <class T>
+  static int64_t host_bytes(const std::vector<T>& v, Bytes kind) {
+    return int64_t((kind == Bytes::Held ? v.capacity() : v.size()) * sizeof(T));
+  }
+  bool upload() const {
+    if (!mats_complete()) return false;
+    if (!check(svxg_set_graph(p_, nodes.data(), int32_t(nodes.size()), bonds.data(), int32_t(bonds.size()),
+                              mats.data())))
+      return false;
     sent_nodes_ = nodes;
     sent_bonds_ = bonds;
+    ++generation_;
+    return true;
   }
   static bool same(const void* a, const void* b, size_t n) { return n == 0 || std::memcmp(a, b, n) == 0; }
-  void upload_if_changed() {
+  bool upload_if_changed() const {
     if (nodes.size() != sent_nodes_.size() || bonds.size() != sent_bonds_.size() ||
         !same(nodes.data(), sent_nodes_.data(), nodes.size() * sizeof(svxg_node)) ||
         !same(bonds.data(), sent_bonds_.data(), bonds.size() * sizeof(svxg_bond)))
-      upload();
+      return upload();
+    return true;
   }
   void pull_flags() {
     std::vector<uint8_t> br(bonds.size()), ik(bonds.size());
-    check(svxg_bond_flags(p_, br.data(), ik.data()));
+    ++generation_;
+    if (!check(svxg_bond_flags(p_, br.data(), ik.data()))) return;
     for (size_t k = 0; k < bonds.size(); ++k) {
       bonds[k].broken = br[k];
       bonds[k].in_k = ik[k];
     }
     sent_bonds_ = bonds;
   }
+  // the per-u loads serve bond b while the graph is the one they were made from and u is the
+  // same at b's ends (a bond's load reads u at its two nodes only, stress.cpp:477-502)
+  bool cache_serves(int32_t b, const std::vector<double>& u) const {
+    if (!cache_.valid || cache_.generation != generation_ || cache_.u.size() != u.size()) return false;
+    const svxg_bond& bd = bonds[size_t(b)];
+    if (bd.a < 0 || size_t(bd.a) >= nodes.size()) return false;
+    if (!same(&u[6 * size_t(bd.a)], &cache_.u[6 * size_t(bd.a)], 6 * sizeof(double))) return false;
+    if (bd.b >= 0 && (size_t(bd.b) >= nodes.size() ||
+                      !same(&u[6 * size_t(bd.b)], &cache_.u[6 * size_t(bd.b)], 6 * sizeof(double))))
+      return false;
+    return true;
+  }
+  struct LoadCache {
+    bool valid = false;
+    uint64_t generation = 0;
+    int64_t device_passes = 0;
+    std::vector<double> u;
+    std::vector<svxg_bond_load> loads;
+  };
   svxg_problem* p_ = nullptr;
-  std::vector<svxg_node> sent_nodes_;
-  std::vector<svxg_bond> sent_bonds_;
+  // (the device's copy of the graph is state behind const members too, as the reference's
+  // bond_load and extend_warm_start read the public members as they are)
+  mutable std::vector<svxg_node> sent_nodes_;
+  mutable std::vector<svxg_bond> sent_bonds_;
+  mutable uint64_t generation_ = 0;
+  mutable LoadCache cache_;
+  mutable std::string error_;
 };
 
 // SecAcc::finish + section_strengths(_general) of every interface (svxg_build_bonds): bond k of
@@ -258,7 +385,7 @@ inline std::vector<svxg_bond> build_bonds(const std::vector<svxg_node>& nodes, c
                                  int64_t(faces.size()), junctions.empty() ? nullptr : junctions.data(),
                                  int64_t(junctions.size()), lattices.empty() ? nullptr : lattices.data(),
                                  int32_t(lattices.size()), samples, mats.data(), out.data());
-  if (e < 0) throw std::runtime_error(std::string("svxg: ") + svxg_last_error());
+  if (e < 0) return {};  // (the message: svxg_last_error())
   return out;
 }
 

@@ -40,7 +40,8 @@ class Info(ctypes.Structure):
     _fields_ = [("nfree", c_i32), ("levels", c_i32), ("block_jacobi", c_i32), ("chol_n", c_i32),
                 ("level_sizes", c_i32 * 16), ("level_blocks", c_i64 * 32), ("matrix_blocks", c_i64),
                 ("work_per_iteration", c_i64), ("assembly_work", c_i64), ("work_per_apply", c_i64),
-                ("build_work", c_i64), ("device_bytes", c_i64), ("precision", c_i32), ("mixed_fallbacks", c_i32)]
+                ("build_work", c_i64), ("device_bytes", c_i64), ("precision", c_i32), ("mixed_fallbacks", c_i32),
+                ("graph_bytes", c_i64)]
 
     def sizes(self) -> list[int]:
         return [self.level_sizes[i] for i in range(self.levels)]

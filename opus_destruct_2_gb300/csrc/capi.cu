@@ -61,6 +61,7 @@ void release_solver(Problem& P) {
   P.mem.release(P.K.val);
   P.mem.release(P.K.val32);
   P.K = Bsr{};
+  P.mem.release(P.d_korder);
   P.mem.release(P.d_jinv);
   P.mem.release(P.d_dof);
   P.mem.release(P.d_chol);
@@ -294,6 +295,34 @@ int svxg_timer_read(svxg_problem* p, double* ms_total, int64_t* launches) {
   return SVXG_OK;
 }
 
+int svxg_time_spmv(svxg_problem* p, int32_t precision, int32_t reps, double* ms_per_launch) {
+  CHECK_P(p);
+  if (!ms_per_launch || reps <= 0) return SVXG_ERR_ARG;
+  Problem& P = p->P;
+  if (!P.assembled) {
+    set_error("svxg_time_spmv: not assembled");
+    return SVXG_ERR_STATE;
+  }
+  DeviceScope ds(P.device);
+  float ms = 0.0f;
+  if (precision == SVXG_PRECISION_FP64) {
+    TRY(time_cg_spmv(P, reps, &ms));
+  } else {
+    if (!P.K.val32) {
+      set_error("svxg_time_spmv: no FP32 copy of K (block-Jacobi problem)");
+      return SVXG_ERR_STATE;
+    }
+    TRY(time_cg_spmv32(P, reps, &ms));
+  }
+  *ms_per_launch = double(ms);
+  return SVXG_OK;
+}
+
+int svxg_measure_fp64_rate(int device, double* tflops) {
+  if (!tflops) return SVXG_ERR_ARG;
+  return measure_fp64_rate(device, tflops);
+}
+
 int svxg_device_count(void) {
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess) {
@@ -471,6 +500,7 @@ static int reassemble_impl(Problem& P, const svxg_node* nodes, int32_t n, const 
   P.mem.release(P.d_un);
   if (P.K.val32 && !P.lv.empty() && P.lv[0].A.val32 != P.K.val32) P.mem.release(P.K.val32);
   P.K = Bsr{};
+  P.mem.release(P.d_korder);
   P.assembled = false;
   P.pc_current = false;
   TRY(upload_graph(P, nodes, n, bonds, nb, mats));
@@ -909,6 +939,10 @@ int svxg_get_info(svxg_problem* p, svxg_info* info) {
   info->device_bytes = P.mem.bytes;
   info->precision = P.opt.precision;
   info->mixed_fallbacks = P.mixed_fallbacks;
+  if (P.have_graph)
+    info->graph_bytes = int64_t(sizeof(svxg_node)) * std::max<int64_t>(P.n, 1) +
+                        int64_t(sizeof(svxg_bond)) * std::max<int64_t>(P.nb, 1) +
+                        int64_t(sizeof(svxg_material)) * SVXG_MAX_MATERIALS;
   return SVXG_OK;
 }
 

@@ -227,6 +227,48 @@ __global__ void __launch_bounds__(kT) k_spmv32_dot(int32_t n, const int32_t* __r
   }
 }
 
+// the same product over K's rows sorted by length (solve.cu build_row_order; spmv_row.cuh
+// sorted_row_product): slot 5 w + g of warp w's row step is row order[slot]
+__global__ void __launch_bounds__(kT) k_spmv32_sorted_dot(int32_t n, const int32_t* __restrict__ order,
+                                                          const int32_t* __restrict__ rowptr,
+                                                          const int32_t* __restrict__ col,
+                                                          const float* __restrict__ val, const float* __restrict__ p,
+                                                          float* __restrict__ q, double* partials, unsigned* counter,
+                                                          MixedScalars* s) {
+  if (s->done) return;
+  const int lane = threadIdx.x & 31;
+  const int g = lane / 6, c = lane - 6 * g;
+  FF acc{0.0f, 0.0f};
+  for (int j = 0; j < kDotSteps; ++j) {
+    const int64_t base = (int64_t(blockIdx.x) * kDotSteps + j) * kRows * 5 + int64_t(threadIdx.x >> 5) * 5;
+    if (base >= n) break;  // (warp-uniform; the warp's slots only grow)
+    const int64_t slot = base + (g < 5 ? g : 4);
+    const bool row_ok = slot < n && g < 5;
+    const int32_t row = row_ok ? __ldg(order + slot) : 0;
+    const float y = sorted_row_product<float, float, float>(row_ok, row, rowptr, col, val, p);
+    if (row_ok) {
+      q[6 * int64_t(row) + c] = y;
+      dot2_add(acc, p[6 * int64_t(row) + c], y);
+    }
+  }
+  double tot;
+  if (reduce_last_ff(dot2_value(acc), 16, partials, counter, &tot) && threadIdx.x == 0) {
+    s->pq = tot;
+    s->iters += 1;
+    if (!(tot > 0)) {
+      s->breakdown = 1;
+      s->done = 1;
+    } else {
+      s->alpha = s->rz / tot;
+    }
+  }
+}
+
+inline unsigned spmv_sorted_blocks(int32_t n) {
+  const int64_t per = int64_t(kRows) * kDotSteps * 5;
+  return unsigned((std::max<int64_t>(n, 1) + per - 1) / per);
+}
+
 // d += alpha p, r -= alpha q (f32), ||r|| -> inner convergence
 __global__ void k_axpy32(int32_t nf, float* __restrict__ d, float* __restrict__ r, const float* __restrict__ p,
                          const float* __restrict__ q, double* partials, unsigned* counter, MixedScalars* s) {
@@ -333,7 +375,11 @@ int mixed_body(Problem& P) {
   float* q32 = d + 4 * m;
   MixedScalars* s = static_cast<MixedScalars*>(P.d_ms);
   if (P.timer_on) TRY(timer_mark(P));
-  if (P.sched_k32 == kGroupRow)
+  if (P.d_korder)
+    (k_spmv32_sorted_dot<<<spmv_sorted_blocks(nf), kT, 0, st>>>(nf, P.d_korder, P.K.rowptr, P.K.col, P.K.val32, p32,
+                                                                 q32, P.d_partials, P.d_counter, s),
+     SVXG_COUNT_LAUNCH());
+  else if (P.sched_k32 == kGroupRow)
     (k_spmv32_dot<kGroupRow><<<spmv_dot_blocks<kGroupRow>(nf), kT, 0, st>>>(nf, P.K.rowptr, P.K.col, P.K.val32, p32,
                                                                           q32, P.d_partials, P.d_counter, s),
      SVXG_COUNT_LAUNCH());
@@ -350,7 +396,69 @@ int mixed_body(Problem& P) {
   return SVXG_OK;
 }
 
+__global__ void k_fill_ones32(int32_t nf, float* x) {
+  const int64_t i = int64_t(blockIdx.x) * kT + threadIdx.x;
+  if (i < nf)
+    for (int c = 0; c < 6; ++c) x[6 * i + c] = 1.0f;
+}
+
 }  // namespace
+
+// The mixed sequence's SpMV timed alone (solve.cu's time_cg_spmv for K32): `reps` launches of
+// k_spmv32_dot, each doing its work (scratch scalars with done = 0), p = 1.
+int time_cg_spmv32(Problem& P, int32_t reps, float* ms_per_launch) {
+  *ms_per_launch = 0.0f;
+  if (P.nfree <= 0 || reps <= 0 || !P.K.val32 || !P.d_partials) return SVXG_OK;
+  const int32_t nf = P.nfree;
+  const size_t m = 6 * size_t(nf);
+  float *x = nullptr, *y = nullptr;
+  MixedScalars* s = nullptr;
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&x), m * sizeof(float), P.stream));
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&y), m * sizeof(float), P.stream));
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&s), sizeof(MixedScalars), P.stream));
+  SVXG_CUDA(cudaMemsetAsync(s, 0, sizeof(MixedScalars), P.stream));
+  (k_fill_ones32<<<vblk(nf), kT, 0, P.stream>>>(nf, x), SVXG_COUNT_LAUNCH());
+  auto launch = [&] {
+    if (P.d_korder)
+      (k_spmv32_sorted_dot<<<spmv_sorted_blocks(nf), kT, 0, P.stream>>>(nf, P.d_korder, P.K.rowptr, P.K.col,
+                                                                         P.K.val32, x, y, P.d_partials, P.d_counter,
+                                                                         s),
+       SVXG_COUNT_LAUNCH());
+    else if (P.sched_k32 == kGroupRow)
+      (k_spmv32_dot<kGroupRow><<<spmv_dot_blocks<kGroupRow>(nf), kT, 0, P.stream>>>(nf, P.K.rowptr, P.K.col,
+                                                                                    P.K.val32, x, y, P.d_partials,
+                                                                                    P.d_counter, s),
+       SVXG_COUNT_LAUNCH());
+    else
+      (k_spmv32_dot<kWarpRow><<<spmv_dot_blocks<kWarpRow>(nf), kT, 0, P.stream>>>(nf, P.K.rowptr, P.K.col, P.K.val32,
+                                                                                  x, y, P.d_partials, P.d_counter, s),
+       SVXG_COUNT_LAUNCH());
+  };
+  cudaEvent_t e0, e1;
+  SVXG_CUDA(cudaEventCreate(&e0));
+  SVXG_CUDA(cudaEventCreate(&e1));
+  launch();  // (warm-up)
+  SVXG_CUDA(cudaEventRecord(e0, P.stream));
+  for (int32_t r = 0; r < reps; ++r) launch();
+  SVXG_CUDA(cudaEventRecord(e1, P.stream));
+  int32_t done_iters = -1;
+  SVXG_CUDA(cudaMemcpyAsync(&done_iters, &s->iters, sizeof(int32_t), cudaMemcpyDeviceToHost, P.stream));
+  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  float ms = 0.0f;
+  SVXG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFreeAsync(x, P.stream);
+  cudaFreeAsync(y, P.stream);
+  cudaFreeAsync(s, P.stream);
+  SVXG_CUDA(cudaGetLastError());
+  if (done_iters != reps + 1) {
+    set_error("time_cg_spmv32: " + std::to_string(done_iters) + " of " + std::to_string(reps + 1) + " launches ran");
+    return SVXG_ERR_STATE;
+  }
+  *ms_per_launch = ms / float(reps);
+  return SVXG_OK;
+}
 
 int mixed_begin(Problem&) { return SVXG_OK; }
 
@@ -440,6 +548,7 @@ int mixed_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
       add_launches(per * std::max<int64_t>(1, hs->iters));
     } else {
       P.host_loops += 1;
+      const size_t timed0 = P.timer_used;
       int32_t queued = 0, batch = 2;
       for (;;) {
         SVXG_CUDA(cudaMemcpyAsync(hs, s, sizeof(MixedScalars), cudaMemcpyDeviceToHost, st));
@@ -451,6 +560,8 @@ int mixed_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
         queued += todo;
         batch = std::min(batch * 2, 32);
       }
+      // (the live timer keeps the SpMV launches that did work: the first `iters` of the sequence)
+      if (P.timer_on) P.timer_used = std::min(P.timer_used, timed0 + size_t(std::max(hs->iters, 0)));
     }
     used += hs->iters;
     (k_outer_update<<<vblk(nf), kT, 0, st>>>(nf, P.d_x, d), SVXG_COUNT_LAUNCH());

@@ -175,6 +175,7 @@ struct Problem {
   double id_scale = 1.0;
   double* d_jinv = nullptr;       // block-Jacobi inverses (36 per free node)
   int sched_k64 = 0, sched_k32 = 0;  // K's SpMV schedules (FP64 CG, FP32 inner), autotuned
+  int32_t* d_korder = nullptr;    // K's block rows by length (the CG products' sorted schedule), or null
   // multigrid
   std::vector<Level> lv;
   double* d_chol = nullptr;       // coarsest dense factor (m x m, lower = L, upper = L^T)
@@ -252,6 +253,9 @@ int gather_solution(Problem& P, double* u_nodes);                        // devi
 int precondition(Problem& P, const double* r, double* z);
 int free_run(Problem& P);
 int tune_k64(Problem& P);
+int time_cg_spmv(Problem& P, int32_t reps, float* ms_per_launch);    // solve.cu
+int time_cg_spmv32(Problem& P, int32_t reps, float* ms_per_launch);  // mixed.cu
+int measure_fp64_rate(int device, double* tflops);                    // tune.cu
 // tune.cu: the row schedule of a BSR operator (spmv_row.cuh), from the committed table (a pure
 // function of the operator's shape, so results never depend on timing); the timings are taken
 // and logged only when the environment asks (SVXG_TUNE_LOG=1; SVXG_TUNE_LIVE=1 also lets them
@@ -283,6 +287,9 @@ int utilization_device(Problem& P, const double* u_nodes, double fragility, doub
 // graphs.cu
 bool use_graphs();
 constexpr int32_t kGraphMinFree = 4096;
+// K of at least this many block rows gets its rows sorted by length for the conjugate-gradient
+// products (solve.cu build_row_order): one host round trip of K's row pointers at assembly.
+constexpr int32_t kSortedMinRows = 4096;
 // Mixed precision runs its FP32 inner sequences for problems of at least kMixedMinFree free nodes;
 // below that the products are latency-bound, FP32 saves nothing, and the FP32 Krylov vectors'
 // extra iterations and the restarts' host round trips cost more than they save, so the FP64

@@ -14,6 +14,7 @@
 // convergence costs only launches.
 #include <cmath>
 #include <cstdlib>
+#include <vector>
 
 #include "problem.cuh"
 #include "spmv_row.cuh"
@@ -177,9 +178,63 @@ __global__ void __launch_bounds__(kSpmvT) k_spmv_dot(int32_t n, const int32_t* _
   }
 }
 
+// The CG products of a K with its rows sorted by length (spmv_row.cuh sorted_row_product): slot
+// 5 w + g of warp w's row step is row order[slot]; kDotSteps row steps per warp before the block's
+// p.q reduction, as k_spmv_dot. With EPI == kPlain: y = K x alone.
+template <int EPI>
+__global__ void __launch_bounds__(kSpmvT) k_spmv_sorted(int32_t n, const int32_t* __restrict__ order,
+                                                        const int32_t* __restrict__ rowptr,
+                                                        const int32_t* __restrict__ col,
+                                                        const double* __restrict__ val, const double* __restrict__ x,
+                                                        double* __restrict__ y, double* partials, unsigned* counter,
+                                                        PcgScalars* s) {
+  __shared__ double sh[kSpmvT / 32];
+  if (EPI == kDotP && s->done) return;
+  const int lane = threadIdx.x & 31;
+  const int g = lane / 6, c = lane - 6 * g;
+  double dp = 0.0;
+  for (int j = 0; j < kDotSteps; ++j) {
+    const int64_t base = (int64_t(blockIdx.x) * kDotSteps + j) * kRowsPerBlock * 5 + int64_t(threadIdx.x >> 5) * 5;
+    if (base >= n) break;  // (warp-uniform; the warp's slots only grow)
+    const int64_t slot = base + (g < 5 ? g : 4);
+    const bool row_ok = slot < n && g < 5;
+    const int32_t row = row_ok ? __ldg(order + slot) : 0;
+    const double yr = sorted_row_product<double, double, double>(row_ok, row, rowptr, col, val, x);
+    if (row_ok) {
+      y[6 * int64_t(row) + c] = yr;
+      if (EPI == kDotP) dp = fma(x[6 * int64_t(row) + c], yr, dp);
+    }
+  }
+  if (EPI == kDotP) {
+    const double bs = block_sum<kSpmvT>(dp, sh);
+    if (publish<1>(&bs, partials, counter)) {
+      double tot;
+      gather_totals<kSpmvT, 1>(partials, counter, &tot, sh);
+      if (threadIdx.x == 0) {
+        s->pq = tot;
+        s->iters += 1;
+        if (!(tot > 0)) {
+          s->breakdown = 1;
+          s->done = 1;
+        } else {
+          s->alpha = s->rz / tot;
+        }
+      }
+    }
+  }
+}
+
 template <int EPI>
 void launch_spmv(cudaStream_t st, int sched, int32_t n, const int32_t* rowptr, const int32_t* col, const double* val,
-                 const double* x, double* y, double* partials, unsigned* counter, PcgScalars* s) {
+                 const double* x, double* y, double* partials, unsigned* counter, PcgScalars* s,
+                 const int32_t* order = nullptr) {
+  if (order) {
+    const int64_t per = int64_t(kRowsPerBlock) * kDotSteps * 5;
+    const unsigned g = unsigned((std::max<int64_t>(n, 1) + per - 1) / per);
+    (k_spmv_sorted<EPI><<<g, kSpmvT, 0, st>>>(n, order, rowptr, col, val, x, y, partials, counter, s),
+     SVXG_COUNT_LAUNCH());
+    return;
+  }
   if (EPI == kDotP) {
     const int per = kRowsPerBlock * kDotSteps * (sched == kGroupRow ? 5 : 1);
     const unsigned g = unsigned((std::max(n, 1) + per - 1) / per);
@@ -400,6 +455,12 @@ __global__ void k_jacobi_apply(int32_t nfree, const double* __restrict__ jinv, c
   }
 }
 
+__global__ void k_fill_ones(int32_t nfree, double* x) {
+  const int32_t i = blockIdx.x * kVecT + threadIdx.x;
+  if (i < nfree)
+    for (int c = 0; c < 6; ++c) x[6 * int64_t(i) + c] = 1.0;
+}
+
 // node order <-> free-DOF order
 __global__ void k_scatter_free(int32_t n, const int32_t* dof, const double* nodes6, double* free6) {
   const int32_t i = blockIdx.x * kVecT + threadIdx.x;
@@ -463,14 +524,38 @@ int ensure_run(Problem& P) {
 int spmv(Problem& P, const Bsr& A, const double* x, double* y) {
   if (A.n == 0) return SVXG_OK;
   launch_spmv<kPlain>(P.stream, &A == &P.K ? P.sched_k64 : 0, A.n, A.rowptr, A.col, A.val, x, y, nullptr, nullptr,
-                      nullptr);
+                      nullptr, &A == &P.K ? P.d_korder : nullptr);
   SVXG_CUDA(cudaGetLastError());
   return SVXG_OK;
 }
 
 // K's FP64 SpMV schedule from the table; with tune timing on, y = K x is also timed with both
 // (a warm-up launch each, then three) and logged
+// K's block rows in order of length (a stable counting sort; lengths of 63 blocks and more share
+// the last class), for the sorted schedule of the CG products; K of fewer than kSortedMinRows rows
+// keeps the table's schedules. The permutation depends on K's pattern only, so the products' bits
+// stay a fixed function of the operator.
+int build_row_order(Problem& P) {
+  P.mem.release(P.d_korder);
+  const int32_t n = P.nfree;
+  if (n < kSortedMinRows || !P.K.rowptr) return SVXG_OK;
+  std::vector<int32_t> rp(size_t(n) + 1), ord(static_cast<size_t>(n));
+  SVXG_CUDA(cudaMemcpyAsync(rp.data(), P.K.rowptr, sizeof(int32_t) * (size_t(n) + 1), cudaMemcpyDeviceToHost,
+                            P.stream));
+  SVXG_CUDA(host_wait(P.stream));
+  constexpr int kClasses = 64;
+  int64_t start[kClasses + 1] = {};
+  for (int32_t i = 0; i < n; ++i) ++start[std::min(rp[size_t(i) + 1] - rp[size_t(i)], kClasses - 1) + 1];
+  for (int k = 0; k < kClasses; ++k) start[k + 1] += start[k];
+  for (int32_t i = 0; i < n; ++i) ord[size_t(start[std::min(rp[size_t(i) + 1] - rp[size_t(i)], kClasses - 1)]++)] = i;
+  TRY(P.mem.alloc(&P.d_korder, size_t(n)));
+  SVXG_CUDA(cudaMemcpyAsync(P.d_korder, ord.data(), sizeof(int32_t) * size_t(n), cudaMemcpyHostToDevice, P.stream));
+  SVXG_CUDA(host_wait(P.stream));  // (ord is freed on return)
+  return SVXG_OK;
+}
+
 int tune_k64(Problem& P) {
+  TRY(build_row_order(P));
   P.sched_k64 = table_sched(kOpK64, P.nfree, P.K.nnzb);
   if (P.nfree <= 0 || !tune_timing()) return SVXG_OK;
   const size_t m = 6 * size_t(P.nfree);
@@ -497,6 +582,53 @@ int tune_k64(Problem& P) {
   cudaFreeAsync(y, P.stream);
   P.sched_k64 = tune_decide(P, kOpK64, 0, P.nfree, P.K.nnzb, ms[0], ms[1]);
   SVXG_CUDA(cudaGetLastError());
+  return SVXG_OK;
+}
+
+// A dedicated timing loop of the conjugate-gradient SpMV: `reps` launches of the kernel an
+// iteration runs (q = K p with p.q fused, alpha on the device), each one doing its work (scratch
+// scalars with done = 0, so none returns early), on K with p = 1; CUDA events on the problem's
+// stream around the loop. The run state of the problem is untouched (scratch vectors and scalars).
+int time_cg_spmv(Problem& P, int32_t reps, float* ms_per_launch) {
+  *ms_per_launch = 0.0f;
+  if (P.nfree <= 0 || reps <= 0 || !P.K.val) return SVXG_OK;
+  TRY(ensure_run(P));
+  const size_t m = 6 * size_t(P.nfree);
+  double *x = nullptr, *y = nullptr;
+  PcgScalars* s = nullptr;
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&x), m * sizeof(double), P.stream));
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&y), m * sizeof(double), P.stream));
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&s), sizeof(PcgScalars), P.stream));
+  SVXG_CUDA(cudaMemsetAsync(s, 0, sizeof(PcgScalars), P.stream));
+  (k_fill_ones<<<vec_blocks(P.nfree), kVecT, 0, P.stream>>>(P.nfree, x), SVXG_COUNT_LAUNCH());
+  cudaEvent_t e0, e1;
+  SVXG_CUDA(cudaEventCreate(&e0));
+  SVXG_CUDA(cudaEventCreate(&e1));
+  launch_spmv<kDotP>(P.stream, P.sched_k64, P.nfree, P.K.rowptr, P.K.col, P.K.val, x, y, P.d_partials, P.d_counter,
+                     s, P.d_korder);  // (warm-up)
+  SVXG_CUDA(cudaEventRecord(e0, P.stream));
+  for (int32_t r = 0; r < reps; ++r)
+    launch_spmv<kDotP>(P.stream, P.sched_k64, P.nfree, P.K.rowptr, P.K.col, P.K.val, x, y, P.d_partials,
+                       P.d_counter, s, P.d_korder);
+  SVXG_CUDA(cudaEventRecord(e1, P.stream));
+  int32_t done_iters = -1;
+  SVXG_CUDA(cudaMemcpyAsync(&done_iters, &s->iters, sizeof(int32_t), cudaMemcpyDeviceToHost, P.stream));
+  SVXG_CUDA(cudaEventSynchronize(e1));
+  SVXG_CUDA(cudaStreamSynchronize(P.stream));
+  float ms = 0.0f;
+  SVXG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFreeAsync(x, P.stream);
+  cudaFreeAsync(y, P.stream);
+  cudaFreeAsync(s, P.stream);
+  SVXG_CUDA(cudaGetLastError());
+  if (done_iters != reps + 1) {
+    // (a launch returned early: p.q <= 0 stopped the scalars - no time is reported)
+    set_error("time_cg_spmv: " + std::to_string(done_iters) + " of " + std::to_string(reps + 1) + " launches ran");
+    return SVXG_ERR_STATE;
+  }
+  *ms_per_launch = ms / float(reps);
   return SVXG_OK;
 }
 
@@ -681,7 +813,7 @@ int plain_body(Problem& P) {
   cudaStream_t st = P.stream;
   if (P.timer_on) TRY(timer_mark(P));
   launch_spmv<kDotP>(st, P.sched_k64, nf, P.K.rowptr, P.K.col, P.K.val, P.d_p, P.d_q, P.d_partials, P.d_counter,
-                     P.d_s);
+                     P.d_s, P.d_korder);
   if (P.timer_on) TRY(timer_mark(P, true));
   (k_axpy_rr<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_x, P.d_r, P.d_p, P.d_q, P.d_partials, P.d_counter, P.d_s),
    SVXG_COUNT_LAUNCH());
@@ -775,6 +907,7 @@ int plain_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
     add_launches(per * std::max<int64_t>(1, P.h_s->iters));
   } else {
     P.host_loops += 1;
+    const size_t timed0 = P.timer_used;
     int32_t queued = 0;
     int32_t batch = 2;
     for (;;) {
@@ -786,6 +919,9 @@ int plain_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
       queued += todo;
       batch = std::min(batch * 2, 32);
     }
+    // the live timer keeps the SpMV launches that did work: the first `iters` of this call (the
+    // bodies queued past convergence return at once and are not SpMV launches)
+    if (P.timer_on) P.timer_used = std::min(P.timer_used, timed0 + size_t(std::max(P.h_s->iters, 0)));
   }
   P.cycle_stop = nullptr;
   out.iters = P.h_s->iters;

@@ -129,6 +129,63 @@ __device__ __forceinline__ A sched_row_product(bool row_ok, int32_t row, const i
   return acc;
 }
 
+// The sorted schedule of the conjugate-gradient products: five block rows per warp, taken in the
+// order of a permutation of the rows by length (built once per K, solve.cu build_row_order), so the
+// warp's five lane groups run rows of one length and none idles behind a longer row. Lane 6g + c
+// (g < 5) sums row c of its row's blocks as FMA chains (alternate blocks in two chains): six FMAs
+// a block, the fewest an FP64-issue-bound product can issue. Lanes 30 and 31 hold no row.
+template <typename V, typename X, typename A>
+__device__ __forceinline__ A sorted_row_product(bool row_ok, int32_t row, const int32_t* __restrict__ rowptr,
+                                                const int32_t* __restrict__ col, const V* __restrict__ val,
+                                                const X* __restrict__ x) {
+  using MV = typename Vec2<V>::T;
+  using XV = typename Vec2<X>::T;
+  const int lane = threadIdx.x & 31;
+  const int g = lane / 6, c = lane - 6 * g;
+  A acc0 = A(0), acc1 = A(0);
+  if (row_ok && g < 5) {
+    const int32_t k1 = __ldg(rowptr + row + 1);
+    int32_t k = __ldg(rowptr + row);
+    for (; k + 1 < k1; k += 2) {
+      const int32_t ca = __ldg(col + k), cb = __ldg(col + k + 1);
+      const MV* ma = reinterpret_cast<const MV*>(val + 36 * int64_t(k) + 6 * c);
+      const MV* mb = reinterpret_cast<const MV*>(val + 36 * int64_t(k + 1) + 6 * c);
+      const XV* xa = reinterpret_cast<const XV*>(x + 6 * int64_t(ca));
+      const XV* xb = reinterpret_cast<const XV*>(x + 6 * int64_t(cb));
+      const MV a0 = __ldg(ma), a1 = __ldg(ma + 1), a2 = __ldg(ma + 2);
+      const MV b0 = __ldg(mb), b1 = __ldg(mb + 1), b2 = __ldg(mb + 2);
+      const XV u0 = __ldg(xa), u1 = __ldg(xa + 1), u2 = __ldg(xa + 2);
+      const XV v0 = __ldg(xb), v1 = __ldg(xb + 1), v2 = __ldg(xb + 2);
+      acc0 = fma(A(a0.x), A(u0.x), acc0);
+      acc1 = fma(A(b0.x), A(v0.x), acc1);
+      acc0 = fma(A(a0.y), A(u0.y), acc0);
+      acc1 = fma(A(b0.y), A(v0.y), acc1);
+      acc0 = fma(A(a1.x), A(u1.x), acc0);
+      acc1 = fma(A(b1.x), A(v1.x), acc1);
+      acc0 = fma(A(a1.y), A(u1.y), acc0);
+      acc1 = fma(A(b1.y), A(v1.y), acc1);
+      acc0 = fma(A(a2.x), A(u2.x), acc0);
+      acc1 = fma(A(b2.x), A(v2.x), acc1);
+      acc0 = fma(A(a2.y), A(u2.y), acc0);
+      acc1 = fma(A(b2.y), A(v2.y), acc1);
+    }
+    if (k < k1) {
+      const int32_t ca = __ldg(col + k);
+      const MV* ma = reinterpret_cast<const MV*>(val + 36 * int64_t(k) + 6 * c);
+      const XV* xa = reinterpret_cast<const XV*>(x + 6 * int64_t(ca));
+      const MV a0 = __ldg(ma), a1 = __ldg(ma + 1), a2 = __ldg(ma + 2);
+      const XV u0 = __ldg(xa), u1 = __ldg(xa + 1), u2 = __ldg(xa + 2);
+      acc0 = fma(A(a0.x), A(u0.x), acc0);
+      acc0 = fma(A(a0.y), A(u0.y), acc0);
+      acc0 = fma(A(a1.x), A(u1.x), acc0);
+      acc0 = fma(A(a1.y), A(u1.y), acc0);
+      acc0 = fma(A(a2.x), A(u2.x), acc0);
+      acc0 = fma(A(a2.y), A(u2.y), acc0);
+    }
+  }
+  return acc0 + acc1;
+}
+
 // component q of the row's 6-vector v (held by the row's lanes) - whole warp must call
 template <int SCHED, typename T>
 __device__ __forceinline__ T row_component(T v, int q) {

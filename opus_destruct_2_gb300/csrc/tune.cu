@@ -68,5 +68,56 @@ int tune_decide(Problem& P, int kind, int level, int64_t rows, int64_t blocks, f
   return table_sched(kind, rows, blocks);
 }
 
+// FP64 throughput of this GPU: every thread runs kChains independent FMA chains (enough in flight
+// to cover the pipe's latency at 8 warps a scheduler), the grid a multiple of the SM count. The
+// chains' values are written only when a flag no caller sets is on, so nothing is optimized away.
+namespace {
+constexpr int kChains = 16;
+__global__ void __launch_bounds__(256) k_dfma_rate(int32_t iters, double m, double c, int32_t write, double* out) {
+  double a[kChains];
+#pragma unroll
+  for (int k = 0; k < kChains; ++k) a[k] = 1e-3 * double(threadIdx.x + k);
+  for (int32_t i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < kChains; ++k) a[k] = fma(a[k], m, c);
+  }
+  double t = 0.0;
+#pragma unroll
+  for (int k = 0; k < kChains; ++k) t += a[k];
+  if (write) out[blockIdx.x * blockDim.x + threadIdx.x] = t;
+}
+}  // namespace
+
+int measure_fp64_rate(int device, double* tflops) {
+  *tflops = 0.0;
+  int sms = 0;
+  SVXG_CUDA(cudaSetDevice(device));
+  SVXG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  const unsigned blocks = unsigned(sms) * 8u;
+  const int32_t iters = 4096;
+  cudaStream_t st;
+  SVXG_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  cudaEvent_t e0, e1;
+  SVXG_CUDA(cudaEventCreate(&e0));
+  SVXG_CUDA(cudaEventCreate(&e1));
+  float best = 0.0f;
+  for (int r = 0; r < 6; ++r) {
+    SVXG_CUDA(cudaEventRecord(e0, st));
+    (k_dfma_rate<<<blocks, 256, 0, st>>>(iters, 0.999999, 1e-9, 0, nullptr), SVXG_COUNT_LAUNCH());
+    SVXG_CUDA(cudaEventRecord(e1, st));
+    SVXG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    SVXG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    if (r > 0 && (best == 0.0f || ms < best)) best = ms;  // (the first launch warms up)
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaStreamDestroy(st);
+  SVXG_CUDA(cudaGetLastError());
+  const double flops = 2.0 * kChains * double(iters) * double(blocks) * 256.0;
+  *tflops = best > 0.0f ? flops / (double(best) * 1e-3) / 1e12 : 0.0;
+  return SVXG_OK;
+}
+
 }  // namespace svxg
 

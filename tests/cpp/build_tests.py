@@ -16,7 +16,8 @@ def build() -> str:
     if os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(p) for p in (src, hdr, lib)):
         return out
     os.makedirs(os.path.dirname(out), exist_ok=True)
-    cmd = ["g++", "-std=c++20", "-O2", "-I", os.path.join(ROOT, "include"), src, "-o", out, "-L", LIBDIR, "-lsvxg",
+    # (the reference's own host flags: no exceptions, no RTTI - the adapter must build under them)
+    cmd = ["g++", "-std=c++20", "-O2", "-fno-exceptions", "-fno-rtti", "-I", os.path.join(ROOT, "include"), src, "-o", out, "-L", LIBDIR, "-lsvxg",
            f"-Wl,-rpath,{LIBDIR}"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode:

@@ -1,5 +1,6 @@
 // test_adapter.cpp - the C++20 host class (include/svxg_stress_problem.hpp) on the device, with the
 // reference's own test cases written as the reference writes them (tests/core/test_stress.cpp).
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -71,6 +72,34 @@ std::vector<double> gravity(const svxg::StressProblem& P) {
   std::vector<double> f(6 * P.nodes.size(), 0.0);
   for (size_t i = 0; i < P.nodes.size(); ++i) f[6 * i + 2] = -9.81 * P.nodes[i].mass;
   return f;
+}
+
+// a grid of nx x ny x nz unit cells (0.5 m), face bonds between neighbours, supports under z = 0
+void lattice(svxg::StressProblem& P, int nx, int ny, int nz) {
+  P.mats = materials();
+  const double h = 0.5;
+  auto id = [&](int x, int y, int z) { return int32_t((z * ny + y) * nx + x); };
+  for (int z = 0; z < nz; ++z)
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nx; ++x) {
+        svxg_node nd{};
+        nd.c = {(x + 0.5) * h, (y + 0.5) * h, (z + 0.5) * h};
+        nd.mass = 300.0;
+        P.nodes.push_back(nd);
+      }
+  for (int z = 0; z < nz; ++z)
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nx; ++x) {
+        const svxg_v3 c = P.nodes[size_t(id(x, y, z))].c;
+        if (z == 0) P.bonds.push_back(bond(P, id(x, y, z), -1, {0, 0, -1}, {c.x, c.y, 0.0}, h));
+        if (x + 1 < nx) P.bonds.push_back(bond(P, id(x, y, z), id(x + 1, y, z), {1, 0, 0}, {c.x + 0.5 * h, c.y, c.z}, h));
+        if (y + 1 < ny) P.bonds.push_back(bond(P, id(x, y, z), id(x, y + 1, z), {0, 1, 0}, {c.x, c.y + 0.5 * h, c.z}, h));
+        if (z + 1 < nz) P.bonds.push_back(bond(P, id(x, y, z), id(x, y, z + 1), {0, 0, 1}, {c.x, c.y, c.z + 0.5 * h}, h));
+      }
+}
+
+bool same_load(const svxg_bond_load& a, const svxg_bond_load& b) {
+  return a.N == b.N && a.V1 == b.V1 && a.V2 == b.V2 && a.T == b.T && a.M1 == b.M1 && a.M2 == b.M2;
 }
 
 double shear(const svxg_bond_load& L) { return std::sqrt(L.V1 * L.V1 + L.V2 * L.V2); }
@@ -217,6 +246,58 @@ int main() {
     const auto b = svxg::build_bonds(nodes, {sec}, {fc}, materials());
     CHECK(b.size() == 1 && b[0].n.x == 1.0 && b[0].area == 0.25 && b[0].la == 0.25 && b[0].lb == 0.25);
     CHECK(b[0].sectioned == 1 && b[0].faces == 1);
+  }
+  {
+    // the reference's callers ask bond_load bond by bond at one u (world.cpp:1174, :1927): over a
+    // graph of about 10k bonds that is one device pass for the whole loop, the same numbers as the
+    // every-bond pass, and a changed u at a bond's ends makes a new pass
+    svxg::StressProblem P;
+    lattice(P, 24, 24, 6);
+    CHECK(P.bonds.size() > 10000);
+    CHECK(P.assemble());
+    std::vector<double> u;
+    CHECK(P.solve(gravity(P), u, 1e-8, 500, false).converged);
+    const auto all = P.bond_loads(u);
+    CHECK(all.size() == P.bonds.size());
+    const auto t0 = std::chrono::steady_clock::now();
+    double sum = 0.0;
+    bool equal = true;
+    for (int32_t b = 0; b < int32_t(P.bonds.size()); ++b) {
+      const svxg_bond_load L = P.bond_load(b, u);
+      sum += std::fabs(L.N);
+      equal = equal && same_load(L, all[size_t(b)]);
+    }
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    CHECK(equal);
+    CHECK(P.bond_load_passes() == 1);
+    std::printf("bond_load loop: %zu bonds, %lld device pass(es), %.3f ms (sum |N| %.6g)\n", P.bonds.size(),
+                (long long)P.bond_load_passes(), ms, sum);
+    std::vector<double> u2 = u;
+    const svxg_bond& b0 = P.bonds[0];
+    u2[6 * size_t(b0.a) + 2] *= 2.0;
+    (void)P.bond_load(0, u2);
+    CHECK(P.bond_load_passes() == 2);
+    CHECK(same_load(P.bond_load(0, u2), P.bond_loads(u2)[0]));
+    // stress.hpp:116-117: the solver's bytes are what release() frees; the graph stays
+    const int64_t held = P.memory_bytes(), used = P.memory_bytes(svxg::Bytes::Used), solver = P.solver_bytes();
+    CHECK(solver > 0 && solver < held && used <= held);
+    P.release();
+    CHECK(P.solver_bytes() < solver);
+    CHECK(!P.assembled());
+  }
+  {
+    // the reference's error contract (no exceptions): a wrong-sized load is no answer
+    svxg::StressProblem P;
+    cantilever(P, 6, 0.5, 100.0);
+    CHECK(P.assemble());
+    std::vector<double> u, f(5, 0.0);
+    const svxg_pcg_result r = P.solve(f, u, 1e-9, 100, false);
+    CHECK(r.breakdown && !r.converged && std::isinf(r.rel_res));
+    CHECK(!P.error().empty());
+    svxg::StressProblem Q;
+    cantilever(Q, 4, 0.5, 100.0);
+    Q.mats.resize(3);  // (an incomplete material table: assemble refuses, nothing throws)
+    CHECK(!Q.assemble());
   }
   std::printf(failures ? "%d failures\n" : "ok\n", failures);
   return failures ? 1 : 0;

@@ -99,6 +99,32 @@ def test_noalloc_matches_existing_judge_on_two_calls_in_a_row():
         assert np.array_equal(over, np.nonzero(phi0 >= 1.0)[0])
 
 
+def test_noalloc_matches_existing_judge_above_a_thousand_blocks():
+    """More than 262,144 bonds: the scan of the per-block counts then gives each of its threads
+    several blocks. Any displacement will do for the judge's arithmetic: a seeded random one, at a
+    fragility that puts about half the bonds over strength."""
+    import torch
+    nodes, bonds = fx.lattice(45)
+    assert len(bonds) > 262_144
+    G = StressProblem(nodes, bonds, MATS)
+    assert G.assemble(StressOptions(amg_min_nodes=1 << 30))
+    rng = np.random.default_rng(17)
+    u = 1e-4 * rng.standard_normal(6 * len(nodes))
+    u[np.repeat(nodes["fixed"] != 0, 6)] = 0.0
+    G.begin(fx.gravity_live(nodes), u)
+    G.iterate(0, 1e-30)
+    phi1, _, _ = existing_judge(G, 1.0)
+    frag = 1.0 / float(np.median(phi1[phi1 > 0]))
+    phi0, mode0, over0 = existing_judge(G, frag)
+    assert 0.3 * len(bonds) < len(over0) < 0.7 * len(bonds)
+    buf = CallerBuffers(nodes, bonds, G.current())
+    for _ in range(2):
+        phi, mode, over = buf.call(frag)
+        torch.cuda.synchronize()
+        assert np.array_equal(phi, phi0) and np.array_equal(mode, mode0)
+        assert np.array_equal(over, over0)
+
+
 def test_noalloc_rejects_sizes_beyond_its_maximum():
     f = noalloc_fn()
     n_over = c_i32(-1)
@@ -112,6 +138,7 @@ def test_noalloc_reports_out_of_range_bonds():
     bad = bonds.copy()
     bad["b"][3] = len(nodes)          # a node index past the end
     bad["ma"][5] = 200                # a material id past the table
+    bad["a"][7] = -1                  # a node index below the start
     buf = CallerBuffers(nodes, bad, np.zeros(6 * len(nodes)))
     n_over = c_i32(-1)
     import torch
@@ -121,4 +148,4 @@ def test_noalloc_reports_out_of_range_bonds():
     assert e == -1 and b"out of range" in load_library().svxg_last_error()
     # the valid bonds are still judged (u = 0: phi = 0)
     phi = buf.phi.cpu().numpy()
-    assert phi[3] == -1.0 and phi[5] == -1.0 and np.all(phi[[0, 1, 2, 4]] == 0.0)
+    assert phi[3] == -1.0 and phi[5] == -1.0 and phi[7] == -1.0 and np.all(phi[[0, 1, 2, 4, 6]] == 0.0)
