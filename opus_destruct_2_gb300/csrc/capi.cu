@@ -61,7 +61,7 @@ void release_solver(Problem& P) {
   P.mem.release(P.K.val);
   P.mem.release(P.K.val32);
   P.K = Bsr{};
-  P.mem.release(P.d_korder);
+  P.mem.release(P.d_kslots);
   P.mem.release(P.d_jinv);
   P.mem.release(P.d_dof);
   P.mem.release(P.d_chol);
@@ -500,7 +500,7 @@ static int reassemble_impl(Problem& P, const svxg_node* nodes, int32_t n, const 
   P.mem.release(P.d_un);
   if (P.K.val32 && !P.lv.empty() && P.lv[0].A.val32 != P.K.val32) P.mem.release(P.K.val32);
   P.K = Bsr{};
-  P.mem.release(P.d_korder);
+  P.mem.release(P.d_kslots);
   P.assembled = false;
   P.pc_current = false;
   TRY(upload_graph(P, nodes, n, bonds, nb, mats));

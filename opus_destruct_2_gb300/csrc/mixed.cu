@@ -227,48 +227,6 @@ __global__ void __launch_bounds__(kT) k_spmv32_dot(int32_t n, const int32_t* __r
   }
 }
 
-// the same product over K's rows sorted by length (solve.cu build_row_order; spmv_row.cuh
-// sorted_row_product): slot 5 w + g of warp w's row step is row order[slot]
-__global__ void __launch_bounds__(kT) k_spmv32_sorted_dot(int32_t n, const int32_t* __restrict__ order,
-                                                          const int32_t* __restrict__ rowptr,
-                                                          const int32_t* __restrict__ col,
-                                                          const float* __restrict__ val, const float* __restrict__ p,
-                                                          float* __restrict__ q, double* partials, unsigned* counter,
-                                                          MixedScalars* s) {
-  if (s->done) return;
-  const int lane = threadIdx.x & 31;
-  const int g = lane / 6, c = lane - 6 * g;
-  FF acc{0.0f, 0.0f};
-  for (int j = 0; j < kDotSteps; ++j) {
-    const int64_t base = (int64_t(blockIdx.x) * kDotSteps + j) * kRows * 5 + int64_t(threadIdx.x >> 5) * 5;
-    if (base >= n) break;  // (warp-uniform; the warp's slots only grow)
-    const int64_t slot = base + (g < 5 ? g : 4);
-    const bool row_ok = slot < n && g < 5;
-    const int32_t row = row_ok ? __ldg(order + slot) : 0;
-    const float y = sorted_row_product<float, float, float>(row_ok, row, rowptr, col, val, p);
-    if (row_ok) {
-      q[6 * int64_t(row) + c] = y;
-      dot2_add(acc, p[6 * int64_t(row) + c], y);
-    }
-  }
-  double tot;
-  if (reduce_last_ff(dot2_value(acc), 16, partials, counter, &tot) && threadIdx.x == 0) {
-    s->pq = tot;
-    s->iters += 1;
-    if (!(tot > 0)) {
-      s->breakdown = 1;
-      s->done = 1;
-    } else {
-      s->alpha = s->rz / tot;
-    }
-  }
-}
-
-inline unsigned spmv_sorted_blocks(int32_t n) {
-  const int64_t per = int64_t(kRows) * kDotSteps * 5;
-  return unsigned((std::max<int64_t>(n, 1) + per - 1) / per);
-}
-
 // d += alpha p, r -= alpha q (f32), ||r|| -> inner convergence
 __global__ void k_axpy32(int32_t nf, float* __restrict__ d, float* __restrict__ r, const float* __restrict__ p,
                          const float* __restrict__ q, double* partials, unsigned* counter, MixedScalars* s) {
@@ -375,11 +333,7 @@ int mixed_body(Problem& P) {
   float* q32 = d + 4 * m;
   MixedScalars* s = static_cast<MixedScalars*>(P.d_ms);
   if (P.timer_on) TRY(timer_mark(P));
-  if (P.d_korder)
-    (k_spmv32_sorted_dot<<<spmv_sorted_blocks(nf), kT, 0, st>>>(nf, P.d_korder, P.K.rowptr, P.K.col, P.K.val32, p32,
-                                                                 q32, P.d_partials, P.d_counter, s),
-     SVXG_COUNT_LAUNCH());
-  else if (P.sched_k32 == kGroupRow)
+  if (P.sched_k32 == kGroupRow)
     (k_spmv32_dot<kGroupRow><<<spmv_dot_blocks<kGroupRow>(nf), kT, 0, st>>>(nf, P.K.rowptr, P.K.col, P.K.val32, p32,
                                                                           q32, P.d_partials, P.d_counter, s),
      SVXG_COUNT_LAUNCH());
@@ -419,12 +373,7 @@ int time_cg_spmv32(Problem& P, int32_t reps, float* ms_per_launch) {
   SVXG_CUDA(cudaMemsetAsync(s, 0, sizeof(MixedScalars), P.stream));
   (k_fill_ones32<<<vblk(nf), kT, 0, P.stream>>>(nf, x), SVXG_COUNT_LAUNCH());
   auto launch = [&] {
-    if (P.d_korder)
-      (k_spmv32_sorted_dot<<<spmv_sorted_blocks(nf), kT, 0, P.stream>>>(nf, P.d_korder, P.K.rowptr, P.K.col,
-                                                                         P.K.val32, x, y, P.d_partials, P.d_counter,
-                                                                         s),
-       SVXG_COUNT_LAUNCH());
-    else if (P.sched_k32 == kGroupRow)
+    if (P.sched_k32 == kGroupRow)
       (k_spmv32_dot<kGroupRow><<<spmv_dot_blocks<kGroupRow>(nf), kT, 0, P.stream>>>(nf, P.K.rowptr, P.K.col,
                                                                                     P.K.val32, x, y, P.d_partials,
                                                                                     P.d_counter, s),

@@ -175,7 +175,7 @@ struct Problem {
   double id_scale = 1.0;
   double* d_jinv = nullptr;       // block-Jacobi inverses (36 per free node)
   int sched_k64 = 0, sched_k32 = 0;  // K's SpMV schedules (FP64 CG, FP32 inner), autotuned
-  int32_t* d_korder = nullptr;    // K's block rows by length (the CG products' sorted schedule), or null
+  int4* d_kslots = nullptr;       // K's block rows by length as slots (the FP64 CG products' schedule), or null
   // multigrid
   std::vector<Level> lv;
   double* d_chol = nullptr;       // coarsest dense factor (m x m, lower = L, upper = L^T)
@@ -288,8 +288,11 @@ int utilization_device(Problem& P, const double* u_nodes, double fragility, doub
 bool use_graphs();
 constexpr int32_t kGraphMinFree = 4096;
 // K of at least this many block rows gets its rows sorted by length for the conjugate-gradient
-// products (solve.cu build_row_order): one host round trip of K's row pointers at assembly.
-constexpr int32_t kSortedMinRows = 4096;
+// products (solve.cu build_row_slots): one host round trip of K's row pointers at assembly.
+#ifndef SVXG_SORTED_MIN_ROWS
+#define SVXG_SORTED_MIN_ROWS 4096
+#endif
+constexpr int32_t kSortedMinRows = SVXG_SORTED_MIN_ROWS;
 // Mixed precision runs its FP32 inner sequences for problems of at least kMixedMinFree free nodes;
 // below that the products are latency-bound, FP32 saves nothing, and the FP32 Krylov vectors'
 // extra iterations and the restarts' host round trips cost more than they save, so the FP64

@@ -178,33 +178,40 @@ __global__ void __launch_bounds__(kSpmvT) k_spmv_dot(int32_t n, const int32_t* _
   }
 }
 
-// The CG products of a K with its rows sorted by length (spmv_row.cuh sorted_row_product): slot
-// 5 w + g of warp w's row step is row order[slot]; kDotSteps row steps per warp before the block's
-// p.q reduction, as k_spmv_dot. With EPI == kPlain: y = K x alone.
+// The CG products over K's row slots (spmv_row.cuh slot_rows_product): warp w of the grid takes
+// slots [5 kSlotRows w, 5 kSlotRows (w + 1)), kSlotRows rows a lane group. With EPI == kPlain:
+// y = K x alone; kDotP adds p.q, alpha and the breakdown test as k_spmv_dot. (kSlotRows 2 at three
+// blocks an SM measured fastest on the city block's K: 109 us, against 112-175 us for 1, 3 and 4
+// rows at the occupancies their registers allow, and 126 us for the table schedules.)
+#ifndef SVXG_SLOT_ROWS
+#define SVXG_SLOT_ROWS 2
+#endif
+#ifndef SVXG_SLOT_MINBLOCKS
+#define SVXG_SLOT_MINBLOCKS 3
+#endif
+constexpr int kSlotRows = SVXG_SLOT_ROWS;
 template <int EPI>
-__global__ void __launch_bounds__(kSpmvT) k_spmv_sorted(int32_t n, const int32_t* __restrict__ order,
-                                                        const int32_t* __restrict__ rowptr,
-                                                        const int32_t* __restrict__ col,
-                                                        const double* __restrict__ val, const double* __restrict__ x,
-                                                        double* __restrict__ y, double* partials, unsigned* counter,
-                                                        PcgScalars* s) {
+__global__ void __launch_bounds__(kSpmvT, SVXG_SLOT_MINBLOCKS) k_spmv_slots(int32_t n, const int4* __restrict__ slots,
+                                                                           const int32_t* __restrict__ col,
+                                                                           const double* __restrict__ val,
+                                                                           const double* __restrict__ x,
+                                                                           double* __restrict__ y, double* partials,
+                                                                           unsigned* counter, PcgScalars* s) {
   __shared__ double sh[kSpmvT / 32];
   if (EPI == kDotP && s->done) return;
-  const int lane = threadIdx.x & 31;
-  const int g = lane / 6, c = lane - 6 * g;
+  const int c = (threadIdx.x & 31) % 6;
+  const int64_t first = (int64_t(blockIdx.x) * kRowsPerBlock + (threadIdx.x >> 5)) * (5 * kSlotRows);
+  int32_t row[kSlotRows];
+  bool ok[kSlotRows];
+  double yr[kSlotRows];
+  slot_rows_product<kSlotRows, double, double, double>(slots, first, n, col, val, x, row, ok, yr);
   double dp = 0.0;
-  for (int j = 0; j < kDotSteps; ++j) {
-    const int64_t base = (int64_t(blockIdx.x) * kDotSteps + j) * kRowsPerBlock * 5 + int64_t(threadIdx.x >> 5) * 5;
-    if (base >= n) break;  // (warp-uniform; the warp's slots only grow)
-    const int64_t slot = base + (g < 5 ? g : 4);
-    const bool row_ok = slot < n && g < 5;
-    const int32_t row = row_ok ? __ldg(order + slot) : 0;
-    const double yr = sorted_row_product<double, double, double>(row_ok, row, rowptr, col, val, x);
-    if (row_ok) {
-      y[6 * int64_t(row) + c] = yr;
-      if (EPI == kDotP) dp = fma(x[6 * int64_t(row) + c], yr, dp);
+#pragma unroll
+  for (int j = 0; j < kSlotRows; ++j)
+    if (ok[j]) {
+      y[6 * int64_t(row[j]) + c] = yr[j];
+      if (EPI == kDotP) dp = fma(x[6 * int64_t(row[j]) + c], yr[j], dp);
     }
-  }
   if (EPI == kDotP) {
     const double bs = block_sum<kSpmvT>(dp, sh);
     if (publish<1>(&bs, partials, counter)) {
@@ -227,12 +234,11 @@ __global__ void __launch_bounds__(kSpmvT) k_spmv_sorted(int32_t n, const int32_t
 template <int EPI>
 void launch_spmv(cudaStream_t st, int sched, int32_t n, const int32_t* rowptr, const int32_t* col, const double* val,
                  const double* x, double* y, double* partials, unsigned* counter, PcgScalars* s,
-                 const int32_t* order = nullptr) {
-  if (order) {
-    const int64_t per = int64_t(kRowsPerBlock) * kDotSteps * 5;
+                 const int4* slots = nullptr) {
+  if (slots) {
+    const int64_t per = int64_t(kRowsPerBlock) * kSlotRows * 5;
     const unsigned g = unsigned((std::max<int64_t>(n, 1) + per - 1) / per);
-    (k_spmv_sorted<EPI><<<g, kSpmvT, 0, st>>>(n, order, rowptr, col, val, x, y, partials, counter, s),
-     SVXG_COUNT_LAUNCH());
+    (k_spmv_slots<EPI><<<g, kSpmvT, 0, st>>>(n, slots, col, val, x, y, partials, counter, s), SVXG_COUNT_LAUNCH());
     return;
   }
   if (EPI == kDotP) {
@@ -524,7 +530,7 @@ int ensure_run(Problem& P) {
 int spmv(Problem& P, const Bsr& A, const double* x, double* y) {
   if (A.n == 0) return SVXG_OK;
   launch_spmv<kPlain>(P.stream, &A == &P.K ? P.sched_k64 : 0, A.n, A.rowptr, A.col, A.val, x, y, nullptr, nullptr,
-                      nullptr, &A == &P.K ? P.d_korder : nullptr);
+                      nullptr, &A == &P.K ? P.d_kslots : nullptr);
   SVXG_CUDA(cudaGetLastError());
   return SVXG_OK;
 }
@@ -532,14 +538,16 @@ int spmv(Problem& P, const Bsr& A, const double* x, double* y) {
 // K's FP64 SpMV schedule from the table; with tune timing on, y = K x is also timed with both
 // (a warm-up launch each, then three) and logged
 // K's block rows in order of length (a stable counting sort; lengths of 63 blocks and more share
-// the last class), for the sorted schedule of the CG products; K of fewer than kSortedMinRows rows
-// keeps the table's schedules. The permutation depends on K's pattern only, so the products' bits
-// stay a fixed function of the operator.
-int build_row_order(Problem& P) {
-  P.mem.release(P.d_korder);
+// the last class) as slots {row, first block, length} for the slot schedule of the FP64 CG
+// products (spmv_row.cuh slot_rows_product); K of fewer than kSortedMinRows rows keeps the table's
+// schedules. The slots depend on K's pattern only, so the products' bits stay a fixed function of
+// the operator.
+int build_row_slots(Problem& P) {
+  P.mem.release(P.d_kslots);
   const int32_t n = P.nfree;
   if (n < kSortedMinRows || !P.K.rowptr) return SVXG_OK;
-  std::vector<int32_t> rp(size_t(n) + 1), ord(static_cast<size_t>(n));
+  std::vector<int32_t> rp(size_t(n) + 1);
+  std::vector<int4> sl(static_cast<size_t>(n));
   SVXG_CUDA(cudaMemcpyAsync(rp.data(), P.K.rowptr, sizeof(int32_t) * (size_t(n) + 1), cudaMemcpyDeviceToHost,
                             P.stream));
   SVXG_CUDA(host_wait(P.stream));
@@ -547,15 +555,18 @@ int build_row_order(Problem& P) {
   int64_t start[kClasses + 1] = {};
   for (int32_t i = 0; i < n; ++i) ++start[std::min(rp[size_t(i) + 1] - rp[size_t(i)], kClasses - 1) + 1];
   for (int k = 0; k < kClasses; ++k) start[k + 1] += start[k];
-  for (int32_t i = 0; i < n; ++i) ord[size_t(start[std::min(rp[size_t(i) + 1] - rp[size_t(i)], kClasses - 1)]++)] = i;
-  TRY(P.mem.alloc(&P.d_korder, size_t(n)));
-  SVXG_CUDA(cudaMemcpyAsync(P.d_korder, ord.data(), sizeof(int32_t) * size_t(n), cudaMemcpyHostToDevice, P.stream));
-  SVXG_CUDA(host_wait(P.stream));  // (ord is freed on return)
+  for (int32_t i = 0; i < n; ++i) {
+    const int32_t len = rp[size_t(i) + 1] - rp[size_t(i)];
+    sl[size_t(start[std::min(len, kClasses - 1)]++)] = make_int4(i, rp[size_t(i)], len, 0);
+  }
+  TRY(P.mem.alloc(&P.d_kslots, size_t(n)));
+  SVXG_CUDA(cudaMemcpyAsync(P.d_kslots, sl.data(), sizeof(int4) * size_t(n), cudaMemcpyHostToDevice, P.stream));
+  SVXG_CUDA(host_wait(P.stream));  // (sl is freed on return)
   return SVXG_OK;
 }
 
 int tune_k64(Problem& P) {
-  TRY(build_row_order(P));
+  TRY(build_row_slots(P));
   P.sched_k64 = table_sched(kOpK64, P.nfree, P.K.nnzb);
   if (P.nfree <= 0 || !tune_timing()) return SVXG_OK;
   const size_t m = 6 * size_t(P.nfree);
@@ -605,11 +616,11 @@ int time_cg_spmv(Problem& P, int32_t reps, float* ms_per_launch) {
   SVXG_CUDA(cudaEventCreate(&e0));
   SVXG_CUDA(cudaEventCreate(&e1));
   launch_spmv<kDotP>(P.stream, P.sched_k64, P.nfree, P.K.rowptr, P.K.col, P.K.val, x, y, P.d_partials, P.d_counter,
-                     s, P.d_korder);  // (warm-up)
+                     s, P.d_kslots);  // (warm-up)
   SVXG_CUDA(cudaEventRecord(e0, P.stream));
   for (int32_t r = 0; r < reps; ++r)
     launch_spmv<kDotP>(P.stream, P.sched_k64, P.nfree, P.K.rowptr, P.K.col, P.K.val, x, y, P.d_partials,
-                       P.d_counter, s, P.d_korder);
+                       P.d_counter, s, P.d_kslots);
   SVXG_CUDA(cudaEventRecord(e1, P.stream));
   int32_t done_iters = -1;
   SVXG_CUDA(cudaMemcpyAsync(&done_iters, &s->iters, sizeof(int32_t), cudaMemcpyDeviceToHost, P.stream));
@@ -813,7 +824,7 @@ int plain_body(Problem& P) {
   cudaStream_t st = P.stream;
   if (P.timer_on) TRY(timer_mark(P));
   launch_spmv<kDotP>(st, P.sched_k64, nf, P.K.rowptr, P.K.col, P.K.val, P.d_p, P.d_q, P.d_partials, P.d_counter,
-                     P.d_s, P.d_korder);
+                     P.d_s, P.d_kslots);
   if (P.timer_on) TRY(timer_mark(P, true));
   (k_axpy_rr<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_x, P.d_r, P.d_p, P.d_q, P.d_partials, P.d_counter, P.d_s),
    SVXG_COUNT_LAUNCH());

@@ -129,61 +129,68 @@ __device__ __forceinline__ A sched_row_product(bool row_ok, int32_t row, const i
   return acc;
 }
 
-// The sorted schedule of the conjugate-gradient products: five block rows per warp, taken in the
-// order of a permutation of the rows by length (built once per K, solve.cu build_row_order), so the
-// warp's five lane groups run rows of one length and none idles behind a longer row. Lane 6g + c
-// (g < 5) sums row c of its row's blocks as FMA chains (alternate blocks in two chains): six FMAs
-// a block, the fewest an FP64-issue-bound product can issue. Lanes 30 and 31 hold no row.
-template <typename V, typename X, typename A>
-__device__ __forceinline__ A sorted_row_product(bool row_ok, int32_t row, const int32_t* __restrict__ rowptr,
-                                                const int32_t* __restrict__ col, const V* __restrict__ val,
-                                                const X* __restrict__ x) {
+// The slot schedule of the FP64 conjugate-gradient products. K's block rows are sorted by length
+// once per K (solve.cu build_row_slots) into slots {row, first block, length}; lane group g (g < 5)
+// of a warp takes R consecutive slots - rows of one length, as the sort puts them - and runs them
+// in lock-step, lane 6g + c summing row c of each: per block step R column loads, then 3R value and
+// 3R x loads, all independent, then 6R FMAs into R chains. The dependent chain per step is
+// slot -> column -> x; lanes 30 and 31 idle. Six FMAs a block and row of output, the fewest the
+// product can issue: GB300's FP64 rate bounds the FP64 product. (The FP32 products keep K's row
+// order, whose neighbouring rows share value sectors and x in L1: sorted rows made the city block's
+// FP32 CG product 41 -> 59-74 us.)
+template <int R, typename V, typename X, typename A>
+__device__ __forceinline__ void slot_rows_product(const int4* __restrict__ slots, int64_t first, int64_t nslots,
+                                                  const int32_t* __restrict__ col, const V* __restrict__ val,
+                                                  const X* __restrict__ x, int32_t row[R], bool ok[R], A out[R]) {
   using MV = typename Vec2<V>::T;
   using XV = typename Vec2<X>::T;
   const int lane = threadIdx.x & 31;
   const int g = lane / 6, c = lane - 6 * g;
-  A acc0 = A(0), acc1 = A(0);
-  if (row_ok && g < 5) {
-    const int32_t k1 = __ldg(rowptr + row + 1);
-    int32_t k = __ldg(rowptr + row);
-    for (; k + 1 < k1; k += 2) {
-      const int32_t ca = __ldg(col + k), cb = __ldg(col + k + 1);
-      const MV* ma = reinterpret_cast<const MV*>(val + 36 * int64_t(k) + 6 * c);
-      const MV* mb = reinterpret_cast<const MV*>(val + 36 * int64_t(k + 1) + 6 * c);
-      const XV* xa = reinterpret_cast<const XV*>(x + 6 * int64_t(ca));
-      const XV* xb = reinterpret_cast<const XV*>(x + 6 * int64_t(cb));
-      const MV a0 = __ldg(ma), a1 = __ldg(ma + 1), a2 = __ldg(ma + 2);
-      const MV b0 = __ldg(mb), b1 = __ldg(mb + 1), b2 = __ldg(mb + 2);
-      const XV u0 = __ldg(xa), u1 = __ldg(xa + 1), u2 = __ldg(xa + 2);
-      const XV v0 = __ldg(xb), v1 = __ldg(xb + 1), v2 = __ldg(xb + 2);
-      acc0 = fma(A(a0.x), A(u0.x), acc0);
-      acc1 = fma(A(b0.x), A(v0.x), acc1);
-      acc0 = fma(A(a0.y), A(u0.y), acc0);
-      acc1 = fma(A(b0.y), A(v0.y), acc1);
-      acc0 = fma(A(a1.x), A(u1.x), acc0);
-      acc1 = fma(A(b1.x), A(v1.x), acc1);
-      acc0 = fma(A(a1.y), A(u1.y), acc0);
-      acc1 = fma(A(b1.y), A(v1.y), acc1);
-      acc0 = fma(A(a2.x), A(u2.x), acc0);
-      acc1 = fma(A(b2.x), A(v2.x), acc1);
-      acc0 = fma(A(a2.y), A(u2.y), acc0);
-      acc1 = fma(A(b2.y), A(v2.y), acc1);
+  int32_t k0[R], len[R];
+  int32_t tmax = 0;
+#pragma unroll
+  for (int j = 0; j < R; ++j) {
+    const int64_t sl = first + int64_t(g) * R + j;
+    ok[j] = g < 5 && sl < nslots;
+    const int4 e = ok[j] ? __ldg(slots + sl) : make_int4(0, 0, 0, 0);
+    row[j] = e.x;
+    k0[j] = e.y;
+    len[j] = e.z;
+    tmax = len[j] > tmax ? len[j] : tmax;
+    out[j] = A(0);
+  }
+  for (int32_t t = 0; t < tmax; ++t) {
+    int32_t cl[R];
+#pragma unroll
+    for (int j = 0; j < R; ++j) cl[j] = t < len[j] ? __ldg(col + k0[j] + t) : 0;
+    MV a[R][3];
+    XV u[R][3];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      if (t < len[j]) {
+        const MV* m = reinterpret_cast<const MV*>(val + 36 * int64_t(k0[j] + t) + 6 * c);
+        const XV* v = reinterpret_cast<const XV*>(x + 6 * int64_t(cl[j]));
+        a[j][0] = __ldg(m);
+        a[j][1] = __ldg(m + 1);
+        a[j][2] = __ldg(m + 2);
+        u[j][0] = __ldg(v);
+        u[j][1] = __ldg(v + 1);
+        u[j][2] = __ldg(v + 2);
+      }
     }
-    if (k < k1) {
-      const int32_t ca = __ldg(col + k);
-      const MV* ma = reinterpret_cast<const MV*>(val + 36 * int64_t(k) + 6 * c);
-      const XV* xa = reinterpret_cast<const XV*>(x + 6 * int64_t(ca));
-      const MV a0 = __ldg(ma), a1 = __ldg(ma + 1), a2 = __ldg(ma + 2);
-      const XV u0 = __ldg(xa), u1 = __ldg(xa + 1), u2 = __ldg(xa + 2);
-      acc0 = fma(A(a0.x), A(u0.x), acc0);
-      acc0 = fma(A(a0.y), A(u0.y), acc0);
-      acc0 = fma(A(a1.x), A(u1.x), acc0);
-      acc0 = fma(A(a1.y), A(u1.y), acc0);
-      acc0 = fma(A(a2.x), A(u2.x), acc0);
-      acc0 = fma(A(a2.y), A(u2.y), acc0);
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      if (t < len[j]) {
+        A acc = out[j];
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          acc = fma(A(a[j][q].x), A(u[j][q].x), acc);
+          acc = fma(A(a[j][q].y), A(u[j][q].y), acc);
+        }
+        out[j] = acc;
+      }
     }
   }
-  return acc0 + acc1;
 }
 
 // component q of the row's 6-vector v (held by the row's lanes) - whole warp must call
