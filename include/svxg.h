@@ -62,6 +62,30 @@ void* svxg_problem_stream(svxg_problem* p);
 int svxg_set_graph(svxg_problem* p, const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb,
                    const svxg_material* mats);
 
+/* The same from device memory of the problem's device (the graph kept on the GPU by the caller,
+ * e.g. bonds made by svxg_build_bonds_device): copied device to device, with the host copies of
+ * the nodes, each bond's nodes and flags and the materials read back; a bond with a node or
+ * material out of range: SVXG_ERR_ARG and no graph. */
+int svxg_set_graph_device(svxg_problem* p, const svxg_node* nodes_dev, int32_t n, const svxg_bond* bonds_dev,
+                          int32_t nb, const svxg_material* mats_dev);
+
+/* No counterpart in the reference (whose callers solve independent graphs one StressProblem each,
+ * concurrently on pool threads, core/src/world/world_pieces.cpp:1460-1463). A batch: `count`
+ * independent graphs as one problem, graph g's nodes and bonds after those of the graphs before it
+ * (its bonds' node indices moved by its node offset), one material table. Assembly and the
+ * multigrid are the reference's over that one graph (disjoint parts couple nowhere in K), so every
+ * launch covers the whole batch; the solve (svxg_solve / svxg_solve_device with f and u the graphs'
+ * vectors one after another) stops when every graph has ||r_g|| <= rtol ||f_g||, whatever the
+ * batch's global residual. The batch lasts until the next svxg_set_graph / _device / reassemble. */
+int svxg_set_graphs(svxg_problem* p, int32_t count, const svxg_node* const* nodes, const int32_t* n,
+                    const svxg_bond* const* bonds, const int32_t* nb, const svxg_material* mats);
+/* The same batch from graphs in device memory (pointer arrays on the host). */
+int svxg_set_graphs_device(svxg_problem* p, int32_t count, const svxg_node* const* nodes_dev, const int32_t* n,
+                           const svxg_bond* const* bonds_dev, const int32_t* nb, const svxg_material* mats_dev);
+/* After a batch's solve: per graph ||r_g|| / ||f_g|| (0 without load) and whether it met its target
+ * (count: the batch's graph count). */
+int svxg_graph_results(svxg_problem* p, int32_t count, double* rel_res, int32_t* converged);
+
 /* StressProblem::assemble (stress.hpp:83, stress.cpp:134-176): K over the intact bonds and the
  * preconditioner. *ok = 1 assembled, 0 singular diagonal (the reference's false). */
 int svxg_assemble(svxg_problem* p, const svxg_stress_options* opt, int32_t* ok);

@@ -20,7 +20,7 @@ from . import build as _build
 from .graph import (BOND_DTYPE, LOAD_DTYPE, MATERIAL_DTYPE, NODE_DTYPE, CascadeOptions, CascadeResult, PcgResult,
                     PieceOptions, PieceResult, StressOptions, default_materials, ptr)
 
-__all__ = ["StressProblem", "StressOptions", "PcgResult", "Info", "load_library", "default_materials",
+__all__ = ["Batch", "StressProblem", "StressOptions", "PcgResult", "Info", "load_library", "default_materials",
            "NODE_DTYPE", "BOND_DTYPE", "SvxgError", "CascadeOptions", "CascadeResult", "build_bonds",
            "PieceOptions", "PieceResult"]
 
@@ -73,6 +73,12 @@ def load_library() -> ctypes.CDLL:
         "svxg_problem_destroy": (None, [c_vp]),
         "svxg_problem_stream": (c_vp, [c_vp]),
         "svxg_set_graph": (c_i32, [c_vp, c_vp, c_i32, c_vp, c_i32, c_vp]),
+        "svxg_set_graph_device": (c_i32, [c_vp, c_vp, c_i32, c_vp, c_i32, c_vp]),
+        "svxg_set_graphs": (c_i32, [c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp]),
+        "svxg_set_graphs_device": (c_i32, [c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp]),
+        "svxg_graph_results": (c_i32, [c_vp, c_i32, c_vp, c_vp]),
+        "svxg_time_spmv": (c_i32, [c_vp, c_i32, c_i32, ctypes.POINTER(c_f64)]),
+        "svxg_measure_fp64_rate": (c_i32, [c_i32, ctypes.POINTER(c_f64)]),
         "svxg_assemble": (c_i32, [c_vp, c_vp, ctypes.POINTER(c_i32)]),
         "svxg_assembled": (c_i32, [c_vp]),
         "svxg_reassemble": (c_i32, [c_vp, c_vp, c_i32, c_vp, c_i32, c_vp, ctypes.POINTER(c_i32)]),
@@ -450,3 +456,83 @@ class StressProblem:
         y = np.zeros_like(x)
         _check(self._L.svxg_debug_apply(self._h, ptr(x), ptr(y)))
         return y
+
+
+class Batch:
+    """Several independent graphs solved as one problem (svxg_set_graphs): every launch of the
+    assembly, the multigrid build and the solve covers the whole batch, and the solve stops when
+    every graph meets its own target ||r_g|| <= rtol ||f_g||. ``graphs``: (nodes, bonds) pairs
+    with one material table."""
+
+    def __init__(self, graphs, mats=None, device: int = 0):
+        L = load_library()
+        if L.svxg_device_count() <= device:
+            raise SvxgError(-6, "no CUDA device")
+        h = c_vp()
+        _check(L.svxg_problem_create(ctypes.byref(h), device))
+        self._h, self._L = h, L
+        self.graphs = [(np.ascontiguousarray(n, dtype=NODE_DTYPE), np.ascontiguousarray(b, dtype=BOND_DTYPE))
+                       for n, b in graphs]
+        self.mats = default_materials() if mats is None else np.ascontiguousarray(mats, dtype=MATERIAL_DTYPE)
+        k = len(self.graphs)
+        P = c_vp * k
+        self._n = np.array([len(g[0]) for g in self.graphs], np.int32)
+        self._nb = np.array([len(g[1]) for g in self.graphs], np.int32)
+        _check(L.svxg_set_graphs(h, k, P(*[ptr(g[0]) for g in self.graphs]), ptr(self._n),
+                                 P(*[ptr(g[1]) for g in self.graphs]), ptr(self._nb), ptr(self.mats)))
+        self.node_off = np.concatenate([[0], np.cumsum(self._n)]).astype(np.int64)
+        self.bond_off = np.concatenate([[0], np.cumsum(self._nb)]).astype(np.int64)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if sys.is_finalizing():
+            return
+        if h is not None and h.value:
+            self._L.svxg_problem_destroy(h)
+            self._h = None
+
+    def assemble(self, opt: StressOptions | None = None) -> bool:
+        ok = c_i32(0)
+        _check(self._L.svxg_assemble(self._h, ctypes.byref(opt) if opt is not None else None, ctypes.byref(ok)))
+        return bool(ok.value)
+
+    def solve(self, fs, rtol: float = 1e-6, maxit: int = -1):
+        """fs: one load per graph (6 per node). Returns (list of u, PcgResult of the batch, per-graph
+        rel. residuals, per-graph converged flags)."""
+        f = np.concatenate([np.ascontiguousarray(x, dtype=np.float64).ravel() for x in fs])
+        if f.size != 6 * int(self.node_off[-1]):
+            raise ValueError("fs: 6 per node of each graph")
+        u = np.zeros_like(f)
+        res = PcgResult()
+        _check(self._L.svxg_solve(self._h, ptr(f), ptr(u), float(rtol), int(maxit), 0, ctypes.byref(res)))
+        k = len(self.graphs)
+        rel = np.zeros(k)
+        conv = np.zeros(k, np.int32)
+        if k > 1:
+            _check(self._L.svxg_graph_results(self._h, k, ptr(rel), ptr(conv)))
+        else:
+            rel[0], conv[0] = res.rel_res, res.converged
+        us = [u[6 * self.node_off[g]:6 * self.node_off[g + 1]] for g in range(k)]
+        return us, res, rel, conv.astype(bool)
+
+    def utilization(self, fragility: float = 1.0):
+        """Per graph (phi, mode, failing bonds in the graph's own numbering) at the last solution."""
+        nb = int(self.bond_off[-1])
+        phi = np.zeros(max(nb, 1))
+        mode = np.zeros(max(nb, 1), np.uint8)
+        over = np.zeros(max(nb, 1), np.int32)
+        cnt = c_i32(0)
+        _check(self._L.svxg_utilization(self._h, float(fragility), ptr(phi), ptr(mode), ptr(over), len(over),
+                                        ctypes.byref(cnt)))
+        over = over[:cnt.value]
+        out = []
+        for g in range(len(self.graphs)):
+            a, b = self.bond_off[g], self.bond_off[g + 1]
+            sel = over[(over >= a) & (over < b)] - a
+            out.append((phi[a:b].copy(), mode[a:b].copy(), sel.astype(np.int32)))
+        return out
+
+    def info(self) -> Info:
+        i = Info()
+        _check(self._L.svxg_get_info(self._h, ctypes.byref(i)))
+        return i

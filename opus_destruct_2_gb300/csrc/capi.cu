@@ -62,6 +62,8 @@ void release_solver(Problem& P) {
   P.mem.release(P.K.val32);
   P.K = Bsr{};
   P.mem.release(P.d_kslots);
+  P.mem.release(P.d_seg_row);
+  P.mem.release(P.d_seg);
   P.mem.release(P.d_jinv);
   P.mem.release(P.d_dof);
   P.mem.release(P.d_chol);
@@ -396,6 +398,9 @@ static int check_graph(const char* who, const svxg_node* nodes, int32_t n, const
 // the graph's device and host copies replaced (the solver is left as it is)
 static int upload_graph(Problem& P, const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb,
                         const svxg_material* mats) {
+  P.seg_n = 0;  // (one graph; svxg_set_graphs makes a batch after this)
+  P.seg_node.clear();
+  P.seg_bond.clear();
   P.mem.release(P.d_nodes);
   P.mem.release(P.d_bonds);
   P.mem.release(P.d_mats);
@@ -425,9 +430,240 @@ static int upload_graph(Problem& P, const svxg_node* nodes, int32_t n, const svx
   return SVXG_OK;
 }
 
+// A device-resident graph's bookkeeping: each bond's nodes and flags for the host copies, and the
+// lowest index of a bond with a bad node or material (atomicMin: the same index whatever the order)
+__global__ void k_graph_book(int32_t n, int32_t nb, const svxg_bond* __restrict__ bonds, int32_t* ab, uint8_t* broken,
+                             uint8_t* in_k, int32_t* bad) {
+  const int64_t k = int64_t(blockIdx.x) * 256 + threadIdx.x;
+  if (k >= nb) return;
+  const svxg_bond b = bonds[k];
+  ab[2 * k] = b.a;
+  ab[2 * k + 1] = b.b;
+  broken[k] = b.broken;
+  in_k[k] = b.in_k;
+  if (b.a < 0 || b.a >= n || b.b >= n || b.b == b.a || b.ma >= SVXG_MAX_MATERIALS || b.mb >= SVXG_MAX_MATERIALS)
+    atomicMin(bad, int32_t(k));
+}
+
+// Bond node indices of a batch moved by their graph's node offset: bond k of graph g (bonds
+// [boff[g], boff[g + 1])) gets noff[g] added to a, and to b unless it is a support (-1).
+__global__ void k_batch_offsets(int32_t nb, int32_t count, const int64_t* __restrict__ boff,
+                                const int64_t* __restrict__ noff, svxg_bond* bonds) {
+  const int64_t k = int64_t(blockIdx.x) * 256 + threadIdx.x;
+  if (k >= nb) return;
+  int32_t lo = 0, hi = count - 1;  // (the last g with boff[g] <= k)
+  while (lo < hi) {
+    const int32_t mid = (lo + hi + 1) / 2;
+    if (boff[mid] <= k) lo = mid;
+    else hi = mid - 1;
+  }
+  const int32_t o = int32_t(noff[lo]);
+  bonds[k].a += o;
+  if (bonds[k].b >= 0) bonds[k].b += o;
+}
+
+// the graph's host bookkeeping read back from its device copies (nodes, each bond's nodes and
+// flags, the materials); a bond with a bad node or material: SVXG_ERR_ARG, no graph
+static int finish_device_graph(Problem& P, const char* who) {
+  const int32_t n = P.n, nb = P.nb;
+  cudaStream_t st = P.stream;
+  // scratch: the bad index, a b pairs, broken, in_k
+  const size_t bytes = sizeof(int32_t) * (2 * size_t(nb) + 1) + 2 * size_t(nb) + 16;
+  char* tmp = nullptr;
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&tmp), bytes, st));
+  int32_t* d_bad = reinterpret_cast<int32_t*>(tmp);
+  int32_t* d_ab = d_bad + 1;
+  uint8_t* d_broken = reinterpret_cast<uint8_t*>(d_ab + 2 * size_t(nb));
+  uint8_t* d_ink = d_broken + nb;
+  SVXG_CUDA(cudaMemsetAsync(d_bad, 0x7f, sizeof(int32_t), st));
+  if (nb)
+    (k_graph_book<<<unsigned((int64_t(nb) + 255) / 256), 256, 0, st>>>(n, nb, P.d_bonds, d_ab, d_broken, d_ink, d_bad),
+     SVXG_COUNT_LAUNCH());
+  SVXG_CUDA(cudaGetLastError());
+  P.h_nodes.resize(size_t(n));
+  P.h_bond_ab.resize(2 * size_t(nb));
+  P.h_broken.resize(size_t(nb));
+  P.h_in_k.resize(size_t(nb));
+  P.h_mats.resize(SVXG_MAX_MATERIALS);
+  int32_t bad = 0;
+  if (n) SVXG_CUDA(cudaMemcpyAsync(P.h_nodes.data(), P.d_nodes, sizeof(svxg_node) * size_t(n), cudaMemcpyDeviceToHost, st));
+  if (nb) {
+    SVXG_CUDA(cudaMemcpyAsync(P.h_bond_ab.data(), d_ab, sizeof(int32_t) * 2 * size_t(nb), cudaMemcpyDeviceToHost, st));
+    SVXG_CUDA(cudaMemcpyAsync(P.h_broken.data(), d_broken, size_t(nb), cudaMemcpyDeviceToHost, st));
+    SVXG_CUDA(cudaMemcpyAsync(P.h_in_k.data(), d_ink, size_t(nb), cudaMemcpyDeviceToHost, st));
+  }
+  SVXG_CUDA(cudaMemcpyAsync(P.h_mats.data(), P.d_mats, sizeof(svxg_material) * SVXG_MAX_MATERIALS,
+                            cudaMemcpyDeviceToHost, st));
+  SVXG_CUDA(cudaMemcpyAsync(&bad, d_bad, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  cudaFreeAsync(tmp, st);
+  SVXG_CUDA(host_wait(st));
+  if (bad < nb) {
+    set_error(std::string(who) + ": bond " + std::to_string(bad) + " has a bad node or material");
+    P.mem.release(P.d_nodes);
+    P.mem.release(P.d_bonds);
+    P.mem.release(P.d_mats);
+    P.n = P.nb = 0;
+    P.seg_n = 0;
+    P.seg_node.clear();
+    P.seg_bond.clear();
+    return SVXG_ERR_ARG;
+  }
+  P.have_graph = true;
+  return SVXG_OK;
+}
+
+// The graphs' device copies from device arrays (one graph: count 1; a batch: graph g after those
+// before it, its bonds' node indices moved by its node offset), then the host bookkeeping.
+static int upload_graphs_device(Problem& P, int32_t count, const svxg_node* const* nodes, const int32_t* n,
+                                const svxg_bond* const* bonds, const int32_t* nb, const svxg_material* mats) {
+  P.seg_n = 0;
+  P.seg_node.clear();
+  P.seg_bond.clear();
+  P.mem.release(P.d_nodes);
+  P.mem.release(P.d_bonds);
+  P.mem.release(P.d_mats);
+  P.mem.release(P.d_un);
+  P.have_graph = false;
+  std::vector<int64_t> so(size_t(count) + 1, 0), sb(size_t(count) + 1, 0);
+  for (int32_t g = 0; g < count; ++g) {
+    so[size_t(g) + 1] = so[size_t(g)] + n[g];
+    sb[size_t(g) + 1] = sb[size_t(g)] + nb[g];
+  }
+  if (so.back() > INT32_MAX || sb.back() > INT32_MAX) {
+    set_error("set_graphs: more than 2^31 nodes or bonds in all");
+    return SVXG_ERR_ARG;
+  }
+  P.n = int32_t(so.back());
+  P.nb = int32_t(sb.back());
+  TRY(P.mem.alloc(&P.d_nodes, size_t(P.n)));
+  TRY(P.mem.alloc(&P.d_bonds, size_t(P.nb)));
+  TRY(P.mem.alloc(&P.d_mats, size_t(SVXG_MAX_MATERIALS)));
+  cudaStream_t st = P.stream;
+  for (int32_t g = 0; g < count; ++g) {
+    if (n[g])
+      SVXG_CUDA(cudaMemcpyAsync(P.d_nodes + so[size_t(g)], nodes[g], sizeof(svxg_node) * size_t(n[g]),
+                                cudaMemcpyDeviceToDevice, st));
+    if (nb[g])
+      SVXG_CUDA(cudaMemcpyAsync(P.d_bonds + sb[size_t(g)], bonds[g], sizeof(svxg_bond) * size_t(nb[g]),
+                                cudaMemcpyDeviceToDevice, st));
+  }
+  SVXG_CUDA(cudaMemcpyAsync(P.d_mats, mats, sizeof(svxg_material) * SVXG_MAX_MATERIALS, cudaMemcpyDeviceToDevice,
+                            st));
+  if (count > 1 && P.nb > 0) {
+    int64_t* off = nullptr;
+    SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&off), sizeof(int64_t) * 2 * (size_t(count) + 1), st));
+    SVXG_CUDA(cudaMemcpyAsync(off, sb.data(), sizeof(int64_t) * sb.size(), cudaMemcpyHostToDevice, st));
+    SVXG_CUDA(cudaMemcpyAsync(off + count + 1, so.data(), sizeof(int64_t) * so.size(), cudaMemcpyHostToDevice, st));
+    (k_batch_offsets<<<unsigned((int64_t(P.nb) + 255) / 256), 256, 0, st>>>(P.nb, count, off, off + count + 1,
+                                                                              P.d_bonds),
+     SVXG_COUNT_LAUNCH());
+    cudaFreeAsync(off, st);
+    SVXG_CUDA(host_wait(st));  // (so and sb are host vectors read by the copies above)
+  }
+  TRY(finish_device_graph(P, count > 1 ? "svxg_set_graphs_device" : "svxg_set_graph_device"));
+  if (count > 1) {
+    P.seg_n = count;
+    P.seg_node = std::move(so);
+    P.seg_bond = std::move(sb);
+  }
+  return SVXG_OK;
+}
+
 }  // namespace svxg
 
 extern "C" {
+
+int svxg_set_graph_device(svxg_problem* p, const svxg_node* nodes_dev, int32_t n, const svxg_bond* bonds_dev,
+                          int32_t nb, const svxg_material* mats_dev) {
+  CHECK_P(p);
+  if (n < 0 || nb < 0 || (n > 0 && !nodes_dev) || (nb > 0 && !bonds_dev) || !mats_dev) {
+    set_error("svxg_set_graph_device: bad sizes or null arrays");
+    return SVXG_ERR_ARG;
+  }
+  Problem& P = p->P;
+  DeviceScope ds(P.device);
+  release_solver(P);
+  return upload_graphs_device(P, 1, &nodes_dev, &n, &bonds_dev, &nb, mats_dev);
+}
+
+int svxg_set_graphs_device(svxg_problem* p, int32_t count, const svxg_node* const* nodes, const int32_t* n,
+                           const svxg_bond* const* bonds, const int32_t* nb, const svxg_material* mats) {
+  CHECK_P(p);
+  if (count < 1 || !nodes || !n || !bonds || !nb || !mats) {
+    set_error("svxg_set_graphs_device: bad count or null arrays");
+    return SVXG_ERR_ARG;
+  }
+  for (int32_t g = 0; g < count; ++g)
+    if (n[g] < 0 || nb[g] < 0 || (n[g] > 0 && !nodes[g]) || (nb[g] > 0 && !bonds[g])) {
+      set_error("svxg_set_graphs_device: graph " + std::to_string(g) + " has bad sizes or null arrays");
+      return SVXG_ERR_ARG;
+    }
+  Problem& P = p->P;
+  DeviceScope ds(P.device);
+  release_solver(P);
+  return upload_graphs_device(P, count, nodes, n, bonds, nb, mats);
+}
+
+int svxg_set_graphs(svxg_problem* p, int32_t count, const svxg_node* const* nodes, const int32_t* n,
+                    const svxg_bond* const* bonds, const int32_t* nb, const svxg_material* mats) {
+  CHECK_P(p);
+  if (count < 1 || !nodes || !n || !bonds || !nb || !mats) {
+    set_error("svxg_set_graphs: bad count or null arrays");
+    return SVXG_ERR_ARG;
+  }
+  int64_t tn = 0, tb = 0;
+  for (int32_t g = 0; g < count; ++g) {
+    TRY(check_graph("svxg_set_graphs", nodes[g], n[g], bonds[g], nb[g], mats));
+    tn += n[g];
+    tb += nb[g];
+  }
+  if (tn > INT32_MAX || tb > INT32_MAX) {
+    set_error("svxg_set_graphs: more than 2^31 nodes or bonds in all");
+    return SVXG_ERR_ARG;
+  }
+  // one graph of them all: graph g's nodes and bonds after those of the graphs before it, its bonds'
+  // node indices moved by its node offset (supports stay -1)
+  std::vector<svxg_node> un(static_cast<size_t>(tn));
+  std::vector<svxg_bond> ub(static_cast<size_t>(tb));
+  std::vector<int64_t> so(size_t(count) + 1, 0), sb(size_t(count) + 1, 0);
+  for (int32_t g = 0; g < count; ++g) {
+    const int64_t o = so[size_t(g)], ob = sb[size_t(g)];
+    if (n[g]) std::memcpy(&un[size_t(o)], nodes[g], sizeof(svxg_node) * size_t(n[g]));
+    for (int32_t k = 0; k < nb[g]; ++k) {
+      svxg_bond b = bonds[g][k];
+      b.a += int32_t(o);
+      if (b.b >= 0) b.b += int32_t(o);
+      ub[size_t(ob + k)] = b;
+    }
+    so[size_t(g) + 1] = o + n[g];
+    sb[size_t(g) + 1] = ob + nb[g];
+  }
+  Problem& P = p->P;
+  DeviceScope ds(P.device);
+  release_solver(P);
+  TRY(upload_graph(P, un.data(), int32_t(tn), ub.data(), int32_t(tb), mats));
+  if (count > 1) {
+    P.seg_n = count;
+    P.seg_node = std::move(so);
+    P.seg_bond = std::move(sb);
+  }
+  return SVXG_OK;
+}
+
+int svxg_graph_results(svxg_problem* p, int32_t count, double* rel_res, int32_t* converged) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  if (P.seg_n <= 0 || count != P.seg_n) {
+    set_error("svxg_graph_results: not a batch of that many graphs");
+    return SVXG_ERR_ARG;
+  }
+  if (!P.d_seg) {
+    set_error("svxg_graph_results: not assembled");
+    return SVXG_ERR_STATE;
+  }
+  DeviceScope ds(P.device);
+  return seg_results(P, rel_res, converged);
+}
 
 int svxg_set_graph(svxg_problem* p, const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb,
                    const svxg_material* mats) {
@@ -472,6 +708,7 @@ static int assemble_impl(Problem& P, const svxg_stress_options* opt, int32_t* ok
   }
   trace_mark(P, "preconditioner built");
   TRY(tune_k64(P));
+  TRY(seg_prepare(P));
   P.sched_k32 = P.jacobi_only || P.lv.empty() ? 0 : P.lv[0].sched_a;  // (K32 is level 0's cycle operator)
   SVXG_CUDA(host_wait(P.stream));
   P.pc_n = P.jacobi_only ? 0 : P.nfree;
@@ -729,13 +966,51 @@ int solve_nodes_host(Problem& P, const double* f, double* u, double rtol, int32_
   const size_t m = 6 * size_t(P.n);
   double* du = P.d_un;
   double* df = P.d_un + m;
-  SVXG_CUDA(cudaMemcpyAsync(df, f, m * sizeof(double), cudaMemcpyHostToDevice, P.stream));
-  if (warm == kWarmHost) SVXG_CUDA(cudaMemcpyAsync(du, u, m * sizeof(double), cudaMemcpyHostToDevice, P.stream));
+  // (f and u may be host or device memory: the copies take their direction from the pointers)
+  SVXG_CUDA(cudaMemcpyAsync(df, f, m * sizeof(double), cudaMemcpyDefault, P.stream));
+  if (warm == kWarmHost) SVXG_CUDA(cudaMemcpyAsync(du, u, m * sizeof(double), cudaMemcpyDefault, P.stream));
   trace_mark(P, "solve: load copied");
   TRY(solve_common(P, df, du, rtol, maxit, warm == kWarmHost || resident ? 1 : 0, res));
-  if (u) SVXG_CUDA(cudaMemcpyAsync(u, du, m * sizeof(double), cudaMemcpyDeviceToHost, P.stream));
+  if (u) SVXG_CUDA(cudaMemcpyAsync(u, du, m * sizeof(double), cudaMemcpyDefault, P.stream));
   SVXG_CUDA(host_wait(P.stream));
   trace_mark(P, "solve: u copied back");
+  return SVXG_OK;
+}
+
+// A batch's solve with graph g's load read from f[g] (host or device memory, 6 per node); a graph
+// with take[g] == 0 keeps the load of the last solve (a repeat of some graphs replaces only theirs;
+// take null: every graph's). warm: from the problem's last solution, still on the device. u of
+// graph g goes to u_out[g] (host or device memory; u_out or u_out[g] null: not copied).
+int batch_solve_loads(Problem& P, const double* const* f, const uint8_t* take, double* const* u_out, double rtol,
+                      int32_t maxit, bool warm, svxg_pcg_result* res) {
+  DeviceScope ds(P.device);
+  if (P.seg_n <= 0) {
+    set_error("batch solve: not a batch");
+    return SVXG_ERR_STATE;
+  }
+  const int a = ensure_assembled(P);
+  if (a < 0) return a;
+  if (a > 0) {
+    failed_result(res);
+    return SVXG_OK;
+  }
+  const bool resident = warm && P.d_un && P.mem.holds(P.d_un, 12 * sizeof(double) * size_t(P.n));
+  TRY(ensure_node_vectors(P));
+  const size_t m = 6 * size_t(P.n);
+  double* du = P.d_un;
+  double* df = P.d_un + m;
+  for (int32_t g = 0; g < P.seg_n; ++g) {
+    const size_t o = 6 * size_t(P.seg_node[size_t(g)]), len = 6 * size_t(P.seg_node[size_t(g) + 1]) - o;
+    if ((!take || take[g]) && len && f[g])
+      SVXG_CUDA(cudaMemcpyAsync(df + o, f[g], len * sizeof(double), cudaMemcpyDefault, P.stream));
+  }
+  TRY(solve_common(P, df, du, rtol, maxit, resident ? 1 : 0, res));
+  for (int32_t g = 0; u_out && g < P.seg_n; ++g) {
+    const size_t o = 6 * size_t(P.seg_node[size_t(g)]), len = 6 * size_t(P.seg_node[size_t(g) + 1]) - o;
+    if (u_out[g] && len)
+      SVXG_CUDA(cudaMemcpyAsync(u_out[g], du + o, len * sizeof(double), cudaMemcpyDefault, P.stream));
+  }
+  SVXG_CUDA(host_wait(P.stream));
   return SVXG_OK;
 }
 

@@ -176,6 +176,13 @@ struct Problem {
   double* d_jinv = nullptr;       // block-Jacobi inverses (36 per free node)
   int sched_k64 = 0, sched_k32 = 0;  // K's SpMV schedules (FP64 CG, FP32 inner), autotuned
   int4* d_kslots = nullptr;       // K's block rows by length as slots (the FP64 CG products' schedule), or null
+  // a batch: several independent graphs as one problem (svxg_set_graphs), graph g its nodes
+  // [seg_node[g], seg_node[g + 1]) and bonds [seg_bond[g], seg_bond[g + 1]); the solve stops when
+  // every graph meets its own target (segmented norms over its free rows d_seg_row[g] ..)
+  int32_t seg_n = 0;
+  std::vector<int64_t> seg_node, seg_bond;
+  int32_t* d_seg_row = nullptr;   // seg_n + 1 free-row offsets (made at assembly)
+  double* d_seg = nullptr;        // per graph: ||f||, target, ||r|| (3 seg_n)
   // multigrid
   std::vector<Level> lv;
   double* d_chol = nullptr;       // coarsest dense factor (m x m, lower = L, upper = L^T)
@@ -228,7 +235,10 @@ void trace_mark(Problem& P, const char* label, bool restart = false);
 // ---- launchers (one translation unit each) ---------------------------------------------------
 // capi.cu
 enum WarmStart { kCold = 0, kWarmHost = 1, kWarmResident = 2 };
-// f, u host (6 per node); kWarmResident starts from the problem's last solution, still on the device
+// f, u (6 per node) host or device memory; kWarmResident starts from the problem's last solution,
+// still on the device
+int batch_solve_loads(Problem& P, const double* const* f, const uint8_t* take, double* const* u_out, double rtol,
+                      int32_t maxit, bool warm, svxg_pcg_result* res);  // capi.cu: a batch's solve
 int solve_nodes_host(Problem& P, const double* f, double* u, double rtol, int32_t maxit, int warm,
                      svxg_pcg_result* res);
 int ensure_node_vectors(Problem& P);
@@ -254,6 +264,8 @@ int precondition(Problem& P, const double* r, double* z);
 int free_run(Problem& P);
 int tune_k64(Problem& P);
 int time_cg_spmv(Problem& P, int32_t reps, float* ms_per_launch);    // solve.cu
+int seg_prepare(Problem& P);   // solve.cu: a batch's free-row offsets and per-graph scalars after assembly
+int seg_results(Problem& P, double* rel_res, int32_t* converged);  // solve.cu: per graph, after a solve
 int time_cg_spmv32(Problem& P, int32_t reps, float* ms_per_launch);  // mixed.cu
 int measure_fp64_rate(int device, double* tflops);                    // tune.cu
 // tune.cu: the row schedule of a BSR operator (spmv_row.cuh), from the committed table (a pure
@@ -299,7 +311,8 @@ constexpr int32_t kSortedMinRows = SVXG_SORTED_MIN_ROWS;
 // sequence runs (with the same FP32 V-cycle)
 constexpr int32_t kMixedMinFree = 65536;
 inline bool mixed_run(const Problem& P) {
-  if (P.jacobi_only || P.pc_n < P.nfree || !P.K.val32) return false;
+  // (a batch runs the FP64 sequence: its stopping test is per graph)
+  if (P.jacobi_only || P.pc_n < P.nfree || !P.K.val32 || P.seg_n > 0) return false;
   return P.opt.precision == SVXG_PRECISION_MIXED_ALL ||
          (P.opt.precision == SVXG_PRECISION_MIXED && P.nfree >= kMixedMinFree);
 }

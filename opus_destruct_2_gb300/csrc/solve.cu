@@ -461,6 +461,64 @@ __global__ void k_jacobi_apply(int32_t nfree, const double* __restrict__ jinv, c
   }
 }
 
+// ---- a batch's per-graph stopping test ----------------------------------------------------------
+// Graph g of a batch owns free rows [row0[g], row0[g + 1]) (6 entries each). Its norms are sums in a
+// fixed order: one warp per graph, lane l over entries l, l + 32, ..., then a fixed shuffle tree -
+// the same bits on every run, whatever else the batch holds. seg: ||f_g||, target_g, ||r_g||.
+constexpr int kSegT = 256;
+
+__device__ __forceinline__ double seg_sumsq(const double* v, int64_t e0, int64_t e1) {
+  double s = 0.0;
+  for (int64_t e = e0 + (threadIdx.x & 31); e < e1; e += 32) s += v[e] * v[e];
+  return warp_sum(s);
+}
+
+// ||f_g|| of every graph (begin)
+__global__ void k_seg_begin(int32_t nseg, const int32_t* __restrict__ row0, const double* __restrict__ f,
+                            double* seg) {
+  const int32_t g = int32_t(blockIdx.x) * (kSegT / 32) + int32_t(threadIdx.x >> 5);
+  if (g >= nseg) return;
+  const double t = seg_sumsq(f, 6 * int64_t(row0[g]), 6 * int64_t(row0[g + 1]));
+  if ((threadIdx.x & 31) == 0) seg[3 * g] = sqrt(t);
+}
+
+// ||r_g|| against target_g for every graph; START (iterate's start) also sets the targets,
+// rtol ||f_g||. One block: the count of graphs not yet at their targets decides the run - all
+// there: converged; otherwise it goes on whatever the batch's global residual (target -1: the
+// global test of k_axpy_rr never stops a batch).
+template <bool START>
+__global__ void __launch_bounds__(kSegT) k_seg_check(int32_t nseg, const int32_t* __restrict__ row0,
+                                                      const double* __restrict__ r, double rtol, double* seg,
+                                                      PcgScalars* s) {
+  __shared__ int32_t open_sh;
+  if (!START && s->done) return;
+  if (threadIdx.x == 0) open_sh = 0;
+  __syncthreads();
+  int32_t open = 0;
+  for (int32_t g = int32_t(threadIdx.x >> 5); g < nseg; g += kSegT / 32) {
+    const double rn = sqrt(seg_sumsq(r, 6 * int64_t(row0[g]), 6 * int64_t(row0[g + 1])));
+    if ((threadIdx.x & 31) == 0) {
+      if (START) seg[3 * g + 1] = rtol * seg[3 * g];
+      seg[3 * g + 2] = rn;
+      // (a graph without load is there at once, as a solve of zero load is, stress.cpp:389-394)
+      if (!(rn <= seg[3 * g + 1]) && seg[3 * g] > 0.0) ++open;
+    }
+  }
+  if (open) atomicAdd(&open_sh, open);
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  if (START) {
+    if (s->breakdown) return;  // (not finite: the global start already ended the run)
+    s->target = -1.0;
+    const bool none = open_sh == 0;
+    s->converged = none ? 1 : 0;
+    s->done = none || s->maxit <= 0 ? 1 : 0;
+  } else if (open_sh == 0) {
+    s->converged = 1;
+    s->done = 1;
+  }
+}
+
 __global__ void k_fill_ones(int32_t nfree, double* x) {
   const int32_t i = blockIdx.x * kVecT + threadIdx.x;
   if (i < nfree)
@@ -689,6 +747,10 @@ int pcg_begin(Problem& P, const double* f_nodes, const double* u0_nodes) {
     TRY(spmv(P, P.K, P.d_x, P.d_q));
     (k_begin_r<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_f, P.d_q, P.d_r, P.d_partials, P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
     (k_begin_zero<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_x, P.d_r, P.d_s), SVXG_COUNT_LAUNCH());
+    if (P.seg_n > 0)
+      (k_seg_begin<<<unsigned((P.seg_n + kSegT / 32 - 1) / (kSegT / 32)), kSegT, 0, st>>>(P.seg_n, P.d_seg_row,
+                                                                                        P.d_f, P.d_seg),
+       SVXG_COUNT_LAUNCH());
     if (P.jacobi_only) {
       (k_jacobi_rz<0><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_jinv, P.d_r, P.d_z, P.d_p, P.d_partials,
                                                        P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
@@ -828,6 +890,8 @@ int plain_body(Problem& P) {
   if (P.timer_on) TRY(timer_mark(P, true));
   (k_axpy_rr<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_x, P.d_r, P.d_p, P.d_q, P.d_partials, P.d_counter, P.d_s),
    SVXG_COUNT_LAUNCH());
+  if (P.seg_n > 0)
+    (k_seg_check<false><<<1, kSegT, 0, st>>>(P.seg_n, P.d_seg_row, P.d_r, 0.0, P.d_seg, P.d_s), SVXG_COUNT_LAUNCH());
   if (P.jacobi_only) {
     (k_jacobi_rz<1><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_jinv, P.d_r, P.d_z, nullptr, P.d_partials, P.d_counter,
                                                       P.d_s), SVXG_COUNT_LAUNCH());
@@ -894,12 +958,14 @@ int plain_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
   P.cycle_stop = &P.d_s->done;
   (k_iter_start<<<vec_blocks(std::max(nf, 1)), kVecT, 0, st>>>(nf, P.d_r, rtol, maxit, P.d_partials, P.d_counter,
                                                              P.d_s), SVXG_COUNT_LAUNCH());
+  if (P.seg_n > 0 && nf > 0)
+    (k_seg_check<true><<<1, kSegT, 0, st>>>(P.seg_n, P.d_seg_row, P.d_r, rtol, P.d_seg, P.d_s), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   SVXG_CUDA(cudaMemcpyAsync(P.h_s, P.d_s, sizeof(PcgScalars), cudaMemcpyDeviceToHost, st));
   SVXG_CUDA(host_wait(st));
   if (P.h_s->done || nf == 0) {
     // (converged, empty or not finite at the start: no iteration)
-  } else if (P.jacobi_only && nf <= kJacobiBlockMax && !P.timer_on) {
+  } else if (P.jacobi_only && nf <= kJacobiBlockMax && !P.timer_on && P.seg_n == 0) {
     (k_jacobi_pcg_block<<<1, kJacobiBlockT, 0, st>>>(nf, P.K.rowptr, P.K.col, P.K.val, P.d_jinv, P.d_x, P.d_r, P.d_z,
                                                       P.d_p, P.d_q, P.d_s),
      SVXG_COUNT_LAUNCH());
@@ -942,6 +1008,43 @@ int plain_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
   P.run_iters += out.iters;
   if (out.breakdown && !std::isfinite(out.rel_res)) P.active = false;
   if (res) *res = out;
+  return SVXG_OK;
+}
+
+// A batch's free-row offsets from the DOF numbering (free nodes numbered in node order, so graph
+// g's free rows are those of its nodes), and its per-graph scalars; after each assembly.
+int seg_prepare(Problem& P) {
+  P.mem.release(P.d_seg_row);
+  P.mem.release(P.d_seg);
+  if (P.seg_n <= 0) return SVXG_OK;
+  std::vector<int32_t> row0(size_t(P.seg_n) + 1, 0);
+  int32_t fr = 0;
+  for (int32_t g = 0; g < P.seg_n; ++g) {
+    row0[size_t(g)] = fr;
+    for (int64_t i = P.seg_node[size_t(g)]; i < P.seg_node[size_t(g) + 1]; ++i) fr += P.h_dof[size_t(i)] >= 0 ? 1 : 0;
+  }
+  row0[size_t(P.seg_n)] = fr;
+  TRY(P.mem.alloc(&P.d_seg_row, size_t(P.seg_n) + 1));
+  TRY(P.mem.alloc(&P.d_seg, 3 * size_t(P.seg_n)));
+  SVXG_CUDA(cudaMemcpyAsync(P.d_seg_row, row0.data(), sizeof(int32_t) * row0.size(), cudaMemcpyHostToDevice,
+                            P.stream));
+  SVXG_CUDA(cudaMemsetAsync(P.d_seg, 0, sizeof(double) * 3 * size_t(P.seg_n), P.stream));
+  SVXG_CUDA(host_wait(P.stream));  // (row0 is freed on return)
+  return SVXG_OK;
+}
+
+// per graph of a batch after a solve: ||r_g|| / ||f_g|| (0 without load) and whether it met its
+// target (at a converged end every graph did)
+int seg_results(Problem& P, double* rel_res, int32_t* converged) {
+  if (P.seg_n <= 0 || !P.d_seg) return SVXG_ERR_STATE;
+  std::vector<double> h(3 * size_t(P.seg_n));
+  SVXG_CUDA(cudaMemcpyAsync(h.data(), P.d_seg, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, P.stream));
+  SVXG_CUDA(host_wait(P.stream));
+  for (int32_t g = 0; g < P.seg_n; ++g) {
+    const double bn = h[3 * size_t(g)], tg = h[3 * size_t(g) + 1], rn = h[3 * size_t(g) + 2];
+    if (rel_res) rel_res[g] = bn > 0.0 ? rn / bn : 0.0;
+    if (converged) converged[g] = (rn <= tg || !(bn > 0.0)) ? 1 : 0;
+  }
   return SVXG_OK;
 }
 
