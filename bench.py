@@ -1,28 +1,32 @@
 #!/usr/bin/env python3
-"""Benchmark of the GB300 stress solve on the city-block workload.
+"""Benchmark of the GB300 stress solve.
 
-One step = one complete stress solve of a structure: K assembled from the bonds, the aggregation
-multigrid built, AMG-preconditioned CG to ||r|| <= rtol ||f|| (cold start), and every bond's
-fibre-stress check with the failure set (the reference's assemble + solve + judge of
-core/src/stress/stress.cpp). The workload is the city block: seeded random towers of 5-40 storeys
-of 0.5 m voxels in four materials (concrete, steel, masonry, wood, each +-20 %), pre-scored into
-fragments; gravity loads; FP64 PCG to rtol 1e-8.
+Default (--workload serve): the serving configuration the metric is quoted on. A seeded Poisson
+stream of solve requests (5,000/s; sizes log-normal, median 500 fragments, 10-50,000; 30 % repeats
+of a recent structure with 1-5 % of its bonds removed, warm-started) through the library's server:
+each request's K assembled (or downdated in place), its multigrid built, PCG to rel. residual 1e-6
+under the mixed-precision policy, and every bond's fibre-stress check. One step = 1000 requests.
 
-  value   solves/s with the graph resident on the device (device f / u / outputs)
-  e2e     solves/s through the C ABI with host buffers: graph upload, f in, u, phi, modes and
-          the failure list out, every step
-  roofline  the conjugate-gradient SpMV (FP64 K), timed live with CUDA events on the problem's
-          stream over the timed region, against the measured HBM copy bandwidth
-  cpu_baseline  the oracle (a C restatement of the reference's solve, OpenMP) on the host's cores,
-          one solve of the same graph
+  value   solves/s with the requests' graphs and loads already in device memory
+  e2e     solves/s of the same stream from host arrays through the C ABI (graph and load copied in,
+          results out), the headline against the reference arm
+  p50/p99 request latency (submission -> result), also at 70 % of the measured capacity
+  plain_fp64_per_request  the plain FP64 drop-in, one request after another (FP64 PCG per
+          structure), over every eighth structure of the same stream with all its repeats
+  cpu_baseline  the oracle (a C restatement of the reference's solve) on the host's cores, one
+          single-threaded process per core (the reference's one small graph per pool thread)
+
+--workload city: one complete solve of the city block per step (seeded towers of 5-40 storeys,
+four jittered materials; FP64 PCG to rtol 1e-8), value device-resident, e2e through the C ABI with
+host buffers, and the conjugate-gradient SpMV's roofline timed live with CUDA events (launches
+that did work) against the measured HBM bandwidth and this GPU's measured FP64 FMA rate.
 
 Launch: python bench.py [--gpus N --steps K --warmup W] (N > 1 under torchrun: one replica per
-GPU, each solving its own seeded city block; value = all ranks' solves / the slowest rank's time).
---workload batch | serve runs the batched solve or the serving loop instead (one JSON line with
-solves/s, latency percentiles and the plain FP64 per-request rate on the same requests).
---workload cascade runs the judge's break rounds of the city block (svxg_cascade) per step.
+GPU, each with its own seeded stream or city block; value = all ranks' solves / the slowest rank's
+time). --workload batch | cascade | sections | pieces run the batched solve, the judge's break
+rounds, bonds from voxel faces and loose pieces' break rounds.
 --impl reference times the reference's CPU implementation of the path (the oracle port on every
-host thread) on the same workload and prints the same JSON line.
+host core) on the same workload and prints the same JSON line.
 """
 from __future__ import annotations
 
@@ -130,6 +134,9 @@ def run_reference(args, rank: int, world: int):
     """The reference's CPU implementation of the path: the oracle port, every host thread."""
     if rank != 0:
         return
+    if args.workload == "serve":
+        run_reference_serve(args, world)
+        return
     import oracle
     from opus_destruct_2_gb300.graph import StressOptions
     nodes, bonds, f, mats, desc = workload(args, 0)
@@ -182,31 +189,235 @@ def cpu_baseline(args, nodes, bonds, f, mats) -> dict:
                       f"{res.iters} PCG iterations"}
 
 
+def _cpu_serve_init():
+    import oracle
+    oracle.set_threads(1)
+
+
+def _cpu_serve_noop(_):
+    return 0
+
+
+def _cpu_serve_run(job):
+    """One structure's requests on the CPU, in arrival order: the first assembled and solved cold,
+    each repeat removing its bonds and solving warm on the kept problem (the oracle restatement, one
+    thread), each judged. Returns (requests done, converged)."""
+    import oracle
+    from opus_destruct_2_gb300.graph import StressOptions, default_materials
+    nodes, bonds, f, removals, rtol = job
+    P = oracle.Port(nodes, bonds, default_materials())
+    P.assemble(StressOptions())
+    u, res = P.solve(f, rtol=rtol, maxit=2000)
+    P.judge(u)
+    done, conv = 1, int(res.converged)
+    for rm in removals:
+        for b in rm:
+            P.remove_bond(int(b))
+        u, res = P.solve(f, u=u, rtol=rtol, maxit=2000, warm=True)
+        P.judge(u)
+        done += 1
+        conv += int(res.converged)
+    return done, conv
+
+
+def cpu_jobs(stream, indices, rtol: float) -> dict:
+    """The requests `indices` grouped by structure (a structure's new request, then its repeats'
+    removals, in arrival order): {structure id: job}."""
+    jobs = {}
+    for k in indices:
+        kind, sid, g, rm = stream.plan[k]
+        if kind == "new":
+            nodes, bonds, f = stream.geoms[g]
+            jobs[sid] = (nodes, bonds, f, [], rtol)
+        elif sid in jobs:
+            jobs[sid][3].append(rm)
+    return jobs
+
+
+def cpu_pool(cores: int):
+    import multiprocessing as mp
+    pool = mp.get_context("spawn").Pool(cores, initializer=_cpu_serve_init)
+    pool.map(_cpu_serve_noop, range(cores))  # (workers up)
+    return pool
+
+
+def cpu_serve(pool, job_list) -> tuple:
+    """The reference's arrangement for many small graphs (world_pieces.cpp:1460-1463): one graph per
+    thread, all cores at once - here one single-threaded oracle process per core, a structure's
+    requests on one process. Returns (requests, converged, seconds)."""
+    t0 = time.perf_counter()
+    out = list(pool.imap_unordered(_cpu_serve_run, job_list, chunksize=1))
+    return sum(o[0] for o in out), sum(o[1] for o in out), time.perf_counter() - t0
+
+
+SERVE_DESC = ("serving: Poisson stream of {req} requests at {rate:g}/s, sizes log-normal (median 500 fragments, "
+              "10-50,000), half free pieces (inertial relief, pinned) and half ground-supported, 30% repeats of "
+              "one of the 256 latest structures with 1-5% of its bonds removed (warm start), 40 GB admission "
+              "budget, rel. residual {rtol:g}")
+
+
+def _serve_bytes(stream, way: str) -> int:
+    """Bytes a host-input run copies per stream: graph records, materials and load in (new), load
+    and removal list in (repeat); the request's result out (64 bytes; no u, no failure list)."""
+    from opus_destruct_2_gb300.graph import MATERIAL_DTYPE
+    tot = 0
+    for kind, sid, g, rm in stream.plan:
+        nodes, bonds, f = stream.geoms[g]
+        if way == "h2d":
+            tot += f.nbytes + (nodes.nbytes + bonds.nbytes + len(stream.mats) * MATERIAL_DTYPE.itemsize
+                               if kind == "new" else 4 * len(rm))
+        else:
+            tot += 64
+    return tot
+
+
+def run_serve(args, rank: int, world: int):
+    """The serving configuration: a Poisson stream of solve requests through the server (slots
+    overlap requests on the device, queued new requests run in batches, kept batches serve their
+    structures' repeats), each request's graph assembled, solved to rtol 1e-6 and judged. One step
+    = 1000 requests of the stream (steps x 1000 in all); warm-up = 100 requests a warm-up step on
+    the same server before the timed stream.
+
+      value   solves/s with every request's graph, materials and load already in device memory
+              (svxg_server_submit_device)
+      e2e     solves/s of the same stream from host arrays (svxg_server_submit / _repeat)
+      plain   the plain FP64 drop-in per request (one StressProblem at a time, FP64 PCG) over every
+              eighth structure of the same stream with all its repeats
+      cpu_baseline  the oracle on the host's cores (one single-threaded process per core, the
+              reference's arrangement for many small graphs) over the first requests of the stream
+    """
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+    import torch
+    from opus_destruct_2_gb300 import load_library, workloads
+    from opus_destruct_2_gb300.graph import PRECISION_FP64, PRECISION_MIXED
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    L = load_library()
+    L.svxg_launch_count.restype = ctypes.c_int64
+    prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    requests = 1000 * args.steps
+    stream = workloads.Stream(requests=requests, rate=args.rate, seed=args.seed + 9 + rank)
+    staged = workloads.DeviceGeometries(stream, local)
+    kw = dict(workers=args.workers, precision=prec, rtol=args.rtol, warmup=100 * args.warmup)
+    if args.batch_graphs is not None:
+        kw["batching"] = (args.batch_graphs, 20000, 65536)
+    # value: device-resident inputs
+    if dist is not None:
+        dist.barrier()
+    clocks = Clocks(local)
+    l0 = L.svxg_launch_count()
+    dev = workloads.serve_stream(stream, inputs="device", staged=staged, **kw)
+    launches = L.svxg_launch_count() - l0
+    clk = clocks.stop()
+    # e2e: host inputs, the same stream
+    host = workloads.serve_stream(stream, inputs="host", **kw)
+    # latency without a growing queue: the first quarter of the stream offered at 70 % of capacity
+    sustained = 0.7 * dev["solves_per_s"]
+    at70 = None
+    if sustained < args.rate:
+        at70 = workloads.serve_stream(stream, inputs="device", staged=staged, rate=sustained,
+                                      indices=range(max(1000, requests // 4)), **kw)
+    plain = workloads.plain_stream(stream, stream.subset(8), rtol=args.rtol)
+    wall = max_over_ranks(dev["wall_s"], dist, "cpu")
+    fewest = -max_over_ranks(-dev["completed"], dist, "cpu")  # (the fewest completed over ranks)
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        jobs = list(cpu_jobs(stream, range(min(requests, 2000)), args.rtol).values())
+        with cpu_pool(cores) as pool:
+            done, conv, dt = cpu_serve(pool, jobs)
+        cpu = {"value": done / dt, "unit": "solves/s", "cores": cores, "kind": "port", "converged": conv,
+               "sample": f"the structures of the first 2000 requests of the same stream with their repeats "
+                         f"({done} requests), one single-threaded oracle process per core (the reference's one "
+                         f"small graph per pool thread); {dt:.1f} s"}
+    keys = ("solves_per_s", "p50_ms", "p99_ms", "new_p50_ms", "new_p99_ms", "repeat_p50_ms", "repeat_p99_ms",
+            "p99_ms_8k_12k_dof", "requests_8k_12k_dof", "offered_rate", "completed", "failed_or_unconverged",
+            "batches", "batched_requests", "pcg_iters_mean")
+    line = {
+        "metric": METRIC, "value": world * fewest / wall, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if prec == PRECISION_FP64 else "f32+f64", "data": "synthetic",
+        "config": {"workload": SERVE_DESC.format(req=requests, rate=args.rate, rtol=args.rtol),
+                   "requests": requests, "workers": args.workers, "rtol": args.rtol,
+                   "precision": ("fp64" if prec == PRECISION_FP64 else
+                                 "mixed policy: fp32 inner sequences from 65,536 free nodes alone, the fp64 "
+                                 "sequence with the fp32 V-cycle below and in batches"),
+                   "step": "1000 requests of the stream: each assembled (or bonds removed in place), solved, "
+                           "judged",
+                   "l2": "the stream's requests together exceed L2 (tens of GB admitted)",
+                   "parallelism": f"replicas x{world}, {args.workers} server slots"},
+        "p50_ms": dev["p50_ms"], "p99_ms": dev["p99_ms"],
+        "block_row_iterations_per_s": world * dev["block_row_iterations_per_s"],
+        "serve": {k: dev[k] for k in keys}, "serve_at_70pct": ({k: at70[k] for k in keys} if at70 else None),
+        "plain_fp64_per_request": plain, "vs_plain_fp64": dev["solves_per_s"] / plain["solves_per_s"],
+        "e2e": {"value": world * host["solves_per_s"], "unit": "solves/s",
+                "h2d_bytes_per_step": int(_serve_bytes(stream, "h2d") * 1000 / requests),
+                "d2h_bytes_per_step": int(_serve_bytes(stream, "d2h") * 1000 / requests),
+                "p50_ms": host["p50_ms"], "p99_ms": host["p99_ms"]},
+        "gpu_launches": int(launches),
+        "roofline": None,
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    if clk is not None:
+        line["clocks"] = clk
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_serve(args, world: int):
+    """The serving stream on the reference's CPU path: the oracle port on every host core, one
+    single-threaded process per core (the reference's one small graph per pool thread), each
+    structure's requests in arrival order on one process. Step i: the structures s of the stream
+    with s mod (warmup + steps) = i, with all their requests; the first `warmup` steps untimed."""
+    from opus_destruct_2_gb300 import workloads
+    requests = 1000 * args.steps
+    stream = workloads.Stream(requests=requests, rate=args.rate, seed=args.seed + 9)
+    jobs = cpu_jobs(stream, range(requests), args.rtol)
+    cores = os.cpu_count() or 1
+    k_all = args.warmup + args.steps
+    done = conv = 0
+    secs = 0.0
+    with cpu_pool(cores) as pool:
+        for step in range(k_all):
+            part = [j for sid, j in jobs.items() if sid % k_all == step]
+            d, c, dt = cpu_serve(pool, part)
+            if step >= args.warmup:
+                done, conv, secs = done + d, conv + c, secs + dt
+    value = done / secs
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": SERVE_DESC.format(req=requests, rate=args.rate, rtol=args.rtol),
+                   "requests": requests, "rtol": args.rtol, "timed_requests": done, "converged": conv},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
+                         "sample": f"each step: the structures of the stream in one residue class of "
+                                   f"{k_all} with all their requests ({done} timed requests in all), one "
+                                   f"single-threaded oracle process per core (the reference tree is not on "
+                                   f"this machine: the oracle's C restatement)"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_many(args, rank: int, world: int):
-    """The batched solve or the serving loop (opus_destruct_2_gb300/workloads.py) on this GPU."""
+    """The batched solve (opus_destruct_2_gb300/workloads.py) on this GPU."""
     # (more hardware queues for the server's streams; read when the CUDA context is created)
     os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     from opus_destruct_2_gb300 import workloads
     from opus_destruct_2_gb300.graph import PRECISION_FP64, PRECISION_MIXED
     prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
     clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
-    if args.workload == "batch":
-        r = workloads.batch(count=args.graphs, workers=args.workers, precision=prec, rtol=1e-6)
-        desc = (f"batch: {args.graphs} fragment graphs, log-normal sizes (median 300, 10-20,000), half free pieces "
-                f"with inertial relief, half ground-supported, gravity + one impact load; rtol 1e-6")
-    else:
-        r = workloads.serve(requests=args.requests, rate=args.rate, workers=args.workers, precision=prec, rtol=1e-6)
-        desc = (f"serve: Poisson stream of {args.requests} requests at {args.rate:g}/s, sizes log-normal (median 500, "
-                f"max 50,000), 30% repeats of recent structures with 1-5% of bonds removed (warm start), 40 GB "
-                f"admission budget; rtol 1e-6")
-        # the same stream offered at 70 % of the rate just served: latency without a growing queue
-        sustained = 0.7 * r["solves_per_s"]
-        if sustained < args.rate:
-            r2 = workloads.serve(requests=min(args.requests, int(20 * sustained)), rate=sustained, workers=args.workers,
-                                 precision=prec, rtol=1e-6, plain_sample=0)
-            r["at_70pct_of_capacity"] = {k: r2[k] for k in ("offered_rate", "requests", "solves_per_s", "p50_ms",
-                                                             "p99_ms", "repeat_p50_ms", "repeat_p99_ms", "new_p50_ms",
-                                                             "new_p99_ms", "p99_ms_8k_12k_dof")}
+    r = workloads.batch(count=args.graphs, workers=args.workers, precision=prec, rtol=args.rtol)
+    desc = (f"batch: {args.graphs} fragment graphs, log-normal sizes (median 300, 10-20,000), half free pieces "
+            f"with inertial relief, half ground-supported, gravity + one impact load; rtol {args.rtol:g}")
     clk = clocks.stop()
     if rank != 0:
         return
@@ -217,7 +428,7 @@ def run_many(args, rank: int, world: int):
         "config": {"workload": desc, "workers": args.workers,
                    "precision": ("fp64" if prec == PRECISION_FP64 else
                                  "mixed (fp32 inner sequences from 65536 free nodes; fp64 sequence below)")},
-        "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"], args.workload: r,
+        "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"], "batch": r,
         "vs_plain_fp64_per_request": r["solves_per_s"] / r["plain_fp64_per_request_solves_per_s"],
         "roofline": None,
     }
@@ -467,8 +678,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["city", "tower", "batch", "serve", "cascade", "sections", "pieces"],
-                    default="city")
+    ap.add_argument("--workload", choices=["serve", "city", "tower", "batch", "cascade", "sections", "pieces"],
+                    default="serve")
+    ap.add_argument("--batch-graphs", type=int, default=None, help="serve: graphs a batch at most (1: no batching)")
     ap.add_argument("--fragility", type=float, default=1.0, help="cascade: strength divisor")
     ap.add_argument("--requests", type=int, default=20000, help="serve: requests in the stream")
     ap.add_argument("--rate", type=float, default=5000.0, help="serve: Poisson arrival rate (requests/s)")
@@ -476,12 +688,17 @@ def main():
     ap.add_argument("--workers", type=int, default=16, help="batch / serve: server slots")
     ap.add_argument("--lots", type=int, default=8)
     ap.add_argument("--seed", type=int, default=2)
-    ap.add_argument("--rtol", type=float, default=1e-8)
+    ap.add_argument("--rtol", type=float, default=None, help="default: 1e-6 serving and batch, 1e-8 otherwise")
     ap.add_argument("--maxit", type=int, default=500)
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default=None,
+                    help="default: mixed (the policy) serving, fp64 otherwise")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.rtol is None:
+        args.rtol = 1e-6 if args.workload in ("serve", "batch") else 1e-8
+    if args.precision is None:
+        args.precision = "mixed" if args.workload == "serve" else "fp64"
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -490,7 +707,10 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
-    if args.workload in ("batch", "serve"):
+    if args.workload == "serve":
+        run_serve(args, rank, world)
+        return
+    if args.workload == "batch":
         run_many(args, rank, world)
         return
     if args.workload == "pieces":

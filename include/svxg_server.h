@@ -12,9 +12,16 @@
  * the device) and records the result under the request's ticket. A new structure is admitted
  * when the bytes of the resident structures, of the requests running and of its own estimate
  * fit in the budget; resident structures no request is using are evicted, least recently used
- * first, to make room. Results are those of the single-problem entry points (svxg.h) for the
- * same graph, load and options, bit for bit: every request runs the same kernels in the same
- * order on its own buffers.
+ * first, to make room.
+ *
+ * Batching: a slot that takes a new request also takes the new requests queued behind it with the
+ * same options (up to a number of graphs and of nodes, svxg_server_set_batching) and runs them as
+ * one problem (svxg_set_graphs: every launch covers the batch, each graph stops at its own
+ * target); a batch whose structures are kept stays resident as one problem (a bundle), and a
+ * repeat of one of them - with the repeats of other members queued behind it - removes its bonds
+ * in place and solves the bundle warm. A request run alone gives the single-problem entry points'
+ * result bit for bit; in a batch, every graph meets the same tolerance (||r_g|| <= rtol ||f_g||)
+ * and gives the same result within it.
  */
 #ifndef SVXG_SERVER_H
 #define SVXG_SERVER_H
@@ -40,13 +47,14 @@ typedef struct svxg_request_result {
   double pad;
 } svxg_request_result;
 
-/* Counters since creation (or the last reset). 96 bytes. */
+/* Counters since creation (or the last reset). 112 bytes. */
 typedef struct svxg_serving_stats {
   int64_t completed, failed, evictions, admission_waits;
   int64_t resident, resident_bytes, peak_bytes; /* structures kept, their bytes, peak admitted bytes */
   int64_t pad;
   double p50_ms, p99_ms, max_ms; /* request latency */
   double wall_s;                 /* first submission -> last completion */
+  int64_t batches, batched_requests; /* batches of new requests run, the requests in them */
 } svxg_serving_stats;
 
 /* A server on `device` with `workers` slots admitting up to `hbm_budget_bytes` of problem memory. */
@@ -73,6 +81,26 @@ int64_t svxg_server_submit_repeat(svxg_server* s, int64_t structure, const int32
                                   const double* f, int32_t n, double rtol, int32_t maxit, double fragility,
                                   double* u_out, int32_t* over_out);
 
+/* The same two submissions with the graph, the material table and the load in device memory of the
+ * server's device (svxg_set_graph_device), read when the request runs: they must stay valid and
+ * unchanged until the request is waited for. u_out may be device or host memory; over_out is host
+ * memory. */
+int64_t svxg_server_submit_device(svxg_server* s, int64_t structure, const svxg_node* nodes_dev, int32_t n,
+                                  const svxg_bond* bonds_dev, int32_t nb, const svxg_material* mats_dev,
+                                  const double* f_dev, const svxg_stress_options* opt, double rtol, int32_t maxit,
+                                  double fragility, double* u_out, int32_t* over_out);
+int64_t svxg_server_submit_repeat_device(svxg_server* s, int64_t structure, const int32_t* remove, int32_t nremove,
+                                         const double* f_dev, int32_t n, double rtol, int32_t maxit,
+                                         double fragility, double* u_out, int32_t* over_out);
+
+/* Batching of new requests: at most max_graphs graphs (1: none), each of at most max_graph_nodes
+ * nodes, max_nodes in all, per problem. Defaults 32, 20,000 and 65,536. */
+int svxg_server_set_batching(svxg_server* s, int32_t max_graphs, int32_t max_graph_nodes, int64_t max_nodes);
+/* hold != 0: slots finish what they run and take no new request (submissions queue); 0: they take
+ * the queue again - a caller that submits a frame's requests together and releases them gets them
+ * batched. Destroying the server runs what is queued, held or not. */
+int svxg_server_hold(svxg_server* s, int32_t hold);
+
 /* Blocks until the ticket's request has finished; its result is handed over once. */
 int svxg_server_wait(svxg_server* s, int64_t ticket, svxg_request_result* out);
 /* Blocks until every submitted request has finished. */
@@ -86,8 +114,10 @@ int64_t svxg_server_estimate_bytes(int32_t n, int32_t nb);
 int svxg_server_forget(svxg_server* s, int64_t structure);
 
 /* The batched solve: `count` independent graphs (arrays of per-graph pointers and sizes; one
- * material table), each assembled, solved from zero and judged as one request of `s`; returns
- * when all have finished. u_out and over_out (arrays of per-graph buffers) may be null. */
+ * material table), each assembled, solved from zero and judged as a request of `s`, all queued
+ * together (the slots held while they are submitted, then released: any earlier hold ends), so
+ * that the slots take them in batches; returns when all have finished. u_out and over_out (arrays
+ * of per-graph buffers) may be null. */
 int svxg_batch_solve(svxg_server* s, int32_t count, const svxg_node* const* nodes, const int32_t* n,
                      const svxg_bond* const* bonds, const int32_t* nb, const svxg_material* mats,
                      const double* const* f, const svxg_stress_options* opt, double rtol, int32_t maxit,

@@ -13,6 +13,7 @@
 #include <cstring>
 #include <deque>
 #include <list>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <thread>
@@ -42,6 +43,15 @@ struct Request {
   std::vector<int32_t> remove;
   std::vector<double> f;
   int32_t n = 0;
+  // a submission from device memory (svxg_server_submit_device / _repeat_device): the caller's
+  // arrays are read when the request runs, in place of the host copies above
+  const svxg_node* nodes_dev = nullptr;
+  const svxg_bond* bonds_dev = nullptr;
+  const svxg_material* mats_dev = nullptr;
+  const double* f_dev = nullptr;
+  int32_t nb_dev = 0;
+  int32_t nbonds() const { return nodes_dev ? nb_dev : int32_t(bonds.size()); }
+  const double* load() const { return f_dev ? f_dev : f.data(); }
   svxg_stress_options opt{};
   double rtol = 1e-6;
   int32_t maxit = -1;
@@ -61,11 +71,26 @@ struct Request {
   svxg_piece_result* piece_out = nullptr;
 };
 
+// New structures solved together as one problem (svxg_set_graphs) and kept for their repeats: the
+// problem holds every member's K, the batch's multigrid and last solution; a repeat of a member
+// removes its bonds in place (offset into the batch) and solves the batch warm with that member's
+// new load. members[g]: graph g's structure id (-1: a one-shot request or a dropped structure).
+struct Bundle {
+  svxg_problem* p = nullptr;
+  std::vector<int64_t> members;
+  std::vector<int32_t> n, nb;
+  std::vector<int64_t> node_off, bond_off;
+  int32_t live = 0;
+  int64_t bytes = 0;
+};
+
 struct Resident {
   svxg_problem* p = nullptr;
   int64_t bytes = 0;
   bool forget = false;
   std::list<int64_t>::iterator lru;
+  std::shared_ptr<Bundle> bundle;  // (a member of a batch: p is the bundle's problem, bytes 0)
+  int32_t member = -1;
 };
 
 // A new structure's device bytes before it exists, from its sizes: K (one diagonal block per
@@ -155,9 +180,54 @@ struct svxg_server {
   bool any = false;
   bool blocking = false;
   Slot admin;  // (lent to problems released outside a slot: forget, destroy)
+  // batching of new requests (svxg_server_set_batching): at most batch_graphs graphs of at most
+  // batch_graph_nodes nodes each and batch_nodes in all go into one problem
+  int32_t batch_graphs = 32;
+  int32_t batch_graph_nodes = 20000;
+  int64_t batch_nodes = 65536;
+  int64_t batches = 0, batched_requests = 0;
+  bool hold = false;  // (svxg_server_hold: slots take no new work)
 };
 
 namespace {
+
+// a bundle released (all its members gone): its problem back to the spares
+void release_bundle_locked(svxg_server* S, Bundle& b, const Slot& slot) {
+  if (!b.p) return;
+  slot.lend(b.p);
+  svxg_release(b.p);
+  S->spare.push_back(b.p);
+  S->resident_bytes -= b.bytes;
+  b.p = nullptr;
+  b.bytes = 0;
+}
+
+// resident structure `it` no longer kept (evicted, forgotten, replaced or failed): a single
+// problem goes back to the spares; a bundle member is dropped, and the bundle with its last member
+void drop_resident_locked(svxg_server* S, std::unordered_map<int64_t, Resident>::iterator it, const Slot& slot) {
+  Resident& r = it->second;
+  if (r.bundle) {
+    Bundle& b = *r.bundle;
+    if (r.member >= 0 && r.member < int32_t(b.members.size()) && b.members[size_t(r.member)] == it->first) {
+      b.members[size_t(r.member)] = -1;
+      --b.live;
+    }
+    if (b.live <= 0) release_bundle_locked(S, b, slot);
+  } else {
+    slot.lend(r.p);
+    svxg_release(r.p);
+    S->spare.push_back(r.p);
+    S->resident_bytes -= r.bytes;
+  }
+  S->lru.erase(r.lru);
+  S->resident.erase(it);
+}
+
+bool bundle_running_locked(const svxg_server* S, const Bundle& b) {
+  for (int64_t m : b.members)
+    if (m >= 0 && S->running_structures.count(m)) return true;
+  return false;
+}
 
 void evict_locked(svxg_server* S, int64_t need, const Slot& slot) {
   for (auto it = S->lru.begin(); it != S->lru.end() && S->resident_bytes + S->running_bytes + need > S->budget;) {
@@ -166,12 +236,25 @@ void evict_locked(svxg_server* S, int64_t need, const Slot& slot) {
       ++it;
       continue;
     }
-    slot.lend(r->second.p);
-    svxg_release(r->second.p);
-    S->spare.push_back(r->second.p);
-    S->resident_bytes -= r->second.bytes;
-    S->resident.erase(r);
-    it = S->lru.erase(it);
+    if (r->second.bundle) {
+      // (a bundle frees memory only as a whole: every member goes, unless one is running)
+      std::shared_ptr<Bundle> b = r->second.bundle;
+      if (bundle_running_locked(S, *b)) {
+        ++it;
+        continue;
+      }
+      for (int64_t m : std::vector<int64_t>(b->members)) {
+        auto q = S->resident.find(m);
+        if (m >= 0 && q != S->resident.end() && q->second.bundle == b) {
+          drop_resident_locked(S, q, slot);
+          ++S->evictions;
+        }
+      }
+      it = S->lru.begin();
+      continue;
+    }
+    ++it;
+    drop_resident_locked(S, r, slot);
     ++S->evictions;
   }
 }
@@ -218,7 +301,8 @@ int run_piece(svxg_problem* p, Request& q, svxg_request_result* res) {
 }
 
 int run_new(svxg_problem* p, Request& q, svxg_request_result* res) {
-  int e = svxg_set_graph(p, q.nodes.data(), q.n, q.bonds.data(), int32_t(q.bonds.size()), q.mats.data());
+  int e = q.nodes_dev ? svxg_set_graph_device(p, q.nodes_dev, q.n, q.bonds_dev, q.nb_dev, q.mats_dev)
+                      : svxg_set_graph(p, q.nodes.data(), q.n, q.bonds.data(), int32_t(q.bonds.size()), q.mats.data());
   if (e) return e;
   if (q.piece) return run_piece(p, q, res);
   int32_t ok = 0;
@@ -236,7 +320,7 @@ int run_new(svxg_problem* p, Request& q, svxg_request_result* res) {
     uo = u.data();
   }
   svxg_pcg_result r{};
-  e = solve_nodes_host(p->P, q.f.data(), uo, q.rtol, q.maxit, kCold, &r);
+  e = solve_nodes_host(p->P, q.load(), uo, q.rtol, q.maxit, kCold, &r);
   if (e) return e;
   res->iters = r.iters;
   res->converged = r.converged;
@@ -255,7 +339,7 @@ int run_repeat(svxg_problem* p, Request& q, svxg_request_result* res) {
     if (e) return e;
   }
   svxg_pcg_result r{};
-  const int e = solve_nodes_host(p->P, q.f.data(), q.u_out, q.rtol, q.maxit, kWarmResident, &r);
+  const int e = solve_nodes_host(p->P, q.load(), q.u_out, q.rtol, q.maxit, kWarmResident, &r);
   if (e) return e;
   res->warm = 1;
   res->iters = r.iters;
@@ -265,17 +349,178 @@ int run_repeat(svxg_problem* p, Request& q, svxg_request_result* res) {
   return judge_into(p, q, res);
 }
 
-// A request for structure s waits while another request for s runs: it parks in deferred[s]
-// and goes back to the head of the queue when that request finishes. (A repeat submitted after
-// its structure's first request therefore always finds it resident, unless it was evicted.)
-void release_to_spare_locked(svxg_server* S, std::unordered_map<int64_t, Resident>::iterator it, const Slot& slot) {
-  slot.lend(it->second.p);
-  svxg_release(it->second.p);
-  S->spare.push_back(it->second.p);
-  S->resident_bytes -= it->second.bytes;
-  S->lru.erase(it->second.lru);
-  S->resident.erase(it);
+// ---- batches -------------------------------------------------------------------------------
+
+bool same_options(const Request& a, const Request& b) {
+  if ((a.nodes_dev != nullptr) != (b.nodes_dev != nullptr)) return false;
+  if (a.rtol != b.rtol || a.maxit != b.maxit || a.fragility != b.fragility) return false;
+  if (std::memcmp(&a.opt, &b.opt, sizeof(a.opt)) != 0) return false;
+  if (a.nodes_dev) return a.mats_dev == b.mats_dev;
+  return a.mats.size() == b.mats.size() &&
+         std::memcmp(a.mats.data(), b.mats.data(), sizeof(svxg_material) * a.mats.size()) == 0;
 }
+
+bool batchable(const svxg_server* S, const Request& q) {
+  return S->batch_graphs > 1 && !q.repeat && !q.piece && q.n > 0 && q.n <= S->batch_graph_nodes;
+}
+
+// the failing bonds of graph g of a batch from the batch's ascending list (its own numbering)
+int32_t member_failures(const std::vector<int32_t>& over, int32_t n_over, int64_t b0, int64_t b1, int32_t* out) {
+  const auto first = std::lower_bound(over.begin(), over.begin() + n_over, int32_t(b0));
+  const auto last = std::lower_bound(first, over.begin() + n_over, int32_t(b1));
+  int32_t k = 0;
+  for (auto it = first; it != last; ++it, ++k)
+    if (out) out[k] = int32_t(*it - b0);
+  return k;
+}
+
+// New requests as one problem: graphs one after another, assembled and solved together (every
+// launch over the whole batch, each graph stopping at its own target), judged, and each request's
+// result (its u, failure list and count, rel. residual) taken out of the batch's.
+int run_batch(svxg_problem* p, std::vector<Request>& B, std::vector<svxg_request_result>& res, Bundle& shape) {
+  const int32_t count = int32_t(B.size());
+  const size_t cnt = static_cast<size_t>(count);
+  const bool dev = B[0].nodes_dev != nullptr;
+  std::vector<const svxg_node*> np(cnt);
+  std::vector<const svxg_bond*> bp(cnt);
+  std::vector<const double*> fp(cnt);
+  std::vector<double*> up(cnt);
+  std::vector<int32_t> n(cnt), nb(cnt);
+  for (size_t g = 0; g < cnt; ++g) {
+    const Request& q = B[g];
+    np[g] = dev ? q.nodes_dev : q.nodes.data();
+    bp[g] = dev ? q.bonds_dev : q.bonds.data();
+    fp[g] = q.load();
+    up[g] = q.u_out;
+    n[g] = q.n;
+    nb[g] = q.nbonds();
+  }
+  int e = dev ? svxg_set_graphs_device(p, count, np.data(), n.data(), bp.data(), nb.data(), B[0].mats_dev)
+              : svxg_set_graphs(p, count, np.data(), n.data(), bp.data(), nb.data(), B[0].mats.data());
+  if (e) return e;
+  shape.n = n;
+  shape.nb = nb;
+  shape.node_off = p->P.seg_node;
+  shape.bond_off = p->P.seg_bond;
+  int32_t ok = 0;
+  e = svxg_assemble(p, &B[0].opt, &ok);
+  if (e) return e;
+  if (!ok) {
+    for (auto& r : res) {
+      r.breakdown = 1;
+      r.rel_res = INFINITY;
+    }
+    return SVXG_OK;
+  }
+  svxg_pcg_result pr{};
+  e = batch_solve_loads(p->P, fp.data(), nullptr, up.data(), B[0].rtol, B[0].maxit, false, &pr);
+  if (e) return e;
+  std::vector<double> rel(cnt, 0.0);
+  std::vector<int32_t> conv(cnt, 0);
+  e = svxg_graph_results(p, count, rel.data(), conv.data());
+  if (e) return e;
+  std::vector<int32_t> over(size_t(std::max(p->P.nb, 1)));
+  int32_t n_over = 0;
+  e = svxg_utilization(p, B[0].fragility, nullptr, nullptr, over.data(), int32_t(over.size()), &n_over);
+  if (e) return e;
+  for (size_t g = 0; g < cnt; ++g) {
+    svxg_request_result& r = res[g];
+    r.iters = pr.iters;
+    r.breakdown = pr.breakdown;
+    r.converged = conv[g] && !pr.breakdown;
+    r.rel_res = pr.breakdown && !std::isfinite(pr.rel_res) ? INFINITY : rel[g];
+    r.failing = member_failures(over, n_over, shape.bond_off[g], shape.bond_off[g + 1], B[g].over_out);
+  }
+  return SVXG_OK;
+}
+
+// Repeats of members of one bundle (distinct members; member[i] is R[i]'s): every member's removals
+// in one in-place pass (offset into the batch), their new loads over theirs, the batch solved warm
+// from its last solution (members without a repeat start at their converged state), each request's
+// result.
+int run_bundle_repeats(Bundle& b, std::vector<Request>& R, const std::vector<int32_t>& member,
+                       std::vector<svxg_request_result>& res) {
+  svxg_problem* p = b.p;
+  const size_t count = b.members.size();
+  std::vector<int32_t> rm;
+  std::vector<const double*> fp(count, nullptr);
+  std::vector<double*> up(count, nullptr);
+  std::vector<uint8_t> take(count, 0);
+  for (size_t i = 0; i < R.size(); ++i) {
+    const size_t g = size_t(member[i]);
+    const Request& q = R[i];
+    if (q.n != b.n[g]) {
+      set_error("repeat request: node count differs from the resident structure's");
+      return SVXG_ERR_ARG;
+    }
+    for (int32_t k : q.remove) {
+      if (k < 0 || k >= b.nb[g]) {
+        set_error("repeat request: bond index out of range");
+        return SVXG_ERR_ARG;
+      }
+      rm.push_back(int32_t(b.bond_off[g] + k));
+    }
+    fp[g] = q.load();
+    up[g] = q.u_out;
+    take[g] = 1;
+  }
+  if (!rm.empty()) {
+    const int e = svxg_remove_bonds(p, rm.data(), int32_t(rm.size()));
+    if (e) return e;
+  }
+  svxg_pcg_result pr{};
+  int e = batch_solve_loads(p->P, fp.data(), take.data(), up.data(), R[0].rtol, R[0].maxit, true, &pr);
+  if (e) return e;
+  std::vector<double> rel(count, 0.0);
+  std::vector<int32_t> conv(count, 0);
+  e = svxg_graph_results(p, int32_t(count), rel.data(), conv.data());
+  if (e) return e;
+  std::vector<int32_t> over(size_t(std::max(p->P.nb, 1)));
+  int32_t n_over = 0;
+  e = svxg_utilization(p, R[0].fragility, nullptr, nullptr, over.data(), int32_t(over.size()), &n_over);
+  if (e) return e;
+  for (size_t i = 0; i < R.size(); ++i) {
+    const size_t g = size_t(member[i]);
+    svxg_request_result& r = res[i];
+    r.warm = 1;
+    r.iters = pr.iters;
+    r.breakdown = pr.breakdown;
+    r.converged = conv[g] && !pr.breakdown;
+    r.rel_res = pr.breakdown && !std::isfinite(pr.rel_res) ? INFINITY : rel[g];
+    r.failing = member_failures(over, n_over, b.bond_off[g], b.bond_off[g + 1], R[i].over_out);
+  }
+  return SVXG_OK;
+}
+
+// the structure ids a piece of work runs under (every live member of a bundle it uses)
+void mark_running_locked(svxg_server* S, const std::vector<int64_t>& ids) {
+  for (int64_t id : ids)
+    if (id >= 0) S->running_structures.insert(id);
+}
+
+// ... and their release: requests parked behind them go back to the head of the queue
+void unmark_running_locked(svxg_server* S, const std::vector<int64_t>& ids) {
+  bool requeued = false;
+  for (int64_t id : ids) {
+    if (id < 0) continue;
+    S->running_structures.erase(id);
+    auto d = S->deferred.find(id);
+    if (d != S->deferred.end()) {
+      for (auto it = d->second.rbegin(); it != d->second.rend(); ++it) S->queue.push_front(std::move(*it));
+      S->deferred.erase(d);
+      requeued = true;
+    }
+  }
+  if (requeued) S->cv_work.notify_all();
+}
+
+// ---- the slots ------------------------------------------------------------------------------
+// A request for structure s waits while another request for s runs (or for any member of s's
+// bundle): it parks in deferred[s] and goes back to the head of the queue when that one finishes.
+// (A repeat submitted after its structure's first request therefore always finds it resident,
+// unless it was evicted.)
+
+constexpr size_t kBatchScan = 512;  // queued requests a slot looks through to fill a batch
 
 void worker(svxg_server* S) {
   cudaSetDevice(S->device);
@@ -284,6 +529,10 @@ void worker(svxg_server* S) {
   svxg_problem* own = nullptr;
   for (;;) {
     Request q;
+    std::vector<Request> group;        // the requests run with q: a batch of new ones, or repeats on one bundle
+    std::vector<int32_t> gmember;      // (repeats on a bundle: each one's member, q's first)
+    std::shared_ptr<Bundle> bundle;
+    std::vector<int64_t> locks;        // structure ids held while this runs
     svxg_problem* p = nullptr;
     int64_t est = 0;
     bool keep = false, admitted = false;
@@ -291,7 +540,7 @@ void worker(svxg_server* S) {
     {
       std::unique_lock<std::mutex> lk(S->mu);
       for (;;) {
-        S->cv_work.wait(lk, [&] { return S->stop || !S->queue.empty(); });
+        S->cv_work.wait(lk, [&] { return S->stop || (!S->queue.empty() && !S->hold); });
         if (S->queue.empty()) break;
         q = std::move(S->queue.front());
         S->queue.pop_front();
@@ -302,19 +551,76 @@ void worker(svxg_server* S) {
         break;
       }
       if (q.ticket == 0) break;  // (stopped, nothing left)
-      if (q.structure >= 0) S->running_structures.insert(q.structure);
       if (q.repeat) {
         auto it = S->resident.find(q.structure);
         if (it == S->resident.end()) {
           set_error("repeat request: the structure is not resident");
           e = SVXG_ERR_STATE;
+          locks.push_back(q.structure);
+        } else if (it->second.bundle) {
+          // repeats of other members of the same bundle queued behind it join this solve
+          bundle = it->second.bundle;
+          gmember.push_back(it->second.member);
+          std::vector<uint8_t> taken(bundle->members.size(), 0);
+          taken[size_t(it->second.member)] = 1;
+          std::vector<Request> rest;
+          for (size_t scanned = 0; scanned < kBatchScan && !S->queue.empty(); ++scanned) {
+            Request r = std::move(S->queue.front());
+            S->queue.pop_front();
+            auto jt = r.repeat ? S->resident.find(r.structure) : S->resident.end();
+            if (jt != S->resident.end() && jt->second.bundle == bundle && !taken[size_t(jt->second.member)] &&
+                r.rtol == q.rtol && r.maxit == q.maxit && r.fragility == q.fragility) {
+              taken[size_t(jt->second.member)] = 1;
+              gmember.push_back(jt->second.member);
+              group.push_back(std::move(r));
+            } else {
+              rest.push_back(std::move(r));
+            }
+          }
+          for (auto rt = rest.rbegin(); rt != rest.rend(); ++rt) S->queue.push_front(std::move(*rt));
+          for (int64_t m : bundle->members)
+            if (m >= 0) {
+              locks.push_back(m);
+              auto mt = S->resident.find(m);
+              if (mt != S->resident.end()) {
+                S->lru.erase(mt->second.lru);
+                mt->second.lru = S->lru.insert(S->lru.end(), m);
+              }
+            }
+          p = bundle->p;
         } else {
           p = it->second.p;
           S->lru.erase(it->second.lru);
           it->second.lru = S->lru.insert(S->lru.end(), q.structure);
+          locks.push_back(q.structure);
         }
       } else {
-        est = estimate_bytes(q.n, int64_t(q.bonds.size()));
+        locks.push_back(q.structure);
+        est = estimate_bytes(q.n, int64_t(q.nbonds()));
+        if (batchable(S, q)) {
+          // further new requests with the same options join it as one problem
+          int64_t nodes = q.n;
+          std::unordered_set<int64_t> ids;
+          if (q.structure >= 0) ids.insert(q.structure);
+          std::vector<Request> rest;
+          for (size_t scanned = 0;
+               scanned < kBatchScan && !S->queue.empty() && int32_t(group.size()) + 1 < S->batch_graphs; ++scanned) {
+            Request r = std::move(S->queue.front());
+            S->queue.pop_front();
+            const bool fits = batchable(S, r) && nodes + r.n <= S->batch_nodes && same_options(q, r) &&
+                              (r.structure < 0 || (!ids.count(r.structure) && !S->running_structures.count(r.structure)));
+            if (fits) {
+              nodes += r.n;
+              if (r.structure >= 0) ids.insert(r.structure);
+              locks.push_back(r.structure);
+              est += estimate_bytes(r.n, int64_t(r.nbonds()));
+              group.push_back(std::move(r));
+            } else {
+              rest.push_back(std::move(r));
+            }
+          }
+          for (auto rt = rest.rbegin(); rt != rest.rend(); ++rt) S->queue.push_front(std::move(*rt));
+        }
         if (est > S->budget) {
           set_error("request exceeds the server's HBM budget");
           e = SVXG_ERR_NOMEM;
@@ -331,19 +637,27 @@ void worker(svxg_server* S) {
           admitted = true;
           S->peak = std::max(S->peak, S->resident_bytes + S->running_bytes);
           keep = q.structure >= 0;
-          if (keep) {
-            auto old = S->resident.find(q.structure);  // (resubmitted: the new graph replaces it)
-            if (old != S->resident.end()) release_to_spare_locked(S, old, slot);
-            if (!S->spare.empty()) {
-              p = S->spare.back();
-              S->spare.pop_back();
-            }
+          for (const Request& r : group) keep = keep || r.structure >= 0;
+          // (resubmitted structures: the new graph replaces the old)
+          for (int64_t id : locks) {
+            auto old = id >= 0 ? S->resident.find(id) : S->resident.end();
+            if (old != S->resident.end()) drop_resident_locked(S, old, slot);
+          }
+          if (keep && !S->spare.empty()) {
+            p = S->spare.back();
+            S->spare.pop_back();
           }
         }
       }
+      mark_running_locked(S, locks);
     }
-    svxg_request_result res{};
-    res.queue_ms = std::chrono::duration<double, std::milli>(Clock::now() - q.submitted).count();
+    // ---- run ----
+    const bool batch = !q.repeat && !group.empty();
+    group.insert(group.begin(), std::move(q));
+    std::vector<svxg_request_result> res(group.size());
+    const auto taken_at = Clock::now();
+    for (size_t i = 0; i < group.size(); ++i)
+      res[i].queue_ms = std::chrono::duration<double, std::milli>(taken_at - group[i].submitted).count();
     if (!e && slot_ok) e = slot_ok;
     if (!e && !p && !keep) {
       if (!own) e = create_bare(&own, S->device);
@@ -351,29 +665,63 @@ void worker(svxg_server* S) {
     } else if (!e && !p) {
       e = create_bare(&p, S->device);
     }
+    Bundle shape;
     if (!e) {
       slot.lend(p);
-      e = q.repeat ? run_repeat(p, q, &res) : run_new(p, q, &res);
+      if (bundle) {
+        e = run_bundle_repeats(*bundle, group, gmember, res);
+      } else if (batch) {
+        e = run_batch(p, group, res, shape);
+      } else {
+        e = group[0].repeat ? run_repeat(p, group[0], &res[0]) : run_new(p, group[0], &res[0]);
+      }
     }
-    res.status = e;
+    for (auto& r : res) r.status = e;
     {
       std::lock_guard<std::mutex> lk(S->mu);
       if (admitted) S->running_bytes -= est;
-      if (q.repeat) {
-        auto it = S->resident.find(q.structure);
+      if (bundle) {
+        const int64_t bb = bundle->p ? bundle->p->P.mem.bytes : 0;
+        S->resident_bytes += bb - bundle->bytes;
+        bundle->bytes = bb;
+        for (int64_t m : std::vector<int64_t>(bundle->members)) {
+          auto mt = m >= 0 ? S->resident.find(m) : S->resident.end();
+          // (a failed repeat: the whole bundle is dropped, its state unknown)
+          if (mt != S->resident.end() && (e || mt->second.forget)) drop_resident_locked(S, mt, slot);
+        }
+      } else if (group[0].repeat) {
+        auto it = S->resident.find(group[0].structure);
         if (it != S->resident.end()) {
           const int64_t b = it->second.p->P.mem.bytes;
           S->resident_bytes += b - it->second.bytes;
           it->second.bytes = b;
-          if (it->second.forget || e) release_to_spare_locked(S, it, slot);  // (a failed repeat: dropped)
+          if (it->second.forget || e) drop_resident_locked(S, it, slot);  // (a failed repeat: dropped)
         }
       } else if (keep && p) {
-        if (!e) {
+        if (!e && batch) {
+          auto b = std::make_shared<Bundle>(std::move(shape));
+          b->p = p;
+          b->bytes = p->P.mem.bytes;
+          b->members.assign(group.size(), -1);
+          for (size_t g = 0; g < group.size(); ++g) {
+            const int64_t id = group[g].structure;
+            if (id < 0) continue;
+            b->members[g] = id;
+            ++b->live;
+            Resident r;
+            r.p = p;
+            r.bundle = b;
+            r.member = int32_t(g);
+            r.lru = S->lru.insert(S->lru.end(), id);
+            S->resident[id] = r;
+          }
+          S->resident_bytes += b->bytes;
+        } else if (!e) {
           Resident r;
           r.p = p;
           r.bytes = p->P.mem.bytes;
-          r.lru = S->lru.insert(S->lru.end(), q.structure);
-          S->resident[q.structure] = r;
+          r.lru = S->lru.insert(S->lru.end(), group[0].structure);
+          S->resident[group[0].structure] = r;
           S->resident_bytes += r.bytes;
         } else {
           svxg_release(p);
@@ -382,19 +730,15 @@ void worker(svxg_server* S) {
       } else if (p && p == own) {
         svxg_release(own);
       }
-      S->peak = std::max(S->peak, S->resident_bytes + S->running_bytes);
-      if (q.structure >= 0) {
-        S->running_structures.erase(q.structure);
-        auto d = S->deferred.find(q.structure);
-        if (d != S->deferred.end()) {
-          for (auto it = d->second.rbegin(); it != d->second.rend(); ++it) S->queue.push_front(std::move(*it));
-          S->deferred.erase(d);
-          S->cv_work.notify_all();
-        }
+      if (batch) {
+        ++S->batches;
+        S->batched_requests += int64_t(group.size());
       }
+      S->peak = std::max(S->peak, S->resident_bytes + S->running_bytes);
+      unmark_running_locked(S, locks);
       S->cv_mem.notify_all();
     }
-    record(S, q, res);
+    for (size_t i = 0; i < group.size(); ++i) record(S, group[i], res[i]);
     pool_trim(size_t(1) << 30);  // (this slot's pool keeps at most 1 GiB it is not using)
   }
   if (own) svxg_problem_destroy(own);
@@ -458,7 +802,10 @@ void svxg_server_destroy(svxg_server* S) {
   }
   S->cv_work.notify_all();
   for (auto& t : S->threads) t.join();
+  // (the members of a bundle share its problem: each problem is destroyed once)
+  std::unordered_set<svxg_problem*> gone;
   for (auto& kv : S->resident) {
+    if (!kv.second.p || !gone.insert(kv.second.p).second) continue;
     S->admin.lend(kv.second.p);
     svxg_problem_destroy(kv.second.p);
   }
@@ -515,6 +862,74 @@ int64_t svxg_server_submit_repeat(svxg_server* S, int64_t structure, const int32
   return submit(S, std::move(q));
 }
 
+int64_t svxg_server_submit_device(svxg_server* S, int64_t structure, const svxg_node* nodes_dev, int32_t n,
+                                  const svxg_bond* bonds_dev, int32_t nb, const svxg_material* mats_dev,
+                                  const double* f_dev, const svxg_stress_options* opt, double rtol, int32_t maxit,
+                                  double fragility, double* u_out, int32_t* over_out) {
+  if (!S || n < 0 || nb < 0 || !mats_dev || (n > 0 && (!nodes_dev || !f_dev)) || (nb > 0 && !bonds_dev)) {
+    set_error("svxg_server_submit_device: bad arguments");
+    return SVXG_ERR_ARG;
+  }
+  Request q;
+  q.structure = structure;
+  q.n = n;
+  q.nodes_dev = nodes_dev;
+  q.bonds_dev = bonds_dev;
+  q.nb_dev = nb;
+  q.mats_dev = mats_dev;
+  q.f_dev = f_dev;
+  q.opt = opt ? *opt : svxg_default_options();
+  q.rtol = rtol;
+  q.maxit = maxit;
+  q.fragility = fragility;
+  q.u_out = u_out;
+  q.over_out = over_out;
+  return submit(S, std::move(q));
+}
+
+int64_t svxg_server_submit_repeat_device(svxg_server* S, int64_t structure, const int32_t* remove, int32_t nremove,
+                                         const double* f_dev, int32_t n, double rtol, int32_t maxit,
+                                         double fragility, double* u_out, int32_t* over_out) {
+  if (!S || structure < 0 || nremove < 0 || (nremove > 0 && !remove) || n < 0 || (n > 0 && !f_dev)) {
+    set_error("svxg_server_submit_repeat_device: bad arguments");
+    return SVXG_ERR_ARG;
+  }
+  Request q;
+  q.structure = structure;
+  q.repeat = true;
+  q.n = n;
+  q.remove.assign(remove, remove + nremove);
+  q.f_dev = f_dev;
+  q.rtol = rtol;
+  q.maxit = maxit;
+  q.fragility = fragility;
+  q.u_out = u_out;
+  q.over_out = over_out;
+  return submit(S, std::move(q));
+}
+
+int svxg_server_set_batching(svxg_server* S, int32_t max_graphs, int32_t max_graph_nodes, int64_t max_nodes) {
+  if (!S || max_graphs < 1 || max_graph_nodes < 0 || max_nodes < 0) {
+    set_error("svxg_server_set_batching: bad arguments");
+    return SVXG_ERR_ARG;
+  }
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->batch_graphs = max_graphs;
+  S->batch_graph_nodes = max_graph_nodes;
+  S->batch_nodes = max_nodes;
+  return SVXG_OK;
+}
+
+int svxg_server_hold(svxg_server* S, int32_t hold) {
+  if (!S) return SVXG_ERR_ARG;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->hold = hold != 0;
+  }
+  S->cv_work.notify_all();
+  return SVXG_OK;
+}
+
 int svxg_server_wait(svxg_server* S, int64_t ticket, svxg_request_result* out) {
   if (!S || ticket <= 0) return SVXG_ERR_ARG;
   std::unique_lock<std::mutex> lk(S->mu);
@@ -546,6 +961,8 @@ int svxg_server_stats(svxg_server* S, svxg_serving_stats* st) {
   st->resident = int64_t(S->resident.size());
   st->resident_bytes = S->resident_bytes;
   st->peak_bytes = S->peak;
+  st->batches = S->batches;
+  st->batched_requests = S->batched_requests;
   std::vector<double> l = S->latencies;
   if (!l.empty()) {
     std::sort(l.begin(), l.end());
@@ -563,6 +980,7 @@ int svxg_server_reset_stats(svxg_server* S) {
   std::lock_guard<std::mutex> lk(S->mu);
   S->latencies.clear();
   S->completed = S->failed = S->evictions = S->admission_waits = 0;
+  S->batches = S->batched_requests = 0;
   S->peak = S->resident_bytes + S->running_bytes;
   S->any = false;
   return SVXG_OK;
@@ -581,7 +999,7 @@ int svxg_server_forget(svxg_server* S, int64_t structure) {
     it->second.forget = true;
     return SVXG_OK;
   }
-  release_to_spare_locked(S, it, S->admin);
+  drop_resident_locked(S, it, S->admin);
   S->cv_mem.notify_all();
   return SVXG_OK;
 }
@@ -597,6 +1015,7 @@ int svxg_batch_solve(svxg_server* S, int32_t count, const svxg_node* const* node
   }
   std::vector<int64_t> t(size_t(count), 0);
   int err = SVXG_OK;
+  svxg_server_hold(S, 1);  // (the graphs queue together, so that slots take them in batches)
   for (int32_t i = 0; i < count; ++i) {
     t[size_t(i)] = svxg_server_submit(S, -1, nodes[i], n[i], bonds[i], nb[i], mats, f[i], opt, rtol, maxit, fragility,
                                       u_out ? u_out[i] : nullptr, over_out ? over_out[i] : nullptr);
@@ -605,6 +1024,7 @@ int svxg_batch_solve(svxg_server* S, int32_t count, const svxg_node* const* node
       break;
     }
   }
+  svxg_server_hold(S, 0);
   for (int32_t i = 0; i < count; ++i) {
     if (t[size_t(i)] <= 0) break;
     svxg_request_result r{};

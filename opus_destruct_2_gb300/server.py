@@ -30,7 +30,8 @@ class RequestResult(ctypes.Structure):
 class ServingStats(ctypes.Structure):
     _fields_ = [("completed", c_i64), ("failed", c_i64), ("evictions", c_i64), ("admission_waits", c_i64),
                 ("resident", c_i64), ("resident_bytes", c_i64), ("peak_bytes", c_i64), ("pad", c_i64),
-                ("p50_ms", c_f64), ("p99_ms", c_f64), ("max_ms", c_f64), ("wall_s", c_f64)]
+                ("p50_ms", c_f64), ("p99_ms", c_f64), ("max_ms", c_f64), ("wall_s", c_f64),
+                ("batches", c_i64), ("batched_requests", c_i64)]
 
 
 _bound = False
@@ -48,6 +49,12 @@ def _bind():
                                        c_f64, c_vp, c_vp]),
         "svxg_server_submit_repeat": (c_i64, [c_vp, c_i64, c_vp, c_i32, c_vp, c_i32, c_f64, c_i32, c_f64, c_vp,
                                               c_vp]),
+        "svxg_server_submit_device": (c_i64, [c_vp, c_i64, c_vp, c_i32, c_vp, c_i32, c_vp, c_vp, c_vp, c_f64,
+                                              c_i32, c_f64, c_vp, c_vp]),
+        "svxg_server_submit_repeat_device": (c_i64, [c_vp, c_i64, c_vp, c_i32, c_vp, c_i32, c_f64, c_i32, c_f64,
+                                                     c_vp, c_vp]),
+        "svxg_server_set_batching": (c_i32, [c_vp, c_i32, c_i32, c_i64]),
+        "svxg_server_hold": (c_i32, [c_vp, c_i32]),
         "svxg_server_wait": (c_i32, [c_vp, c_i64, c_vp]),
         "svxg_server_drain": (c_i32, [c_vp]),
         "svxg_server_stats": (c_i32, [c_vp, c_vp]),
@@ -138,6 +145,40 @@ class Server:
         _check(int(t) if t < 0 else 0)
         self._keep[int(t)] = (u, over)
         return int(t)
+
+    def submit_device(self, nodes_dev: int, n: int, bonds_dev: int, nb: int, mats_dev: int, f_dev: int,
+                      structure: int = -1, opt: StressOptions | None = None, rtol: float = 1e-6, maxit: int = -1,
+                      fragility: float = 1.0, u_dev: int | None = None) -> int:
+        """A new graph whose records, material table and load are in device memory (addresses that
+        stay valid until waited for); u_dev: where the solution goes (device address) or None."""
+        t = self._L.svxg_server_submit_device(self._h, int(structure), c_vp(nodes_dev), int(n), c_vp(bonds_dev),
+                                              int(nb), c_vp(mats_dev), c_vp(f_dev),
+                                              ctypes.byref(opt) if opt is not None else None, float(rtol),
+                                              int(maxit), float(fragility), c_vp(u_dev) if u_dev else None, None)
+        _check(int(t) if t < 0 else 0)
+        self._keep[int(t)] = (None, None)
+        return int(t)
+
+    def submit_repeat_device(self, structure: int, remove, f_dev: int, n: int, rtol: float = 1e-6,
+                             maxit: int = -1, fragility: float = 1.0, u_dev: int | None = None) -> int:
+        """A repeat of resident `structure` with its load in device memory."""
+        remove = np.ascontiguousarray(remove, dtype=np.int32)
+        t = self._L.svxg_server_submit_repeat_device(self._h, int(structure), ptr(remove), len(remove), c_vp(f_dev),
+                                                     int(n), float(rtol), int(maxit), float(fragility),
+                                                     c_vp(u_dev) if u_dev else None, None)
+        _check(int(t) if t < 0 else 0)
+        self._keep[int(t)] = (None, None)
+        return int(t)
+
+    def set_batching(self, max_graphs: int = 32, max_graph_nodes: int = 20000, max_nodes: int = 65536):
+        """New requests queued together run as one problem: at most max_graphs graphs (1: none) of at
+        most max_graph_nodes nodes, max_nodes in all."""
+        _check(self._L.svxg_server_set_batching(self._h, int(max_graphs), int(max_graph_nodes), int(max_nodes)))
+
+    def hold(self, on: bool = True):
+        """Slots take no new request while held (submissions queue); release to run them - together,
+        batched."""
+        _check(self._L.svxg_server_hold(self._h, int(bool(on))))
 
     def wait(self, ticket: int):
         """(RequestResult, u or None, failing bonds or None)."""

@@ -58,3 +58,19 @@ def test_reference_arm_two_ranks():
     line = json.loads(outs[0].splitlines()[-1])
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_reference_arm_serving_stream():
+    """The default workload's reference arm: the serving stream on the host's cores, the same line
+    keys as the device arm."""
+    pytest.importorskip("oracle")
+    if not os.path.exists(os.path.join(ROOT, "oracle", "_build", "libsvxo.so")):
+        pytest.skip("the oracle is not built")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "3"], cwd=ROOT, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "solves/s" and line["value"] > 0
+    assert line["config"]["rtol"] == 1e-6 and line["config"]["timed_requests"] > 0
+    assert line["config"]["converged"] == line["config"]["timed_requests"]
+    assert line["e2e"]["value"] == line["value"] and line["cpu_baseline"]["kind"] == "port"
