@@ -73,18 +73,21 @@ int svxg_set_graph_device(svxg_problem* p, const svxg_node* nodes_dev, int32_t n
  * concurrently on pool threads, core/src/world/world_pieces.cpp:1460-1463). A batch: `count`
  * independent graphs as one problem, graph g's nodes and bonds after those of the graphs before it
  * (its bonds' node indices moved by its node offset), one material table. Assembly and the
- * multigrid are the reference's over that one graph (disjoint parts couple nowhere in K), so every
- * launch covers the whole batch; the solve (svxg_solve / svxg_solve_device with f and u the graphs'
- * vectors one after another) stops when every graph has ||r_g|| <= rtol ||f_g||, whatever the
- * batch's global residual. The batch lasts until the next svxg_set_graph / _device / reassemble. */
+ * multigrid are the reference's over that one graph (disjoint parts couple nowhere in K) with one
+ * difference: aggregation keeps uncoupled leftover rows single instead of grouping them eight at a
+ * time, so that the multigrid couples no two graphs either. Every launch covers the whole batch,
+ * and the solve (svxg_solve / svxg_solve_device with f and u the graphs' vectors one after another)
+ * runs one conjugate-gradient sequence per graph - its own alpha, beta, breakdown and stopping test
+ * ||r_g|| <= rtol ||f_g|| - inside the shared launches, until every graph has stopped. The batch
+ * lasts until the next svxg_set_graph / _device / reassemble. */
 int svxg_set_graphs(svxg_problem* p, int32_t count, const svxg_node* const* nodes, const int32_t* n,
                     const svxg_bond* const* bonds, const int32_t* nb, const svxg_material* mats);
 /* The same batch from graphs in device memory (pointer arrays on the host). */
 int svxg_set_graphs_device(svxg_problem* p, int32_t count, const svxg_node* const* nodes_dev, const int32_t* n,
                            const svxg_bond* const* bonds_dev, const int32_t* nb, const svxg_material* mats_dev);
-/* After a batch's solve: per graph ||r_g|| / ||f_g|| (0 without load) and whether it met its target
- * (count: the batch's graph count). */
-int svxg_graph_results(svxg_problem* p, int32_t count, double* rel_res, int32_t* converged);
+/* After a batch's solve: per graph ||r_g|| / ||f_g|| (0 without load), whether it met its target and
+ * the iterations its sequence ran (count: the batch's graph count; any array may be null). */
+int svxg_graph_results(svxg_problem* p, int32_t count, double* rel_res, int32_t* converged, int32_t* iters);
 
 /* StressProblem::assemble (stress.hpp:83, stress.cpp:134-176): K over the intact bonds and the
  * preconditioner. *ok = 1 assembled, 0 singular diagonal (the reference's false). */

@@ -76,7 +76,7 @@ def load_library() -> ctypes.CDLL:
         "svxg_set_graph_device": (c_i32, [c_vp, c_vp, c_i32, c_vp, c_i32, c_vp]),
         "svxg_set_graphs": (c_i32, [c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp]),
         "svxg_set_graphs_device": (c_i32, [c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp]),
-        "svxg_graph_results": (c_i32, [c_vp, c_i32, c_vp, c_vp]),
+        "svxg_graph_results": (c_i32, [c_vp, c_i32, c_vp, c_vp, c_vp]),
         "svxg_time_spmv": (c_i32, [c_vp, c_i32, c_i32, ctypes.POINTER(c_f64)]),
         "svxg_measure_fp64_rate": (c_i32, [c_i32, ctypes.POINTER(c_f64)]),
         "svxg_assemble": (c_i32, [c_vp, c_vp, ctypes.POINTER(c_i32)]),
@@ -498,7 +498,7 @@ class Batch:
 
     def solve(self, fs, rtol: float = 1e-6, maxit: int = -1):
         """fs: one load per graph (6 per node). Returns (list of u, PcgResult of the batch, per-graph
-        rel. residuals, per-graph converged flags)."""
+        rel. residuals, per-graph converged flags); per-graph iterations in self.iters."""
         f = np.concatenate([np.ascontiguousarray(x, dtype=np.float64).ravel() for x in fs])
         if f.size != 6 * int(self.node_off[-1]):
             raise ValueError("fs: 6 per node of each graph")
@@ -508,10 +508,12 @@ class Batch:
         k = len(self.graphs)
         rel = np.zeros(k)
         conv = np.zeros(k, np.int32)
+        its = np.zeros(k, np.int32)
         if k > 1:
-            _check(self._L.svxg_graph_results(self._h, k, ptr(rel), ptr(conv)))
+            _check(self._L.svxg_graph_results(self._h, k, ptr(rel), ptr(conv), ptr(its)))
         else:
-            rel[0], conv[0] = res.rel_res, res.converged
+            rel[0], conv[0], its[0] = res.rel_res, res.converged, res.iters
+        self.iters = its
         us = [u[6 * self.node_off[g]:6 * self.node_off[g + 1]] for g in range(k)]
         return us, res, rel, conv.astype(bool)
 

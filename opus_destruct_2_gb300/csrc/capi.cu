@@ -64,6 +64,8 @@ void release_solver(Problem& P) {
   P.mem.release(P.d_kslots);
   P.mem.release(P.d_seg_row);
   P.mem.release(P.d_seg);
+  P.mem.release(P.d_seg_flag);
+  P.mem.release(P.d_seg_of_row);
   P.mem.release(P.d_jinv);
   P.mem.release(P.d_dof);
   P.mem.release(P.d_chol);
@@ -650,7 +652,7 @@ int svxg_set_graphs(svxg_problem* p, int32_t count, const svxg_node* const* node
   return SVXG_OK;
 }
 
-int svxg_graph_results(svxg_problem* p, int32_t count, double* rel_res, int32_t* converged) {
+int svxg_graph_results(svxg_problem* p, int32_t count, double* rel_res, int32_t* converged, int32_t* iters) {
   CHECK_P(p);
   Problem& P = p->P;
   if (P.seg_n <= 0 || count != P.seg_n) {
@@ -662,7 +664,7 @@ int svxg_graph_results(svxg_problem* p, int32_t count, double* rel_res, int32_t*
     return SVXG_ERR_STATE;
   }
   DeviceScope ds(P.device);
-  return seg_results(P, rel_res, converged);
+  return seg_results(P, rel_res, converged, iters);
 }
 
 int svxg_set_graph(svxg_problem* p, const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb,

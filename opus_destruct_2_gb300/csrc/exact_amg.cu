@@ -617,22 +617,24 @@ __global__ void k_pass3_flags(int32_t n, const int32_t* rowptr, const int32_t* a
   noniso[i] = (left && !isolated) ? 1 : 0;
 }
 
-// an id is opened by every non-isolated leftover and by every eighth isolated one
+// an id is opened by every non-isolated leftover and by every eighth isolated one (group == 0, a
+// batch of graphs: by every isolated one - eight of them may belong to eight graphs, and the
+// batch's multigrid must not couple its graphs)
 __global__ void k_pass3_alloc(int32_t n, const int32_t* iso, const int32_t* isorank, const int32_t* noniso,
-                              int32_t* alloc, int32_t* group_first) {
+                              int32_t group, int32_t* alloc, int32_t* group_first) {
   const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const bool opens = noniso[i] || (iso[i] && isorank[i] % 8 == 0);
+  const bool opens = noniso[i] || (iso[i] && (!group || isorank[i] % 8 == 0));
   alloc[i] = opens ? 1 : 0;
-  if (iso[i] && isorank[i] % 8 == 0) group_first[isorank[i] / 8] = i;
+  if (group && iso[i] && isorank[i] % 8 == 0) group_first[isorank[i] / 8] = i;
 }
 
 __global__ void k_pass3_assign(int32_t n, int32_t base, const int32_t* iso, const int32_t* isorank,
-                               const int32_t* noniso, const int32_t* allocscan, const int32_t* group_first,
-                               int32_t* agg) {
+                               const int32_t* noniso, int32_t group, const int32_t* allocscan,
+                               const int32_t* group_first, int32_t* agg) {
   const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  if (noniso[i]) agg[i] = base + allocscan[i];
+  if (noniso[i] || (iso[i] && !group)) agg[i] = base + allocscan[i];
   else if (iso[i]) agg[i] = base + allocscan[group_first[isorank[i] / 8]];
 }
 
@@ -1470,10 +1472,13 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     (k_agg_pass2<<<nblk(n), kT, 0, st>>>(n, A.rowptr, A.col, fro.p, agg1.p, agg), SVXG_COUNT_LAUNCH());
     (k_pass3_flags<<<nblk(n), kT, 0, st>>>(n, A.rowptr, agg, iso.p, noniso.p), SVXG_COUNT_LAUNCH());
     TRY(exclusive_scan_i32(P, iso.p, isorank.p, n, nullptr));
-    (k_pass3_alloc<<<nblk(n), kT, 0, st>>>(n, iso.p, isorank.p, noniso.p, alloc.p, gfirst.p), SVXG_COUNT_LAUNCH());
+    const int32_t group = P.seg_n > 0 ? 0 : 1;  // (a batch: isolated leftovers stay single, graphs apart)
+    (k_pass3_alloc<<<nblk(n), kT, 0, st>>>(n, iso.p, isorank.p, noniso.p, group, alloc.p, gfirst.p),
+     SVXG_COUNT_LAUNCH());
     int32_t nalloc = 0;
     TRY(exclusive_scan_i32(P, alloc.p, allocscan.p, n, &nalloc));
-    (k_pass3_assign<<<nblk(n), kT, 0, st>>>(n, na1, iso.p, isorank.p, noniso.p, allocscan.p, gfirst.p, agg), SVXG_COUNT_LAUNCH());
+    (k_pass3_assign<<<nblk(n), kT, 0, st>>>(n, na1, iso.p, isorank.p, noniso.p, group, allocscan.p, gfirst.p, agg),
+     SVXG_COUNT_LAUNCH());
     SVXG_CUDA(cudaGetLastError());
     na = na1 + nalloc;
     if (!opt.reaggregate || round == 3 || 2 * int64_t(na) <= n) break;

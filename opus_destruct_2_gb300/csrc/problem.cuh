@@ -182,7 +182,9 @@ struct Problem {
   int32_t seg_n = 0;
   std::vector<int64_t> seg_node, seg_bond;
   int32_t* d_seg_row = nullptr;   // seg_n + 1 free-row offsets (made at assembly)
-  double* d_seg = nullptr;        // per graph: ||f||, target, ||r|| (3 seg_n)
+  int32_t* d_seg_of_row = nullptr;  // each free row's graph
+  double* d_seg = nullptr;        // per graph: its sequence's scalars (solve.cu kSegF)
+  int32_t* d_seg_flag = nullptr;  // per graph: 0 running, 1 converged, 2 broken down
   // multigrid
   std::vector<Level> lv;
   double* d_chol = nullptr;       // coarsest dense factor (m x m, lower = L, upper = L^T)
@@ -265,7 +267,8 @@ int free_run(Problem& P);
 int tune_k64(Problem& P);
 int time_cg_spmv(Problem& P, int32_t reps, float* ms_per_launch);    // solve.cu
 int seg_prepare(Problem& P);   // solve.cu: a batch's free-row offsets and per-graph scalars after assembly
-int seg_results(Problem& P, double* rel_res, int32_t* converged);  // solve.cu: per graph, after a solve
+int seg_results(Problem& P, double* rel_res, int32_t* converged, int32_t* iters);  // solve.cu: per graph
+int seg_launch(Problem& P, int op, const double* a, const double* b, double rtol);  // solve.cu
 int time_cg_spmv32(Problem& P, int32_t reps, float* ms_per_launch);  // mixed.cu
 int measure_fp64_rate(int device, double* tflops);                    // tune.cu
 // tune.cu: the row schedule of a BSR operator (spmv_row.cuh), from the committed table (a pure

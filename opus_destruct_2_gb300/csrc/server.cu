@@ -416,8 +416,8 @@ int run_batch(svxg_problem* p, std::vector<Request>& B, std::vector<svxg_request
   e = batch_solve_loads(p->P, fp.data(), nullptr, up.data(), B[0].rtol, B[0].maxit, false, &pr);
   if (e) return e;
   std::vector<double> rel(cnt, 0.0);
-  std::vector<int32_t> conv(cnt, 0);
-  e = svxg_graph_results(p, count, rel.data(), conv.data());
+  std::vector<int32_t> conv(cnt, 0), iters(cnt, 0);
+  e = svxg_graph_results(p, count, rel.data(), conv.data(), iters.data());
   if (e) return e;
   std::vector<int32_t> over(size_t(std::max(p->P.nb, 1)));
   int32_t n_over = 0;
@@ -425,7 +425,7 @@ int run_batch(svxg_problem* p, std::vector<Request>& B, std::vector<svxg_request
   if (e) return e;
   for (size_t g = 0; g < cnt; ++g) {
     svxg_request_result& r = res[g];
-    r.iters = pr.iters;
+    r.iters = iters[g];
     r.breakdown = pr.breakdown;
     r.converged = conv[g] && !pr.breakdown;
     r.rel_res = pr.breakdown && !std::isfinite(pr.rel_res) ? INFINITY : rel[g];
@@ -472,8 +472,8 @@ int run_bundle_repeats(Bundle& b, std::vector<Request>& R, const std::vector<int
   int e = batch_solve_loads(p->P, fp.data(), take.data(), up.data(), R[0].rtol, R[0].maxit, true, &pr);
   if (e) return e;
   std::vector<double> rel(count, 0.0);
-  std::vector<int32_t> conv(count, 0);
-  e = svxg_graph_results(p, int32_t(count), rel.data(), conv.data());
+  std::vector<int32_t> conv(count, 0), iters(count, 0);
+  e = svxg_graph_results(p, int32_t(count), rel.data(), conv.data(), iters.data());
   if (e) return e;
   std::vector<int32_t> over(size_t(std::max(p->P.nb, 1)));
   int32_t n_over = 0;
@@ -483,7 +483,7 @@ int run_bundle_repeats(Bundle& b, std::vector<Request>& R, const std::vector<int
     const size_t g = size_t(member[i]);
     svxg_request_result& r = res[i];
     r.warm = 1;
-    r.iters = pr.iters;
+    r.iters = iters[g];
     r.breakdown = pr.breakdown;
     r.converged = conv[g] && !pr.breakdown;
     r.rel_res = pr.breakdown && !std::isfinite(pr.rel_res) ? INFINITY : rel[g];

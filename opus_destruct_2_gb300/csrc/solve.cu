@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(kSpmvT) k_spmv(int32_t n, const int32_t* __res
                                                  const double* __restrict__ x, double* __restrict__ y,
                                                  double* partials, unsigned* counter, PcgScalars* s) {
   __shared__ double sh[kSpmvT / 32];
-  if (EPI == kDotP && s->done) return;
+  if (s && s->done) return;  // (the product of a running sequence: nothing once it is done)
   int c;
   bool lane_ok;
   const int32_t row = sched_row<SCHED>(kRowsPerBlock, &c, &lane_ok);
@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(kSpmvT, SVXG_SLOT_MINBLOCKS) k_spmv_slots(int3
                                                                            double* __restrict__ y, double* partials,
                                                                            unsigned* counter, PcgScalars* s) {
   __shared__ double sh[kSpmvT / 32];
-  if (EPI == kDotP && s->done) return;
+  if (s && s->done) return;  // (the product of a running sequence: nothing once it is done)
   const int c = (threadIdx.x & 31) % 6;
   const int64_t first = (int64_t(blockIdx.x) * kRowsPerBlock + (threadIdx.x >> 5)) * (5 * kSlotRows);
   int32_t row[kSlotRows];
@@ -461,61 +461,154 @@ __global__ void k_jacobi_apply(int32_t nfree, const double* __restrict__ jinv, c
   }
 }
 
-// ---- a batch's per-graph stopping test ----------------------------------------------------------
-// Graph g of a batch owns free rows [row0[g], row0[g + 1]) (6 entries each). Its norms are sums in a
-// fixed order: one warp per graph, lane l over entries l, l + 32, ..., then a fixed shuffle tree -
-// the same bits on every run, whatever else the batch holds. seg: ||f_g||, target_g, ||r_g||.
+// ---- a batch: one conjugate-gradient sequence per graph ------------------------------------------
+// Graph g of a batch owns free rows [row0[g], row0[g + 1]) (6 entries each), and the batch's
+// multigrid couples no two graphs (aggregation keeps them apart), so each graph runs its own
+// sequence - its own alpha, beta, breakdown and stopping test, as if it were alone - inside launches
+// shared by all. A graph's dots are sums in a fixed order (one block per graph, thread t over
+// entries t, t + 256, ..., then a fixed tree): the same bits whatever else the batch holds. The last
+// block to finish a reduction sets the run's flags: done when no graph is still running.
+// seg (kSegF doubles per graph): ||f||, target, ||r||, r.z, p.q, alpha, beta, iterations at its end;
+// flag per graph: 0 running, 1 converged, 2 broken down.
 constexpr int kSegT = 256;
+constexpr int kSegF = 8;
+enum SegOp { kSegBn = 0, kSegRz0 = 1, kSegStart = 2, kSegPq = 3, kSegRn = 4, kSegRz = 5 };
 
-__device__ __forceinline__ double seg_sumsq(const double* v, int64_t e0, int64_t e1) {
-  double s = 0.0;
-  for (int64_t e = e0 + (threadIdx.x & 31); e < e1; e += 32) s += v[e] * v[e];
-  return warp_sum(s);
-}
-
-// ||f_g|| of every graph (begin)
-__global__ void k_seg_begin(int32_t nseg, const int32_t* __restrict__ row0, const double* __restrict__ f,
-                            double* seg) {
-  const int32_t g = int32_t(blockIdx.x) * (kSegT / 32) + int32_t(threadIdx.x >> 5);
-  if (g >= nseg) return;
-  const double t = seg_sumsq(f, 6 * int64_t(row0[g]), 6 * int64_t(row0[g + 1]));
-  if ((threadIdx.x & 31) == 0) seg[3 * g] = sqrt(t);
-}
-
-// ||r_g|| against target_g for every graph; START (iterate's start) also sets the targets,
-// rtol ||f_g||. One block: the count of graphs not yet at their targets decides the run - all
-// there: converged; otherwise it goes on whatever the batch's global residual (target -1: the
-// global test of k_axpy_rr never stops a batch).
-template <bool START>
-__global__ void __launch_bounds__(kSegT) k_seg_check(int32_t nseg, const int32_t* __restrict__ row0,
-                                                      const double* __restrict__ r, double rtol, double* seg,
-                                                      PcgScalars* s) {
-  __shared__ int32_t open_sh;
-  if (!START && s->done) return;
-  if (threadIdx.x == 0) open_sh = 0;
+template <int OP>
+__global__ void __launch_bounds__(kSegT) k_seg_reduce(int32_t nseg, const int32_t* __restrict__ row0,
+                                                       const double* __restrict__ a, const double* __restrict__ b,
+                                                       double rtol, double* seg, int32_t* flag, double* partials,
+                                                       unsigned* counter, PcgScalars* s) {
+  __shared__ double sh[kSegT];
+  __shared__ bool last;
+  if ((OP == kSegPq || OP == kSegRn || OP == kSegRz) && s->done) return;
+  const int32_t g = int32_t(blockIdx.x);
+  const int64_t e0 = 6 * int64_t(row0[g]), e1 = 6 * int64_t(row0[g + 1]);
+  double t = 0.0;
+  for (int64_t e = e0 + threadIdx.x; e < e1; e += kSegT) t += a[e] * b[e];
+  sh[threadIdx.x] = t;
   __syncthreads();
-  int32_t open = 0;
-  for (int32_t g = int32_t(threadIdx.x >> 5); g < nseg; g += kSegT / 32) {
-    const double rn = sqrt(seg_sumsq(r, 6 * int64_t(row0[g]), 6 * int64_t(row0[g + 1])));
-    if ((threadIdx.x & 31) == 0) {
-      if (START) seg[3 * g + 1] = rtol * seg[3 * g];
-      seg[3 * g + 2] = rn;
+  for (int d = kSegT / 2; d > 0; d >>= 1) {
+    if (int(threadIdx.x) < d) sh[threadIdx.x] += sh[threadIdx.x + d];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double* q = seg + size_t(kSegF) * g;
+    const double v = sh[0];
+    if (OP == kSegBn) {
+      q[0] = sqrt(v);
+    } else if (OP == kSegRz0) {
+      q[3] = v;
+    } else if (OP == kSegStart) {
+      q[2] = sqrt(v);
+      q[1] = rtol * q[0];
+      q[7] = 0.0;
       // (a graph without load is there at once, as a solve of zero load is, stress.cpp:389-394)
-      if (!(rn <= seg[3 * g + 1]) && seg[3 * g] > 0.0) ++open;
+      flag[g] = (q[0] > 0.0 && !(q[2] <= q[1])) ? 0 : 1;
+    } else if (flag[g] == 0) {
+      if (OP == kSegPq) {
+        q[4] = v;
+        if (!(v > 0.0)) {
+          flag[g] = 2;
+          q[5] = 0.0;
+          q[7] = double(s->iters + 1);
+        } else {
+          q[5] = q[3] / v;
+        }
+      } else if (OP == kSegRn) {
+        q[2] = sqrt(v);
+        if (q[2] <= q[1]) {
+          flag[g] = 1;
+          q[7] = double(s->iters);
+        }
+      } else {  // kSegRz
+        if (!(v > 0.0)) {
+          flag[g] = 2;
+          q[7] = double(s->iters);
+        } else {
+          q[6] = v / q[3];
+          q[3] = v;
+        }
+      }
+    }
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last || OP == kSegBn || OP == kSegRz0) {
+    if (last && threadIdx.x == 0) *counter = 0u;
+    return;
+  }
+  __threadfence();
+  // the last block: graphs still running, broken down
+  int32_t run = 0, bad = 0;
+  for (int32_t k = threadIdx.x; k < nseg; k += kSegT) {
+    const int32_t f = __ldcg(&flag[k]);
+    run += f == 0;
+    bad += f == 2;
+  }
+  sh[threadIdx.x] = double(run) + 65536.0 * double(bad);
+  __syncthreads();
+  for (int d = kSegT / 2; d > 0; d >>= 1) {
+    if (int(threadIdx.x) < d) sh[threadIdx.x] += sh[threadIdx.x + d];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    *counter = 0u;
+    const int64_t tot = int64_t(sh[0]);
+    const int64_t nrun = tot % 65536, nbad = tot / 65536;
+    if (OP == kSegPq) s->iters += 1;
+    if (OP == kSegStart) {
+      if (s->breakdown) return;  // (not finite: the global start already ended the run)
+      s->target = -1.0;          // (k_axpy_rr's global test never stops a batch)
+      s->converged = nrun == 0 && nbad == 0 ? 1 : 0;
+      s->done = nrun == 0 || s->maxit <= 0 ? 1 : 0;
+    } else if (nrun == 0) {
+      s->converged = nbad == 0 ? 1 : 0;
+      s->breakdown = nbad > 0 ? 1 : 0;
+      s->done = 1;
     }
   }
-  if (open) atomicAdd(&open_sh, open);
-  __syncthreads();
-  if (threadIdx.x != 0) return;
-  if (START) {
-    if (s->breakdown) return;  // (not finite: the global start already ended the run)
-    s->target = -1.0;
-    const bool none = open_sh == 0;
-    s->converged = none ? 1 : 0;
-    s->done = none || s->maxit <= 0 ? 1 : 0;
-  } else if (open_sh == 0) {
-    s->converged = 1;
-    s->done = 1;
+}
+
+// x = r = 0 for graphs without load (begin)
+__global__ void k_seg_zero(int32_t nf, const int32_t* __restrict__ seg_of_row, const double* __restrict__ seg,
+                           double* x, double* r) {
+  const int32_t i = blockIdx.x * kVecT + threadIdx.x;
+  if (i >= nf || seg[size_t(kSegF) * seg_of_row[i]] > 0.0) return;
+  for (int c = 0; c < 6; ++c) x[6 * int64_t(i) + c] = r[6 * int64_t(i) + c] = 0.0;
+}
+
+// x += alpha_g p, r -= alpha_g q for the rows of graphs still running
+__global__ void k_seg_axpy(int32_t nf, const int32_t* __restrict__ seg_of_row, const double* __restrict__ seg,
+                           const int32_t* __restrict__ flag, double* __restrict__ x, double* __restrict__ r,
+                           const double* __restrict__ p, const double* __restrict__ q, const PcgScalars* s) {
+  if (s->done) return;
+  const int32_t i = blockIdx.x * kVecT + threadIdx.x;
+  if (i >= nf) return;
+  const int32_t g = seg_of_row[i];
+  if (flag[g] != 0) return;
+  const double alpha = seg[size_t(kSegF) * g + 5];
+  for (int c = 0; c < 6; ++c) {
+    const int64_t k = 6 * int64_t(i) + c;
+    x[k] += alpha * p[k];
+    r[k] -= alpha * q[k];
+  }
+}
+
+// p = z + beta_g p for the rows of graphs still running
+__global__ void k_seg_pupdate(int32_t nf, const int32_t* __restrict__ seg_of_row, const double* __restrict__ seg,
+                              const int32_t* __restrict__ flag, const double* __restrict__ z, double* __restrict__ p,
+                              const PcgScalars* s) {
+  if (s->done) return;
+  const int32_t i = blockIdx.x * kVecT + threadIdx.x;
+  if (i >= nf) return;
+  const int32_t g = seg_of_row[i];
+  if (flag[g] != 0) return;
+  const double beta = seg[size_t(kSegF) * g + 6];
+  for (int c = 0; c < 6; ++c) {
+    const int64_t k = 6 * int64_t(i) + c;
+    p[k] = z[k] + beta * p[k];
   }
 }
 
@@ -747,11 +840,15 @@ int pcg_begin(Problem& P, const double* f_nodes, const double* u0_nodes) {
     TRY(spmv(P, P.K, P.d_x, P.d_q));
     (k_begin_r<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_f, P.d_q, P.d_r, P.d_partials, P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
     (k_begin_zero<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_x, P.d_r, P.d_s), SVXG_COUNT_LAUNCH());
-    if (P.seg_n > 0)
-      (k_seg_begin<<<unsigned((P.seg_n + kSegT / 32 - 1) / (kSegT / 32)), kSegT, 0, st>>>(P.seg_n, P.d_seg_row,
-                                                                                        P.d_f, P.d_seg),
+    if (P.seg_n > 0) {
+      // a batch: per graph ||f||, zero-load graphs at rest, z = M r, p = z, r.z
+      TRY(seg_launch(P, kSegBn, P.d_f, P.d_f, 0.0));
+      (k_seg_zero<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_seg_of_row, P.d_seg, P.d_x, P.d_r), SVXG_COUNT_LAUNCH());
+      TRY(precondition(P, P.d_r, P.d_z));
+      (k_rz<0><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_r, P.d_z, P.d_p, P.d_partials, P.d_counter, P.d_s),
        SVXG_COUNT_LAUNCH());
-    if (P.jacobi_only) {
+      TRY(seg_launch(P, kSegRz0, P.d_r, P.d_z, 0.0));
+    } else if (P.jacobi_only) {
       (k_jacobi_rz<0><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_jinv, P.d_r, P.d_z, P.d_p, P.d_partials,
                                                        P.d_counter, P.d_s), SVXG_COUNT_LAUNCH());
     } else if (mixed_run(P)) {
@@ -880,8 +977,29 @@ __global__ void __launch_bounds__(kJacobiBlockT) k_jacobi_pcg_block(int32_t nf, 
   }
 }
 
+// one iteration of every graph of a batch: q = K p, per graph p.q and alpha, x and r, ||r|| and
+// the stopping test, z = M r, r.z and beta, p (the batch's sequences, each as stress.cpp:428-461)
+int seg_body(Problem& P) {
+  const int32_t nf = P.nfree;
+  cudaStream_t st = P.stream;
+  launch_spmv<kPlain>(st, P.sched_k64, nf, P.K.rowptr, P.K.col, P.K.val, P.d_p, P.d_q, nullptr, nullptr, P.d_s,
+                      P.d_kslots);
+  TRY(seg_launch(P, kSegPq, P.d_p, P.d_q, 0.0));
+  (k_seg_axpy<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_seg_of_row, P.d_seg, P.d_seg_flag, P.d_x, P.d_r, P.d_p,
+                                                P.d_q, P.d_s), SVXG_COUNT_LAUNCH());
+  TRY(seg_launch(P, kSegRn, P.d_r, P.d_r, 0.0));
+  TRY(precondition(P, P.d_r, P.d_z));
+  TRY(seg_launch(P, kSegRz, P.d_r, P.d_z, 0.0));
+  (k_seg_pupdate<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_seg_of_row, P.d_seg, P.d_seg_flag, P.d_z, P.d_p, P.d_s),
+   SVXG_COUNT_LAUNCH());
+  (k_mark_cap<<<1, 32, 0, st>>>(P.d_s), SVXG_COUNT_LAUNCH());
+  SVXG_CUDA(cudaGetLastError());
+  return SVXG_OK;
+}
+
 // one iteration of the sequence (stress.cpp:428-461), enqueued on P.stream
 int plain_body(Problem& P) {
+  if (P.seg_n > 0) return seg_body(P);
   const int32_t nf = P.nfree;
   cudaStream_t st = P.stream;
   if (P.timer_on) TRY(timer_mark(P));
@@ -890,8 +1008,6 @@ int plain_body(Problem& P) {
   if (P.timer_on) TRY(timer_mark(P, true));
   (k_axpy_rr<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_x, P.d_r, P.d_p, P.d_q, P.d_partials, P.d_counter, P.d_s),
    SVXG_COUNT_LAUNCH());
-  if (P.seg_n > 0)
-    (k_seg_check<false><<<1, kSegT, 0, st>>>(P.seg_n, P.d_seg_row, P.d_r, 0.0, P.d_seg, P.d_s), SVXG_COUNT_LAUNCH());
   if (P.jacobi_only) {
     (k_jacobi_rz<1><<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_jinv, P.d_r, P.d_z, nullptr, P.d_partials, P.d_counter,
                                                       P.d_s), SVXG_COUNT_LAUNCH());
@@ -958,8 +1074,7 @@ int plain_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
   P.cycle_stop = &P.d_s->done;
   (k_iter_start<<<vec_blocks(std::max(nf, 1)), kVecT, 0, st>>>(nf, P.d_r, rtol, maxit, P.d_partials, P.d_counter,
                                                              P.d_s), SVXG_COUNT_LAUNCH());
-  if (P.seg_n > 0 && nf > 0)
-    (k_seg_check<true><<<1, kSegT, 0, st>>>(P.seg_n, P.d_seg_row, P.d_r, rtol, P.d_seg, P.d_s), SVXG_COUNT_LAUNCH());
+  if (P.seg_n > 0 && nf > 0) TRY(seg_launch(P, kSegStart, P.d_r, P.d_r, rtol));
   SVXG_CUDA(cudaGetLastError());
   SVXG_CUDA(cudaMemcpyAsync(P.h_s, P.d_s, sizeof(PcgScalars), cudaMemcpyDeviceToHost, st));
   SVXG_CUDA(host_wait(st));
@@ -1011,39 +1126,86 @@ int plain_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
   return SVXG_OK;
 }
 
-// A batch's free-row offsets from the DOF numbering (free nodes numbered in node order, so graph
-// g's free rows are those of its nodes), and its per-graph scalars; after each assembly.
+// A batch's free-row offsets and each free row's graph from the DOF numbering (free nodes numbered
+// in node order, so graph g's free rows are those of its nodes), and its per-graph state; after each
+// assembly.
 int seg_prepare(Problem& P) {
   P.mem.release(P.d_seg_row);
   P.mem.release(P.d_seg);
+  P.mem.release(P.d_seg_flag);
+  P.mem.release(P.d_seg_of_row);
   if (P.seg_n <= 0) return SVXG_OK;
-  std::vector<int32_t> row0(size_t(P.seg_n) + 1, 0);
+  std::vector<int32_t> row0(size_t(P.seg_n) + 1, 0), of_row(size_t(std::max(P.nfree, 1)), 0);
   int32_t fr = 0;
   for (int32_t g = 0; g < P.seg_n; ++g) {
     row0[size_t(g)] = fr;
-    for (int64_t i = P.seg_node[size_t(g)]; i < P.seg_node[size_t(g) + 1]; ++i) fr += P.h_dof[size_t(i)] >= 0 ? 1 : 0;
+    for (int64_t i = P.seg_node[size_t(g)]; i < P.seg_node[size_t(g) + 1]; ++i)
+      if (P.h_dof[size_t(i)] >= 0) of_row[size_t(fr++)] = g;
   }
   row0[size_t(P.seg_n)] = fr;
   TRY(P.mem.alloc(&P.d_seg_row, size_t(P.seg_n) + 1));
-  TRY(P.mem.alloc(&P.d_seg, 3 * size_t(P.seg_n)));
+  TRY(P.mem.alloc(&P.d_seg, size_t(kSegF) * size_t(P.seg_n)));
+  TRY(P.mem.alloc(&P.d_seg_flag, size_t(P.seg_n)));
+  TRY(P.mem.alloc(&P.d_seg_of_row, of_row.size()));
   SVXG_CUDA(cudaMemcpyAsync(P.d_seg_row, row0.data(), sizeof(int32_t) * row0.size(), cudaMemcpyHostToDevice,
                             P.stream));
-  SVXG_CUDA(cudaMemsetAsync(P.d_seg, 0, sizeof(double) * 3 * size_t(P.seg_n), P.stream));
-  SVXG_CUDA(host_wait(P.stream));  // (row0 is freed on return)
+  SVXG_CUDA(cudaMemcpyAsync(P.d_seg_of_row, of_row.data(), sizeof(int32_t) * of_row.size(), cudaMemcpyHostToDevice,
+                            P.stream));
+  SVXG_CUDA(cudaMemsetAsync(P.d_seg, 0, sizeof(double) * size_t(kSegF) * size_t(P.seg_n), P.stream));
+  SVXG_CUDA(cudaMemsetAsync(P.d_seg_flag, 0, sizeof(int32_t) * size_t(P.seg_n), P.stream));
+  SVXG_CUDA(host_wait(P.stream));  // (row0 and of_row are freed on return)
   return SVXG_OK;
 }
 
-// per graph of a batch after a solve: ||r_g|| / ||f_g|| (0 without load) and whether it met its
-// target (at a converged end every graph did)
-int seg_results(Problem& P, double* rel_res, int32_t* converged) {
+// a reduction over every graph of the batch (one block each), its partials counter the problem's
+int seg_launch(Problem& P, int op, const double* a, const double* b, double rtol) {
+  const unsigned g = unsigned(P.seg_n);
+  unsigned* ctr = P.d_counter + 1;  // (a counter of its own: the global reductions use the first)
+  switch (op) {
+    case kSegBn:
+      (k_seg_reduce<kSegBn><<<g, kSegT, 0, P.stream>>>(P.seg_n, P.d_seg_row, a, b, rtol, P.d_seg, P.d_seg_flag,
+                                                        P.d_partials, ctr, P.d_s), SVXG_COUNT_LAUNCH());
+      break;
+    case kSegRz0:
+      (k_seg_reduce<kSegRz0><<<g, kSegT, 0, P.stream>>>(P.seg_n, P.d_seg_row, a, b, rtol, P.d_seg, P.d_seg_flag,
+                                                         P.d_partials, ctr, P.d_s), SVXG_COUNT_LAUNCH());
+      break;
+    case kSegStart:
+      (k_seg_reduce<kSegStart><<<g, kSegT, 0, P.stream>>>(P.seg_n, P.d_seg_row, a, b, rtol, P.d_seg,
+                                                           P.d_seg_flag, P.d_partials, ctr, P.d_s),
+       SVXG_COUNT_LAUNCH());
+      break;
+    case kSegPq:
+      (k_seg_reduce<kSegPq><<<g, kSegT, 0, P.stream>>>(P.seg_n, P.d_seg_row, a, b, rtol, P.d_seg, P.d_seg_flag,
+                                                        P.d_partials, ctr, P.d_s), SVXG_COUNT_LAUNCH());
+      break;
+    case kSegRn:
+      (k_seg_reduce<kSegRn><<<g, kSegT, 0, P.stream>>>(P.seg_n, P.d_seg_row, a, b, rtol, P.d_seg, P.d_seg_flag,
+                                                        P.d_partials, ctr, P.d_s), SVXG_COUNT_LAUNCH());
+      break;
+    default:
+      (k_seg_reduce<kSegRz><<<g, kSegT, 0, P.stream>>>(P.seg_n, P.d_seg_row, a, b, rtol, P.d_seg, P.d_seg_flag,
+                                                        P.d_partials, ctr, P.d_s), SVXG_COUNT_LAUNCH());
+  }
+  SVXG_CUDA(cudaGetLastError());
+  return SVXG_OK;
+}
+
+// per graph of a batch after a solve: ||r_g|| / ||f_g|| (0 without load), whether it met its target,
+// and the iterations its sequence ran
+int seg_results(Problem& P, double* rel_res, int32_t* converged, int32_t* iters) {
   if (P.seg_n <= 0 || !P.d_seg) return SVXG_ERR_STATE;
-  std::vector<double> h(3 * size_t(P.seg_n));
+  std::vector<double> h(size_t(kSegF) * size_t(P.seg_n));
+  std::vector<int32_t> fl(size_t(P.seg_n));
   SVXG_CUDA(cudaMemcpyAsync(h.data(), P.d_seg, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, P.stream));
+  SVXG_CUDA(cudaMemcpyAsync(fl.data(), P.d_seg_flag, sizeof(int32_t) * fl.size(), cudaMemcpyDeviceToHost, P.stream));
+  SVXG_CUDA(cudaMemcpyAsync(P.h_s, P.d_s, sizeof(PcgScalars), cudaMemcpyDeviceToHost, P.stream));
   SVXG_CUDA(host_wait(P.stream));
   for (int32_t g = 0; g < P.seg_n; ++g) {
-    const double bn = h[3 * size_t(g)], tg = h[3 * size_t(g) + 1], rn = h[3 * size_t(g) + 2];
-    if (rel_res) rel_res[g] = bn > 0.0 ? rn / bn : 0.0;
-    if (converged) converged[g] = (rn <= tg || !(bn > 0.0)) ? 1 : 0;
+    const double* q = &h[size_t(kSegF) * size_t(g)];
+    if (rel_res) rel_res[g] = q[0] > 0.0 ? q[2] / q[0] : 0.0;
+    if (converged) converged[g] = fl[size_t(g)] == 1 ? 1 : 0;
+    if (iters) iters[g] = fl[size_t(g)] == 0 ? P.h_s->iters : int32_t(q[7]);
   }
   return SVXG_OK;
 }

@@ -75,6 +75,7 @@ def port_lib() -> ctypes.CDLL:
         lib.svxo_precondition.argtypes = [c_vp, c_vp, c_vp]
         lib.svxo_apply_k.argtypes = [c_vp, c_vp, c_vp]
         lib.svxo_set_threads.argtypes = [ctypes.c_int]
+        lib.svxo_set_group_isolated.argtypes = [ctypes.c_int]
         lib.svxo_seq_sum.restype = c_f64
         lib.svxo_utilization_many.argtypes = [c_vp, c_vp, c_f64, c_vp, c_vp]
         lib.svxo_build_bonds.argtypes = [c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp]
@@ -133,6 +134,13 @@ def reference_lib() -> ctypes.CDLL | None:
         lib.svxr_p_matrix.argtypes = [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]
         _ref = lib
     return _ref
+
+
+def set_group_isolated(on: bool) -> None:
+    """Pass 3 of the aggregation groups uncoupled leftover rows eight at a time (on: the
+    reference) or keeps each single (off: the library's batches of graphs, which must not couple
+    their graphs)."""
+    port_lib().svxo_set_group_isolated(int(bool(on)))
 
 
 def set_threads(n: int) -> None:

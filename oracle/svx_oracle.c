@@ -441,6 +441,11 @@ static double* acc_slot(acc_row* row, int32_t* slot, int32_t c) {
 }
 
 /* Amg::coarsen, amg.cpp:320-533. Appends level l + 1; 0 if coarsening does not pay. */
+/* Pass 3's grouping of uncoupled leftover rows (the reference's, on); off only for checking the
+   library's batches of graphs, whose multigrid keeps such rows single (svxo_set_group_isolated). */
+static int g_group_isolated = 1;
+void svxo_set_group_isolated(int on) { g_group_isolated = on != 0; }
+
 static int coarsen(amg* M, int32_t l, int smoothed) {
   level* F = &M->lv[l];
   const bsr* A = &F->A;
@@ -487,12 +492,13 @@ static int coarsen(amg* M, int32_t l, int smoothed) {
       }
       agg[i] = ba;
     }
-    /* pass 3: leftovers; uncoupled rows grouped eight at a time */
+    /* pass 3: leftovers; uncoupled rows grouped eight at a time (each its own with
+       g_group_isolated off: the batch form of the library, whose graphs must stay apart) */
     {
       int32_t open = -1, fill = 0;
       for (int32_t i = 0; i < n; ++i) {
         if (agg[i] >= 0) continue;
-        if (!ISOLATED(i)) {
+        if (!ISOLATED(i) || !g_group_isolated) {
           agg[i] = na++;
           continue;
         }

@@ -36,6 +36,9 @@ typedef struct svxo_info {
 } svxo_info;
 
 void svxo_set_threads(int n);
+/* pass 3 groups uncoupled leftover rows eight at a time (1, the reference) or keeps each single (0,
+   the library's batches of graphs) */
+void svxo_set_group_isolated(int on);
 int svxo_num_threads(void);
 
 svxo_problem* svxo_create(const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb,

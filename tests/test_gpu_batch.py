@@ -1,7 +1,10 @@
 """A batch of independent graphs as one problem (svxg_set_graphs) against the oracle.
 
 * the batch is one graph to the setup: its level sizes and blocks and the work counters equal the
-  oracle's for the same union graph (the reference's algorithm applied to it);
+  oracle's for the same union graph (the reference's algorithm applied to it, with uncoupled
+  leftover rows kept single as the batch keeps them);
+* one sequence per graph: each graph's iteration count stays near its count alone as the batch
+  grows (a shared sequence's would grow with the number of graphs);
 * per-graph stopping: at rtol 1e-6 every graph's own residual, recomputed on the host with the
   oracle's K of that graph alone, is within the target (the batch's global residual decides
   nothing), and the per-graph rel. residuals the library reports are those residuals;
@@ -14,6 +17,7 @@ import pytest
 
 from opus_destruct_2_gb300 import Batch, StressProblem, synth
 from opus_destruct_2_gb300.graph import BOND_DTYPE, StressOptions, default_materials
+import oracle
 from oracle import Port
 
 pytestmark = pytest.mark.gpu
@@ -52,8 +56,12 @@ def test_batch_setup_is_the_union_graphs():
     B = Batch([(g[0], g[1]) for g in gs], MATS)
     assert B.assemble(StressOptions())
     n, b, _ = union(gs)
-    O = Port(n, b, MATS)
-    assert O.assemble(StressOptions())
+    oracle.set_group_isolated(False)
+    try:
+        O = Port(n, b, MATS)
+        assert O.assemble(StressOptions())
+    finally:
+        oracle.set_group_isolated(True)
     bi, oi = B.info(), O.info()
     assert bi.sizes() == oi.sizes() and bi.blocks() == oi.blocks()
     for k in ("nfree", "chol_n", "matrix_blocks", "work_per_apply", "build_work", "assembly_work"):
@@ -115,3 +123,22 @@ def test_batch_of_one_is_the_problem():
     ug, rg = G.solve(f, rtol=1e-8, maxit=2000)
     assert res.converged and conv[0] and rg.converged
     assert np.array_equal(us[0], ug) and res.iters == rg.iters
+
+
+def test_batch_iterations_stay_per_graph():
+    """64 pieces of the serving sizes in one batch: every graph's own sequence stops near its
+    iteration count alone (the batch's multigrid differs from each graph's own, so not exactly)."""
+    from opus_destruct_2_gb300 import workloads
+    st = workloads.Stream(requests=64, rate=5000.0, pool=64, repeat_share=0.0, seed=29)
+    gs = [st.geoms[p[2]] for p in st.plan][:64]
+    B = Batch([(g[0], g[1]) for g in gs], MATS)
+    assert B.assemble(StressOptions())
+    us, res, rel, conv = B.solve([g[2] for g in gs], rtol=1e-6, maxit=2000)
+    assert res.converged and conv.all() and (rel <= 1e-6).all()
+    alone = []
+    for n, b, f in gs:
+        G = StressProblem(n, b, MATS)
+        assert G.assemble(StressOptions(amg_min_nodes=0))
+        alone.append(G.solve(f, rtol=1e-6, maxit=2000)[1].iters)
+    assert int(np.max(B.iters)) <= 2 * int(np.max(alone)) + 5, (np.max(B.iters), np.max(alone))
+    assert float(np.mean(B.iters)) <= 2.0 * float(np.mean(alone)) + 5.0, (np.mean(B.iters), np.mean(alone))
