@@ -685,7 +685,7 @@ def main():
     ap.add_argument("--requests", type=int, default=20000, help="serve: requests in the stream")
     ap.add_argument("--rate", type=float, default=5000.0, help="serve: Poisson arrival rate (requests/s)")
     ap.add_argument("--graphs", type=int, default=512, help="batch: graphs")
-    ap.add_argument("--workers", type=int, default=16, help="batch / serve: server slots")
+    ap.add_argument("--workers", type=int, default=32, help="batch / serve: server slots")
     ap.add_argument("--lots", type=int, default=8)
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--rtol", type=float, default=None, help="default: 1e-6 serving and batch, 1e-8 otherwise")
