@@ -45,6 +45,9 @@ typedef struct svxg_info {
   int32_t mixed_fallbacks;  /* mixed-precision solves since then finished in FP64 (FP32 stalled) */
   int64_t graph_bytes;      /* of device_bytes: the graph's copy (nodes, bonds, materials); the rest
                                is what svxg_release frees (StressProblem::solver_bytes) */
+  double error_estimate;    /* the last solve's error against the FP64 solution, estimated as
+                               ||M^-1 r|| / ||u|| from its final FP64 residual (solves under the
+                               mixed-precision policy; 0 for FP64 ones) */
 } svxg_info;
 
 const char* svxg_last_error(void);
@@ -85,9 +88,11 @@ int svxg_set_graphs(svxg_problem* p, int32_t count, const svxg_node* const* node
 /* The same batch from graphs in device memory (pointer arrays on the host). */
 int svxg_set_graphs_device(svxg_problem* p, int32_t count, const svxg_node* const* nodes_dev, const int32_t* n,
                            const svxg_bond* const* bonds_dev, const int32_t* nb, const svxg_material* mats_dev);
-/* After a batch's solve: per graph ||r_g|| / ||f_g|| (0 without load), whether it met its target and
- * the iterations its sequence ran (count: the batch's graph count; any array may be null). */
-int svxg_graph_results(svxg_problem* p, int32_t count, double* rel_res, int32_t* converged, int32_t* iters);
+/* After a batch's solve: per graph ||r_g|| / ||f_g|| (0 without load), whether it met its target,
+ * the iterations its sequence ran and, under the mixed-precision policy, its error estimate
+ * (svxg_info.error_estimate; 0 otherwise). count: the batch's graph count; any array may be null. */
+int svxg_graph_results(svxg_problem* p, int32_t count, double* rel_res, int32_t* converged, int32_t* iters,
+                       double* err_est);
 
 /* StressProblem::assemble (stress.hpp:83, stress.cpp:134-176): K over the intact bonds and the
  * preconditioner. *ok = 1 assembled, 0 singular diagonal (the reference's false). */

@@ -44,7 +44,7 @@ typedef struct svxg_request_result {
   double rel_res;
   double queue_ms;    /* submission -> a slot took it */
   double latency_ms;  /* submission -> result recorded */
-  double pad;
+  double err_est;     /* the solve's error estimate under the mixed-precision policy (svxg_info) */
 } svxg_request_result;
 
 /* Counters since creation (or the last reset). 112 bytes. */

@@ -41,7 +41,7 @@ class Info(ctypes.Structure):
                 ("level_sizes", c_i32 * 16), ("level_blocks", c_i64 * 32), ("matrix_blocks", c_i64),
                 ("work_per_iteration", c_i64), ("assembly_work", c_i64), ("work_per_apply", c_i64),
                 ("build_work", c_i64), ("device_bytes", c_i64), ("precision", c_i32), ("mixed_fallbacks", c_i32),
-                ("graph_bytes", c_i64)]
+                ("graph_bytes", c_i64), ("error_estimate", c_f64)]
 
     def sizes(self) -> list[int]:
         return [self.level_sizes[i] for i in range(self.levels)]
@@ -76,7 +76,7 @@ def load_library() -> ctypes.CDLL:
         "svxg_set_graph_device": (c_i32, [c_vp, c_vp, c_i32, c_vp, c_i32, c_vp]),
         "svxg_set_graphs": (c_i32, [c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp]),
         "svxg_set_graphs_device": (c_i32, [c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp]),
-        "svxg_graph_results": (c_i32, [c_vp, c_i32, c_vp, c_vp, c_vp]),
+        "svxg_graph_results": (c_i32, [c_vp, c_i32, c_vp, c_vp, c_vp, c_vp]),
         "svxg_time_spmv": (c_i32, [c_vp, c_i32, c_i32, ctypes.POINTER(c_f64)]),
         "svxg_measure_fp64_rate": (c_i32, [c_i32, ctypes.POINTER(c_f64)]),
         "svxg_assemble": (c_i32, [c_vp, c_vp, ctypes.POINTER(c_i32)]),
@@ -498,7 +498,8 @@ class Batch:
 
     def solve(self, fs, rtol: float = 1e-6, maxit: int = -1):
         """fs: one load per graph (6 per node). Returns (list of u, PcgResult of the batch, per-graph
-        rel. residuals, per-graph converged flags); per-graph iterations in self.iters."""
+        rel. residuals, per-graph converged flags); per-graph iterations in self.iters and, under the
+        mixed-precision policy, error estimates in self.error_estimate."""
         f = np.concatenate([np.ascontiguousarray(x, dtype=np.float64).ravel() for x in fs])
         if f.size != 6 * int(self.node_off[-1]):
             raise ValueError("fs: 6 per node of each graph")
@@ -509,11 +510,13 @@ class Batch:
         rel = np.zeros(k)
         conv = np.zeros(k, np.int32)
         its = np.zeros(k, np.int32)
+        est = np.zeros(k)
         if k > 1:
-            _check(self._L.svxg_graph_results(self._h, k, ptr(rel), ptr(conv), ptr(its)))
+            _check(self._L.svxg_graph_results(self._h, k, ptr(rel), ptr(conv), ptr(its), ptr(est)))
         else:
             rel[0], conv[0], its[0] = res.rel_res, res.converged, res.iters
-        self.iters = its
+            est[0] = self.info().error_estimate
+        self.iters, self.error_estimate = its, est
         us = [u[6 * self.node_off[g]:6 * self.node_off[g + 1]] for g in range(k)]
         return us, res, rel, conv.astype(bool)
 

@@ -652,7 +652,8 @@ int svxg_set_graphs(svxg_problem* p, int32_t count, const svxg_node* const* node
   return SVXG_OK;
 }
 
-int svxg_graph_results(svxg_problem* p, int32_t count, double* rel_res, int32_t* converged, int32_t* iters) {
+int svxg_graph_results(svxg_problem* p, int32_t count, double* rel_res, int32_t* converged, int32_t* iters,
+                       double* err_est) {
   CHECK_P(p);
   Problem& P = p->P;
   if (P.seg_n <= 0 || count != P.seg_n) {
@@ -664,7 +665,7 @@ int svxg_graph_results(svxg_problem* p, int32_t count, double* rel_res, int32_t*
     return SVXG_ERR_STATE;
   }
   DeviceScope ds(P.device);
-  return seg_results(P, rel_res, converged, iters);
+  return seg_results(P, rel_res, converged, iters, err_est);
 }
 
 int svxg_set_graph(svxg_problem* p, const svxg_node* nodes, int32_t n, const svxg_bond* bonds, int32_t nb,
@@ -945,6 +946,9 @@ static int solve_common(Problem& P, const double* f_dev, double* u_dev, double r
   trace_mark(P, "solve: begin");
   TRY(pcg_iterate(P, maxit < 0 ? 100000 : maxit, rtol, res));
   trace_mark(P, "solve: iterate");
+  // (the mixed-precision policy states each solve's error: the estimate of solve.cu error_estimate)
+  P.last_err_est = 0.0;
+  if (P.opt.precision != SVXG_PRECISION_FP64 && res && std::isfinite(res->rel_res)) TRY(error_estimate(P));
   TRY(gather_solution(P, u_dev));
   P.active = false;
   return SVXG_OK;
@@ -1216,6 +1220,7 @@ int svxg_get_info(svxg_problem* p, svxg_info* info) {
   info->device_bytes = P.mem.bytes;
   info->precision = P.opt.precision;
   info->mixed_fallbacks = P.mixed_fallbacks;
+  info->error_estimate = P.last_err_est;
   if (P.have_graph)
     info->graph_bytes = int64_t(sizeof(svxg_node)) * std::max<int64_t>(P.n, 1) +
                         int64_t(sizeof(svxg_bond)) * std::max<int64_t>(P.nb, 1) +

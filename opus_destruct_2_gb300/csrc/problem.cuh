@@ -203,6 +203,7 @@ struct Problem {
   void* h_ms = nullptr;           // ... pinned mirror
   int32_t mx_maxit = 0;
   int32_t mixed_fallbacks = 0;    // mixed runs finished by the FP64 sequence (since assemble)
+  double last_err_est = 0.0;      // the last mixed-policy solve's error estimate (solve.cu error_estimate)
   double* d_partials = nullptr;   // block partial sums
   unsigned* d_counter = nullptr;  // last-block counters
   int32_t partial_blocks = 0;
@@ -267,7 +268,8 @@ int free_run(Problem& P);
 int tune_k64(Problem& P);
 int time_cg_spmv(Problem& P, int32_t reps, float* ms_per_launch);    // solve.cu
 int seg_prepare(Problem& P);   // solve.cu: a batch's free-row offsets and per-graph scalars after assembly
-int seg_results(Problem& P, double* rel_res, int32_t* converged, int32_t* iters);  // solve.cu: per graph
+int seg_results(Problem& P, double* rel_res, int32_t* converged, int32_t* iters, double* err_est);  // solve.cu
+int error_estimate(Problem& P);  // solve.cu: ||M^-1 r|| / ||x|| after a solve (per graph in a batch)
 int seg_launch(Problem& P, int op, const double* a, const double* b, double rtol);  // solve.cu
 int time_cg_spmv32(Problem& P, int32_t reps, float* ms_per_launch);  // mixed.cu
 int measure_fp64_rate(int device, double* tflops);                    // tune.cu

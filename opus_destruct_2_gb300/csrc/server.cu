@@ -326,6 +326,7 @@ int run_new(svxg_problem* p, Request& q, svxg_request_result* res) {
   res->converged = r.converged;
   res->breakdown = r.breakdown;
   res->rel_res = r.rel_res;
+  res->err_est = p->P.last_err_est;
   return judge_into(p, q, res);
 }
 
@@ -346,6 +347,7 @@ int run_repeat(svxg_problem* p, Request& q, svxg_request_result* res) {
   res->converged = r.converged;
   res->breakdown = r.breakdown;
   res->rel_res = r.rel_res;
+  res->err_est = p->P.last_err_est;
   return judge_into(p, q, res);
 }
 
@@ -417,7 +419,8 @@ int run_batch(svxg_problem* p, std::vector<Request>& B, std::vector<svxg_request
   if (e) return e;
   std::vector<double> rel(cnt, 0.0);
   std::vector<int32_t> conv(cnt, 0), iters(cnt, 0);
-  e = svxg_graph_results(p, count, rel.data(), conv.data(), iters.data());
+  std::vector<double> est(cnt, 0.0);
+  e = svxg_graph_results(p, count, rel.data(), conv.data(), iters.data(), est.data());
   if (e) return e;
   std::vector<int32_t> over(size_t(std::max(p->P.nb, 1)));
   int32_t n_over = 0;
@@ -426,6 +429,7 @@ int run_batch(svxg_problem* p, std::vector<Request>& B, std::vector<svxg_request
   for (size_t g = 0; g < cnt; ++g) {
     svxg_request_result& r = res[g];
     r.iters = iters[g];
+    r.err_est = est[g];
     r.breakdown = pr.breakdown;
     r.converged = conv[g] && !pr.breakdown;
     r.rel_res = pr.breakdown && !std::isfinite(pr.rel_res) ? INFINITY : rel[g];
@@ -473,7 +477,8 @@ int run_bundle_repeats(Bundle& b, std::vector<Request>& R, const std::vector<int
   if (e) return e;
   std::vector<double> rel(count, 0.0);
   std::vector<int32_t> conv(count, 0), iters(count, 0);
-  e = svxg_graph_results(p, int32_t(count), rel.data(), conv.data(), iters.data());
+  std::vector<double> est(count, 0.0);
+  e = svxg_graph_results(p, int32_t(count), rel.data(), conv.data(), iters.data(), est.data());
   if (e) return e;
   std::vector<int32_t> over(size_t(std::max(p->P.nb, 1)));
   int32_t n_over = 0;
@@ -484,6 +489,7 @@ int run_bundle_repeats(Bundle& b, std::vector<Request>& R, const std::vector<int
     svxg_request_result& r = res[i];
     r.warm = 1;
     r.iters = iters[g];
+    r.err_est = est[g];
     r.breakdown = pr.breakdown;
     r.converged = conv[g] && !pr.breakdown;
     r.rel_res = pr.breakdown && !std::isfinite(pr.rel_res) ? INFINITY : rel[g];

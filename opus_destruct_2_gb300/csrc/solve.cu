@@ -468,11 +468,12 @@ __global__ void k_jacobi_apply(int32_t nfree, const double* __restrict__ jinv, c
 // shared by all. A graph's dots are sums in a fixed order (one block per graph, thread t over
 // entries t, t + 256, ..., then a fixed tree): the same bits whatever else the batch holds. The last
 // block to finish a reduction sets the run's flags: done when no graph is still running.
-// seg (kSegF doubles per graph): ||f||, target, ||r||, r.z, p.q, alpha, beta, iterations at its end;
+// seg (kSegF doubles per graph): ||f||, target, ||r||, r.z, p.q, alpha, beta, iterations at its end,
+// and for the error estimate after the solve ||M^-1 r||^2, ||x||^2;
 // flag per graph: 0 running, 1 converged, 2 broken down.
 constexpr int kSegT = 256;
-constexpr int kSegF = 8;
-enum SegOp { kSegBn = 0, kSegRz0 = 1, kSegStart = 2, kSegPq = 3, kSegRn = 4, kSegRz = 5 };
+constexpr int kSegF = 10;
+enum SegOp { kSegBn = 0, kSegRz0 = 1, kSegStart = 2, kSegPq = 3, kSegRn = 4, kSegRz = 5, kSegZz = 6, kSegXx = 7 };
 
 template <int OP>
 __global__ void __launch_bounds__(kSegT) k_seg_reduce(int32_t nseg, const int32_t* __restrict__ row0,
@@ -497,6 +498,10 @@ __global__ void __launch_bounds__(kSegT) k_seg_reduce(int32_t nseg, const int32_
     const double v = sh[0];
     if (OP == kSegBn) {
       q[0] = sqrt(v);
+    } else if (OP == kSegZz) {
+      q[8] = v;
+    } else if (OP == kSegXx) {
+      q[9] = v;
     } else if (OP == kSegRz0) {
       q[3] = v;
     } else if (OP == kSegStart) {
@@ -535,7 +540,7 @@ __global__ void __launch_bounds__(kSegT) k_seg_reduce(int32_t nseg, const int32_
     last = atomicAdd(counter, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (!last || OP == kSegBn || OP == kSegRz0) {
+  if (!last || OP == kSegBn || OP == kSegRz0 || OP == kSegZz || OP == kSegXx) {
     if (last && threadIdx.x == 0) *counter = 0u;
     return;
   }
@@ -1183,6 +1188,14 @@ int seg_launch(Problem& P, int op, const double* a, const double* b, double rtol
       (k_seg_reduce<kSegRn><<<g, kSegT, 0, P.stream>>>(P.seg_n, P.d_seg_row, a, b, rtol, P.d_seg, P.d_seg_flag,
                                                         P.d_partials, ctr, P.d_s), SVXG_COUNT_LAUNCH());
       break;
+    case kSegZz:
+      (k_seg_reduce<kSegZz><<<g, kSegT, 0, P.stream>>>(P.seg_n, P.d_seg_row, a, b, rtol, P.d_seg, P.d_seg_flag,
+                                                        P.d_partials, ctr, P.d_s), SVXG_COUNT_LAUNCH());
+      break;
+    case kSegXx:
+      (k_seg_reduce<kSegXx><<<g, kSegT, 0, P.stream>>>(P.seg_n, P.d_seg_row, a, b, rtol, P.d_seg, P.d_seg_flag,
+                                                        P.d_partials, ctr, P.d_s), SVXG_COUNT_LAUNCH());
+      break;
     default:
       (k_seg_reduce<kSegRz><<<g, kSegT, 0, P.stream>>>(P.seg_n, P.d_seg_row, a, b, rtol, P.d_seg, P.d_seg_flag,
                                                         P.d_partials, ctr, P.d_s), SVXG_COUNT_LAUNCH());
@@ -1193,7 +1206,7 @@ int seg_launch(Problem& P, int op, const double* a, const double* b, double rtol
 
 // per graph of a batch after a solve: ||r_g|| / ||f_g|| (0 without load), whether it met its target,
 // and the iterations its sequence ran
-int seg_results(Problem& P, double* rel_res, int32_t* converged, int32_t* iters) {
+int seg_results(Problem& P, double* rel_res, int32_t* converged, int32_t* iters, double* err_est) {
   if (P.seg_n <= 0 || !P.d_seg) return SVXG_ERR_STATE;
   std::vector<double> h(size_t(kSegF) * size_t(P.seg_n));
   std::vector<int32_t> fl(size_t(P.seg_n));
@@ -1206,7 +1219,58 @@ int seg_results(Problem& P, double* rel_res, int32_t* converged, int32_t* iters)
     if (rel_res) rel_res[g] = q[0] > 0.0 ? q[2] / q[0] : 0.0;
     if (converged) converged[g] = fl[size_t(g)] == 1 ? 1 : 0;
     if (iters) iters[g] = fl[size_t(g)] == 0 ? P.h_s->iters : int32_t(q[7]);
+    if (err_est) err_est[g] = q[9] > 0.0 ? sqrt(q[8] / q[9]) : 0.0;
   }
+  return SVXG_OK;
+}
+
+// ||z||^2 and ||x||^2 over the free DOFs (two-level, fixed order)
+__global__ void k_norm_pair(int32_t nf, const double* __restrict__ z, const double* __restrict__ x, double* partials,
+                            unsigned* counter, double* out) {
+  __shared__ double sh[kVecT / 32];
+  const int32_t i = blockIdx.x * kVecT + threadIdx.x;
+  double v[2] = {0.0, 0.0};
+  if (i < nf)
+    for (int c = 0; c < 6; ++c) {
+      const double a = z[6 * int64_t(i) + c], b = x[6 * int64_t(i) + c];
+      v[0] += a * a;
+      v[1] += b * b;
+    }
+  double bs[2];
+  bs[0] = block_sum<kVecT>(v[0], sh);
+  bs[1] = block_sum<kVecT>(v[1], sh);
+  if (publish<2>(bs, partials, counter)) {
+    double tot[2];
+    gather_totals<kVecT, 2>(partials, counter, tot, sh);
+    if (threadIdx.x == 0) {
+      out[0] = tot[0];
+      out[1] = tot[1];
+    }
+  }
+}
+
+// The solve's error estimate, ||M^-1 r|| / ||x||: one application of the preconditioner to the
+// final residual (the FP64 one: the mixed run's last outer residual, the FP64 sequence's own),
+// which a multigrid close to K^-1 maps close to the error x* - x itself. Per graph in a batch.
+int error_estimate(Problem& P) {
+  P.last_err_est = 0.0;
+  if (P.nfree <= 0 || !P.d_x) return SVXG_OK;
+  P.cycle_stop = nullptr;
+  TRY(precondition(P, P.d_r, P.d_z));
+  if (P.seg_n > 0) {
+    TRY(seg_launch(P, kSegZz, P.d_z, P.d_z, 0.0));
+    TRY(seg_launch(P, kSegXx, P.d_x, P.d_x, 0.0));
+    return SVXG_OK;
+  }
+  double* out = nullptr;
+  SVXG_CUDA(pool_malloc_async(reinterpret_cast<void**>(&out), 2 * sizeof(double), P.stream));
+  (k_norm_pair<<<vec_blocks(P.nfree), kVecT, 0, P.stream>>>(P.nfree, P.d_z, P.d_x, P.d_partials, P.d_counter, out),
+   SVXG_COUNT_LAUNCH());
+  double h[2] = {0.0, 0.0};
+  SVXG_CUDA(cudaMemcpyAsync(h, out, sizeof(h), cudaMemcpyDeviceToHost, P.stream));
+  cudaFreeAsync(out, P.stream);
+  SVXG_CUDA(host_wait(P.stream));
+  P.last_err_est = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : 0.0;
   return SVXG_OK;
 }
 

@@ -24,7 +24,7 @@ c_i32, c_i64, c_f64, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, cty
 class RequestResult(ctypes.Structure):
     _fields_ = [("ticket", c_i64), ("status", c_i32), ("iters", c_i32), ("converged", c_i32),
                 ("breakdown", c_i32), ("failing", c_i32), ("warm", c_i32), ("rel_res", c_f64),
-                ("queue_ms", c_f64), ("latency_ms", c_f64), ("pad", c_f64)]
+                ("queue_ms", c_f64), ("latency_ms", c_f64), ("err_est", c_f64)]
 
 
 class ServingStats(ctypes.Structure):

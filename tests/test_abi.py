@@ -35,7 +35,7 @@ def test_library_exports_every_declared_function():
 def test_record_layouts():
     assert NODE_DTYPE.itemsize == 40 and BOND_DTYPE.itemsize == 216 and MATERIAL_DTYPE.itemsize == 64
     assert ctypes.sizeof(StressOptions) == 72 and ctypes.sizeof(PcgResult) == 24
-    assert ctypes.sizeof(Info) == 16 + 64 + 256 + 40 + 8 + 8 + 8
+    assert ctypes.sizeof(Info) == 16 + 64 + 256 + 40 + 8 + 8 + 8 + 8
 
 
 def test_built_for_sm_103a():

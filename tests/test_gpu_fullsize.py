@@ -5,7 +5,9 @@ Bars: K and the whole multigrid hierarchy's integer structure (level sizes, bloc
 prolongation sizes, work counters) bit for bit; u within 1e-6 relative for the FP64 solve and
 1e-5 for the mixed-precision one (FP32 K and V-cycle inside FP64 refinement), both solved to
 rel. residual 1e-10; the set of failing bonds identical; the device's residual, recomputed on the
-host from the device's own K, at the requested tolerance."""
+host from the device's own K, at the requested tolerance. The mixed-precision configuration itself:
+the same city at rel. residual 1e-6 with per-bond thresholds (strength x U(0.9, 1.1)), its
+failure set identical to the oracle's, its error within 1e-5 and its error estimate stated."""
 import numpy as np
 import pytest
 
@@ -73,3 +75,25 @@ def test_city_block_mixed(city):
     assert residual(G, u, city["f"]) <= 1e-10 * 1.01
     _, _, failing = G.utilization(1.0)
     assert np.array_equal(np.sort(failing), city["failing"])
+
+
+def test_city_block_mixed_at_1e6_jittered_thresholds(city):
+    b = city["bonds"].copy()
+    b["strength"] = b["strength"] * np.random.default_rng(2468).uniform(0.9, 1.1, size=len(b))
+    J = oracle.Port(city["nodes"], b, city["mats"])
+    _, phi_o, _ = J.judge(city["uo"])  # (strength is not in K: the oracle's u stands)
+    G = StressProblem(city["nodes"], b, city["mats"])
+    assert G.assemble(StressOptions(precision=1))  # (the policy: FP32 inner sequences at this size)
+    u, r = G.solve(city["f"], rtol=1e-6, maxit=2000)
+    assert r.converged and r.rel_res <= 1e-6
+    err = relerr(u, city["uo"])
+    est = G.info().error_estimate
+    print(f"city, mixed at 1e-6: error {err:.2e} (max norm), estimate {est:.2e}, {r.iters} iterations")
+    assert err <= 1e-5 and est > 0.0
+    phi, _, failing = G.utilization(1.0)
+    e = float(np.max(np.abs(phi - phi_o)))
+    band = np.nonzero(np.abs(phi_o - 1.0) <= e)[0]
+    want = np.nonzero(phi_o >= 1.0)[0]
+    print(f"city: {len(want)} failing, min |phi - 1| {float(np.min(np.abs(phi_o - 1.0))):.3e}, phi error {e:.2e}, "
+          f"bonds within the error band: {band.tolist()}")
+    assert np.array_equal(np.sort(failing), want), (np.setxor1d(failing, want).tolist(), band.tolist())

@@ -1,7 +1,9 @@
 """Mixed precision (FP32 K SpMV and FP32 V-cycle inside FP64 iterative refinement) against the
-oracle's FP64 solve: displacements and bond loads within 1e-5 (relative) at rel. residual 1e-6,
-the failure set identical outside the solve's error band, and the FP64 refinement reaching the
-tight tolerances the plain solve reaches."""
+oracle's FP64 solve: displacements within 1e-5 (relative) at rel. residual 1e-6, each solve's
+error estimate (||M^-1 r|| / ||u||) within a factor 20 of its measured error, the failure set
+identical with per-bond thresholds drawn as material strength x U(0.9, 1.1) (bonds within the
+solve's error band of phi = 1 listed, none dropped), and the FP64 refinement reaching the tight
+tolerances the plain solve reaches."""
 import numpy as np
 import pytest
 
@@ -38,13 +40,13 @@ def test_mixed_matches_fp64_oracle(name):
     O = Port(nodes, bonds, MATS)
     O.assemble(StressOptions(**opts))
     uo, ro = O.solve(f, rtol=1e-12, maxit=5000)
-    # the bar at rel. residual 1e-6 is the solve's conditioning times 1e-6; the refinement's
-    # result is the FP64 operator's, so it is held to the FP64 solve at the same residual
-    G64 = StressProblem(nodes, bonds, MATS)
-    assert G64.assemble(StressOptions(**opts))
-    u64, r64 = G64.solve(f, rtol=1e-6, maxit=2000)
-    e_mixed, e_plain = relerr(u, uo), relerr(u64, uo)
-    assert e_mixed <= max(1e-5, 3.0 * e_plain), (e_mixed, e_plain)
+    e_mixed = relerr(u, uo)
+    assert e_mixed <= 1e-5, e_mixed
+    # the solve's own statement of its error (against the FP64 solution), in the 2-norm
+    est = G.info().error_estimate
+    e2 = float(np.linalg.norm(u - uo) / np.linalg.norm(uo))
+    print(f"{name}: error {e2:.2e}, estimate {est:.2e}")
+    assert e2 / 20.0 <= est <= 20.0 * e2 + 1e-14, (est, e2)
     # at rel. residual 1e-10 both reach the 1e-6 bar
     u2, r2 = G.solve(f, rtol=1e-10, maxit=4000)
     assert r2.converged and relerr(u2, uo) <= 1e-6
@@ -54,26 +56,60 @@ def test_mixed_matches_fp64_oracle(name):
         assert np.max(np.abs(lg[k] - lo[k])) <= 1e-5 * max(scale, 1e-300) + 1e-6 * np.max(np.abs(lo[k]))
 
 
+def jittered(bonds, seed):
+    """Per-bond thresholds: each bond's strength (the multiplier of all four of its criteria) times
+    U(0.9, 1.1), from a recorded seed."""
+    b = bonds.copy()
+    b["strength"] = b["strength"] * np.random.default_rng(seed).uniform(0.9, 1.1, size=len(b))
+    return b
+
+
+def same_failures(phi, phi_o, what):
+    """The failure sets equal; bonds whose oracle phi lies within the measured phi error of 1 are
+    listed in the message (none is dropped from the comparison)."""
+    err = float(np.max(np.abs(phi - phi_o)))
+    band = np.nonzero(np.abs(phi_o - 1.0) <= err)[0]
+    a, b = np.nonzero(phi >= 1.0)[0], np.nonzero(phi_o >= 1.0)[0]
+    print(f"{what}: {len(b)} failing, min |phi - 1| {float(np.min(np.abs(phi_o - 1.0))):.3e}, phi error {err:.2e}, "
+          f"bonds within the error band: {band.tolist()}")
+    assert np.array_equal(a, b), (what, np.setxor1d(a, b).tolist(), band.tolist())
+
+
 @pytest.mark.parametrize("name", ["tower10", "piece_free"])
 def test_mixed_failure_set(name):
     make, opts = CASES[name]
     nodes, bonds = make()
+    bonds = jittered(bonds, seed=1234)
     f = fx.gravity_live(nodes)
     O = Port(nodes, bonds, MATS)
     O.assemble(StressOptions(**opts))
     uo, _ = O.solve(f, rtol=1e-12, maxit=5000)
     _, po, _ = O.judge(uo)
-    frag = 1.0 / float(np.quantile(po[po > 0], 0.85))
-    _, po, mo = O.judge(uo, frag)
+    frag = 1.0 / float(np.quantile(po[po > 0], 0.85))  # (about 15 % of the bonds over strength)
+    _, po, _ = O.judge(uo, frag)
     G = StressProblem(nodes, bonds, MATS)
     assert G.assemble(StressOptions(precision=MIXED, **opts))
     u, res = G.solve(f, rtol=1e-6, maxit=2000)
+    assert res.converged
     phi, mode, over = G.utilization(frag)
-    band = np.abs(phi - po) .max()
-    safe = np.abs(po - 1.0) > 2 * band
-    assert np.array_equal((phi >= 1.0)[safe], (po >= 1.0)[safe])
-    print(f"{name}: failing {int((po >= 1).sum())} bonds, min |phi-1| {np.min(np.abs(po - 1)):.2e}, "
-          f"phi error {band:.2e}, {int((~safe).sum())} bonds inside the error band")
+    same_failures(phi, po, name)
+
+
+def test_tower_config_mixed_policy_failures():
+    """The CPU-runnable configuration (10-storey tower of about 2,000 fragments) under the
+    mixed-precision policy at rel. residual 1e-6, thresholds jittered per bond, fragility 1."""
+    nodes, bonds, f, mats = synth.tower_graph(storeys=10, seed=1)
+    bonds = jittered(bonds, seed=4321)
+    O = Port(nodes, bonds, mats)
+    O.assemble(StressOptions())
+    uo, _ = O.solve(f, rtol=1e-12, maxit=5000)
+    _, po, _ = O.judge(uo)
+    G = StressProblem(nodes, bonds, mats)
+    assert G.assemble(StressOptions(precision=1))
+    u, res = G.solve(f, rtol=1e-6, maxit=2000)
+    assert res.converged and relerr(u, uo) <= 1e-5
+    phi, _, _ = G.utilization(1.0)
+    same_failures(phi, po, "tower10 (mixed policy, rtol 1e-6)")
 
 
 def test_mixed_cap_and_resume_and_edge_loads():
