@@ -181,6 +181,30 @@ int svxg_utilization_noalloc(const svxg_node* nodes_dev, int32_t n, const svxg_b
                              const svxg_material* mats_dev, const double* u_dev, double fragility, double* phi_dev,
                              uint8_t* mode_dev, int32_t* over_dev, int32_t* n_over, void* stream);
 
+/* bond_strength / bond_utilization (stress.hpp:53-66, stress.cpp:14-57), the reference's free
+ * functions, on the host from the same source as the device judge: out = ft, fb, fc, cohesion,
+ * friction of the bond at `fragility`; utilization returns phi (-1 for a bad material id) and the
+ * governing mode (SVXG_FAIL_*) in *mode (may be null). */
+int svxg_bond_strength(const svxg_bond* b, double fragility, const svxg_material* mats, double* out);
+double svxg_bond_utilization(const svxg_bond* b, const svxg_bond_load* L, double fragility, const svxg_material* mats,
+                             uint8_t* mode);
+
+/* --- loads ------------------------------------------------------------------------------------ */
+/* World::Impl::load_vector (core/src/world/world.cpp:966-974): f (6 n) = each node's weight down z
+ * plus ext (6 n, the loads applied to the structure; may be null). Host arrays. */
+int svxg_structure_loads(int32_t n, const double* weight, const double* ext, double* f);
+/* pin_reference (core/src/world/world_pieces.cpp:313-326): every node's `fixed` cleared, then the
+ * node nearest com (the first of equals) fixed; returns its index (-1: no nodes). */
+int32_t svxg_pin_reference(svxg_node* nodes, int32_t n, svxg_v3 com);
+/* A loose piece's load (World::Impl::body_stress_run, world_pieces.cpp:566-603): with `inertia`,
+ * each node's inertial relief from the piece's acceleration under gravity and the point forces -
+ * translation and rotation of its centre (node_com, shape frame), its mass and inertia (node_inertia,
+ * 9 per node, body frame) - then every point force on its node through add_force, in the shape
+ * frame. f: 6 n, written. Host arrays. */
+int svxg_body_loads(const svxg_body_state* b, const svxg_node* nodes, int32_t n, const svxg_v3* node_com,
+                    const double* node_mass, const double* node_inertia, const svxg_point_force* forces,
+                    int32_t nforces, int32_t inertia, double* f);
+
 /* --- bonds from voxel faces -------------------------------------------------------------------- */
 /* Replaces SecAcc::finish (finish_lattice / finish_general) + section_strengths /
  * section_strengths_general (core/src/world/world_internal.hpp:130-441), the section geometry

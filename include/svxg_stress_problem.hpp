@@ -389,4 +389,47 @@ inline std::vector<svxg_bond> build_bonds(const std::vector<svxg_node>& nodes, c
   return out;
 }
 
+// bond_strength / bond_utilization (stress.hpp:53-66): the reference's free functions, the same
+// arithmetic as the device judge. strength: {ft, fb, fc, cohesion, friction}; a bad material id
+// gives phi -1 and an empty strength.
+inline std::vector<double> bond_strength(const svxg_bond& b, double fragility, const std::vector<svxg_material>& mats) {
+  std::vector<double> s(5);
+  if (mats.size() < SVXG_MAX_MATERIALS || svxg_bond_strength(&b, fragility, mats.data(), s.data()) != SVXG_OK) return {};
+  return s;
+}
+inline double bond_utilization(const svxg_bond& b, const svxg_bond_load& L, double fragility,
+                               const std::vector<svxg_material>& mats, uint8_t* mode = nullptr) {
+  if (mats.size() < SVXG_MAX_MATERIALS) return -1.0;
+  return svxg_bond_utilization(&b, &L, fragility, mats.data(), mode);
+}
+
+// The world's loads (svxg_structure_loads, svxg_pin_reference, svxg_body_loads): a structure's
+// load vector (World::Impl::load_vector, world.cpp:966-974), a free piece's pinned node
+// (pin_reference, world_pieces.cpp:313-326) and a moving piece's loads (world_pieces.cpp:566-603).
+inline std::vector<double> load_vector(const std::vector<double>& weight, const std::vector<double>& ext = {}) {
+  std::vector<double> f(6 * weight.size());
+  if (!ext.empty() && ext.size() != f.size()) return {};
+  if (svxg_structure_loads(int32_t(weight.size()), weight.data(), ext.empty() ? nullptr : ext.data(), f.data()) !=
+      SVXG_OK)
+    return {};
+  return f;
+}
+inline int32_t pin_reference(std::vector<svxg_node>& nodes, svxg_v3 com) {
+  return svxg_pin_reference(nodes.data(), int32_t(nodes.size()), com);
+}
+// node_inertia: 9 per node (body frame, about node_com); forces name their node (-1: none)
+inline std::vector<double> body_loads(const svxg_body_state& b, const std::vector<svxg_node>& nodes,
+                                      const std::vector<svxg_v3>& node_com, const std::vector<double>& node_mass,
+                                      const std::vector<double>& node_inertia,
+                                      const std::vector<svxg_point_force>& forces, bool inertia) {
+  const size_t n = nodes.size();
+  if (inertia && (node_com.size() != n || node_mass.size() != n || node_inertia.size() != 9 * n)) return {};
+  std::vector<double> f(6 * n);
+  if (svxg_body_loads(&b, nodes.data(), int32_t(n), inertia ? node_com.data() : nullptr,
+                      inertia ? node_mass.data() : nullptr, inertia ? node_inertia.data() : nullptr, forces.data(),
+                      int32_t(forces.size()), inertia ? 1 : 0, f.data()) != SVXG_OK)
+    return {};
+  return f;
+}
+
 }  // namespace svxg

@@ -66,6 +66,30 @@ typedef struct svxg_material {
   double ft, fb, fc, cohesion, friction;
 } svxg_material;
 
+/* A moving piece's rigid-body state for its loads (the world's Body, core/include/svx/phys/rigid.hpp):
+ * centre of mass x (world), orientation q (x, y, z, w), centre of mass in the shape frame com,
+ * angular velocity w (world), inertia and its inverse (body frame, row-major), 1 / mass, and
+ * gravity's magnitude (along -z). 200 bytes. */
+typedef struct svxg_body_state {
+  svxg_v3 x;
+  double q[4];
+  svxg_v3 com;
+  svxg_v3 w;
+  double inertia[9];
+  double inv_inertia[9];
+  double inv_mass;
+  double gravity;
+} svxg_body_state;
+
+/* A point force on a piece: F at point p (both world), acting on graph node `node` (the world's
+ * fragment-to-node map; out of range: it enters the piece's motion only). 56 bytes. */
+typedef struct svxg_point_force {
+  svxg_v3 F;
+  svxg_v3 p;
+  int32_t node;
+  int32_t pad;
+} svxg_point_force;
+
 typedef struct svxg_amg_options {
   int32_t coarse_max;     /* dense solve at or below this many nodes (48) */
   int32_t smoothed;       /* smoothed aggregation (1) */

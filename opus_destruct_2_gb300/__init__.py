@@ -78,6 +78,10 @@ def load_library() -> ctypes.CDLL:
         "svxg_set_graphs_device": (c_i32, [c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp]),
         "svxg_graph_results": (c_i32, [c_vp, c_i32, c_vp, c_vp, c_vp, c_vp]),
         "svxg_time_spmv": (c_i32, [c_vp, c_i32, c_i32, ctypes.POINTER(c_f64)]),
+        "svxg_structure_loads": (c_i32, [c_i32, c_vp, c_vp, c_vp]),
+        "svxg_body_loads": (c_i32, [c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_i32, c_i32, c_vp]),
+        "svxg_bond_strength": (c_i32, [c_vp, c_f64, c_vp, c_vp]),
+        "svxg_bond_utilization": (c_f64, [c_vp, c_vp, c_f64, c_vp, c_vp]),
         "svxg_measure_fp64_rate": (c_i32, [c_i32, ctypes.POINTER(c_f64)]),
         "svxg_assemble": (c_i32, [c_vp, c_vp, ctypes.POINTER(c_i32)]),
         "svxg_assembled": (c_i32, [c_vp]),
@@ -541,3 +545,49 @@ class Batch:
         i = Info()
         _check(self._L.svxg_get_info(self._h, ctypes.byref(i)))
         return i
+
+
+# ---- loads and the judge's free functions (host) ----------------------------------------------------
+
+def structure_loads(weight, ext=None) -> np.ndarray:
+    """World::Impl::load_vector (world.cpp:966-974): each node's weight down z plus ext (6 per node)."""
+    w = np.ascontiguousarray(weight, dtype=np.float64)
+    e = None if ext is None else np.ascontiguousarray(ext, dtype=np.float64)
+    f = np.zeros(6 * len(w))
+    _check(load_library().svxg_structure_loads(len(w), ptr(w), ptr(e), ptr(f)))
+    return f
+
+
+def pin_reference(nodes, com) -> int:
+    """pin_reference (world_pieces.cpp:313-326): `fixed` cleared, the node nearest com fixed (in
+    place, nodes a NODE_DTYPE array); returns its index."""
+    from .graph import V3
+    fn = load_library().svxg_pin_reference
+    fn.restype, fn.argtypes = c_i32, [c_vp, c_i32, V3]
+    if nodes.dtype != NODE_DTYPE or not nodes.flags["C_CONTIGUOUS"]:
+        raise ValueError("nodes: a contiguous NODE_DTYPE array (changed in place)")
+    return int(fn(ptr(nodes), len(nodes), V3(*[float(v) for v in com])))
+
+
+def body_loads(state, nodes, forces, node_com=None, node_mass=None, node_inertia=None, inertia: bool = True):
+    """A loose piece's load (world_pieces.cpp:566-603): state a graph.BodyState, forces a
+    POINT_FORCE_DTYPE array, node_com (n x 3), node_mass (n), node_inertia (n x 9) for the inertial
+    relief. Returns f (6 per node)."""
+    from .graph import POINT_FORCE_DTYPE
+    nodes = np.ascontiguousarray(nodes, dtype=NODE_DTYPE)
+    forces = np.ascontiguousarray(forces, dtype=POINT_FORCE_DTYPE)
+    arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (node_com, node_mass,
+                                                                                        node_inertia)]
+    f = np.zeros(6 * len(nodes))
+    _check(load_library().svxg_body_loads(ctypes.byref(state), ptr(nodes), len(nodes), ptr(arrs[0]), ptr(arrs[1]),
+                                          ptr(arrs[2]), ptr(forces), len(forces), int(bool(inertia)), ptr(f)))
+    return f
+
+
+def bond_utilization(bond, load, fragility: float, mats):
+    """bond_utilization (stress.cpp:23-57) of one bond record under one load record: (phi, mode)."""
+    b = np.ascontiguousarray(np.array([bond], dtype=BOND_DTYPE))
+    ld = np.ascontiguousarray(np.array([load], dtype=LOAD_DTYPE))
+    mode = np.zeros(1, np.uint8)
+    phi = load_library().svxg_bond_utilization(ptr(b), ptr(ld), float(fragility), ptr(mats), ptr(mode))
+    return float(phi), int(mode[0])

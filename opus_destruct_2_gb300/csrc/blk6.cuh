@@ -222,10 +222,9 @@ SVXG_HD void mul6_add(const double* A, const double* B, double* C) {
     }
 }
 
-// bond_strength / bond_utilization (stress.cpp:14-57); mode: SVXG_FAIL_*
-SVXG_HD double bond_utilization(const svxg_bond& b, const svxg_bond_load& L, double fragility,
-                                const svxg_material* mats, uint8_t* mode) {
-  double S[5];
+// bond_strength (stress.cpp:14-21): ft, fb, fc, cohesion, friction of the weaker side (or the
+// bond's own section), scaled by strength / fragility
+SVXG_HD void bond_strength(const svxg_bond& b, double fragility, const svxg_material* mats, double* S) {
   const double s = b.strength / maxd(1e-6, fragility);
   if (b.sectioned) {
     S[0] = s * (double)b.ft;
@@ -242,6 +241,13 @@ SVXG_HD double bond_utilization(const svxg_bond& b, const svxg_bond_load& L, dou
     S[3] = s * mind(A.cohesion, B.cohesion);
     S[4] = mind(A.friction, B.friction);
   }
+}
+
+// bond_utilization (stress.cpp:23-57); mode: SVXG_FAIL_*
+SVXG_HD double bond_utilization(const svxg_bond& b, const svxg_bond_load& L, double fragility,
+                                const svxg_material* mats, uint8_t* mode) {
+  double S[5];
+  bond_strength(b, fragility, mats, S);
   const double kWeakest = 1e-9;
   S[0] = maxd(S[0], kWeakest);
   S[1] = maxd(S[1], kWeakest);

@@ -256,3 +256,20 @@ def default_fracture_energies() -> np.ndarray:
 
 def ptr(a: np.ndarray | None):
     return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+class V3(ctypes.Structure):
+    """svxg_v3 by value."""
+    _fields_ = [("x", ctypes.c_double), ("y", ctypes.c_double), ("z", ctypes.c_double)]
+
+
+class BodyState(ctypes.Structure):
+    """svxg_body_state: a moving piece's rigid-body state (x, q = (x, y, z, w), com in the shape
+    frame, angular velocity w, body-frame inertia and inverse, 1 / mass, gravity)."""
+    _fields_ = [("x", ctypes.c_double * 3), ("q", ctypes.c_double * 4), ("com", ctypes.c_double * 3),
+                ("w", ctypes.c_double * 3), ("inertia", ctypes.c_double * 9), ("inv_inertia", ctypes.c_double * 9),
+                ("inv_mass", ctypes.c_double), ("gravity", ctypes.c_double)]
+
+
+POINT_FORCE_DTYPE = np.dtype([("F", np.float64, 3), ("p", np.float64, 3), ("node", np.int32), ("pad", np.int32)],
+                             align=True)

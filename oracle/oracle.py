@@ -22,8 +22,8 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 import build_oracle  # noqa: E402
-from opus_destruct_2_gb300.graph import (BOND_DTYPE, LOAD_DTYPE, MATERIAL_DTYPE, NODE_DTYPE, PcgResult,  # noqa: E402
-                                         StressOptions, ptr)
+from opus_destruct_2_gb300.graph import (BOND_DTYPE, LOAD_DTYPE, MATERIAL_DTYPE, NODE_DTYPE,  # noqa: E402
+                                         POINT_FORCE_DTYPE, V3, PcgResult, StressOptions, ptr)
 
 c_i32, c_i64, c_f64, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p
 
@@ -84,6 +84,10 @@ def port_lib() -> ctypes.CDLL:
         lib.svxo_assembled.argtypes = [c_vp]
         lib.svxo_preconditioner_current.argtypes = [c_vp]
         lib.svxo_seq_sum.argtypes = [c_vp, c_i64]
+        lib.svxo_structure_loads.argtypes = [c_i32, c_vp, c_vp, c_vp]
+        lib.svxo_pin_reference.restype = c_i32
+        lib.svxo_pin_reference.argtypes = [c_vp, c_i32, V3]
+        lib.svxo_body_loads.argtypes = [c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_i32, c_i32, c_vp]
         _port = lib
     return _port
 
@@ -132,6 +136,7 @@ def reference_lib() -> ctypes.CDLL | None:
         lib.svxr_p_judge.argtypes = [c_vp, c_vp, c_f64, c_vp, c_vp, c_vp]
         lib.svxr_p_utilization_many.argtypes = [c_vp, c_vp, c_f64, c_vp, c_vp]
         lib.svxr_p_matrix.argtypes = [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]
+        lib.svxr_body_loads.argtypes = [c_vp, c_vp, c_i32, c_vp, c_vp, c_vp, c_vp, c_i32, c_i32, c_vp]
         _ref = lib
     return _ref
 
@@ -141,6 +146,46 @@ def set_group_isolated(on: bool) -> None:
     reference) or keeps each single (off: the library's batches of graphs, which must not couple
     their graphs)."""
     port_lib().svxo_set_group_isolated(int(bool(on)))
+
+
+def structure_loads(weight, ext=None) -> np.ndarray:
+    """World::Impl::load_vector (core/src/world/world.cpp:966-974), restated in C."""
+    w = np.ascontiguousarray(weight, dtype=np.float64)
+    e = None if ext is None else np.ascontiguousarray(ext, dtype=np.float64)
+    f = np.zeros(6 * len(w))
+    port_lib().svxo_structure_loads(len(w), ptr(w), ptr(e), ptr(f))
+    return f
+
+
+def pin_reference(nodes, com) -> int:
+    """pin_reference (core/src/world/world_pieces.cpp:313-326), restated in C; nodes in place."""
+    assert nodes.dtype == NODE_DTYPE and nodes.flags["C_CONTIGUOUS"]
+    return int(port_lib().svxo_pin_reference(ptr(nodes), len(nodes), V3(*[float(v) for v in com])))
+
+
+def _body_args(state, nodes, forces, node_com, node_mass, node_inertia):
+    nodes = np.ascontiguousarray(nodes, dtype=NODE_DTYPE)
+    forces = np.ascontiguousarray(forces, dtype=POINT_FORCE_DTYPE)
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (node_com, node_mass, node_inertia)]
+    return nodes, forces, arrs
+
+
+def body_loads(state, nodes, forces, node_com, node_mass, node_inertia, inertia=True, reference=False):
+    """A loose piece's loads (core/src/world/world_pieces.cpp:566-603): the C restatement, or with
+    reference=True the reference's own vector operators and StressProblem::add_force (None where
+    the reference tree is absent)."""
+    nodes, forces, arrs = _body_args(state, nodes, forces, node_com, node_mass, node_inertia)
+    f = np.zeros(6 * len(nodes))
+    args = (ctypes.byref(state), ptr(nodes), len(nodes), ptr(arrs[0]), ptr(arrs[1]), ptr(arrs[2]), ptr(forces),
+            len(forces), int(bool(inertia)), ptr(f))
+    if reference:
+        lib = reference_lib()
+        if lib is None:
+            return None
+        lib.svxr_body_loads(*args)
+    else:
+        port_lib().svxo_body_loads(*args)
+    return f
 
 
 def set_threads(n: int) -> None:

@@ -558,4 +558,59 @@ void svxr_p_matrix(void* h, int32_t* nfree, int64_t* nnzb, int32_t* rowptr, int3
   if (val) std::memcpy(val, P.K_.val.data(), sizeof(double) * P.K_.val.size());
 }
 
+// A loose piece's loads with the reference's own vector types, operators and
+// StressProblem::add_force, in the lines of World::Impl::body_stress_run
+// (core/src/world/world_pieces.cpp:566-603); the node of each force is given (the world maps a
+// fragment through BodyGraph::frag_node).
+void svxr_body_loads(const svxg_body_state* bs, const svxg_node* nodes, int32_t n, const svxg_v3* node_com,
+                     const double* node_mass, const double* node_inertia, const svxg_point_force* forces,
+                     int32_t nforces, int32_t inertia, double* out) {
+  Body b;
+  b.x = v3(bs->x);
+  b.q = Quat{bs->q[0], bs->q[1], bs->q[2], bs->q[3]};
+  b.com = v3(bs->com);
+  b.w = v3(bs->w);
+  for (int k = 0; k < 9; ++k) {
+    b.inertia.m[size_t(k)] = bs->inertia[k];
+    b.inv_inertia.m[size_t(k)] = bs->inv_inertia[k];
+  }
+  b.inv_mass = bs->inv_mass;
+  const M3 R = to_matrix(b.q), Rt = transpose(R);
+  std::vector<f64> f(6 * size_t(n), 0.0);
+  const V3 g{0, 0, -bs->gravity};
+  if (inertia) {
+    V3 Ft, tau;
+    for (int32_t k = 0; k < nforces; ++k) {
+      Ft += v3(forces[k].F);
+      tau += cross(v3(forces[k].p) - b.x, v3(forces[k].F));
+    }
+    const M3 Iw = R * b.inertia * Rt;
+    const M3 Iwi = R * b.inv_inertia * Rt;
+    const V3 a = Ft * b.inv_mass + g;
+    const V3 alpha = Iwi * (tau - cross(b.w, Iw * b.w));
+    for (int32_t i = 0; i < n; ++i) {
+      M3 In;
+      for (int k = 0; k < 9; ++k) In.m[size_t(k)] = node_inertia[9 * size_t(i) + size_t(k)];
+      const V3 rw = R * (v3(node_com[i]) - b.com);
+      const V3 ai = a + cross(alpha, rw) + cross(b.w, cross(b.w, rw));
+      const V3 Fi = Rt * ((g - ai) * node_mass[i]);
+      const M3 Ii = R * In * Rt;
+      const V3 Mi = Rt * ((Ii * alpha + cross(b.w, Ii * b.w)) * -1.0);
+      f64* fi = &f[6 * size_t(i)];
+      fi[0] += Fi.x;
+      fi[1] += Fi.y;
+      fi[2] += Fi.z;
+      fi[3] += Mi.x;
+      fi[4] += Mi.y;
+      fi[5] += Mi.z;
+    }
+  }
+  for (int32_t k = 0; k < nforces; ++k) {
+    const int32_t i = forces[k].node;
+    if (i < 0 || i >= n) continue;
+    StressProblem::add_force(f, i, v3(nodes[i].c), Rt * v3(forces[k].F), b.to_shape(v3(forces[k].p)));
+  }
+  std::memcpy(out, f.data(), sizeof(double) * f.size());
+}
+
 }  // extern "C"

@@ -1958,3 +1958,114 @@ double svxo_seq_sum(const double* a, int64_t n) {
   for (int64_t k = 0; k < n; ++k) s += a[k];
   return s;
 }
+
+/* ---- loads (the checker of the library's load builders) --------------------------------------- */
+
+static v3 v3_add(v3 a, v3 b) { v3 r = {a.x + b.x, a.y + b.y, a.z + b.z}; return r; }
+/* M3 * V3 and M3 * M3, row-major (core/include/svx/base/vec.hpp:63-72) */
+static v3 m3_v(const double* A, v3 v) {
+  v3 r = {A[0] * v.x + A[1] * v.y + A[2] * v.z, A[3] * v.x + A[4] * v.y + A[5] * v.z,
+          A[6] * v.x + A[7] * v.y + A[8] * v.z};
+  return r;
+}
+static void m3_m(const double* A, const double* B, double* R) {
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) R[3 * r + c] = A[3 * r] * B[c] + A[3 * r + 1] * B[3 + c] + A[3 * r + 2] * B[6 + c];
+}
+/* R * A * R^T, left to right as the reference writes it: (R * A) * Rt */
+static void m3_conj(const double* R, const double* A, const double* Rt, double* out) {
+  double T[9];
+  m3_m(R, A, T);
+  m3_m(T, Rt, out);
+}
+
+void svxo_structure_loads(int32_t n, const double* weight, const double* ext, double* f) {
+  /* World::Impl::load_vector, core/src/world/world.cpp:966-974 */
+  for (int64_t i = 0; i < n; ++i) {
+    for (int q = 0; q < 6; ++q) f[6 * i + q] = 0.0;
+    f[6 * i + 2] = -weight[i];
+    for (int q = 0; q < 6; ++q) f[6 * i + q] += ext ? ext[6 * i + q] : 0.0;
+  }
+}
+
+int32_t svxo_pin_reference(svxg_node* nodes, int32_t n, svxg_v3 com) {
+  /* pin_reference, core/src/world/world_pieces.cpp:313-326 */
+  int32_t pin = 0;
+  double best = 1e300;
+  for (int32_t i = 0; i < n; ++i) {
+    nodes[i].fixed = 0;
+    v3 d = v3_sub(v3_of(nodes[i].c), v3_of(com));
+    double d2 = v3_dot(d, d);
+    if (d2 < best) {
+      best = d2;
+      pin = i;
+    }
+  }
+  if (n > 0) nodes[pin].fixed = 1;
+  return n > 0 ? pin : -1;
+}
+
+void svxo_body_loads(const svxg_body_state* b, const svxg_node* nodes, int32_t n, const svxg_v3* node_com,
+                     const double* node_mass, const double* node_inertia, const svxg_point_force* forces,
+                     int32_t nforces, int32_t inertia, double* f) {
+  /* World::Impl::body_stress_run's loads, core/src/world/world_pieces.cpp:566-603 */
+  const double* q = b->q;
+  /* to_matrix (vec.hpp:111-120) */
+  const double xx = q[0] * q[0], yy = q[1] * q[1], zz = q[2] * q[2];
+  const double xy = q[0] * q[1], xz = q[0] * q[2], yz = q[1] * q[2];
+  const double wx = q[3] * q[0], wy = q[3] * q[1], wz = q[3] * q[2];
+  const double R[9] = {1 - 2 * (yy + zz), 2 * (xy - wz), 2 * (xz + wy), 2 * (xy + wz), 1 - 2 * (xx + zz),
+                       2 * (yz - wx), 2 * (xz - wy), 2 * (yz + wx), 1 - 2 * (xx + yy)};
+  double Rt[9];
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) Rt[3 * r + c] = R[3 * c + r];
+  for (int64_t k = 0; k < 6 * (int64_t)n; ++k) f[k] = 0.0;
+  const v3 g = {0, 0, -b->gravity};
+  const v3 x = v3_of(b->x), bc = v3_of(b->com), w = v3_of(b->w);
+  if (inertia) {
+    v3 Ft = {0, 0, 0}, tau = {0, 0, 0};
+    for (int32_t k = 0; k < nforces; ++k) {
+      Ft = v3_add(Ft, v3_of(forces[k].F));
+      tau = v3_add(tau, v3_cross(v3_sub(v3_of(forces[k].p), x), v3_of(forces[k].F)));
+    }
+    double Iw[9], Iwi[9];
+    m3_conj(R, b->inertia, Rt, Iw);
+    m3_conj(R, b->inv_inertia, Rt, Iwi);
+    const v3 a = v3_add(v3_scale(Ft, b->inv_mass), g);
+    const v3 alpha = m3_v(Iwi, v3_sub(tau, v3_cross(w, m3_v(Iw, w))));
+    for (int32_t i = 0; i < n; ++i) {
+      const v3 rw = m3_v(R, v3_sub(v3_of(node_com[i]), bc));
+      const v3 ai = v3_add(v3_add(a, v3_cross(alpha, rw)), v3_cross(w, v3_cross(w, rw)));
+      const v3 Fi = m3_v(Rt, v3_scale(v3_sub(g, ai), node_mass[i]));
+      double Ii[9];
+      m3_conj(R, node_inertia + 9 * (int64_t)i, Rt, Ii);
+      const v3 Mi = m3_v(Rt, v3_scale(v3_add(m3_v(Ii, alpha), v3_cross(w, m3_v(Ii, w))), -1.0));
+      double* fi = f + 6 * (int64_t)i;
+      fi[0] += Fi.x;
+      fi[1] += Fi.y;
+      fi[2] += Fi.z;
+      fi[3] += Mi.x;
+      fi[4] += Mi.y;
+      fi[5] += Mi.z;
+    }
+  }
+  for (int32_t k = 0; k < nforces; ++k) {
+    const int32_t i = forces[k].node;
+    if (i < 0 || i >= n) continue;
+    /* Body::to_shape (phys/rigid.hpp:206) with rotate_inv = rotate by conj(q) (vec.hpp:105-110) */
+    const v3 u = {-q[0], -q[1], -q[2]};
+    const v3 d = v3_sub(v3_of(forces[k].p), x);
+    const v3 t = v3_scale(v3_cross(u, d), 2.0);
+    const v3 at = v3_add(bc, v3_add(v3_add(d, v3_scale(t, q[3])), v3_cross(u, t)));
+    /* StressProblem::add_force (core/src/stress/stress.cpp:504-513) */
+    const v3 F = m3_v(Rt, v3_of(forces[k].F));
+    double* fi = f + 6 * (int64_t)i;
+    fi[0] += F.x;
+    fi[1] += F.y;
+    fi[2] += F.z;
+    const v3 M = v3_cross(v3_sub(at, v3_of(nodes[i].c)), F);
+    fi[3] += M.x;
+    fi[4] += M.y;
+    fi[5] += M.z;
+  }
+}

@@ -106,6 +106,14 @@ void svxo_apply_k(const svxo_problem* P, const double* x, double* y);
  * `s += a[k]`): a helper for checking the device's exact summation. */
 double svxo_seq_sum(const double* a, int64_t n);
 
+/* Loads: World::Impl::load_vector (world.cpp:966-974), pin_reference (world_pieces.cpp:313-326),
+ * body_stress_run's inertial relief and point forces (world_pieces.cpp:566-603). */
+void svxo_structure_loads(int32_t n, const double* weight, const double* ext, double* f);
+int32_t svxo_pin_reference(svxg_node* nodes, int32_t n, svxg_v3 com);
+void svxo_body_loads(const svxg_body_state* b, const svxg_node* nodes, int32_t n, const svxg_v3* node_com,
+                     const double* node_mass, const double* node_inertia, const svxg_point_force* forces,
+                     int32_t nforces, int32_t inertia, double* f);
+
 #ifdef __cplusplus
 }
 #endif
