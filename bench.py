@@ -75,6 +75,41 @@ def workload(args, rank: int):
     return nodes, bonds, f, mats, desc
 
 
+# setup phases by the library's boundary labels (svxg_phase_times)
+SETUP_GROUPS = {
+    "assemble: DOF numbering": "K", "assemble: incidences": "K", "assemble: pattern": "K",
+    "assemble: block values": "K", "K assembled": "K",
+    "level 0 finalized": "level finalize (D^-1, FP32 copies)", "level coarsened": "level finalize (D^-1, FP32 copies)",
+    "coarsen: aggregated": "aggregation", "coarsen: positions": "coarse positions",
+    "coarsen: lmax": "lambda_max (power iteration)", "coarsen: prolongation": "prolongation",
+    "coarsen: restriction lists": "restriction lists", "coarsen: A P": "Galerkin A P",
+    "coarsen: coarse pattern": "Galerkin pattern", "coarsen: coarse values": "Galerkin P^T (A P)",
+    "coarsest factored": "coarsest factor", "preconditioner built": "other",
+}
+
+
+def setup_phases(L, h, check) -> dict:
+    """Milliseconds per setup phase of the last assemble (summed over levels), and per level."""
+    from opus_destruct_2_gb300.graph import PhaseTime
+    cnt = ctypes.c_int32()
+    out = (PhaseTime * 512)()
+    check(L.svxg_phase_times(h, out, 512, ctypes.byref(cnt)))
+    groups: dict[str, float] = {}
+    levels: list[float] = []
+    cur = 0.0
+    for i in range(min(cnt.value, 512)):
+        label, ms = out[i].label.decode(), float(out[i].ms)
+        g = SETUP_GROUPS.get(label, "other")
+        groups[g] = groups.get(g, 0.0) + ms
+        if g != "K":
+            cur += ms
+        if label in ("level 0 finalized", "level coarsened"):
+            levels.append(cur)
+            cur = 0.0
+    return {"total": sum(groups.values()), "phases": groups, "per_level": levels,
+            "how": "CUDA events on the problem's stream at each phase boundary of one assemble (no host waits)"}
+
+
 class Clocks:
     """nvidia-smi samples (200 ms) during the timed region."""
 
@@ -739,6 +774,8 @@ def main():
     L.svxg_timer_read.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int64)]
     L.svxg_time_spmv.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]
     L.svxg_measure_fp64_rate.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    L.svxg_phase_timing.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+    L.svxg_phase_times.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
     L.svxg_utilization_device.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]
 
@@ -843,6 +880,11 @@ def main():
     loop_ms, fp64_tf = ctypes.c_double(), ctypes.c_double()
     check(L.svxg_time_spmv(h, prec_code, 50, ctypes.byref(loop_ms)))
     check(L.svxg_measure_fp64_rate(local_rank, ctypes.byref(fp64_tf)))
+    # the setup's phases: one more assemble with a CUDA event at each phase boundary
+    check(L.svxg_phase_timing(h, 1))
+    check(L.svxg_assemble(h, ctypes.byref(opt), ctypes.byref(ok)))
+    setup_ms = setup_phases(L, h, check)
+    check(L.svxg_phase_timing(h, 0))
     # --- timed: end to end through the C ABI with host buffers ---
     step_host()
     barrier()
@@ -919,6 +961,7 @@ def main():
         "p50_ms": 1e3 * float(np.percentile(lat, 50)),
         "p99_ms": 1e3 * float(np.percentile(lat, 99)),
         "phase_ms": {k: 1e3 * float(np.mean(v)) for k, v in phases.items() if v},
+        "setup_ms": setup_ms,
     }
     if clk is not None:
         line["clocks"] = clk

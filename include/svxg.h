@@ -314,6 +314,19 @@ typedef struct svxg_tune_entry {
 } svxg_tune_entry;
 int svxg_debug_tune_log(svxg_problem* p, svxg_tune_entry* out, int32_t cap, int32_t* count);
 
+/* Per-phase device times of the calls made while on (an event recorded on the problem's stream at
+ * each phase boundary of assemble - K, then per level aggregation, positions, lambda_max,
+ * prolongation, restriction lists, A P, coarse pattern, coarse values, the level's end - the
+ * coarsest factor, and of a host solve; no host wait). svxg_phase_times waits for the stream and
+ * gives, from the last assemble (or reassemble) on, each phase's label and milliseconds since the
+ * previous boundary; *count = the phases recorded (out holds at most cap). */
+typedef struct svxg_phase_time {
+  char label[48];
+  double ms;
+} svxg_phase_time;
+int svxg_phase_timing(svxg_problem* p, int32_t on);
+int svxg_phase_times(svxg_problem* p, svxg_phase_time* out, int32_t cap, int32_t* count);
+
 /* The host-side trace of the last assemble and host solve when the environment sets SVXG_TRACE=1
  * before the library loads (the stream is drained at each mark, so device time lands on the
  * phase that queued it): lines of "microseconds since the assemble began, since the previous

@@ -282,6 +282,31 @@ int svxg_timer_enable(svxg_problem* p, int32_t on) {
   return SVXG_OK;
 }
 
+int svxg_phase_timing(svxg_problem* p, int32_t on) {
+  CHECK_P(p);
+  p->P.phase_on = on != 0;
+  p->P.phase_used = 0;
+  return SVXG_OK;
+}
+
+int svxg_phase_times(svxg_problem* p, svxg_phase_time* out, int32_t cap, int32_t* count) {
+  CHECK_P(p);
+  Problem& P = p->P;
+  DeviceScope ds(P.device);
+  SVXG_CUDA(host_wait(P.stream));
+  const int32_t n = P.phase_used > 1 ? int32_t(P.phase_used - 1) : 0;
+  if (count) *count = n;
+  for (int32_t i = 0; out && i < std::min(n, cap); ++i) {
+    float ms = 0.0f;
+    SVXG_CUDA(cudaEventElapsedTime(&ms, P.phase_events[size_t(i)], P.phase_events[size_t(i) + 1]));
+    out[i].ms = ms;
+    std::memset(out[i].label, 0, sizeof(out[i].label));
+    const char* l = P.phase_labels[size_t(i) + 1];
+    std::strncpy(out[i].label, l ? l : "", sizeof(out[i].label) - 1);
+  }
+  return SVXG_OK;
+}
+
 int svxg_timer_read(svxg_problem* p, double* ms_total, int64_t* launches) {
   CHECK_P(p);
   Problem& P = p->P;
@@ -367,6 +392,7 @@ void svxg_problem_destroy(svxg_problem* p) {
   p->P.mem.release_all();
   host_wait(p->P.stream);
   for (cudaEvent_t e : p->P.timer_events) cudaEventDestroy(e);
+  for (cudaEvent_t e : p->P.phase_events) cudaEventDestroy(e);
   if (!p->P.borrowed) {
     if (p->P.h_s) cudaFreeHost(p->P.h_s);
     if (p->P.h_ms) cudaFreeHost(p->P.h_ms);

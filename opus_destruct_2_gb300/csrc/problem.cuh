@@ -219,6 +219,12 @@ struct Problem {
   bool timer_on = false;
   std::vector<cudaEvent_t> timer_events;
   size_t timer_used = 0;          // event pairs recorded since the last read
+  // per-phase device timing (svxg_phase_timing): an event on the stream at each trace mark, no
+  // host wait; read back by svxg_phase_times
+  bool phase_on = false;
+  std::vector<cudaEvent_t> phase_events;
+  std::vector<const char*> phase_labels;
+  size_t phase_used = 0;
   // host-side trace of the last assemble and solve (SVXG_TRACE=1): label, microseconds since the
   // assemble began, with the stream drained at each mark so device time is attributed
   std::vector<std::pair<const char*, double>> trace;

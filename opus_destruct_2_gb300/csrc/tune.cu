@@ -44,6 +44,18 @@ double now_us() {
 }  // namespace
 
 void trace_mark(Problem& P, const char* label, bool restart) {
+  if (P.phase_on) {
+    if (restart) P.phase_used = 0;
+    if (P.phase_used == P.phase_events.size()) {
+      cudaEvent_t e = nullptr;
+      if (cudaEventCreate(&e) == cudaSuccess) {
+        P.phase_events.push_back(e);
+        P.phase_labels.push_back(nullptr);
+      }
+    }
+    if (P.phase_used < P.phase_events.size() && cudaEventRecord(P.phase_events[P.phase_used], P.stream) == cudaSuccess)
+      P.phase_labels[P.phase_used++] = label;
+  }
   if (!g_trace) return;
   cudaStreamSynchronize(P.stream);
   const double t = now_us();

@@ -273,3 +273,8 @@ class BodyState(ctypes.Structure):
 
 POINT_FORCE_DTYPE = np.dtype([("F", np.float64, 3), ("p", np.float64, 3), ("node", np.int32), ("pad", np.int32)],
                              align=True)
+
+
+class PhaseTime(ctypes.Structure):
+    """svxg_phase_time: a setup or solve phase's label and its milliseconds since the previous one."""
+    _fields_ = [("label", ctypes.c_char * 48), ("ms", ctypes.c_double)]

@@ -8,7 +8,8 @@ Two libraries:
   (core/src/solve/amg.cpp, core/src/stress/stress.cpp, core/src/material/material.cpp,
   core/src/base/parallel.cpp under the reference tree) with its own flags (Release,
   ``-ffp-contract=off -fno-fast-math -fno-exceptions -fno-rtti``, CMakeLists.txt:17, :53), plus
-  ``oracle/ref_shim.cpp``. Built only where the reference tree exists; nothing is copied.
+  ``oracle/ref_shim.cpp``. Built only where the reference tree exists (``SVX_REFERENCE_TREE``, or a
+  checkout named ``reference`` beside this repository); nothing is copied.
 """
 from __future__ import annotations
 
@@ -19,7 +20,9 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
-REFERENCE = os.environ.get("SVX_REFERENCE_TREE", "/root/reference")
+# The reference tree: SVX_REFERENCE_TREE, else a checkout named `reference` beside this repository
+# (absent on machines that only run the prebuilt checker: then only the C restatement is built).
+REFERENCE = os.environ.get("SVX_REFERENCE_TREE") or os.path.join(os.path.dirname(ROOT), "reference")
 REF_SOURCES = [
     "core/src/solve/amg.cpp",
     "core/src/stress/stress.cpp",
