@@ -548,12 +548,15 @@ void worker(svxg_server* S) {
       for (;;) {
         S->cv_work.wait(lk, [&] { return S->stop || (!S->queue.empty() && !S->hold); });
         if (S->queue.empty()) break;
-        q = std::move(S->queue.front());
+        // (taken into its own variable: a deferred request leaves q as it was - ticket 0 - so a
+        // stop that finds the queue empty afterwards runs nothing)
+        Request r = std::move(S->queue.front());
         S->queue.pop_front();
-        if (q.structure >= 0 && S->running_structures.count(q.structure)) {
-          S->deferred[q.structure].push_back(std::move(q));
+        if (r.structure >= 0 && S->running_structures.count(r.structure)) {
+          S->deferred[r.structure].push_back(std::move(r));
           continue;
         }
+        q = std::move(r);
         break;
       }
       if (q.ticket == 0) break;  // (stopped, nothing left)

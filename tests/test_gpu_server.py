@@ -204,3 +204,21 @@ def test_admission_evicts_bundles_whole():
         assert S.wait(S.submit_repeat(1, [], a[2]))[0].status == -4
         r = S.wait(S.submit_repeat(4, [], b[2]))[0]
         assert r.status == 0 and r.warm == 1
+
+
+def test_shutdown_after_deferred_repeats():
+    """Repeats of one structure queued behind its first request are deferred by the slots that
+    find it running; after every result is in, closing the server runs nothing more (a slot whose
+    last act was a deferral has no request left to run), lifecycle after lifecycle."""
+    nodes, bonds, f, _ = synth.piece_graph(300, free=False, seed=17)
+    for rep in range(6):
+        with Server(workers=8, budget=8 << 30) as S:
+            S.set_batching(1)
+            S.hold(True)
+            t = [S.submit(nodes, bonds, MATS, f, structure=1)]
+            t += [S.submit_repeat(1, [], f) for _ in range(12)]
+            S.hold(False)
+            out = [S.wait(x)[0] for x in t]
+            st = S.stats()
+        assert all(r.status == 0 for r in out)
+        assert st.completed == len(t) and st.failed == 0
