@@ -397,13 +397,55 @@ def run_serve(args, rank: int, world: int):
                 "d2h_bytes_per_step": int(_serve_bytes(stream, "d2h") * 1000 / requests),
                 "p50_ms": host["p50_ms"], "p99_ms": host["p99_ms"]},
         "gpu_launches": int(launches),
-        "roofline": None,
+        "roofline": serve_roofline(stream, L, local),
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
     if clk is not None:
         line["clocks"] = clk
     print(json.dumps(line), flush=True)
+
+
+def serve_roofline(stream, L, device: int) -> dict:
+    """The serving step's dominant kernel by device time - the multigrid build's Galerkin A P values
+    kernel (FP64 6x6 block products in the reference's summation order, no contraction) - timed
+    with CUDA events on its problem's stream over five assembles of a typical batch of the stream
+    (its first 32 new structures as one problem, as the server batches them), against this GPU's
+    FP64 rate measured in the same run."""
+    from opus_destruct_2_gb300 import Batch
+    from opus_destruct_2_gb300.graph import StressOptions
+    L.svxg_timer_enable_kernel.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]
+    L.svxg_timer_read_work.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                       ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
+    L.svxg_measure_fp64_rate.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    news = [stream.geoms[p[2]] for p in stream.plan if p[0] == "new"][:32]
+    B = Batch([(g[0], g[1]) for g in news], stream.mats, device=device)
+    opt = StressOptions(precision=1)
+    B.assemble(opt)
+    L.svxg_timer_enable_kernel(B._h, 1, 1)
+    for _ in range(5):
+        B.assemble(opt)
+    ms, launches, work = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+    L.svxg_timer_read_work(B._h, ctypes.byref(ms), ctypes.byref(launches), ctypes.byref(work))
+    L.svxg_timer_enable_kernel(B._h, 1, 0)
+    rate = ctypes.c_double()
+    L.svxg_measure_fp64_rate(device, ctypes.byref(rate))
+    flops = 432.0 * work.value  # (36 entries x (6 mul + 5 add + 1 accumulate) per block product)
+    achieved = flops / (ms.value / 1e3) / 1e12 if ms.value > 0 else 0.0
+    return {"kernel": "Galerkin A P values (k_ap_values_acc): FP64 6x6 block products in the reference's "
+                      "summation order, no contraction", "bound": "fp64",
+            "achieved": achieved, "peak": rate.value, "unit": "TFLOP/s",
+            "frac": achieved / rate.value if rate.value > 0 else None,
+            "issue_frac": 2.0 * achieved / rate.value if rate.value > 0 else None,
+            "peak_source": "this GPU's FP64 FMA rate measured in this run (an FMA = 2 flops); issue_frac: "
+                           "against the FP64 instruction rate (half of it), the ceiling of code without "
+                           "contraction",
+            "traffic": None, "flops_per_launch": flops / max(launches.value, 1), "launches": int(launches.value),
+            "avg_us": 1e3 * ms.value / max(launches.value, 1),
+            "workload": f"one batch of the stream's first 32 new structures ({sum(len(g[0]) for g in news)} "
+                        f"fragments), 5 assembles, every level's launch",
+            "how": "CUDA events around each launch on the problem's stream; algorithmic FP64 operations from the "
+                   "block products counted on the host (the reference's build-work count of A P / 6)"}
 
 
 def run_reference_serve(args, world: int):

@@ -278,6 +278,13 @@ int64_t svxg_launch_count(void);
  * its launches while enabled; read returns their summed duration (ms) and count, and resets. */
 int svxg_timer_enable(svxg_problem* p, int32_t on);
 int svxg_timer_read(svxg_problem* p, double* ms_total, int64_t* launches);
+/* The same for a chosen kernel: SVXG_TIMER_CG_SPMV (as svxg_timer_enable) or
+ * SVXG_TIMER_GALERKIN_AP (the multigrid build's A P values kernel, every level of each assemble);
+ * read_work also gives the timed launches' algorithmic units (Galerkin: 6x6 by 6x6 block products,
+ * 432 FP64 operations each) and resets. */
+enum { SVXG_TIMER_CG_SPMV = 0, SVXG_TIMER_GALERKIN_AP = 1 };
+int svxg_timer_enable_kernel(svxg_problem* p, int32_t kind, int32_t on);
+int svxg_timer_read_work(svxg_problem* p, double* ms_total, int64_t* launches, int64_t* work);
 /* The conjugate-gradient SpMV timed alone: `reps` back-to-back launches of the kernel an iteration
  * runs on the assembled K (q = K p with p.q fused; precision SVXG_PRECISION_FP64: the FP64 K,
  * otherwise the mixed sequence's FP32 K), each doing its work, CUDA events on the problem's

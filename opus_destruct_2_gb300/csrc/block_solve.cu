@@ -284,7 +284,7 @@ void cheb_coeffs(double lmax, double ratio, int degree, BLevel* L) {
 
 bool block_solve_fits(const Problem& P) {
   return !P.jacobi_only && !P.lv.empty() && P.pc_n == P.nfree && P.nfree > 0 && P.nfree <= kBlockSolveMax &&
-         int(P.lv.size()) <= kMaxLevels && !P.timer_on && P.seg_n == 0;
+         int(P.lv.size()) <= kMaxLevels && !P.spmv_timer() && P.seg_n == 0;
 }
 
 // the descriptor (and the FP32 coarsest inverse) of an assembled problem, made once

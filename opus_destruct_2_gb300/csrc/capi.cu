@@ -279,6 +279,30 @@ int64_t svxg_launch_count(void) { return g_launches.load(std::memory_order_relax
 int svxg_timer_enable(svxg_problem* p, int32_t on) {
   CHECK_P(p);
   p->P.timer_on = on != 0;
+  p->P.timer_kind = SVXG_TIMER_CG_SPMV;
+  return SVXG_OK;
+}
+
+int svxg_timer_enable_kernel(svxg_problem* p, int32_t kind, int32_t on) {
+  CHECK_P(p);
+  if (kind != SVXG_TIMER_CG_SPMV && kind != SVXG_TIMER_GALERKIN_AP) {
+    set_error("svxg_timer_enable_kernel: unknown kernel");
+    return SVXG_ERR_ARG;
+  }
+  p->P.timer_on = on != 0;
+  p->P.timer_kind = kind;
+  p->P.timer_used = 0;
+  p->P.timer_work = 0;
+  return SVXG_OK;
+}
+
+int svxg_timer_read_work(svxg_problem* p, double* ms_total, int64_t* launches, int64_t* work) {
+  CHECK_P(p);
+  const int64_t w = p->P.timer_work;
+  const int e = svxg_timer_read(p, ms_total, launches);
+  if (e) return e;
+  if (work) *work = w;
+  p->P.timer_work = 0;
   return SVXG_OK;
 }
 

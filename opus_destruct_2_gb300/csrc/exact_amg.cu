@@ -1041,69 +1041,71 @@ __global__ void __launch_bounds__(32 * kAccWarps) k_c_values_acc(int32_t na, con
     for (int32_t q = lane; q < 36 * len; q += 32) cval[36 * int64_t(c0) + q] = acc[q];
 }
 
-// The same for levels with few coarse rows (too few warps to fill the GPU): a block per coarse
-// row, whose threads take (A P entry, group of nine of the 36 entries) items of one restriction
-// entry at a time, with a barrier between restriction entries - every entry of C still sees its
-// additions in the same order.
-constexpr int kRowT = 128;
-constexpr int32_t kFewRows = 2432;  // (16 warps on each of 152 SMs)
-__global__ void __launch_bounds__(kRowT) k_c_values_rows(int32_t na, const int32_t* rrow, const int32_t* rent_i,
-                                                         const int32_t* rent_e, const double* pval,
-                                                         const int32_t* aprow, const int32_t* apcol,
-                                                         const double* apval, const int32_t* crow,
-                                                         const int32_t* scratch, const int64_t* soff, int32_t* ccol,
-                                                         double* cval, double scale) {
-  __shared__ double acc_sh[kAccSlots * 36];
-  __shared__ int32_t col_sh[kAccSlots];
-  const int32_t I = blockIdx.x;
-  if (I >= na) return;
-  const int32_t c0 = crow[I], c1 = crow[I + 1], len = c1 - c0;
-  const bool local = len <= kAccSlots;
-  double* acc = local ? acc_sh : cval + 36 * int64_t(c0);
-  const int32_t* cols = local ? col_sh : ccol + c0;
-  for (int32_t c = threadIdx.x; c < len; c += kRowT) {
-    const int32_t v = scratch[soff[I] + c];
-    ccol[c0 + c] = v;
-    if (local) col_sh[c] = v;
+constexpr int32_t kFewRows = 2432;  // (coarse rows: 16 warps on each of 152 SMs)
+
+// C = P^T (A P) a warp per block of C: block k = (I, J) - I its coarse row, J its column - has
+// its 36 entries in the lanes' registers (entry lane, and 32 + lane for the first four lanes).
+// The warp walks row I's restriction entries (fine row i, block P_iI) in restriction order, finds
+// J in A P's row i (32 columns a step, by ballot; a row holds a column at most once) and adds
+// the entry's 6-term sum P_iI^T (A P)_iJ: every C entry receives one 6-term sum per restriction
+// entry whose A P row holds J, in restriction order - the sums of the row-at-a-time forms, with
+// no barrier, no shared accumulator and a warp for each block of C (coarse levels of a few
+// hundred rows still give thousands of warps).
+constexpr int kCWarps = 4;
+__global__ void __launch_bounds__(32 * kCWarps) k_c_values_warp(int32_t na, int64_t cnnz, const int32_t* rrow,
+                                                                const int32_t* rent_i, const int32_t* rent_e,
+                                                                const double* pval, const int32_t* aprow,
+                                                                const int32_t* apcol, const double* apval,
+                                                                const int32_t* crow, const int32_t* scratch,
+                                                                const int64_t* soff, int32_t* ccol, double* cval,
+                                                                double scale) {
+  const int lane = threadIdx.x & 31;
+  const int64_t k = int64_t(blockIdx.x) * kCWarps + (threadIdx.x >> 5);
+  if (k >= cnnz) return;
+  // (the coarse row of block k: the last I with crow[I] <= k)
+  int32_t lo = 0, hi = na - 1;
+  while (lo < hi) {
+    const int32_t mid = (lo + hi + 1) >> 1;
+    if (crow[mid] <= k) lo = mid;
+    else hi = mid - 1;
   }
-  for (int32_t q = threadIdx.x; q < 36 * len; q += kRowT) acc[q] = 0.0;
-  __syncthreads();
+  const int32_t I = lo;
+  const int32_t J = scratch[soff[I] + (k - crow[I])];
+  if (lane == 0) ccol[k] = J;
+  const int ra = lane / 6, ca = lane - 6 * (lane / 6);
+  const bool two = lane < 4;
+  const int rb = (lane + 32) / 6, cb = (lane + 32) - 6 * ((lane + 32) / 6);
+  double a0 = 0.0, a1 = 0.0;
   for (int32_t r = rrow[I]; r < rrow[I + 1]; ++r) {
     const int32_t i = rent_i[r];
-    const double* Pi = pval + 36 * int64_t(rent_e[r]);
     const int32_t e0 = aprow[i], ne = aprow[i + 1] - e0;
-    for (int32_t item = threadIdx.x; item < 4 * ne; item += kRowT) {
-      const int32_t e = e0 + item / 4;
-      const int g = item % 4;
-      const int32_t J = apcol[e];
-      int32_t slot;
-      if (J == I) {
-        slot = 0;
-      } else {
-        int32_t lo = 1, hi = len - 1;
-        while (lo < hi) {
-          const int32_t mid = (lo + hi) >> 1;
-          if (cols[mid] < J) lo = mid + 1;
-          else hi = mid;
-        }
-        slot = lo;
-      }
-      const double* B = apval + 36 * int64_t(e);
-      double* C = acc + 36 * int64_t(slot);
-      for (int ent = 9 * g; ent < 9 * g + 9; ++ent) {
-        const int rr = ent / 6, cc = ent - 6 * (ent / 6);
-        double sacc = plus_zero(Pi[rr] * B[cc]);
-        for (int q = 1; q < 6; ++q) sacc += Pi[q * 6 + rr] * B[q * 6 + cc];
-        C[ent] = C[ent] + sacc;
+    int32_t found = -1;
+    for (int32_t b = 0; b < ne; b += 32) {
+      const bool hit = b + lane < ne && apcol[e0 + b + lane] == J;
+      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      if (m) {
+        found = e0 + b + __ffs(int(m)) - 1;
+        break;
       }
     }
-    __syncthreads();
+    if (found < 0) continue;
+    const double* Pi = pval + 36 * int64_t(rent_e[r]);
+    const double* B = apval + 36 * int64_t(found);
+    double s0 = plus_zero(Pi[ra] * B[ca]);
+    for (int q = 1; q < 6; ++q) s0 += Pi[q * 6 + ra] * B[q * 6 + ca];
+    a0 = a0 + s0;
+    if (two) {
+      double s1 = plus_zero(Pi[rb] * B[cb]);
+      for (int q = 1; q < 6; ++q) s1 += Pi[q * 6 + rb] * B[q * 6 + cb];
+      a1 = a1 + s1;
+    }
   }
-  if (scale != 1.0)
-    for (int32_t q = threadIdx.x; q < 36 * len; q += kRowT) acc[q] *= scale;
-  __syncthreads();
-  if (local)
-    for (int32_t q = threadIdx.x; q < 36 * len; q += kRowT) cval[36 * int64_t(c0) + q] = acc[q];
+  if (scale != 1.0) {
+    a0 *= scale;
+    a1 *= scale;
+  }
+  cval[36 * k + lane] = a0;
+  if (two) cval[36 * k + 32 + lane] = a1;
 }
 
 // build work of P^T (A P): 6 |P row i| |AP row i|
@@ -1539,6 +1541,7 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
                                               scratch.p, F.pcol, F.pval), SVXG_COUNT_LAUNCH());
   }
   if (smoothed) P.amg_build_work += 12 * nnzb;
+  int64_t ap_products = 0;  // (the block products of A P: |P row col(k)| for every block k of A)
   {
     Tmp<unsigned long long> acc(st);
     TRY(acc.alloc(1));
@@ -1547,6 +1550,7 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     unsigned long long w = 0;
     TRY(copy_to_host(P, &w, acc.p, sizeof(w)));
     P.amg_build_work += int64_t(w);
+    ap_products = int64_t(w / 6);
   }
   trace_mark(P, "coarsen: prolongation");
   // restriction lists
@@ -1597,9 +1601,15 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     apnnz_total = apnnz;
     TRY(apcol.alloc(size_t(apnnz)));
     TRY(apval.alloc(size_t(apnnz) * 36));
+    const bool timed = P.timer_on && P.timer_kind == SVXG_TIMER_GALERKIN_AP;
+    if (timed) TRY(timer_mark(P));
     (k_ap_values_acc<<<unsigned((n + kAccWarps - 1) / kAccWarps), 32 * kAccWarps, 0, st>>>(
          n, F.A.rowptr, F.A.col, F.A.val, F.prow, F.pcol, F.pval, aprow.p, scratch.p, soff.p, apcol.p, apval.p),
      SVXG_COUNT_LAUNCH());
+    if (timed) {
+      TRY(timer_mark(P, true));
+      P.timer_work += ap_products;  // (6x6 by 6x6 block products: 432 FP64 operations each, no contraction)
+    }
   }
   {
     Tmp<unsigned long long> acc(st);
@@ -1639,22 +1649,25 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     TRY(P.mem.alloc(&C.A.col, size_t(cnnz)));
     TRY(P.mem.alloc(&C.A.val, size_t(cnnz) * 36));
     const double scale = (!smoothed && opt.coarse_scale != 1.0) ? opt.coarse_scale : 1.0;
-    // (A P rows of 6 entries or more on average: the lanes over each row's entries)
-    if (na < kFewRows)
-      (k_c_values_rows<<<unsigned(na), kRowT, 0, st>>>(na, F.rrow, F.rent_i, F.rent_e, F.pval, aprow.p, apcol.p,
-                                                        apval.p, C.A.rowptr, scratch.p, soff.p, C.A.col, C.A.val,
-                                                        scale),
-       SVXG_COUNT_LAUNCH());
-    else if (apnnz_total >= 6 * int64_t(n))
+    // (levels of few coarse rows: a warp per block of C; wider levels: a warp per coarse row, whose
+    // restriction entries are walked once rather than once per block of the row)
+    if (na < kFewRows) {
+      if (cnnz > 0)
+        (k_c_values_warp<<<unsigned((int64_t(cnnz) + kCWarps - 1) / kCWarps), 32 * kCWarps, 0, st>>>(
+             na, int64_t(cnnz), F.rrow, F.rent_i, F.rent_e, F.pval, aprow.p, apcol.p, apval.p, C.A.rowptr, scratch.p,
+             soff.p, C.A.col, C.A.val, scale),
+         SVXG_COUNT_LAUNCH());
+    } else if (apnnz_total >= 6 * int64_t(n)) {
       (k_c_values_acc<<<unsigned((na + kAccWarps - 1) / kAccWarps), 32 * kAccWarps, 0, st>>>(
            na, F.rrow, F.rent_i, F.rent_e, F.pval, aprow.p, apcol.p, apval.p, C.A.rowptr, scratch.p, soff.p, C.A.col,
            C.A.val, scale),
        SVXG_COUNT_LAUNCH());
-    else
+    } else {
       (k_c_values<<<nblk(32 * int64_t(na), 128), 128, 0, st>>>(na, F.rrow, F.rent_i, F.rent_e, F.pval, aprow.p, apcol.p,
                                                                 apval.p, C.A.rowptr, scratch.p, soff.p, C.A.col, C.A.val,
                                                                 scale),
        SVXG_COUNT_LAUNCH());
+    }
   }
   SVXG_CUDA(cudaGetLastError());
   trace_mark(P, "coarsen: coarse values");

@@ -332,7 +332,7 @@ int mixed_body(Problem& P) {
   float* p32 = d + 3 * m;
   float* q32 = d + 4 * m;
   MixedScalars* s = static_cast<MixedScalars*>(P.d_ms);
-  if (P.timer_on) TRY(timer_mark(P));
+  if (P.spmv_timer()) TRY(timer_mark(P));
   if (P.sched_k32 == kGroupRow)
     (k_spmv32_dot<kGroupRow><<<spmv_dot_blocks<kGroupRow>(nf), kT, 0, st>>>(nf, P.K.rowptr, P.K.col, P.K.val32, p32,
                                                                           q32, P.d_partials, P.d_counter, s),
@@ -341,7 +341,7 @@ int mixed_body(Problem& P) {
     (k_spmv32_dot<kWarpRow><<<spmv_dot_blocks<kWarpRow>(nf), kT, 0, st>>>(nf, P.K.rowptr, P.K.col, P.K.val32, p32,
                                                                         q32, P.d_partials, P.d_counter, s),
      SVXG_COUNT_LAUNCH());
-  if (P.timer_on) TRY(timer_mark(P, true));
+  if (P.spmv_timer()) TRY(timer_mark(P, true));
   (k_axpy32<<<vblk(nf), kT, 0, st>>>(nf, d, r32, p32, q32, P.d_partials, P.d_counter, s), SVXG_COUNT_LAUNCH());
   TRY(vcycle32(P, r32, z32));
   (k_rz32<1><<<vblk(nf), kT, 0, st>>>(nf, r32, z32, nullptr, P.d_partials, P.d_counter, s), SVXG_COUNT_LAUNCH());
@@ -510,7 +510,7 @@ int mixed_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
         batch = std::min(batch * 2, 32);
       }
       // (the live timer keeps the SpMV launches that did work: the first `iters` of the sequence)
-      if (P.timer_on) P.timer_used = std::min(P.timer_used, timed0 + size_t(std::max(hs->iters, 0)));
+      if (P.spmv_timer()) P.timer_used = std::min(P.timer_used, timed0 + size_t(std::max(hs->iters, 0)));
     }
     used += hs->iters;
     (k_outer_update<<<vblk(nf), kT, 0, st>>>(nf, P.d_x, d), SVXG_COUNT_LAUNCH());

@@ -217,8 +217,11 @@ struct Problem {
   void* loop_mixed = nullptr;
   // live kernel timing (CUDA events around each conjugate-gradient SpMV launch)
   bool timer_on = false;
+  int32_t timer_kind = 0;         // SVXG_TIMER_*: the kernel timed
   std::vector<cudaEvent_t> timer_events;
   size_t timer_used = 0;          // event pairs recorded since the last read
+  int64_t timer_work = 0;         // algorithmic units of the timed launches (SVXG_TIMER_GALERKIN_AP: block products)
+  bool spmv_timer() const { return timer_on && timer_kind == SVXG_TIMER_CG_SPMV; }
   // per-phase device timing (svxg_phase_timing): an event on the stream at each trace mark, no
   // host wait; read back by svxg_phase_times
   bool phase_on = false;

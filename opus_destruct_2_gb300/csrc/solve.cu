@@ -1007,10 +1007,10 @@ int plain_body(Problem& P) {
   if (P.seg_n > 0) return seg_body(P);
   const int32_t nf = P.nfree;
   cudaStream_t st = P.stream;
-  if (P.timer_on) TRY(timer_mark(P));
+  if (P.spmv_timer()) TRY(timer_mark(P));
   launch_spmv<kDotP>(st, P.sched_k64, nf, P.K.rowptr, P.K.col, P.K.val, P.d_p, P.d_q, P.d_partials, P.d_counter,
                      P.d_s, P.d_kslots);
-  if (P.timer_on) TRY(timer_mark(P, true));
+  if (P.spmv_timer()) TRY(timer_mark(P, true));
   (k_axpy_rr<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_x, P.d_r, P.d_p, P.d_q, P.d_partials, P.d_counter, P.d_s),
    SVXG_COUNT_LAUNCH());
   if (P.jacobi_only) {
@@ -1039,7 +1039,7 @@ bool use_graphs() {
 // host-side cost that also serializes concurrent problems, so a small problem solved once is
 // better served by host-driven batches of launches (the live timer also needs those).
 bool loop_graph_worth(const Problem& P, const void* slot) {
-  if (!use_graphs() || P.timer_on) return false;
+  if (!use_graphs() || P.spmv_timer()) return false;
   return slot != nullptr || P.nfree >= kGraphMinFree || P.host_loops > 0;
 }
 
@@ -1085,7 +1085,7 @@ int plain_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
   SVXG_CUDA(host_wait(st));
   if (P.h_s->done || nf == 0) {
     // (converged, empty or not finite at the start: no iteration)
-  } else if (P.jacobi_only && nf <= kJacobiBlockMax && !P.timer_on && P.seg_n == 0) {
+  } else if (P.jacobi_only && nf <= kJacobiBlockMax && !P.spmv_timer() && P.seg_n == 0) {
     (k_jacobi_pcg_block<<<1, kJacobiBlockT, 0, st>>>(nf, P.K.rowptr, P.K.col, P.K.val, P.d_jinv, P.d_x, P.d_r, P.d_z,
                                                       P.d_p, P.d_q, P.d_s),
      SVXG_COUNT_LAUNCH());
@@ -1118,7 +1118,7 @@ int plain_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
     }
     // the live timer keeps the SpMV launches that did work: the first `iters` of this call (the
     // bodies queued past convergence return at once and are not SpMV launches)
-    if (P.timer_on) P.timer_used = std::min(P.timer_used, timed0 + size_t(std::max(P.h_s->iters, 0)));
+    if (P.spmv_timer()) P.timer_used = std::min(P.timer_used, timed0 + size_t(std::max(P.h_s->iters, 0)));
   }
   P.cycle_stop = nullptr;
   out.iters = P.h_s->iters;

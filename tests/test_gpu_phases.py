@@ -46,3 +46,26 @@ def test_setup_phases_recorded():
     assert L.svxg_phase_timing(h, 0) == 0
     assert G.assemble(StressOptions())
     assert phases(L, h) == []
+
+
+def test_galerkin_kernel_timer():
+    """svxg_timer_enable_kernel(SVXG_TIMER_GALERKIN_AP): one timed launch per coarsening with its
+    block products counted (the build-work count of A P / 6); the solve's SpMV is not timed
+    meanwhile and the results are unchanged."""
+    nodes, bonds, f, mats = synth.tower_graph(storeys=10, seed=1)
+    L = load_library()
+    L.svxg_timer_enable_kernel.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]
+    L.svxg_timer_read_work.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                       ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
+    G = StressProblem(nodes, bonds, mats)
+    assert G.assemble(StressOptions())
+    u0, _ = G.solve(f, rtol=1e-8, maxit=500)
+    assert L.svxg_timer_enable_kernel(G._h, 1, 1) == 0
+    assert G.assemble(StressOptions())
+    u1, _ = G.solve(f, rtol=1e-8, maxit=500)
+    ms, n, work = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+    assert L.svxg_timer_read_work(G._h, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(work)) == 0
+    assert n.value == G.info().levels - 1 and work.value > 0 and ms.value > 0.0
+    assert np.array_equal(u0, u1)
+    assert L.svxg_timer_enable_kernel(G._h, 7, 1) == -1
+    assert L.svxg_timer_enable_kernel(G._h, 1, 0) == 0
