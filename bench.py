@@ -408,10 +408,10 @@ def run_serve(args, rank: int, world: int):
 
 def serve_roofline(stream, L, device: int) -> dict:
     """The serving step's dominant kernel by device time - the multigrid build's Galerkin A P values
-    kernel (FP64 6x6 block products in the reference's summation order, no contraction) - timed
-    with CUDA events on its problem's stream over five assembles of a typical batch of the stream
-    (its first 32 new structures as one problem, as the server batches them), against this GPU's
-    FP64 rate measured in the same run."""
+    kernel (FP64 6x6 block products in the reference's summation order; the mixed-precision
+    policy's build contracts them into FMAs) - timed with CUDA events on its problem's stream over
+    five assembles of a typical batch of the stream (its first 32 new structures as one problem,
+    as the server batches them), against this GPU's FP64 rate measured in the same run."""
     from opus_destruct_2_gb300 import Batch
     from opus_destruct_2_gb300.graph import StressOptions
     L.svxg_timer_enable_kernel.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32]
@@ -430,16 +430,15 @@ def serve_roofline(stream, L, device: int) -> dict:
     L.svxg_timer_enable_kernel(B._h, 1, 0)
     rate = ctypes.c_double()
     L.svxg_measure_fp64_rate(device, ctypes.byref(rate))
-    flops = 432.0 * work.value  # (36 entries x (6 mul + 5 add + 1 accumulate) per block product)
+    flops = 432.0 * work.value  # (36 entries x 12 flops - 6 products, 5 sums, 1 accumulate - per block product)
     achieved = flops / (ms.value / 1e3) / 1e12 if ms.value > 0 else 0.0
-    return {"kernel": "Galerkin A P values (k_ap_values_acc): FP64 6x6 block products in the reference's "
-                      "summation order, no contraction", "bound": "fp64",
+    return {"kernel": "Galerkin A P values (k_ap_values_acc) of the mixed-precision policy's multigrid build: "
+                      "FP64 6x6 block products in the reference's summation order, as FMAs", "bound": "fp64",
             "achieved": achieved, "peak": rate.value, "unit": "TFLOP/s",
             "frac": achieved / rate.value if rate.value > 0 else None,
             "issue_frac": 2.0 * achieved / rate.value if rate.value > 0 else None,
             "peak_source": "this GPU's FP64 FMA rate measured in this run (an FMA = 2 flops); issue_frac: "
-                           "against the FP64 instruction rate (half of it), the ceiling of code without "
-                           "contraction",
+                           "against the FP64 instruction rate (half of it)",
             "traffic": None, "flops_per_launch": flops / max(launches.value, 1), "launches": int(launches.value),
             "avg_us": 1e3 * ms.value / max(launches.value, 1),
             "workload": f"one batch of the stream's first 32 new structures ({sum(len(g[0]) for g in news)} "

@@ -752,7 +752,7 @@ static int assemble_impl(Problem& P, const svxg_stress_options* opt, int32_t* ok
     P.assembly_work += 12 * int64_t(P.nfree);
   } else {
     int32_t built = 0;
-    TRY(build_hierarchy(P, &built));
+    TRY(build_multigrid(P, &built));
     if (!built) {
       P.assembled = false;
       return SVXG_OK;

@@ -3,6 +3,14 @@
 // core/src/solve/amg.cpp:228-578). Compiled with -fmad=false: every sum runs in the reference's
 // order with separate multiplies and adds, divisions and square roots IEEE-rounded.
 //
+// fast_amg.cu compiles this file a second time with SVXG_FAST_SETUP defined and without
+// -fmad=false (build_hierarchy_fast, the mixed-precision policy's setup): the same algorithm and
+// summation orders with multiplies and adds contracted into FMAs, and the power iteration's norm
+// as a fixed-order tree sum instead of the sequential sum - deterministic, within rounding of the
+// reference's values, at about half the FP64 instructions (this part issues FP64 at two lanes a
+// clock per SM, and the bit-exact products are bound by that). Its aggregates can differ from
+// the reference's where a strength test sits within rounding of its threshold.
+//
 // The reference's aggregation is sequential (amg.cpp:339-349: node i becomes a root when it is
 // not aggregated and none of its strong neighbours is, then claims them). Its roots are the
 // lexicographically first independent set of the conflict graph "N[r] and N[i] meet"
@@ -278,10 +286,21 @@ __global__ void __launch_bounds__(exact::kThreads) k_lmax_step_small(int32_t n, 
   __threadfence();
   // (every block has read v and written w: the last one may rescale v)
   const int64_t mm = 6 * int64_t(n);
+#ifdef SVXG_FAST_SETUP
+  (void)rec;
+  (void)cnt;
+  double part = 0.0;
+  for (int64_t k = threadIdx.x; k < mm; k += exact::kThreads) {
+    const double x = __ldcg(w + k);
+    part += x * x;
+  }
+  const double sum = exact::block_sum_approx(part);  // (a fixed tree: deterministic)
+#else
   const int32_t ns = exact::build_segments(0, mm, 0.0, SqTermCG{w}, rec);
   if (threadIdx.x == 0) cnt[0] = ns > exact::kTileSegs ? -1 : ns;
   __syncthreads();
   const double sum = exact::walk_segments(0.0, 0, 1, cnt, rec, mm, SqTermCG{w});
+#endif
   if (threadIdx.x == 0) {
     nv_sh = sqrt(sum);
     set_norm(state, nv_sh);
@@ -337,6 +356,50 @@ __global__ void k_norm_rescale(int64_t m, const double* w, double* v, const doub
   const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (k < m) v[k] = w[k] / nv;
 }
+
+#ifdef SVXG_FAST_SETUP
+// the norm as a fixed-order tree sum: each block's squares summed in a fixed tree, the last block
+// to finish adds the blocks' sums in block order and sets state (the grid is fixed by m)
+constexpr int kFastNormT = 256;
+constexpr int kFastNormBlocks = 1024;
+__global__ void __launch_bounds__(kFastNormT) k_norm_fast(int64_t m, const double* w, double* part,
+                                                          unsigned* counter, double* state) {
+  __shared__ double sh[kFastNormT];
+  __shared__ bool last;
+  if (state[2] != 0.0) return;
+  double s = 0.0;
+  for (int64_t k = int64_t(blockIdx.x) * kFastNormT + threadIdx.x; k < m; k += int64_t(gridDim.x) * kFastNormT) {
+    const double x = w[k];
+    s += x * x;
+  }
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int d = kFastNormT / 2; d > 0; d >>= 1) {
+    if (int(threadIdx.x) < d) sh[threadIdx.x] += sh[threadIdx.x + d];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = sh[0];
+    __threadfence();
+    last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double t = 0.0;
+  for (int b = int(threadIdx.x); b < int(gridDim.x); b += kFastNormT) t += __ldcg(part + b);
+  sh[threadIdx.x] = t;
+  __syncthreads();
+  for (int d = kFastNormT / 2; d > 0; d >>= 1) {
+    if (int(threadIdx.x) < d) sh[threadIdx.x] += sh[threadIdx.x + d];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    set_norm(state, sqrt(sh[0]));
+    *counter = 0u;
+  }
+}
+#endif
 
 // scratch of the exact norm of vectors of m terms
 struct NormScratch {
@@ -1370,6 +1433,16 @@ int estimate_lmax(Problem& P, const Level& L, double* out) {
                                                                ns.rec.p, ns.cnt.p, counter.p, st.p),
        SVXG_COUNT_LAUNCH());
   }
+#ifdef SVXG_FAST_SETUP
+  const unsigned fb = unsigned(std::min<int64_t>(kFastNormBlocks, (m + kFastNormT - 1) / kFastNormT));
+  Tmp<double> part(P.stream);
+  Tmp<unsigned> fcounter(P.stream);
+  if (m > exact::kTile) {
+    TRY(part.alloc(fb));
+    TRY(fcounter.alloc(1));
+    SVXG_CUDA(cudaMemsetAsync(fcounter.p, 0, sizeof(unsigned), P.stream));
+  }
+#endif
   for (int it = 0; m > exact::kTile && it < 15; ++it) {
     if (n <= kApplyRowsMax)
       (k_lmax_apply_rows<<<unsigned((n + kApplyWarps - 1) / kApplyWarps), 32 * kApplyWarps, 0, P.stream>>>(
@@ -1378,7 +1451,12 @@ int estimate_lmax(Problem& P, const Level& L, double* out) {
     else
       (k_lmax_apply<<<ab, 6 * kApplyNodes, 0, P.stream>>>(n, L.A.rowptr, L.A.col, L.A.val, L.dinv, v.p, w.p, st.p),
        SVXG_COUNT_LAUNCH());
+#ifdef SVXG_FAST_SETUP
+    (k_norm_fast<<<fb, kFastNormT, 0, P.stream>>>(m, w.p, part.p, fcounter.p, st.p), SVXG_COUNT_LAUNCH());
+    (k_norm_rescale<<<nblk(m), kT, 0, P.stream>>>(m, w.p, v.p, st.p), SVXG_COUNT_LAUNCH());
+#else
     TRY(launch_norm(P.stream, m, w.p, v.p, st.p, ns));
+#endif
   }
   SVXG_CUDA(cudaGetLastError());
   double h[3];
@@ -1719,12 +1797,13 @@ __global__ void k_level0_pos(int32_t n, const svxg_node* nodes, const int32_t* d
   pos[3 * int64_t(d) + 2] = nodes[i].c.z;
 }
 
-}  // namespace
-
 __global__ void k_state_norm_out(const double* state, double* out) {
   if (threadIdx.x == 0 && blockIdx.x == 0) *out = state[1];
 }
 
+}  // namespace
+
+#ifndef SVXG_FAST_SETUP
 // sqrt of the sequential sum of squares of n device doubles (the power iteration's norm), by the
 // path estimate_lmax takes for a vector of that length
 int debug_seq_norm(cudaStream_t st, const double* v, int64_t n, double* out_dev) {
@@ -1740,8 +1819,14 @@ int debug_seq_norm(cudaStream_t st, const double* v, int64_t n, double* out_dev)
   return SVXG_OK;
 }
 
+#endif
+
 // Amg::build (amg.cpp:277-318) over K
+#ifdef SVXG_FAST_SETUP
+int build_hierarchy_fast(Problem& P, int32_t* ok) {
+#else
 int build_hierarchy(Problem& P, int32_t* ok) {
+#endif
   *ok = 0;
   P.lv.clear();
   P.chol_n = 0;

@@ -188,7 +188,7 @@ int build_appended(Problem& P) {
   }
   if (len) S->mem.release(len);
   int32_t built = 0;
-  if (!e) e = build_hierarchy(*S, &built);
+  if (!e) e = build_multigrid(*S, &built);
   if (e || !built) {
     S->mem.release_all();
     delete S;

@@ -260,7 +260,13 @@ int build_jacobi(Problem& P);                    // block-Jacobi inverses
 int remove_bonds_device(Problem& P, const int32_t* bonds, int32_t count);  // sequential, in order
 int set_identity_rows(Problem& P, const int32_t* rows, int32_t count);
 // exact_amg.cu
-int build_hierarchy(Problem& P, int32_t* ok);    // Amg::build on the device
+int build_hierarchy(Problem& P, int32_t* ok);    // Amg::build on the device, bit for bit
+int build_hierarchy_fast(Problem& P, int32_t* ok);  // the same with FMAs and a tree-summed norm
+// the multigrid of the problem's arithmetic: bit for bit in FP64, the fast build under the
+// mixed-precision policy (whose cycle and inner sequences run in FP32 anyway)
+inline int build_multigrid(Problem& P, int32_t* ok) {
+  return P.opt.precision == SVXG_PRECISION_FP64 ? build_hierarchy(P, ok) : build_hierarchy_fast(P, ok);
+}
 int debug_seq_norm(cudaStream_t st, const double* v, int64_t n, double* out_dev);
 // dense.cu: C (m x m, the coarsest operator) -> chol (L, L^T mirrored above; may alias C) and
 // cinv (L^-1, then L^-T), all device, m x m row-major

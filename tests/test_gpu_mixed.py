@@ -147,3 +147,24 @@ def test_mixed_below_its_size_runs_the_fp64_sequence():
         out[prec] = G.solve(f, rtol=1e-8, maxit=500)
     assert out[0][1].iters == out[1][1].iters
     assert np.array_equal(out[0][0], out[1][0])
+
+
+@pytest.mark.parametrize("name", ["tower10", "piece_free", "cantilever40"])
+def test_mixed_policy_setup_within_rounding_of_the_exact_build(name):
+    """Under the mixed-precision policy the multigrid is built with FMAs and a tree-summed power
+    iteration norm (build_hierarchy_fast): the same number of levels with sizes within 2 % of the
+    bit-exact build's, the solve's iteration count within 2, and the displacement within 1e-6 of
+    the FP64 build's at rel. residual 1e-10."""
+    make, opts = CASES[name]
+    nodes, bonds = make()
+    f = fx.gravity_live(nodes)
+    A = StressProblem(nodes, bonds, MATS)
+    assert A.assemble(StressOptions(precision=0, **opts))
+    B = StressProblem(nodes, bonds, MATS)
+    assert B.assemble(StressOptions(precision=1, **opts))
+    sa, sb = A.info().sizes(), B.info().sizes()
+    assert len(sa) == len(sb) and all(abs(x - y) <= 0.02 * x for x, y in zip(sa, sb)), (sa, sb)
+    ua, ra = A.solve(f, rtol=1e-10, maxit=4000)
+    ub, rb = B.solve(f, rtol=1e-10, maxit=4000)
+    assert ra.converged and rb.converged and abs(ra.iters - rb.iters) <= 2, (ra.iters, rb.iters)
+    assert relerr(ub, ua) <= 1e-6
