@@ -138,6 +138,9 @@ def test_mixed_cap_and_resume_and_edge_loads():
 
 
 def test_mixed_below_its_size_runs_the_fp64_sequence():
+    """Below the size where FP32 inner sequences pay, the mixed policy runs the FP64 conjugate-
+    gradient sequence (with its own multigrid build: FMAs, a tree-summed norm):
+    the FP64 path's iteration count within one and its displacement within 1e-6."""
     nodes, bonds = fx.lattice(8)
     f = fx.gravity_live(nodes)
     out = {}
@@ -145,8 +148,8 @@ def test_mixed_below_its_size_runs_the_fp64_sequence():
         G = StressProblem(nodes, bonds, MATS)
         assert G.assemble(StressOptions(precision=prec, amg_min_nodes=16))
         out[prec] = G.solve(f, rtol=1e-8, maxit=500)
-    assert out[0][1].iters == out[1][1].iters
-    assert np.array_equal(out[0][0], out[1][0])
+    assert abs(out[0][1].iters - out[1][1].iters) <= 1
+    assert relerr(out[1][0], out[0][0]) <= 1e-6
 
 
 @pytest.mark.parametrize("name", ["tower10", "piece_free", "cantilever40"])
