@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(6 * kApplyNodes) k_lmax_apply(int32_t n, const
 // The same step for shorter levels with longer rows, a warp per node: the six-term products of
 // the row's blocks (entry, block items over the lanes, chunks of kApplyChunk blocks) first, then
 // lanes 0-5 add them in block order - the same sums as spmv_exact_entry - and D^-1 (A v).
-constexpr int kApplyChunk = 16;
+constexpr int kApplyChunk = 48;
 constexpr int kApplyWarps = 4;
 constexpr int32_t kApplyRowsMax = 16384;  // levels up to this many nodes take the warp-per-node form
 __global__ void __launch_bounds__(32 * kApplyWarps) k_lmax_apply_rows(int32_t n, const int32_t* rowptr,
@@ -239,7 +239,7 @@ struct SqTermCG {
 // apply D^-1 A v a node each (k_lmax_apply_rows' sums), and the last block to finish takes the
 // exact norm and the scaling (k_norm_small's) - one launch a step instead of two, for the small
 // problems whose setup is bound by launches.
-constexpr int kStepChunk = 8;
+constexpr int kStepChunk = 12;  // (blocks of a row a warp takes per round: fewer dependent round trips on long coarse rows)
 __global__ void __launch_bounds__(exact::kThreads) k_lmax_step_small(int32_t n, const int32_t* rowptr,
                                                                     const int32_t* col, const double* val,
                                                                     const double* dinv, double* v, double* w,
