@@ -33,6 +33,7 @@
 #include "exact_runs.cuh"
 #include "exact_sum.cuh"
 #include "problem.cuh"
+#include "spmv_row.cuh"
 
 namespace svxg {
 namespace {
@@ -135,6 +136,10 @@ __global__ void __launch_bounds__(32 * kApplyWarps) k_lmax_apply_rows(int32_t n,
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int32_t i = int32_t(blockIdx.x) * kApplyWarps + wid;
   if (i >= n) return;
+#ifdef SVXG_FAST_SETUP
+  (void)d_sh;
+  const double yr = warp_row_product<double, double, double>(rowptr[i], rowptr[i + 1], col, val, v);
+#else
   double yr = 0.0;
   for (int32_t kb = rowptr[i]; kb < rowptr[i + 1]; kb += kApplyChunk) {
     const int32_t nk = rowptr[i + 1] - kb < kApplyChunk ? rowptr[i + 1] - kb : kApplyChunk;
@@ -150,6 +155,7 @@ __global__ void __launch_bounds__(32 * kApplyWarps) k_lmax_apply_rows(int32_t n,
       for (int32_t kl = 0; kl < nk; ++kl) yr += d_sh[wid][6 * kl + lane];
     __syncwarp();
   }
+#endif
   if (lane < 6) y_sh[wid][lane] = yr;
   __syncwarp();
   if (lane < 6) {
@@ -253,6 +259,10 @@ __global__ void __launch_bounds__(exact::kThreads) k_lmax_step_small(int32_t n, 
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int32_t i = int32_t(blockIdx.x) * (exact::kThreads / 32) + wid;
   if (i < n) {
+#ifdef SVXG_FAST_SETUP
+    // (the fast build: the SpMV's warp-per-row product, its sums in the lanes' order)
+    const double yr = warp_row_product<double, double, double>(rowptr[i], rowptr[i + 1], col, val, v);
+#else
     double yr = 0.0;
     for (int32_t kb = rowptr[i]; kb < rowptr[i + 1]; kb += kStepChunk) {
       const int32_t nk = rowptr[i + 1] - kb < kStepChunk ? rowptr[i + 1] - kb : kStepChunk;
@@ -268,6 +278,7 @@ __global__ void __launch_bounds__(exact::kThreads) k_lmax_step_small(int32_t n, 
         for (int32_t kl = 0; kl < nk; ++kl) yr += d_sh[wid][6 * kl + lane];
       __syncwarp();
     }
+#endif
     if (lane < 6) y_sh[wid][lane] = yr;
     __syncwarp();
     if (lane < 6) {
