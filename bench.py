@@ -324,12 +324,12 @@ def run_serve(args, rank: int, world: int):
     os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     import torch
     from opus_destruct_2_gb300 import load_library, workloads
-    from opus_destruct_2_gb300.graph import PRECISION_FP64, PRECISION_MIXED
+    from opus_destruct_2_gb300.graph import PRECISION_FP64, PRECISION_MIXED, PRECISION_MIXED_ALL
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     L = load_library()
     L.svxg_launch_count.restype = ctypes.c_int64
-    prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
+    prec = {"fp64": PRECISION_FP64, "mixed": PRECISION_MIXED, "mixed-all": PRECISION_MIXED_ALL}[args.precision]
     dist = None
     if world > 1:
         import torch.distributed as dist
@@ -382,8 +382,8 @@ def run_serve(args, rank: int, world: int):
         "config": {"workload": SERVE_DESC.format(req=requests, rate=args.rate, rtol=args.rtol),
                    "requests": requests, "workers": args.workers, "rtol": args.rtol,
                    "precision": ("fp64" if prec == PRECISION_FP64 else
-                                 "mixed policy: fp32 inner sequences from 65,536 free nodes alone, the fp64 "
-                                 "sequence with the fp32 V-cycle below and in batches"),
+                                 "mixed policy: fp32 V-cycle, multigrid built with FMAs and a tree-summed "
+                                 "power-iteration norm, fp64 K and Krylov vectors"),
                    "step": "1000 requests of the stream: each assembled (or bonds removed in place), solved, "
                            "judged",
                    "l2": "the stream's requests together exceed L2 (tens of GB admitted)",
@@ -488,8 +488,8 @@ def run_many(args, rank: int, world: int):
     # (more hardware queues for the server's streams; read when the CUDA context is created)
     os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     from opus_destruct_2_gb300 import workloads
-    from opus_destruct_2_gb300.graph import PRECISION_FP64, PRECISION_MIXED
-    prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
+    from opus_destruct_2_gb300.graph import PRECISION_FP64, PRECISION_MIXED, PRECISION_MIXED_ALL
+    prec = {"fp64": PRECISION_FP64, "mixed": PRECISION_MIXED, "mixed-all": PRECISION_MIXED_ALL}[args.precision]
     clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
     r = workloads.batch(count=args.graphs, workers=args.workers, precision=prec, rtol=args.rtol)
     desc = (f"batch: {args.graphs} fragment graphs, log-normal sizes (median 300, 10-20,000), half free pieces "
@@ -503,7 +503,7 @@ def run_many(args, rank: int, world: int):
         "vs_baseline": None, "dtype": "f64" if prec == PRECISION_FP64 else "f32+f64", "data": "synthetic",
         "config": {"workload": desc, "workers": args.workers,
                    "precision": ("fp64" if prec == PRECISION_FP64 else
-                                 "mixed (fp32 inner sequences from 65536 free nodes; fp64 sequence below)")},
+                                 "mixed policy: fp32 V-cycle, fast multigrid build, fp64 K and Krylov vectors")},
         "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"], "batch": r,
         "vs_plain_fp64_per_request": r["solves_per_s"] / r["plain_fp64_per_request_solves_per_s"],
         "roofline": None,
@@ -766,8 +766,9 @@ def main():
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--rtol", type=float, default=None, help="default: 1e-6 serving and batch, 1e-8 otherwise")
     ap.add_argument("--maxit", type=int, default=500)
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default=None,
-                    help="default: mixed (the policy) serving, fp64 otherwise")
+    ap.add_argument("--precision", choices=["fp64", "mixed", "mixed-all"], default=None,
+                    help="default: mixed (the policy) serving, fp64 otherwise; mixed-all: the policy with FP32 "
+                         "inner sequences")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -830,7 +831,8 @@ def main():
     h = ctypes.c_void_p()
     check(L.svxg_problem_create(ctypes.byref(h), local_rank))
     stream = torch.cuda.ExternalStream(L.svxg_problem_stream(h), device=dev)
-    opt = StressOptions(amg_min_nodes=160, precision=1 if args.precision == "mixed" else 0)
+    opt = StressOptions(amg_min_nodes=160, precision={"fp64": 0, "mixed": 1, "mixed-all": 2}[args.precision])
+    fp32_spmv = args.precision == "mixed-all"  # (the FP32 K conjugate-gradient product: inner sequences)
     ok = ctypes.c_int32()
     res = PcgResult()
     n_over = ctypes.c_int32()
@@ -917,7 +919,7 @@ def main():
     L.svxg_timer_read(h, ctypes.byref(tm), ctypes.byref(tl))
     L.svxg_timer_enable(h, 0)
     # the same kernel in a dedicated loop (every launch does its work) and this GPU's FP64 FMA rate
-    prec_code = 0 if args.precision == "fp64" else 1
+    prec_code = 1 if fp32_spmv else 0
     loop_ms, fp64_tf = ctypes.c_double(), ctypes.c_double()
     check(L.svxg_time_spmv(h, prec_code, 50, ctypes.byref(loop_ms)))
     check(L.svxg_measure_fp64_rate(local_rank, ctypes.byref(fp64_tf)))
@@ -940,12 +942,12 @@ def main():
     info = Info()
     check(L.svxg_get_info(h, ctypes.byref(info)))
     nfree, nnzb = info.nfree, info.matrix_blocks
-    vb = 8 if args.precision == "fp64" else 4
+    vb = 4 if fp32_spmv else 8
     spmv_bytes = nnzb * (36 * vb + 4) + nfree * (4 + 6 * vb + 6 * vb)
     peaks = measured_peaks()
     achieved = (spmv_bytes * tl.value / (tm.value / 1e3) / 1e9) if tm.value > 0 else 0.0
     traffic = None
-    tp = os.path.join(ROOT, "profiles", f"spmv_traffic_{args.precision}.json")
+    tp = os.path.join(ROOT, "profiles", f"spmv_traffic_{'fp32' if fp32_spmv else 'fp64'}.json")
     if os.path.exists(tp):
         with open(tp) as fh:
             tj = json.load(fh)
@@ -973,12 +975,13 @@ def main():
         "config": {"workload": desc, "nodes": int(n), "bonds": int(nb), "dof": int(6 * nfree), "blocks": int(nnzb),
                    "levels": info.sizes(), "rtol": args.rtol, "pcg_iters": int(iters), "failing_bonds": int(info_fail),
                    "precision": ("fp64 K and CG, f32 V-cycle" if args.precision == "fp64" else
-                                 "f32 K SpMV and V-cycle inside fp64 refinement (fp64 residual, dots, coarsest)"),
+                                 "mixed policy: f32 V-cycle, multigrid built with FMAs and a tree-summed "
+                                 "power-iteration norm, fp64 K and Krylov vectors"),
                    "step": "assemble + multigrid build + PCG + judge",
                    "l2": "inputs larger than L2 (K alone is %.0f MB)" % (nnzb * 288 / 1e6),
                    "parallelism": f"replicas x{world}"},
-        "roofline": {"kernel": ("conjugate-gradient SpMV (FP64 BSR 6x6, p.q fused)" if args.precision == "fp64" else
-                                "conjugate-gradient SpMV (FP32 BSR 6x6, p.q fused in FP64)"), "bound": "hbm",
+        "roofline": {"kernel": ("conjugate-gradient SpMV (FP32 BSR 6x6, p.q fused in FP64)" if fp32_spmv else
+                                "conjugate-gradient SpMV (FP64 BSR 6x6, p.q fused)"), "bound": "hbm",
                      "how": "CUDA events around each SpMV launch that did work (the first `iters` of each "
                             "solve) on the problem's stream, over a timed pass of the same solves; loop_avg_us: "
                             "the same kernel in a dedicated loop of 50 launches",
@@ -995,7 +998,7 @@ def main():
                                "frac": (72 * nnzb * tl.value / (tm.value / 1e3) / 1e12) / fp64_tf.value
                                if tm.value > 0 and fp64_tf.value > 0 else None,
                                "peak_source": "measured in this run (independent FMA chains on every SM)"}
-                              if args.precision == "fp64" else None)},
+                              if not fp32_spmv else None)},
         "e2e": {"value": world * args.steps / e2e_elapsed, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),

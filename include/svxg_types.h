@@ -108,10 +108,12 @@ typedef struct svxg_amg_options {
 /* Arithmetic of the solve. */
 enum {
   SVXG_PRECISION_FP64 = 0,      /* FP64 K, FP64 PCG; FP32 V-cycle (as the reference) */
-  SVXG_PRECISION_MIXED = 1,     /* FP32 K and V-cycle inside FP64 iterative refinement, for
-                                   problems of 65536 free nodes or more (smaller ones are
-                                   latency-bound: they run the FP64 sequence) */
-  SVXG_PRECISION_MIXED_ALL = 2  /* the same at every size */
+  SVXG_PRECISION_MIXED = 1,     /* the mixed-precision policy: FP32 V-cycle, the multigrid built
+                                   with FMAs and a tree-summed power-iteration norm (values within
+                                   rounding of the reference's), FP64 K and Krylov vectors; the
+                                   solve states its error against the FP64 solution */
+  SVXG_PRECISION_MIXED_ALL = 2  /* that, and FP32 K and Krylov vectors inside FP64 iterative
+                                   refinement (inner sequences) */
 };
 
 typedef struct svxg_stress_options {

@@ -140,8 +140,8 @@ class AmgOptions(ctypes.Structure):
                 ("reaggregate", ctypes.c_int32)]
 
 
-# StressOptions.precision (svxg_types.h): FP64; mixed for problems of 65536 free nodes or more
-# (smaller ones run the FP64 sequence); mixed at every size
+# StressOptions.precision (svxg_types.h): FP64 (bit-exact setup); the mixed-precision policy (fast
+# multigrid build, FP32 V-cycle, FP64 Krylov vectors); that with FP32 inner sequences
 PRECISION_FP64, PRECISION_MIXED, PRECISION_MIXED_ALL = 0, 1, 2
 
 

@@ -83,7 +83,7 @@ def test_city_block_mixed_at_1e6_jittered_thresholds(city):
     J = oracle.Port(city["nodes"], b, city["mats"])
     _, phi_o, _ = J.judge(city["uo"])  # (strength is not in K: the oracle's u stands)
     G = StressProblem(city["nodes"], b, city["mats"])
-    assert G.assemble(StressOptions(precision=1))  # (the policy: FP32 inner sequences at this size)
+    assert G.assemble(StressOptions(precision=1))  # (the policy: fast multigrid build, FP32 V-cycle)
     u, r = G.solve(city["f"], rtol=1e-6, maxit=2000)
     assert r.converged and r.rel_res <= 1e-6
     err = relerr(u, city["uo"])

@@ -1,5 +1,6 @@
-"""Mixed precision (FP32 K SpMV and FP32 V-cycle inside FP64 iterative refinement) against the
-oracle's FP64 solve: displacements within 1e-5 (relative) at rel. residual 1e-6, each solve's
+"""Mixed precision - the policy (precision 1: the fast multigrid build, FP32 V-cycle, FP64 K and
+Krylov vectors) and its FP32 inner sequences (precision 2: FP32 K SpMV and V-cycle inside FP64
+iterative refinement) - against the oracle's FP64 solve: displacements within 1e-5 (relative) at rel. residual 1e-6, each solve's
 error estimate (||M^-1 r|| / ||u||) within a factor 20 of its measured error, the failure set
 identical with per-bond thresholds drawn as material strength x U(0.9, 1.1) (bonds within the
 solve's error band of phi = 1 listed, none dropped), and the FP64 refinement reaching the tight
@@ -138,8 +139,8 @@ def test_mixed_cap_and_resume_and_edge_loads():
 
 
 def test_mixed_below_its_size_runs_the_fp64_sequence():
-    """Below the size where FP32 inner sequences pay, the mixed policy runs the FP64 conjugate-
-    gradient sequence (with its own multigrid build: FMAs, a tree-summed norm):
+    """The mixed policy runs the FP64 conjugate-gradient sequence (FP32 inner sequences only under
+    MIXED_ALL) with its own multigrid build (FMAs, a tree-summed norm):
     the FP64 path's iteration count within one and its displacement within 1e-6."""
     nodes, bonds = fx.lattice(8)
     f = fx.gravity_live(nodes)
