@@ -534,7 +534,9 @@ def run_pieces(args, rank: int, world: int):
     os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     from opus_destruct_2_gb300 import workloads
     clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
-    r = workloads.pieces(count=args.graphs, workers=args.workers)
+    from opus_destruct_2_gb300.graph import PRECISION_FP64, PRECISION_MIXED, PRECISION_MIXED_ALL
+    prec = {"fp64": PRECISION_FP64, "mixed": PRECISION_MIXED, "mixed-all": PRECISION_MIXED_ALL}[args.precision]
+    r = workloads.pieces(count=args.graphs, workers=args.workers, precision=prec)
     clk = clocks.stop()
     if rank != 0:
         return
@@ -564,7 +566,8 @@ def run_pieces(args, rank: int, world: int):
         "metric": METRIC, "value": r["pieces_per_s"] * world, "unit": "pieces/s", "n_gpus": world, "steps": 1,
         "warmup": 32, "ms_per_step": 1e3 * r["wall_s"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"pieces: {args.graphs} free pieces of log-normal size (median 300 fragments, "
+        "config": {"precision": args.precision,
+                   "workload": f"pieces: {args.graphs} free pieces of log-normal size (median 300 fragments, "
                                f"10-20,000), inertial relief plus one impact each, break rounds at the world's "
                                f"settings (rtol 1e-2, 60 iterations, 8 rounds, resting loads)",
                    "workers": args.workers},

@@ -97,12 +97,14 @@ def batch(count: int = 512, workers: int = 16, precision: int = PRECISION_MIXED,
     }
 
 
-def pieces(count: int = 512, workers: int = 16, seed: int = 5, plain_sample: int = 64, impact_scale: float = 20.0):
+def pieces(count: int = 512, workers: int = 16, seed: int = 5, plain_sample: int = 64, impact_scale: float = 20.0,
+           precision: int = PRECISION_FP64):
     """A substep's loose pieces through their break rounds (svxg_batch_piece_rounds): the batched
     workload's piece sizes (log-normal, median 300 fragments, 10-20,000), every piece free with
     inertial-relief loads and one impact of log-uniform 1e4-1e6 N scaled by `impact_scale` (so
     that most pieces crack), the world's settings (rtol 1e-2, 60 iterations, 8 rounds), resting
-    loads (no energy limit). Reports pieces/s beside one piece after another on one problem."""
+    loads (no energy limit), under `precision` (FP64: the bit-exact multigrid; the mixed policy:
+    its fast build). Reports pieces/s beside one piece after another on one problem."""
     from .graph import PieceOptions
     sizes = synth.lognormal_sizes(count, 300, 10, 20000, seed=seed)
     rng = np.random.default_rng(seed + 1)
@@ -113,11 +115,12 @@ def pieces(count: int = 512, workers: int = 16, seed: int = 5, plain_sample: int
         ps.append((nodes, bonds, f))
     mats = default_materials()
     o = PieceOptions()
+    so = StressOptions(precision=precision)
     with Server(workers=workers, budget=40 << 30) as S:
-        S.batch_piece_rounds(ps[:min(32, count)], mats, options=o)  # (warm-up)
+        S.batch_piece_rounds(ps[:min(32, count)], mats, options=o, opt=so)  # (warm-up)
         S.reset_stats()
         t0 = time.perf_counter()
-        pres, res, _, _, _ = S.batch_piece_rounds(ps, mats, options=o)
+        pres, res, _, _, _ = S.batch_piece_rounds(ps, mats, options=o, opt=so)
         wall = time.perf_counter() - t0
         st = S.stats()
     # one piece after another on one problem (the plain per-request path), on a sample
@@ -125,7 +128,7 @@ def pieces(count: int = 512, workers: int = 16, seed: int = 5, plain_sample: int
     t0 = time.perf_counter()
     for nodes, bonds, f in ps[:lim]:
         G = StressProblem(nodes, bonds, mats)
-        G.piece_rounds(f, options=o)
+        G.piece_rounds(f, options=o, opt=so)
         del G
     plain = lim / (time.perf_counter() - t0)
     return {
