@@ -387,7 +387,8 @@ def run_serve(args, rank: int, world: int):
                    "step": "1000 requests of the stream: each assembled (or bonds removed in place), solved, "
                            "judged",
                    "l2": "the stream's requests together exceed L2 (tens of GB admitted)",
-                   "parallelism": f"replicas x{world}, {args.workers} server slots"},
+                   "parallelism": f"replicas x{world}, {args.workers} server slots, new requests in batches "
+                                  f"of <= {args.batch_graphs or 16} graphs"},
         "p50_ms": dev["p50_ms"], "p99_ms": dev["p99_ms"],
         "block_row_iterations_per_s": world * dev["block_row_iterations_per_s"],
         "serve": {k: dev[k] for k in keys}, "serve_at_70pct": ({k: at70[k] for k in keys} if at70 else None),
@@ -410,7 +411,7 @@ def serve_roofline(stream, L, device: int) -> dict:
     """The serving step's dominant kernel by device time - the multigrid build's Galerkin A P values
     kernel (FP64 6x6 block products in the reference's summation order; the mixed-precision
     policy's build contracts them into FMAs) - timed with CUDA events on its problem's stream over
-    five assembles of a typical batch of the stream (its first 32 new structures as one problem,
+    five assembles of a typical batch of the stream (its first 16 new structures as one problem,
     as the server batches them), against this GPU's FP64 rate measured in the same run."""
     from opus_destruct_2_gb300 import Batch
     from opus_destruct_2_gb300.graph import StressOptions
@@ -418,7 +419,7 @@ def serve_roofline(stream, L, device: int) -> dict:
     L.svxg_timer_read_work.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
                                        ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
     L.svxg_measure_fp64_rate.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
-    news = [stream.geoms[p[2]] for p in stream.plan if p[0] == "new"][:32]
+    news = [stream.geoms[p[2]] for p in stream.plan if p[0] == "new"][:16]
     B = Batch([(g[0], g[1]) for g in news], stream.mats, device=device)
     opt = StressOptions(precision=1)
     B.assemble(opt)
@@ -441,7 +442,7 @@ def serve_roofline(stream, L, device: int) -> dict:
                            "against the FP64 instruction rate (half of it)",
             "traffic": None, "flops_per_launch": flops / max(launches.value, 1), "launches": int(launches.value),
             "avg_us": 1e3 * ms.value / max(launches.value, 1),
-            "workload": f"one batch of the stream's first 32 new structures ({sum(len(g[0]) for g in news)} "
+            "workload": f"one batch of the stream's first 16 new structures ({sum(len(g[0]) for g in news)} "
                         f"fragments), 5 assembles, every level's launch",
             "how": "CUDA events around each launch on the problem's stream; algorithmic FP64 operations from the "
                    "block products counted on the host (the reference's build-work count of A P / 6)"}

@@ -94,7 +94,7 @@ int64_t svxg_server_submit_repeat_device(svxg_server* s, int64_t structure, cons
                                          double fragility, double* u_out, int32_t* over_out);
 
 /* Batching of new requests: at most max_graphs graphs (1: none), each of at most max_graph_nodes
- * nodes, max_nodes in all, per problem. Defaults 32, 20,000 and 65,536. */
+ * nodes, max_nodes in all, per problem. Defaults 16, 20,000 and 65,536. */
 int svxg_server_set_batching(svxg_server* s, int32_t max_graphs, int32_t max_graph_nodes, int64_t max_nodes);
 /* hold != 0: slots finish what they run and take no new request (submissions queue); 0: they take
  * the queue again - a caller that submits a frame's requests together and releases them gets them

@@ -182,7 +182,7 @@ struct svxg_server {
   Slot admin;  // (lent to problems released outside a slot: forget, destroy)
   // batching of new requests (svxg_server_set_batching): at most batch_graphs graphs of at most
   // batch_graph_nodes nodes each and batch_nodes in all go into one problem
-  int32_t batch_graphs = 32;
+  int32_t batch_graphs = 16;
   int32_t batch_graph_nodes = 20000;
   int64_t batch_nodes = 65536;
   int64_t batches = 0, batched_requests = 0;

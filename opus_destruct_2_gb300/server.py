@@ -170,7 +170,7 @@ class Server:
         self._keep[int(t)] = (None, None)
         return int(t)
 
-    def set_batching(self, max_graphs: int = 32, max_graph_nodes: int = 20000, max_nodes: int = 65536):
+    def set_batching(self, max_graphs: int = 16, max_graph_nodes: int = 20000, max_nodes: int = 65536):
         """New requests queued together run as one problem: at most max_graphs graphs (1: none) of at
         most max_graph_nodes nodes, max_nodes in all."""
         _check(self._L.svxg_server_set_batching(self._h, int(max_graphs), int(max_graph_nodes), int(max_nodes)))
