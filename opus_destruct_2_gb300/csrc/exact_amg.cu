@@ -1047,6 +1047,63 @@ __global__ void __launch_bounds__(32 * kAccWarps) k_ap_values_acc(int32_t n, con
     for (int32_t q = lane; q < 36 * len; q += 32) apval[36 * int64_t(e0) + q] = acc[q];
 }
 
+// A P a warp per block of A P for levels of few rows (too few warps to fill the GPU a row each):
+// block k = (i, J) has its 36 entries in the lanes' registers; the warp walks A's row i in order
+// and, for each block A_ij, finds J in P's row j (32 entries a step, by ballot; a row holds a
+// column at most once) and adds the entry's 6-term sum - every entry receives one 6-term sum per
+// A block whose P row holds J, in row order: k_ap_values_acc's sums.
+constexpr int kApWarps = 4;
+__global__ void __launch_bounds__(32 * kApWarps) k_ap_values_warp(int32_t n, int64_t apnnz, const int32_t* rowptr,
+                                                                  const int32_t* col, const double* val,
+                                                                  const int32_t* prow, const int32_t* pcol,
+                                                                  const double* pval, const int32_t* aprow,
+                                                                  const int32_t* scratch, const int64_t* soff,
+                                                                  int32_t* apcol, double* apval) {
+  const int lane = threadIdx.x & 31;
+  const int64_t k = int64_t(blockIdx.x) * kApWarps + (threadIdx.x >> 5);
+  if (k >= apnnz) return;
+  // (the row of block k: the last i with aprow[i] <= k)
+  int32_t lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int32_t mid = (lo + hi + 1) >> 1;
+    if (aprow[mid] <= k) lo = mid;
+    else hi = mid - 1;
+  }
+  const int32_t i = lo;
+  const int32_t J = scratch[soff[i] + (k - aprow[i])];
+  if (lane == 0) apcol[k] = J;
+  const int ra = lane / 6, ca = lane - 6 * (lane / 6);
+  const bool two = lane < 4;
+  const int rb = (lane + 32) / 6, cb = (lane + 32) - 6 * ((lane + 32) / 6);
+  double a0 = 0.0, a1 = 0.0;
+  for (int32_t kk = rowptr[i]; kk < rowptr[i + 1]; ++kk) {
+    const int32_t j = col[kk];
+    const int32_t p0 = prow[j], np = prow[j + 1] - p0;
+    int32_t found = -1;
+    for (int32_t b = 0; b < np; b += 32) {
+      const bool hit = b + lane < np && pcol[p0 + b + lane] == J;
+      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      if (m) {
+        found = p0 + b + __ffs(int(m)) - 1;
+        break;
+      }
+    }
+    if (found < 0) continue;
+    const double* A = val + 36 * int64_t(kk);
+    const double* B = pval + 36 * int64_t(found);
+    double s0 = plus_zero(A[ra * 6] * B[ca]);
+    for (int q = 1; q < 6; ++q) s0 += A[ra * 6 + q] * B[q * 6 + ca];
+    a0 = a0 + s0;
+    if (two) {
+      double s1 = plus_zero(A[rb * 6] * B[cb]);
+      for (int q = 1; q < 6; ++q) s1 += A[rb * 6 + q] * B[q * 6 + cb];
+      a1 = a1 + s1;
+    }
+  }
+  apval[36 * k + lane] = a0;
+  if (two) apval[36 * k + 32 + lane] = a1;
+}
+
 // The coarse rows C = P^T (A P) in the same way: a warp per coarse row, accumulated in shared
 // memory when it has at most kAccSlots blocks. For each restriction entry (fine row i, block P_iI)
 // the blocks of A P's row i are taken 32 at a time and their (block, C entry) items spread over
@@ -1116,6 +1173,7 @@ __global__ void __launch_bounds__(32 * kAccWarps) k_c_values_acc(int32_t na, con
 }
 
 constexpr int32_t kFewRows = 2432;  // (coarse rows: 16 warps on each of 152 SMs)
+constexpr int32_t kFewRowsAP = 2432;  // (fine rows of A P likewise)
 
 // C = P^T (A P) a warp per block of C: block k = (I, J) - I its coarse row, J its column - has
 // its 36 entries in the lanes' registers (entry lane, and 32 + lane for the first four lanes).
@@ -1692,9 +1750,17 @@ int coarsen(Problem& P, size_t l, bool smoothed, bool* made) {
     TRY(apval.alloc(size_t(apnnz) * 36));
     const bool timed = P.timer_on && P.timer_kind == SVXG_TIMER_GALERKIN_AP;
     if (timed) TRY(timer_mark(P));
-    (k_ap_values_acc<<<unsigned((n + kAccWarps - 1) / kAccWarps), 32 * kAccWarps, 0, st>>>(
-         n, F.A.rowptr, F.A.col, F.A.val, F.prow, F.pcol, F.pval, aprow.p, scratch.p, soff.p, apcol.p, apval.p),
-     SVXG_COUNT_LAUNCH());
+    if (n < kFewRowsAP) {  // (levels of few rows: a warp per block of A P)
+      if (apnnz > 0)
+        (k_ap_values_warp<<<unsigned((int64_t(apnnz) + kApWarps - 1) / kApWarps), 32 * kApWarps, 0, st>>>(
+             n, int64_t(apnnz), F.A.rowptr, F.A.col, F.A.val, F.prow, F.pcol, F.pval, aprow.p, scratch.p, soff.p,
+             apcol.p, apval.p),
+         SVXG_COUNT_LAUNCH());
+    } else {
+      (k_ap_values_acc<<<unsigned((n + kAccWarps - 1) / kAccWarps), 32 * kAccWarps, 0, st>>>(
+           n, F.A.rowptr, F.A.col, F.A.val, F.prow, F.pcol, F.pval, aprow.p, scratch.p, soff.p, apcol.p, apval.p),
+       SVXG_COUNT_LAUNCH());
+    }
     if (timed) {
       TRY(timer_mark(P, true));
       P.timer_work += ap_products;  // (6x6 by 6x6 block products: 432 FP64 operations each, no contraction)
