@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(exact::kThreads) k_norm_small(int64_t m, const
 
 // a vector of a few tiles in one block, tile after tile: each tile's segments, then the walk over
 // them from the running sum (a launch instead of four: small requests are launch-bound)
-constexpr int64_t kNormLoopMax = 8 * exact::kTile;
+constexpr int64_t kNormLoopMax = 2 * exact::kTile;  // (beyond two tiles the per-tile launches are faster)
 __global__ void __launch_bounds__(exact::kThreads) k_norm_loop(int64_t m, const double* w, double* v,
                                                               exact::Seg* rec, int32_t* cnt, double* state) {
   __shared__ double nv_sh;
