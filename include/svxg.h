@@ -173,9 +173,9 @@ int svxg_utilization_device(svxg_problem* p, double fragility, double* phi_dev, 
  * the failure count after the stream synchronizes. Allocates nothing: its scratch is one
  * 512 KiB array in the library's device image, so at most 16,777,216 bonds (more: SVXG_ERR_ARG).
  * A device's first call looks that array up (cudaGetSymbolAddress) and keeps its address for the
- * life of the process, so make it before any stream capture, and do not call this after a
- * cudaDeviceReset of that device. Each call synchronizes `stream` before it returns (it reads the
- * count back). Calls share the array: calls that overlap on the GPU race and must be ordered by
+ * life of the process; do not call this after a cudaDeviceReset of that device. Each call
+ * synchronizes `stream` before it returns (it reads the count back), so no call can run inside a
+ * stream capture. Calls share the array: calls that overlap on the GPU race and must be ordered by
  * the caller. Node indices and material ids out of range: SVXG_ERR_ARG, those bonds skipped. */
 int svxg_utilization_noalloc(const svxg_node* nodes_dev, int32_t n, const svxg_bond* bonds_dev, int32_t nb,
                              const svxg_material* mats_dev, const double* u_dev, double fragility, double* phi_dev,
@@ -274,6 +274,9 @@ int svxg_piece_rounds(svxg_problem* p, const svxg_stress_options* opt, const svx
 int svxg_get_info(svxg_problem* p, svxg_info* info);
 /* Kernel launches made by this library since it was loaded (all problems, all threads). */
 int64_t svxg_launch_count(void);
+/* The part of svxg_launch_count run as nodes of the solver's loop graphs (one graph launch per
+ * solve from the host; the rest were launched one by one from host threads). */
+int64_t svxg_graph_launch_count(void);
 /* Live timing of the conjugate-gradient SpMV: CUDA events on the problem's stream around each of
  * its launches while enabled; read returns their summed duration (ms) and count, and resets. */
 int svxg_timer_enable(svxg_problem* p, int32_t on);

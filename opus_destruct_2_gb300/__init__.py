@@ -115,6 +115,7 @@ def load_library() -> ctypes.CDLL:
         "svxg_debug_apply": (c_i32, [c_vp, c_vp, c_vp]),
         "svxg_debug_seq_norm": (c_i32, [c_vp, c_i64, ctypes.POINTER(c_f64)]),
         "svxg_launch_count": (c_i64, []),
+        "svxg_graph_launch_count": (c_i64, []),
         "svxg_utilization_device": (c_i32, [c_vp, c_f64, c_vp, c_vp, c_vp, ctypes.POINTER(c_i32)]),
         "svxg_timer_enable": (c_i32, [c_vp, c_i32]),
         "svxg_timer_read": (c_i32, [c_vp, ctypes.POINTER(c_f64), ctypes.POINTER(c_i64)]),

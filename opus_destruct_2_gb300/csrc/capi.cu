@@ -127,10 +127,19 @@ void set_error(const std::string& msg) { g_error = msg; }
 
 namespace {
 std::atomic<int64_t> g_launches{0};
+std::atomic<int64_t> g_graph_launches{0};  // (the part of g_launches run inside loop graphs)
+thread_local int64_t t_launches = 0;       // (this thread's: what a capture on it enqueued)
 }
-void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_launch() {
+  g_launches.fetch_add(1, std::memory_order_relaxed);
+  ++t_launches;
+}
+int64_t thread_launch_count() { return t_launches; }
 void uncount_launches(int64_t n) { g_launches.fetch_sub(n, std::memory_order_relaxed); }
-void add_launches(int64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+void add_launches(int64_t n) {
+  g_launches.fetch_add(n, std::memory_order_relaxed);
+  g_graph_launches.fetch_add(n, std::memory_order_relaxed);
+}
 
 namespace {
 
@@ -275,6 +284,7 @@ extern "C" {
 const char* svxg_last_error(void) { return g_error.c_str(); }
 
 int64_t svxg_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+int64_t svxg_graph_launch_count(void) { return g_graph_launches.load(std::memory_order_relaxed); }
 
 int svxg_timer_enable(svxg_problem* p, int32_t on) {
   CHECK_P(p);

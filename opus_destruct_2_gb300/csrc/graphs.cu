@@ -61,7 +61,8 @@ int run_loop(Problem& P, void*& slot, const int32_t* done, int (*body)(Problem&)
     cudaGraph_t body_graph = np.conditional.phGraph_out[0];
     SVXG_CUDA(cudaStreamBeginCaptureToGraph(P.stream, body_graph, nullptr, nullptr, 0,
                                             cudaStreamCaptureModeThreadLocal));
-    const int64_t c0 = svxg_launch_count();
+    // (counted on this thread: slots on other threads launch meanwhile)
+    const int64_t c0 = thread_launch_count();
     int e = body(P);
     if (!e) {
       (k_loop_cond<<<1, 32, 0, P.stream>>>(h, done), SVXG_COUNT_LAUNCH());
@@ -69,7 +70,7 @@ int run_loop(Problem& P, void*& slot, const int32_t* done, int (*body)(Problem&)
     }
     cudaGraph_t captured = nullptr;
     const cudaError_t ce = cudaStreamEndCapture(P.stream, &captured);
-    L->body_launches = svxg_launch_count() - c0;
+    L->body_launches = thread_launch_count() - c0;
     uncount_launches(L->body_launches);  // (captured, not run)
     if (e || ce != cudaSuccess) {
       if (ce != cudaSuccess) set_error(std::string("cudaStreamEndCapture: ") + cudaGetErrorString(ce));

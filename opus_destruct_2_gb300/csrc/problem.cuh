@@ -341,6 +341,7 @@ int run_loop(Problem& P, void*& slot, const int32_t* done, int (*body)(Problem&)
 void destroy_loop(void*& slot);
 void uncount_launches(int64_t n);
 void add_launches(int64_t n);
+int64_t thread_launch_count();  // launches counted on the calling thread
 // exact_sections.cu: the bonds of voxel-face interfaces (bad: device counter of sections whose
 // indices lie outside the arrays, or null)
 int build_bonds_device(const svxg_node* nodes, int32_t n, const svxg_section* secs, int32_t nb, const svxg_face* faces,

@@ -20,7 +20,7 @@ import time
 
 import numpy as np
 
-from . import StressProblem, synth
+from . import StressProblem, load_library, synth
 from .graph import PRECISION_FP64, PRECISION_MIXED, StressOptions, default_materials
 from .server import Server
 
@@ -225,6 +225,7 @@ def serve_stream(stream: Stream, workers: int = 16, precision: int = PRECISION_M
     scale = 1.0 if rate is None else stream.rate / rate
     opt = StressOptions(precision=precision)
     mats = stream.mats
+    L = load_library()
     with Server(workers=workers, budget=budget) as S:
         if batching is not None:
             S.set_batching(*batching)
@@ -233,6 +234,7 @@ def serve_stream(stream: Stream, workers: int = 16, precision: int = PRECISION_M
             S.submit(*stream.geoms[g][:2], mats, stream.geoms[g][2], opt=opt, rtol=rtol, maxit=maxit, want_u=False)
         S.drain()
         S.reset_stats()
+        l0, g0 = L.svxg_launch_count(), L.svxg_graph_launch_count()
         tickets = []
         t_start = time.perf_counter()
         t_next = t_start
@@ -258,6 +260,7 @@ def serve_stream(stream: Stream, workers: int = 16, precision: int = PRECISION_M
         submit_s = time.perf_counter() - t_start
         res = [S.wait(t)[0] for t in tickets]
         wall = time.perf_counter() - t_start
+        launches, in_graphs = L.svxg_launch_count() - l0, L.svxg_graph_launch_count() - g0
         st = S.stats()
     lat = np.array([r.latency_ms for r in res])
     ok = np.array([bool(r.status == 0 and r.converged) for r in res])
@@ -283,6 +286,8 @@ def serve_stream(stream: Stream, workers: int = 16, precision: int = PRECISION_M
         "batches": int(st.batches), "batched_requests": int(st.batched_requests),
         "evictions": int(st.evictions), "admission_waits": int(st.admission_waits),
         "peak_admitted_bytes": int(st.peak_bytes), "workers": workers, "inputs": inputs,
+        "launches": int(launches), "launches_in_graphs": int(in_graphs),
+        "host_launches_per_s": float(launches - in_graphs) / wall,
     }
 
 
