@@ -66,6 +66,7 @@ void release_solver(Problem& P) {
   P.mem.release(P.d_seg);
   P.mem.release(P.d_seg_flag);
   P.mem.release(P.d_seg_of_row);
+  P.mem.release(P.d_seg_lmap);
   P.mem.release(P.d_jinv);
   P.mem.release(P.d_dof);
   P.mem.release(P.d_chol);

@@ -140,6 +140,7 @@ struct Level {
   float* t32 = nullptr;
   float* u32 = nullptr;
   int sched_a = 0, sched_p = 0, sched_r = 0;  // row-product schedules (spmv_row.cuh), autotuned
+  const int32_t* gmap = nullptr;  // a batch's: each row's graph (-1: unknown), in Problem::d_seg_lmap
 };
 
 struct Problem {
@@ -185,6 +186,9 @@ struct Problem {
   int32_t* d_seg_of_row = nullptr;  // each free row's graph
   double* d_seg = nullptr;        // per graph: its sequence's scalars (solve.cu kSegF)
   int32_t* d_seg_flag = nullptr;  // per graph: 0 running, 1 converged, 2 broken down
+  int32_t* d_seg_lmap = nullptr;  // every coarse level's row -> graph (Level::gmap; level 0: d_seg_of_row)
+  // set while a batch's iteration body is enqueued: its kernels skip the rows of stopped graphs
+  const int32_t* skip_flag = nullptr;
   // multigrid
   std::vector<Level> lv;
   double* d_chol = nullptr;       // coarsest dense factor (m x m, lower = L, upper = L^T)
@@ -318,6 +322,7 @@ int utilization_device(Problem& P, const double* u_nodes, double fragility, doub
                        int32_t* over, int32_t* n_over);
 // graphs.cu
 bool use_graphs();
+bool seg_skip(const Problem& P);  // a batch's iteration bodies skip stopped graphs' rows
 constexpr int32_t kGraphMinFree = 4096;
 // K of at least this many block rows gets its rows sorted by length for the conjugate-gradient
 // products (solve.cu build_row_slots): one host round trip of K's row pointers at assembly.

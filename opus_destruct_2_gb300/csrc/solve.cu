@@ -103,13 +103,14 @@ template <int EPI, int SCHED>
 __global__ void __launch_bounds__(kSpmvT) k_spmv(int32_t n, const int32_t* __restrict__ rowptr,
                                                  const int32_t* __restrict__ col, const double* __restrict__ val,
                                                  const double* __restrict__ x, double* __restrict__ y,
-                                                 double* partials, unsigned* counter, PcgScalars* s) {
+                                                 double* partials, unsigned* counter, PcgScalars* s,
+                                                 RowSkip skip) {
   __shared__ double sh[kSpmvT / 32];
   if (s && s->done) return;  // (the product of a running sequence: nothing once it is done)
   int c;
   bool lane_ok;
   const int32_t row = sched_row<SCHED>(kRowsPerBlock, &c, &lane_ok);
-  const bool row_ok = row < n;
+  const bool row_ok = row < n && !row_skipped(skip, row);
   const double yr = sched_row_product<SCHED, double, double, double>(row_ok, row, rowptr, col, val, x);
   double dp = 0.0;
   if (row_ok && lane_ok) {
@@ -190,13 +191,14 @@ __global__ void __launch_bounds__(kSpmvT) k_spmv_dot(int32_t n, const int32_t* _
 #define SVXG_SLOT_MINBLOCKS 3
 #endif
 constexpr int kSlotRows = SVXG_SLOT_ROWS;
-template <int EPI>
+template <int EPI, bool SKIP = false>
 __global__ void __launch_bounds__(kSpmvT, SVXG_SLOT_MINBLOCKS) k_spmv_slots(int32_t n, const int4* __restrict__ slots,
                                                                            const int32_t* __restrict__ col,
                                                                            const double* __restrict__ val,
                                                                            const double* __restrict__ x,
                                                                            double* __restrict__ y, double* partials,
-                                                                           unsigned* counter, PcgScalars* s) {
+                                                                           unsigned* counter, PcgScalars* s,
+                                                                           RowSkip skip) {
   __shared__ double sh[kSpmvT / 32];
   if (s && s->done) return;  // (the product of a running sequence: nothing once it is done)
   const int c = (threadIdx.x & 31) % 6;
@@ -204,7 +206,7 @@ __global__ void __launch_bounds__(kSpmvT, SVXG_SLOT_MINBLOCKS) k_spmv_slots(int3
   int32_t row[kSlotRows];
   bool ok[kSlotRows];
   double yr[kSlotRows];
-  slot_rows_product<kSlotRows, double, double, double>(slots, first, n, col, val, x, row, ok, yr);
+  slot_rows_product<kSlotRows, double, double, double, SKIP>(slots, first, n, col, val, x, row, ok, yr, skip);
   double dp = 0.0;
 #pragma unroll
   for (int j = 0; j < kSlotRows; ++j)
@@ -231,14 +233,20 @@ __global__ void __launch_bounds__(kSpmvT, SVXG_SLOT_MINBLOCKS) k_spmv_slots(int3
   }
 }
 
+// skip (EPI kPlain only): rows of stopped graphs of a batch get no product
 template <int EPI>
 void launch_spmv(cudaStream_t st, int sched, int32_t n, const int32_t* rowptr, const int32_t* col, const double* val,
                  const double* x, double* y, double* partials, unsigned* counter, PcgScalars* s,
-                 const int4* slots = nullptr) {
+                 const int4* slots = nullptr, RowSkip skip = RowSkip{}) {
   if (slots) {
     const int64_t per = int64_t(kRowsPerBlock) * kSlotRows * 5;
     const unsigned g = unsigned((std::max<int64_t>(n, 1) + per - 1) / per);
-    (k_spmv_slots<EPI><<<g, kSpmvT, 0, st>>>(n, slots, col, val, x, y, partials, counter, s), SVXG_COUNT_LAUNCH());
+    if (EPI == kPlain && skip.flag)
+      (k_spmv_slots<kPlain, true><<<g, kSpmvT, 0, st>>>(n, slots, col, val, x, y, partials, counter, s, skip),
+       SVXG_COUNT_LAUNCH());
+    else
+      (k_spmv_slots<EPI><<<g, kSpmvT, 0, st>>>(n, slots, col, val, x, y, partials, counter, s, RowSkip{}),
+       SVXG_COUNT_LAUNCH());
     return;
   }
   if (EPI == kDotP) {
@@ -252,10 +260,11 @@ void launch_spmv(cudaStream_t st, int sched, int32_t n, const int32_t* rowptr, c
        SVXG_COUNT_LAUNCH());
   } else if (sched == kGroupRow) {
     const unsigned g = unsigned((std::max(n, 1) + 5 * kRowsPerBlock - 1) / (5 * kRowsPerBlock));
-    (k_spmv<EPI, kGroupRow><<<g, kSpmvT, 0, st>>>(n, rowptr, col, val, x, y, partials, counter, s),
+    (k_spmv<EPI, kGroupRow><<<g, kSpmvT, 0, st>>>(n, rowptr, col, val, x, y, partials, counter, s, skip),
      SVXG_COUNT_LAUNCH());
   } else {
-    (k_spmv<EPI, kWarpRow><<<spmv_blocks(n), kSpmvT, 0, st>>>(n, rowptr, col, val, x, y, partials, counter, s),
+    (k_spmv<EPI, kWarpRow><<<spmv_blocks(n), kSpmvT, 0, st>>>(n, rowptr, col, val, x, y, partials, counter, s,
+                                                               skip),
      SVXG_COUNT_LAUNCH());
   }
 }
@@ -987,13 +996,23 @@ __global__ void __launch_bounds__(kJacobiBlockT) k_jacobi_pcg_block(int32_t nf, 
 int seg_body(Problem& P) {
   const int32_t nf = P.nfree;
   cudaStream_t st = P.stream;
+  // (the rows of graphs whose sequence has stopped: no product, no cycle - their q and z are read
+  // by nothing until the next begin recomputes every row)
+  RowSkip skip;
+  if (seg_skip(P)) {
+    skip.gmap = P.d_seg_of_row;
+    skip.flag = P.d_seg_flag;
+  }
   launch_spmv<kPlain>(st, P.sched_k64, nf, P.K.rowptr, P.K.col, P.K.val, P.d_p, P.d_q, nullptr, nullptr, P.d_s,
-                      P.d_kslots);
+                      P.d_kslots, skip);
   TRY(seg_launch(P, kSegPq, P.d_p, P.d_q, 0.0));
   (k_seg_axpy<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_seg_of_row, P.d_seg, P.d_seg_flag, P.d_x, P.d_r, P.d_p,
                                                 P.d_q, P.d_s), SVXG_COUNT_LAUNCH());
   TRY(seg_launch(P, kSegRn, P.d_r, P.d_r, 0.0));
-  TRY(precondition(P, P.d_r, P.d_z));
+  P.skip_flag = P.pc_n == nf ? skip.flag : nullptr;
+  const int e = precondition(P, P.d_r, P.d_z);
+  P.skip_flag = nullptr;
+  TRY(e);
   TRY(seg_launch(P, kSegRz, P.d_r, P.d_z, 0.0));
   (k_seg_pupdate<<<vec_blocks(nf), kVecT, 0, st>>>(nf, P.d_seg_of_row, P.d_seg, P.d_seg_flag, P.d_z, P.d_p, P.d_s),
    SVXG_COUNT_LAUNCH());
@@ -1025,6 +1044,13 @@ int plain_body(Problem& P) {
   (k_mark_cap<<<1, 32, 0, st>>>(P.d_s), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   return SVXG_OK;
+}
+
+// Whether a batch's iteration bodies skip the rows of its stopped graphs (SVXG_NO_ROW_SKIP=1:
+// never; the running graphs' results are the same bits either way).
+bool seg_skip(const Problem& P) {
+  static const bool off = std::getenv("SVXG_NO_ROW_SKIP") != nullptr;
+  return !off && P.seg_n > 1 && P.d_seg_of_row && P.d_seg_flag;
 }
 
 // whole iterate() calls as one graph launch (SVXG_NO_GRAPHS=1: host-driven batches instead)
@@ -1131,6 +1157,47 @@ int plain_iterate(Problem& P, int32_t maxit, double rtol, svxg_pcg_result* res) 
   return SVXG_OK;
 }
 
+// graph of each coarse row from its fine rows' prolongation entries (every entry of a fine row
+// names an aggregate of the same graph: a batch's hierarchy is block diagonal)
+__global__ void k_coarse_gmap(int32_t n, const int32_t* __restrict__ prow, const int32_t* __restrict__ pcol,
+                              const int32_t* __restrict__ fine, int32_t* coarse) {
+  const int32_t i = blockIdx.x * kVecT + threadIdx.x;
+  if (i >= n) return;
+  const int32_t g = fine[i];
+  for (int32_t k = prow[i]; k < prow[i + 1]; ++k) coarse[pcol[k]] = g;
+}
+
+// Each level's rows by graph, for the skipping in a batch's iteration bodies (level 0: the free
+// rows' graphs; a coarse row: its fine rows'; -1 where no fine row names it, never skipped), and
+// the cycle's vectors zeroed: a skipped row keeps its last, finite values, which the coarsest
+// dense inverse multiplies by its exact zeros between graphs.
+int seg_level_maps(Problem& P) {
+  if (P.jacobi_only || P.lv.empty() || P.lv[0].A.n != P.nfree) return SVXG_OK;
+  cudaStream_t st = P.stream;
+  int64_t tot = 0;
+  for (size_t l = 1; l < P.lv.size(); ++l) tot += std::max(P.lv[l].A.n, 0);
+  if (tot > 0) {
+    TRY(P.mem.alloc(&P.d_seg_lmap, size_t(tot)));
+    SVXG_CUDA(cudaMemsetAsync(P.d_seg_lmap, 0xff, sizeof(int32_t) * size_t(tot), st));
+  }
+  P.lv[0].gmap = P.d_seg_of_row;
+  int64_t off = 0;
+  for (size_t l = 1; l < P.lv.size(); ++l) {
+    int32_t* map = P.d_seg_lmap + off;
+    off += std::max(P.lv[l].A.n, 0);
+    const Level& F = P.lv[l - 1];
+    if (F.A.n > 0 && F.prow && F.pcol)
+      (k_coarse_gmap<<<vec_blocks(F.A.n), kVecT, 0, st>>>(F.A.n, F.prow, F.pcol, F.gmap, map), SVXG_COUNT_LAUNCH());
+    P.lv[l].gmap = map;
+  }
+  for (Level& L : P.lv)
+    for (float* v : {L.b32, L.x32, L.r32, L.t32, L.u32})
+      if (v) SVXG_CUDA(cudaMemsetAsync(v, 0, sizeof(float) * 6 * size_t(std::max(L.A.n, 1)), st));
+  if (P.d_cvec && P.chol_n > 0) SVXG_CUDA(cudaMemsetAsync(P.d_cvec, 0, sizeof(double) * 2 * size_t(P.chol_n), st));
+  SVXG_CUDA(cudaGetLastError());
+  return SVXG_OK;
+}
+
 // A batch's free-row offsets and each free row's graph from the DOF numbering (free nodes numbered
 // in node order, so graph g's free rows are those of its nodes), and its per-graph state; after each
 // assembly.
@@ -1139,6 +1206,8 @@ int seg_prepare(Problem& P) {
   P.mem.release(P.d_seg);
   P.mem.release(P.d_seg_flag);
   P.mem.release(P.d_seg_of_row);
+  P.mem.release(P.d_seg_lmap);
+  for (Level& L : P.lv) L.gmap = nullptr;
   if (P.seg_n <= 0) return SVXG_OK;
   std::vector<int32_t> row0(size_t(P.seg_n) + 1, 0), of_row(size_t(std::max(P.nfree, 1)), 0);
   int32_t fr = 0;
@@ -1158,6 +1227,7 @@ int seg_prepare(Problem& P) {
                             P.stream));
   SVXG_CUDA(cudaMemsetAsync(P.d_seg, 0, sizeof(double) * size_t(kSegF) * size_t(P.seg_n), P.stream));
   SVXG_CUDA(cudaMemsetAsync(P.d_seg_flag, 0, sizeof(int32_t) * size_t(P.seg_n), P.stream));
+  TRY(seg_level_maps(P));
   SVXG_CUDA(host_wait(P.stream));  // (row0 and of_row are freed on return)
   return SVXG_OK;
 }

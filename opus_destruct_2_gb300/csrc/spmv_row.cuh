@@ -23,6 +23,21 @@ struct Vec2<double> {
   using T = double2;
 };
 
+// Rows of a batch (many graphs as one block-diagonal problem, every level of its multigrid block
+// diagonal too) whose graph's conjugate-gradient sequence has stopped: inside an iteration the
+// products and the cycle skip them. gmap: each row's graph (-1: never skipped), flag: per graph,
+// nonzero once its sequence stopped; flag null: nothing is skipped.
+struct RowSkip {
+  const int32_t* gmap = nullptr;
+  const int32_t* flag = nullptr;
+};
+
+__device__ __forceinline__ bool row_skipped(const RowSkip& k, int32_t row) {
+  if (!k.flag) return false;
+  const int32_t g = k.gmap[row];
+  return g >= 0 && k.flag[g] != 0;
+}
+
 // m: row c of a block (6 values), x: the column's 6 values; V and X are float or double
 template <typename V, typename X, typename A>
 __device__ __forceinline__ A dot6(const V* __restrict__ m, const X* __restrict__ x) {
@@ -138,10 +153,12 @@ __device__ __forceinline__ A sched_row_product(bool row_ok, int32_t row, const i
 // product can issue: GB300's FP64 rate bounds the FP64 product. (The FP32 products keep K's row
 // order, whose neighbouring rows share value sectors and x in L1: sorted rows made the city block's
 // FP32 CG product 41 -> 59-74 us.)
-template <int R, typename V, typename X, typename A>
+// SKIP: rows of stopped graphs (skip) come out not ok, with no product.
+template <int R, typename V, typename X, typename A, bool SKIP = false>
 __device__ __forceinline__ void slot_rows_product(const int4* __restrict__ slots, int64_t first, int64_t nslots,
                                                   const int32_t* __restrict__ col, const V* __restrict__ val,
-                                                  const X* __restrict__ x, int32_t row[R], bool ok[R], A out[R]) {
+                                                  const X* __restrict__ x, int32_t row[R], bool ok[R], A out[R],
+                                                  RowSkip skip = RowSkip{}) {
   using MV = typename Vec2<V>::T;
   using XV = typename Vec2<X>::T;
   const int lane = threadIdx.x & 31;
@@ -152,7 +169,11 @@ __device__ __forceinline__ void slot_rows_product(const int4* __restrict__ slots
   for (int j = 0; j < R; ++j) {
     const int64_t sl = first + int64_t(g) * R + j;
     ok[j] = g < 5 && sl < nslots;
-    const int4 e = ok[j] ? __ldg(slots + sl) : make_int4(0, 0, 0, 0);
+    int4 e = ok[j] ? __ldg(slots + sl) : make_int4(0, 0, 0, 0);
+    if (SKIP && ok[j] && row_skipped(skip, e.x)) {
+      ok[j] = false;
+      e.z = 0;
+    }
     row[j] = e.x;
     k0[j] = e.y;
     len[j] = e.z;

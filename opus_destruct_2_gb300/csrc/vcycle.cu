@@ -14,6 +14,12 @@
 // Per level and cycle: pre-smoothing (2 kernels), residual (1), restriction (1, an SpMV over
 // P^T stored by coarse row), prolongation (1, an SpMV over P by fine row, accumulating),
 // post-smoothing (2).
+//
+// In a batch's iteration (P.skip_flag set) every kernel skips the rows of the graphs whose
+// sequence has stopped (each level's rows carry their graph, Level::gmap): the hierarchy is block
+// diagonal, so a running graph's rows read only its own rows, except in the coarsest dense
+// inverse, whose entries between graphs are exact zeros (times the skipped rows' earlier, finite
+// values). A running graph's z is the same bits with and without the skipping.
 #include <algorithm>
 #include <cmath>
 
@@ -38,16 +44,17 @@ constexpr int kChebDegree = 2;      // smoothing polynomial degree (each side)
 constexpr double kChebRatio = 10.0; // lmax / lmin of the smoothed interval
 constexpr int kCoarseDegree = 8;    // stalled coarsest level: polynomial degree in place of a solve
 
-__global__ void k_cvt(int64_t m, const double* in, float* out, const int32_t* stop = nullptr) {
+__global__ void k_cvt(int64_t m, const double* in, float* out, const int32_t* stop = nullptr,
+                      RowSkip skip = RowSkip{}) {
   if (stop && *stop) return;
   const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k < m) out[k] = float(in[k]);
+  if (k < m && !row_skipped(skip, int32_t(k / 6))) out[k] = float(in[k]);
 }
 
-__global__ void k_widen(int64_t m, const float* in, double* out, const int32_t* stop) {
+__global__ void k_widen(int64_t m, const float* in, double* out, const int32_t* stop, RowSkip skip) {
   if (stop && *stop) return;
   const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k < m) out[k] = double(in[k]);
+  if (k < m && !row_skipped(skip, int32_t(k / 6))) out[k] = double(in[k]);
 }
 
 // R (P^T blocks) in restriction order: R_r = P_{rent_e[r]}^T, row-major
@@ -89,6 +96,7 @@ enum Mode {
 
 struct StepArgs {
   const int32_t* stop;  // nonzero: the run is over, return at once
+  RowSkip skip;         // output rows of stopped graphs: no product, nothing written
   const float* rin;  // kStep / kResPend: previous residual; kPostStart: b
   float* r;          // residual out
   float* dout;       // next direction
@@ -107,7 +115,7 @@ __global__ void __launch_bounds__(kT) k_bsr32(int32_t n, const int32_t* __restri
   int c;
   bool lane_ok;
   const int32_t row = sched_row<SCHED>(kRows, &c, &lane_ok);
-  const bool row_ok = row < n;
+  const bool row_ok = row < n && !row_skipped(s.skip, row);
   if (SCHED == kWarpRow && !row_ok) return;  // (whole warps exit together)
   const float av = sched_row_product<SCHED, float, float, float>(row_ok, row, rowptr, col, val, v);
   const bool act = lane_ok && row_ok;
@@ -157,10 +165,10 @@ void bsr32(cudaStream_t st, int sched, int32_t n, const int32_t* rowptr, const i
 
 // d = D^-1 b / theta (the first Chebyshev direction from x = 0); one thread per node
 __global__ void k_cheb_first(int32_t n, const float* __restrict__ D, const float* __restrict__ b, float inv_theta,
-                             float* d, const int32_t* stop) {
+                             float* d, const int32_t* stop, RowSkip skip) {
   if (stop && *stop) return;
   const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= n || row_skipped(skip, i)) return;
   const float* Di = D + 36 * int64_t(i);
   float bv[6];
   for (int q = 0; q < 6; ++q) bv[q] = b[6 * int64_t(i) + q];
@@ -171,19 +179,20 @@ __global__ void k_cheb_first(int32_t n, const float* __restrict__ D, const float
   }
 }
 
-__global__ void k_add(int64_t m, const float* d, float* x, const int32_t* stop) {
+__global__ void k_add(int64_t m, const float* d, float* x, const int32_t* stop, RowSkip skip) {
   if (stop && *stop) return;
   const int64_t k = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (k < m) x[k] += d[k];
+  if (k < m && !row_skipped(skip, int32_t(k / 6))) x[k] += d[k];
 }
 
 // coarsest level: x = L^-T (L^-1 b) in f64 (warp per row, rows of L^-1 and of L^-T)
 __global__ void k_dense_mv(int32_t m, const double* __restrict__ M, const float* __restrict__ b32,
-                           const double* __restrict__ b64, double* y64, float* y32, const int32_t* stop) {
+                           const double* __restrict__ b64, double* y64, float* y32, const int32_t* stop,
+                           RowSkip skip) {
   if (stop && *stop) return;
   const int lane = threadIdx.x & 31;
   const int32_t row = blockIdx.x * kRows + (threadIdx.x >> 5);
-  if (row >= m) return;
+  if (row >= m || row_skipped(skip, row / 6)) return;  // (m: 6 per node; warp-uniform)
   double s = 0.0;
   const double* Mr = M + int64_t(row) * m;
   for (int32_t k = lane; k < m; k += 32) s += Mr[k] * (b32 ? double(b32[k]) : b64[k]);
@@ -284,6 +293,16 @@ Cheb chebyshev(double lmax, double ratio, int degree) {
   return C;
 }
 
+// the rows of stopped graphs a level's kernels skip (none outside a batch's iteration)
+RowSkip level_skip(const Problem& P, const Level& L) {
+  RowSkip k;
+  if (P.skip_flag && L.gmap) {
+    k.gmap = L.gmap;
+    k.flag = P.skip_flag;
+  }
+  return k;
+}
+
 // Chebyshev smoothing of A x = b. from_zero: x = p(D^-1 A) D^-1 b; else x += p(D^-1 A) D^-1 (b - A x).
 // Leaves r = b - A x (from_zero, want_residual) for the restriction.
 int smooth(Problem& P, const Level& L, const float* b, float* x, bool from_zero, int degree, double ratio,
@@ -295,9 +314,11 @@ int smooth(Problem& P, const Level& L, const float* b, float* x, bool from_zero,
   float* d1 = L.u32;
   StepArgs s{};
   s.stop = P.cycle_stop;
+  s.skip = level_skip(P, L);
   s.D = L.dinv32;
   if (from_zero) {
-    (k_cheb_first<<<nblk(n), kT, 0, st>>>(n, L.dinv32, b, C.inv_theta, d0, P.cycle_stop), SVXG_COUNT_LAUNCH());
+    (k_cheb_first<<<nblk(n), kT, 0, st>>>(n, L.dinv32, b, C.inv_theta, d0, P.cycle_stop, s.skip),
+     SVXG_COUNT_LAUNCH());
     s.rin = b;
   } else {
     s.rin = b;
@@ -331,7 +352,7 @@ int smooth(Problem& P, const Level& L, const float* b, float* x, bool from_zero,
     if (from_zero) {
       SVXG_CUDA(cudaMemcpyAsync(x, d0, sizeof(float) * 6 * size_t(n), cudaMemcpyDeviceToDevice, st));
     } else {
-      (k_add<<<nblk(6 * int64_t(n)), kT, 0, st>>>(6 * int64_t(n), d0, x, P.cycle_stop), SVXG_COUNT_LAUNCH());
+      (k_add<<<nblk(6 * int64_t(n)), kT, 0, st>>>(6 * int64_t(n), d0, x, P.cycle_stop, s.skip), SVXG_COUNT_LAUNCH());
     }
   }
   return SVXG_OK;
@@ -344,21 +365,27 @@ int cycle(Problem& P, size_t l, const float* b, float* x) {
   if (l + 1 == P.lv.size()) {
     if (P.chol_n > 0) {
       const int32_t m = P.chol_n;
-      (k_dense_mv<<<rblk(m), kT, 0, st>>>(m, P.d_cinv, b, nullptr, P.d_cvec, nullptr, P.cycle_stop), SVXG_COUNT_LAUNCH());
-      (k_dense_mv<<<rblk(m), kT, 0, st>>>(m, P.d_cinv + int64_t(m) * m, nullptr, P.d_cvec, nullptr, x, P.cycle_stop), SVXG_COUNT_LAUNCH());
+      const RowSkip sk = level_skip(P, L);
+      (k_dense_mv<<<rblk(m), kT, 0, st>>>(m, P.d_cinv, b, nullptr, P.d_cvec, nullptr, P.cycle_stop, sk),
+       SVXG_COUNT_LAUNCH());
+      (k_dense_mv<<<rblk(m), kT, 0, st>>>(m, P.d_cinv + int64_t(m) * m, nullptr, P.d_cvec, nullptr, x, P.cycle_stop,
+                                          sk),
+       SVXG_COUNT_LAUNCH());
       return SVXG_OK;
     }
     return smooth(P, L, b, x, true, kCoarseDegree, 30.0, false);
   }
   TRY(smooth(P, L, b, x, true, kChebDegree, kChebRatio, true));
   const Level& C = P.lv[l + 1];
-  StepArgs none{};
-  none.stop = P.cycle_stop;
+  StepArgs coarse{}, fine{};
+  coarse.stop = fine.stop = P.cycle_stop;
+  coarse.skip = level_skip(P, C);
+  fine.skip = level_skip(P, L);
   // restriction: bc = P^T r
-  bsr32<kY>(st, L.sched_r, C.A.n, L.rrow, L.rent_i, L.pval32 + 36 * L.pnnz, L.r32, C.b32, none);
+  bsr32<kY>(st, L.sched_r, C.A.n, L.rrow, L.rent_i, L.pval32 + 36 * L.pnnz, L.r32, C.b32, coarse);
   TRY(cycle(P, l + 1, C.b32, C.x32));
   // prolongation: x += P xc
-  bsr32<kAcc>(st, L.sched_p, n, L.prow, L.pcol, L.pval32, C.x32, x, none);
+  bsr32<kAcc>(st, L.sched_p, n, L.prow, L.pcol, L.pval32, C.x32, x, fine);
   TRY(smooth(P, L, b, x, false, kChebDegree, kChebRatio, false));
   return SVXG_OK;
 }
@@ -431,9 +458,10 @@ int vcycle(Problem& P, const double* r, double* z) {
   cudaStream_t st = P.stream;
   Level& L0 = P.lv[0];
   const int64_t m = 6 * int64_t(L0.A.n);
-  (k_cvt<<<nblk(m), kT, 0, st>>>(m, r, L0.b32, P.cycle_stop), SVXG_COUNT_LAUNCH());
+  const RowSkip sk = level_skip(P, L0);
+  (k_cvt<<<nblk(m), kT, 0, st>>>(m, r, L0.b32, P.cycle_stop, sk), SVXG_COUNT_LAUNCH());
   TRY(cycle(P, 0, L0.b32, L0.x32));
-  (k_widen<<<nblk(m), kT, 0, st>>>(m, L0.x32, z, P.cycle_stop), SVXG_COUNT_LAUNCH());
+  (k_widen<<<nblk(m), kT, 0, st>>>(m, L0.x32, z, P.cycle_stop, sk), SVXG_COUNT_LAUNCH());
   SVXG_CUDA(cudaGetLastError());
   return SVXG_OK;
 }
