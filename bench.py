@@ -543,7 +543,8 @@ def run_pieces(args, rank: int, world: int):
     clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
     from opus_destruct_2_gb300.graph import PRECISION_FP64, PRECISION_MIXED, PRECISION_MIXED_ALL
     prec = {"fp64": PRECISION_FP64, "mixed": PRECISION_MIXED, "mixed-all": PRECISION_MIXED_ALL}[args.precision]
-    r = workloads.pieces(count=args.graphs, workers=args.workers, precision=prec)
+    r = workloads.pieces(count=args.graphs, workers=args.workers, precision=prec, steps=args.steps,
+                         warmup=args.warmup)
     clk = clocks.stop()
     if rank != 0:
         return
@@ -570,8 +571,9 @@ def run_pieces(args, rank: int, world: int):
                "sample": f"all {done} pieces of the same substep, one single-threaded oracle process per core "
                          f"(the reference's one piece per pool thread)"}
     line = {
-        "metric": METRIC, "value": r["pieces_per_s"] * world, "unit": "pieces/s", "n_gpus": world, "steps": 1,
-        "warmup": 32, "ms_per_step": 1e3 * r["wall_s"], "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": r["pieces_per_s"] * world, "unit": "pieces/s", "n_gpus": world,
+        "steps": r["substeps"], "warmup": r["warmup_substeps"], "ms_per_step": 1e3 * r["wall_s"] / r["substeps"],
+        "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"precision": args.precision,
                    "workload": f"pieces: {args.graphs} free pieces of log-normal size (median 300 fragments, "

@@ -126,6 +126,13 @@ int upload_bond_flags(Problem& P, int32_t b) {
 
 void set_error(const std::string& msg) { g_error = msg; }
 
+// More hardware work queues than the driver's default of 8: a server's slots (and hosts that solve
+// on many threads) run a stream each, and streams beyond the queue count share queues and
+// serialize (the loose-pieces batch ran at half its rate with 8). The driver reads the variable
+// when the process's CUDA context is made, so it is set when the library loads, unless the host
+// chose a value; a context made before the library loaded keeps its own.
+__attribute__((constructor)) static void default_connections() { setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0); }
+
 namespace {
 std::atomic<int64_t> g_launches{0};
 std::atomic<int64_t> g_graph_launches{0};  // (the part of g_launches run inside loop graphs)

@@ -1057,12 +1057,17 @@ int svxg_batch_piece_rounds(svxg_server* S, int32_t count, const svxg_node* cons
   }
   std::vector<int64_t> t(size_t(count), 0);
   int err = SVXG_OK;
-  for (int32_t i = 0; i < count; ++i) {
+  for (int32_t i = 0; i < count; ++i)
     if (n[i] < 0 || nb[i] < 0 || (n[i] > 0 && (!nodes[i] || !f[i])) || (nb[i] > 0 && !bonds[i])) {
-      err = SVXG_ERR_ARG;
       set_error("svxg_batch_piece_rounds: bad piece");
-      break;
+      return SVXG_ERR_ARG;
     }
+  // the largest pieces first (by bonds), so that the longest rounds start early and the small
+  // pieces fill the slots around them; each piece's result is its own whatever the order
+  std::vector<int32_t> order(static_cast<size_t>(count));
+  for (int32_t i = 0; i < count; ++i) order[size_t(i)] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return nb[a] > nb[b]; });
+  for (const int32_t i : order) {
     Request q;
     q.n = n[i];
     q.nodes.assign(nodes[i], nodes[i] + n[i]);
@@ -1088,7 +1093,7 @@ int svxg_batch_piece_rounds(svxg_server* S, int32_t count, const svxg_node* cons
     }
   }
   for (int32_t i = 0; i < count; ++i) {
-    if (t[size_t(i)] <= 0) break;
+    if (t[size_t(i)] <= 0) continue;  // (not submitted: a submission failed)
     svxg_request_result r{};
     const int e = svxg_server_wait(S, t[size_t(i)], &r);
     if (e && !err) err = e;

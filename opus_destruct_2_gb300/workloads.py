@@ -98,13 +98,15 @@ def batch(count: int = 512, workers: int = 16, precision: int = PRECISION_MIXED,
 
 
 def pieces(count: int = 512, workers: int = 16, seed: int = 5, plain_sample: int = 64, impact_scale: float = 20.0,
-           precision: int = PRECISION_FP64):
+           precision: int = PRECISION_FP64, steps: int = 1, warmup: int = 1):
     """A substep's loose pieces through their break rounds (svxg_batch_piece_rounds): the batched
     workload's piece sizes (log-normal, median 300 fragments, 10-20,000), every piece free with
     inertial-relief loads and one impact of log-uniform 1e4-1e6 N scaled by `impact_scale` (so
     that most pieces crack), the world's settings (rtol 1e-2, 60 iterations, 8 rounds), resting
     loads (no energy limit), under `precision` (FP64: the bit-exact multigrid; the mixed policy:
-    its fast build). Reports pieces/s beside one piece after another on one problem."""
+    its fast build). `warmup` untimed substeps, then `steps` timed ones (every piece's rounds from
+    its original graph each time, on a fresh problem). Reports pieces/s beside one piece after
+    another on one problem."""
     from .graph import PieceOptions
     sizes = synth.lognormal_sizes(count, 300, 10, 20000, seed=seed)
     rng = np.random.default_rng(seed + 1)
@@ -117,10 +119,12 @@ def pieces(count: int = 512, workers: int = 16, seed: int = 5, plain_sample: int
     o = PieceOptions()
     so = StressOptions(precision=precision)
     with Server(workers=workers, budget=40 << 30) as S:
-        S.batch_piece_rounds(ps[:min(32, count)], mats, options=o, opt=so)  # (warm-up)
+        for _ in range(max(warmup, 1)):
+            S.batch_piece_rounds(ps, mats, options=o, opt=so)  # (warm-up substeps)
         S.reset_stats()
         t0 = time.perf_counter()
-        pres, res, _, _, _ = S.batch_piece_rounds(ps, mats, options=o, opt=so)
+        for _ in range(max(steps, 1)):
+            pres, res, _, _, _ = S.batch_piece_rounds(ps, mats, options=o, opt=so)
         wall = time.perf_counter() - t0
         st = S.stats()
     # one piece after another on one problem (the plain per-request path), on a sample
@@ -132,7 +136,8 @@ def pieces(count: int = 512, workers: int = 16, seed: int = 5, plain_sample: int
         del G
     plain = lim / (time.perf_counter() - t0)
     return {
-        "pieces_per_s": count / wall, "wall_s": wall, "p50_ms": st.p50_ms, "p99_ms": st.p99_ms, "pieces": count,
+        "pieces_per_s": max(steps, 1) * count / wall, "wall_s": wall, "substeps": max(steps, 1),
+        "warmup_substeps": max(warmup, 1), "p50_ms": st.p50_ms, "p99_ms": st.p99_ms, "pieces": count,
         "nodes": int(sum(len(p[0]) for p in ps)), "bonds_broken": int(sum(r.bonds_broken for r in pres)),
         "chips": int(sum(r.chips for r in pres)), "rounds": int(sum(r.checks for r in pres)),
         "statuses": {str(s_): int(sum(1 for r in pres if r.status == s_)) for s_ in range(7)},
