@@ -108,8 +108,11 @@ def test_failure_set_identical(name):
     phi, mode, over = G.utilization(frag)
     margin = np.min(np.abs(po - 1.0))
     band = 1e-6 * np.max(po)
-    safe = np.abs(po - 1.0) > band
-    assert np.array_equal((phi >= 1.0)[safe], (po >= 1.0)[safe]), f"min margin {margin:.3e}"
-    if margin > band:
+    # bonds within the solve's error of phi = 1 are listed, not dropped: every bond judged
+    # differently must be one of them
+    in_band = np.nonzero(np.abs(po - 1.0) <= band)[0]
+    differ = np.nonzero((phi >= 1.0) != (po >= 1.0))[0]
+    assert np.isin(differ, in_band).all(), (f"min margin {margin:.3e}", differ.tolist(), in_band.tolist())
+    if len(in_band) == 0:
         assert np.array_equal(over, np.nonzero(po >= 1.0)[0])
         assert np.array_equal(mode, mo)
