@@ -5,7 +5,8 @@ Default (--workload serve): the serving configuration the metric is quoted on. A
 stream of solve requests (5,000/s; sizes log-normal, median 500 fragments, 10-50,000; 30 % repeats
 of a recent structure with 1-5 % of its bonds removed, warm-started) through the library's server:
 each request's K assembled (or downdated in place), its multigrid built, PCG to rel. residual 1e-6
-under the mixed-precision policy, and every bond's fibre-stress check. One step = 1000 requests.
+under the mixed-precision policy, and every bond's fibre-stress check. The stream has --requests
+requests (20,000, the configuration's) or 1,000 a step if more; one step = requests / K of them.
 
   value   solves/s with the requests' graphs and loads already in device memory
   e2e     solves/s of the same stream from host arrays through the C ABI (graph and load copied in,
@@ -309,9 +310,9 @@ def _serve_bytes(stream, way: str) -> int:
 def run_serve(args, rank: int, world: int):
     """The serving configuration: a Poisson stream of solve requests through the server (slots
     overlap requests on the device, queued new requests run in batches, kept batches serve their
-    structures' repeats), each request's graph assembled, solved to rtol 1e-6 and judged. One step
-    = 1000 requests of the stream (steps x 1000 in all); warm-up = 100 requests a warm-up step on
-    the same server before the timed stream.
+    structures' repeats), each request's graph assembled, solved to rtol 1e-6 and judged. The stream:
+    max(--requests, 1000 x steps) requests, one step = requests / steps of them; warm-up = 100
+    requests a warm-up step on the same server before the timed stream.
 
       value   solves/s with every request's graph, materials and load already in device memory
               (svxg_server_submit_device)
@@ -334,7 +335,9 @@ def run_serve(args, rank: int, world: int):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
-    requests = 1000 * args.steps
+    # (the configuration's stream of --requests requests, 20,000 by default, in K steps; at least
+    # 1,000 requests a step)
+    requests = max(args.requests, 1000 * args.steps)
     stream = workloads.Stream(requests=requests, rate=args.rate, seed=args.seed + 9 + rank)
     staged = workloads.DeviceGeometries(stream, local)
     kw = dict(workers=args.workers, precision=prec, rtol=args.rtol, warmup=100 * args.warmup)
@@ -382,8 +385,8 @@ def run_serve(args, rank: int, world: int):
                    "precision": ("fp64" if prec == PRECISION_FP64 else
                                  "mixed policy: fp32 V-cycle, multigrid built with FMAs and a tree-summed "
                                  "power-iteration norm, fp64 K and Krylov vectors"),
-                   "step": "1000 requests of the stream: each assembled (or bonds removed in place), solved, "
-                           "judged",
+                   "step": f"{requests / args.steps:g} requests of the stream: each assembled (or bonds "
+                           f"removed in place), solved, judged",
                    "l2": "the stream's requests together exceed L2 (tens of GB admitted)",
                    "parallelism": f"replicas x{world}, {args.workers} server slots, new requests in batches "
                                   f"of <= {args.batch_graphs or 16} graphs"},
@@ -392,8 +395,8 @@ def run_serve(args, rank: int, world: int):
         "serve": {k: dev[k] for k in keys}, "serve_at_70pct": ({k: at70[k] for k in keys} if at70 else None),
         "plain_fp64_per_request": plain, "vs_plain_fp64": dev["solves_per_s"] / plain["solves_per_s"],
         "e2e": {"value": world * host["solves_per_s"], "unit": "solves/s",
-                "h2d_bytes_per_step": int(_serve_bytes(stream, "h2d") * 1000 / requests),
-                "d2h_bytes_per_step": int(_serve_bytes(stream, "d2h") * 1000 / requests),
+                "h2d_bytes_per_step": int(_serve_bytes(stream, "h2d") / args.steps),
+                "d2h_bytes_per_step": int(_serve_bytes(stream, "d2h") / args.steps),
                 "p50_ms": host["p50_ms"], "p99_ms": host["p99_ms"]},
         "gpu_launches": dev["launches"],
         "gpu_launches_in_graphs": dev["launches_in_graphs"],
@@ -460,7 +463,7 @@ def run_reference_serve(args, world: int):
     structure's requests in arrival order on one process. Step i: the structures s of the stream
     with s mod (warmup + steps) = i, with all their requests; the first `warmup` steps untimed."""
     from opus_destruct_2_gb300 import workloads
-    requests = 1000 * args.steps
+    requests = max(args.requests, 1000 * args.steps)
     stream = workloads.Stream(requests=requests, rate=args.rate, seed=args.seed + 9)
     jobs = cpu_jobs(stream, range(requests), args.rtol)
     cores = os.cpu_count() or 1
