@@ -67,10 +67,12 @@ def test_reference_arm_serving_stream():
     if not os.path.exists(os.path.join(ROOT, "oracle", "_build", "libsvxo.so")):
         pytest.skip("the oracle is not built")
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
-                        "--warmup", "3"], cwd=ROOT, capture_output=True, text=True, timeout=900)
+                        "--warmup", "3", "--requests", "1000"], cwd=ROOT, capture_output=True, text=True,
+                       timeout=900)
     assert r.returncode == 0, r.stderr[-2000:]
     line = json.loads(r.stdout.strip().splitlines()[-1])
     assert line["impl"] == "reference" and line["unit"] == "solves/s" and line["value"] > 0
     assert line["config"]["rtol"] == 1e-6 and line["config"]["timed_requests"] > 0
     assert line["config"]["converged"] == line["config"]["timed_requests"]
     assert line["e2e"]["value"] == line["value"] and line["cpu_baseline"]["kind"] == "port"
+    assert line["config"]["requests"] == 1000
